@@ -1,0 +1,211 @@
+/*
+ * nhwave_gb300.h -- C-ABI of the GB300 (sm_103a) implementation of NHWAVE's
+ * time-step hot path.
+ *
+ * Every entry point uses plain C types (no CUDA or torch types), returns an
+ * int status (NHW_OK == 0) and never keeps a host pointer after it returns.
+ * Host arrays use the reference's own memory layout: Fortran column-major
+ * order over the ghosted local extents of module GLOBAL
+ * (src/mod_global.F:212-243), i.e. element (i,j,k) with 1-based Fortran
+ * indices sits at offset (i-1) + Mloc*((j-1) + Nloc*(k-1)), with
+ *   Mloc = Mglob+4, Nloc = Nglob+4, Kloc = Kglob+4        (Nghost = 2)
+ * and face arrays one longer in their face direction (Mloc1 = Mloc+1 ...),
+ * exactly as allocated in src/initialize.F:1423-1643.
+ *
+ * The entry points replace, one for one, the argument-less subroutines that
+ * program NHWAVE calls inside its time loop (src/nhwave.F:119-258):
+ *
+ *   nhw_estimate_dt        <- estimate_dt          src/nhwave.F:3694-3874
+ *   nhw_update_bathymetry  <- update_bathymetry    src/nhwave.F:5755-6071 (RIGID_3D)
+ *   nhw_update_mask        <- update_mask          src/nhwave.F:5403-5456
+ *   nhw_update_vars        <- update_vars          src/nhwave.F:5459-5511
+ *   nhw_source_terms       <- source_terms         src/source_terms.F:1-455 (INT_LIN + bed slope)
+ *   nhw_fluxes             <- fluxes               src/nhwave.F:1686-1714
+ *   nhw_eval_duvw          <- eval_duvw(ISTEP)     src/nhwave.F:539-1300 (inviscid path,
+ *                             incl. poisson_solver src/pressure.F:63-245 and
+ *                             generate_coef_rhs src/pressure.F:475-840)
+ *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
+ *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
+ *   nhw_mass               <- statistics' MassVolume  src/nhwave.F:3139-3148
+ *
+ * Set-up (the work of read_bathymetry src/initialize.F:1734-2175, generate_grid
+ * src/initialize.F:1647-1729 and initial src/initialize.F:2502-3408) is offered
+ * by nhw_setup for callers without the Fortran driver; a Fortran driver that
+ * runs its own set-up hands its arrays over with nhw_set_field instead.
+ */
+#ifndef NHWAVE_GB300_H
+#define NHWAVE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum nhw_status {
+  NHW_OK = 0,
+  NHW_ERR_ARG = 1,           /* null pointer, bad size or bad field id            */
+  NHW_ERR_UNSUPPORTED = 2,   /* option outside this path (HLLC, viscous, open BC) */
+  NHW_ERR_CUDA = 3,          /* CUDA runtime error (message: nhw_last_error)      */
+  NHW_ERR_NOMEM = 4,         /* device allocation failed                          */
+  NHW_ERR_DT_MIN = 5,        /* dt < DT_MIN: the reference stops here             */
+  NHW_ERR_KRYLOV_NOCONV = 6, /* Poisson solve reached ITMAX above TOL             */
+  NHW_ERR_NAN = 7,           /* non-finite value in the Poisson residual          */
+  NHW_ERR_TIMEOUT = 8,       /* a bounded device wait gave up                     */
+  NHW_ERR_STATE = 9,         /* call out of order (e.g. step before set-up)       */
+  NHW_ERR_CAPACITY = 10,     /* serving: HBM budget or slot table exhausted       */
+  NHW_ERR_NOT_FOUND = 11     /* serving: unknown request id                       */
+};
+
+/* arithmetic form of the state arrays */
+enum nhw_precision {
+  NHW_FP64 = 0,     /* plain FP64 drop-in: every array and the Krylov solve in FP64   */
+  NHW_FP32_IR = 1   /* FP32 3-D state, fluxes and Krylov inner iterations; FP64 2-D
+                       depth/eta/mask fields, FP64 Poisson residual + refinement     */
+};
+
+enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2 };
+enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
+enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
+
+/*
+ * Run-time parameters: the input.txt keys that the path reads
+ * (src/initialize.F:141-1321), parsed to double exactly as Get_Float_Val
+ * does (src/mod_util.F:138).  Names follow the input.txt keys.
+ */
+typedef struct nhw_params {
+  int32_t Mglob, Nglob, Kglob;             /* Mglob Nglob Kglob                       */
+  double  dx, dy;                          /* DX DY                                   */
+  int32_t ivgrd;  double grd_r;            /* IVGRD GRD_R                             */
+  double  dt_ini, dt_min, dt_max;          /* DT_INI DT_MIN DT_MAX                    */
+  double  total_time; int32_t sim_steps;   /* TOTAL_TIME SIM_STEPS                    */
+  double  cfl;                             /* CFL                                     */
+  int32_t froude_cap_on; double froude_cap;/* -DFROUDE_CAP build flag, FROUDE_CAP     */
+  double  min_dep;                         /* MinDep                                  */
+  int32_t non_hydro;                       /* NON_HYDRO                               */
+  int32_t time_order;                      /* 1,2,3 <- TIME_ORDER FIRST/SECOND/THIRD  */
+  int32_t hllc;                            /* HLLC (must be 0)                        */
+  int32_t viscous_flow;                    /* VISCOUS_FLOW (must be 0)                */
+  int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
+  int32_t itmax; double tol;               /* ITMAX TOL                               */
+  int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn (1 or 2)        */
+  int32_t bc_z0;                           /* BC_Z0 (1)                               */
+  double  visc;                            /* VISCOSITY (initial Cmu)                 */
+  double  slat;                            /* slat -> fcor                            */
+  double  wind_u, wind_v;                  /* WindU WindV (Iws = 1)                   */
+  int32_t depth_type;                      /* DEPTH_TYPE                              */
+  int32_t wavemaker;                       /* WAVEMAKER                               */
+  double  amp_wave, per_wave, dep_wave, theta_wave, cur_wave; /* AMP PER DEP THETA CUR */
+  double  xsource_west, xsource_east, ysource_suth, ysource_nrth;
+  int32_t sponge_on;                       /* SPONGE_ON                               */
+  double  sponge_west_width, sponge_east_width, sponge_south_width, sponge_north_width;
+  double  tramp;                           /* TRAMP                                   */
+  int32_t slide_type;                      /* SlideType (-DLANDSLIDE build)            */
+  double  slide_t, slide_l, slide_w, slide_angle, slope_angle, slide_x0, slide_y0;
+  double  slide_ut, slide_a0;              /* SlideUt SlideA0                         */
+  int32_t precision;                       /* enum nhw_precision                      */
+  int32_t reserved[8];
+} nhw_params;
+
+/* Scalars the driver reads back after a step (module GLOBAL scalars). */
+typedef struct nhw_scalars {
+  double  time;          /* TIME                                          */
+  double  dt;            /* dt                                            */
+  double  dt_old;        /* dt_old                                        */
+  int32_t run_step;      /* RUN_STEP                                      */
+  int32_t last_krylov_iters;   /* inner iterations of the last Poisson solve */
+  int64_t total_krylov_iters;  /* since set-up                              */
+  int64_t poisson_solves;      /* since set-up                              */
+  double  last_rel_residual;   /* FP64 ||b-Ax||/||b|| of the last solve     */
+  int32_t last_refinements;    /* FP64 refinement sweeps of the last solve  */
+  int32_t status;              /* sticky device status (enum nhw_status)    */
+} nhw_scalars;
+
+/* Field ids for nhw_get_field / nhw_set_field.  Shapes are the reference's
+ * ghosted allocations; integer fields are int32, all others double. */
+enum nhw_field {
+  /* 2-D cell (Mloc,Nloc) */
+  NHW_F_D = 0, NHW_F_D0, NHW_F_ETA, NHW_F_ETA0, NHW_F_HC, NHW_F_HC0,
+  NHW_F_DELXH, NHW_F_DELYH, NHW_F_DELXETA, NHW_F_DELYETA, NHW_F_DELTH, NHW_F_DELT2H,
+  NHW_F_SOURCEX, NHW_F_SOURCEY, NHW_F_SOURCEC, NHW_F_SPONGE, NHW_F_R1,
+  /* 2-D x faces (Mloc1,Nloc) */
+  NHW_F_HFX, NHW_F_HFX0, NHW_F_ETAXL, NHW_F_ETAXR,
+  /* 2-D y faces (Mloc,Nloc1) */
+  NHW_F_HFY, NHW_F_HFY0, NHW_F_ETAYL, NHW_F_ETAYR,
+  /* 2-D int (Mloc,Nloc) */
+  NHW_F_MASK, NHW_F_MASK_STRUCT, NHW_F_MASK9,
+  /* 3-D cell (Mloc,Nloc,Kloc) */
+  NHW_F_U, NHW_F_V, NHW_F_W, NHW_F_DU, NHW_F_DV, NHW_F_DW,
+  NHW_F_DU0, NHW_F_DV0, NHW_F_DW0, NHW_F_P,
+  /* 3-D z faces (Mloc,Nloc,Kloc1) */
+  NHW_F_OMEGA,
+  /* 3-D x faces (Mloc1,Nloc,Kloc) */
+  NHW_F_EX, NHW_F_FX, NHW_F_GX, NHW_F_HX,
+  /* 3-D y faces (Mloc,Nloc1,Kloc) */
+  NHW_F_EY, NHW_F_FY, NHW_F_GY, NHW_F_HY,
+  /* 3-D z faces (Mloc,Nloc,Kloc1) */
+  NHW_F_FZ, NHW_F_GZ, NHW_F_HZ,
+  NHW_F_COUNT
+};
+
+typedef struct nhw_handle nhw_handle;
+
+/* ------------------------------------------------------------- lifecycle */
+/* Validate parameters, size and allocate the device state (index +
+ * allocate_variables, src/initialize.F:1339-1643).  One CUDA stream per
+ * handle; one host thread per handle. */
+int nhw_create(const nhw_params* params, nhw_handle** out);
+int nhw_destroy(nhw_handle* h);
+
+/* Set-up without the Fortran driver: generate_grid + read_bathymetry (from
+ * `depth`, Mglob x Nglob for CELL_CENTER, (Mglob+1) x (Nglob+1) for
+ * CELL_GRID, i fastest, as the rows of depth.txt) + initial (eta0/uvw0 may be
+ * NULL for a state at rest; uvw0 holds U, V then W, each Mglob x Nglob x
+ * Kglob with i fastest, as uvw0.txt).  src/initialize.F:1647-2175, 2502-3408 */
+int nhw_setup(nhw_handle* h, const double* depth, const double* eta0, const double* uvw0);
+
+/* Copy one whole ghosted field between host and device (Fortran layout). */
+int nhw_get_field(nhw_handle* h, int field, void* host);
+int nhw_set_field(nhw_handle* h, int field, const void* host);
+/* Shape of a field: dims[0..2] (dims[2] == 1 for 2-D), elem_bytes. */
+int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* elem_bytes);
+
+int nhw_get_scalars(nhw_handle* h, nhw_scalars* out);
+int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step);
+
+/* ------------------------------------------- the reference's subroutines */
+int nhw_estimate_dt(nhw_handle* h);
+int nhw_update_bathymetry(nhw_handle* h);
+int nhw_update_mask(nhw_handle* h);
+int nhw_update_vars(nhw_handle* h);
+int nhw_source_terms(nhw_handle* h);
+int nhw_fluxes(nhw_handle* h);
+int nhw_eval_duvw(nhw_handle* h, int32_t istep);
+int nhw_sponge_damping(nhw_handle* h);
+
+/* One full time step (estimate_dt ... last RK stage), replayed from a CUDA
+ * graph after the first call.  Writes TIME, dt and RUN_STEP if non-NULL. */
+int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step);
+/* Up to nsteps steps while TIME < TOTAL_TIME and RUN_STEP < SIM_STEPS (the
+ * reference's do-while condition, src/nhwave.F:119). */
+int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done);
+
+/* FP64 device reduction of statistics' MassVolume = sum(D*dx*dy). */
+int nhw_mass(nhw_handle* h, double* mass);
+
+/* Wait for the handle's stream. */
+int nhw_synchronize(nhw_handle* h);
+
+/* sizeof(nhw_params) and sizeof(nhw_scalars) as compiled into the library,
+ * for bindings to check their struct images (no GPU needed). */
+int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes);
+
+/* Human-readable text of a status code, and the last CUDA error text. */
+const char* nhw_status_string(int status);
+const char* nhw_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NHWAVE_GB300_H */

@@ -1,0 +1,170 @@
+// capi.cu -- the C-ABI of include/nhwave_gb300.h over the device solvers.
+#include <cstdio>
+#include <mutex>
+#include <string>
+
+#include "solver.cuh"
+
+struct nhw_handle {
+  nhw::SolverBase* s = nullptr;
+  nhw_params p{};
+};
+
+namespace nhw {
+namespace {
+std::mutex g_err_mu;
+std::string g_err;
+thread_local std::string t_err_copy;
+}  // namespace
+void set_last_error(const std::string& s) {
+  std::lock_guard<std::mutex> g(g_err_mu);
+  g_err = s;
+}
+}  // namespace nhw
+
+using nhw::SolverBase;
+
+#define NHW_GUARD(h)                              \
+  if (!(h) || !(h)->s) return NHW_ERR_ARG;        \
+  if (!(h)->s->is_setup()) return NHW_ERR_STATE;
+
+extern "C" {
+
+int nhw_create(const nhw_params* params, nhw_handle** out) {
+  if (!params || !out) return NHW_ERR_ARG;
+  *out = nullptr;
+  int st = NHW_OK;
+  SolverBase* s = params->precision == NHW_FP32_IR ? nhw::make_solver_fp32(*params, &st)
+                                                   : nhw::make_solver_fp64(*params, &st);
+  if (!s) return st ? st : NHW_ERR_NOMEM;
+  nhw_handle* h = new nhw_handle();
+  h->s = s;
+  h->p = *params;
+  *out = h;
+  return NHW_OK;
+}
+
+int nhw_destroy(nhw_handle* h) {
+  if (!h) return NHW_ERR_ARG;
+  delete h->s;
+  delete h;
+  return NHW_OK;
+}
+
+int nhw_setup(nhw_handle* h, const double* depth, const double* eta0, const double* uvw0) {
+  if (!h || !h->s || !depth) return NHW_ERR_ARG;
+  return h->s->setup(depth, eta0, uvw0);
+}
+
+int nhw_get_field(nhw_handle* h, int field, void* host) {
+  if (!h || !h->s) return NHW_ERR_ARG;
+  return h->s->get_field(field, host);
+}
+int nhw_set_field(nhw_handle* h, int field, const void* host) {
+  if (!h || !h->s) return NHW_ERR_ARG;
+  return h->s->set_field(field, host);
+}
+int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* elem_bytes) {
+  if (!h || !h->s || !dims || !elem_bytes) return NHW_ERR_ARG;
+  int d[3], eb;
+  int rc = h->s->field_shape(field, d, &eb);
+  if (rc) return rc;
+  dims[0] = d[0]; dims[1] = d[1]; dims[2] = d[2];
+  *elem_bytes = eb;
+  return NHW_OK;
+}
+int nhw_get_scalars(nhw_handle* h, nhw_scalars* out) {
+  if (!h || !h->s || !out) return NHW_ERR_ARG;
+  return h->s->get_scalars(out);
+}
+int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step) {
+  if (!h || !h->s) return NHW_ERR_ARG;
+  return h->s->set_time(time, dt, run_step);
+}
+
+int nhw_estimate_dt(nhw_handle* h) { NHW_GUARD(h); return h->s->estimate_dt(); }
+int nhw_update_bathymetry(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_bathymetry(); return rc ? rc : h->s->sync(); }
+int nhw_update_mask(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_mask(); return rc ? rc : h->s->sync(); }
+int nhw_update_vars(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_vars(); return rc ? rc : h->s->sync(); }
+int nhw_source_terms(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->source_terms(); return rc ? rc : h->s->sync(); }
+int nhw_fluxes(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->fluxes(); return rc ? rc : h->s->sync(); }
+int nhw_eval_duvw(nhw_handle* h, int32_t istep) {
+  NHW_GUARD(h);
+  int rc = h->s->eval_duvw(istep);
+  int rs = h->s->sync();
+  return rs ? rs : rc;
+}
+int nhw_sponge_damping(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->sponge_damping(); return rc ? rc : h->s->sync(); }
+
+int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step) {
+  NHW_GUARD(h);
+  int rc = h->s->step();
+  if (rc == NHW_ERR_CUDA) return rc;
+  if (time || dt || run_step) {
+    nhw_scalars sc;
+    int r2 = h->s->get_scalars(&sc);
+    if (r2) return r2;
+    if (time) *time = sc.time;
+    if (dt) *dt = sc.dt;
+    if (run_step) *run_step = sc.run_step;
+  }
+  return rc;
+}
+
+int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done) {
+  NHW_GUARD(h);
+  int done = 0, rc = NHW_OK;
+  nhw_scalars sc;
+  for (; done < nsteps; ++done) {
+    rc = h->s->get_scalars(&sc);
+    if (rc) break;
+    if (!(sc.time < h->s->total_time() && sc.run_step < h->s->sim_steps())) break;
+    rc = h->s->step();
+    if (rc != NHW_OK && rc != NHW_ERR_KRYLOV_NOCONV) { ++done; break; }
+    rc = NHW_OK;
+  }
+  if (steps_done) *steps_done = done;
+  return rc;
+}
+
+int nhw_mass(nhw_handle* h, double* mass) {
+  NHW_GUARD(h);
+  if (!mass) return NHW_ERR_ARG;
+  return h->s->mass(mass);
+}
+int nhw_synchronize(nhw_handle* h) {
+  if (!h || !h->s) return NHW_ERR_ARG;
+  return h->s->sync();
+}
+
+int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes) {
+  if (!params_bytes || !scalars_bytes) return NHW_ERR_ARG;
+  *params_bytes = (int32_t)sizeof(nhw_params);
+  *scalars_bytes = (int32_t)sizeof(nhw_scalars);
+  return NHW_OK;
+}
+
+const char* nhw_status_string(int status) {
+  switch (status) {
+    case NHW_OK: return "ok";
+    case NHW_ERR_ARG: return "bad argument";
+    case NHW_ERR_UNSUPPORTED: return "option outside the GPU path";
+    case NHW_ERR_CUDA: return "CUDA error";
+    case NHW_ERR_NOMEM: return "device allocation failed";
+    case NHW_ERR_DT_MIN: return "time step too small (dt < DT_MIN)";
+    case NHW_ERR_KRYLOV_NOCONV: return "Poisson solve did not reach TOL within ITMAX";
+    case NHW_ERR_NAN: return "non-finite Poisson residual";
+    case NHW_ERR_TIMEOUT: return "bounded device wait timed out";
+    case NHW_ERR_STATE: return "call out of order";
+    case NHW_ERR_CAPACITY: return "capacity exhausted";
+    case NHW_ERR_NOT_FOUND: return "unknown id";
+    default: return "unknown status";
+  }
+}
+const char* nhw_last_error(void) {
+  std::lock_guard<std::mutex> g(nhw::g_err_mu);
+  nhw::t_err_copy = nhw::g_err;
+  return nhw::t_err_copy.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,1091 @@
+// kernels.cuh -- device operations of the NHWAVE time step, templated on the
+// 3-D storage type T (double: plain FP64 form; float: FP32+IR form).
+//
+// Each operation is a functor applied to one work item (a cell, a face, or a
+// water column) of one scenario; generic __global__ launchers map threads to
+// work items.  Arithmetic follows the reference's evaluation order term by
+// term (the FP64 instantiation is compiled without FMA contraction), so the
+// FP64 form reproduces the CPU restatement of the reference exactly wherever
+// no libm transcendental (cos, cosh, log, atan2) or parallel reduction is
+// involved.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include "state.h"
+
+namespace nhw {
+
+// ----------------------------------------------------------------- helpers
+__device__ __forceinline__ double dmax_(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dmin_(double a, double b) { return a < b ? a : b; }
+template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+template <class R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
+
+// van Leer LIMITER (src/nhwave.F:2889-2906)
+template <class R>
+__device__ __forceinline__ R limiter(R A, R B) {
+  return (A * fabs(B) + fabs(A) * B) / (fabs(A) + fabs(B));
+}
+// limited slope of delx/y/zFun (src/nhwave.F:2060-2351): zero if |T1|+|T2| < Small
+template <class R>
+__device__ __forceinline__ R lim_slope(R am, R a0, R ap, R dm, R dp) {
+  R t1 = (ap - a0) / dp;
+  R t2 = (a0 - am) / dm;
+  return (fabs(t1) + fabs(t2)) < (R)kSmall ? (R)0 : limiter(t1, t2);
+}
+// 0.5*Grav*(eta*eta + 2*eta*h0): hydrostatic part of the momentum flux
+template <class R>
+__device__ __forceinline__ R hydro(R eta, R h0) {
+  return (R)0.5 * (R)kGrav * (eta * eta + (R)2.0 * eta * h0);
+}
+template <class R>
+__device__ __forceinline__ R hll(R sl, R sr, R fl, R fr, R ul, R ur) {
+  // HLL (src/nhwave.F:2741-2776)
+  if (sl >= (R)0) return fl;
+  if (sr <= (R)0) return fr;
+  R f = sr * fl - sl * fr + sl * sr * (ur - ul);
+  if (fabs(sr - sl) < (R)kSmall) return f / (R)kSmall;
+  return f / (sr - sl);
+}
+
+__device__ __forceinline__ int mirror(int i, int b, int e) {
+  return i < b ? 2 * b - 1 - i : (i > e ? 2 * e + 1 - i : i);
+}
+
+// ---------------------------------------------------------------- launchers
+// work-item decoders
+struct AllCols { template <class T> __device__ static int n(const Dev<T>& S) { return S.Mloc * S.Nloc; } };
+
+template <class T, class Op>
+__global__ void __launch_bounds__(256) k_allcols(Dev<T> S, Op op) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.Mloc * S.Nloc) return;
+  op(S, t % S.Mloc, t / S.Mloc);
+}
+template <class T, class Op>
+__global__ void __launch_bounds__(256) k_incols(Dev<T> S, Op op) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.M * S.N) return;
+  op(S, S.IB + t % S.M, S.JB + t / S.M);
+}
+// cells over an (nx x ny x nz) box starting at (ox, oy, oz)
+template <class T, class Op>
+__global__ void __launch_bounds__(256) k_box(Dev<T> S, Op op, int nx, int ny, int nz, int ox, int oy, int oz) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long n = (long long)nx * ny * nz;
+  if (t >= n) return;
+  int i = (int)(t % nx);
+  long long r = t / nx;
+  int j = (int)(r % ny);
+  int k = (int)(r / ny);
+  op(S, ox + i, oy + j, oz + k);
+}
+// all cells of the ghosted array
+template <class T, class Op>
+__global__ void __launch_bounds__(256) k_allcells(Dev<T> S, Op op) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long n = (long long)S.Mloc * S.Nloc * S.Kloc;
+  if (t >= n) return;
+  int i = (int)(t % S.Mloc);
+  long long r = t / S.Mloc;
+  op(S, i, (int)(r % S.Nloc), (int)(r / S.Nloc));
+}
+
+// ------------------------------------------------------------ reductions
+// Deterministic block reduction of NV doubles; the last block to finish
+// combines the per-block partials in a fixed order and calls fin(S, vals).
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
+  // sh: at least NV * 32 doubles
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  __syncthreads();
+  if (lane == 0)
+    for (int q = 0; q < NV; ++q) sh[q * 32 + warp] = v[q];
+  __syncthreads();
+  if (warp == 0) {
+    for (int q = 0; q < NV; ++q) {
+      double x = lane < nw ? sh[q * 32 + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      v[q] = x;
+    }
+  }
+}
+
+template <int NV, class T, class Fin>
+__device__ __forceinline__ void reduce_finalize(const Dev<T>& S, double (&v)[NV], int slot, Fin fin) {
+  __shared__ double sh[NV * 32];
+  __shared__ bool last;
+  block_sum<NV>(v, sh);
+  const int nb = gridDim.x;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NV; ++q) S.partials[(size_t)blockIdx.x * 8 + q] = v[q];
+    __threadfence();
+    unsigned prev = atomicAdd(&S.sc->counter[slot], 1u);
+    last = (prev == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[NV];
+  for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int q = 0; q < NV; ++q) acc[q] += ((volatile double*)S.partials)[(size_t)b * 8 + q];
+  block_sum<NV>(acc, sh);
+  if (threadIdx.x == 0) {
+    S.sc->counter[slot] = 0u;
+    fin(S, acc);
+  }
+}
+
+// =========================================================================
+//                        2-D slopes of eta (delx/yFun_2D)
+// =========================================================================
+struct OpSlopeEta {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const double* E = S.Eta;
+    const long long c = i2(S, i, j);
+    double sx, sy;
+    if (i == 0) sx = (E[c + 1] - E[c]) / S.dx;
+    else if (i == S.Mloc - 1) sx = (E[c] - E[c - 1]) / S.dx;
+    else if (S.Mask[c] == 0) sx = 0.0;
+    else sx = lim_slope<double>(E[c - 1], E[c], E[c + 1], S.dx, S.dx);
+    if (j == 0) sy = (E[c + S.sy] - E[c]) / S.dy;
+    else if (j == S.Nloc - 1) sy = (E[c] - E[c - S.sy]) / S.dy;
+    else if (S.Mask[c] == 0) sy = 0.0;
+    else sy = lim_slope<double>(E[c - S.sy], E[c], E[c + S.sy], S.dy, S.dy);
+    S.DelxEta[c] = sx;
+    S.DelyEta[c] = sy;
+  }
+};
+
+// =========================================================================
+//              source_terms (src/source_terms.F:30-67, 418-455)
+// =========================================================================
+struct OpSourceArea {  // one thread: Source_Area = sum over i of dx*D(i,Jbeg+1), in order
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int, int) const {
+    double a = 0.0;
+    const int jrow = S.JB + 1;
+    for (int i = S.IB; i <= S.IE; ++i)
+      if (S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe) a = a + S.dx * S.D[i2(S, i, jrow)];
+    S.sc->source_area = a;
+  }
+};
+struct OpSource {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    const double time = S.sc->time;
+    if (S.wavemaker != 0 && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys &&
+        S.yc[j] <= S.wm_yn) {
+      const double area = S.sc->source_area;
+      if (S.wavemaker == 1) {
+        const double phs = S.yc[j] * S.wm_wnumy;
+        S.SourceC[c] = S.wm_celerity * S.wm_amp / area * cos(kPi / 2 - S.wm_segma * time + phs);
+      } else {
+        const double ch = cosh(S.wm_atmp * (S.wm_xstart - S.wm_celerity * time));
+        S.SourceC[c] = 2.0 * S.wm_celerity / area * S.wm_amp / (ch * ch);
+      }
+    }
+    const double m = (double)S.Mask[c];
+    S.SourceX[c] = kGrav * 0.5 * (S.EtaxL[c + 1] + S.EtaxR[c]) * (S.Hfx0[c + 1] - S.Hfx0[c]) / S.dx * m;
+    S.SourceY[c] = kGrav * 0.5 * (S.EtayL[c + S.sy] + S.EtayR[c]) * (S.Hfy0[c + S.sy] - S.Hfy0[c]) / S.dy * m;
+  }
+};
+
+// =========================================================================
+//    fluxes: delxyzFun + construction + wave_speed + HLL + flux_bc
+//    (src/nhwave.F:1686-2351, 2354-2552, 2673-2738, 2813-2886)
+// =========================================================================
+// x faces: face f between cells f-1 and f, row j, level k (all interior)
+struct OpFluxX {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int f, int j, int k) const {
+    using R = T;
+    const int c0 = f - 1, c1 = f;
+    const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
+    const long long q0 = i2(S, c0, j), q1 = q0 + 1;
+    const int mL = S.Mask[q0], mR = S.Mask[q1];
+    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx;
+    // limited x slopes of the two cells (zero in dry cells)
+    auto sl = [&](const T* A, long long e, int m) -> R {
+      return m == 0 ? (R)0 : lim_slope<R>(A[e - 1], A[e], A[e + 1], rdx, rdx);
+    };
+    R uL = S.U[e0] + hdx * sl(S.U, e0, mL), uR = S.U[e1] - hdx * sl(S.U, e1, mR);
+    R vL = S.V[e0] + hdx * sl(S.V, e0, mL), vR = S.V[e1] - hdx * sl(S.V, e1, mR);
+    R wL = S.W[e0] + hdx * sl(S.W, e0, mL), wR = S.W[e1] - hdx * sl(S.W, e1, mR);
+    R duL = S.DU[e0] + hdx * sl(S.DU, e0, mL), duR = S.DU[e1] - hdx * sl(S.DU, e1, mR);
+    R dvL = S.DV[e0] + hdx * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdx * sl(S.DV, e1, mR);
+    R dwL = S.DW[e0] + hdx * sl(S.DW, e0, mL), dwR = S.DW[e1] - hdx * sl(S.DW, e1, mR);
+    double etaL = S.Eta[q0] + 0.5 * S.dx * S.DelxEta[q0];
+    double etaR = S.Eta[q1] - 0.5 * S.dx * S.DelxEta[q1];
+    const double hf = S.Hfx[q1];
+    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
+    double h0 = S.Hfx0[q1];
+    bool wrote_h0 = false;
+    // wet/dry front fix (src/nhwave.F:1745-1788)
+    if (c0 >= S.IB && c0 <= S.IE) {
+      if (mL == 1 && mR == 0) {
+        etaL = S.Eta[q0]; dL = S.D[q0]; h0 = S.Hc[q0]; wrote_h0 = true;
+        uL = vL = wL = duL = dvL = dwL = (R)0;
+      } else if (mL == 0) {
+        etaL = S.Eta[q0]; dL = S.D[q0];
+        uL = vL = wL = duL = dvL = dwL = (R)0;
+      }
+    }
+    if (c1 >= S.IB && c1 <= S.IE) {
+      const int mRR = S.Mask[q1 + 1];
+      if (mR == 1 && mRR == 0) {
+        // case 1 of cell c1 concerns face c1+1
+      } else if (mR == 1 && mL == 0) {
+        etaR = S.Eta[q1]; dR = S.D[q1]; h0 = S.Hc[q1]; wrote_h0 = true;
+        uR = vR = wR = duR = dvR = dwR = (R)0;
+      } else if (mR == 0) {
+        etaR = S.Eta[q1]; dR = S.D[q1];
+        uR = vR = wR = duR = dvR = dwR = (R)0;
+      }
+    }
+    if (wrote_h0 && k == S.KB) S.Hfx0[q1] = h0;
+    const R reL = (R)etaL, reR = (R)etaR, rh0 = (R)h0, rdL = (R)dL, rdR = (R)dR;
+    // physical fluxes at the faces
+    const R FxL = duL * uL + hydro<R>(reL, rh0), FxR = duR * uR + hydro<R>(reR, rh0);
+    const R GxL = rdL * uL * vL, GxR = rdR * uR * vR;
+    const R HxL = rdL * uL * wL, HxR = rdR * uR * wR;
+    // wave speeds (src/nhwave.F:2813-2849)
+    R SL = (R)0, SR = (R)0;
+    if (mL == 1 && mR == 1) {
+      R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
+      R pS = (R)0.5 * (pL + pR) + (R)0.25 * (uL - uR);
+      R uS = (R)0.5 * (uL + uR) + pL - pR;
+      SL = rmin<R>(uL - pL, uS - pS);
+      SR = rmax<R>(uR + pR, uS + pS);
+    } else if (mL == 0 && mR == 1) {
+      R pR = sqrt((R)kGrav * fabs(rdR));
+      SL = uR - (R)2.0 * pR;
+      SR = uR + pR;
+    } else if (mL == 1 && mR == 0) {
+      R pL = sqrt((R)kGrav * fabs(rdL));
+      SL = uL - pL;
+      SR = uL + (R)2.0 * pL;
+    }
+    R Ex = hll<R>(SL, SR, duL, duR, rdL, rdR);
+    R Fx = hll<R>(SL, SR, FxL, FxR, duL, duR);
+    R Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
+    R Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
+    // flux_bc: walls, then dry cells (src/nhwave.F:2366-2434, 2508-2549)
+    if (f == S.IB) { Ex = (R)0; Fx = hydro<R>(reR, rh0); Gx = (R)0; Hx = (R)0; }
+    if (f == S.IE + 1) { Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0; }
+    if (mR == 0) {
+      Ex = (R)0; Gx = (R)0; Hx = (R)0;
+      Fx = (f == S.IB) ? (R)0 : hydro<R>(reL, rh0) * (R)mL;
+    } else if (mL == 0) {
+      Ex = (R)0; Gx = (R)0; Hx = (R)0;
+      Fx = (c0 == S.IE) ? (R)0 : hydro<R>(reR, rh0) * (R)mR;
+    }
+    const long long o = i3(S, f, j, k);
+    S.Ex[o] = Ex; S.Fx[o] = Fx; S.Gx[o] = Gx; S.Hx[o] = Hx;
+  }
+};
+
+// y faces: face g between cells g-1 and g in column i
+struct OpFluxY {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int g, int k) const {
+    using R = T;
+    const int c0 = g - 1, c1 = g;
+    const long long sy = S.sy;
+    const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
+    const long long q0 = i2(S, i, c0), q1 = q0 + sy;
+    const int mL = S.Mask[q0], mR = S.Mask[q1];
+    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy;
+    auto sl = [&](const T* A, long long e, int m) -> R {
+      return m == 0 ? (R)0 : lim_slope<R>(A[e - sy], A[e], A[e + sy], rdy, rdy);
+    };
+    R uL = S.U[e0] + hdy * sl(S.U, e0, mL), uR = S.U[e1] - hdy * sl(S.U, e1, mR);
+    R vL = S.V[e0] + hdy * sl(S.V, e0, mL), vR = S.V[e1] - hdy * sl(S.V, e1, mR);
+    R wL = S.W[e0] + hdy * sl(S.W, e0, mL), wR = S.W[e1] - hdy * sl(S.W, e1, mR);
+    R duL = S.DU[e0] + hdy * sl(S.DU, e0, mL), duR = S.DU[e1] - hdy * sl(S.DU, e1, mR);
+    R dvL = S.DV[e0] + hdy * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdy * sl(S.DV, e1, mR);
+    R dwL = S.DW[e0] + hdy * sl(S.DW, e0, mL), dwR = S.DW[e1] - hdy * sl(S.DW, e1, mR);
+    double etaL = S.Eta[q0] + 0.5 * S.dy * S.DelyEta[q0];
+    double etaR = S.Eta[q1] - 0.5 * S.dy * S.DelyEta[q1];
+    const double hf = S.Hfy[q1];
+    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
+    double h0 = S.Hfy0[q1];
+    bool wrote_h0 = false;
+    if (c0 >= S.JB && c0 <= S.JE) {
+      if (mL == 1 && mR == 0) {
+        etaL = S.Eta[q0]; dL = S.D[q0]; h0 = S.Hc[q0]; wrote_h0 = true;
+        uL = vL = wL = duL = dvL = dwL = (R)0;
+      } else if (mL == 0) {
+        etaL = S.Eta[q0]; dL = S.D[q0];
+        uL = vL = wL = duL = dvL = dwL = (R)0;
+      }
+    }
+    if (c1 >= S.JB && c1 <= S.JE) {
+      const int mRR = S.Mask[q1 + sy];
+      if (mR == 1 && mRR == 0) {
+      } else if (mR == 1 && mL == 0) {
+        etaR = S.Eta[q1]; dR = S.D[q1]; h0 = S.Hc[q1]; wrote_h0 = true;
+        uR = vR = wR = duR = dvR = dwR = (R)0;
+      } else if (mR == 0) {
+        etaR = S.Eta[q1]; dR = S.D[q1];
+        uR = vR = wR = duR = dvR = dwR = (R)0;
+      }
+    }
+    if (wrote_h0 && k == S.KB) S.Hfy0[q1] = h0;
+    const R reL = (R)etaL, reR = (R)etaR, rh0 = (R)h0, rdL = (R)dL, rdR = (R)dR;
+    const R FyL = rdL * uL * vL, FyR = rdR * uR * vR;
+    const R GyL = dvL * vL + hydro<R>(reL, rh0), GyR = dvR * vR + hydro<R>(reR, rh0);
+    const R HyL = rdL * vL * wL, HyR = rdR * vR * wR;
+    R SL = (R)0, SR = (R)0;
+    if (mL == 1 && mR == 1) {
+      R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
+      R pS = (R)0.5 * (pL + pR) + (R)0.25 * (vL - vR);
+      R uS = (R)0.5 * (vL + vR) + pL - pR;
+      SL = rmin<R>(vL - pL, uS - pS);
+      SR = rmax<R>(vR + pR, uS + pS);
+    } else if (mL == 0 && mR == 1) {
+      R pR = sqrt((R)kGrav * fabs(rdR));
+      SL = vR - (R)2.0 * pR;
+      SR = vR + pR;
+    } else if (mL == 1 && mR == 0) {
+      R pL = sqrt((R)kGrav * fabs(rdL));
+      SL = vL - pL;
+      SR = vL + (R)2.0 * pL;
+    }
+    R Ey = hll<R>(SL, SR, dvL, dvR, rdL, rdR);
+    R Fy = hll<R>(SL, SR, FyL, FyR, duL, duR);
+    R Gy = hll<R>(SL, SR, GyL, GyR, dvL, dvR);
+    R Hy = hll<R>(SL, SR, HyL, HyR, dwL, dwR);
+    if (g == S.JB) { Ey = (R)0; Fy = (R)0; Gy = hydro<R>(reR, rh0); Hy = (R)0; }
+    if (g == S.JE + 1) { Ey = (R)0; Fy = (R)0; Gy = hydro<R>(reL, rh0); Hy = (R)0; }
+    if (mR == 0) {
+      Ey = (R)0; Fy = (R)0; Hy = (R)0;
+      Gy = (g == S.JB) ? (R)0 : hydro<R>(reL, rh0) * (R)mL;
+    } else if (mL == 0) {
+      Ey = (R)0; Fy = (R)0; Hy = (R)0;
+      Gy = (c0 == S.JE) ? (R)0 : hydro<R>(reR, rh0) * (R)mR;
+    }
+    const long long o = i3(S, i, g, k);
+    S.Ey[o] = Ey; S.Fy[o] = Fy; S.Gy[o] = Gy; S.Hy[o] = Hy;
+  }
+};
+
+// z faces k in [KB, KE+1] of an interior column (src/nhwave.F:1998-2023, 2719-2730)
+struct OpFluxZ {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    using R = T;
+    const long long o = i3(S, i, j, k);
+    if (k == S.KB || k == S.KE + 1) { S.Fz[o] = (R)0; S.Gz[o] = (R)0; S.Hz[o] = (R)0; return; }
+    const long long sz = S.sz;
+    const R dm = (R)(S.sigc[k - 1] - S.sigc[k - 2]), d0 = (R)(S.sigc[k] - S.sigc[k - 1]),
+            dp = (R)(S.sigc[k + 1] - S.sigc[k]);
+    const R hm = (R)(0.5 * S.dsig[k - 1]), h0 = (R)(0.5 * S.dsig[k]);
+    auto face = [&](const T* A, R& L, R& Rr) {
+      const R am = A[o - 2 * sz], a0 = A[o - sz], a1 = A[o], a2 = A[o + sz];
+      L = a0 + hm * lim_slope<R>(am, a0, a1, dm, d0);
+      Rr = a1 - h0 * lim_slope<R>(a0, a1, a2, d0, dp);
+    };
+    R uL, uR, vL, vR, wL, wR;
+    face(S.U, uL, uR); face(S.V, vL, vR); face(S.W, wL, wR);
+    const R om = S.Omega[o], ao = fabs(om);
+    S.Fz[o] = (R)0.5 * (om * (uL + uR) - ao * (uR - uL));
+    S.Gz[o] = (R)0.5 * (om * (vL + vR) - ao * (vR - vL));
+    S.Hz[o] = (R)0.5 * (om * (wL + wR) - ao * (wR - wL));
+  }
+};
+
+// =========================================================================
+//   eval_duvw, explicit part: R1, D, R2-R4, DU/DV/DW (src/nhwave.F:611-1182)
+// =========================================================================
+struct OpExplicit {
+  int istep;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    using R = T;
+    const long long c = i2(S, i, j);
+    const double dt = S.sc->dt;
+    double r1 = 0.0;
+    if (S.Mask[c] != 0) {
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k);
+        const double dEx = (double)S.Ex[o + 1] - (double)S.Ex[o];
+        const double dEy = (double)S.Ey[o + S.sy] - (double)S.Ey[o];
+        r1 = r1 - 1.0 / S.dx * dEx * S.dsig[k] - 1.0 / S.dy * dEy * S.dsig[k];
+      }
+      r1 = r1 + S.D[c] * S.SourceC[c];
+      S.D[c] = S.alpha[istep] * S.D0[c] + S.beta[istep] * (S.D[c] + dt * r1);
+      const R rdx = (R)(1.0 / S.dx), rdy = (R)(1.0 / S.dy), rdt = (R)dt, fc = (R)S.fcor;
+      const R sx = (R)S.SourceX[c], syy = (R)S.SourceY[c];
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k);
+        const R rds = (R)(1.0 / S.dsig[k]);
+        const R du = S.DU[o], dv = S.DV[o], dw = S.DW[o];
+        const R R2 = -rdx * (S.Fx[o + 1] - S.Fx[o]) - rdy * (S.Fy[o + S.sy] - S.Fy[o]) -
+                     rds * (S.Fz[o + S.sz] - S.Fz[o]) + fc * dv + sx;
+        const R R3 = -rdx * (S.Gx[o + 1] - S.Gx[o]) - rdy * (S.Gy[o + S.sy] - S.Gy[o]) -
+                     rds * (S.Gz[o + S.sz] - S.Gz[o]) - fc * du + syy;
+        const R R4 = -rdx * (S.Hx[o + 1] - S.Hx[o]) - rdy * (S.Hy[o + S.sy] - S.Hy[o]) -
+                     rds * (S.Hz[o + S.sz] - S.Hz[o]);
+        S.DU[o] = du + rdt * R2;
+        S.DV[o] = dv + rdt * R3;
+        S.DW[o] = dw + rdt * R4;
+      }
+    } else {
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k);
+        S.DU[o] = (R)0; S.DV[o] = (R)0; S.DW[o] = (R)0;
+      }
+    }
+    S.R1[c] = r1;
+    S.D[c] = dmax_(S.D[c], S.min_dep);
+  }
+};
+
+// D ghosts (wl_bc, walls) and Eta = D - Hc over the whole ghosted array
+struct OpWlBcEta {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
+    if (mi != i || mj != j) S.D[c] = S.D[i2(S, mi, mj)];
+    S.Eta[c] = S.D[c] - S.Hc[c];
+  }
+};
+
+// =========================================================================
+//              get_UVW + vel_bc (src/nhwave.F:1651-1683, 4416-5117)
+// =========================================================================
+struct OpGetUVW {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    const T d = (T)S.D[i2(S, i, j)];
+    S.U[o] = S.DU[o] / d;
+    S.V[o] = S.DV[o] / d;
+    S.W[o] = S.DW[o] / d;
+  }
+};
+
+// vel_bc, part A: lateral ghosts (walls) and the surface/bed face states of
+// every interior column after the kinematic conditions (KBC_surface/bottom).
+struct OpVelBcA {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
+    const long long c = i2(S, i, j);
+    if (ii && jj) {
+      const long long sz = S.sz;
+      auto zface = [&](const T* A, double& top, double& bot) {
+        // top: UzL(Kend1) = U(Kend) + 0.5 dsig(Kend) DelzU(Kend)
+        const int kt = S.KE, kb = S.KB;
+        const long long ot = i3(S, i, j, kt), ob = i3(S, i, j, kb);
+        double s_t = lim_slope<double>((double)A[ot - sz], (double)A[ot], (double)A[ot + sz],
+                                       S.sigc[kt] - S.sigc[kt - 1], S.sigc[kt + 1] - S.sigc[kt]);
+        double s_b = lim_slope<double>((double)A[ob - sz], (double)A[ob], (double)A[ob + sz],
+                                       S.sigc[kb] - S.sigc[kb - 1], S.sigc[kb + 1] - S.sigc[kb]);
+        top = (double)A[ot] + 0.5 * S.dsig[kt] * s_t;
+        bot = (double)A[ob] - 0.5 * S.dsig[kb] * s_b;
+      };
+      double uL, uR, vL, vR, wL, wR;
+      zface(S.U, uL, uR); zface(S.V, vL, vR); zface(S.W, wL, wR);
+      const double dt = S.sc->dt;
+      wL = (S.Eta[c] - S.Eta0[c]) / dt + S.DelxEta[c] * uL + S.DelyEta[c] * vL;
+      wR = -S.DeltH[c] - S.DelxH[c] * uR - S.DelyH[c] * vR;
+      S.zUL[c] = uL; S.zVL[c] = vL; S.zWL[c] = wL;
+      S.zUR[c] = uR; S.zVR[c] = vR; S.zWR[c] = wR;
+      return;
+    }
+    if (!ii && jj) {  // west/east ghost columns of interior rows
+      const int src = mirror(i, S.IB, S.IE);
+      const T s = (T)((i < S.IB ? S.bc_x0 : S.bc_xn) == 1 ? 1 : -1);
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k), q = i3(S, src, j, k);
+        S.U[o] = -S.U[q]; S.V[o] = s * S.V[q]; S.W[o] = s * S.W[q];
+        S.DU[o] = -S.DU[q]; S.DV[o] = s * S.DV[q]; S.DW[o] = s * S.DW[q];
+      }
+    } else if (ii && !jj) {  // south/north ghost rows of interior columns
+      const int src = mirror(j, S.JB, S.JE);
+      const T s = (T)((j < S.JB ? S.bc_y0 : S.bc_yn) == 1 ? 1 : -1);
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k), q = i3(S, i, src, k);
+        S.U[o] = s * S.U[q]; S.V[o] = -S.V[q]; S.W[o] = s * S.W[q];
+        S.DU[o] = s * S.DU[q]; S.DV[o] = -S.DV[q]; S.DW[o] = s * S.DW[q];
+      }
+    }
+  }
+};
+
+// vel_bc, part B: bed and surface ghosts of interior columns
+// (free-slip bed; Derakhti et al. stress condition at the surface)
+struct OpVelBcB {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    auto zl = [&](const double* a, int x, int y) -> double {
+      return (x >= S.IB && x <= S.IE && y >= S.JB && y <= S.JE) ? a[i2(S, x, y)] : 0.0;
+    };
+    const bool wet = S.Mask[c] != 0;
+    auto dx_ = [&](const double* a) -> double {
+      return wet ? lim_slope<double>(zl(a, i - 1, j), a[c], zl(a, i + 1, j), S.dx, S.dx) : 0.0;
+    };
+    auto dy_ = [&](const double* a) -> double {
+      return wet ? lim_slope<double>(zl(a, i, j - 1), a[c], zl(a, i, j + 1), S.dy, S.dy) : 0.0;
+    };
+    const double DelxUzL = dx_(S.zUL), DelxVzL = dx_(S.zVL), DelxWzL = dx_(S.zWL);
+    const double DelyUzL = dy_(S.zUL), DelyVzL = dy_(S.zVL), DelyWzL = dy_(S.zWL);
+    const double dxe = S.DelxEta[c], dye = S.DelyEta[c], Dij = S.D[c];
+    const double Atop = sqrt(1.0 + dxe * dxe + dye * dye);
+    const double Fext_Wind1 = 1.0 / Atop * ((1 - dxe * dxe) * S.Wsx[c] - dxe * dye * S.Wsy[c]);
+    const double Fext_Wind2 = 1.0 / Atop * ((1 - dye * dye) * S.Wsy[c] - dxe * dye * S.Wsx[c]);
+    const double MinDepBC = (double)0.01f;
+    const double WzLt = S.zWL[c], WzRb = S.zWR[c], UzLt = S.zUL[c], VzLt = S.zVL[c];
+    const int KB = S.KB, KE = S.KE;
+    for (int k = 1; k <= NG; ++k) {
+      const long long ob = i3(S, i, j, KB - k), oi = i3(S, i, j, KB + k - 1);
+      const long long ot = i3(S, i, j, KE + k), os = i3(S, i, j, KE - k + 1);
+      S.DW[ob] = (T)(2.0 * Dij * WzRb - (double)S.DW[oi]);
+      S.DU[ob] = S.DU[oi];
+      S.DV[ob] = S.DV[oi];
+      const double dsg = S.sigc[KE + k] - S.sigc[KE - k + 1];
+      const double DWs = (double)S.DW[os], DUs = (double)S.DU[os], DVs = (double)S.DV[os];
+      S.DW[ot] = (T)(2.0 * Dij * WzLt - DWs);
+      double du = DUs + dsg * (Fext_Wind1 * (Dij * Dij / Atop / S.visc_top) -
+                               dxe * (Dij * WzLt - DWs) / (dsg / 2.0) +
+                               Dij * Dij / (Atop * Atop) *
+                                   (+2.0 * dxe * DelxUzL - (1.0 - dxe * dxe) * DelxWzL +
+                                    dye * (DelyUzL + DelxVzL + dxe * DelyWzL)));
+      const double DUtop_old = 2.0 * Dij * UzLt - DUs;
+      if (DUtop_old > 0.) du = dmin_(3.0 * DUtop_old, dmax_(-1.0 * DUtop_old, du));
+      else if (DUtop_old < 0.) du = dmax_(3.0 * DUtop_old, dmin_(-1.0 * DUtop_old, du));
+      if (Dij < MinDepBC) du = DUs;
+      double dv = DVs + dsg * (Fext_Wind2 * (Dij * Dij / Atop / S.visc_top) -
+                               dye * (Dij * WzLt - DWs) / (dsg / 2.0) +
+                               Dij * Dij / (Atop * Atop) *
+                                   (+2.0 * dye * DelyVzL - (1.0 - dye * dye) * DelyWzL +
+                                    dxe * (DelxVzL + DelyUzL + dye * DelxWzL)));
+      const double DVtop_old = 2.0 * Dij * VzLt - DVs;
+      if (DVtop_old > 0.) dv = dmin_(3.0 * DVtop_old, dmax_(-1.0 * DVtop_old, dv));
+      else if (DVtop_old < 0.) dv = dmax_(3.0 * DVtop_old, dmin_(-1.0 * DVtop_old, dv));
+      if (Dij < MinDepBC) dv = DVs;
+      S.DU[ot] = (T)du;
+      S.DV[ot] = (T)dv;
+      const T d = (T)Dij;
+      S.U[ob] = S.DU[ob] / d; S.V[ob] = S.DV[ob] / d; S.W[ob] = S.DW[ob] / d;
+      S.U[ot] = S.DU[ot] / d; S.V[ot] = S.DV[ot] / d; S.W[ot] = S.DW[ot] / d;
+    }
+  }
+};
+
+// initial: DU = D*U*Mask over all cells (src/initialize.F:3160-3170)
+struct OpInitDU {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long c = i2(S, i, j), o = i3(S, i, j, k);
+    const double d = S.D[c], m = (double)S.Mask[c];
+    S.DU[o] = (T)((double)(T)(d * (double)S.U[o]) * m);
+    S.DV[o] = (T)((double)(T)(d * (double)S.V[o]) * m);
+    S.DW[o] = (T)((double)(T)(d * (double)S.W[o]) * m);
+  }
+};
+
+// =========================================================================
+//      Poisson: generate_coef_rhs (src/pressure.F:475-840), FP64
+// =========================================================================
+struct OpPoissonCoef {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const int ic = ic_of(S, i, j, k);
+    const long long sy = S.sy, sz = S.sz;
+    auto inside = [&](int x, int y) { return x >= S.IB && x <= S.IE && y >= S.JB && y <= S.JE; };
+    const double sgk = S.sig[k];
+    // DelxS/DelyS at level sig(k) of interior columns, zero outside (src/pressure.F:494-505)
+    auto dxs = [&](int x, int y) -> double {
+      if (!inside(x, y)) return 0.0;
+      const long long q = i2(S, x, y);
+      return (1. - sgk) / S.D[q] * S.DelxH[q] - sgk / S.D[q] * S.DelxEta[q];
+    };
+    auto dys = [&](int x, int y) -> double {
+      if (!inside(x, y)) return 0.0;
+      const long long q = i2(S, x, y);
+      return (1. - sgk) / S.D[q] * S.DelyH[q] - sgk / S.D[q] * S.DelyEta[q];
+    };
+    const long long q = i2(S, i, j);
+    const double Dq = S.D[q];
+    const double DelxS = dxs(i, j), DelyS = dys(i, j), DelzS = 1. / Dq;
+    const double A1 = DelxS * DelxS + DelyS * DelyS + DelzS * DelzS;
+    const double dsk = S.dsig[k], dskm = S.dsig[k - 1];
+    const double s = dsk + dskm, hk = 0.5 * (dsk + dskm);
+    const double dx = S.dx, dy = S.dy;
+    // Rhs (src/pressure.F:521-525); Uf/Vf: linear interpolation to sig(k) (src/nhwave.F:1346-1355)
+    const double fint = dsk / (dsk + dskm);
+    const long long o = i3(S, i, j, k);
+    auto uf = [&](const T* A, long long e) -> double {
+      return (1.0 - fint) * (double)A[e] + fint * (double)A[e - sz];
+    };
+    double rhs = -((uf(S.U, o + 1) - uf(S.U, o - 1)) / (2.0 * dx) +
+                   ((double)S.U[o] - (double)S.U[o - sz]) / hk * DelxS +
+                   (uf(S.V, o + sy) - uf(S.V, o - sy)) / (2.0 * dy) +
+                   ((double)S.V[o] - (double)S.V[o - sz]) / hk * DelyS +
+                   ((double)S.W[o] - (double)S.W[o - sz]) / hk * DelzS - S.SourceC[q]) *
+                 kRho0 / S.sc->dt;
+    double C[NCOEF + 1];
+    C[1] = 2. / (dx * dx) + 2. / (dy * dy) + A1 / (hk * dsk) + A1 / (hk * dskm);
+    C[2] = -1. / (dx * dx);
+    C[3] = -1. / (dy * dy);
+    C[4] = dys(i, j - 1) / (2. * dy * s) + DelyS / (2. * dy * s);
+    C[5] = dxs(i - 1, j) / (2. * dx * s) + DelxS / (2. * dx * s);
+    C[6] = -A1 / (hk * dsk);
+    C[7] = -(dxs(i + 1, j) / (2. * dx * s) + DelxS / (2. * dx * s));
+    C[8] = -(dys(i, j + 1) / (2. * dy * s) + DelyS / (2. * dy * s));
+    C[9] = -1. / (dx * dx);
+    C[10] = -1. / (dy * dy);
+    C[11] = dys(i, j + 1) / (2. * dy * s) + DelyS / (2. * dy * s);
+    C[12] = dxs(i + 1, j) / (2. * dx * s) + DelxS / (2. * dx * s);
+    C[13] = -A1 / (hk * dskm);
+    C[14] = -(dxs(i - 1, j) / (2. * dx * s) + DelxS / (2. * dx * s));
+    C[15] = -(dys(i, j - 1) / (2. * dy * s) + DelyS / (2. * dy * s));
+    // boundary folds in the reference's order (src/pressure.F:649-814)
+    if (i == S.IB) { C[1] = C[1] + C[9]; C[6] = C[6] + C[5]; C[13] = C[13] + C[14]; C[9] = C[5] = C[14] = 0.0; }
+    if (i == S.IE) { C[1] = C[1] + C[2]; C[6] = C[6] + C[7]; C[13] = C[13] + C[12]; C[2] = C[7] = C[12] = 0.0; }
+    if (j == S.JB) { C[1] = C[1] + C[10]; C[6] = C[6] + C[4]; C[13] = C[13] + C[15]; C[10] = C[4] = C[15] = 0.0; }
+    if (j == S.JE) { C[1] = C[1] + C[3]; C[6] = C[6] + C[8]; C[13] = C[13] + C[11]; C[3] = C[8] = C[11] = 0.0; }
+    if (k == S.KB) {
+      if (S.slide) {
+        const double* D = S.D;
+        const double* H2 = S.Delt2H;
+        rhs = rhs + kRho0 * (dsk + dskm) *
+                        (C[13] * D[q] * H2[q] + C[12] * D[q + 1] * H2[q + 1] + C[11] * D[q + sy] * H2[q + sy] +
+                         C[14] * D[q - 1] * H2[q - 1] + C[15] * D[q - sy] * H2[q - sy]);
+      }
+      C[6] = C[6] + C[13]; C[7] = C[7] + C[12]; C[8] = C[8] + C[11]; C[5] = C[5] + C[14]; C[4] = C[4] + C[15];
+      C[13] = C[12] = C[11] = C[14] = C[15] = 0.0;
+    }
+    if (k == S.KE) { C[4] = C[5] = C[6] = C[7] = C[8] = 0.0; }
+    const size_t n = (size_t)S.neq;
+    for (int m = 1; m <= NCOEF; ++m) S.coef64[(m - 1) * n + ic] = C[m];
+    S.rhs64[ic] = rhs;
+  }
+};
+
+// copy of the FP64 operator into the inner precision (FP32 form only)
+struct OpCoefToT {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const int ic = ic_of(S, i, j, k);
+    const size_t n = (size_t)S.neq;
+    for (int m = 0; m < NCOEF; ++m) S.coefT[m * n + ic] = (T)S.coef64[m * n + ic];
+  }
+};
+
+// vertical-line preconditioner factors: tridiagonal (C13, C1, C6) per column
+struct OpLineFactor {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const size_t n = (size_t)S.neq, mn = (size_t)S.M * S.N;
+    const size_t base = (size_t)(i - S.IB) + (size_t)S.M * (j - S.JB);
+    double cpm = 0.0;
+    for (int k = 0; k < S.K; ++k) {
+      const size_t ic = base + mn * k;
+      const double a = k > 0 ? S.coef64[12 * n + ic] : 0.0;
+      const double b = S.coef64[ic];
+      const double c = k < S.K - 1 ? S.coef64[5 * n + ic] : 0.0;
+      const double den = b - a * cpm;
+      const double inv = 1.0 / den;
+      cpm = c * inv;
+      S.lcp[ic] = (T)cpm;
+      S.linv[ic] = (T)inv;
+    }
+  }
+};
+
+// P interior <- FP64 solution; lateral P ghosts (src/pressure.F:185-239)
+struct OpPFromX {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    S.P[i3(S, i, j, k)] = S.xsol64[ic_of(S, i, j, k)];
+  }
+};
+struct OpXFromP {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    S.xsol64[ic_of(S, i, j, k)] = S.P[i3(S, i, j, k)];
+  }
+};
+struct OpPGhost {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
+    if (ii == jj) return;  // interior or corner
+    const int si = mirror(i, S.IB, S.IE), sj = mirror(j, S.JB, S.JE);
+    for (int k = S.KB; k <= S.KE; ++k) S.P[i3(S, i, j, k)] = S.P[i3(S, si, sj, k)];
+  }
+};
+
+// projection_corrector (src/nhwave.F:487-536)
+struct OpProjection {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j);
+    if (S.Mask[q] == 0) return;
+    const long long o = i3(S, i, j, k), sy = S.sy, sz = S.sz;
+    const double* P = S.P;
+    const double dx = S.dx, dy = S.dy;
+    const double DelxP = 0.5 * ((P[o + 1] - P[o - 1]) / (2. * dx) + (P[o + 1 + sz] - P[o - 1 + sz]) / (2. * dx));
+    const double DelyP = 0.5 * ((P[o + sy] - P[o - sy]) / (2. * dy) + (P[o + sy + sz] - P[o - sy + sz]) / (2. * dy));
+    const double DelzP = (P[o + sz] - P[o]) / S.dsig[k];
+    const double Dq = S.D[q], sc = S.sigc[k];
+    const double DelxSc = (1.0 - sc) / Dq * S.DelxH[q] - sc / Dq * S.DelxEta[q];
+    const double DelySc = (1.0 - sc) / Dq * S.DelyH[q] - sc / Dq * S.DelyEta[q];
+    const double dt = S.sc->dt;
+    S.DU[o] = (T)((double)S.DU[o] - Dq * dt / kRho0 * (DelxP + DelzP * DelxSc));
+    S.DV[o] = (T)((double)S.DV[o] - Dq * dt / kRho0 * (DelyP + DelzP * DelySc));
+    S.DW[o] = (T)((double)S.DW[o] - dt / kRho0 * DelzP);
+  }
+};
+
+// SSP-RK combination, mask and Froude cap (src/nhwave.F:1227-1261)
+struct OpSSP {
+  int istep;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    using R = T;
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    const R al = (R)S.alpha[istep], be = (R)S.beta[istep];
+    R du = al * S.DU0[o] + be * S.DU[o];
+    R dv = al * S.DV0[o] + be * S.DV[o];
+    R dw = al * S.DW0[o] + be * S.DW[o];
+    const int m = S.Mask[q];
+    if (m == 0) { du = (R)0; dv = (R)0; dw = (R)0; }
+    if (S.froude_on && m > 0) {
+      const double Dq = S.D[q];
+      const double FroudeU = sqrt(kGrav * Dq) * S.froude_cap * Dq;
+      const double a = (double)du, b = (double)dv, cc = (double)dw;
+      const double DUU = sqrt(a * a + b * b + cc * cc);
+      if (DUU > FroudeU) {
+        const double ang = atan2(b, a);
+        du = (R)(FroudeU * cos(ang));
+        dv = (R)(FroudeU * sin(ang));
+        dw = (R)0;
+      }
+    }
+    S.DU[o] = du; S.DV[o] = dv; S.DW[o] = dw;
+  }
+};
+
+// =========================================================================
+//               get_Omega (src/nhwave.F:1411-1648)
+// =========================================================================
+struct OpOmegaX {  // Ex on x faces from the new state; EtaxL/EtaxR kept for source_terms
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int f, int j, int k) const {
+    using R = T;
+    const int c0 = f - 1, c1 = f;
+    const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
+    const long long q0 = i2(S, c0, j), q1 = q0 + 1;
+    const int mL = S.Mask[q0], mR = S.Mask[q1];
+    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx;
+    auto sl = [&](const T* A, long long e, int m) -> R {
+      return m == 0 ? (R)0 : lim_slope<R>(A[e - 1], A[e], A[e + 1], rdx, rdx);
+    };
+    const R uL = S.U[e0] + hdx * sl(S.U, e0, mL), uR = S.U[e1] - hdx * sl(S.U, e1, mR);
+    R duL = S.DU[e0] + hdx * sl(S.DU, e0, mL), duR = S.DU[e1] - hdx * sl(S.DU, e1, mR);
+    double etaL = S.Eta[q0] + 0.5 * S.dx * S.DelxEta[q0];
+    double etaR = S.Eta[q1] - 0.5 * S.dx * S.DelxEta[q1];
+    const double hf = S.Hfx[q1];
+    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
+    if (c0 >= S.IB && c0 <= S.IE) {
+      if ((mL == 1 && mR == 0) || mL == 0) { etaL = S.Eta[q0]; dL = S.D[q0]; duL = (R)0; }
+    }
+    if (c1 >= S.IB && c1 <= S.IE) {
+      const int mRR = S.Mask[q1 + 1];
+      if (mR == 1 && mRR == 0) {
+      } else if ((mR == 1 && mL == 0) || mR == 0) { etaR = S.Eta[q1]; dR = S.D[q1]; duR = (R)0; }
+    }
+    if (k == S.KB) { S.EtaxL[q1] = etaL; S.EtaxR[q1] = etaR; }
+    const R rdL = (R)dL, rdR = (R)dR;
+    R SL = (R)0, SR = (R)0;
+    if (mL == 1 && mR == 1) {
+      R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
+      R pS = (R)0.5 * (pL + pR) + (R)0.25 * (uL - uR);
+      R uS = (R)0.5 * (uL + uR) + pL - pR;
+      SL = rmin<R>(uL - pL, uS - pS);
+      SR = rmax<R>(uR + pR, uS + pS);
+    } else if (mL == 0 && mR == 1) {
+      R pR = sqrt((R)kGrav * fabs(rdR));
+      SL = uR - (R)2.0 * pR;
+      SR = uR + pR;
+    } else if (mL == 1 && mR == 0) {
+      R pL = sqrt((R)kGrav * fabs(rdL));
+      SL = uL - pL;
+      SR = uL + (R)2.0 * pL;
+    }
+    R Ex = hll<R>(SL, SR, duL, duR, rdL, rdR);
+    if (f == S.IB || f == S.IE + 1) Ex = (R)0;
+    S.Ex[i3(S, f, j, k)] = Ex;
+  }
+};
+struct OpOmegaY {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int g, int k) const {
+    using R = T;
+    const int c0 = g - 1, c1 = g;
+    const long long sy = S.sy;
+    const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
+    const long long q0 = i2(S, i, c0), q1 = q0 + sy;
+    const int mL = S.Mask[q0], mR = S.Mask[q1];
+    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy;
+    auto sl = [&](const T* A, long long e, int m) -> R {
+      return m == 0 ? (R)0 : lim_slope<R>(A[e - sy], A[e], A[e + sy], rdy, rdy);
+    };
+    const R vL = S.V[e0] + hdy * sl(S.V, e0, mL), vR = S.V[e1] - hdy * sl(S.V, e1, mR);
+    R dvL = S.DV[e0] + hdy * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdy * sl(S.DV, e1, mR);
+    double etaL = S.Eta[q0] + 0.5 * S.dy * S.DelyEta[q0];
+    double etaR = S.Eta[q1] - 0.5 * S.dy * S.DelyEta[q1];
+    const double hf = S.Hfy[q1];
+    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
+    if (c0 >= S.JB && c0 <= S.JE) {
+      if ((mL == 1 && mR == 0) || mL == 0) { etaL = S.Eta[q0]; dL = S.D[q0]; dvL = (R)0; }
+    }
+    if (c1 >= S.JB && c1 <= S.JE) {
+      const int mRR = S.Mask[q1 + sy];
+      if (mR == 1 && mRR == 0) {
+      } else if ((mR == 1 && mL == 0) || mR == 0) { etaR = S.Eta[q1]; dR = S.D[q1]; dvR = (R)0; }
+    }
+    if (k == S.KB) { S.EtayL[q1] = etaL; S.EtayR[q1] = etaR; }
+    const R rdL = (R)dL, rdR = (R)dR;
+    R SL = (R)0, SR = (R)0;
+    if (mL == 1 && mR == 1) {
+      R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
+      R pS = (R)0.5 * (pL + pR) + (R)0.25 * (vL - vR);
+      R uS = (R)0.5 * (vL + vR) + pL - pR;
+      SL = rmin<R>(vL - pL, uS - pS);
+      SR = rmax<R>(vR + pR, uS + pS);
+    } else if (mL == 0 && mR == 1) {
+      R pR = sqrt((R)kGrav * fabs(rdR));
+      SL = vR - (R)2.0 * pR;
+      SR = vR + pR;
+    } else if (mL == 1 && mR == 0) {
+      R pL = sqrt((R)kGrav * fabs(rdL));
+      SL = vL - pL;
+      SR = vL + (R)2.0 * pL;
+    }
+    R Ey = hll<R>(SL, SR, dvL, dvR, rdL, rdR);
+    if (g == S.JB || g == S.JE + 1) Ey = (R)0;
+    S.Ey[i3(S, i, g, k)] = Ey;
+  }
+};
+// Omega column scan (src/nhwave.F:1617-1628)
+struct OpOmegaScan {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const bool wet = S.Mask[q] != 0;
+    const double r1 = S.R1[q];
+    double om = 0.0;
+    S.Omega[i3(S, i, j, S.KB)] = (T)0;
+    for (int k = S.KB + 1; k <= S.KE + 1; ++k) {
+      const long long o = i3(S, i, j, k - 1);
+      const double dEx = (double)S.Ex[o + 1] - (double)S.Ex[o];
+      const double dEy = (double)S.Ey[o + S.sy] - (double)S.Ey[o];
+      double v = om - S.dsig[k - 1] * (r1 + dEx / S.dx + dEy / S.dy);
+      if (!wet) v = 0.0;
+      S.Omega[i3(S, i, j, k)] = (T)v;
+      om = (double)(T)v;
+    }
+  }
+};
+
+// sponge_damping over every wet cell of the ghosted array (src/nhwave.F:6463-6502)
+struct OpSponge {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    if (S.Mask[c] != 1) return;
+    const double time = S.sc->time;
+    const double Ramp = S.tramp > 0.0 ? tanh(time / S.tramp) : 1.0;
+    const double Ucur = Ramp * S.cur_wave;
+    const double sp = S.Sponge[c];
+    S.Eta[c] = S.Eta[c] * sp;
+    S.D[c] = S.Eta[c] + S.Hc[c];
+    const double d = S.D[c];
+    for (int k = 0; k < S.Kloc; ++k) {
+      const long long o = i3(S, i, j, k);
+      const double u = ((double)S.U[o] - Ucur) * sp + Ucur;
+      const double v = (double)S.V[o] * sp;
+      S.U[o] = (T)u;
+      S.V[o] = (T)v;
+      S.DU[o] = (T)(d * (double)(T)u);
+      S.DV[o] = (T)(d * (double)(T)v);
+    }
+  }
+};
+
+// =========================================================================
+//                 estimate_dt (src/nhwave.F:3694-3874)
+// =========================================================================
+template <class T>
+__global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n = (long long)S.neq;
+  double m = kLarge;
+  for (; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = S.IB + (int)(t % S.M);
+    const long long r = t / S.M;
+    const int j = S.JB + (int)(r % S.N), k = S.KB + (int)(r / S.N);
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    const double Dq = S.D[q];
+    double tmp1 = fabs((double)S.U[o]) + sqrt(kGrav * Dq);
+    tmp1 = dmax_(tmp1, kSmall);
+    m = dmin_(m, S.dx / tmp1);
+    tmp1 = fabs((double)S.V[o]) + sqrt(kGrav * Dq);
+    tmp1 = dmax_(tmp1, kSmall);
+    m = dmin_(m, S.dy / tmp1);
+    tmp1 = dmax_(fabs((double)S.W[o]), kSmall);
+    m = dmin_(m, S.dsig[k] * Dq / tmp1);
+  }
+  for (int o = 16; o > 0; o >>= 1) m = dmin_(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+}
+template <class T>
+__global__ void k_dt_finalize(Dev<T> S) {
+  DevScal* sc = S.sc;
+  const double tmp2 = __longlong_as_double((long long)sc->dtmin_bits);
+  sc->dtmin_bits = (unsigned long long)__double_as_longlong(kLarge);
+  sc->dt_old = sc->dt;
+  const double dt_growth = (double)1.05f * sc->dt_old;
+  const double dt_courant = S.cfl * tmp2;
+  double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), kLarge), S.dt_max);
+  sc->dt = dt;
+  if (dt < S.dt_min) { sc->status = 5; return; }
+  sc->time = sc->time + dt;
+  sc->run_step = sc->run_step + 1;
+}
+
+// =========================================================================
+//            update_bathymetry, RIGID_3D (src/nhwave.F:5755-6071)
+// =========================================================================
+struct OpSlideA {  // Ho = Hc everywhere; new Hc in the interior
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    S.Ho[c] = S.Hc[c];
+    if (i < S.IB || i > S.IE || j < S.JB || j > S.JE) return;
+    const double time = S.sc->time;
+    const double st = S.sl_s0 * log(cosh(time / S.sl_t0)) * S.sl_cosslope;
+    const double x0 = S.sl_x0 + st * S.sl_cosa, y0 = S.sl_y0 + st * S.sl_sina;
+    const double xt = (S.xc[i] - x0) * S.sl_cosa + (S.yc[j] - y0) * S.sl_sina;
+    const double yt = -((S.xc[i] - x0) * S.sl_sina) + (S.yc[j] - y0) * S.sl_cosa;
+    const double zt = S.sl_T / (1 - S.sl_e) * (1.0 / cosh(S.sl_kb * xt) / cosh(S.sl_kw * yt) - S.sl_e);
+    S.Hc[c] = S.Hc0[c] - dmax_(0.0, zt);
+  }
+};
+struct OpSlideB {  // Hc ghosts (phi_2D_coll)
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
+    if (mi != i || mj != j) S.Hc[i2(S, i, j)] = S.Hc[i2(S, mi, mj)];
+  }
+};
+struct OpSlideC {  // face depths, slopes, dH/dt (src/nhwave.F:6026-6069); grid (Mloc+1) x (Nloc+1)
+  template <class T>
+  __device__ double hcx(const Dev<T>& S, int i, int j) const {
+    // Hc(i,j) with the Fortran column-major continuation past the last row/column
+    if (i == S.Mloc) { i = 0; ++j; }
+    if (j >= S.Nloc) return 0.0;
+    return S.Hc[i2(S, i, j)];
+  }
+  template <class T>
+  __device__ double hfx(const Dev<T>& S, int i, int j) const {  // i in [0, Mloc], j < Nloc
+    if (i == 0) i = 1;
+    if (i == S.Mloc) i = S.Mloc - 1;
+    return 0.5 * (S.Hc[i2(S, i, j)] + hcx(S, i + 1, j));
+  }
+  template <class T>
+  __device__ double hfy(const Dev<T>& S, int i, int j) const {  // j in [0, Nloc], i < Mloc
+    if (j == 0) j = 1;
+    if (j == S.Nloc) j = S.Nloc - 1;
+    return 0.5 * (S.Hc[i2(S, i, j)] + hcx(S, i, j + 1));
+  }
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int) const {
+    const long long c = i2(S, i, j);
+    if (j < S.Nloc) { const double h = hfx(S, i, j); S.Hfx[c] = h; S.Hfx0[c] = h; }
+    if (i < S.Mloc) { const double h = hfy(S, i, j); S.Hfy[c] = h; S.Hfy0[c] = h; }
+    if (i < S.Mloc && j < S.Nloc) {
+      S.DelxH[c] = (hfx(S, i + 1, j) - hfx(S, i, j)) / S.dx;
+      S.DelyH[c] = (hfy(S, i, j + 1) - hfy(S, i, j)) / S.dy;
+      const double dt = S.sc->dt;
+      const double old = S.DeltH[c];
+      const double nw = (S.Hc[c] - S.Ho[c]) / dt;
+      S.DeltHo[c] = old;
+      S.DeltH[c] = nw;
+      if (S.sc->run_step > 2) S.Delt2H[c] = (nw - old) / dt;
+    }
+  }
+};
+
+// =========================================================================
+//                 update_mask (src/nhwave.F:5403-5456)
+// =========================================================================
+struct OpMaskA {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    int m = S.Mask[c];
+    if (i >= S.IB && i <= S.IE && j >= S.JB && j <= S.JE && S.Mask_Struct[c] != 0) {
+      const double thr = (double)1.e-6f, md = S.min_dep;
+      const double* E = S.Eta;
+      const double* D = S.D;
+      const int* Mk = S.Mask;
+      if (Mk[c] == 0) {
+        const long long nb[4] = {c - 1, c + 1, c - S.sy, c + S.sy};
+        for (int q = 0; q < 4; ++q)
+          if (Mk[nb[q]] == 1 && E[nb[q]] > E[c] && D[nb[q]] - md > thr) m = 1;
+      } else if (fabs(D[c] - md) <= thr) {
+        m = 0;
+        // the neighbours read E/D only under a D > MinDep + 1e-6 test, which a
+        // cell that dries fails before and after this write
+        const double e = md - S.Hc[c];
+        S.Eta[c] = e;
+        S.D[c] = e + S.Hc[c];
+      }
+    }
+    S.MaskT[c] = m;
+  }
+};
+struct OpMaskB {
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    const int* Mt = S.MaskT;
+    S.Mask[c] = Mt[c] * S.Mask_Struct[c];
+    if (i >= S.IB && i <= S.IE && j >= S.JB && j <= S.JE) {
+      auto m = [&](long long x) { return Mt[x] * S.Mask_Struct[x]; };
+      const long long sy = S.sy;
+      S.Mask9[c] = m(c) * m(c - 1) * m(c + 1) * m(c + 1 + sy) * m(c + sy) * m(c - 1 + sy) * m(c + 1 - sy) *
+                   m(c - sy) * m(c - 1 - sy);
+    }
+  }
+};
+
+// =========================================================================
+//                             diagnostics
+// =========================================================================
+template <class T>
+__global__ void k_mass(Dev<T> S, double* out) {
+  // MassVolume = sum over interior (j outer, i inner) of D*dx*dy, FP64, in order
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double m = 0.0;
+  for (int j = S.JB; j <= S.JE; ++j)
+    for (int i = S.IB; i <= S.IE; ++i) m = m + S.D[i2(S, i, j)] * S.dx * S.dy;
+  *out = m;
+}
+
+}  // namespace nhw

@@ -1,0 +1,255 @@
+// setup_host.cpp -- host-side set-up of one scenario: generate_grid
+// (src/initialize.F:1647-1729), read_bathymetry (src/initialize.F:1734-2175,
+// CELL_CENTER / CELL_GRID and the RIGID_3D slide), update_wind for a constant
+// wind (src/nhwave.F:5333-5400), calculate_sponge (src/nhwave.F:6405-6460) and
+// the non-optional parts of initial (src/initialize.F:2502-3408) up to the
+// vel_bc call, which runs on the device.  Built with -ffp-contract=off so the
+// arithmetic is the reference's, operation for operation.
+#include "setup_host.h"
+
+#include <cmath>
+#include <cstring>
+
+namespace nhw {
+namespace {
+const double kPiH = (double)3.141592653f;
+const double kGravH = (double)9.81f;
+inline double dmx(double a, double b) { return a > b ? a : b; }
+inline double dmn(double a, double b) { return a < b ? a : b; }
+}  // namespace
+
+int check_params(const nhw_params& p) {
+  if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1) return NHW_ERR_ARG;
+  if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
+  if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
+  if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+  for (int b : {p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn})
+    if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+  if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > 2) return NHW_ERR_UNSUPPORTED;
+  if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
+  if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
+  if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
+  if (p.wavemaker && !(p.per_wave > 0 && p.dep_wave > 0)) return NHW_ERR_ARG;
+  return NHW_OK;
+}
+
+double wave_number(double Segma, double Dep) {
+  double Wn = (Segma * Segma) / (kGravH * std::pow(std::tanh(Segma * Segma * Dep / kGravH), 0.5));
+  double error = 100.;
+  int guard = 0;
+  while (error >= (double)1.0e-8f && guard++ < 200) {
+    const double Fk = Segma * Segma - kGravH * Wn * std::tanh(Wn * Dep);
+    const double ch = std::cosh(Wn * Dep);
+    const double Fkdif = -(kGravH * (std::tanh(Wn * Dep) + (Wn * Dep) / (ch * ch)));
+    const double Wn_new = Wn - Fk / Fkdif;
+    error = std::fabs((Wn - Wn_new) / Wn);
+    Wn = Wn_new;
+  }
+  return Wn;
+}
+
+int host_setup(const nhw_params& p, const double* depth, const double* eta0, const double* uvw0,
+               HostInit& h) {
+  const int M = p.Mglob, N = p.Nglob, K = p.Kglob;
+  const int Ml = M + 4, Nl = N + 4, Kl = K + 4, Ml1 = Ml + 1, Nl1 = Nl + 1, Kl1 = Kl + 1;
+  h.Mloc = Ml; h.Nloc = Nl; h.Kloc = Kl;
+  // Fortran 1-based accessors
+  auto a2 = [&](std::vector<double>& v, int n1, int i, int j) -> double& { return v[(size_t)(i - 1) + (size_t)n1 * (j - 1)]; };
+  auto m2 = [&](std::vector<int32_t>& v, int i, int j) -> int32_t& { return v[(size_t)(i - 1) + (size_t)Ml * (j - 1)]; };
+  const size_t c2 = (size_t)Ml * Nl;
+  h.x.assign(Ml1, 0.0); h.xc.assign(Ml, 0.0); h.y.assign(Nl1, 0.0); h.yc.assign(Nl, 0.0);
+  h.sig.assign(Kl1, 0.0); h.dsig.assign(Kl, 0.0); h.sigc.assign(Kl, 0.0);
+  for (auto* v : {&h.Hc, &h.Hc0, &h.DelxH, &h.DelyH, &h.Eta, &h.D, &h.Sponge, &h.Wsx, &h.Wsy}) v->assign(c2, 0.0);
+  h.Hfx.assign((size_t)Ml1 * Nl, 0.0); h.Hfy.assign((size_t)Ml * Nl1, 0.0);
+  h.Mask.assign(c2, 0); h.Mask_Struct.assign(c2, 0); h.Mask9.assign(c2, 0);
+  const size_t c3 = c2 * Kl;
+  h.U.assign(c3, 0.0); h.V.assign(c3, 0.0); h.W.assign(c3, 0.0);
+  const int Ib = 3, Ie = Ml - 2, Jb = 3, Je = Nl - 2, Kb = 3, Ke = Kl - 2;
+  const double dx = p.dx, dy = p.dy;
+  // ---- generate_grid
+  auto X = [&](int i) -> double& { return h.x[i - 1]; };
+  auto XC = [&](int i) -> double& { return h.xc[i - 1]; };
+  auto Y = [&](int j) -> double& { return h.y[j - 1]; };
+  auto YC = [&](int j) -> double& { return h.yc[j - 1]; };
+  X(Ib) = 0.0;
+  for (int i = Ib + 1; i <= Ml1; ++i) { X(i) = X(i - 1) + dx; XC(i - 1) = X(i - 1) + 0.5 * dx; }
+  for (int i = Ib - 1; i >= Ib - 2; --i) { X(i) = X(i + 1) - dx; XC(i) = X(i + 1) - 0.5 * dx; }
+  Y(Jb) = 0.0;
+  for (int j = Jb + 1; j <= Nl1; ++j) { Y(j) = Y(j - 1) + dy; YC(j - 1) = Y(j - 1) + 0.5 * dy; }
+  for (int j = Jb - 1; j >= Jb - 2; --j) { Y(j) = Y(j + 1) - dy; YC(j) = Y(j + 1) - 0.5 * dy; }
+  auto DS = [&](int k) -> double& { return h.dsig[k - 1]; };
+  auto SG = [&](int k) -> double& { return h.sig[k - 1]; };
+  auto SC = [&](int k) -> double& { return h.sigc[k - 1]; };
+  if (p.ivgrd == 2) {
+    DS(Kb) = (p.grd_r - 1.0) / (std::pow(p.grd_r, (double)(float)K) - 1.0);
+    for (int k = Kb + 1; k <= Ke; ++k) DS(k) = DS(k - 1) * p.grd_r;
+    for (int k = 1; k <= 2; ++k) DS(Kb - k) = DS(Kb + k - 1);
+    for (int k = 1; k <= 2; ++k) DS(Ke + k) = DS(Ke - k + 1);
+  } else {
+    const double d = (double)(1.0f / (float)K);
+    for (int k = 1; k <= Kl; ++k) DS(k) = d;
+  }
+  SG(Kb) = 0.0;
+  for (int k = Kb + 1; k <= Kl1; ++k) { SG(k) = SG(k - 1) + DS(k - 1); SC(k - 1) = SG(k - 1) + 0.5 * DS(k - 1); }
+  for (int k = Kb - 1; k >= 1; --k) { SG(k) = SG(k + 1) - DS(k); SC(k) = SG(k + 1) - 0.5 * DS(k); }
+  // ---- read_bathymetry
+  auto HC = [&](int i, int j) -> double& { return a2(h.Hc, Ml, i, j); };
+  if (p.depth_type == NHW_DEPTH_CELL_GRID) {
+    auto HG = [&](int i, int j) { return depth[(size_t)(i - 1) + (size_t)(M + 1) * (j - 1)]; };
+    auto Mp = [&](int i, int j) { return HG(i, j) < -1000.0 ? 0 : 1; };
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = Ib; i <= Ie; ++i) {
+        const int ig = i - 2, jg = j - 2;
+        const int ms = Mp(ig, jg) + Mp(ig + 1, jg) + Mp(ig, jg + 1) + Mp(ig + 1, jg + 1);
+        const double num = HG(ig, jg) * Mp(ig, jg) + HG(ig + 1, jg) * Mp(ig + 1, jg) +
+                           HG(ig, jg + 1) * Mp(ig, jg + 1) + HG(ig + 1, jg + 1) * Mp(ig + 1, jg + 1);
+        HC(i, j) = num / (double)((float)ms + 1.e-16f);
+      }
+  } else {
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = Ib; i <= Ie; ++i) HC(i, j) = depth[(size_t)(i - 3) + (size_t)M * (j - 3)];
+  }
+  auto coll = [&](std::vector<double>& v) {  // phi_2D_coll
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = 1; i <= 2; ++i) { a2(v, Ml, i, j) = a2(v, Ml, Ib + 2 - i, j); a2(v, Ml, Ie + i, j) = a2(v, Ml, Ie - i + 1, j); }
+    for (int i = 1; i <= Ml; ++i)
+      for (int j = 1; j <= 2; ++j) { a2(v, Ml, i, j) = a2(v, Ml, i, Jb + 2 - j); a2(v, Ml, i, Je + j) = a2(v, Ml, i, Je - j + 1); }
+  };
+  coll(h.Hc);
+  h.Hc0 = h.Hc;
+  if (p.slide_type == NHW_SLIDE_RIGID_3D) {
+    const double e = (double)0.717f;
+    const double alpha0 = p.slide_angle * kPiH / 180.;
+    const double kb = 2.0 * std::acosh(1.0 / e) / p.slide_l;
+    const double kw = 2.0 * std::acosh(1.0 / e) / p.slide_w;
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = Ib; i <= Ie; ++i) {
+        const double xt = (XC(i) - p.slide_x0) * std::cos(alpha0) + (YC(j) - p.slide_y0) * std::sin(alpha0);
+        const double yt = -((XC(i) - p.slide_x0) * std::sin(alpha0)) + (YC(j) - p.slide_y0) * std::cos(alpha0);
+        const double zt = p.slide_t / (1 - e) * (1.0 / std::cosh(kb * xt) / std::cosh(kw * yt) - e);
+        HC(i, j) = a2(h.Hc0, Ml, i, j) - dmx(0.0, zt);
+      }
+  }
+  for (int j = 1; j <= Nl; ++j)
+    for (int i = 1; i <= Ml; ++i) m2(h.Mask_Struct, i, j) = 1;
+  for (int j = Jb; j <= Je; ++j)
+    for (int i = Ib; i <= Ie; ++i)
+      if (HC(i, j) < -1000.0) m2(h.Mask_Struct, i, j) = 0;
+  for (int j = 1; j <= Nl; ++j) {
+    for (int i = 2; i <= Ml; ++i) a2(h.Hfx, Ml1, i, j) = 0.5 * (HC(i - 1, j) + HC(i, j));
+    a2(h.Hfx, Ml1, 1, j) = HC(1, j);
+    a2(h.Hfx, Ml1, Ml1, j) = HC(Ml, j);
+  }
+  h.Hfx0 = h.Hfx;
+  for (int i = 1; i <= Ml; ++i) {
+    for (int j = 2; j <= Nl; ++j) a2(h.Hfy, Ml, i, j) = 0.5 * (HC(i, j - 1) + HC(i, j));
+    a2(h.Hfy, Ml, i, 1) = HC(i, 1);
+    a2(h.Hfy, Ml, i, Nl1) = HC(i, Nl);
+  }
+  h.Hfy0 = h.Hfy;
+  for (int j = 1; j <= Nl; ++j)
+    for (int i = 1; i <= Ml; ++i) {
+      a2(h.DelxH, Ml, i, j) = (a2(h.Hfx, Ml1, i + 1, j) - a2(h.Hfx, Ml1, i, j)) / dx;
+      a2(h.DelyH, Ml, i, j) = (a2(h.Hfy, Ml, i, j + 1) - a2(h.Hfy, Ml, i, j)) / dy;
+    }
+  // ---- initial
+  auto ETA = [&](int i, int j) -> double& { return a2(h.Eta, Ml, i, j); };
+  if (eta0 || uvw0) {
+    const size_t g2 = (size_t)M * N, g3 = g2 * K;
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = Ib; i <= Ie; ++i) {
+        const size_t g = (size_t)(i - 3) + (size_t)M * (j - 3);
+        if (eta0) ETA(i, j) = eta0[g];
+        if (uvw0)
+          for (int k = Kb; k <= Ke; ++k) {
+            const size_t gk = g + g2 * (k - 3);
+            const size_t o = (size_t)(i - 1) + (size_t)Ml * ((j - 1) + (size_t)Nl * (k - 1));
+            h.U[o] = uvw0[gk];
+            h.V[o] = uvw0[gk + g3];
+            h.W[o] = uvw0[gk + 2 * g3];
+          }
+      }
+  }
+  for (int j = 1; j <= Nl; ++j)
+    for (int i = 1; i <= Ml; ++i) {
+      if ((ETA(i, j) + HC(i, j)) <= p.min_dep) { m2(h.Mask, i, j) = 0; ETA(i, j) = p.min_dep - HC(i, j); }
+      else m2(h.Mask, i, j) = 1;
+    }
+  for (int j = 1; j <= Nl; ++j)
+    for (int i = 1; i <= Ml; ++i) m2(h.Mask, i, j) = m2(h.Mask, i, j) * m2(h.Mask_Struct, i, j);
+  coll(h.Eta);
+  for (int j = Jb; j <= Je; ++j)
+    for (int i = Ib; i <= Ie; ++i)
+      m2(h.Mask9, i, j) = m2(h.Mask, i, j) * m2(h.Mask, i - 1, j) * m2(h.Mask, i + 1, j) * m2(h.Mask, i + 1, j + 1) *
+                          m2(h.Mask, i, j + 1) * m2(h.Mask, i - 1, j + 1) * m2(h.Mask, i + 1, j - 1) *
+                          m2(h.Mask, i, j - 1) * m2(h.Mask, i - 1, j - 1);
+  for (int j = 1; j <= Nl; ++j)
+    for (int i = 1; i <= Ml; ++i) a2(h.D, Ml, i, j) = dmx(HC(i, j) + ETA(i, j), p.min_dep);
+  // update_wind, Iws = 1: constant in time
+  {
+    const double Cdsmin = (double)(1.e-3f * (0.61f + 0.063f * 6.0f));
+    const double Cdsmax = (double)(1.e-3f * (0.61f + 0.063f * 50.0f));
+    const double WdU = p.wind_u, WdV = p.wind_v;
+    const double Wds = std::sqrt(WdU * WdU + WdV * WdV);
+    double Cds = (double)1.e-3f * ((double)0.61f + (double)0.063f * Wds);
+    Cds = dmn(dmx(Cds, Cdsmin), Cdsmax);
+    for (int j = Jb; j <= Je; ++j)
+      for (int i = Ib; i <= Ie; ++i) {
+        a2(h.Wsx, Ml, i, j) = (double)0.001293f * Cds * WdU * Wds;
+        a2(h.Wsy, Ml, i, j) = (double)0.001293f * Cds * WdV * Wds;
+      }
+  }
+  // SSP-RK coefficients (default-real divisions)
+  if (p.time_order == 3) {
+    h.it_order = 3;
+    h.alpha[0] = 0.0; h.alpha[1] = (double)(3.0f / 4.0f); h.alpha[2] = (double)(1.0f / 3.0f);
+    h.beta[0] = 1.0; h.beta[1] = (double)(1.0f / 4.0f); h.beta[2] = (double)(2.0f / 3.0f);
+  } else if (p.time_order == 2) {
+    h.it_order = 2;
+    h.alpha[0] = 0.0; h.alpha[1] = (double)(1.0f / 2.0f);
+    h.beta[0] = 1.0; h.beta[1] = (double)(1.0f / 2.0f);
+  } else {
+    h.it_order = 1; h.alpha[0] = 0.0; h.beta[0] = 1.0;
+  }
+  // sponge
+  for (auto& s : h.Sponge) s = 1.0;
+  if (p.sponge_on) {
+    auto SP = [&](int i, int j) -> double& { return a2(h.Sponge, Ml, i, j); };
+    auto f = [&](double t) { return std::sqrt(1.0 - dmn(t * t, 1.0)); };
+    if (p.sponge_west_width > 0.0)
+      for (int j = 1; j <= Nl; ++j)
+        for (int i = 1; i <= Ml; ++i)
+          if (XC(i) <= p.sponge_west_width) SP(i, j) = f((XC(i) - p.sponge_west_width) / p.sponge_west_width);
+    if (p.sponge_east_width > 0.0)
+      for (int j = 1; j <= Nl; ++j)
+        for (int i = 1; i <= Ml; ++i)
+          if (XC(i) >= M * dx - p.sponge_east_width)
+            SP(i, j) = f((XC(i) - (M * dx - p.sponge_east_width)) / p.sponge_east_width);
+    if (p.sponge_south_width > 0.0)
+      for (int j = 1; j <= Nl; ++j)
+        for (int i = 1; i <= Ml; ++i)
+          if (YC(j) <= p.sponge_south_width) SP(i, j) = f((YC(j) - p.sponge_south_width) / p.sponge_south_width);
+    if (p.sponge_north_width > 0.0)
+      for (int j = 1; j <= Nl; ++j)
+        for (int i = 1; i <= Ml; ++i)
+          if (YC(j) >= N * dy - p.sponge_north_width)
+            SP(i, j) = f((YC(j) - (N * dy - p.sponge_north_width)) / p.sponge_north_width);
+  }
+  // wavemaker constants (src/source_terms.F:30-45, 418-424)
+  if (p.wavemaker == NHW_WM_INT_LIN) {
+    h.wm_segma = 2.0 * kPiH / p.per_wave;
+    const double wn = wave_number(h.wm_segma, p.dep_wave);
+    const double wl = 2.0 * kPiH / wn;
+    h.wm_celerity = wl / p.per_wave;
+    h.wm_wnumy = wn * std::sin(p.theta_wave * kPiH / 180.);
+  } else if (p.wavemaker == NHW_WM_INT_SOL) {
+    const double A = p.amp_wave, Dep = p.dep_wave;
+    h.wm_celerity = std::sqrt(kGravH * Dep * (1.0 + A / Dep));
+    h.wm_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
+    h.wm_xstart = 4.0 * Dep / std::sqrt(A / Dep);
+  }
+  return NHW_OK;
+}
+
+}  // namespace nhw

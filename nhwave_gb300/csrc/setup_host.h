@@ -1,0 +1,32 @@
+// setup_host.h -- host-side scenario set-up (the work of generate_grid,
+// read_bathymetry and initial), producing Fortran-layout arrays to upload.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include "../../include/nhwave_gb300.h"
+
+namespace nhw {
+
+struct HostInit {
+  int Mloc = 0, Nloc = 0, Kloc = 0;
+  std::vector<double> x, xc, y, yc, sig, dsig, sigc;                 // 1-D grid
+  std::vector<double> Hc, Hc0, DelxH, DelyH, Eta, D, Sponge, Wsx, Wsy; // (Mloc,Nloc)
+  std::vector<double> Hfx, Hfx0;                                      // (Mloc+1,Nloc)
+  std::vector<double> Hfy, Hfy0;                                      // (Mloc,Nloc+1)
+  std::vector<int32_t> Mask, Mask_Struct, Mask9;                      // (Mloc,Nloc)
+  std::vector<double> U, V, W;                                        // (Mloc,Nloc,Kloc)
+  double alpha[3] = {0, 0, 0}, beta[3] = {0, 0, 0};
+  int it_order = 1;
+  // host-computed wavemaker constants
+  double wm_segma = 0, wm_celerity = 0, wm_wnumy = 0, wm_atmp = 0, wm_xstart = 0;
+};
+
+// Validate parameters against the path's scope; NHW_OK or an error code.
+int check_params(const nhw_params& p);
+// Build the initial state.  depth/eta0/uvw0 follow nhw_setup's contract.
+int host_setup(const nhw_params& p, const double* depth, const double* eta0, const double* uvw0,
+               HostInit& out);
+// Wave number of linear dispersion by Newton iteration (src/waves.F:61-91).
+double wave_number(double segma, double dep);
+
+}  // namespace nhw

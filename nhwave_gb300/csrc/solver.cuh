@@ -1,0 +1,554 @@
+// solver.cuh -- host orchestration of one scenario on one CUDA stream:
+// device arena, the reference's subroutine sequence as kernel launches, the
+// Poisson solve with FP64 iterative refinement, and field transfer.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "krylov.cuh"
+#include "setup_host.h"
+
+namespace nhw {
+
+void set_last_error(const std::string& s);
+
+#define NHW_CU(x)                                                                   \
+  do {                                                                              \
+    cudaError_t e_ = (x);                                                           \
+    if (e_ != cudaSuccess) {                                                        \
+      set_last_error(std::string(#x) + ": " + cudaGetErrorString(e_));              \
+      return NHW_ERR_CUDA;                                                          \
+    }                                                                               \
+  } while (0)
+
+inline unsigned cdiv(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+class SolverBase {
+ public:
+  virtual ~SolverBase() {}
+  virtual int setup(const double* depth, const double* eta0, const double* uvw0) = 0;
+  virtual int get_field(int f, void* host) = 0;
+  virtual int set_field(int f, const void* host) = 0;
+  virtual int field_shape(int f, int dims[3], int* eb) const = 0;
+  virtual int get_scalars(nhw_scalars* out) = 0;
+  virtual int set_time(double t, double dt, int rs) = 0;
+  virtual int estimate_dt() = 0;
+  virtual int update_bathymetry() = 0;
+  virtual int update_mask() = 0;
+  virtual int update_vars() = 0;
+  virtual int source_terms() = 0;
+  virtual int fluxes() = 0;
+  virtual int eval_duvw(int istep) = 0;
+  virtual int sponge_damping() = 0;
+  virtual int step() = 0;
+  virtual int mass(double* m) = 0;
+  virtual int sync() = 0;
+  virtual bool is_setup() const = 0;
+  virtual double total_time() const = 0;
+  virtual int sim_steps() const = 0;
+};
+
+template <class T>
+__global__ void k_pack(const void* src, int kind, double* dd, int* di, int nx, int ny, int nz, int sy,
+                       long long sz) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nx * ny * nz) return;
+  const int i = (int)(t % nx);
+  const long long r = t / nx;
+  const int j = (int)(r % ny), k = (int)(r / ny);
+  const long long s = i + (long long)sy * j + sz * k;
+  if (kind == 0) dd[t] = (double)((const T*)src)[s];
+  else if (kind == 1) dd[t] = ((const double*)src)[s];
+  else di[t] = ((const int*)src)[s];
+}
+template <class T>
+__global__ void k_unpack(void* dst, int kind, const double* sd, const int* si, int nx, int ny, int nz, int sy,
+                         long long sz) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nx * ny * nz) return;
+  const int i = (int)(t % nx);
+  const long long r = t / nx;
+  const int j = (int)(r % ny), k = (int)(r / ny);
+  const long long s = i + (long long)sy * j + sz * k;
+  if (kind == 0) ((T*)dst)[s] = (T)sd[t];
+  else if (kind == 1) ((double*)dst)[s] = sd[t];
+  else ((int*)dst)[s] = si[t];
+}
+template <class T>
+__global__ void k_single(Dev<T> S, int what) {
+  if (what == 0) OpSourceArea{}(S, 0, 0);
+}
+
+template <class T>
+class Solver final : public SolverBase {
+ public:
+  nhw_params p{};
+  Dev<T> S{};
+  cudaStream_t st = nullptr;
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  DevScal* h_sc = nullptr;     // pinned mirror of S.sc
+  double* d_out = nullptr;     // small device output
+  double* h_out = nullptr;
+  double* d_stage = nullptr;   // field staging (double / int32)
+  size_t stage_elems = 0;
+  size_t n2 = 0, n3 = 0;
+  bool ready = false;
+  int last_inner = 0, last_refine = 0;
+  int64_t solves = 0;
+  int it_order = 3;
+  static constexpr bool kFP32 = sizeof(T) == 4;
+
+  ~Solver() override {
+    if (st) cudaStreamSynchronize(st);
+    if (arena) cudaFree(arena);
+    if (h_sc) cudaFreeHost(h_sc);
+    if (h_out) cudaFreeHost(h_out);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  int create(const nhw_params& q) {
+    p = q;
+    int rc = check_params(p);
+    if (rc) return rc;
+    const int M = p.Mglob, N = p.Nglob, K = p.Kglob;
+    S.M = M; S.N = N; S.K = K;
+    S.Mloc = M + 2 * NG; S.Nloc = N + 2 * NG; S.Kloc = K + 2 * NG;
+    S.sy = S.Mloc + 1;
+    S.sz = (long long)S.sy * (S.Nloc + 1);
+    S.IB = NG; S.IE = M + NG - 1; S.JB = NG; S.JE = N + NG - 1; S.KB = NG; S.KE = K + NG - 1;
+    S.neq = M * N * K;
+    S.dx = p.dx; S.dy = p.dy; S.min_dep = p.min_dep; S.cfl = p.cfl;
+    S.dt_min = p.dt_min; S.dt_max = p.dt_max;
+    S.fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);
+    S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
+    S.non_hydro = p.non_hydro; S.sponge_on = p.sponge_on;
+    S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
+    S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
+    S.wavemaker = p.wavemaker;
+    S.wm_amp = p.amp_wave; S.wm_xw = p.xsource_west; S.wm_xe = p.xsource_east;
+    S.wm_ys = p.ysource_suth; S.wm_yn = p.ysource_nrth;
+    S.cur_wave = p.cur_wave; S.tramp = p.tramp;
+    S.slide = p.slide_type == NHW_SLIDE_RIGID_3D;
+    if (S.slide) {
+      S.sl_e = (double)0.717f;
+      const double alpha0 = p.slide_angle * kPi / 180.;
+      const double slope0 = p.slope_angle * kPi / 180.;
+      S.sl_kb = 2.0 * std::acosh(1.0 / S.sl_e) / p.slide_l;
+      S.sl_kw = 2.0 * std::acosh(1.0 / S.sl_e) / p.slide_w;
+      S.sl_cosa = std::cos(alpha0); S.sl_sina = std::sin(alpha0);
+      S.sl_cosslope = std::cos(slope0);
+      S.sl_t0 = p.slide_ut / p.slide_a0;
+      S.sl_s0 = p.slide_ut * p.slide_ut / p.slide_a0;
+      S.sl_T = p.slide_t; S.sl_x0 = p.slide_x0; S.sl_y0 = p.slide_y0;
+    }
+    n2 = (size_t)S.sy * (S.Nloc + 1);
+    n3 = (size_t)S.sz * (S.Kloc + 1);
+    const size_t neq = (size_t)S.neq;
+    // ---- arena layout
+    std::vector<std::pair<void**, size_t>> plan;
+    auto add = [&](auto** ptr, size_t bytes) { plan.push_back({(void**)ptr, bytes}); };
+    add(&S.sig, sizeof(double) * (S.Kloc + 1));
+    add(&S.dsig, sizeof(double) * S.Kloc);
+    add(&S.sigc, sizeof(double) * S.Kloc);
+    add(&S.xc, sizeof(double) * S.Mloc);
+    add(&S.yc, sizeof(double) * S.Nloc);
+    double** d2[] = {&S.D, &S.D0, &S.Eta, &S.Eta0, &S.Hc, &S.Hc0, &S.Ho, &S.Hfx, &S.Hfy, &S.Hfx0, &S.Hfy0,
+                     &S.DelxH, &S.DelyH, &S.DeltH, &S.DeltHo, &S.Delt2H, &S.DelxEta, &S.DelyEta, &S.SourceX,
+                     &S.SourceY, &S.SourceC, &S.Sponge, &S.R1, &S.Wsx, &S.Wsy, &S.EtaxL, &S.EtaxR, &S.EtayL,
+                     &S.EtayR, &S.zUL, &S.zVL, &S.zWL, &S.zUR, &S.zVR, &S.zWR};
+    for (auto pp : d2) add(pp, sizeof(double) * n2);
+    int** i2p[] = {&S.Mask, &S.MaskT, &S.Mask_Struct, &S.Mask9};
+    for (auto pp : i2p) add(pp, sizeof(int) * n2);
+    T** t3[] = {&S.U, &S.V, &S.W, &S.DU, &S.DV, &S.DW, &S.DU0, &S.DV0, &S.DW0, &S.Omega,
+                &S.Ex, &S.Fx, &S.Gx, &S.Hx, &S.Ey, &S.Fy, &S.Gy, &S.Hy, &S.Fz, &S.Gz, &S.Hz};
+    for (auto pp : t3) add(pp, sizeof(T) * n3);
+    add(&S.P, sizeof(double) * n3);
+    add(&S.coef64, sizeof(double) * NCOEF * neq);
+    add(&S.rhs64, sizeof(double) * neq);
+    add(&S.xsol64, sizeof(double) * neq);
+    add(&S.res64, sizeof(double) * neq);
+    if (kFP32) add(&S.coefT, sizeof(T) * NCOEF * neq);
+    T** tk[] = {&S.lcp, &S.linv, &S.kx, &S.kr, &S.kr0, &S.kp, &S.kph, &S.kv, &S.ks, &S.ksh, &S.kt};
+    for (auto pp : tk) add(pp, sizeof(T) * neq);
+    add(&S.partials, sizeof(double) * 8 * kRedBlocks);
+    add(&S.sc, sizeof(DevScal));
+    add(&d_out, sizeof(double) * 8);
+    stage_elems = std::max(n3, (size_t)(S.Mloc + 1) * (S.Nloc + 1) * (S.Kloc + 1));
+    add(&d_stage, sizeof(double) * stage_elems);
+    size_t total = 0;
+    for (auto& e : plan) total += (e.second + 255) & ~size_t(255);
+    NHW_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaError_t e = cudaMalloc((void**)&arena, total);
+    if (e != cudaSuccess) {
+      set_last_error(std::string("cudaMalloc arena: ") + cudaGetErrorString(e));
+      arena = nullptr;
+      return NHW_ERR_NOMEM;
+    }
+    arena_bytes = total;
+    NHW_CU(cudaMemsetAsync(arena, 0, total, st));
+    size_t off = 0;
+    for (auto& e2 : plan) { *e2.first = arena + off; off += (e2.second + 255) & ~size_t(255); }
+    if (!kFP32) S.coefT = (T*)S.coef64;
+    NHW_CU(cudaMallocHost((void**)&h_sc, sizeof(DevScal)));
+    NHW_CU(cudaMallocHost((void**)&h_out, sizeof(double) * 8));
+    std::memset(h_sc, 0, sizeof(DevScal));
+    h_sc->dt = p.dt_ini;
+    h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
+    NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
+  static long long dbits(double x) { long long b; std::memcpy(&b, &x, 8); return b; }
+
+  // ---------------------------------------------------------------- launchers
+  template <class Op> void allcols(Op op) {
+    k_allcols<T, Op><<<cdiv((long long)S.Mloc * S.Nloc, 256), 256, 0, st>>>(S, op);
+  }
+  template <class Op> void incols(Op op) {
+    k_incols<T, Op><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S, op);
+  }
+  template <class Op> void box(Op op, int nx, int ny, int nz, int ox, int oy, int oz) {
+    k_box<T, Op><<<cdiv((long long)nx * ny * nz, 256), 256, 0, st>>>(S, op, nx, ny, nz, ox, oy, oz);
+  }
+  template <class Op> void cells(Op op) { box(op, S.M, S.N, S.K, S.IB, S.JB, S.KB); }
+  unsigned red_blocks() const { return std::min<unsigned>(cdiv(S.neq, 256), kRedBlocks); }
+
+  int check() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_last_error(std::string("kernel launch: ") + cudaGetErrorString(e)); return NHW_ERR_CUDA; }
+    return NHW_OK;
+  }
+  int pull_scalars() {
+    NHW_CU(cudaMemcpyAsync(h_sc, S.sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
+  int sync() override {
+    NHW_CU(cudaStreamSynchronize(st));
+    return check();
+  }
+  bool is_setup() const override { return ready; }
+  double total_time() const override { return p.total_time; }
+  int sim_steps() const override { return p.sim_steps; }
+
+  // -------------------------------------------------------------- fields
+  struct FieldDesc { void* ptr; int kind; int nx, ny, nz; };  // kind 0 = T, 1 = double, 2 = int
+  FieldDesc desc(int f) const {
+    const int Ml = S.Mloc, Nl = S.Nloc, Kl = S.Kloc;
+    switch (f) {
+      case NHW_F_D: return {S.D, 1, Ml, Nl, 1};
+      case NHW_F_D0: return {S.D0, 1, Ml, Nl, 1};
+      case NHW_F_ETA: return {S.Eta, 1, Ml, Nl, 1};
+      case NHW_F_ETA0: return {S.Eta0, 1, Ml, Nl, 1};
+      case NHW_F_HC: return {S.Hc, 1, Ml, Nl, 1};
+      case NHW_F_HC0: return {S.Hc0, 1, Ml, Nl, 1};
+      case NHW_F_DELXH: return {S.DelxH, 1, Ml, Nl, 1};
+      case NHW_F_DELYH: return {S.DelyH, 1, Ml, Nl, 1};
+      case NHW_F_DELXETA: return {S.DelxEta, 1, Ml, Nl, 1};
+      case NHW_F_DELYETA: return {S.DelyEta, 1, Ml, Nl, 1};
+      case NHW_F_DELTH: return {S.DeltH, 1, Ml, Nl, 1};
+      case NHW_F_DELT2H: return {S.Delt2H, 1, Ml, Nl, 1};
+      case NHW_F_SOURCEX: return {S.SourceX, 1, Ml, Nl, 1};
+      case NHW_F_SOURCEY: return {S.SourceY, 1, Ml, Nl, 1};
+      case NHW_F_SOURCEC: return {S.SourceC, 1, Ml, Nl, 1};
+      case NHW_F_SPONGE: return {S.Sponge, 1, Ml, Nl, 1};
+      case NHW_F_R1: return {S.R1, 1, Ml, Nl, 1};
+      case NHW_F_HFX: return {S.Hfx, 1, Ml + 1, Nl, 1};
+      case NHW_F_HFX0: return {S.Hfx0, 1, Ml + 1, Nl, 1};
+      case NHW_F_ETAXL: return {S.EtaxL, 1, Ml + 1, Nl, 1};
+      case NHW_F_ETAXR: return {S.EtaxR, 1, Ml + 1, Nl, 1};
+      case NHW_F_HFY: return {S.Hfy, 1, Ml, Nl + 1, 1};
+      case NHW_F_HFY0: return {S.Hfy0, 1, Ml, Nl + 1, 1};
+      case NHW_F_ETAYL: return {S.EtayL, 1, Ml, Nl + 1, 1};
+      case NHW_F_ETAYR: return {S.EtayR, 1, Ml, Nl + 1, 1};
+      case NHW_F_MASK: return {S.Mask, 2, Ml, Nl, 1};
+      case NHW_F_MASK_STRUCT: return {S.Mask_Struct, 2, Ml, Nl, 1};
+      case NHW_F_MASK9: return {S.Mask9, 2, Ml, Nl, 1};
+      case NHW_F_U: return {S.U, 0, Ml, Nl, Kl};
+      case NHW_F_V: return {S.V, 0, Ml, Nl, Kl};
+      case NHW_F_W: return {S.W, 0, Ml, Nl, Kl};
+      case NHW_F_DU: return {S.DU, 0, Ml, Nl, Kl};
+      case NHW_F_DV: return {S.DV, 0, Ml, Nl, Kl};
+      case NHW_F_DW: return {S.DW, 0, Ml, Nl, Kl};
+      case NHW_F_DU0: return {S.DU0, 0, Ml, Nl, Kl};
+      case NHW_F_DV0: return {S.DV0, 0, Ml, Nl, Kl};
+      case NHW_F_DW0: return {S.DW0, 0, Ml, Nl, Kl};
+      case NHW_F_P: return {S.P, 1, Ml, Nl, Kl};
+      case NHW_F_OMEGA: return {S.Omega, 0, Ml, Nl, Kl + 1};
+      case NHW_F_EX: return {S.Ex, 0, Ml + 1, Nl, Kl};
+      case NHW_F_FX: return {S.Fx, 0, Ml + 1, Nl, Kl};
+      case NHW_F_GX: return {S.Gx, 0, Ml + 1, Nl, Kl};
+      case NHW_F_HX: return {S.Hx, 0, Ml + 1, Nl, Kl};
+      case NHW_F_EY: return {S.Ey, 0, Ml, Nl + 1, Kl};
+      case NHW_F_FY: return {S.Fy, 0, Ml, Nl + 1, Kl};
+      case NHW_F_GY: return {S.Gy, 0, Ml, Nl + 1, Kl};
+      case NHW_F_HY: return {S.Hy, 0, Ml, Nl + 1, Kl};
+      case NHW_F_FZ: return {S.Fz, 0, Ml, Nl, Kl + 1};
+      case NHW_F_GZ: return {S.Gz, 0, Ml, Nl, Kl + 1};
+      case NHW_F_HZ: return {S.Hz, 0, Ml, Nl, Kl + 1};
+      default: return {nullptr, -1, 0, 0, 0};
+    }
+  }
+  int field_shape(int f, int dims[3], int* eb) const override {
+    FieldDesc d = desc(f);
+    if (!d.ptr) return NHW_ERR_ARG;
+    dims[0] = d.nx; dims[1] = d.ny; dims[2] = d.nz;
+    *eb = d.kind == 2 ? 4 : 8;
+    return NHW_OK;
+  }
+  int get_field(int f, void* host) override {
+    FieldDesc d = desc(f);
+    if (!d.ptr || !host) return NHW_ERR_ARG;
+    const long long n = (long long)d.nx * d.ny * d.nz;
+    k_pack<T><<<cdiv(n, 256), 256, 0, st>>>(d.ptr, d.kind, d_stage, (int*)d_stage, d.nx, d.ny, d.nz, S.sy, S.sz);
+    NHW_CU(cudaGetLastError());
+    NHW_CU(cudaMemcpyAsync(host, d_stage, n * (d.kind == 2 ? 4 : 8), cudaMemcpyDeviceToHost, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
+  int set_field(int f, const void* host) override {
+    FieldDesc d = desc(f);
+    if (!d.ptr || !host) return NHW_ERR_ARG;
+    const long long n = (long long)d.nx * d.ny * d.nz;
+    NHW_CU(cudaMemcpyAsync(d_stage, host, n * (d.kind == 2 ? 4 : 8), cudaMemcpyHostToDevice, st));
+    k_unpack<T><<<cdiv(n, 256), 256, 0, st>>>(d.ptr, d.kind, d_stage, (const int*)d_stage, d.nx, d.ny, d.nz, S.sy, S.sz);
+    NHW_CU(cudaGetLastError());
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
+
+  // ----------------------------------------------------------------- setup
+  int setup(const double* depth, const double* eta0, const double* uvw0) override {
+    HostInit h;
+    int rc = host_setup(p, depth, eta0, uvw0, h);
+    if (rc) return rc;
+    it_order = h.it_order;
+    for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
+    S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
+    S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
+    NHW_CU(cudaMemcpyAsync((void*)S.sig, h.sig.data(), sizeof(double) * h.sig.size(), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaMemcpyAsync((void*)S.dsig, h.dsig.data(), sizeof(double) * h.dsig.size(), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaMemcpyAsync((void*)S.sigc, h.sigc.data(), sizeof(double) * h.sigc.size(), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaMemcpyAsync((void*)S.xc, h.xc.data(), sizeof(double) * h.xc.size(), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaMemcpyAsync((void*)S.yc, h.yc.data(), sizeof(double) * h.yc.size(), cudaMemcpyHostToDevice, st));
+    struct Up { int f; const void* src; } ups[] = {
+        {NHW_F_HC, h.Hc.data()}, {NHW_F_HC0, h.Hc0.data()}, {NHW_F_DELXH, h.DelxH.data()},
+        {NHW_F_DELYH, h.DelyH.data()}, {NHW_F_ETA, h.Eta.data()}, {NHW_F_ETA0, h.Eta.data()},
+        {NHW_F_D, h.D.data()}, {NHW_F_SPONGE, h.Sponge.data()}, {NHW_F_HFX, h.Hfx.data()},
+        {NHW_F_HFX0, h.Hfx.data()}, {NHW_F_HFY, h.Hfy.data()}, {NHW_F_HFY0, h.Hfy.data()},
+        {NHW_F_MASK, h.Mask.data()}, {NHW_F_MASK_STRUCT, h.Mask_Struct.data()},
+        {NHW_F_MASK9, h.Mask9.data()}, {NHW_F_U, h.U.data()}, {NHW_F_V, h.V.data()}, {NHW_F_W, h.W.data()}};
+    for (auto& u : ups) {
+      rc = set_field(u.f, u.src);
+      if (rc) return rc;
+    }
+    {  // Wsx / Wsy are not public fields
+      FieldDesc dx_{S.Wsx, 1, S.Mloc, S.Nloc, 1}, dy_{S.Wsy, 1, S.Mloc, S.Nloc, 1};
+      for (auto pr : {std::make_pair(dx_, h.Wsx.data()), std::make_pair(dy_, h.Wsy.data())}) {
+        const long long n = (long long)S.Mloc * S.Nloc;
+        NHW_CU(cudaMemcpyAsync(d_stage, pr.second, n * 8, cudaMemcpyHostToDevice, st));
+        k_unpack<T><<<cdiv(n, 256), 256, 0, st>>>(pr.first.ptr, 1, d_stage, nullptr, S.Mloc, S.Nloc, 1, S.sy, S.sz);
+        NHW_CU(cudaStreamSynchronize(st));
+      }
+    }
+    std::memset(h_sc, 0, sizeof(DevScal));
+    h_sc->time = 0.0; h_sc->dt = p.dt_ini; h_sc->run_step = 0;
+    h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
+    NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
+    // initial: vel_bc on the initial velocities, then DU = D*U*Mask
+    allcols(OpVelBcA{});
+    incols(OpVelBcB{});
+    k_allcells<T, OpInitDU><<<cdiv((long long)S.Mloc * S.Nloc * S.Kloc, 256), 256, 0, st>>>(S, OpInitDU{});
+    rc = sync();
+    if (rc) return rc;
+    ready = true;
+    return NHW_OK;
+  }
+
+  int get_scalars(nhw_scalars* o) override {
+    int rc = pull_scalars();
+    if (rc) return rc;
+    std::memset(o, 0, sizeof(*o));
+    o->time = h_sc->time; o->dt = h_sc->dt; o->dt_old = h_sc->dt_old; o->run_step = h_sc->run_step;
+    o->last_krylov_iters = last_inner; o->total_krylov_iters = h_sc->total_it;
+    o->poisson_solves = solves; o->last_rel_residual = h_sc->relres64;
+    o->last_refinements = last_refine; o->status = h_sc->status;
+    return NHW_OK;
+  }
+  int set_time(double t, double dt, int rs) override {
+    int rc = pull_scalars();
+    if (rc) return rc;
+    h_sc->time = t; h_sc->dt = dt; h_sc->run_step = rs;
+    NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
+    return sync();
+  }
+
+  // -------------------------------------------------- reference subroutines
+  int estimate_dt() override {
+    k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S);
+    k_dt_finalize<T><<<1, 1, 0, st>>>(S);
+    int rc = pull_scalars();
+    if (rc) return rc;
+    if (h_sc->status == NHW_ERR_DT_MIN) return NHW_ERR_DT_MIN;
+    return check();
+  }
+  int update_bathymetry() override {
+    if (!S.slide) return NHW_OK;
+    allcols(OpSlideA{});
+    allcols(OpSlideB{});
+    box(OpSlideC{}, S.Mloc + 1, S.Nloc + 1, 1, 0, 0, 0);
+    return check();
+  }
+  int update_mask() override {
+    allcols(OpMaskA{});
+    allcols(OpMaskB{});
+    return check();
+  }
+  int update_vars() override {
+    NHW_CU(cudaMemcpyAsync(S.D0, S.D, sizeof(double) * n2, cudaMemcpyDeviceToDevice, st));
+    NHW_CU(cudaMemcpyAsync(S.Eta0, S.Eta, sizeof(double) * n2, cudaMemcpyDeviceToDevice, st));
+    NHW_CU(cudaMemcpyAsync(S.DU0, S.DU, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
+    NHW_CU(cudaMemcpyAsync(S.DV0, S.DV, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
+    NHW_CU(cudaMemcpyAsync(S.DW0, S.DW, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
+    return NHW_OK;
+  }
+  int source_terms() override {
+    if (S.wavemaker) k_single<T><<<1, 1, 0, st>>>(S, 0);
+    incols(OpSource{});
+    return check();
+  }
+  int fluxes() override {
+    allcols(OpSlopeEta{});
+    box(OpFluxX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
+    box(OpFluxY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
+    box(OpFluxZ{}, S.M, S.N, S.K + 1, S.IB, S.JB, S.KB);
+    return check();
+  }
+  void get_uvw() {
+    cells(OpGetUVW{});
+    allcols(OpVelBcA{});
+    incols(OpVelBcB{});
+  }
+  int poisson() {
+    cells(OpPoissonCoef{});
+    if (kFP32) cells(OpCoefToT{});
+    incols(OpLineFactor{});
+    cells(OpXFromP{});
+    const int max_ir = kFP32 ? 12 : 4;
+    int inner_total = 0, ir = 0, status = NHW_OK;
+    for (ir = 0; ir <= max_ir; ++ir) {
+      k_res64<T><<<red_blocks(), 256, 0, st>>>(S);
+      int rc = pull_scalars();
+      if (rc) return rc;
+      const double rel = h_sc->relres64;
+      if (!(rel == rel)) { status = NHW_ERR_NAN; break; }
+      if (h_sc->bnorm == 0.0) {  // HYPRE returns x = 0 for b = 0
+        NHW_CU(cudaMemsetAsync(S.xsol64, 0, sizeof(double) * S.neq, st));
+        break;
+      }
+      if (rel <= p.tol) break;
+      if (ir == max_ir || inner_total >= p.itmax) { status = NHW_ERR_KRYLOV_NOCONV; break; }
+      double tol_in = 0.5 * p.tol / rel;
+      if (kFP32 && tol_in < 2e-5) tol_in = 2e-5;
+      const int itmax_in = p.itmax - inner_total;
+      k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S);
+      int chunk = 4;
+      while (true) {
+        for (int c = 0; c < chunk; ++c) {
+          const unsigned cb = cdiv((long long)S.M * S.N, 256);
+          k_bicg_p<T><<<cb, 256, 0, st>>>(S);
+          k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S);
+          k_bicg_s<T><<<cb, 256, 0, st>>>(S);
+          k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S);
+          k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in);
+        }
+        rc = pull_scalars();
+        if (rc) return rc;
+        if (h_sc->conv != 0) break;
+        if (chunk < 16) chunk *= 2;
+      }
+      inner_total += h_sc->it;
+      k_xupd<T><<<red_blocks(), 256, 0, st>>>(S);
+      if (h_sc->conv == 5) { status = NHW_ERR_NAN; break; }
+    }
+    last_inner = inner_total;
+    last_refine = ir;
+    ++solves;
+    cells(OpPFromX{});
+    allcols(OpPGhost{});
+    int rc = check();
+    return rc ? rc : status;
+  }
+  int eval_duvw(int istep) override {
+    if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
+    const int s = istep - 1;
+    incols(OpExplicit{s});
+    allcols(OpWlBcEta{});
+    allcols(OpSlopeEta{});
+    int status = NHW_OK;
+    if (S.non_hydro) {
+      get_uvw();
+      status = poisson();
+      if (status == NHW_ERR_CUDA) return status;
+      cells(OpProjection{});
+    }
+    cells(OpSSP{s});
+    get_uvw();
+    box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
+    box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
+    incols(OpOmegaScan{});
+    int rc = check();
+    return rc ? rc : status;
+  }
+  int sponge_damping() override {
+    allcols(OpSponge{});
+    return check();
+  }
+  int step() override {
+    if (!ready) return NHW_ERR_STATE;
+    int rc = estimate_dt();
+    if (rc) return rc;
+    if (S.slide) update_bathymetry();
+    update_mask();
+    rc = update_vars();
+    if (rc) return rc;
+    int worst = NHW_OK;
+    for (int s = 1; s <= it_order; ++s) {
+      source_terms();
+      fluxes();
+      rc = eval_duvw(s);
+      if (rc == NHW_ERR_CUDA) return rc;
+      if (rc != NHW_OK && worst == NHW_OK) worst = rc;
+      if (S.sponge_on) sponge_damping();
+    }
+    rc = check();
+    return rc ? rc : worst;
+  }
+  int mass(double* m) override {
+    k_mass<T><<<1, 1, 0, st>>>(S, d_out);
+    NHW_CU(cudaMemcpyAsync(h_out, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    *m = h_out[0];
+    return check();
+  }
+};
+
+SolverBase* make_solver_fp64(const nhw_params& p, int* status);
+SolverBase* make_solver_fp32(const nhw_params& p, int* status);
+
+template <class T>
+SolverBase* make_solver_t(const nhw_params& p, int* status) {
+  auto* s = new Solver<T>();
+  int rc = s->create(p);
+  if (status) *status = rc;
+  if (rc) { delete s; return nullptr; }
+  return s;
+}
+
+}  // namespace nhw

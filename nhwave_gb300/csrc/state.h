@@ -1,0 +1,113 @@
+// state.h -- device-side state of one NHWAVE scenario.
+//
+// Layout in HBM: every array of a scenario uses the same padded, ghosted,
+// i-fastest layout, 0-based:
+//     2-D  (i, j)     -> i + sy*j                 i in [0, Mloc], j in [0, Nloc]
+//     3-D  (i, j, k)  -> i + sy*j + sz*k          k in [0, Kloc]
+// with sy = Mloc+1 and sz = sy*(Nloc+1), so cell, x-face, y-face and z-face
+// arrays (the reference's (Mloc,Nloc,Kloc), (Mloc1,Nloc,Kloc), (Mloc,Nloc1,Kloc)
+// and (Mloc,Nloc,Kloc1) allocations, src/initialize.F:1423-1643) share one index
+// formula; Fortran (i,j,k) is (i-1, j-1, k-1) here.  Interior cells are
+// i in [IB, IE] = [2, M+1] (likewise j, k); face f lies between cells f-1 and f.
+//
+// 2-D fields (depth, elevation, masks, bathymetry derivatives) are always FP64;
+// 3-D fields use the scenario's storage type T (double for the plain FP64
+// form, float for the FP32+IR form).  Poisson vectors use a compact interior
+// ordering  ic = (i-IB) + M*((j-JB) + N*(k-KB)).
+#pragma once
+#include <cstdint>
+#include <cstddef>
+
+namespace nhw {
+
+constexpr int NG = 2;          // Nghost (src/mod_global.F:35)
+constexpr int KMAX = 64;       // largest Kglob a column kernel holds in registers/local memory
+constexpr int NCOEF = 15;      // Poisson stencil entries (src/pressure.F:276-278)
+
+// Constants of module GLOBAL (src/mod_global.F:21-30): default-real literals,
+// i.e. rounded to single precision then widened.
+constexpr double kPi = (double)3.141592653f;
+constexpr double kSmall = (double)1.0e-16f;
+constexpr double kLarge = 10000000.0;
+constexpr double kGrav = (double)9.81f;
+constexpr double kRho0 = 1000.0;
+
+// Per-scenario scalars that live on the device (written by kernels).
+struct DevScal {
+  double time, dt, dt_old;
+  int32_t run_step, status;
+  unsigned long long dtmin_bits;   // estimate_dt minimum (bit pattern of a positive double)
+  double source_area;
+  // Krylov state
+  double rho, alpha, omega, beta;
+  double red[8];                    // reduction results
+  double bnorm, relres, relres64;
+  int32_t it, conv, ir, pad0;
+  unsigned int counter[4];          // last-block-done counters
+  int64_t total_it, solves;
+};
+
+template <class T>
+struct Dev {
+  // dimensions (interior M x N x K; ghosted Mloc x Nloc x Kloc)
+  int M, N, K, Mloc, Nloc, Kloc;
+  int sy;            // j stride
+  long long sz;      // k stride
+  int IB, IE, JB, JE, KB, KE;   // interior bounds (inclusive), 0-based
+  int neq;           // M*N*K
+  // parameters
+  double dx, dy, min_dep, cfl, dt_min, dt_max, fcor, froude_cap;
+  int froude_on, non_hydro, sponge_on, it_order;
+  int bc_x0, bc_xn, bc_y0, bc_yn;
+  double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt)
+  double alpha[3], beta[3];        // SSP-RK coefficients
+  // wavemaker (INT_LIN / INT_SOL): host-computed constants
+  int wavemaker;
+  double wm_segma, wm_celerity, wm_amp, wm_wnumy, wm_xw, wm_xe, wm_ys, wm_yn;
+  double wm_atmp, wm_xstart;
+  // sponge current
+  double cur_wave, tramp;
+  // rigid slide (RIGID_3D)
+  int slide;
+  double sl_e, sl_kb, sl_kw, sl_cosa, sl_sina, sl_cosslope, sl_s0, sl_t0, sl_T, sl_x0, sl_y0;
+  // 1-D grid
+  const double *sig, *dsig, *sigc, *xc, *yc;
+  // 2-D FP64 fields
+  double *D, *D0, *Eta, *Eta0, *Hc, *Hc0, *Ho;
+  double *Hfx, *Hfy, *Hfx0, *Hfy0, *DelxH, *DelyH, *DeltH, *DeltHo, *Delt2H;
+  double *DelxEta, *DelyEta, *SourceX, *SourceY, *SourceC, *Sponge, *R1, *Wsx, *Wsy;
+  double *EtaxL, *EtaxR, *EtayL, *EtayR;
+  double *zUL, *zVL, *zWL, *zUR, *zVR, *zWR;   // vel_bc face states at the surface / bed
+  int *Mask, *MaskT, *Mask_Struct, *Mask9;
+  // 3-D fields (storage type T); P is FP64 in both forms
+  T *U, *V, *W, *DU, *DV, *DW, *DU0, *DV0, *DW0, *Omega;
+  T *Ex, *Fx, *Gx, *Hx, *Ey, *Fy, *Gy, *Hy, *Fz, *Gz, *Hz;
+  double* P;
+  // Poisson: FP64 operator (15 diagonals, compact interior order) + rhs
+  double* coef64;     // [NCOEF][neq]
+  double* rhs64;      // [neq]
+  double* xsol64;     // [neq]  FP64 solution (= P interior)
+  double* res64;      // [neq]  FP64 residual for refinement
+  // Krylov working vectors in the inner precision T (compact interior order)
+  T* coefT;           // [NCOEF][neq] (aliases coef64 when T == double)
+  T *lcp, *linv;      // line preconditioner factors [neq]
+  T *kx, *kr, *kr0, *kp, *kph, *kv, *ks, *ksh, *kt;
+  double* partials;   // reduction partials [nblocks * 8]
+  DevScal* sc;
+};
+
+// -------------------------------------------------------------- indexing
+template <class T>
+__host__ __device__ __forceinline__ long long i2(const Dev<T>& S, int i, int j) {
+  return (long long)i + (long long)S.sy * j;
+}
+template <class T>
+__host__ __device__ __forceinline__ long long i3(const Dev<T>& S, int i, int j, int k) {
+  return (long long)i + (long long)S.sy * j + S.sz * k;
+}
+template <class T>
+__host__ __device__ __forceinline__ int ic_of(const Dev<T>& S, int i, int j, int k) {
+  return (i - S.IB) + S.M * ((j - S.JB) + S.N * (k - S.KB));
+}
+
+}  // namespace nhw

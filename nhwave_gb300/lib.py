@@ -1,0 +1,205 @@
+"""ctypes binding of ``libnhw_gpu.so`` -- the C-ABI of include/nhwave_gb300.h.
+
+``Scenario`` mirrors the reference's subroutine interface for the time-step
+path: one method per replaced subroutine (``estimate_dt``, ``update_mask``,
+``update_vars``, ``source_terms``, ``fluxes``, ``eval_duvw(istep)``,
+``sponge_damping``; src/nhwave.F:119-258), plus ``step``/``run`` for the whole
+loop body and field access in the reference's ghosted Fortran layout.  There is
+no CPU fallback: without the built library every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import warnings
+
+import numpy as np
+
+from . import fields as F
+from .params import NhwParams, NhwScalars
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnhw_gpu.so")
+
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_DT_MIN, ERR_KRYLOV_NOCONV, ERR_NAN, \
+    ERR_TIMEOUT, ERR_STATE, ERR_CAPACITY, ERR_NOT_FOUND = range(12)
+
+# every entry point declared in include/nhwave_gb300.h
+EXPORTS = [
+    "nhw_create", "nhw_destroy", "nhw_setup", "nhw_get_field", "nhw_set_field", "nhw_field_shape",
+    "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_mask",
+    "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
+    "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_abi_sizes", "nhw_status_string",
+    "nhw_last_error",
+]
+
+
+class NhwError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        msg = f"{where}: {status_string(status)}"
+        if status == ERR_CUDA:
+            msg += f" ({last_error()})"
+        super().__init__(msg)
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the library (it must have been built: ``nhwave_gb300.build.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with nhwave_gb300.build.build() (there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    vp, i32, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_double
+    P = ctypes.POINTER
+    L.nhw_create.argtypes = [P(NhwParams), P(vp)]
+    L.nhw_destroy.argtypes = [vp]
+    L.nhw_setup.argtypes = [vp, vp, vp, vp]
+    L.nhw_get_field.argtypes = [vp, i32, vp]
+    L.nhw_set_field.argtypes = [vp, i32, vp]
+    L.nhw_field_shape.argtypes = [vp, i32, P(i32 * 3), P(i32)]
+    L.nhw_get_scalars.argtypes = [vp, P(NhwScalars)]
+    L.nhw_set_time.argtypes = [vp, dbl, dbl, i32]
+    for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_mask", "nhw_update_vars",
+              "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_synchronize"):
+        getattr(L, n).argtypes = [vp]
+    L.nhw_eval_duvw.argtypes = [vp, i32]
+    L.nhw_step.argtypes = [vp, P(dbl), P(dbl), P(i32)]
+    L.nhw_run.argtypes = [vp, i32, P(i32)]
+    L.nhw_mass.argtypes = [vp, P(dbl)]
+    L.nhw_abi_sizes.argtypes = [P(i32), P(i32)]
+    L.nhw_status_string.argtypes = [ctypes.c_int]
+    L.nhw_status_string.restype = ctypes.c_char_p
+    L.nhw_last_error.argtypes = []
+    L.nhw_last_error.restype = ctypes.c_char_p
+    for n in EXPORTS:
+        if n not in ("nhw_status_string", "nhw_last_error"):
+            getattr(L, n).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def status_string(st: int) -> str:
+    return load().nhw_status_string(st).decode()
+
+
+def last_error() -> str:
+    return load().nhw_last_error().decode()
+
+
+_HARD = {ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_DT_MIN, ERR_NAN, ERR_TIMEOUT, ERR_STATE}
+
+
+def _chk(st: int, where: str) -> int:
+    if st in _HARD:
+        raise NhwError(st, where)
+    if st == ERR_KRYLOV_NOCONV:
+        warnings.warn(f"{where}: Poisson solve stopped at ITMAX above TOL", RuntimeWarning, stacklevel=3)
+    return st
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Scenario:
+    """One scenario on the GPU through the C-ABI."""
+
+    def __init__(self, params: NhwParams, depth=None, eta0=None, uvw0=None):
+        L = load()
+        self.params = params.copy()
+        self.shape = F.Shapes(params)
+        h = ctypes.c_void_p()
+        _chk(L.nhw_create(ctypes.byref(self.params), ctypes.byref(h)), "nhw_create")
+        self._h = h
+        if depth is not None:
+            self.setup(depth, eta0, uvw0)
+
+    def setup(self, depth, eta0=None, uvw0=None):
+        keep = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (depth, eta0, uvw0)]
+        _chk(load().nhw_setup(self._h, *[_ptr(a) for a in keep]), "nhw_setup")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().nhw_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- the reference's subroutines
+    def estimate_dt(self):
+        return _chk(load().nhw_estimate_dt(self._h), "estimate_dt")
+
+    def update_bathymetry(self):
+        return _chk(load().nhw_update_bathymetry(self._h), "update_bathymetry")
+
+    def update_mask(self):
+        return _chk(load().nhw_update_mask(self._h), "update_mask")
+
+    def update_vars(self):
+        return _chk(load().nhw_update_vars(self._h), "update_vars")
+
+    def source_terms(self):
+        return _chk(load().nhw_source_terms(self._h), "source_terms")
+
+    def fluxes(self):
+        return _chk(load().nhw_fluxes(self._h), "fluxes")
+
+    def eval_duvw(self, istep: int):
+        return _chk(load().nhw_eval_duvw(self._h, istep), "eval_duvw")
+
+    def sponge_damping(self):
+        return _chk(load().nhw_sponge_damping(self._h), "sponge_damping")
+
+    def step(self):
+        return _chk(load().nhw_step(self._h, None, None, None), "nhw_step")
+
+    def run(self, n: int) -> int:
+        done = ctypes.c_int32(0)
+        _chk(load().nhw_run(self._h, n, ctypes.byref(done)), "nhw_run")
+        return done.value
+
+    def synchronize(self):
+        return _chk(load().nhw_synchronize(self._h), "nhw_synchronize")
+
+    def mass(self) -> float:
+        m = ctypes.c_double(0.0)
+        _chk(load().nhw_mass(self._h, ctypes.byref(m)), "nhw_mass")
+        return m.value
+
+    def scalars(self) -> NhwScalars:
+        s = NhwScalars()
+        _chk(load().nhw_get_scalars(self._h, ctypes.byref(s)), "nhw_get_scalars")
+        return s
+
+    def set_time(self, time: float, dt: float, run_step: int):
+        _chk(load().nhw_set_time(self._h, time, dt, run_step), "nhw_set_time")
+
+    def get(self, field: int) -> np.ndarray:
+        shp, dtype = self.shape.of(field)
+        out = np.empty(int(np.prod(shp)), dtype=dtype)
+        _chk(load().nhw_get_field(self._h, field, _ptr(out)), "nhw_get_field")
+        return out.reshape(shp[::-1])
+
+    def set(self, field: int, arr):
+        shp, dtype = self.shape.of(field)
+        a = np.ascontiguousarray(arr, dtype=dtype).ravel()
+        if a.size != int(np.prod(shp)):
+            raise ValueError(f"field {F.NAMES[field]} wants {shp}, got {a.size} elements")
+        _chk(load().nhw_set_field(self._h, field, _ptr(a)), "nhw_set_field")

@@ -1,0 +1,172 @@
+"""Seeded synthetic scenarios in the reference's input formats.
+
+No public benchmark-suite data is used: every input is generated here from a
+recorded seed and written in the shapes the reference reads -- ``depth.txt``
+(CELL_CENTER: Nglob rows of Mglob values, src/initialize.F:1833-1836),
+``eta0.txt`` and ``uvw0.txt`` (src/initialize.F:2994-3017: eta as Nglob rows
+of Mglob, then U, V, W each as Kglob x Nglob rows of Mglob).  Arrays returned
+here are flat float64 in that order (i fastest).
+
+Workloads (sizes and physics of the five configurations this path is
+measured on):
+  c1  solitary wave in a flat channel           256 x 8 x 10,   dx=dy=0.1 m
+  c2  monochromatic wave over a submerged bar   1024 x 64 x 20, dx=0.025, dy=0.05 m
+  c3  rigid submarine landslide, wet/dry beach  512 x 512 x 10, dx=dy=2 m
+  c4  ensemble member: random smooth bathymetry, Gaussian hump, walls
+plus small versions of each (``tiny_*``) that the CPU oracle runs in seconds.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .params import (
+    NHW_FP64, SLIDE_RIGID_3D, WM_INT_LIN, NhwParams, default_params,
+)
+
+GRAV = 9.81
+
+
+def _xc(p: NhwParams) -> np.ndarray:
+    return (np.arange(p.Mglob) + 0.5) * p.dx
+
+
+def _yc(p: NhwParams) -> np.ndarray:
+    return (np.arange(p.Nglob) + 0.5) * p.dy
+
+
+# ------------------------------------------------------------------- c1
+def solitary_channel(M=256, N=8, K=10, dx=0.1, h=1.0, amp=0.2, x0=5.0, **kw):
+    """KdV solitary wave eta = A sech^2(sqrt(3A/4h^3)(x-x0)), u = sqrt(g/h) eta."""
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dx, dt_ini=0.001, dt_min=1e-6,
+                       dt_max=1.0, cfl=0.5, min_dep=0.01, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, sim_steps=1000)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    depth = np.full((N, M), h)
+    xs = _xc(p)
+    eta1 = amp / np.cosh(math.sqrt(3.0 * amp / (4.0 * h ** 3)) * (xs - x0)) ** 2
+    eta = np.broadcast_to(eta1, (N, M)).copy()
+    u = math.sqrt(GRAV / h) * eta
+    uvw = np.zeros((3, K, N, M))
+    uvw[0] = u[None, :, :]
+    return p, depth.ravel(), eta.ravel(), uvw.ravel()
+
+
+# ------------------------------------------------------------------- c2
+def bar_depth(x: np.ndarray) -> np.ndarray:
+    """Trapezoidal bar: 0.4 m, 1:20 rise over 6-12 m to 0.1 m, flat to 14 m, 1:10 fall to 17 m."""
+    d = np.full_like(x, 0.4)
+    up = (x > 6.0) & (x <= 12.0)
+    d[up] = 0.4 - (x[up] - 6.0) * 0.05
+    d[(x > 12.0) & (x <= 14.0)] = 0.1
+    dn = (x > 14.0) & (x < 17.0)
+    d[dn] = 0.1 + (x[dn] - 14.0) * 0.1
+    return d
+
+
+def submerged_bar(M=1024, N=64, K=20, dx=0.025, dy=0.05, **kw):
+    """Internal wavemaker INT_LIN (T=2.02 s, a=0.01 m, h=0.4 m) and 2 m sponges at both ends."""
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.001, dt_min=1e-6,
+                       dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, total_time=20.0)
+    p.wavemaker = WM_INT_LIN
+    p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave, p.cur_wave = 0.01, 2.02, 0.4, 0.0, 0.0
+    p.xsource_west, p.xsource_east = 4.0, 4.2
+    p.ysource_suth, p.ysource_nrth = 0.0, N * dy
+    p.sponge_on = 1
+    p.sponge_west_width = p.sponge_east_width = 2.0
+    for k, v in kw.items():
+        setattr(p, k, v)
+    xs = _xc(p) * (25.6 / (M * dx))  # keep the bar's shape on smaller grids
+    depth = np.broadcast_to(bar_depth(xs), (N, M)).copy()
+    return p, depth.ravel(), None, None
+
+
+# ------------------------------------------------------------------- c3
+def landslide_beach(M=512, N=512, K=10, dx=2.0, **kw):
+    """Plane beach h = 60 - x/15 (dry land past x = 900 m) with a RIGID_3D slide."""
+    L = M * dx
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dx, dt_ini=0.01, dt_min=1e-6,
+                       dt_max=5.0, cfl=0.5, min_dep=0.01, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, total_time=200.0)
+    p.slide_type = SLIDE_RIGID_3D
+    p.slide_t, p.slide_l, p.slide_w = 8.0, 100.0 * L / 1024.0, 100.0 * L / 1024.0
+    p.slide_ut, p.slide_a0 = 15.0, 0.75            # s0 = ut^2/a0 = 300 m, t0 = ut/a0 = 20 s
+    p.slope_angle = math.degrees(math.atan(1.0 / 15.0))
+    p.slide_angle = 180.0                            # moving towards deep water (-x)
+    p.slide_x0, p.slide_y0 = 0.6 * L, 0.5 * N * dx
+    for k, v in kw.items():
+        setattr(p, k, v)
+    xs = _xc(p) * (1024.0 / L)
+    depth = np.broadcast_to(60.0 - xs / 15.0, (N, M)).copy()
+    return p, depth.ravel(), None, None
+
+
+# ------------------------------------------------------------------- c4
+def ensemble_member(rng: np.random.Generator, Kchoices=(5, 10, 15, 20), side=(64, 512),
+                    dxr=(1.0, 20.0), **kw):
+    """One scenario of the uneven ensemble: sides log-uniform in ``side``, K from
+    ``Kchoices``, dx log-uniform in ``dxr``; Gaussian-filtered white-noise
+    bathymetry (correlation length 20 cells) scaled to 5-200 m; Gaussian eta hump
+    of amplitude U[0.01,0.1]*h_local and width 10-40 cells; at rest; walls."""
+    from scipy.ndimage import gaussian_filter
+
+    lo, hi = math.log(side[0]), math.log(side[1])
+    M = int(round(math.exp(rng.uniform(lo, hi))))
+    N = int(round(math.exp(rng.uniform(lo, hi))))
+    K = int(rng.choice(Kchoices))
+    dx = float(math.exp(rng.uniform(math.log(dxr[0]), math.log(dxr[1]))))
+    noise = rng.standard_normal((N, M))
+    f = gaussian_filter(noise, sigma=20.0 / 2.0, mode="reflect")
+    f = (f - f.min()) / max(f.max() - f.min(), 1e-30)
+    depth = 5.0 + 195.0 * f
+    ci, cj = rng.uniform(0.25, 0.75) * M, rng.uniform(0.25, 0.75) * N
+    h_loc = float(depth[min(int(cj), N - 1), min(int(ci), M - 1)])
+    amp = rng.uniform(0.01, 0.1) * h_loc
+    width = rng.uniform(10.0, 40.0)
+    ii, jj = np.meshgrid(np.arange(M) + 0.5, np.arange(N) + 0.5)
+    eta = amp * np.exp(-((ii - ci) ** 2 + (jj - cj) ** 2) / width ** 2)
+    c = math.sqrt(GRAV * 200.0)
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dx, dt_ini=0.4 * dx / c,
+                       dt_min=1e-8, dt_max=60.0, cfl=0.5, min_dep=0.01, non_hydro=1,
+                       time_order=3, tol=1e-8, itmax=1000, sim_steps=500)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, depth.ravel(), eta.ravel(), np.zeros(3 * K * N * M)
+
+
+def ensemble(n: int, seed: int = 2024, **kw):
+    rng = np.random.default_rng(seed)
+    return [ensemble_member(rng, **kw) for _ in range(n)]
+
+
+# ------------------------------------------------------------ registry
+def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
+    """Return ``(params, depth, eta0, uvw0)`` for a named scenario."""
+    if name == "c1":
+        out = solitary_channel(**kw)
+    elif name == "c2":
+        out = submerged_bar(**kw)
+    elif name == "c3":
+        out = landslide_beach(**kw)
+    elif name == "c4":
+        out = ensemble_member(np.random.default_rng(seed), **kw)
+    elif name == "tiny_c1":
+        out = solitary_channel(M=48, N=4, K=5, x0=1.5, amp=0.1, **kw)
+    elif name == "tiny_c2":
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_c3":
+        out = landslide_beach(M=48, N=40, K=5, dx=2.0 * 1024 / 48 / 2, **kw)
+    elif name == "tiny_c4":
+        out = ensemble_member(np.random.default_rng(seed), Kchoices=(4, 5), side=(24, 48), **kw)
+    else:
+        raise KeyError(name)
+    p = out[0]
+    p.precision = precision
+    return out
+
+
+def cell_updates(p: NhwParams, steps: int) -> int:
+    return int(p.Mglob) * int(p.Nglob) * int(p.Kglob) * int(steps)

@@ -1,0 +1,1631 @@
+// nhw_oracle.cpp -- TEST INFRASTRUCTURE, not product code.
+//
+// A plain single-threaded FP64 C++ restatement of NHWAVE's time-step hot path,
+// written loop by loop after the reference Fortran so that each routine can be
+// checked against its source lines.  Only tests/, __graft_entry__.smoke() and
+// bench.py's CPU-baseline leg load it, and only as the checker / CPU baseline.
+//
+// Parity status: the reference is Fortran and no Fortran compiler exists in
+// this build environment, and the reference ships no golden outputs; this
+// restatement is therefore "parity unpinned" against the reference binary.  It
+// is pinned instead by known-answer tests (lake at rest, mass conservation,
+// mirror symmetry, linear dispersion, hand-computed limiter / HLL / Poisson
+// coefficients) in tests/test_oracle_*.py.
+//
+// Reference routines restated here (file:line in the reference project):
+//   generate_grid              src/initialize.F:1647-1729
+//   read_bathymetry            src/initialize.F:1734-2175 (CELL_CENTER/CELL_GRID, RIGID_3D slide)
+//   initial                    src/initialize.F:2502-3408 (non-optional parts)
+//   calculate_sponge           src/nhwave.F:6405-6460
+//   estimate_dt                src/nhwave.F:3694-3874
+//   update_bathymetry RIGID_3D src/nhwave.F:5755-5857, 6024-6071
+//   update_mask / update_vars  src/nhwave.F:5403-5511
+//   update_wind (Iws=1)        src/nhwave.F:5333-5400
+//   source_terms               src/source_terms.F:1-67, 418-455; wave_dispersion src/waves.F:61-91
+//   fluxes & co.               src/nhwave.F:1686-2351, 2354-2552, 2673-2776, 2813-2906
+//   eval_duvw (inviscid)       src/nhwave.F:539-1300
+//   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117
+//   interpolate_velocity_to_faces src/nhwave.F:1332-1368
+//   get_Omega                  src/nhwave.F:1411-1648
+//   wl_bc / phi_2D_coll        src/nhwave.F:5119-5330
+//   projection_corrector       src/nhwave.F:487-536
+//   poisson_solver             src/pressure.F:63-245 (solver replaced, see below)
+//   generate_coef_rhs          src/pressure.F:475-840
+//   sponge_damping             src/nhwave.F:6463-6502
+//   sigma_transform            src/nhwave.F:6505-6541
+//   statistics (MassVolume)    src/nhwave.F:3139-3148
+//
+// Arithmetic: IEEE FP64 with the reference's evaluation order written out
+// (left-to-right products and quotients, explicit parentheses) and built with
+// -ffp-contract=off.  Default-real literals of the reference (Grav=9.81,
+// pi, Small=1e-16, 1.05, 1e-6, 1/3, 2/3, 0.717, dsig=1.0/float(Kglob) ...)
+// are rounded to single precision and widened, as the reference's double build
+// does with empty FFLAGS (src/Makefile.farber.mpif90:40).
+//
+// The Poisson system is solved by restarted GMRES with a vertical-line
+// (tridiagonal) right preconditioner -- a solver of this file's own, standing in
+// for NSPCG (src/nspcg.f) / HYPRE GMRES+SMG (src/pressure.F:260-462) -- with the
+// same stopping test as HYPRE (||b-Ax||_2 <= TOL*||b||_2) and the previous P as
+// the initial guess (src/pressure.F:104-113, 386-397).
+
+#include "../include/nhwave_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+// reference parameters (src/mod_global.F:21-35): default-real literals
+const double pi = (double)3.141592653f;
+const double Small = (double)1.0e-16f;
+const double Large = 10000000.0;
+const double Grav = (double)9.81f;
+const double Zero = 0.0;
+const double Rho0 = 1000.0;
+const int Nghost = 2;
+
+inline double dmax(double a, double b) { return a > b ? a : b; }
+inline double dmin(double a, double b) { return a < b ? a : b; }
+
+struct A1 {
+  std::vector<double> v;
+  void init(int n) { v.assign(n, 0.0); }
+  double& operator()(int i) { return v[i - 1]; }
+};
+struct A2 {
+  int n1 = 0, n2 = 0;
+  std::vector<double> v;
+  void init(int a, int b) { n1 = a; n2 = b; v.assign((size_t)a * b, 0.0); }
+  double& operator()(int i, int j) { return v[(size_t)(i - 1) + (size_t)n1 * (j - 1)]; }
+  void fill(double x) { std::fill(v.begin(), v.end(), x); }
+};
+struct I2 {
+  int n1 = 0, n2 = 0;
+  std::vector<int32_t> v;
+  void init(int a, int b) { n1 = a; n2 = b; v.assign((size_t)a * b, 0); }
+  int32_t& operator()(int i, int j) { return v[(size_t)(i - 1) + (size_t)n1 * (j - 1)]; }
+};
+struct A3 {
+  int n1 = 0, n2 = 0, n3 = 0;
+  std::vector<double> v;
+  void init(int a, int b, int c) { n1 = a; n2 = b; n3 = c; v.assign((size_t)a * b * c, 0.0); }
+  double& operator()(int i, int j, int k) {
+    return v[(size_t)(i - 1) + (size_t)n1 * ((size_t)(j - 1) + (size_t)n2 * (k - 1))];
+  }
+  void fill(double x) { std::fill(v.begin(), v.end(), x); }
+};
+
+// LIMITER, van Leer (src/nhwave.F:2889-2906)
+inline double LIMITER(double A, double B) {
+  return (A * std::fabs(B) + std::fabs(A) * B) / (std::fabs(A) + std::fabs(B));
+}
+
+struct Model {
+  nhw_params p;
+  int Mloc, Nloc, Kloc, Mloc1, Nloc1, Kloc1;
+  int Ibeg, Iend, Iend1, Jbeg, Jend, Jend1, Kbeg, Kend, Kend1;
+  double dx, dy, dt = 0, dt_old = 0, TIME = 0, MinDep, fcor;
+  int RUN_STEP = 0, It_Order = 3;
+  double ALPHA[3], BETA[3];
+  int last_iters = 0, last_refine = 0;
+  int64_t total_iters = 0, solves = 0;
+  double last_relres = 0;
+  int status = NHW_OK;
+
+  A1 x, xc, y, yc, sig, dsig, sigc;
+  A2 Hc, Hc0, Ho, Hfx, Hfy, Hfx0, Hfy0, DeltH, DeltHo, Delt2H, DelxH, DelyH;
+  A2 D, D0, Eta, Eta0, SourceX, SourceY, SourceC, DxL, DxR, DyL, DyR;
+  A2 EtaxL, EtaxR, EtayL, EtayR, DelxEta, DelyEta, Sponge, Wsx, Wsy, R1s;
+  I2 Mask, Mask_Struct, Mask9;
+  A3 U, V, W, DU, DV, DW, DU0, DV0, DW0, P, Omega, Uf, Vf, Wf;
+  A3 UxL, UxR, VxL, VxR, WxL, WxR, DUxL, DUxR, DVxL, DVxR, DWxL, DWxR;
+  A3 UyL, UyR, VyL, VyR, WyL, WyR, DUyL, DUyR, DVyL, DVyR, DWyL, DWyR;
+  A3 UzL, UzR, VzL, VzR, WzL, WzR;
+  A3 SxL, SxR, SxS, SyL, SyR, SyS;
+  A3 ExL, ExR, FxL, FxR, GxL, GxR, HxL, HxR, EyL, EyR, FyL, FyR, GyL, GyR, HyL, HyR;
+  A3 Ex, Ey, Fx, Fy, Fz, Gx, Gy, Gz, Hx, Hy, Hz;
+  A3 DelxU, DelyU, DelzU, DelxV, DelyV, DelzV, DelxW, DelyW, DelzW;
+  A3 DelxDU, DelyDU, DelxDV, DelyDV, DelxDW, DelyDW, DelxSc, DelySc;
+  // Poisson system (Coef(neqns,15), Rhs(neqns); src/mod_global.F:239-243)
+  int neqns = 0;
+  std::vector<double> Coef, Rhs;
+  // Cmu = Visc, CmuR = CmuVt = 0 on the inviscid path (src/initialize.F:2663-2666)
+  double Cmu = 0, CmuR = 0, CmuVt = 0;
+
+  // ------------------------------------------------------------ index/alloc
+  int create(const nhw_params& q) {
+    p = q;
+    if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
+    if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+    for (int b : {p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn})
+      if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+    if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
+    // index (src/initialize.F:1339-1419), serial build
+    Mloc = p.Mglob + 2 * Nghost; Nloc = p.Nglob + 2 * Nghost; Kloc = p.Kglob + 2 * Nghost;
+    Mloc1 = Mloc + 1; Nloc1 = Nloc + 1; Kloc1 = Kloc + 1;
+    Ibeg = Nghost + 1; Iend = Mloc - Nghost; Iend1 = Mloc1 - Nghost;
+    Jbeg = Nghost + 1; Jend = Nloc - Nghost; Jend1 = Nloc1 - Nghost;
+    Kbeg = Nghost + 1; Kend = Kloc - Nghost; Kend1 = Kloc1 - Nghost;
+    dx = p.dx; dy = p.dy; MinDep = p.min_dep;
+    fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);  // src/initialize.F:494
+    x.init(Mloc1); xc.init(Mloc); y.init(Nloc1); yc.init(Nloc);
+    sig.init(Kloc1); dsig.init(Kloc); sigc.init(Kloc);
+    for (A2* a : {&Hc, &Hc0, &Ho, &DeltH, &DeltHo, &Delt2H, &DelxH, &DelyH, &D, &D0, &Eta, &Eta0,
+                  &SourceX, &SourceY, &SourceC, &DelxEta, &DelyEta, &Sponge, &Wsx, &Wsy, &R1s})
+      a->init(Mloc, Nloc);
+    for (A2* a : {&Hfx, &Hfx0, &DxL, &DxR, &EtaxL, &EtaxR}) a->init(Mloc1, Nloc);
+    for (A2* a : {&Hfy, &Hfy0, &DyL, &DyR, &EtayL, &EtayR}) a->init(Mloc, Nloc1);
+    Mask.init(Mloc, Nloc); Mask_Struct.init(Mloc, Nloc); Mask9.init(Mloc, Nloc);
+    for (A3* a : {&U, &V, &W, &DU, &DV, &DW, &DU0, &DV0, &DW0, &P, &DelxU, &DelyU, &DelzU, &DelxV,
+                  &DelyV, &DelzV, &DelxW, &DelyW, &DelzW, &DelxDU, &DelyDU, &DelxDV, &DelyDV,
+                  &DelxDW, &DelyDW, &DelxSc, &DelySc})
+      a->init(Mloc, Nloc, Kloc);
+    for (A3* a : {&Omega, &Uf, &Vf, &Wf, &UzL, &UzR, &VzL, &VzR, &WzL, &WzR, &Fz, &Gz, &Hz})
+      a->init(Mloc, Nloc, Kloc1);
+    for (A3* a : {&UxL, &UxR, &VxL, &VxR, &WxL, &WxR, &DUxL, &DUxR, &DVxL, &DVxR, &DWxL, &DWxR,
+                  &SxL, &SxR, &SxS, &ExL, &ExR, &FxL, &FxR, &GxL, &GxR, &HxL, &HxR, &Ex, &Fx,
+                  &Gx, &Hx})
+      a->init(Mloc1, Nloc, Kloc);
+    for (A3* a : {&UyL, &UyR, &VyL, &VyR, &WyL, &WyR, &DUyL, &DUyR, &DVyL, &DVyR, &DWyL, &DWyR,
+                  &SyL, &SyR, &SyS, &EyL, &EyR, &FyL, &FyR, &GyL, &GyR, &HyL, &HyR, &Ey, &Fy,
+                  &Gy, &Hy})
+      a->init(Mloc, Nloc1, Kloc);
+    neqns = p.Mglob * p.Nglob * p.Kglob;
+    Coef.assign((size_t)neqns * 15, 0.0);
+    Rhs.assign(neqns, 0.0);
+    return NHW_OK;
+  }
+
+  // -------------------------------------------------------- generate_grid
+  void generate_grid() {
+    x(Ibeg) = Zero;
+    for (int i = Ibeg + 1; i <= Mloc1; ++i) { x(i) = x(i - 1) + dx; xc(i - 1) = x(i - 1) + 0.5 * dx; }
+    for (int i = Ibeg - 1; i >= Ibeg - Nghost; --i) { x(i) = x(i + 1) - dx; xc(i) = x(i + 1) - 0.5 * dx; }
+    y(Jbeg) = Zero;
+    for (int j = Jbeg + 1; j <= Nloc1; ++j) { y(j) = y(j - 1) + dy; yc(j - 1) = y(j - 1) + 0.5 * dy; }
+    for (int j = Jbeg - 1; j >= Jbeg - Nghost; --j) { y(j) = y(j + 1) - dy; yc(j) = y(j + 1) - 0.5 * dy; }
+    if (p.ivgrd == 2) {
+      dsig(Kbeg) = (p.grd_r - 1.0) / (std::pow(p.grd_r, (double)(float)p.Kglob) - 1.0);
+      for (int k = Kbeg + 1; k <= Kend; ++k) dsig(k) = dsig(k - 1) * p.grd_r;
+      for (int k = 1; k <= Nghost; ++k) dsig(Kbeg - k) = dsig(Kbeg + k - 1);
+      for (int k = 1; k <= Nghost; ++k) dsig(Kend + k) = dsig(Kend - k + 1);
+    } else {
+      const double d = (double)(1.0f / (float)p.Kglob);  // 1.0/float(Kglob) in default real
+      for (int k = 1; k <= Kloc; ++k) dsig(k) = d;
+    }
+    sig(Kbeg) = Zero;
+    for (int k = Kbeg + 1; k <= Kloc1; ++k) { sig(k) = sig(k - 1) + dsig(k - 1); sigc(k - 1) = sig(k - 1) + 0.5 * dsig(k - 1); }
+    for (int k = Kbeg - 1; k >= 1; --k) { sig(k) = sig(k + 1) - dsig(k); sigc(k) = sig(k + 1) - 0.5 * dsig(k); }
+  }
+
+  // ---------------------------------------------------------- phi_2D_coll
+  void phi_2D_coll(A2& phi) {
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = 1; i <= Nghost; ++i) phi(i, j) = phi(Ibeg + Nghost - i, j);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = 1; i <= Nghost; ++i) phi(Iend + i, j) = phi(Iend - i + 1, j);
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nghost; ++j) phi(i, j) = phi(i, Jbeg + Nghost - j);
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nghost; ++j) phi(i, Jend + j) = phi(i, Jend - j + 1);
+  }
+
+  // ------------------------------------------------------ read_bathymetry
+  void slide_shape_rigid3d(double x0, double y0) {
+    const double e = (double)0.717f;
+    const double alpha0 = p.slide_angle * pi / 180.;
+    const double kb = 2.0 * std::acosh(1.0 / e) / p.slide_l;
+    const double kw = 2.0 * std::acosh(1.0 / e) / p.slide_w;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        double xt = (xc(i) - x0) * std::cos(alpha0) + (yc(j) - y0) * std::sin(alpha0);
+        double yt = -((xc(i) - x0) * std::sin(alpha0)) + (yc(j) - y0) * std::cos(alpha0);
+        double zt = p.slide_t / (1 - e) * (1.0 / std::cosh(kb * xt) / std::cosh(kw * yt) - e);
+        Hc(i, j) = Hc0(i, j) - dmax(0.0, zt);
+      }
+  }
+
+  void read_bathymetry(const double* depth) {
+    Hc.fill(0.0);
+    const int Mg = p.Mglob, Ng = p.Nglob;
+    if (p.depth_type == NHW_DEPTH_CELL_GRID) {
+      auto HG = [&](int i, int j) { return depth[(size_t)(i - 1) + (size_t)(Mg + 1) * (j - 1)]; };
+      auto Maskp = [&](int i, int j) { return HG(i, j) < -1000.0 ? 0 : 1; };
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          int ig = i - Nghost, jg = j - Nghost;
+          int ms = Maskp(ig, jg) + Maskp(ig + 1, jg) + Maskp(ig, jg + 1) + Maskp(ig + 1, jg + 1);
+          double num = HG(ig, jg) * Maskp(ig, jg) + HG(ig + 1, jg) * Maskp(ig + 1, jg) +
+                       HG(ig, jg + 1) * Maskp(ig, jg + 1) + HG(ig + 1, jg + 1) * Maskp(ig + 1, jg + 1);
+          // integer + default-real literal is evaluated in single precision
+          Hc(i, j) = num / (double)((float)ms + 1.e-16f);
+        }
+    } else {
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          Hc(i, j) = depth[(size_t)(i - Nghost - 1) + (size_t)Mg * (j - Nghost - 1)];
+    }
+    phi_2D_coll(Hc);
+    Hc0 = Hc;
+    if (p.slide_type == NHW_SLIDE_RIGID_3D) slide_shape_rigid3d(p.slide_x0, p.slide_y0);
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) Mask_Struct(i, j) = 1;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i)
+        if (Hc(i, j) < -1000.0) Mask_Struct(i, j) = 0;
+    for (int j = 1; j <= Nloc; ++j) {
+      for (int i = 2; i <= Mloc; ++i) Hfx(i, j) = 0.5 * (Hc(i - 1, j) + Hc(i, j));
+      Hfx(1, j) = Hc(1, j);
+      Hfx(Mloc1, j) = Hc(Mloc, j);
+    }
+    Hfx0 = Hfx;
+    for (int i = 1; i <= Mloc; ++i) {
+      for (int j = 2; j <= Nloc; ++j) Hfy(i, j) = 0.5 * (Hc(i, j - 1) + Hc(i, j));
+      Hfy(i, 1) = Hc(i, 1);
+      Hfy(i, Nloc1) = Hc(i, Nloc);
+    }
+    Hfy0 = Hfy;
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) {
+        DelxH(i, j) = (Hfx(i + 1, j) - Hfx(i, j)) / dx;
+        DelyH(i, j) = (Hfy(i, j + 1) - Hfy(i, j)) / dy;
+      }
+  }
+
+  // -------------------------------------------------------------- initial
+  void update_wind() {
+    // Iws = 1 (src/nhwave.F:5343-5398); constant in time for a constant wind
+    const double Cdsmin = (double)(1.e-3f * (0.61f + 0.063f * 6.0f));
+    const double Cdsmax = (double)(1.e-3f * (0.61f + 0.063f * 50.0f));
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        double WdU = p.wind_u, WdV = p.wind_v;
+        double Wds = std::sqrt(WdU * WdU + WdV * WdV);
+        double Cds = (double)1.e-3f * ((double)0.61f + (double)0.063f * Wds);
+        Cds = dmin(dmax(Cds, Cdsmin), Cdsmax);
+        Wsx(i, j) = (double)0.001293f * Cds * WdU * Wds;
+        Wsy(i, j) = (double)0.001293f * Cds * WdV * Wds;
+      }
+  }
+
+  void calculate_sponge() {
+    if (p.sponge_west_width > Zero)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i)
+          if (xc(i) <= p.sponge_west_width) {
+            double t = (xc(i) - p.sponge_west_width) / p.sponge_west_width;
+            Sponge(i, j) = std::sqrt(1.0 - dmin(t * t, 1.0));
+          }
+    if (p.sponge_east_width > Zero)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i)
+          if (xc(i) >= p.Mglob * dx - p.sponge_east_width) {
+            double t = (xc(i) - (p.Mglob * dx - p.sponge_east_width)) / p.sponge_east_width;
+            Sponge(i, j) = std::sqrt(1.0 - dmin(t * t, 1.0));
+          }
+    if (p.sponge_south_width > Zero)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i)
+          if (yc(j) <= p.sponge_south_width) {
+            double t = (yc(j) - p.sponge_south_width) / p.sponge_south_width;
+            Sponge(i, j) = std::sqrt(1.0 - dmin(t * t, 1.0));
+          }
+    if (p.sponge_north_width > Zero)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i)
+          if (yc(j) >= p.Nglob * dy - p.sponge_north_width) {
+            double t = (yc(j) - (p.Nglob * dy - p.sponge_north_width)) / p.sponge_north_width;
+            Sponge(i, j) = std::sqrt(1.0 - dmin(t * t, 1.0));
+          }
+  }
+
+  void initial(const double* eta0, const double* uvw0) {
+    TIME = Zero; RUN_STEP = 0; dt = p.dt_ini;
+    Sponge.fill(1.0);
+    Cmu = p.visc; CmuR = 0.0; CmuVt = 0.0;
+    Eta.fill(0.0);
+    const int Mg = p.Mglob, Ng = p.Nglob, Kg = p.Kglob;
+    if (eta0 || uvw0) {
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          size_t g = (size_t)(i - Nghost - 1) + (size_t)Mg * (j - Nghost - 1);
+          if (eta0) Eta(i, j) = eta0[g];
+          if (uvw0)
+            for (int k = Kbeg; k <= Kend; ++k) {
+              size_t g3 = g + (size_t)Mg * Ng * (k - Nghost - 1);
+              U(i, j, k) = uvw0[g3];
+              V(i, j, k) = uvw0[g3 + (size_t)Mg * Ng * Kg];
+              W(i, j, k) = uvw0[g3 + 2 * (size_t)Mg * Ng * Kg];
+            }
+        }
+    }
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) {
+        if ((Eta(i, j) + Hc(i, j)) <= MinDep) { Mask(i, j) = 0; Eta(i, j) = MinDep - Hc(i, j); }
+        else Mask(i, j) = 1;
+      }
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) Mask(i, j) = Mask(i, j) * Mask_Struct(i, j);
+    phi_2D_coll(Eta);
+    Eta0 = Eta;
+    compute_mask9();
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) D(i, j) = dmax(Hc(i, j) + Eta(i, j), MinDep);
+    update_wind();
+    vel_bc();
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          DU(i, j, k) = D(i, j) * U(i, j, k) * Mask(i, j);
+          DV(i, j, k) = D(i, j) * V(i, j, k) * Mask(i, j);
+          DW(i, j, k) = D(i, j) * W(i, j, k) * Mask(i, j);
+        }
+    if (p.time_order == 3) {
+      It_Order = 3;
+      ALPHA[0] = 0.0; ALPHA[1] = (double)(3.0f / 4.0f); ALPHA[2] = (double)(1.0f / 3.0f);
+      BETA[0] = 1.0; BETA[1] = (double)(1.0f / 4.0f); BETA[2] = (double)(2.0f / 3.0f);
+    } else if (p.time_order == 2) {
+      It_Order = 2;
+      ALPHA[0] = 0.0; ALPHA[1] = (double)(1.0f / 2.0f); BETA[0] = 1.0; BETA[1] = (double)(1.0f / 2.0f);
+    } else {
+      It_Order = 1; ALPHA[0] = 0.0; BETA[0] = 1.0;
+    }
+    if (p.sponge_on) calculate_sponge();
+  }
+
+  void compute_mask9() {
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i)
+        Mask9(i, j) = Mask(i, j) * Mask(i - 1, j) * Mask(i + 1, j) * Mask(i + 1, j + 1) * Mask(i, j + 1) *
+                      Mask(i - 1, j + 1) * Mask(i + 1, j - 1) * Mask(i, j - 1) * Mask(i - 1, j - 1);
+  }
+
+  // ---------------------------------------------------------- estimate_dt
+  int estimate_dt() {
+    dt_old = dt;
+    const double dt_growth = (double)1.05f * dt_old;
+    double tmp2 = Large;
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          double tmp1 = std::fabs(U(i, j, k)) + std::sqrt(Grav * D(i, j));
+          tmp1 = dmax(tmp1, Small);
+          double dxonu = dx / tmp1;
+          if (dxonu < tmp2) tmp2 = dxonu;
+          tmp1 = std::fabs(V(i, j, k)) + std::sqrt(Grav * D(i, j));
+          tmp1 = dmax(tmp1, Small);
+          double dyonv = dy / tmp1;
+          if (dyonv < tmp2) tmp2 = dyonv;
+          tmp1 = dmax(std::fabs(W(i, j, k)), Small);
+          double dzonw = dsig(k) * D(i, j) / tmp1;
+          if (dzonw < tmp2) tmp2 = dzonw;
+        }
+    const double dt_courant = p.cfl * tmp2;
+    const double dt_viscous = Large;
+    dt = dmin(dmin(dmin(dt_growth, dt_courant), dt_viscous), p.dt_max);
+    if (dt < p.dt_min) return NHW_ERR_DT_MIN;
+    TIME = TIME + dt;
+    RUN_STEP = RUN_STEP + 1;
+    return NHW_OK;
+  }
+
+  // ---------------------------------------------------- update_bathymetry
+  double hc_ext(int i, int j) {
+    // Hfx/Hfy below read Hc(Mloc+1,j) and Hc(i,Nloc+1): past the column, the
+    // Fortran storage continues with Hc(1,j+1); past the array it is undefined
+    // and taken as 0 here.  Only ghost-face values depend on it.
+    if (i == Mloc + 1) { i = 1; ++j; }
+    if (j > Nloc) return 0.0;
+    return Hc(i, j);
+  }
+
+  void update_bathymetry() {
+    Ho = Hc;
+    if (p.slide_type == NHW_SLIDE_RIGID_3D) {
+      const double alpha0 = p.slide_angle * pi / 180.;
+      const double slope0 = p.slope_angle * pi / 180.;
+      const double ut = p.slide_ut, a0 = p.slide_a0;
+      const double t0 = ut / a0;
+      const double s0 = ut * ut / a0;
+      const double st = s0 * std::log(std::cosh(TIME / t0)) * std::cos(slope0);
+      const double x0 = p.slide_x0 + st * std::cos(alpha0);
+      const double y0 = p.slide_y0 + st * std::sin(alpha0);
+      slide_shape_rigid3d(x0, y0);
+    }
+    phi_2D_coll(Hc);
+    for (int j = 1; j <= Nloc; ++j) {
+      for (int i = 2; i <= Mloc; ++i) Hfx(i, j) = 0.5 * (Hc(i, j) + hc_ext(i + 1, j));
+      Hfx(1, j) = Hfx(2, j);
+      Hfx(Mloc1, j) = Hfx(Mloc, j);
+    }
+    Hfx0 = Hfx;
+    for (int i = 1; i <= Mloc; ++i) {
+      for (int j = 2; j <= Nloc; ++j) Hfy(i, j) = 0.5 * (Hc(i, j) + hc_ext(i, j + 1));
+      Hfy(i, 1) = Hfy(i, 2);
+      Hfy(i, Nloc1) = Hfy(i, Nloc);
+    }
+    Hfy0 = Hfy;
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) {
+        DelxH(i, j) = (Hfx(i + 1, j) - Hfx(i, j)) / dx;
+        DelyH(i, j) = (Hfy(i, j + 1) - Hfy(i, j)) / dy;
+      }
+    DeltHo = DeltH;
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) DeltH(i, j) = (Hc(i, j) - Ho(i, j)) / dt;
+    if (RUN_STEP > 2)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) Delt2H(i, j) = (DeltH(i, j) - DeltHo(i, j)) / dt;
+  }
+
+  // ---------------------------------------------------------- update_mask
+  void update_mask() {
+    I2 Masktmp = Mask;
+    const double thr = (double)1.e-6f;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        if (Mask_Struct(i, j) == 0) continue;
+        if (Mask(i, j) == 0) {
+          if (Mask(i - 1, j) == 1 && Eta(i - 1, j) > Eta(i, j) && D(i - 1, j) - MinDep > thr) Masktmp(i, j) = 1;
+          if (Mask(i + 1, j) == 1 && Eta(i + 1, j) > Eta(i, j) && D(i + 1, j) - MinDep > thr) Masktmp(i, j) = 1;
+          if (Mask(i, j - 1) == 1 && Eta(i, j - 1) > Eta(i, j) && D(i, j - 1) - MinDep > thr) Masktmp(i, j) = 1;
+          if (Mask(i, j + 1) == 1 && Eta(i, j + 1) > Eta(i, j) && D(i, j + 1) - MinDep > thr) Masktmp(i, j) = 1;
+        } else {
+          if (std::fabs(D(i, j) - MinDep) <= thr) {
+            Masktmp(i, j) = 0;
+            Eta(i, j) = MinDep - Hc(i, j);
+            D(i, j) = Eta(i, j) + Hc(i, j);
+          }
+        }
+      }
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) Mask(i, j) = Masktmp(i, j) * Mask_Struct(i, j);
+    compute_mask9();
+  }
+
+  void update_vars() { D0 = D; Eta0 = Eta; DU0 = DU; DV0 = DV; DW0 = DW; }
+
+  // --------------------------------------------------------- source_terms
+  double wave_dispersion(double Segma) {
+    const double Dep = p.dep_wave;
+    double Wn = (Segma * Segma) / (Grav * std::pow(std::tanh(Segma * Segma * Dep / Grav), 0.5));
+    double error = 100.;
+    while (error >= (double)1.0e-8f) {
+      double Fk = Segma * Segma - Grav * Wn * std::tanh(Wn * Dep);
+      double ch = std::cosh(Wn * Dep);
+      double Fkdif = -(Grav * (std::tanh(Wn * Dep) + (Wn * Dep) / (ch * ch)));
+      double Wn_new = Wn - Fk / Fkdif;
+      error = std::fabs((Wn - Wn_new) / Wn);
+      Wn = Wn_new;
+    }
+    return Wn;
+  }
+
+  double source_area() {
+    double Source_Area = 0.0;
+    for (int i = Ibeg; i <= Iend; ++i)
+      if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east) Source_Area = Source_Area + dx * D(i, Jbeg + 1);
+    return Source_Area;
+  }
+
+  void source_terms() {
+    if (p.wavemaker == NHW_WM_INT_LIN) {
+      const double Segma = 2.0 * pi / p.per_wave;
+      const double Wave_Number = wave_dispersion(Segma);
+      const double Wave_Length = 2.0 * pi / Wave_Number;
+      const double Celerity = Wave_Length / p.per_wave;
+      const double WnumY = Wave_Number * std::sin(p.theta_wave * pi / 180.);
+      const double Source_Area = source_area();
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+              yc(j) <= p.ysource_nrth) {
+            double Phs_lag = yc(j) * WnumY;
+            SourceC(i, j) = Celerity * p.amp_wave / Source_Area * std::cos(pi / 2 - Segma * TIME + Phs_lag);
+          }
+    } else if (p.wavemaker == NHW_WM_INT_SOL) {
+      const double A = p.amp_wave, Dep = p.dep_wave;
+      const double Celerity = std::sqrt(Grav * Dep * (1.0 + A / Dep));
+      const double Atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
+      const double Xstart = 4.0 * Dep / std::sqrt(A / Dep);
+      const double Source_Area = source_area();
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+              yc(j) <= p.ysource_nrth) {
+            double ch = std::cosh(Atmp * (Xstart - Celerity * TIME));
+            SourceC(i, j) = 2.0 * Celerity / Source_Area * A / (ch * ch);
+          }
+    }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        SourceX(i, j) = Grav * 0.5 * (EtaxL(i + 1, j) + EtaxR(i, j)) * (Hfx0(i + 1, j) - Hfx0(i, j)) / dx * Mask(i, j);
+        SourceY(i, j) = Grav * 0.5 * (EtayL(i, j + 1) + EtayR(i, j)) * (Hfy0(i, j + 1) - Hfy0(i, j)) / dy * Mask(i, j);
+      }
+  }
+
+  // ------------------------------------------------------------ delxyzFun
+  void delxFun_2D(A2& Din, A2& Dout) {
+    for (int i = 2; i <= Mloc - 1; ++i)
+      for (int j = 1; j <= Nloc; ++j) {
+        if (Mask(i, j) == 0) Dout(i, j) = Zero;
+        else {
+          double T1 = (Din(i + 1, j) - Din(i, j)) / dx, T2 = (Din(i, j) - Din(i - 1, j)) / dx;
+          Dout(i, j) = (std::fabs(T1) + std::fabs(T2)) < Small ? Zero : LIMITER(T1, T2);
+        }
+      }
+    for (int j = 1; j <= Nloc; ++j) {
+      Dout(1, j) = (Din(2, j) - Din(1, j)) / dx;
+      Dout(Mloc, j) = (Din(Mloc, j) - Din(Mloc - 1, j)) / dx;
+    }
+  }
+  void delyFun_2D(A2& Din, A2& Dout) {
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 2; j <= Nloc - 1; ++j) {
+        if (Mask(i, j) == 0) Dout(i, j) = Zero;
+        else {
+          double T1 = (Din(i, j + 1) - Din(i, j)) / dy, T2 = (Din(i, j) - Din(i, j - 1)) / dy;
+          Dout(i, j) = (std::fabs(T1) + std::fabs(T2)) < Small ? Zero : LIMITER(T1, T2);
+        }
+      }
+    for (int i = 1; i <= Mloc; ++i) {
+      Dout(i, 1) = (Din(i, 2) - Din(i, 1)) / dy;
+      Dout(i, Nloc) = (Din(i, Nloc) - Din(i, Nloc - 1)) / dy;
+    }
+  }
+  // delxFun_3D / delxFun1_3D (same body over Kloc or Kloc1 levels)
+  void delxFun_3D(A3& Din, A3& Dout) {
+    const int L = Din.n3;
+    for (int i = 2; i <= Mloc - 1; ++i)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int k = 1; k <= L; ++k) {
+          if (Mask(i, j) == 0) Dout(i, j, k) = Zero;
+          else {
+            double T1 = (Din(i + 1, j, k) - Din(i, j, k)) / dx, T2 = (Din(i, j, k) - Din(i - 1, j, k)) / dx;
+            Dout(i, j, k) = (std::fabs(T1) + std::fabs(T2)) < Small ? Zero : LIMITER(T1, T2);
+          }
+        }
+    for (int j = 1; j <= Nloc; ++j)
+      for (int k = 1; k <= L; ++k) {
+        Dout(1, j, k) = (Din(2, j, k) - Din(1, j, k)) / dx;
+        Dout(Mloc, j, k) = (Din(Mloc, j, k) - Din(Mloc - 1, j, k)) / dx;
+      }
+  }
+  void delyFun_3D(A3& Din, A3& Dout) {
+    const int L = Din.n3;
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 2; j <= Nloc - 1; ++j)
+        for (int k = 1; k <= L; ++k) {
+          if (Mask(i, j) == 0) Dout(i, j, k) = Zero;
+          else {
+            double T1 = (Din(i, j + 1, k) - Din(i, j, k)) / dy, T2 = (Din(i, j, k) - Din(i, j - 1, k)) / dy;
+            Dout(i, j, k) = (std::fabs(T1) + std::fabs(T2)) < Small ? Zero : LIMITER(T1, T2);
+          }
+        }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int k = 1; k <= L; ++k) {
+        Dout(i, 1, k) = (Din(i, 2, k) - Din(i, 1, k)) / dy;
+        Dout(i, Nloc, k) = (Din(i, Nloc, k) - Din(i, Nloc - 1, k)) / dy;
+      }
+  }
+  void delzFun_3D(A3& Din, A3& Dout) {
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int k = 2; k <= Kloc - 1; ++k) {
+          double T1 = (Din(i, j, k + 1) - Din(i, j, k)) / (sigc(k + 1) - sigc(k));
+          double T2 = (Din(i, j, k) - Din(i, j, k - 1)) / (sigc(k) - sigc(k - 1));
+          Dout(i, j, k) = (std::fabs(T1) + std::fabs(T2)) < Small ? Zero : LIMITER(T1, T2);
+        }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nloc; ++j) {
+        Dout(i, j, 1) = (Din(i, j, 2) - Din(i, j, 1)) / (0.5 * (dsig(1) + dsig(2)));
+        Dout(i, j, Kloc) = (Din(i, j, Kloc) - Din(i, j, Kloc - 1)) / (0.5 * (dsig(Kloc - 1) + dsig(Kloc)));
+      }
+  }
+
+  void delxyzFun() {
+    delxFun_2D(Eta, DelxEta);
+    delxFun_3D(U, DelxU); delxFun_3D(V, DelxV); delxFun_3D(W, DelxW);
+    delxFun_3D(DU, DelxDU); delxFun_3D(DV, DelxDV); delxFun_3D(DW, DelxDW);
+    delyFun_2D(Eta, DelyEta);
+    delyFun_3D(U, DelyU); delyFun_3D(V, DelyV); delyFun_3D(W, DelyW);
+    delyFun_3D(DU, DelyDU); delyFun_3D(DV, DelyDV); delyFun_3D(DW, DelyDW);
+    delzFun_3D(U, DelzU); delzFun_3D(V, DelzV); delzFun_3D(W, DelzW);
+  }
+
+  // ----------------------------------------------------------- construct_*
+  void construct_2D_x(A2& Vin, A2& Din, A2& OutL, A2& OutR) {
+    OutL.fill(0.0); OutR.fill(0.0);
+    for (int i = Ibeg; i <= Iend1; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        OutL(i, j) = Vin(i - 1, j) + 0.5 * dx * Din(i - 1, j);
+        OutR(i, j) = Vin(i, j) - 0.5 * dx * Din(i, j);
+      }
+  }
+  void construct_3D_x(A3& Vin, A3& Din, A3& OutL, A3& OutR) {
+    OutL.fill(0.0); OutR.fill(0.0);
+    for (int i = Ibeg; i <= Iend1; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          OutL(i, j, k) = Vin(i - 1, j, k) + 0.5 * dx * Din(i - 1, j, k);
+          OutR(i, j, k) = Vin(i, j, k) - 0.5 * dx * Din(i, j, k);
+        }
+  }
+  void construct_2D_y(A2& Vin, A2& Din, A2& OutL, A2& OutR) {
+    OutL.fill(0.0); OutR.fill(0.0);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend1; ++j) {
+        OutL(i, j) = Vin(i, j - 1) + 0.5 * dy * Din(i, j - 1);
+        OutR(i, j) = Vin(i, j) - 0.5 * dy * Din(i, j);
+      }
+  }
+  void construct_3D_y(A3& Vin, A3& Din, A3& OutL, A3& OutR) {
+    OutL.fill(0.0); OutR.fill(0.0);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend1; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          OutL(i, j, k) = Vin(i, j - 1, k) + 0.5 * dy * Din(i, j - 1, k);
+          OutR(i, j, k) = Vin(i, j, k) - 0.5 * dy * Din(i, j, k);
+        }
+  }
+  void construct_3D_z(A3& Vin, A3& Din, A3& OutL, A3& OutR) {
+    OutL.fill(0.0); OutR.fill(0.0);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend1; ++k) {
+          OutL(i, j, k) = Vin(i, j, k - 1) + 0.5 * dsig(k - 1) * Din(i, j, k - 1);
+          OutR(i, j, k) = Vin(i, j, k) - 0.5 * dsig(k) * Din(i, j, k);
+        }
+  }
+  void KBC_surface() {
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        WzL(i, j, Kend1) = (Eta(i, j) - Eta0(i, j)) / dt + DelxEta(i, j) * UzL(i, j, Kend1) +
+                           DelyEta(i, j) * VzL(i, j, Kend1);
+  }
+  void KBC_bottom() {
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        WzR(i, j, Kbeg) = -DeltH(i, j) - DelxH(i, j) * UzR(i, j, Kbeg) - DelyH(i, j) * VzR(i, j, Kbeg);
+  }
+
+  double hydro(double eta, double h0) { return 0.5 * Grav * (eta * eta + 2.0 * eta * h0); }
+
+  void construction() {
+    construct_2D_x(Eta, DelxEta, EtaxL, EtaxR);
+    construct_3D_x(U, DelxU, UxL, UxR); construct_3D_x(V, DelxV, VxL, VxR);
+    construct_3D_x(W, DelxW, WxL, WxR); construct_3D_x(DU, DelxDU, DUxL, DUxR);
+    construct_3D_x(DV, DelxDV, DVxL, DVxR); construct_3D_x(DW, DelxDW, DWxL, DWxR);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend1; ++i) {
+        DxL(i, j) = EtaxL(i, j) + Hfx(i, j);
+        DxR(i, j) = EtaxR(i, j) + Hfx(i, j);
+      }
+    for (double& v : DxL.v) v = dmax(v, MinDep);
+    for (double& v : DxR.v) v = dmax(v, MinDep);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 1 && Mask(i + 1, j) == 0) {
+            EtaxL(i + 1, j) = Eta(i, j); DxL(i + 1, j) = D(i, j); Hfx0(i + 1, j) = Hc(i, j);
+            DUxL(i + 1, j, k) = Zero; DVxL(i + 1, j, k) = Zero; DWxL(i + 1, j, k) = Zero;
+            UxL(i + 1, j, k) = Zero; VxL(i + 1, j, k) = Zero; WxL(i + 1, j, k) = Zero;
+          } else if (Mask(i, j) == 1 && Mask(i - 1, j) == 0) {
+            EtaxR(i, j) = Eta(i, j); DxR(i, j) = D(i, j); Hfx0(i, j) = Hc(i, j);
+            DUxR(i, j, k) = Zero; DVxR(i, j, k) = Zero; DWxR(i, j, k) = Zero;
+            UxR(i, j, k) = Zero; VxR(i, j, k) = Zero; WxR(i, j, k) = Zero;
+          } else if (Mask(i, j) == 0) {
+            EtaxL(i + 1, j) = Eta(i, j); DxL(i + 1, j) = D(i, j);
+            DUxL(i + 1, j, k) = Zero; DVxL(i + 1, j, k) = Zero; DWxL(i + 1, j, k) = Zero;
+            UxL(i + 1, j, k) = Zero; VxL(i + 1, j, k) = Zero; WxL(i + 1, j, k) = Zero;
+            EtaxR(i, j) = Eta(i, j); DxR(i, j) = D(i, j);
+            DUxR(i, j, k) = Zero; DVxR(i, j, k) = Zero; DWxR(i, j, k) = Zero;
+            UxR(i, j, k) = Zero; VxR(i, j, k) = Zero; WxR(i, j, k) = Zero;
+          }
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend1; ++i) {
+          ExL(i, j, k) = DUxL(i, j, k);
+          ExR(i, j, k) = DUxR(i, j, k);
+          FxL(i, j, k) = DUxL(i, j, k) * UxL(i, j, k) + hydro(EtaxL(i, j), Hfx0(i, j));
+          FxR(i, j, k) = DUxR(i, j, k) * UxR(i, j, k) + hydro(EtaxR(i, j), Hfx0(i, j));
+          GxL(i, j, k) = DxL(i, j) * UxL(i, j, k) * VxL(i, j, k);
+          GxR(i, j, k) = DxR(i, j) * UxR(i, j, k) * VxR(i, j, k);
+          HxL(i, j, k) = DxL(i, j) * UxL(i, j, k) * WxL(i, j, k);
+          HxR(i, j, k) = DxR(i, j) * UxR(i, j, k) * WxR(i, j, k);
+        }
+    construct_2D_y(Eta, DelyEta, EtayL, EtayR);
+    construct_3D_y(U, DelyU, UyL, UyR); construct_3D_y(V, DelyV, VyL, VyR);
+    construct_3D_y(W, DelyW, WyL, WyR); construct_3D_y(DU, DelyDU, DUyL, DUyR);
+    construct_3D_y(DV, DelyDV, DVyL, DVyR); construct_3D_y(DW, DelyDW, DWyL, DWyR);
+    for (int j = Jbeg; j <= Jend1; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        DyL(i, j) = EtayL(i, j) + Hfy(i, j);
+        DyR(i, j) = EtayR(i, j) + Hfy(i, j);
+      }
+    for (double& v : DyL.v) v = dmax(v, MinDep);
+    for (double& v : DyR.v) v = dmax(v, MinDep);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 1 && Mask(i, j + 1) == 0) {
+            EtayL(i, j + 1) = Eta(i, j); DyL(i, j + 1) = D(i, j); Hfy0(i, j + 1) = Hc(i, j);
+            DUyL(i, j + 1, k) = Zero; DVyL(i, j + 1, k) = Zero; DWyL(i, j + 1, k) = Zero;
+            UyL(i, j + 1, k) = Zero; VyL(i, j + 1, k) = Zero; WyL(i, j + 1, k) = Zero;
+          } else if (Mask(i, j) == 1 && Mask(i, j - 1) == 0) {
+            EtayR(i, j) = Eta(i, j); DyR(i, j) = D(i, j); Hfy0(i, j) = Hc(i, j);
+            DUyR(i, j, k) = Zero; DVyR(i, j, k) = Zero; DWyR(i, j, k) = Zero;
+            UyR(i, j, k) = Zero; VyR(i, j, k) = Zero; WyR(i, j, k) = Zero;
+          } else if (Mask(i, j) == 0) {
+            EtayL(i, j + 1) = Eta(i, j); DyL(i, j + 1) = D(i, j);
+            DUyL(i, j + 1, k) = Zero; DVyL(i, j + 1, k) = Zero; DWyL(i, j + 1, k) = Zero;
+            UyL(i, j + 1, k) = Zero; VyL(i, j + 1, k) = Zero; WyL(i, j + 1, k) = Zero;
+            EtayR(i, j) = Eta(i, j); DyR(i, j) = D(i, j);
+            DUyR(i, j, k) = Zero; DVyR(i, j, k) = Zero; DWyR(i, j, k) = Zero;
+            UyR(i, j, k) = Zero; VyR(i, j, k) = Zero; WyR(i, j, k) = Zero;
+          }
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend1; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          EyL(i, j, k) = DVyL(i, j, k);
+          EyR(i, j, k) = DVyR(i, j, k);
+          FyL(i, j, k) = DyL(i, j) * UyL(i, j, k) * VyL(i, j, k);
+          FyR(i, j, k) = DyR(i, j) * UyR(i, j, k) * VyR(i, j, k);
+          GyL(i, j, k) = DVyL(i, j, k) * VyL(i, j, k) + hydro(EtayL(i, j), Hfy0(i, j));
+          GyR(i, j, k) = DVyR(i, j, k) * VyR(i, j, k) + hydro(EtayR(i, j), Hfy0(i, j));
+          HyL(i, j, k) = DyL(i, j) * VyL(i, j, k) * WyL(i, j, k);
+          HyR(i, j, k) = DyR(i, j) * VyR(i, j, k) * WyR(i, j, k);
+        }
+    construct_3D_z(U, DelzU, UzL, UzR); construct_3D_z(V, DelzV, VzL, VzR);
+    construct_3D_z(W, DelzW, WzL, WzR);
+    KBC_surface();
+    KBC_bottom();
+  }
+
+  // ------------------------------------------------------------ wave_speed
+  void wave_speed() {
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend1; ++i) {
+          if (Mask(i - 1, j) == 1 && Mask(i, j) == 1) {
+            double L = std::sqrt(Grav * std::fabs(DxL(i, j))), R = std::sqrt(Grav * std::fabs(DxR(i, j)));
+            double S = 0.5 * (L + R) + 0.25 * (UxL(i, j, k) - UxR(i, j, k));
+            double US = 0.5 * (UxL(i, j, k) + UxR(i, j, k)) + L - R;
+            SxL(i, j, k) = dmin(UxL(i, j, k) - L, US - S);
+            SxR(i, j, k) = dmax(UxR(i, j, k) + R, US + S);
+            SxS(i, j, k) = US;
+          } else if (Mask(i - 1, j) == 0 && Mask(i, j) == 1) {
+            double R = std::sqrt(Grav * std::fabs(DxR(i, j)));
+            SxL(i, j, k) = UxR(i, j, k) - 2.0 * R;
+            SxR(i, j, k) = UxR(i, j, k) + R;
+            SxS(i, j, k) = SxL(i, j, k);
+          } else if (Mask(i - 1, j) == 1 && Mask(i, j) == 0) {
+            double L = std::sqrt(Grav * std::fabs(DxL(i, j)));
+            SxL(i, j, k) = UxL(i, j, k) - L;
+            SxR(i, j, k) = UxL(i, j, k) + 2.0 * L;
+            SxS(i, j, k) = SxR(i, j, k);
+          }
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend1; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j - 1) == 1 && Mask(i, j) == 1) {
+            double L = std::sqrt(Grav * std::fabs(DyL(i, j))), R = std::sqrt(Grav * std::fabs(DyR(i, j)));
+            double S = 0.5 * (L + R) + 0.25 * (VyL(i, j, k) - VyR(i, j, k));
+            double US = 0.5 * (VyL(i, j, k) + VyR(i, j, k)) + L - R;
+            SyL(i, j, k) = dmin(VyL(i, j, k) - L, US - S);
+            SyR(i, j, k) = dmax(VyR(i, j, k) + R, US + S);
+            SyS(i, j, k) = US;
+          } else if (Mask(i, j - 1) == 0 && Mask(i, j) == 1) {
+            double R = std::sqrt(Grav * std::fabs(DyR(i, j)));
+            SyL(i, j, k) = VyR(i, j, k) - 2.0 * R;
+            SyR(i, j, k) = VyR(i, j, k) + R;
+            SyS(i, j, k) = SyL(i, j, k);
+          } else if (Mask(i, j - 1) == 1 && Mask(i, j) == 0) {
+            double L = std::sqrt(Grav * std::fabs(DyL(i, j)));
+            SyL(i, j, k) = VyL(i, j, k) - L;
+            SyR(i, j, k) = VyL(i, j, k) + 2.0 * L;
+            SyS(i, j, k) = SyR(i, j, k);
+          }
+        }
+  }
+
+  // HLL (src/nhwave.F:2741-2776) over a whole face array; UL/UR given per face
+  void HLL(A3& SL, A3& SR, A3& FL, A3& FR, A3* UL3, A3* UR3, A2* UL2, A2* UR2, A3& FOUT) {
+    for (int k = 1; k <= FOUT.n3; ++k)
+      for (int j = 1; j <= FOUT.n2; ++j)
+        for (int i = 1; i <= FOUT.n1; ++i) {
+          double sl = SL(i, j, k), sr = SR(i, j, k);
+          if (sl >= Zero) FOUT(i, j, k) = FL(i, j, k);
+          else if (sr <= Zero) FOUT(i, j, k) = FR(i, j, k);
+          else {
+            double ul = UL3 ? (*UL3)(i, j, k) : (*UL2)(i, j);
+            double ur = UR3 ? (*UR3)(i, j, k) : (*UR2)(i, j);
+            double f = sr * FL(i, j, k) - sl * FR(i, j, k) + sl * sr * (ur - ul);
+            if (std::fabs(sr - sl) < Small) f = f / Small;
+            else f = f / (sr - sl);
+            FOUT(i, j, k) = f;
+          }
+        }
+  }
+
+  void fluxes_at_faces_HLL() {
+    HLL(SxL, SxR, ExL, ExR, nullptr, nullptr, &DxL, &DxR, Ex);
+    HLL(SyL, SyR, EyL, EyR, nullptr, nullptr, &DyL, &DyR, Ey);
+    HLL(SxL, SxR, FxL, FxR, &DUxL, &DUxR, nullptr, nullptr, Fx);
+    HLL(SyL, SyR, FyL, FyR, &DUyL, &DUyR, nullptr, nullptr, Fy);
+    HLL(SxL, SxR, GxL, GxR, &DVxL, &DVxR, nullptr, nullptr, Gx);
+    HLL(SyL, SyR, GyL, GyR, &DVyL, &DVyR, nullptr, nullptr, Gy);
+    HLL(SxL, SxR, HxL, HxR, &DWxL, &DWxR, nullptr, nullptr, Hx);
+    HLL(SyL, SyR, HyL, HyR, &DWyL, &DWyR, nullptr, nullptr, Hy);
+    for (int k = Kbeg + 1; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          double om = Omega(i, j, k);
+          Fz(i, j, k) = 0.5 * (om * (UzL(i, j, k) + UzR(i, j, k)) - std::fabs(om) * (UzR(i, j, k) - UzL(i, j, k)));
+          Gz(i, j, k) = 0.5 * (om * (VzL(i, j, k) + VzR(i, j, k)) - std::fabs(om) * (VzR(i, j, k) - VzL(i, j, k)));
+          Hz(i, j, k) = 0.5 * (om * (WzL(i, j, k) + WzR(i, j, k)) - std::fabs(om) * (WzR(i, j, k) - WzL(i, j, k)));
+        }
+  }
+
+  void flux_bc() {
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) {  // walls: Bc 1, 2 (5)
+        Ex(Ibeg, j, k) = Zero; Fx(Ibeg, j, k) = hydro(EtaxR(Ibeg, j), Hfx0(Ibeg, j));
+        Gx(Ibeg, j, k) = Zero; Hx(Ibeg, j, k) = Zero;
+        Ex(Iend1, j, k) = Zero; Fx(Iend1, j, k) = hydro(EtaxL(Iend1, j), Hfx0(Iend1, j));
+        Gx(Iend1, j, k) = Zero; Hx(Iend1, j, k) = Zero;
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        Ey(i, Jbeg, k) = Zero; Fy(i, Jbeg, k) = Zero;
+        Gy(i, Jbeg, k) = hydro(EtayR(i, Jbeg), Hfy0(i, Jbeg)); Hy(i, Jbeg, k) = Zero;
+        Ey(i, Jend1, k) = Zero; Fy(i, Jend1, k) = Zero;
+        Gy(i, Jend1, k) = hydro(EtayL(i, Jend1), Hfy0(i, Jend1)); Hy(i, Jend1, k) = Zero;
+      }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        Fz(i, j, Kbeg) = Zero; Gz(i, j, Kbeg) = Zero; Hz(i, j, Kbeg) = Zero;
+        Fz(i, j, Kend1) = Zero; Gz(i, j, Kend1) = Zero; Hz(i, j, Kend1) = Zero;
+      }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg - 1; j <= Jend + 1; ++j)
+        for (int i = Ibeg - 1; i <= Iend + 1; ++i)
+          if (Mask(i, j) == 0) {
+            Ex(i, j, k) = Zero;
+            Fx(i, j, k) = (i == Ibeg) ? Zero : hydro(EtaxL(i, j), Hfx0(i, j)) * Mask(i - 1, j);
+            Gx(i, j, k) = Zero; Hx(i, j, k) = Zero;
+            Ex(i + 1, j, k) = Zero;
+            Fx(i + 1, j, k) = (i == Iend) ? Zero : hydro(EtaxR(i + 1, j), Hfx0(i + 1, j)) * Mask(i + 1, j);
+            Gx(i + 1, j, k) = Zero; Hx(i + 1, j, k) = Zero;
+            Ey(i, j, k) = Zero; Fy(i, j, k) = Zero;
+            Gy(i, j, k) = (j == Jbeg) ? Zero : hydro(EtayL(i, j), Hfy0(i, j)) * Mask(i, j - 1);
+            Hy(i, j, k) = Zero;
+            Ey(i, j + 1, k) = Zero; Fy(i, j + 1, k) = Zero;
+            Gy(i, j + 1, k) = (j == Jend) ? Zero : hydro(EtayR(i, j + 1), Hfy0(i, j + 1)) * Mask(i, j + 1);
+            Hy(i, j + 1, k) = Zero;
+          }
+  }
+
+  void fluxes() {
+    delxyzFun();
+    construction();
+    wave_speed();
+    fluxes_at_faces_HLL();
+    flux_bc();
+  }
+
+  // -------------------------------------------------------------- wl_bc
+  void wl_bc() {
+    for (int j = Jbeg; j <= Jend; ++j) {
+      for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);
+      for (int i = 1; i <= Nghost; ++i) D(Iend + i, j) = D(Iend - i + 1, j);
+    }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nghost; ++j) D(i, j) = D(i, Jbeg + Nghost - j);
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nghost; ++j) D(i, Jend + j) = D(i, Jend - j + 1);
+  }
+
+  void sigma_transform() {
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          DelxSc(i, j, k) = (1.0 - sigc(k)) / D(i, j) * DelxH(i, j) - sigc(k) / D(i, j) * DelxEta(i, j);
+          DelySc(i, j, k) = (1.0 - sigc(k)) / D(i, j) * DelyH(i, j) - sigc(k) / D(i, j) * DelyEta(i, j);
+        }
+  }
+
+  // ------------------------------------------------------- get_UVW/vel_bc
+  void vel_bc() {
+    const int sx0 = p.bc_x0 == 1 ? 1 : -1, sxn = p.bc_xn == 1 ? 1 : -1;
+    const int sy0 = p.bc_y0 == 1 ? 1 : -1, syn = p.bc_yn == 1 ? 1 : -1;
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = 1; i <= Nghost; ++i) {
+          U(Ibeg - i, j, k) = -U(Ibeg + i - 1, j, k);
+          V(Ibeg - i, j, k) = sx0 * V(Ibeg + i - 1, j, k);
+          W(Ibeg - i, j, k) = sx0 * W(Ibeg + i - 1, j, k);
+          DU(Ibeg - i, j, k) = -DU(Ibeg + i - 1, j, k);
+          DV(Ibeg - i, j, k) = sx0 * DV(Ibeg + i - 1, j, k);
+          DW(Ibeg - i, j, k) = sx0 * DW(Ibeg + i - 1, j, k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = 1; i <= Nghost; ++i) {
+          U(Iend + i, j, k) = -U(Iend - i + 1, j, k);
+          V(Iend + i, j, k) = sxn * V(Iend - i + 1, j, k);
+          W(Iend + i, j, k) = sxn * W(Iend - i + 1, j, k);
+          DU(Iend + i, j, k) = -DU(Iend - i + 1, j, k);
+          DV(Iend + i, j, k) = sxn * DV(Iend - i + 1, j, k);
+          DW(Iend + i, j, k) = sxn * DW(Iend - i + 1, j, k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int j = 1; j <= Nghost; ++j) {
+          U(i, Jbeg - j, k) = sy0 * U(i, Jbeg + j - 1, k);
+          V(i, Jbeg - j, k) = -V(i, Jbeg + j - 1, k);
+          W(i, Jbeg - j, k) = sy0 * W(i, Jbeg + j - 1, k);
+          DU(i, Jbeg - j, k) = sy0 * DU(i, Jbeg + j - 1, k);
+          DV(i, Jbeg - j, k) = -DV(i, Jbeg + j - 1, k);
+          DW(i, Jbeg - j, k) = sy0 * DW(i, Jbeg + j - 1, k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int j = 1; j <= Nghost; ++j) {
+          U(i, Jend + j, k) = syn * U(i, Jend - j + 1, k);
+          V(i, Jend + j, k) = -V(i, Jend - j + 1, k);
+          W(i, Jend + j, k) = syn * W(i, Jend - j + 1, k);
+          DU(i, Jend + j, k) = syn * DU(i, Jend - j + 1, k);
+          DV(i, Jend + j, k) = -DV(i, Jend - j + 1, k);
+          DW(i, Jend + j, k) = syn * DW(i, Jend - j + 1, k);
+        }
+    A3 DelxUzL, DelxVzL, DelxWzL, DelyUzL, DelyVzL, DelyWzL;
+    for (A3* a : {&DelxUzL, &DelxVzL, &DelxWzL, &DelyUzL, &DelyVzL, &DelyWzL}) a->init(Mloc, Nloc, Kloc1);
+    delzFun_3D(U, DelzU); delzFun_3D(V, DelzV); delzFun_3D(W, DelzW);
+    construct_3D_z(U, DelzU, UzL, UzR); construct_3D_z(V, DelzV, VzL, VzR);
+    construct_3D_z(W, DelzW, WzL, WzR);
+    KBC_surface();
+    KBC_bottom();
+    delxFun_3D(UzL, DelxUzL); delxFun_3D(VzL, DelxVzL); delxFun_3D(WzL, DelxWzL);
+    delyFun_3D(UzL, DelyUzL); delyFun_3D(VzL, DelyVzL); delyFun_3D(WzL, DelyWzL);
+    const double MinDepBC = (double)0.01f;
+    const double visc_top = Small + 0.5 * (Cmu + CmuR + CmuVt + Cmu + CmuR + CmuVt);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        const double dxe = DelxEta(i, j), dye = DelyEta(i, j), Dij = D(i, j);
+        const double Atop = std::sqrt(1.0 + dxe * dxe + dye * dye);
+        const double Fext_Wind1 = 1.0 / Atop * ((1 - dxe * dxe) * Wsx(i, j) - dxe * dye * Wsy(i, j));
+        const double Fext_Wind2 = 1.0 / Atop * ((1 - dye * dye) * Wsy(i, j) - dxe * dye * Wsx(i, j));
+        for (int k = 1; k <= Nghost; ++k) {
+          // bottom, free slip (Bc_Z0 = 1)
+          DW(i, j, Kbeg - k) = 2.0 * Dij * WzR(i, j, Kbeg) - DW(i, j, Kbeg + k - 1);
+          DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1);
+          DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1);
+          // surface
+          const double dsg = sigc(Kend + k) - sigc(Kend - k + 1);
+          DW(i, j, Kend + k) = 2.0 * Dij * WzL(i, j, Kend1) - DW(i, j, Kend - k + 1);
+          DU(i, j, Kend + k) = DU(i, j, Kend - k + 1) +
+              dsg * (Fext_Wind1 * (Dij * Dij / Atop / visc_top) -
+                     dxe * (Dij * WzL(i, j, Kend1) - DW(i, j, Kend - k + 1)) / (dsg / 2.0) +
+                     Dij * Dij / (Atop * Atop) *
+                         (+2.0 * dxe * DelxUzL(i, j, Kend1) - (1.0 - dxe * dxe) * DelxWzL(i, j, Kend1) +
+                          dye * (DelyUzL(i, j, Kend1) + DelxVzL(i, j, Kend1) + dxe * DelyWzL(i, j, Kend1))));
+          const double DUtop_old = 2.0 * Dij * UzL(i, j, Kend1) - DU(i, j, Kend - k + 1);
+          if (DUtop_old > 0.) DU(i, j, Kend + k) = dmin(3.0 * DUtop_old, dmax(-1.0 * DUtop_old, DU(i, j, Kend + k)));
+          else if (DUtop_old < 0.) DU(i, j, Kend + k) = dmax(3.0 * DUtop_old, dmin(-1.0 * DUtop_old, DU(i, j, Kend + k)));
+          if (Dij < MinDepBC) DU(i, j, Kend + k) = DU(i, j, Kend - k + 1);
+          DV(i, j, Kend + k) = DV(i, j, Kend - k + 1) +
+              dsg * (Fext_Wind2 * (Dij * Dij / Atop / visc_top) -
+                     dye * (Dij * WzL(i, j, Kend1) - DW(i, j, Kend - k + 1)) / (dsg / 2.0) +
+                     Dij * Dij / (Atop * Atop) *
+                         (+2.0 * dye * DelyVzL(i, j, Kend1) - (1.0 - dye * dye) * DelyWzL(i, j, Kend1) +
+                          dxe * (DelxVzL(i, j, Kend1) + DelyUzL(i, j, Kend1) + dye * DelxWzL(i, j, Kend1))));
+          const double DVtop_old = 2.0 * Dij * VzL(i, j, Kend1) - DV(i, j, Kend - k + 1);
+          if (DVtop_old > 0.) DV(i, j, Kend + k) = dmin(3.0 * DVtop_old, dmax(-1.0 * DVtop_old, DV(i, j, Kend + k)));
+          else if (DVtop_old < 0.) DV(i, j, Kend + k) = dmax(3.0 * DVtop_old, dmin(-1.0 * DVtop_old, DV(i, j, Kend + k)));
+          if (Dij < MinDepBC) DV(i, j, Kend + k) = DV(i, j, Kend - k + 1);
+          U(i, j, Kbeg - k) = DU(i, j, Kbeg - k) / Dij;
+          V(i, j, Kbeg - k) = DV(i, j, Kbeg - k) / Dij;
+          W(i, j, Kbeg - k) = DW(i, j, Kbeg - k) / Dij;
+          U(i, j, Kend + k) = DU(i, j, Kend + k) / Dij;
+          V(i, j, Kend + k) = DV(i, j, Kend + k) / Dij;
+          W(i, j, Kend + k) = DW(i, j, Kend + k) / Dij;
+        }
+      }
+  }
+
+  void get_UVW() {
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          U(i, j, k) = DU(i, j, k) / D(i, j);
+          V(i, j, k) = DV(i, j, k) / D(i, j);
+          W(i, j, k) = DW(i, j, k) / D(i, j);
+        }
+    vel_bc();
+  }
+
+  void interpolate_velocity_to_faces() {
+    for (int k = 2; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          double f = dsig(k) / (dsig(k) + dsig(k - 1));
+          Uf(i, j, k) = (1.0 - f) * U(i, j, k) + f * U(i, j, k - 1);
+          Vf(i, j, k) = (1.0 - f) * V(i, j, k) + f * V(i, j, k - 1);
+          Wf(i, j, k) = (1.0 - f) * W(i, j, k) + f * W(i, j, k - 1);
+        }
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) {
+        Uf(i, j, 1) = U(i, j, 1); Vf(i, j, 1) = V(i, j, 1); Wf(i, j, 1) = W(i, j, 1);
+        Uf(i, j, Kloc1) = U(i, j, Kloc); Vf(i, j, Kloc1) = V(i, j, Kloc); Wf(i, j, Kloc1) = W(i, j, Kloc);
+      }
+  }
+
+  // ---------------------------------------------------- generate_coef_rhs
+  int idx(int i, int j, int k) { return (i - Ibeg) + p.Mglob * ((j - Jbeg) + p.Nglob * (k - Kbeg)); }
+  double& C(int ic, int n) { return Coef[(size_t)(n - 1) * neqns + ic]; }
+
+  void generate_coef_rhs() {
+    A3 DelxS, DelyS, DelzS, A1s;
+    for (A3* a : {&DelxS, &DelyS, &DelzS, &A1s}) a->init(Mloc, Nloc, Kloc1);
+    for (int k = Kbeg; k <= Kend1; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          DelxS(i, j, k) = (1. - sig(k)) / D(i, j) * DelxH(i, j) - sig(k) / D(i, j) * DelxEta(i, j);
+          DelyS(i, j, k) = (1. - sig(k)) / D(i, j) * DelyH(i, j) - sig(k) / D(i, j) * DelyEta(i, j);
+          DelzS(i, j, k) = 1. / D(i, j);
+          A1s(i, j, k) = DelxS(i, j, k) * DelxS(i, j, k) + DelyS(i, j, k) * DelyS(i, j, k) +
+                         DelzS(i, j, k) * DelzS(i, j, k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          const double hk = 0.5 * (dsig(k) + dsig(k - 1));
+          Rhs[idx(i, j, k)] =
+              -((Uf(i + 1, j, k) - Uf(i - 1, j, k)) / (2.0 * dx) + (U(i, j, k) - U(i, j, k - 1)) / hk * DelxS(i, j, k) +
+                (Vf(i, j + 1, k) - Vf(i, j - 1, k)) / (2.0 * dy) + (V(i, j, k) - V(i, j, k - 1)) / hk * DelyS(i, j, k) +
+                (W(i, j, k) - W(i, j, k - 1)) / hk * DelzS(i, j, k) - SourceC(i, j)) *
+              Rho0 / dt;
+        }
+    std::fill(Coef.begin(), Coef.end(), 0.0);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          const int ic = idx(i, j, k);
+          const double s = dsig(k) + dsig(k - 1), hk = 0.5 * (dsig(k) + dsig(k - 1));
+          const double a1 = A1s(i, j, k);
+          C(ic, 1) = 2. / (dx * dx) + 2. / (dy * dy) + a1 / (hk * dsig(k)) + a1 / (hk * dsig(k - 1));
+          C(ic, 2) = -1. / (dx * dx);
+          C(ic, 3) = -1. / (dy * dy);
+          C(ic, 4) = DelyS(i, j - 1, k) / (2. * dy * s) + DelyS(i, j, k) / (2. * dy * s);
+          C(ic, 5) = DelxS(i - 1, j, k) / (2. * dx * s) + DelxS(i, j, k) / (2. * dx * s);
+          C(ic, 6) = -a1 / (hk * dsig(k));
+          C(ic, 7) = -(DelxS(i + 1, j, k) / (2. * dx * s) + DelxS(i, j, k) / (2. * dx * s));
+          C(ic, 8) = -(DelyS(i, j + 1, k) / (2. * dy * s) + DelyS(i, j, k) / (2. * dy * s));
+          C(ic, 9) = -1. / (dx * dx);
+          C(ic, 10) = -1. / (dy * dy);
+          C(ic, 11) = DelyS(i, j + 1, k) / (2. * dy * s) + DelyS(i, j, k) / (2. * dy * s);
+          C(ic, 12) = DelxS(i + 1, j, k) / (2. * dx * s) + DelxS(i, j, k) / (2. * dx * s);
+          C(ic, 13) = -a1 / (hk * dsig(k - 1));
+          C(ic, 14) = -(DelxS(i - 1, j, k) / (2. * dx * s) + DelxS(i, j, k) / (2. * dx * s));
+          C(ic, 15) = -(DelyS(i, j - 1, k) / (2. * dy * s) + DelyS(i, j, k) / (2. * dy * s));
+        }
+    auto fold = [&](int ic, int dst, int src) { C(ic, dst) = C(ic, dst) + C(ic, src); };
+    for (int k = Kbeg; k <= Kend; ++k)  // left
+      for (int j = Jbeg; j <= Jend; ++j) {
+        int ic = idx(Ibeg, j, k);
+        fold(ic, 1, 9); fold(ic, 6, 5); fold(ic, 13, 14);
+        C(ic, 9) = Zero; C(ic, 5) = Zero; C(ic, 14) = Zero;
+      }
+    for (int k = Kbeg; k <= Kend; ++k)  // right
+      for (int j = Jbeg; j <= Jend; ++j) {
+        int ic = idx(Iend, j, k);
+        fold(ic, 1, 2); fold(ic, 6, 7); fold(ic, 13, 12);
+        C(ic, 2) = Zero; C(ic, 7) = Zero; C(ic, 12) = Zero;
+      }
+    for (int k = Kbeg; k <= Kend; ++k)  // front
+      for (int i = Ibeg; i <= Iend; ++i) {
+        int ic = idx(i, Jbeg, k);
+        fold(ic, 1, 10); fold(ic, 6, 4); fold(ic, 13, 15);
+        C(ic, 10) = Zero; C(ic, 4) = Zero; C(ic, 15) = Zero;
+      }
+    for (int k = Kbeg; k <= Kend; ++k)  // back
+      for (int i = Ibeg; i <= Iend; ++i) {
+        int ic = idx(i, Jend, k);
+        fold(ic, 1, 3); fold(ic, 6, 8); fold(ic, 13, 11);
+        C(ic, 3) = Zero; C(ic, 8) = Zero; C(ic, 11) = Zero;
+      }
+    for (int j = Jbeg; j <= Jend; ++j)  // bottom (Neumann)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        int ic = idx(i, j, Kbeg);
+        if (p.slide_type == NHW_SLIDE_RIGID_3D)
+          Rhs[ic] = Rhs[ic] + Rho0 * (dsig(Kbeg) + dsig(Kbeg - 1)) *
+                                  (C(ic, 13) * D(i, j) * Delt2H(i, j) + C(ic, 12) * D(i + 1, j) * Delt2H(i + 1, j) +
+                                   C(ic, 11) * D(i, j + 1) * Delt2H(i, j + 1) + C(ic, 14) * D(i - 1, j) * Delt2H(i - 1, j) +
+                                   C(ic, 15) * D(i, j - 1) * Delt2H(i, j - 1));
+        fold(ic, 6, 13); fold(ic, 7, 12); fold(ic, 8, 11); fold(ic, 5, 14); fold(ic, 4, 15);
+        C(ic, 13) = Zero; C(ic, 12) = Zero; C(ic, 11) = Zero; C(ic, 14) = Zero; C(ic, 15) = Zero;
+      }
+    for (int j = Jbeg; j <= Jend; ++j)  // top (Dirichlet)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        int ic = idx(i, j, Kend);
+        C(ic, 4) = Zero; C(ic, 5) = Zero; C(ic, 6) = Zero; C(ic, 7) = Zero; C(ic, 8) = Zero;
+      }
+  }
+
+  // ------------------------------------------- Poisson solve (oracle's own)
+  // stencil offsets of src/pressure.F:276-278 (diagonals 1..15)
+  const int OFF[15][3] = {{0, 0, 0},  {1, 0, 0},  {0, 1, 0},   {0, -1, 1}, {-1, 0, 1},
+                          {0, 0, 1},  {1, 0, 1},  {0, 1, 1},   {-1, 0, 0}, {0, -1, 0},
+                          {0, 1, -1}, {1, 0, -1}, {0, 0, -1},  {-1, 0, -1}, {0, -1, -1}};
+
+  void matvec(const std::vector<double>& xv, std::vector<double>& yv) {
+    const int M = p.Mglob, N = p.Nglob, K = p.Kglob;
+    for (int k = 0; k < K; ++k)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < M; ++i) {
+          int ic = i + M * (j + N * k);
+          double s = 0.0;
+          for (int n = 0; n < 15; ++n) {
+            int ii = i + OFF[n][0], jj = j + OFF[n][1], kk = k + OFF[n][2];
+            if (ii < 0 || ii >= M || jj < 0 || jj >= N || kk < 0 || kk >= K) continue;
+            s += Coef[(size_t)n * neqns + ic] * xv[ii + M * (jj + N * kk)];
+          }
+          yv[ic] = s;
+        }
+  }
+  // vertical-line preconditioner: tridiagonal (Coef 13, 1, 6) per column
+  void precond(const std::vector<double>& r, std::vector<double>& z) {
+    const int M = p.Mglob, N = p.Nglob, K = p.Kglob, MN = M * N;
+    std::vector<double> cp(K), dp(K);
+    for (int c = 0; c < MN; ++c) {
+      for (int k = 0; k < K; ++k) {
+        int ic = c + MN * k;
+        double a = k > 0 ? Coef[(size_t)12 * neqns + ic] : 0.0;
+        double b = Coef[ic];
+        double cc = k < K - 1 ? Coef[(size_t)5 * neqns + ic] : 0.0;
+        double den = b - (k > 0 ? a * cp[k - 1] : 0.0);
+        cp[k] = cc / den;
+        dp[k] = (r[ic] - (k > 0 ? a * dp[k - 1] : 0.0)) / den;
+      }
+      for (int k = K - 1; k >= 0; --k) {
+        int ic = c + MN * k;
+        z[ic] = dp[k] - (k < K - 1 ? cp[k] * z[ic + MN] : 0.0);
+      }
+    }
+  }
+  static double dot(const std::vector<double>& a, const std::vector<double>& b) {
+    double s = 0.0;
+    for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+    return s;
+  }
+
+  // restarted GMRES(m), right preconditioned; returns status
+  int solve(std::vector<double>& xsol) {
+    const int n = neqns, m = 40;
+    const double bnorm = std::sqrt(dot(Rhs, Rhs));
+    last_iters = 0;
+    if (bnorm == 0.0) { std::fill(xsol.begin(), xsol.end(), 0.0); last_relres = 0.0; return NHW_OK; }
+    std::vector<double> r(n), w(n), z(n);
+    std::vector<std::vector<double>> Vb(m + 1, std::vector<double>(n)), Zb(m, std::vector<double>(n));
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
+    int it = 0;
+    double relres = 0.0;
+    while (true) {
+      matvec(xsol, w);
+      for (int i = 0; i < n; ++i) r[i] = Rhs[i] - w[i];
+      double beta = std::sqrt(dot(r, r));
+      relres = beta / bnorm;
+      if (!(relres == relres)) { last_relres = relres; return NHW_ERR_NAN; }
+      if (relres <= p.tol || it >= p.itmax) break;
+      for (int i = 0; i < n; ++i) Vb[0][i] = r[i] / beta;
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0] = beta;
+      int j = 0;
+      for (; j < m && it < p.itmax; ++j) {
+        ++it;
+        precond(Vb[j], Zb[j]);
+        matvec(Zb[j], w);
+        for (int i2 = 0; i2 <= j; ++i2) {
+          double h = dot(w, Vb[i2]);
+          H[(size_t)i2 * m + j] = h;
+          for (int q = 0; q < n; ++q) w[q] -= h * Vb[i2][q];
+        }
+        double hn = std::sqrt(dot(w, w));
+        H[(size_t)(j + 1) * m + j] = hn;
+        if (hn != 0.0)
+          for (int q = 0; q < n; ++q) Vb[j + 1][q] = w[q] / hn;
+        for (int i2 = 0; i2 < j; ++i2) {
+          double a = H[(size_t)i2 * m + j], b = H[(size_t)(i2 + 1) * m + j];
+          H[(size_t)i2 * m + j] = cs[i2] * a + sn[i2] * b;
+          H[(size_t)(i2 + 1) * m + j] = -sn[i2] * a + cs[i2] * b;
+        }
+        double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+        double den = std::sqrt(a * a + b * b);
+        cs[j] = den == 0.0 ? 1.0 : a / den;
+        sn[j] = den == 0.0 ? 0.0 : b / den;
+        H[(size_t)j * m + j] = den;
+        H[(size_t)(j + 1) * m + j] = 0.0;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        if (std::fabs(g[j + 1]) / bnorm <= p.tol * 0.5 || hn == 0.0) { ++j; break; }
+      }
+      // back-substitution and update x += Z y
+      std::vector<double> yv(j, 0.0);
+      for (int i2 = j - 1; i2 >= 0; --i2) {
+        double s = g[i2];
+        for (int q = i2 + 1; q < j; ++q) s -= H[(size_t)i2 * m + q] * yv[q];
+        yv[i2] = s / H[(size_t)i2 * m + i2];
+      }
+      for (int i2 = 0; i2 < j; ++i2)
+        for (int q = 0; q < n; ++q) xsol[q] += yv[i2] * Zb[i2][q];
+    }
+    last_iters = it;
+    last_relres = relres;
+    total_iters += it;
+    ++solves;
+    return relres <= p.tol ? NHW_OK : NHW_ERR_KRYLOV_NOCONV;
+  }
+
+  int poisson_solver() {
+    generate_coef_rhs();
+    std::vector<double> Phi(neqns);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) Phi[idx(i, j, k)] = P(i, j, k);
+    int st = solve(Phi);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) P(i, j, k) = Phi[idx(i, j, k)];
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = 1; i <= Nghost; ++i) {
+          P(Ibeg - i, j, k) = P(Ibeg + i - 1, j, k);
+          P(Iend + i, j, k) = P(Iend - i + 1, j, k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int j = 1; j <= Nghost; ++j) {
+          P(i, Jbeg - j, k) = P(i, Jbeg + j - 1, k);
+          P(i, Jend + j, k) = P(i, Jend - j + 1, k);
+        }
+    return st;
+  }
+
+  void projection_corrector() {
+    A3 DelxP, DelyP, DelzP;
+    for (A3* a : {&DelxP, &DelyP, &DelzP}) a->init(Mloc, Nloc, Kloc);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          DelxP(i, j, k) = 0.5 * ((P(i + 1, j, k) - P(i - 1, j, k)) / (2. * dx) +
+                                  (P(i + 1, j, k + 1) - P(i - 1, j, k + 1)) / (2. * dx));
+          DelyP(i, j, k) = 0.5 * ((P(i, j + 1, k) - P(i, j - 1, k)) / (2. * dy) +
+                                  (P(i, j + 1, k + 1) - P(i, j - 1, k + 1)) / (2. * dy));
+          DelzP(i, j, k) = (P(i, j, k + 1) - P(i, j, k)) / dsig(k);
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 0) continue;
+          DU(i, j, k) = DU(i, j, k) - D(i, j) * dt / Rho0 * (DelxP(i, j, k) + DelzP(i, j, k) * DelxSc(i, j, k));
+          DV(i, j, k) = DV(i, j, k) - D(i, j) * dt / Rho0 * (DelyP(i, j, k) + DelzP(i, j, k) * DelySc(i, j, k));
+          DW(i, j, k) = DW(i, j, k) - dt / Rho0 * DelzP(i, j, k);
+        }
+  }
+
+  // ------------------------------------------------------------ get_Omega
+  void get_Omega() {
+    delxFun_2D(Eta, DelxEta); delyFun_2D(Eta, DelyEta);
+    delxFun_3D(U, DelxU); delxFun_3D(V, DelxV); delyFun_3D(U, DelyU); delyFun_3D(V, DelyV);
+    delxFun_3D(DU, DelxDU); delxFun_3D(DV, DelxDV); delyFun_3D(DU, DelyDU); delyFun_3D(DV, DelyDV);
+    construct_2D_x(Eta, DelxEta, EtaxL, EtaxR); construct_2D_y(Eta, DelyEta, EtayL, EtayR);
+    construct_3D_x(U, DelxU, UxL, UxR); construct_3D_x(V, DelxV, VxL, VxR);
+    construct_3D_y(U, DelyU, UyL, UyR); construct_3D_y(V, DelyV, VyL, VyR);
+    construct_3D_x(DU, DelxDU, DUxL, DUxR); construct_3D_x(DV, DelxDV, DVxL, DVxR);
+    construct_3D_y(DU, DelyDU, DUyL, DUyR); construct_3D_y(DV, DelyDV, DVyL, DVyR);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend1; ++i) { DxL(i, j) = EtaxL(i, j) + Hfx(i, j); DxR(i, j) = EtaxR(i, j) + Hfx(i, j); }
+    for (double& v : DxL.v) v = dmax(v, MinDep);
+    for (double& v : DxR.v) v = dmax(v, MinDep);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 1 && Mask(i + 1, j) == 0) {
+            EtaxL(i + 1, j) = Eta(i, j); DxL(i + 1, j) = D(i, j); DUxL(i + 1, j, k) = Zero;
+          } else if (Mask(i, j) == 1 && Mask(i - 1, j) == 0) {
+            EtaxR(i, j) = Eta(i, j); DxR(i, j) = D(i, j); DUxR(i, j, k) = Zero;
+          } else if (Mask(i, j) == 0) {
+            EtaxL(i + 1, j) = Eta(i, j); DxL(i + 1, j) = D(i, j); DUxL(i + 1, j, k) = Zero; DVxL(i + 1, j, k) = Zero;
+            EtaxR(i, j) = Eta(i, j); DxR(i, j) = D(i, j); DUxR(i, j, k) = Zero;
+          }
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend1; ++i) { ExL(i, j, k) = DUxL(i, j, k); ExR(i, j, k) = DUxR(i, j, k); }
+    for (int j = Jbeg; j <= Jend1; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) { DyL(i, j) = EtayL(i, j) + Hfy(i, j); DyR(i, j) = EtayR(i, j) + Hfy(i, j); }
+    for (double& v : DyL.v) v = dmax(v, MinDep);
+    for (double& v : DyR.v) v = dmax(v, MinDep);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 1 && Mask(i, j + 1) == 0) {
+            EtayL(i, j + 1) = Eta(i, j); DyL(i, j + 1) = D(i, j); DVyL(i, j + 1, k) = Zero;
+          } else if (Mask(i, j) == 1 && Mask(i, j - 1) == 0) {
+            EtayR(i, j) = Eta(i, j); DyR(i, j) = D(i, j); DVyR(i, j, k) = Zero;
+          } else if (Mask(i, j) == 0) {
+            EtayL(i, j + 1) = Eta(i, j); DyL(i, j + 1) = D(i, j); DVyL(i, j + 1, k) = Zero;
+            EtayR(i, j) = Eta(i, j); DyR(i, j) = D(i, j); DVyR(i, j, k) = Zero;
+          }
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend1; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) { EyL(i, j, k) = DVyL(i, j, k); EyR(i, j, k) = DVyR(i, j, k); }
+    wave_speed();
+    HLL(SxL, SxR, ExL, ExR, nullptr, nullptr, &DxL, &DxR, Ex);
+    HLL(SyL, SyR, EyL, EyR, nullptr, nullptr, &DyL, &DyR, Ey);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) { Ex(Ibeg, j, k) = Zero; Ex(Iend1, j, k) = Zero; }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k) { Ey(i, Jbeg, k) = Zero; Ey(i, Jend1, k) = Zero; }
+    Omega.fill(0.0);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg + 1; k <= Kend1; ++k) {
+          Omega(i, j, k) = Omega(i, j, k - 1) - dsig(k - 1) * (R1s(i, j) + (Ex(i + 1, j, k - 1) - Ex(i, j, k - 1)) / dx +
+                                                              (Ey(i, j + 1, k - 1) - Ey(i, j, k - 1)) / dy);
+          if (Mask(i, j) == 0) Omega(i, j, k) = Zero;
+        }
+  }
+
+  // ------------------------------------------------------------ eval_duvw
+  int eval_duvw(int ISTEP) {
+    const double al = ALPHA[ISTEP - 1], be = BETA[ISTEP - 1];
+    int st = NHW_OK;
+    R1s.fill(0.0);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        if (Mask(i, j) == 0) continue;
+        for (int k = Kbeg; k <= Kend; ++k)
+          R1s(i, j) = R1s(i, j) - 1.0 / dx * (Ex(i + 1, j, k) - Ex(i, j, k)) * dsig(k) -
+                      1.0 / dy * (Ey(i, j + 1, k) - Ey(i, j, k)) * dsig(k);
+        R1s(i, j) = R1s(i, j) + D(i, j) * SourceC(i, j);
+        D(i, j) = al * D0(i, j) + be * (D(i, j) + dt * R1s(i, j));
+      }
+    for (double& v : D.v) v = dmax(v, MinDep);
+    wl_bc();
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i) Eta(i, j) = D(i, j) - Hc(i, j);
+    delxFun_2D(Eta, DelxEta);
+    delyFun_2D(Eta, DelyEta);
+    sigma_transform();
+    A3 R2, R3, R4;
+    R2.init(Mloc, Nloc, Kloc); R3.init(Mloc, Nloc, Kloc); R4.init(Mloc, Nloc, Kloc);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (Mask(i, j) == 0) continue;
+        for (int k = Kbeg; k <= Kend; ++k) {
+          R2(i, j, k) = -1.0 / dx * (Fx(i + 1, j, k) - Fx(i, j, k)) - 1.0 / dy * (Fy(i, j + 1, k) - Fy(i, j, k)) -
+                        1.0 / dsig(k) * (Fz(i, j, k + 1) - Fz(i, j, k)) + fcor * DV(i, j, k) + SourceX(i, j);
+          R3(i, j, k) = -1.0 / dx * (Gx(i + 1, j, k) - Gx(i, j, k)) - 1.0 / dy * (Gy(i, j + 1, k) - Gy(i, j, k)) -
+                        1.0 / dsig(k) * (Gz(i, j, k + 1) - Gz(i, j, k)) - fcor * DU(i, j, k) + SourceY(i, j);
+          R4(i, j, k) = -1.0 / dx * (Hx(i + 1, j, k) - Hx(i, j, k)) - 1.0 / dy * (Hy(i, j + 1, k) - Hy(i, j, k)) -
+                        1.0 / dsig(k) * (Hz(i, j, k + 1) - Hz(i, j, k));
+        }
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (Mask(i, j) == 0) continue;
+        for (int k = Kbeg; k <= Kend; ++k) DU(i, j, k) = DU(i, j, k) + dt * R2(i, j, k);
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (Mask(i, j) == 0) continue;
+        for (int k = Kbeg; k <= Kend; ++k) DV(i, j, k) = DV(i, j, k) + dt * R3(i, j, k);
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (Mask(i, j) == 0) continue;
+        for (int k = Kbeg; k <= Kend; ++k) DW(i, j, k) = DW(i, j, k) + dt * R4(i, j, k);
+      }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (Mask(i, j) == 0) { DU(i, j, k) = Zero; DV(i, j, k) = Zero; DW(i, j, k) = Zero; }
+    if (p.non_hydro) {
+      get_UVW();
+      interpolate_velocity_to_faces();
+      st = poisson_solver();
+      projection_corrector();
+    }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          DU(i, j, k) = al * DU0(i, j, k) + be * DU(i, j, k);
+          DV(i, j, k) = al * DV0(i, j, k) + be * DV(i, j, k);
+          DW(i, j, k) = al * DW0(i, j, k) + be * DW(i, j, k);
+          if (Mask(i, j) == 0) { DU(i, j, k) = Zero; DV(i, j, k) = Zero; DW(i, j, k) = Zero; }
+        }
+    if (p.froude_cap_on)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          double FroudeU = std::sqrt(Grav * D(i, j)) * p.froude_cap * D(i, j);
+          if (Mask(i, j) > 0)
+            for (int k = Kbeg; k <= Kend; ++k) {
+              double DUU = std::sqrt(DU(i, j, k) * DU(i, j, k) + DV(i, j, k) * DV(i, j, k) + DW(i, j, k) * DW(i, j, k));
+              if (DUU > FroudeU) {
+                double Dangle = std::atan2(DV(i, j, k), DU(i, j, k));
+                DU(i, j, k) = FroudeU * std::cos(Dangle);
+                DV(i, j, k) = FroudeU * std::sin(Dangle);
+                DW(i, j, k) = Zero;
+              }
+            }
+        }
+    get_UVW();
+    get_Omega();
+    return st;
+  }
+
+  void sponge_damping() {
+    const double Ramp = p.tramp > 0.0 ? std::tanh(TIME / p.tramp) : 1.0;
+    const double Ucur = Ramp * p.cur_wave;
+    for (int j = 1; j <= Nloc; ++j)
+      for (int i = 1; i <= Mloc; ++i)
+        if (Mask(i, j) == 1) {
+          Eta(i, j) = Eta(i, j) * Sponge(i, j);
+          D(i, j) = Eta(i, j) + Hc(i, j);
+          for (int k = 1; k <= Kloc; ++k) {
+            U(i, j, k) = (U(i, j, k) - Ucur) * Sponge(i, j) + Ucur;
+            V(i, j, k) = V(i, j, k) * Sponge(i, j);
+            DU(i, j, k) = D(i, j) * U(i, j, k);
+            DV(i, j, k) = D(i, j) * V(i, j, k);
+          }
+        }
+  }
+
+  int step() {
+    int st = estimate_dt();
+    if (st) return status = st;
+    if (p.slide_type != NHW_SLIDE_NONE) update_bathymetry();
+    update_mask();
+    update_wind();
+    update_vars();
+    int worst = NHW_OK;
+    for (int s = 1; s <= It_Order; ++s) {
+      source_terms();
+      fluxes();
+      int e = eval_duvw(s);
+      if (e != NHW_OK && worst == NHW_OK) worst = e;
+      if (p.sponge_on) sponge_damping();
+    }
+    if (worst == NHW_ERR_NAN) status = worst;
+    return worst;
+  }
+
+  double mass() {
+    double MassVolume = Zero;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) MassVolume = MassVolume + D(i, j) * dx * dy;
+    return MassVolume;
+  }
+
+  // ------------------------------------------------------- field access
+  struct FieldRef { double* d = nullptr; int32_t* i = nullptr; size_t n = 0; };
+  FieldRef field(int f) {
+    FieldRef r;
+    auto a2 = [&](A2& a) { r.d = a.v.data(); r.n = a.v.size(); };
+    auto a3 = [&](A3& a) { r.d = a.v.data(); r.n = a.v.size(); };
+    auto i2 = [&](I2& a) { r.i = a.v.data(); r.n = a.v.size(); };
+    switch (f) {
+      case NHW_F_D: a2(D); break;            case NHW_F_D0: a2(D0); break;
+      case NHW_F_ETA: a2(Eta); break;        case NHW_F_ETA0: a2(Eta0); break;
+      case NHW_F_HC: a2(Hc); break;          case NHW_F_HC0: a2(Hc0); break;
+      case NHW_F_DELXH: a2(DelxH); break;    case NHW_F_DELYH: a2(DelyH); break;
+      case NHW_F_DELXETA: a2(DelxEta); break; case NHW_F_DELYETA: a2(DelyEta); break;
+      case NHW_F_DELTH: a2(DeltH); break;    case NHW_F_DELT2H: a2(Delt2H); break;
+      case NHW_F_SOURCEX: a2(SourceX); break; case NHW_F_SOURCEY: a2(SourceY); break;
+      case NHW_F_SOURCEC: a2(SourceC); break; case NHW_F_SPONGE: a2(Sponge); break;
+      case NHW_F_R1: a2(R1s); break;
+      case NHW_F_HFX: a2(Hfx); break;        case NHW_F_HFX0: a2(Hfx0); break;
+      case NHW_F_ETAXL: a2(EtaxL); break;    case NHW_F_ETAXR: a2(EtaxR); break;
+      case NHW_F_HFY: a2(Hfy); break;        case NHW_F_HFY0: a2(Hfy0); break;
+      case NHW_F_ETAYL: a2(EtayL); break;    case NHW_F_ETAYR: a2(EtayR); break;
+      case NHW_F_MASK: i2(Mask); break;      case NHW_F_MASK_STRUCT: i2(Mask_Struct); break;
+      case NHW_F_MASK9: i2(Mask9); break;
+      case NHW_F_U: a3(U); break; case NHW_F_V: a3(V); break; case NHW_F_W: a3(W); break;
+      case NHW_F_DU: a3(DU); break; case NHW_F_DV: a3(DV); break; case NHW_F_DW: a3(DW); break;
+      case NHW_F_DU0: a3(DU0); break; case NHW_F_DV0: a3(DV0); break; case NHW_F_DW0: a3(DW0); break;
+      case NHW_F_P: a3(P); break; case NHW_F_OMEGA: a3(Omega); break;
+      case NHW_F_EX: a3(Ex); break; case NHW_F_FX: a3(Fx); break; case NHW_F_GX: a3(Gx); break;
+      case NHW_F_HX: a3(Hx); break; case NHW_F_EY: a3(Ey); break; case NHW_F_FY: a3(Fy); break;
+      case NHW_F_GY: a3(Gy); break; case NHW_F_HY: a3(Hy); break; case NHW_F_FZ: a3(Fz); break;
+      case NHW_F_GZ: a3(Gz); break; case NHW_F_HZ: a3(Hz); break;
+      default: break;
+    }
+    return r;
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+void* orc_create(const nhw_params* p, int* status) {
+  Model* m = new Model();
+  int st = p ? m->create(*p) : NHW_ERR_ARG;
+  if (status) *status = st;
+  if (st != NHW_OK) { delete m; return nullptr; }
+  return m;
+}
+void orc_destroy(void* o) { delete static_cast<Model*>(o); }
+int orc_setup(void* o, const double* depth, const double* eta0, const double* uvw0) {
+  Model* m = static_cast<Model*>(o);
+  if (!m || !depth) return NHW_ERR_ARG;
+  m->generate_grid();
+  m->read_bathymetry(depth);
+  m->initial(eta0, uvw0);
+  return NHW_OK;
+}
+int orc_estimate_dt(void* o) { return static_cast<Model*>(o)->estimate_dt(); }
+void orc_update_bathymetry(void* o) { static_cast<Model*>(o)->update_bathymetry(); }
+void orc_update_mask(void* o) { static_cast<Model*>(o)->update_mask(); }
+void orc_update_vars(void* o) { Model* m = static_cast<Model*>(o); m->update_wind(); m->update_vars(); }
+void orc_source_terms(void* o) { static_cast<Model*>(o)->source_terms(); }
+void orc_fluxes(void* o) { static_cast<Model*>(o)->fluxes(); }
+int orc_eval_duvw(void* o, int istep) { return static_cast<Model*>(o)->eval_duvw(istep); }
+void orc_sponge_damping(void* o) { static_cast<Model*>(o)->sponge_damping(); }
+int orc_step(void* o) { return static_cast<Model*>(o)->step(); }
+double orc_mass(void* o) { return static_cast<Model*>(o)->mass(); }
+int orc_get_field(void* o, int f, void* out) {
+  auto r = static_cast<Model*>(o)->field(f);
+  if (!out || r.n == 0) return NHW_ERR_ARG;
+  if (r.d) std::memcpy(out, r.d, r.n * sizeof(double));
+  else std::memcpy(out, r.i, r.n * sizeof(int32_t));
+  return NHW_OK;
+}
+int orc_set_field(void* o, int f, const void* in) {
+  auto r = static_cast<Model*>(o)->field(f);
+  if (!in || r.n == 0) return NHW_ERR_ARG;
+  if (r.d) std::memcpy(r.d, in, r.n * sizeof(double));
+  else std::memcpy(r.i, in, r.n * sizeof(int32_t));
+  return NHW_OK;
+}
+void orc_get_scalars(void* o, nhw_scalars* s) {
+  Model* m = static_cast<Model*>(o);
+  std::memset(s, 0, sizeof(*s));
+  s->time = m->TIME; s->dt = m->dt; s->dt_old = m->dt_old; s->run_step = m->RUN_STEP;
+  s->last_krylov_iters = m->last_iters; s->total_krylov_iters = m->total_iters;
+  s->poisson_solves = m->solves; s->last_rel_residual = m->last_relres; s->status = m->status;
+}
+void orc_set_time(void* o, double time, double dt, int run_step) {
+  Model* m = static_cast<Model*>(o);
+  m->TIME = time; m->dt = dt; m->RUN_STEP = run_step;
+}
+// grid vectors for tests: which = 0 x, 1 xc, 2 y, 3 yc, 4 sig, 5 dsig, 6 sigc
+int orc_get_grid(void* o, int which, double* out) {
+  Model* m = static_cast<Model*>(o);
+  A1* a[] = {&m->x, &m->xc, &m->y, &m->yc, &m->sig, &m->dsig, &m->sigc};
+  if (which < 0 || which > 6 || !out) return NHW_ERR_ARG;
+  std::memcpy(out, a[which]->v.data(), a[which]->v.size() * sizeof(double));
+  return (int)a[which]->v.size();
+}
+// Poisson operator access for tests: coefficient n (1..15) and Rhs
+int orc_get_coef(void* o, double* coef15, double* rhs) {
+  Model* m = static_cast<Model*>(o);
+  if (coef15) std::memcpy(coef15, m->Coef.data(), m->Coef.size() * sizeof(double));
+  if (rhs) std::memcpy(rhs, m->Rhs.data(), m->Rhs.size() * sizeof(double));
+  return m->neqns;
+}
+void orc_generate_coef_rhs(void* o) { static_cast<Model*>(o)->generate_coef_rhs(); }
+double orc_limiter(double a, double b) { return LIMITER(a, b); }
+double orc_wave_number(void* o, double segma) { return static_cast<Model*>(o)->wave_dispersion(segma); }
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+"""The C-ABI library on a machine without a GPU: it loads, exports every entry
+point declared in include/*.h, agrees with the ctypes struct images, and
+rejects out-of-scope parameters on the host before touching the device."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import REPO
+
+
+def _declared():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"\b(nhw_[a-z0-9_]+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    declared = _declared()
+    assert len(declared) >= 20
+    missing = [n for n in declared if not hasattr(gpu_lib, n)]
+    assert not missing, missing
+    from nhwave_gb300 import lib
+    assert sorted(lib.EXPORTS) == declared
+
+
+def test_abi_sizes_match_ctypes(gpu_lib):
+    from nhwave_gb300.params import NhwParams, NhwScalars
+    a, b = ctypes.c_int32(), ctypes.c_int32()
+    assert gpu_lib.nhw_abi_sizes(ctypes.byref(a), ctypes.byref(b)) == 0
+    assert a.value == ctypes.sizeof(NhwParams)
+    assert b.value == ctypes.sizeof(NhwScalars)
+
+
+def test_status_strings(gpu_lib):
+    from nhwave_gb300 import lib
+    assert lib.status_string(0) == "ok"
+    assert "DT_MIN" in lib.status_string(lib.ERR_DT_MIN)
+
+
+@pytest.mark.parametrize("field,value", [("hllc", 1), ("viscous_flow", 1), ("barotropic", 0),
+                                         ("bc_x0", 3), ("bc_yn", 6), ("bc_z0", 2), ("Kglob", 65)])
+def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
+    from nhwave_gb300 import default_params, lib
+    p = default_params(**{field: value})
+    h = ctypes.c_void_p()
+    st = gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h))
+    assert st == lib.ERR_UNSUPPORTED and not h.value
+
+
+@pytest.mark.parametrize("field,value", [("Mglob", 0), ("dx", 0.0), ("precision", 7), ("time_order", 4)])
+def test_bad_arguments_rejected(field, value, gpu_lib):
+    from nhwave_gb300 import default_params, lib
+    p = default_params(**{field: value})
+    h = ctypes.c_void_p()
+    assert gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h)) == lib.ERR_ARG
+
+
+def test_null_arguments(gpu_lib):
+    from nhwave_gb300 import lib
+    assert gpu_lib.nhw_create(None, None) == lib.ERR_ARG
+    assert gpu_lib.nhw_step(None, None, None, None) == lib.ERR_ARG
+    assert gpu_lib.nhw_destroy(None) == lib.ERR_ARG

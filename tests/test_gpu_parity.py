@@ -1,0 +1,166 @@
+"""GPU parity: the C-ABI library against the CPU oracle on the same seeded inputs.
+
+Bars (FP64 form): masks bit-exact; set-up and the explicit routines bit-exact
+(the FP64 kernels are built without FMA contraction and follow the reference's
+evaluation order); after full steps, whose Poisson solves differ only by the
+solver's stopping point, eta/U/V/W/P within 1e-10 relative L2 with TOL=1e-12.
+FP32+IR form: eta within 1e-6 relative L2 of the FP64 oracle, masks bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
+STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
+STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
+
+
+def vel_err(g, o, name):
+    """Error of one velocity component relative to the whole velocity field
+    (a component that is zero up to roundoff has no relative error of its own)."""
+    from nhwave_gb300 import fields as F
+    fid = getattr(F, name)
+    sl = o.shape.interior(fid)
+    ref = np.sqrt(sum(np.linalg.norm(o.get(getattr(F, c))[sl]) ** 2 for c in ("U", "V", "W")))
+    return np.linalg.norm(g.get(fid)[sl] - o.get(fid)[sl]) / ref
+
+
+def _pair(name, oracle_mod, precision=0, tol=1e-14, seed=7, **kw):
+    from nhwave_gb300 import lib, scenarios as S
+    p, d, e, u = S.make(name, precision=precision, seed=seed, **kw)
+    p.tol = tol
+    p.itmax = 5000
+    g = lib.Scenario(p, d, e, u)
+    q = p.copy()
+    q.precision = 0
+    o = oracle_mod.Oracle(q, d, e, u)
+    return g, o
+
+
+def _cmp_exact(g, o, names, where):
+    from nhwave_gb300 import fields as F
+    for n in names:
+        fid = getattr(F, n)
+        a, b = g.get(fid), o.get(fid)
+        sl = o.shape.interior(fid) if n in ("HFX0", "HFY0", "DELXH", "DELYH") else Ellipsis
+        bad = np.argwhere(a[sl] != b[sl])
+        assert bad.size == 0, f"{where}: {n} differs at {bad[:5].tolist()} (max |d| {np.abs(a[sl]-b[sl]).max():.3e})"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_setup_bit_exact(name, oracle_mod, gpu_lib):
+    g, o = _pair(name, oracle_mod)
+    _cmp_exact(g, o, ["MASK", "MASK_STRUCT", "MASK9"] + STATE2D + ["SPONGE"] + STATE3D, "setup")
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_explicit_routines_bit_exact(name, oracle_mod, gpu_lib):
+    """estimate_dt .. fluxes, and a hydrostatic eval_duvw, match operation for operation."""
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod, non_hydro=0)
+    for rnd in range(2):
+        for obj in (g, o):
+            assert obj.estimate_dt() == 0
+            if obj.params.slide_type:
+                obj.update_bathymetry()
+            obj.update_mask()
+            obj.update_vars()
+        sg, so = g.scalars(), o.scalars()
+        assert sg.dt == so.dt and sg.time == so.time and sg.run_step == so.run_step
+        if g.params.slide_type:
+            # the slide shape uses cosh/log: CUDA's and the host libm's may differ
+            # in the last bit, so compare with a tolerance and pin the inputs
+            for n in ("HC", "HFX", "HFY", "HFX0", "HFY0", "DELXH", "DELYH", "DELTH", "DELT2H"):
+                fid = getattr(F, n)
+                sl = o.shape.interior(fid)
+                # DeltH = (Hc - Ho)/dt amplifies last-bit differences of Hc
+                lim = 1e-8 if n in ("DELTH", "DELT2H") else 1e-13
+                r = rel_l2(g.get(fid)[sl], o.get(fid)[sl])
+                assert r < lim, f"{n} after update_bathymetry: {r:.3e}"
+                g.set(fid, o.get(fid))
+        _cmp_exact(g, o, ["MASK", "MASK9", "D", "ETA", "HC", "DELXH", "DELYH"], f"prologue {rnd}")
+        for s in range(1, 4):
+            g.source_terms(); o.source_terms()
+            _cmp_exact(g, o, ["SOURCEX", "SOURCEY"], f"source_terms {rnd}.{s}")
+            sc = rel_l2(g.get(F.SOURCEC), o.get(F.SOURCEC))
+            assert sc < 1e-14, f"SourceC rel {sc}"
+            g.set(F.SOURCEC, o.get(F.SOURCEC))  # cos() of CUDA vs libm: pin the input
+            g.fluxes(); o.fluxes()
+            sl = o.shape.interior
+            for n in ("EX", "FX", "GX", "HX", "EY", "FY", "GY", "HY", "FZ", "GZ", "HZ"):
+                fid = getattr(F, n)
+                a, b = g.get(fid)[sl(fid)], o.get(fid)[sl(fid)]
+                assert np.array_equal(a, b), f"fluxes {rnd}.{s}: {n} max |d| {np.abs(a-b).max():.3e}"
+            g.eval_duvw(s); o.eval_duvw(s)
+            _cmp_exact(g, o, ["D", "ETA", "MASK", "R1", "DELXETA", "DELYETA"] + STATE3D, f"eval_duvw {rnd}.{s}")
+            a, b = g.get(F.OMEGA), o.get(F.OMEGA)
+            assert np.array_equal(a, b), f"omega max |d| {np.abs(a-b).max():.3e}"
+            if g.params.sponge_on:
+                g.sponge_damping(); o.sponge_damping()
+                _cmp_exact(g, o, ["D", "ETA"] + STATE3D, f"sponge {rnd}.{s}")
+    g.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_steps_fp64(name, oracle_mod, gpu_lib):
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod)
+    for n in range(6):
+        assert g.step() == 0
+        assert o.step() == 0
+        assert np.array_equal(g.get(F.MASK), o.get(F.MASK)), f"mask differs after step {n}"
+    sl = o.shape.interior
+    for f in ("ETA", "P"):
+        fid = getattr(F, f)
+        r = rel_l2(g.get(fid)[sl(fid)], o.get(fid)[sl(fid)])
+        assert r < 1e-10, f"{name} {f}: rel L2 {r:.3e}"
+    for f in ("U", "V", "W"):
+        r = vel_err(g, o, f)
+        assert r < 1e-10, f"{name} {f}: rel L2 {r:.3e}"
+    sg, so = g.scalars(), o.scalars()
+    assert abs(sg.time - so.time) <= 1e-12 * so.time
+    assert sg.last_rel_residual <= 1e-14
+    g.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_steps_fp32_ir(name, oracle_mod, gpu_lib):
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod, precision=1, tol=1e-10)
+    eta0 = o.get(F.ETA)[o.shape.interior(F.ETA)].copy()
+    for n in range(6):
+        assert g.step() == 0
+        assert o.step() == 0
+    sl = o.shape.interior
+    assert np.array_equal(g.get(F.MASK), o.get(F.MASK))
+    r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
+    assert r < 1e-6, f"{name} eta rel L2 {r:.3e} (|eta| {np.abs(eta0).max():.3e})"
+    assert g.scalars().last_rel_residual <= 1e-10
+    g.close()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_fixtures(name, gpu_lib):
+    import os
+    from nhwave_gb300 import fields as F, lib, scenarios as S
+    from test_oracle import GOLDEN, golden_path
+    steps = GOLDEN[name]
+    ref = np.load(golden_path(name, steps))
+    p, d, e, u = S.make(name, seed=7)
+    p.tol = 1e-14
+    p.itmax = 5000
+    g = lib.Scenario(p, d, e, u)
+    for _ in range(steps):
+        assert g.step() == 0
+    vref = np.sqrt(sum(np.linalg.norm(ref[c]) ** 2 for c in ("U", "V", "W")))
+    for f in ("ETA", "D", "U", "V", "W", "P", "OMEGA"):
+        fid = getattr(F, f)
+        a = g.get(fid)[g.shape.interior(fid)]
+        den = vref if f in ("U", "V", "W") else np.linalg.norm(ref[f])
+        r = np.linalg.norm(a - ref[f]) / den
+        assert r < 1e-10, f"{name} {f}: rel L2 {r:.3e}"
+    assert np.array_equal(g.get(F.MASK)[g.shape.interior(F.MASK)], ref["MASK"])
+    g.close()

@@ -1,0 +1,137 @@
+"""The CPU oracle against known answers and its committed golden fixtures.
+
+No golden outputs exist for the reference (it ships no tests and no model
+outputs) and it cannot be compiled here (no Fortran compiler), so the oracle
+is pinned by known-answer tests that follow from the reference's algorithm:
+the van Leer limiter, linear dispersion, the Poisson coefficients of a flat
+bed, a lake at rest staying at rest (well-balanced bed-slope source,
+src/source_terms.F:447-453), mass growing by exactly (ALPHA(3)+BETA(3)) per
+SSP-RK3 step (1/3 and 2/3 are default-real literals, src/initialize.F:3386-3391),
+and mirror symmetry.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = {"tiny_c1": 6, "tiny_c2": 6, "tiny_c3": 6, "tiny_c4": 4}
+
+
+def golden_path(name, steps):
+    return os.path.join(HERE, "golden", f"{name}_{steps}steps.npz")
+
+
+def test_limiter_known_values(oracle_mod):
+    L = oracle_mod.limiter
+    assert L(1.0, 1.0) == 1.0
+    assert L(1.0, -1.0) == 0.0
+    assert L(2.0, 1.0) == pytest.approx(4.0 / 3.0, rel=1e-15)   # 2ab/(a+b)
+    assert L(-3.0, -1.0) == pytest.approx(-1.5, rel=1e-15)
+
+
+def test_wave_dispersion(oracle_mod):
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_c2")
+    o = oracle_mod.Oracle(p, d, e, u)
+    sigma = 2.0 * math.pi / 2.02
+    k = o.params and oracle_mod.lib().orc_wave_number(o._h, sigma)
+    g = float(np.float32(9.81))
+    assert sigma ** 2 == pytest.approx(g * k * math.tanh(k * 0.4), rel=1e-7)
+
+
+def test_flat_bed_poisson_coefficients(oracle_mod):
+    from nhwave_gb300 import default_params
+    M, N, K = 4, 3, 3
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.25, tol=1e-12)
+    depth = np.full(M * N, 2.0)
+    o = oracle_mod.Oracle(p, depth)
+    oracle_mod.lib().orc_generate_coef_rhs(o._h)
+    coef, rhs = o.coef_rhs()
+    ds = float(np.float32(1.0) / np.float32(K))
+    a1 = 1.0 / 4.0                       # DelzS^2 with D = 2, flat bed, eta = 0
+    ic = 1 + M * (1 + N * 1)             # interior point, away from every boundary
+    assert coef[0, ic] == pytest.approx(2 / 0.25 + 2 / 0.0625 + 2 * a1 / ds ** 2, rel=1e-14)
+    assert coef[5, ic] == pytest.approx(-a1 / ds ** 2, rel=1e-14)
+    assert coef[12, ic] == pytest.approx(-a1 / ds ** 2, rel=1e-14)
+    assert coef[1, ic] == coef[8, ic] == -1 / 0.25
+    assert np.all(coef[[3, 4, 6, 7, 10, 11, 13, 14], ic] == 0.0)  # no slope terms on a flat bed
+    assert np.all(rhs == 0.0)                                        # fluid at rest
+    top = 1 + M * (1 + N * (K - 1))
+    assert np.all(coef[[3, 4, 5, 6, 7], top] == 0.0)                 # Dirichlet P = 0 above
+
+
+def test_lake_at_rest(oracle_mod):
+    """A lake at rest stays at rest but for the SSP-RK3 coefficient sum: each step
+    scales D by ALPHA(3)+BETA(3) = 1 + 2.98e-8, lifting eta by Hc*(g^n - 1)."""
+    from nhwave_gb300 import default_params, fields as F
+    rng = np.random.default_rng(3)
+    M, N, K = 24, 10, 4
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=1.0, dy=1.0, tol=1e-12, dt_ini=0.05)
+    depth = 5.0 + rng.uniform(0.0, 2.0, size=M * N)
+    o = oracle_mod.Oracle(p, depth)
+    n = 4
+    for _ in range(n):
+        assert o.step() == 0
+    sl = o.shape.interior
+    g = float(np.float32(1.0) / np.float32(3.0)) + float(np.float32(2.0) / np.float32(3.0))
+    hc = depth.reshape(N, M)
+    eta = o.get(F.ETA)[sl(F.ETA)]
+    lift = hc * (g ** n - 1.0)
+    # the non-uniform lift itself drives a flow of the same tiny order
+    assert np.abs(eta - lift).max() < 0.2 * lift.max()
+    assert np.abs(o.get(F.U)[sl(F.U)]).max() < 1e-6
+
+
+def test_mass_grows_by_rk_coefficient_sum(oracle_mod):
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_c1")
+    p.tol = 1e-12
+    o = oracle_mod.Oracle(p, d, e, u)
+    m0 = o.mass()
+    n = 5
+    for _ in range(n):
+        assert o.step() == 0
+    growth = float(np.float32(1.0) / np.float32(3.0)) + float(np.float32(2.0) / np.float32(3.0))
+    assert o.mass() / m0 == pytest.approx(growth ** n, abs=1e-13)
+
+
+def test_mirror_symmetry(oracle_mod):
+    from nhwave_gb300 import default_params, fields as F
+    M, N, K = 30, 6, 4
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.5, tol=1e-13, dt_ini=0.01)
+    x = (np.arange(M) + 0.5) * 0.5
+    eta = 0.05 * np.exp(-((x - 7.5) / 2.0) ** 2)
+    o = oracle_mod.Oracle(p, np.full(M * N, 2.0), np.tile(eta, N))
+    for _ in range(4):
+        assert o.step() == 0
+    e2 = o.get(F.ETA)[o.shape.interior(F.ETA)]
+    assert np.abs(e2 - e2[:, ::-1]).max() < 1e-12 * np.abs(e2).max()
+
+
+@pytest.mark.parametrize("name", list(GOLDEN))
+def test_oracle_reproduces_golden(name, oracle_mod):
+    from nhwave_gb300 import fields as F, scenarios as S
+    steps = GOLDEN[name]
+    ref = np.load(golden_path(name, steps))
+    p, d, e, u = S.make(name, seed=7)
+    p.tol = 1e-14
+    p.itmax = 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    for _ in range(steps):
+        assert o.step() == 0
+    for f in ("ETA", "D", "U", "V", "W", "P", "OMEGA"):
+        fid = getattr(F, f)
+        assert rel_l2(o.get(fid)[o.shape.interior(fid)], ref[f]) < 1e-12, f
+    assert np.array_equal(o.get(F.MASK)[o.shape.interior(F.MASK)], ref["MASK"])
+    s = o.scalars()
+    assert s.time == pytest.approx(ref["scalars"][0], rel=1e-14)
+
+
+def test_wet_dry_front_exists_in_slide_case(oracle_mod):
+    ref = np.load(golden_path("tiny_c3", GOLDEN["tiny_c3"]))
+    mask = ref["MASK"]
+    assert 0 < (mask == 0).sum() < mask.size

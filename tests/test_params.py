@@ -1,0 +1,77 @@
+"""input.txt reader (src/mod_util.F:8-463 / read_input src/initialize.F:141-1321)."""
+import pytest
+
+SAMPLE = """! INPUT FILE FOR NHWAVE
+TITLE = test
+Mglob = 1024
+Nglob = 64
+Kglob = 20
+DX = 0.025
+DY = 0.05
+IVGRD = 1
+GRD_R = 1.1
+DT_INI = 0.01000
+DT_MIN = 0.00001
+DT_MAX = 60.0000
+SIM_STEPS = 100000000
+TOTAL_TIME = 20.0
+CFL = 0.5
+FROUDE_CAP = 100.0
+NON_HYDRO = T
+MinDep = 1.e-3
+ISOLVER = 2
+ITMAX = 1000
+TOL = 1.e-8
+BC_X0 = 1
+BC_Xn = 1
+BC_Y0 = 1
+BC_Yn = 1
+BC_Z0 = 1
+WAVEMAKER = INT_LIN
+AMP = 0.01
+PER = 2.02
+DEP = 0.4
+THETA = 0.0
+CUR = 0.0
+Xsource_West = 4.0   ! a comment
+Xsource_East = 4.2
+Ysource_Suth = 0.0
+Ysource_Nrth = 3.2
+SPONGE_ON = T
+Sponge_West_Width =  2.0
+Sponge_East_Width =  2.0
+Sponge_South_Width = 0.0
+Sponge_North_Width = 0.0
+TIME_ORDER = THIRD
+HLLC = F
+VISCOUS_FLOW = F
+BAROTROPIC = T
+"""
+
+
+def test_read_input(tmp_path):
+    from nhwave_gb300 import params as P
+    f = tmp_path / "input.txt"
+    f.write_text(SAMPLE)
+    p = P.read_input(str(f))
+    assert (p.Mglob, p.Nglob, p.Kglob) == (1024, 64, 20)
+    assert p.dx == 0.025 and p.dy == 0.05 and p.min_dep == 1e-3 and p.tol == 1e-8
+    assert p.wavemaker == P.WM_INT_LIN and p.per_wave == 2.02 and p.xsource_west == 4.0
+    assert p.sponge_on == 1 and p.sponge_west_width == 2.0 and p.non_hydro == 1
+    assert p.time_order == 3 and p.total_time == 20.0
+    assert P.unsupported_reason(p) is None
+
+
+def test_missing_key_halts(tmp_path):
+    from nhwave_gb300 import params as P
+    f = tmp_path / "input.txt"
+    f.write_text(SAMPLE.replace("DX = 0.025\n", ""))
+    with pytest.raises(ValueError, match="DX"):
+        P.read_input(str(f))
+
+
+def test_out_of_scope_reason(tmp_path):
+    from nhwave_gb300 import params as P
+    f = tmp_path / "input.txt"
+    f.write_text(SAMPLE.replace("HLLC = F", "HLLC = T"))
+    assert "HLLC" in P.unsupported_reason(P.read_input(str(f)))
