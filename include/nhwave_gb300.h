@@ -105,7 +105,8 @@ typedef struct nhw_params {
   double  slide_t, slide_l, slide_w, slide_angle, slope_angle, slide_x0, slide_y0;
   double  slide_ut, slide_a0;              /* SlideUt SlideA0                         */
   int32_t precision;                       /* enum nhw_precision                      */
-  int32_t reserved[8];
+  int32_t device;                          /* CUDA device ordinal of the handle       */
+  int32_t reserved[7];
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */
@@ -196,6 +197,19 @@ int nhw_mass(nhw_handle* h, double* mass);
 
 /* Wait for the handle's stream. */
 int nhw_synchronize(nhw_handle* h);
+
+/* Run nsteps full steps (no TOTAL_TIME / SIM_STEPS test) and report the
+ * device time of the whole sequence, from CUDA events recorded on the
+ * handle's stream before the first and after the last kernel. */
+int nhw_run_timed(nhw_handle* h, int32_t nsteps, double* device_ms);
+
+/* Per-kernel timing with CUDA events on the handle's stream (on = 1 starts a
+ * fresh record, 0 stops).  The report lists, one line per kernel,
+ * "name launches total_ms", plus a first line "launches N" counting every
+ * kernel the handle launched since set-up (counted whether or not timing is
+ * on).  Returns the bytes written (without the terminating NUL). */
+int nhw_profile(nhw_handle* h, int32_t on);
+int nhw_profile_report(nhw_handle* h, char* buf, int32_t buflen);
 
 /* sizeof(nhw_params) and sizeof(nhw_scalars) as compiled into the library,
  * for bindings to check their struct images (no GPU needed). */

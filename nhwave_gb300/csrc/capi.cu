@@ -26,7 +26,11 @@ using nhw::SolverBase;
 
 #define NHW_GUARD(h)                              \
   if (!(h) || !(h)->s) return NHW_ERR_ARG;        \
-  if (!(h)->s->is_setup()) return NHW_ERR_STATE;
+  if (!(h)->s->is_setup()) return NHW_ERR_STATE;  \
+  { int b_ = (h)->s->bind(); if (b_) return b_; }
+#define NHW_BIND(h)                               \
+  if (!(h) || !(h)->s) return NHW_ERR_ARG;        \
+  { int b_ = (h)->s->bind(); if (b_) return b_; }
 
 extern "C" {
 
@@ -46,22 +50,24 @@ int nhw_create(const nhw_params* params, nhw_handle** out) {
 
 int nhw_destroy(nhw_handle* h) {
   if (!h) return NHW_ERR_ARG;
+  if (h->s) h->s->bind();
   delete h->s;
   delete h;
   return NHW_OK;
 }
 
 int nhw_setup(nhw_handle* h, const double* depth, const double* eta0, const double* uvw0) {
-  if (!h || !h->s || !depth) return NHW_ERR_ARG;
+  if (!depth) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->setup(depth, eta0, uvw0);
 }
 
 int nhw_get_field(nhw_handle* h, int field, void* host) {
-  if (!h || !h->s) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->get_field(field, host);
 }
 int nhw_set_field(nhw_handle* h, int field, const void* host) {
-  if (!h || !h->s) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->set_field(field, host);
 }
 int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* elem_bytes) {
@@ -74,11 +80,12 @@ int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* el
   return NHW_OK;
 }
 int nhw_get_scalars(nhw_handle* h, nhw_scalars* out) {
-  if (!h || !h->s || !out) return NHW_ERR_ARG;
+  if (!out) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->get_scalars(out);
 }
 int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step) {
-  if (!h || !h->s) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->set_time(time, dt, run_step);
 }
 
@@ -133,8 +140,22 @@ int nhw_mass(nhw_handle* h, double* mass) {
   return h->s->mass(mass);
 }
 int nhw_synchronize(nhw_handle* h) {
-  if (!h || !h->s) return NHW_ERR_ARG;
+  NHW_BIND(h);
   return h->s->sync();
+}
+
+int nhw_run_timed(nhw_handle* h, int32_t nsteps, double* device_ms) {
+  NHW_GUARD(h);
+  if (!device_ms || nsteps < 0) return NHW_ERR_ARG;
+  return h->s->run_timed(nsteps, device_ms);
+}
+int nhw_profile(nhw_handle* h, int32_t on) {
+  NHW_BIND(h);
+  return h->s->profile(on);
+}
+int nhw_profile_report(nhw_handle* h, char* buf, int32_t buflen) {
+  NHW_BIND(h);
+  return h->s->profile_report(buf, buflen);
 }
 
 int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes) {

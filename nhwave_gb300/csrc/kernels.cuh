@@ -144,6 +144,7 @@ __device__ __forceinline__ void reduce_finalize(const Dev<T>& S, double (&v)[NV]
 //                        2-D slopes of eta (delx/yFun_2D)
 // =========================================================================
 struct OpSlopeEta {
+  static constexpr const char* kName = "slope_eta";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const double* E = S.Eta;
@@ -165,7 +166,8 @@ struct OpSlopeEta {
 // =========================================================================
 //              source_terms (src/source_terms.F:30-67, 418-455)
 // =========================================================================
-struct OpSourceArea {  // one thread: Source_Area = sum over i of dx*D(i,Jbeg+1), in order
+struct OpSourceArea {
+  static constexpr const char* kName = "source_area";  // one thread: Source_Area = sum over i of dx*D(i,Jbeg+1), in order
   template <class T>
   __device__ void operator()(const Dev<T>& S, int, int) const {
     double a = 0.0;
@@ -176,6 +178,7 @@ struct OpSourceArea {  // one thread: Source_Area = sum over i of dx*D(i,Jbeg+1)
   }
 };
 struct OpSource {
+  static constexpr const char* kName = "source_terms";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -203,6 +206,7 @@ struct OpSource {
 // =========================================================================
 // x faces: face f between cells f-1 and f, row j, level k (all interior)
 struct OpFluxX {
+  static constexpr const char* kName = "flux_x";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int f, int j, int k) const {
     using R = T;
@@ -293,6 +297,7 @@ struct OpFluxX {
 
 // y faces: face g between cells g-1 and g in column i
 struct OpFluxY {
+  static constexpr const char* kName = "flux_y";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int g, int k) const {
     using R = T;
@@ -378,6 +383,7 @@ struct OpFluxY {
 
 // z faces k in [KB, KE+1] of an interior column (src/nhwave.F:1998-2023, 2719-2730)
 struct OpFluxZ {
+  static constexpr const char* kName = "flux_z";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     using R = T;
@@ -405,6 +411,7 @@ struct OpFluxZ {
 //   eval_duvw, explicit part: R1, D, R2-R4, DU/DV/DW (src/nhwave.F:611-1182)
 // =========================================================================
 struct OpExplicit {
+  static constexpr const char* kName = "stage_explicit";
   int istep;
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
@@ -450,6 +457,7 @@ struct OpExplicit {
 
 // D ghosts (wl_bc, walls) and Eta = D - Hc over the whole ghosted array
 struct OpWlBcEta {
+  static constexpr const char* kName = "wl_bc_eta";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -463,6 +471,7 @@ struct OpWlBcEta {
 //              get_UVW + vel_bc (src/nhwave.F:1651-1683, 4416-5117)
 // =========================================================================
 struct OpGetUVW {
+  static constexpr const char* kName = "get_uvw";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const long long o = i3(S, i, j, k);
@@ -476,6 +485,7 @@ struct OpGetUVW {
 // vel_bc, part A: lateral ghosts (walls) and the surface/bed face states of
 // every interior column after the kinematic conditions (KBC_surface/bottom).
 struct OpVelBcA {
+  static constexpr const char* kName = "vel_bc_a";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
@@ -525,6 +535,7 @@ struct OpVelBcA {
 // vel_bc, part B: bed and surface ghosts of interior columns
 // (free-slip bed; Derakhti et al. stress condition at the surface)
 struct OpVelBcB {
+  static constexpr const char* kName = "vel_bc_b";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -585,6 +596,7 @@ struct OpVelBcB {
 
 // initial: DU = D*U*Mask over all cells (src/initialize.F:3160-3170)
 struct OpInitDU {
+  static constexpr const char* kName = "init_du";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const long long c = i2(S, i, j), o = i3(S, i, j, k);
@@ -599,6 +611,7 @@ struct OpInitDU {
 //      Poisson: generate_coef_rhs (src/pressure.F:475-840), FP64
 // =========================================================================
 struct OpPoissonCoef {
+  static constexpr const char* kName = "poisson_coef";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const int ic = ic_of(S, i, j, k);
@@ -676,6 +689,7 @@ struct OpPoissonCoef {
 
 // copy of the FP64 operator into the inner precision (FP32 form only)
 struct OpCoefToT {
+  static constexpr const char* kName = "coef_to_inner";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const int ic = ic_of(S, i, j, k);
@@ -686,6 +700,7 @@ struct OpCoefToT {
 
 // vertical-line preconditioner factors: tridiagonal (C13, C1, C6) per column
 struct OpLineFactor {
+  static constexpr const char* kName = "line_factor";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const size_t n = (size_t)S.neq, mn = (size_t)S.M * S.N;
@@ -707,18 +722,21 @@ struct OpLineFactor {
 
 // P interior <- FP64 solution; lateral P ghosts (src/pressure.F:185-239)
 struct OpPFromX {
+  static constexpr const char* kName = "p_from_x";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     S.P[i3(S, i, j, k)] = S.xsol64[ic_of(S, i, j, k)];
   }
 };
 struct OpXFromP {
+  static constexpr const char* kName = "x_from_p";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     S.xsol64[ic_of(S, i, j, k)] = S.P[i3(S, i, j, k)];
   }
 };
 struct OpPGhost {
+  static constexpr const char* kName = "p_ghost";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
@@ -730,6 +748,7 @@ struct OpPGhost {
 
 // projection_corrector (src/nhwave.F:487-536)
 struct OpProjection {
+  static constexpr const char* kName = "projection";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const long long q = i2(S, i, j);
@@ -752,6 +771,7 @@ struct OpProjection {
 
 // SSP-RK combination, mask and Froude cap (src/nhwave.F:1227-1261)
 struct OpSSP {
+  static constexpr const char* kName = "ssp_combine";
   int istep;
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
@@ -782,7 +802,8 @@ struct OpSSP {
 // =========================================================================
 //               get_Omega (src/nhwave.F:1411-1648)
 // =========================================================================
-struct OpOmegaX {  // Ex on x faces from the new state; EtaxL/EtaxR kept for source_terms
+struct OpOmegaX {
+  static constexpr const char* kName = "omega_x";  // Ex on x faces from the new state; EtaxL/EtaxR kept for source_terms
   template <class T>
   __device__ void operator()(const Dev<T>& S, int f, int j, int k) const {
     using R = T;
@@ -832,6 +853,7 @@ struct OpOmegaX {  // Ex on x faces from the new state; EtaxL/EtaxR kept for sou
   }
 };
 struct OpOmegaY {
+  static constexpr const char* kName = "omega_y";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int g, int k) const {
     using R = T;
@@ -883,6 +905,7 @@ struct OpOmegaY {
 };
 // Omega column scan (src/nhwave.F:1617-1628)
 struct OpOmegaScan {
+  static constexpr const char* kName = "omega_scan";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long q = i2(S, i, j);
@@ -904,6 +927,7 @@ struct OpOmegaScan {
 
 // sponge_damping over every wet cell of the ghosted array (src/nhwave.F:6463-6502)
 struct OpSponge {
+  static constexpr const char* kName = "sponge";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -971,7 +995,8 @@ __global__ void k_dt_finalize(Dev<T> S) {
 // =========================================================================
 //            update_bathymetry, RIGID_3D (src/nhwave.F:5755-6071)
 // =========================================================================
-struct OpSlideA {  // Ho = Hc everywhere; new Hc in the interior
+struct OpSlideA {
+  static constexpr const char* kName = "slide_a";  // Ho = Hc everywhere; new Hc in the interior
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -986,14 +1011,16 @@ struct OpSlideA {  // Ho = Hc everywhere; new Hc in the interior
     S.Hc[c] = S.Hc0[c] - dmax_(0.0, zt);
   }
 };
-struct OpSlideB {  // Hc ghosts (phi_2D_coll)
+struct OpSlideB {
+  static constexpr const char* kName = "slide_b";  // Hc ghosts (phi_2D_coll)
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
     if (mi != i || mj != j) S.Hc[i2(S, i, j)] = S.Hc[i2(S, mi, mj)];
   }
 };
-struct OpSlideC {  // face depths, slopes, dH/dt (src/nhwave.F:6026-6069); grid (Mloc+1) x (Nloc+1)
+struct OpSlideC {
+  static constexpr const char* kName = "slide_c";  // face depths, slopes, dH/dt (src/nhwave.F:6026-6069); grid (Mloc+1) x (Nloc+1)
   template <class T>
   __device__ double hcx(const Dev<T>& S, int i, int j) const {
     // Hc(i,j) with the Fortran column-major continuation past the last row/column
@@ -1035,6 +1062,7 @@ struct OpSlideC {  // face depths, slopes, dH/dt (src/nhwave.F:6026-6069); grid 
 //                 update_mask (src/nhwave.F:5403-5456)
 // =========================================================================
 struct OpMaskA {
+  static constexpr const char* kName = "mask_a";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
@@ -1061,6 +1089,7 @@ struct OpMaskA {
   }
 };
 struct OpMaskB {
+  static constexpr const char* kName = "mask_b";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);

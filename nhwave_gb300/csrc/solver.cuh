@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -51,6 +52,10 @@ class SolverBase {
   virtual bool is_setup() const = 0;
   virtual double total_time() const = 0;
   virtual int sim_steps() const = 0;
+  virtual int bind() = 0;
+  virtual int run_timed(int nsteps, double* ms) = 0;
+  virtual int profile(int on) = 0;
+  virtual int profile_report(char* buf, int len) = 0;
 };
 
 template <class T>
@@ -103,18 +108,54 @@ class Solver final : public SolverBase {
   int64_t solves = 0;
   int it_order = 3;
   static constexpr bool kFP32 = sizeof(T) == 4;
+  // launch accounting and optional per-kernel CUDA-event timing
+  long long launches = 0;
+  bool prof_on = false;
+  struct Rec { const char* name; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+  cudaEvent_t ev_run0 = nullptr, ev_run1 = nullptr;
+
+  cudaEvent_t take_event() {
+    if (evused == evpool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      evpool.push_back(e);
+    }
+    return evpool[evused++];
+  }
+  template <class F>
+  void L(const char* name, F f) {
+    ++launches;
+    if (!prof_on) { f(); return; }
+    cudaEvent_t a = take_event(), b = take_event();
+    cudaEventRecord(a, st);
+    f();
+    cudaEventRecord(b, st);
+    recs.push_back({name, a, b});
+  }
 
   ~Solver() override {
     if (st) cudaStreamSynchronize(st);
+    for (auto e : evpool) cudaEventDestroy(e);
+    if (ev_run0) cudaEventDestroy(ev_run0);
+    if (ev_run1) cudaEventDestroy(ev_run1);
     if (arena) cudaFree(arena);
     if (h_sc) cudaFreeHost(h_sc);
     if (h_out) cudaFreeHost(h_out);
     if (st) cudaStreamDestroy(st);
   }
 
+  int bind() override {
+    NHW_CU(cudaSetDevice(p.device));
+    return NHW_OK;
+  }
   int create(const nhw_params& q) {
     p = q;
     int rc = check_params(p);
+    if (rc) return rc;
+    rc = bind();
     if (rc) return rc;
     const int M = p.Mglob, N = p.Nglob, K = p.Kglob;
     S.M = M; S.N = N; S.K = K;
@@ -208,13 +249,15 @@ class Solver final : public SolverBase {
 
   // ---------------------------------------------------------------- launchers
   template <class Op> void allcols(Op op) {
-    k_allcols<T, Op><<<cdiv((long long)S.Mloc * S.Nloc, 256), 256, 0, st>>>(S, op);
+    L(Op::kName, [&] { k_allcols<T, Op><<<cdiv((long long)S.Mloc * S.Nloc, 256), 256, 0, st>>>(S, op); });
   }
   template <class Op> void incols(Op op) {
-    k_incols<T, Op><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S, op);
+    L(Op::kName, [&] { k_incols<T, Op><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S, op); });
   }
   template <class Op> void box(Op op, int nx, int ny, int nz, int ox, int oy, int oz) {
-    k_box<T, Op><<<cdiv((long long)nx * ny * nz, 256), 256, 0, st>>>(S, op, nx, ny, nz, ox, oy, oz);
+    L(Op::kName, [&] {
+      k_box<T, Op><<<cdiv((long long)nx * ny * nz, 256), 256, 0, st>>>(S, op, nx, ny, nz, ox, oy, oz);
+    });
   }
   template <class Op> void cells(Op op) { box(op, S.M, S.N, S.K, S.IB, S.JB, S.KB); }
   unsigned red_blocks() const { return std::min<unsigned>(cdiv(S.neq, 256), kRedBlocks); }
@@ -364,7 +407,9 @@ class Solver final : public SolverBase {
     // initial: vel_bc on the initial velocities, then DU = D*U*Mask
     allcols(OpVelBcA{});
     incols(OpVelBcB{});
-    k_allcells<T, OpInitDU><<<cdiv((long long)S.Mloc * S.Nloc * S.Kloc, 256), 256, 0, st>>>(S, OpInitDU{});
+    L(OpInitDU::kName, [&] {
+      k_allcells<T, OpInitDU><<<cdiv((long long)S.Mloc * S.Nloc * S.Kloc, 256), 256, 0, st>>>(S, OpInitDU{});
+    });
     rc = sync();
     if (rc) return rc;
     ready = true;
@@ -391,8 +436,8 @@ class Solver final : public SolverBase {
 
   // -------------------------------------------------- reference subroutines
   int estimate_dt() override {
-    k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S);
-    k_dt_finalize<T><<<1, 1, 0, st>>>(S);
+    L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+    L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S); });
     int rc = pull_scalars();
     if (rc) return rc;
     if (h_sc->status == NHW_ERR_DT_MIN) return NHW_ERR_DT_MIN;
@@ -419,7 +464,7 @@ class Solver final : public SolverBase {
     return NHW_OK;
   }
   int source_terms() override {
-    if (S.wavemaker) k_single<T><<<1, 1, 0, st>>>(S, 0);
+    if (S.wavemaker) L("source_area", [&] { k_single<T><<<1, 1, 0, st>>>(S, 0); });
     incols(OpSource{});
     return check();
   }
@@ -443,7 +488,7 @@ class Solver final : public SolverBase {
     const int max_ir = kFP32 ? 12 : 4;
     int inner_total = 0, ir = 0, status = NHW_OK;
     for (ir = 0; ir <= max_ir; ++ir) {
-      k_res64<T><<<red_blocks(), 256, 0, st>>>(S);
+      L("res64", [&] { k_res64<T><<<red_blocks(), 256, 0, st>>>(S); });
       int rc = pull_scalars();
       if (rc) return rc;
       const double rel = h_sc->relres64;
@@ -457,16 +502,16 @@ class Solver final : public SolverBase {
       double tol_in = 0.5 * p.tol / rel;
       if (kFP32 && tol_in < 2e-5) tol_in = 2e-5;
       const int itmax_in = p.itmax - inner_total;
-      k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S);
+      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
       int chunk = 4;
       while (true) {
         for (int c = 0; c < chunk; ++c) {
           const unsigned cb = cdiv((long long)S.M * S.N, 256);
-          k_bicg_p<T><<<cb, 256, 0, st>>>(S);
-          k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S);
-          k_bicg_s<T><<<cb, 256, 0, st>>>(S);
-          k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S);
-          k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in);
+          L("bicg_p", [&] { k_bicg_p<T><<<cb, 256, 0, st>>>(S); });
+          L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
+          L("bicg_s", [&] { k_bicg_s<T><<<cb, 256, 0, st>>>(S); });
+          L("bicg_t", [&] { k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S); });
+          L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in); });
         }
         rc = pull_scalars();
         if (rc) return rc;
@@ -474,7 +519,7 @@ class Solver final : public SolverBase {
         if (chunk < 16) chunk *= 2;
       }
       inner_total += h_sc->it;
-      k_xupd<T><<<red_blocks(), 256, 0, st>>>(S);
+      L("x_update", [&] { k_xupd<T><<<red_blocks(), 256, 0, st>>>(S); });
       if (h_sc->conv == 5) { status = NHW_ERR_NAN; break; }
     }
     last_inner = inner_total;
@@ -530,8 +575,59 @@ class Solver final : public SolverBase {
     rc = check();
     return rc ? rc : worst;
   }
+  int run_timed(int nsteps, double* ms) override {
+    if (!ready) return NHW_ERR_STATE;
+    if (!ev_run0) { NHW_CU(cudaEventCreate(&ev_run0)); NHW_CU(cudaEventCreate(&ev_run1)); }
+    NHW_CU(cudaStreamSynchronize(st));
+    NHW_CU(cudaEventRecord(ev_run0, st));
+    int worst = NHW_OK;
+    for (int n = 0; n < nsteps; ++n) {
+      int rc = step();
+      if (rc != NHW_OK && rc != NHW_ERR_KRYLOV_NOCONV) return rc;
+      if (rc != NHW_OK) worst = rc;
+    }
+    NHW_CU(cudaEventRecord(ev_run1, st));
+    NHW_CU(cudaEventSynchronize(ev_run1));
+    float f = 0.f;
+    NHW_CU(cudaEventElapsedTime(&f, ev_run0, ev_run1));
+    *ms = (double)f;
+    return worst;
+  }
+  int profile(int on) override {
+    NHW_CU(cudaStreamSynchronize(st));
+    if (on) { recs.clear(); evused = 0; }
+    prof_on = on != 0;
+    return NHW_OK;
+  }
+  int profile_report(char* buf, int len) override {
+    NHW_CU(cudaStreamSynchronize(st));
+    std::vector<std::string> names;
+    std::vector<long long> cnt;
+    std::vector<double> tot;
+    for (auto& r : recs) {
+      float f = 0.f;
+      cudaEventElapsedTime(&f, r.a, r.b);
+      size_t q = 0;
+      while (q < names.size() && names[q] != r.name) ++q;
+      if (q == names.size()) { names.push_back(r.name); cnt.push_back(0); tot.push_back(0.0); }
+      ++cnt[q];
+      tot[q] += f;
+    }
+    std::string out = "launches " + std::to_string(launches) + "\n";
+    char line[160];
+    for (size_t q = 0; q < names.size(); ++q) {
+      std::snprintf(line, sizeof(line), "%s %lld %.6f\n", names[q].c_str(), cnt[q], tot[q]);
+      out += line;
+    }
+    if (buf && len > 0) {
+      const int n = std::min<int>((int)out.size(), len - 1);
+      std::memcpy(buf, out.data(), n);
+      buf[n] = 0;
+    }
+    return (int)out.size();
+  }
   int mass(double* m) override {
-    k_mass<T><<<1, 1, 0, st>>>(S, d_out);
+    L("mass", [&] { k_mass<T><<<1, 1, 0, st>>>(S, d_out); });
     NHW_CU(cudaMemcpyAsync(h_out, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
     NHW_CU(cudaStreamSynchronize(st));
     *m = h_out[0];

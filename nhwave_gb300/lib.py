@@ -29,8 +29,8 @@ EXPORTS = [
     "nhw_create", "nhw_destroy", "nhw_setup", "nhw_get_field", "nhw_set_field", "nhw_field_shape",
     "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
-    "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_abi_sizes", "nhw_status_string",
-    "nhw_last_error",
+    "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
+    "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
 ]
 
 
@@ -74,6 +74,9 @@ def load(path: str | None = None):
     L.nhw_run.argtypes = [vp, i32, P(i32)]
     L.nhw_mass.argtypes = [vp, P(dbl)]
     L.nhw_abi_sizes.argtypes = [P(i32), P(i32)]
+    L.nhw_run_timed.argtypes = [vp, i32, P(dbl)]
+    L.nhw_profile.argtypes = [vp, i32]
+    L.nhw_profile_report.argtypes = [vp, ctypes.c_char_p, i32]
     L.nhw_status_string.argtypes = [ctypes.c_int]
     L.nhw_status_string.restype = ctypes.c_char_p
     L.nhw_last_error.argtypes = []
@@ -175,6 +178,28 @@ class Scenario:
         _chk(load().nhw_run(self._h, n, ctypes.byref(done)), "nhw_run")
         return done.value
 
+    def run_timed(self, n: int) -> float:
+        """Run n steps; device milliseconds from CUDA events on the handle's stream."""
+        ms = ctypes.c_double(0.0)
+        _chk(load().nhw_run_timed(self._h, n, ctypes.byref(ms)), "nhw_run_timed")
+        return ms.value
+
+    def profile(self, on: bool):
+        _chk(load().nhw_profile(self._h, 1 if on else 0), "nhw_profile")
+
+    def profile_report(self) -> dict:
+        """{'launches': N, 'kernels': {name: (launches, total_ms)}}"""
+        L = load()
+        n = L.nhw_profile_report(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n + 1)
+        L.nhw_profile_report(self._h, buf, n + 1)
+        lines = buf.value.decode().strip().splitlines()
+        out = {"launches": int(lines[0].split()[1]), "kernels": {}}
+        for ln in lines[1:]:
+            name, c, t = ln.split()
+            out["kernels"][name] = (int(c), float(t))
+        return out
+
     def synchronize(self):
         return _chk(load().nhw_synchronize(self._h), "nhw_synchronize")
 
@@ -191,9 +216,15 @@ class Scenario:
     def set_time(self, time: float, dt: float, run_step: int):
         _chk(load().nhw_set_time(self._h, time, dt, run_step), "nhw_set_time")
 
-    def get(self, field: int) -> np.ndarray:
+    def get(self, field: int, out: np.ndarray | None = None) -> np.ndarray:
+        """Whole ghosted field as a [k][j][i] array (into ``out`` when given: a
+        C-contiguous array of the field's size and dtype, e.g. pinned memory)."""
         shp, dtype = self.shape.of(field)
-        out = np.empty(int(np.prod(shp)), dtype=dtype)
+        n = int(np.prod(shp))
+        if out is None:
+            out = np.empty(n, dtype=dtype)
+        elif out.dtype != dtype or out.size != n or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be C-contiguous {dtype} with {n} elements")
         _chk(load().nhw_get_field(self._h, field, _ptr(out)), "nhw_get_field")
         return out.reshape(shp[::-1])
 

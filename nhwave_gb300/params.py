@@ -52,7 +52,8 @@ class NhwParams(ctypes.Structure):
         ("slide_x0", ctypes.c_double), ("slide_y0", ctypes.c_double),
         ("slide_ut", ctypes.c_double), ("slide_a0", ctypes.c_double),
         ("precision", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 8),
+        ("device", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
     ]
 
     def copy(self) -> "NhwParams":
