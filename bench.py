@@ -212,7 +212,7 @@ def load_ncu_traffic():
 
 def roofline(prof, cells, elem_bytes):
     kern = prof["kernels"]
-    total = sum(t for _, t in kern.values())
+    total = sum(v[1] for v in kern.values())
     cand = {k: v for k, v in kern.items() if k in ALG_BYTES_PER_CELL}
     name, (launches, tot_ms) = max(cand.items(), key=lambda kv: kv[1][1])
     avg_s = tot_ms / launches / 1000.0
@@ -221,7 +221,7 @@ def roofline(prof, cells, elem_bytes):
     peak, peak_kind = load_peaks()
     tr = load_ncu_traffic().get(name)
     traffic = tr * cells if tr is not None else None
-    shares = {k: round(t / total, 4) for k, t in sorted(kern.items(), key=lambda kv: -kv[1][1])[:8]}
+    shares = {k: round(v[1] / total, 4) for k, v in sorted(kern.items(), key=lambda kv: -kv[1][1])[:8]}
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": traffic, "alg_bytes_per_launch": alg, "avg_launch_us": round(avg_s * 1e6, 2),

@@ -39,13 +39,17 @@ __device__ __forceinline__ R hydro(R eta, R h0) {
   return (R)0.5 * (R)kGrav * (eta * eta + (R)2.0 * eta * h0);
 }
 template <class R>
-__device__ __forceinline__ R hll(R sl, R sr, R fl, R fr, R ul, R ur) {
-  // HLL (src/nhwave.F:2741-2776)
+__device__ __forceinline__ R hll_d(R sl, R sr, R fl, R fr, R d_ur_ul) {
+  // HLL (src/nhwave.F:2741-2776) with UR-UL given
   if (sl >= (R)0) return fl;
   if (sr <= (R)0) return fr;
-  R f = sr * fl - sl * fr + sl * sr * (ur - ul);
+  R f = sr * fl - sl * fr + sl * sr * d_ur_ul;
   if (fabs(sr - sl) < (R)kSmall) return f / (R)kSmall;
   return f / (sr - sl);
+}
+template <class R>
+__device__ __forceinline__ R hll(R sl, R sr, R fl, R fr, R ul, R ur) {
+  return hll_d<R>(sl, sr, fl, fr, ur - ul);
 }
 
 __device__ __forceinline__ int mirror(int i, int b, int e) {
@@ -276,7 +280,7 @@ struct OpFluxX {
       SL = uL - pL;
       SR = uL + (R)2.0 * pL;
     }
-    R Ex = hll<R>(SL, SR, duL, duR, rdL, rdR);
+    R Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
     R Fx = hll<R>(SL, SR, FxL, FxR, duL, duR);
     R Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
     R Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
@@ -363,7 +367,7 @@ struct OpFluxY {
       SL = vL - pL;
       SR = vL + (R)2.0 * pL;
     }
-    R Ey = hll<R>(SL, SR, dvL, dvR, rdL, rdR);
+    R Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
     R Fy = hll<R>(SL, SR, FyL, FyR, duL, duR);
     R Gy = hll<R>(SL, SR, GyL, GyR, dvL, dvR);
     R Hy = hll<R>(SL, SR, HyL, HyR, dwL, dwR);
@@ -847,7 +851,7 @@ struct OpOmegaX {
       SL = uL - pL;
       SR = uL + (R)2.0 * pL;
     }
-    R Ex = hll<R>(SL, SR, duL, duR, rdL, rdR);
+    R Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
     if (f == S.IB || f == S.IE + 1) Ex = (R)0;
     S.Ex[i3(S, f, j, k)] = Ex;
   }
@@ -898,7 +902,7 @@ struct OpOmegaY {
       SL = vL - pL;
       SR = vL + (R)2.0 * pL;
     }
-    R Ey = hll<R>(SL, SR, dvL, dvR, rdL, rdR);
+    R Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
     if (g == S.JB || g == S.JE + 1) Ey = (R)0;
     S.Ey[i3(S, i, g, k)] = Ey;
   }

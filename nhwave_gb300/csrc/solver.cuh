@@ -485,7 +485,7 @@ class Solver final : public SolverBase {
     if (kFP32) cells(OpCoefToT{});
     incols(OpLineFactor{});
     cells(OpXFromP{});
-    const int max_ir = kFP32 ? 12 : 4;
+    const int max_ir = kFP32 ? 12 : 30;
     int inner_total = 0, ir = 0, status = NHW_OK;
     for (ir = 0; ir <= max_ir; ++ir) {
       L("res64", [&] { k_res64<T><<<red_blocks(), 256, 0, st>>>(S); });
