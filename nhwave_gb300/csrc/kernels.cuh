@@ -176,8 +176,7 @@ struct OpSourceArea {
   __device__ void operator()(const Dev<T>& S, int, int) const {
     double a = 0.0;
     const int jrow = S.JB + 1;
-    for (int i = S.IB; i <= S.IE; ++i)
-      if (S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe) a = a + S.dx * S.D[i2(S, i, jrow)];
+    for (int i = S.wm_i0; i <= S.wm_i1; ++i) a = a + S.dx * S.D[i2(S, i, jrow)];
     S.sc->source_area = a;
   }
 };
@@ -684,9 +683,13 @@ struct OpPoissonCoef {
       C[6] = C[6] + C[13]; C[7] = C[7] + C[12]; C[8] = C[8] + C[11]; C[5] = C[5] + C[14]; C[4] = C[4] + C[15];
       C[13] = C[12] = C[11] = C[14] = C[15] = 0.0;
     }
-    if (k == S.KE) { C[4] = C[5] = C[6] = C[7] = C[8] = 0.0; }
+    // compact form: C1, C6, C13 after every fold; the k+1 cross terms before
+    // the top row's zeroing (their negatives are the k-1 terms of this cell)
     const size_t n = (size_t)S.neq;
-    for (int m = 1; m <= NCOEF; ++m) S.coef64[(m - 1) * n + ic] = C[m];
+    double* o7 = S.coef64 + ic;
+    o7[3 * n] = C[4]; o7[4 * n] = C[5]; o7[5 * n] = C[7]; o7[6 * n] = C[8];
+    if (k == S.KE) { C[4] = C[5] = C[6] = C[7] = C[8] = 0.0; }
+    o7[0] = C[1]; o7[n] = C[6]; o7[2 * n] = C[13];
     S.rhs64[ic] = rhs;
   }
 };
@@ -698,7 +701,7 @@ struct OpCoefToT {
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
     const int ic = ic_of(S, i, j, k);
     const size_t n = (size_t)S.neq;
-    for (int m = 0; m < NCOEF; ++m) S.coefT[m * n + ic] = (T)S.coef64[m * n + ic];
+    for (int m = 0; m < 7; ++m) S.coefT[m * n + ic] = (T)S.coef64[m * n + ic];
   }
 };
 
@@ -712,9 +715,9 @@ struct OpLineFactor {
     double cpm = 0.0;
     for (int k = 0; k < S.K; ++k) {
       const size_t ic = base + mn * k;
-      const double a = k > 0 ? S.coef64[12 * n + ic] : 0.0;
+      const double a = k > 0 ? S.coef64[2 * n + ic] : 0.0;
       const double b = S.coef64[ic];
-      const double c = k < S.K - 1 ? S.coef64[5 * n + ic] : 0.0;
+      const double c = k < S.K - 1 ? S.coef64[n + ic] : 0.0;
       const double den = b - a * cpm;
       const double inv = 1.0 / den;
       cpm = c * inv;

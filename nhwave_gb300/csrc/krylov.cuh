@@ -6,105 +6,178 @@
 // the FP64 operator, and the initial guess is the previous P
 // (src/pressure.F:104-113, 386-397).
 //
-// Vectors use the compact interior order ic = i + M*(j + N*k).  Every
-// iteration kernel returns at once when the solve has already stopped
-// (sc->conv != 0), so a run of iterations can be queued without host round
-// trips.  Dot products are deterministic block reductions finished by the last
-// block of each kernel.
+// Operator storage.  After the boundary folds of generate_coef_rhs
+// (src/pressure.F:649-814) the 15 diagonals of a cell are fully described by
+// seven numbers: C1, C6, C13 and the k+1 cross terms C4, C5, C7, C8 (stored
+// before the top row's zeroing); the in-level neighbours are -1/dx^2 and
+// -1/dy^2, and the k-1 cross terms are exact negatives of the k+1 ones
+// (C15 = -C4, C14 = -C5, C12 = -C7, C11 = -C8), a relation every fold
+// preserves.  Neighbours outside the domain are skipped, which realises the
+// folds' zero coefficients.  Layout [7][neq], compact interior order
+// ic = i + M*(j + N*k); slot order C1, C6, C13, C4, C5, C7, C8.
+//
+// Every iteration kernel returns at once when the solve has stopped
+// (sc->conv != 0), so iterations can be queued without host round trips.  Dot
+// products are deterministic block reductions finished by the last block.
 #pragma once
 #include "kernels.cuh"
 
 namespace nhw {
 
-constexpr int kRedBlocks = 152 * 8;   // bounded grid of the reduction kernels
+constexpr int NCOMPACT = 7;
+constexpr int KREG = 32;   // columns up to this height are held in registers
 
-// y = A x on the 15-point stencil; C is [NCOEF][neq] in diagonal order 1..15
+template <class T>
+struct Acc { using type = double; };
+template <>
+struct Acc<float> { using type = float; };
+
+// y_ic = (A x)_ic on the compact operator
 template <class C, class V>
-__device__ __forceinline__ V spmv_at(const C* __restrict__ Cf, const V* __restrict__ x, size_t n, int ic,
-                                     int ii, int jj, int kk, int M, int N, int K) {
+__device__ __forceinline__ V spmv_c(const C* __restrict__ cf, const V* __restrict__ x, size_t n, int ic, int ii,
+                                    int jj, int kk, int M, int N, int K, V cxx, V cyy) {
   const int MN = M * N;
   const bool im = ii > 0, ip = ii < M - 1, jm = jj > 0, jp = jj < N - 1, km = kk > 0, kp = kk < K - 1;
-  V s = (V)Cf[ic] * x[ic];
-  if (ip) s += (V)Cf[1 * n + ic] * x[ic + 1];
-  if (jp) s += (V)Cf[2 * n + ic] * x[ic + M];
-  if (jm && kp) s += (V)Cf[3 * n + ic] * x[ic - M + MN];
-  if (im && kp) s += (V)Cf[4 * n + ic] * x[ic - 1 + MN];
-  if (kp) s += (V)Cf[5 * n + ic] * x[ic + MN];
-  if (ip && kp) s += (V)Cf[6 * n + ic] * x[ic + 1 + MN];
-  if (jp && kp) s += (V)Cf[7 * n + ic] * x[ic + M + MN];
-  if (im) s += (V)Cf[8 * n + ic] * x[ic - 1];
-  if (jm) s += (V)Cf[9 * n + ic] * x[ic - M];
-  if (jp && km) s += (V)Cf[10 * n + ic] * x[ic + M - MN];
-  if (ip && km) s += (V)Cf[11 * n + ic] * x[ic + 1 - MN];
-  if (km) s += (V)Cf[12 * n + ic] * x[ic - MN];
-  if (im && km) s += (V)Cf[13 * n + ic] * x[ic - 1 - MN];
-  if (jm && km) s += (V)Cf[14 * n + ic] * x[ic - M - MN];
+  V s = (V)cf[ic] * x[ic];
+  V h = (V)0;
+  if (ip) h += x[ic + 1];
+  if (im) h += x[ic - 1];
+  s += cxx * h;
+  h = (V)0;
+  if (jp) h += x[ic + M];
+  if (jm) h += x[ic - M];
+  s += cyy * h;
+  const V c4 = (V)cf[3 * n + ic], c5 = (V)cf[4 * n + ic], c7 = (V)cf[5 * n + ic], c8 = (V)cf[6 * n + ic];
+  if (kp) {
+    const int u = ic + MN;
+    s += (V)cf[n + ic] * x[u];
+    if (ip) s += c7 * x[u + 1];
+    if (im) s += c5 * x[u - 1];
+    if (jp) s += c8 * x[u + M];
+    if (jm) s += c4 * x[u - M];
+  }
+  if (km) {
+    const int d = ic - MN;
+    s += (V)cf[2 * n + ic] * x[d];
+    if (ip) s -= c7 * x[d + 1];
+    if (im) s -= c5 * x[d - 1];
+    if (jp) s -= c8 * x[d + M];
+    if (jm) s -= c4 * x[d - M];
+  }
   return s;
 }
 
-// out = M^-1 in on one column (Thomas sweeps with stored factors)
-template <class T>
-__device__ __forceinline__ void line_solve(const Dev<T>& S, const T* __restrict__ in, T* __restrict__ out,
-                                           size_t base) {
-  const size_t mn = (size_t)S.M * S.N, n = (size_t)S.neq;
-  const T* a = S.coefT + 12 * n;
-  T dp = (T)0;
-  for (int k = 0; k < S.K; ++k) {
-    const size_t ic = base + mn * k;
-    const T am = k > 0 ? a[ic] : (T)0;
-    dp = (in[ic] - am * dp) * S.linv[ic];
-    out[ic] = dp;
-  }
-  T z = out[base + mn * (S.K - 1)];
-  for (int k = S.K - 2; k >= 0; --k) {
-    const size_t ic = base + mn * k;
-    z = out[ic] - S.lcp[ic] * z;
-    out[ic] = z;
+// block-wide sum of NV accumulators (A = float or double), result in lane 0 of warp 0
+template <int NV, class A>
+__device__ __forceinline__ void block_sum_t(A (&v)[NV], double (&out)[NV]) {
+  __shared__ double sh[NV * 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+  __syncthreads();
+  if (lane == 0)
+    for (int q = 0; q < NV; ++q) sh[q * 32 + warp] = (double)v[q];
+  __syncthreads();
+  if (warp == 0) {
+    for (int q = 0; q < NV; ++q) {
+      double x = lane < nw ? sh[q * 32 + lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      out[q] = x;
+    }
   }
 }
 
-#define NHW_GRID_STRIDE(t, n) \
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (n); t += (long long)gridDim.x * blockDim.x)
+// partials + last-block finalisation (fixed order)
+template <int NV, class T, class Fin>
+__device__ __forceinline__ void finish_reduce(const Dev<T>& S, double (&v)[NV], Fin fin) {
+  __shared__ bool last;
+  __shared__ double sh2[NV * 32];
+  const int nb = gridDim.x;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NV; ++q) S.partials[(size_t)blockIdx.x * 8 + q] = v[q];
+    __threadfence();
+    const unsigned prev = atomicAdd(&S.sc->counter[0], 1u);
+    last = (prev == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[NV];
+  for (int q = 0; q < NV; ++q) acc[q] = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int q = 0; q < NV; ++q) acc[q] += ((volatile double*)S.partials)[(size_t)b * 8 + q];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int q = 0; q < NV; ++q)
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+  if (lane == 0)
+    for (int q = 0; q < NV; ++q) sh2[q * 32 + warp] = acc[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[NV];
+    for (int q = 0; q < NV; ++q) {
+      tot[q] = 0.0;
+      for (int w = 0; w < nw; ++w) tot[q] += sh2[q * 32 + w];
+    }
+    S.sc->counter[0] = 0u;
+    fin(S, tot);
+  }
+}
 
-// r64 = b - A64 x64 (FP64); inner rhs rT = (T) r64; ||r64||, ||b||
+__device__ __forceinline__ void decode(int ic, int M, int N, int& ii, int& jj, int& kk) {
+  ii = ic % M;
+  const int r = ic / M;
+  jj = r % N;
+  kk = r / N;
+}
+
+// ------------------------------------------------------------------ FP64 residual
+// r64 = b - A64 x64; inner right-hand side rT = (T) r64; ||r64||, ||b||
 template <class T>
 __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
   const int M = S.M, N = S.N, K = S.K;
   const size_t n = (size_t)S.neq;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double v[2] = {0.0, 0.0};
-  NHW_GRID_STRIDE(t, (long long)n) {
-    const int ic = (int)t, ii = ic % M, jj = (ic / M) % N, kk = ic / (M * N);
+  if (ic < S.neq) {
+    int ii, jj, kk;
+    decode(ic, M, N, ii, jj, kk);
     const double b = S.rhs64[ic];
-    const double r = b - spmv_at<double, double>(S.coef64, S.xsol64, n, ic, ii, jj, kk, M, N, K);
+    const double r = b - spmv_c<double, double>(S.coef64, S.xsol64, n, ic, ii, jj, kk, M, N, K, S.cxx, S.cyy);
     S.res64[ic] = r;
-    S.kr0[ic] = (T)r;   // inner right-hand side (kr0 doubles as its store)
-    v[0] += r * r;
-    v[1] += b * b;
+    S.kr0[ic] = (T)r;
+    v[0] = r * r;
+    v[1] = b * b;
   }
-  reduce_finalize<2>(S, v, 0, [] __device__(const Dev<T>& S2, double* a) {
+  double out[2];
+  block_sum_t<2, double>(v, out);
+  finish_reduce<2>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
     sc->bnorm = sqrt(a[1]);
     sc->relres64 = sc->bnorm > 0.0 ? sqrt(a[0]) / sc->bnorm : 0.0;
   });
 }
 
-// start of an inner solve from c = 0: r = r0 = rT, p = v = 0
+// start of an inner solve from c = 0: r = r0 = rT, p = v = 0, rho = (r, r)
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S) {
-  const size_t n = (size_t)S.neq;
-  double v[1] = {0.0};
-  NHW_GRID_STRIDE(t, (long long)n) {
+  using A = typename Acc<T>::type;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  A v[1] = {(A)0};
+  if (t < S.neq) {
     const T r = S.kr0[t];
     S.kr[t] = r;
     S.kx[t] = (T)0;
     S.kp[t] = (T)0;
     S.kv[t] = (T)0;
-    v[0] += (double)r * (double)r;
+    v[0] = (A)r * (A)r;
   }
-  reduce_finalize<1>(S, v, 0, [] __device__(const Dev<T>& S2, double* a) {
+  double out[1];
+  block_sum_t<1, A>(v, out);
+  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
     sc->rho = a[0];
-    sc->red[0] = sqrt(a[0]);   // inner reference norm
+    sc->red[0] = sqrt(a[0]);
     sc->alpha = 1.0;
     sc->omega = 1.0;
     sc->beta = 0.0;
@@ -114,71 +187,130 @@ __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S) {
   });
 }
 
+// Thomas sweeps of one column held in registers: dp forward then back-substitution.
+// `in(k)` yields the right-hand side of level k; the result is written to out.
+template <class T, class In>
+__device__ __forceinline__ void line_solve_reg(const Dev<T>& S, size_t col, In in, T* __restrict__ out) {
+  const size_t mn = (size_t)S.M * S.N, n = (size_t)S.neq;
+  const T* __restrict__ a = S.coefT + 2 * n;   // C13: coupling to k-1
+  const int K = S.K;
+  if (K <= KREG) {
+    T dp[KREG];
+    T prev = (T)0;
+#pragma unroll
+    for (int k = 0; k < KREG; ++k) {
+      if (k < K) {
+        const size_t ic = col + mn * k;
+        const T am = k > 0 ? a[ic] : (T)0;
+        prev = (in(k) - am * prev) * S.linv[ic];
+        dp[k] = prev;
+      }
+    }
+    T z = (T)0;
+#pragma unroll
+    for (int k = KREG - 1; k >= 0; --k) {
+      if (k < K) {
+        const size_t ic = col + mn * k;
+        z = (k == K - 1) ? dp[k] : dp[k] - S.lcp[ic] * z;
+        out[ic] = z;
+      }
+    }
+  } else {
+    T prev = (T)0;
+    for (int k = 0; k < K; ++k) {
+      const size_t ic = col + mn * k;
+      const T am = k > 0 ? a[ic] : (T)0;
+      prev = (in(k) - am * prev) * S.linv[ic];
+      out[ic] = prev;
+    }
+    T z = out[col + mn * (K - 1)];
+    for (int k = K - 2; k >= 0; --k) {
+      const size_t ic = col + mn * k;
+      z = out[ic] - S.lcp[ic] * z;
+      out[ic] = z;
+    }
+  }
+}
+
 // p = r + beta (p - omega v); ph = M^-1 p  (one column per thread)
 template <class T>
-__global__ void __launch_bounds__(256) k_bicg_p(Dev<T> S) {
+__global__ void __launch_bounds__(128) k_bicg_p(Dev<T> S) {
   if (S.sc->conv) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.M * S.N) return;
   const T beta = (T)S.sc->beta, omega = (T)S.sc->omega;
-  const size_t mn = (size_t)S.M * S.N;
-  for (int k = 0; k < S.K; ++k) {
-    const size_t ic = (size_t)t + mn * k;
-    S.kp[ic] = S.kr[ic] + beta * (S.kp[ic] - omega * S.kv[ic]);
-  }
-  line_solve(S, S.kp, S.kph, (size_t)t);
+  const size_t mn = (size_t)S.M * S.N, col = (size_t)t;
+  const T* __restrict__ r = S.kr;
+  const T* __restrict__ v = S.kv;
+  T* __restrict__ p = S.kp;
+  line_solve_reg<T>(S, col, [&](int k) {
+    const size_t ic = col + mn * k;
+    const T pk = r[ic] + beta * (p[ic] - omega * v[ic]);
+    p[ic] = pk;
+    return pk;
+  }, S.kph);
+}
+
+// s = r - alpha v; sh = M^-1 s
+template <class T>
+__global__ void __launch_bounds__(128) k_bicg_s(Dev<T> S) {
+  if (S.sc->conv) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.M * S.N) return;
+  const T alpha = (T)S.sc->alpha;
+  const size_t mn = (size_t)S.M * S.N, col = (size_t)t;
+  const T* __restrict__ r = S.kr;
+  const T* __restrict__ v = S.kv;
+  T* __restrict__ s = S.ks;
+  line_solve_reg<T>(S, col, [&](int k) {
+    const size_t ic = col + mn * k;
+    const T sk = r[ic] - alpha * v[ic];
+    s[ic] = sk;
+    return sk;
+  }, S.ksh);
 }
 
 // v = A ph; alpha = rho / (r0, v)
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_v(Dev<T> S) {
   if (S.sc->conv) return;
-  const int M = S.M, N = S.N, K = S.K;
-  const size_t n = (size_t)S.neq;
-  double v[1] = {0.0};
-  NHW_GRID_STRIDE(t, (long long)n) {
-    const int ic = (int)t, ii = ic % M, jj = (ic / M) % N, kk = ic / (M * N);
-    const T y = spmv_at<T, T>(S.coefT, S.kph, n, ic, ii, jj, kk, M, N, K);
+  using A = typename Acc<T>::type;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  A v[1] = {(A)0};
+  if (ic < S.neq) {
+    int ii, jj, kk;
+    decode(ic, S.M, S.N, ii, jj, kk);
+    const T y = spmv_c<T, T>(S.coefT, S.kph, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
     S.kv[ic] = y;
-    v[0] += (double)S.kr0[ic] * (double)y;
+    v[0] = (A)S.kr0[ic] * (A)y;
   }
-  reduce_finalize<1>(S, v, 0, [] __device__(const Dev<T>& S2, double* a) {
+  double out[1];
+  block_sum_t<1, A>(v, out);
+  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
     if (a[0] == 0.0 || !(a[0] == a[0])) { sc->conv = 2; return; }
     sc->alpha = sc->rho / a[0];
   });
 }
 
-// s = r - alpha v; sh = M^-1 s
-template <class T>
-__global__ void __launch_bounds__(256) k_bicg_s(Dev<T> S) {
-  if (S.sc->conv) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= S.M * S.N) return;
-  const T alpha = (T)S.sc->alpha;
-  const size_t mn = (size_t)S.M * S.N;
-  for (int k = 0; k < S.K; ++k) {
-    const size_t ic = (size_t)t + mn * k;
-    S.ks[ic] = S.kr[ic] - alpha * S.kv[ic];
-  }
-  line_solve(S, S.ks, S.ksh, (size_t)t);
-}
-
 // t = A sh; omega = (t, s) / (t, t)
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
   if (S.sc->conv) return;
-  const int M = S.M, N = S.N, K = S.K;
-  const size_t n = (size_t)S.neq;
-  double v[2] = {0.0, 0.0};
-  NHW_GRID_STRIDE(t, (long long)n) {
-    const int ic = (int)t, ii = ic % M, jj = (ic / M) % N, kk = ic / (M * N);
-    const T y = spmv_at<T, T>(S.coefT, S.ksh, n, ic, ii, jj, kk, M, N, K);
+  using A = typename Acc<T>::type;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  A v[2] = {(A)0, (A)0};
+  if (ic < S.neq) {
+    int ii, jj, kk;
+    decode(ic, S.M, S.N, ii, jj, kk);
+    const T y = spmv_c<T, T>(S.coefT, S.ksh, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
     S.kt[ic] = y;
-    v[0] += (double)y * (double)S.ks[ic];
-    v[1] += (double)y * (double)y;
+    v[0] = (A)y * (A)S.ks[ic];
+    v[1] = (A)y * (A)y;
   }
-  reduce_finalize<2>(S, v, 0, [] __device__(const Dev<T>& S2, double* a) {
+  double out[2];
+  block_sum_t<2, A>(v, out);
+  finish_reduce<2>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
     sc->omega = a[1] > 0.0 ? a[0] / a[1] : 0.0;
   });
@@ -188,17 +320,20 @@ __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S, double tol_in, int itmax_in) {
   if (S.sc->conv) return;
-  const size_t n = (size_t)S.neq;
+  using A = typename Acc<T>::type;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const T alpha = (T)S.sc->alpha, omega = (T)S.sc->omega;
-  double v[2] = {0.0, 0.0};
-  NHW_GRID_STRIDE(t, (long long)n) {
+  A v[2] = {(A)0, (A)0};
+  if (t < S.neq) {
     S.kx[t] = S.kx[t] + alpha * S.kph[t] + omega * S.ksh[t];
     const T r = S.ks[t] - omega * S.kt[t];
     S.kr[t] = r;
-    v[0] += (double)S.kr0[t] * (double)r;
-    v[1] += (double)r * (double)r;
+    v[0] = (A)S.kr0[t] * (A)r;
+    v[1] = (A)r * (A)r;
   }
-  reduce_finalize<2>(S, v, 0, [tol_in, itmax_in] __device__(const Dev<T>& S2, double* a) {
+  double out[2];
+  block_sum_t<2, A>(v, out);
+  finish_reduce<2>(S, out, [tol_in, itmax_in] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
     sc->it = sc->it + 1;
     sc->total_it = sc->total_it + 1;
@@ -216,7 +351,8 @@ __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S, double tol_in, int it
 // x64 += c
 template <class T>
 __global__ void __launch_bounds__(256) k_xupd(Dev<T> S) {
-  NHW_GRID_STRIDE(t, (long long)S.neq) { S.xsol64[t] = S.xsol64[t] + (double)S.kx[t]; }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < S.neq) S.xsol64[t] = S.xsol64[t] + (double)S.kx[t];
 }
 
 }  // namespace nhw

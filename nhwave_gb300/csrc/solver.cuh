@@ -165,6 +165,7 @@ class Solver final : public SolverBase {
     S.IB = NG; S.IE = M + NG - 1; S.JB = NG; S.JE = N + NG - 1; S.KB = NG; S.KE = K + NG - 1;
     S.neq = M * N * K;
     S.dx = p.dx; S.dy = p.dy; S.min_dep = p.min_dep; S.cfl = p.cfl;
+    S.cxx = -1. / (p.dx * p.dx); S.cyy = -1. / (p.dy * p.dy);
     S.dt_min = p.dt_min; S.dt_max = p.dt_max;
     S.fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);
     S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
@@ -210,14 +211,14 @@ class Solver final : public SolverBase {
                 &S.Ex, &S.Fx, &S.Gx, &S.Hx, &S.Ey, &S.Fy, &S.Gy, &S.Hy, &S.Fz, &S.Gz, &S.Hz};
     for (auto pp : t3) add(pp, sizeof(T) * n3);
     add(&S.P, sizeof(double) * n3);
-    add(&S.coef64, sizeof(double) * NCOEF * neq);
+    add(&S.coef64, sizeof(double) * NCOMPACT * neq);
     add(&S.rhs64, sizeof(double) * neq);
     add(&S.xsol64, sizeof(double) * neq);
     add(&S.res64, sizeof(double) * neq);
-    if (kFP32) add(&S.coefT, sizeof(T) * NCOEF * neq);
+    if (kFP32) add(&S.coefT, sizeof(T) * NCOMPACT * neq);
     T** tk[] = {&S.lcp, &S.linv, &S.kx, &S.kr, &S.kr0, &S.kp, &S.kph, &S.kv, &S.ks, &S.ksh, &S.kt};
     for (auto pp : tk) add(pp, sizeof(T) * neq);
-    add(&S.partials, sizeof(double) * 8 * kRedBlocks);
+    add(&S.partials, sizeof(double) * 8 * (cdiv((long long)neq, 256) + 8));
     add(&S.sc, sizeof(DevScal));
     add(&d_out, sizeof(double) * 8);
     stage_elems = std::max(n3, (size_t)(S.Mloc + 1) * (S.Nloc + 1) * (S.Kloc + 1));
@@ -260,7 +261,7 @@ class Solver final : public SolverBase {
     });
   }
   template <class Op> void cells(Op op) { box(op, S.M, S.N, S.K, S.IB, S.JB, S.KB); }
-  unsigned red_blocks() const { return std::min<unsigned>(cdiv(S.neq, 256), kRedBlocks); }
+  unsigned red_blocks() const { return cdiv(S.neq, 256); }
 
   int check() {
     cudaError_t e = cudaGetLastError();
@@ -375,6 +376,12 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
+    S.wm_i0 = S.IB; S.wm_i1 = S.IB - 1;   // empty unless a source column exists
+    for (int i = S.IB; i <= S.IE; ++i)
+      if (h.xc[i] >= p.xsource_west && h.xc[i] <= p.xsource_east) {
+        if (S.wm_i1 < S.wm_i0) S.wm_i0 = i;
+        S.wm_i1 = i;
+      }
     NHW_CU(cudaMemcpyAsync((void*)S.sig, h.sig.data(), sizeof(double) * h.sig.size(), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaMemcpyAsync((void*)S.dsig, h.dsig.data(), sizeof(double) * h.dsig.size(), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaMemcpyAsync((void*)S.sigc, h.sigc.data(), sizeof(double) * h.sigc.size(), cudaMemcpyHostToDevice, st));
@@ -506,10 +513,10 @@ class Solver final : public SolverBase {
       int chunk = 4;
       while (true) {
         for (int c = 0; c < chunk; ++c) {
-          const unsigned cb = cdiv((long long)S.M * S.N, 256);
-          L("bicg_p", [&] { k_bicg_p<T><<<cb, 256, 0, st>>>(S); });
+          const unsigned cb = cdiv((long long)S.M * S.N, 128);
+          L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
           L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
-          L("bicg_s", [&] { k_bicg_s<T><<<cb, 256, 0, st>>>(S); });
+          L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
           L("bicg_t", [&] { k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S); });
           L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in); });
         }
@@ -519,7 +526,7 @@ class Solver final : public SolverBase {
         if (chunk < 16) chunk *= 2;
       }
       inner_total += h_sc->it;
-      L("x_update", [&] { k_xupd<T><<<red_blocks(), 256, 0, st>>>(S); });
+      L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
       if (h_sc->conv == 5) { status = NHW_ERR_NAN; break; }
     }
     last_inner = inner_total;

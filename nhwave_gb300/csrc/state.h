@@ -57,6 +57,7 @@ struct Dev {
   int neq;           // M*N*K
   // parameters
   double dx, dy, min_dep, cfl, dt_min, dt_max, fcor, froude_cap;
+  double cxx, cyy;                 // Poisson in-level couplings -1/dx^2, -1/dy^2
   int froude_on, non_hydro, sponge_on, it_order;
   int bc_x0, bc_xn, bc_y0, bc_yn;
   double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt)
@@ -65,6 +66,7 @@ struct Dev {
   int wavemaker;
   double wm_segma, wm_celerity, wm_amp, wm_wnumy, wm_xw, wm_xe, wm_ys, wm_yn;
   double wm_atmp, wm_xstart;
+  int wm_i0, wm_i1;                // interior i range of the source strip (xc is monotonic)
   // sponge current
   double cur_wave, tramp;
   // rigid slide (RIGID_3D)
@@ -83,13 +85,13 @@ struct Dev {
   T *U, *V, *W, *DU, *DV, *DW, *DU0, *DV0, *DW0, *Omega;
   T *Ex, *Fx, *Gx, *Hx, *Ey, *Fy, *Gy, *Hy, *Fz, *Gz, *Hz;
   double* P;
-  // Poisson: FP64 operator (15 diagonals, compact interior order) + rhs
-  double* coef64;     // [NCOEF][neq]
+  // Poisson: FP64 operator (compact 7-slot form, see krylov.cuh) + rhs
+  double* coef64;     // [7][neq]
   double* rhs64;      // [neq]
   double* xsol64;     // [neq]  FP64 solution (= P interior)
   double* res64;      // [neq]  FP64 residual for refinement
   // Krylov working vectors in the inner precision T (compact interior order)
-  T* coefT;           // [NCOEF][neq] (aliases coef64 when T == double)
+  T* coefT;           // [7][neq] (aliases coef64 when T == double)
   T *lcp, *linv;      // line preconditioner factors [neq]
   T *kx, *kr, *kr0, *kp, *kph, *kv, *ks, *ksh, *kt;
   double* partials;   // reduction partials [nblocks * 8]
