@@ -106,7 +106,10 @@ typedef struct nhw_params {
   double  slide_ut, slide_a0;              /* SlideUt SlideA0                         */
   int32_t precision;                       /* enum nhw_precision                      */
   int32_t device;                          /* CUDA device ordinal of the handle       */
-  int32_t reserved[7];
+  int32_t precond;                         /* Poisson preconditioner: 0 multigrid V-cycle,
+                                              1 vertical-line (tridiagonal) only     */
+  float   mg_weight;                       /* multigrid coarse-correction weight (0: 1.0) */
+  int32_t reserved[5];
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

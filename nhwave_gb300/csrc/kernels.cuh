@@ -613,6 +613,22 @@ struct OpInitDU {
 // =========================================================================
 //      Poisson: generate_coef_rhs (src/pressure.F:475-840), FP64
 // =========================================================================
+// per-column factors of the sigma transformation, used by the Poisson
+// assembly and the projection: DelxS(k) = (1-sig_k) DelxH/D - sig_k DelxEta/D
+struct OpColFactors {
+  static constexpr const char* kName = "col_factors";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const double inv = 1.0 / S.D[q];
+    S.cf_invD[q] = inv;
+    S.cf_hx[q] = S.DelxH[q] * inv;
+    S.cf_ex[q] = S.DelxEta[q] * inv;
+    S.cf_hy[q] = S.DelyH[q] * inv;
+    S.cf_ey[q] = S.DelyEta[q] * inv;
+  }
+};
+
 struct OpPoissonCoef {
   static constexpr const char* kName = "poisson_coef";
   template <class T>
@@ -620,53 +636,51 @@ struct OpPoissonCoef {
     const int ic = ic_of(S, i, j, k);
     const long long sy = S.sy, sz = S.sz;
     auto inside = [&](int x, int y) { return x >= S.IB && x <= S.IE && y >= S.JB && y <= S.JE; };
-    const double sgk = S.sig[k];
+    const double sgk = S.sig[k], omk = 1. - sgk;
     // DelxS/DelyS at level sig(k) of interior columns, zero outside (src/pressure.F:494-505)
     auto dxs = [&](int x, int y) -> double {
       if (!inside(x, y)) return 0.0;
       const long long q = i2(S, x, y);
-      return (1. - sgk) / S.D[q] * S.DelxH[q] - sgk / S.D[q] * S.DelxEta[q];
+      return omk * S.cf_hx[q] - sgk * S.cf_ex[q];
     };
     auto dys = [&](int x, int y) -> double {
       if (!inside(x, y)) return 0.0;
       const long long q = i2(S, x, y);
-      return (1. - sgk) / S.D[q] * S.DelyH[q] - sgk / S.D[q] * S.DelyEta[q];
+      return omk * S.cf_hy[q] - sgk * S.cf_ey[q];
     };
     const long long q = i2(S, i, j);
-    const double Dq = S.D[q];
-    const double DelxS = dxs(i, j), DelyS = dys(i, j), DelzS = 1. / Dq;
+    const double DelxS = dxs(i, j), DelyS = dys(i, j), DelzS = S.cf_invD[q];
     const double A1 = DelxS * DelxS + DelyS * DelyS + DelzS * DelzS;
-    const double dsk = S.dsig[k], dskm = S.dsig[k - 1];
-    const double s = dsk + dskm, hk = 0.5 * (dsk + dskm);
-    const double dx = S.dx, dy = S.dy;
+    const double lx = S.lv_x[k], ly = S.lv_y[k], ih = S.lv_h[k];
     // Rhs (src/pressure.F:521-525); Uf/Vf: linear interpolation to sig(k) (src/nhwave.F:1346-1355)
+    const double dsk = S.dsig[k], dskm = S.dsig[k - 1];
     const double fint = dsk / (dsk + dskm);
     const long long o = i3(S, i, j, k);
     auto uf = [&](const T* A, long long e) -> double {
       return (1.0 - fint) * (double)A[e] + fint * (double)A[e - sz];
     };
-    double rhs = -((uf(S.U, o + 1) - uf(S.U, o - 1)) / (2.0 * dx) +
-                   ((double)S.U[o] - (double)S.U[o - sz]) / hk * DelxS +
-                   (uf(S.V, o + sy) - uf(S.V, o - sy)) / (2.0 * dy) +
-                   ((double)S.V[o] - (double)S.V[o - sz]) / hk * DelyS +
-                   ((double)S.W[o] - (double)S.W[o - sz]) / hk * DelzS - S.SourceC[q]) *
-                 kRho0 / S.sc->dt;
+    const double i2dx = 0.5 / S.dx, i2dy = 0.5 / S.dy;
+    double rhs = -((uf(S.U, o + 1) - uf(S.U, o - 1)) * i2dx + ((double)S.U[o] - (double)S.U[o - sz]) * ih * DelxS +
+                   (uf(S.V, o + sy) - uf(S.V, o - sy)) * i2dy + ((double)S.V[o] - (double)S.V[o - sz]) * ih * DelyS +
+                   ((double)S.W[o] - (double)S.W[o - sz]) * ih * DelzS - S.SourceC[q]) *
+                 (kRho0 / S.sc->dt);
     double C[NCOEF + 1];
-    C[1] = 2. / (dx * dx) + 2. / (dy * dy) + A1 / (hk * dsk) + A1 / (hk * dskm);
-    C[2] = -1. / (dx * dx);
-    C[3] = -1. / (dy * dy);
-    C[4] = dys(i, j - 1) / (2. * dy * s) + DelyS / (2. * dy * s);
-    C[5] = dxs(i - 1, j) / (2. * dx * s) + DelxS / (2. * dx * s);
-    C[6] = -A1 / (hk * dsk);
-    C[7] = -(dxs(i + 1, j) / (2. * dx * s) + DelxS / (2. * dx * s));
-    C[8] = -(dys(i, j + 1) / (2. * dy * s) + DelyS / (2. * dy * s));
-    C[9] = -1. / (dx * dx);
-    C[10] = -1. / (dy * dy);
-    C[11] = dys(i, j + 1) / (2. * dy * s) + DelyS / (2. * dy * s);
-    C[12] = dxs(i + 1, j) / (2. * dx * s) + DelxS / (2. * dx * s);
-    C[13] = -A1 / (hk * dskm);
-    C[14] = -(dxs(i - 1, j) / (2. * dx * s) + DelxS / (2. * dx * s));
-    C[15] = -(dys(i, j - 1) / (2. * dy * s) + DelyS / (2. * dy * s));
+    const double cxx = S.cxx, cyy = S.cyy;
+    C[1] = -2. * cxx - 2. * cyy + A1 * S.lv_up[k] + A1 * S.lv_dn[k];
+    C[2] = cxx;
+    C[3] = cyy;
+    C[4] = (dys(i, j - 1) + DelyS) * ly;
+    C[5] = (dxs(i - 1, j) + DelxS) * lx;
+    C[6] = -A1 * S.lv_up[k];
+    C[7] = -(dxs(i + 1, j) + DelxS) * lx;
+    C[8] = -(dys(i, j + 1) + DelyS) * ly;
+    C[9] = cxx;
+    C[10] = cyy;
+    C[11] = -C[8];
+    C[12] = -C[7];
+    C[13] = -A1 * S.lv_dn[k];
+    C[14] = -C[5];
+    C[15] = -C[4];
     // boundary folds in the reference's order (src/pressure.F:649-814)
     if (i == S.IB) { C[1] = C[1] + C[9]; C[6] = C[6] + C[5]; C[13] = C[13] + C[14]; C[9] = C[5] = C[14] = 0.0; }
     if (i == S.IE) { C[1] = C[1] + C[2]; C[6] = C[6] + C[7]; C[13] = C[13] + C[12]; C[2] = C[7] = C[12] = 0.0; }
@@ -762,17 +776,17 @@ struct OpProjection {
     if (S.Mask[q] == 0) return;
     const long long o = i3(S, i, j, k), sy = S.sy, sz = S.sz;
     const double* P = S.P;
-    const double dx = S.dx, dy = S.dy;
-    const double DelxP = 0.5 * ((P[o + 1] - P[o - 1]) / (2. * dx) + (P[o + 1 + sz] - P[o - 1 + sz]) / (2. * dx));
-    const double DelyP = 0.5 * ((P[o + sy] - P[o - sy]) / (2. * dy) + (P[o + sy + sz] - P[o - sy + sz]) / (2. * dy));
-    const double DelzP = (P[o + sz] - P[o]) / S.dsig[k];
-    const double Dq = S.D[q], sc = S.sigc[k];
-    const double DelxSc = (1.0 - sc) / Dq * S.DelxH[q] - sc / Dq * S.DelxEta[q];
-    const double DelySc = (1.0 - sc) / Dq * S.DelyH[q] - sc / Dq * S.DelyEta[q];
-    const double dt = S.sc->dt;
-    S.DU[o] = (T)((double)S.DU[o] - Dq * dt / kRho0 * (DelxP + DelzP * DelxSc));
-    S.DV[o] = (T)((double)S.DV[o] - Dq * dt / kRho0 * (DelyP + DelzP * DelySc));
-    S.DW[o] = (T)((double)S.DW[o] - dt / kRho0 * DelzP);
+    const double i2dx = 0.5 / S.dx, i2dy = 0.5 / S.dy;
+    const double DelxP = 0.5 * ((P[o + 1] - P[o - 1]) * i2dx + (P[o + 1 + sz] - P[o - 1 + sz]) * i2dx);
+    const double DelyP = 0.5 * ((P[o + sy] - P[o - sy]) * i2dy + (P[o + sy + sz] - P[o - sy + sz]) * i2dy);
+    const double DelzP = (P[o + sz] - P[o]) * S.lv_ds[k];
+    const double sc = S.sigc[k], omc = 1.0 - sc;
+    const double DelxSc = omc * S.cf_hx[q] - sc * S.cf_ex[q];
+    const double DelySc = omc * S.cf_hy[q] - sc * S.cf_ey[q];
+    const double f = S.D[q] * (S.sc->dt / kRho0), g = S.sc->dt / kRho0;
+    S.DU[o] = (T)((double)S.DU[o] - f * (DelxP + DelzP * DelxSc));
+    S.DV[o] = (T)((double)S.DV[o] - f * (DelyP + DelzP * DelySc));
+    S.DW[o] = (T)((double)S.DW[o] - g * DelzP);
   }
 };
 

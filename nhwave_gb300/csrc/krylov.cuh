@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
 
 // start of an inner solve from c = 0: r = r0 = rT, p = v = 0, rho = (r, r)
 template <class T>
-__global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S) {
+__global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S, double tol_in, int itmax_in) {
   using A = typename Acc<T>::type;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   A v[1] = {(A)0};
@@ -174,8 +174,10 @@ __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S) {
   }
   double out[1];
   block_sum_t<1, A>(v, out);
-  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
+  finish_reduce<1>(S, out, [tol_in, itmax_in] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
+    sc->tol_in = tol_in;
+    sc->itmax_in = itmax_in;
     sc->rho = a[0];
     sc->red[0] = sqrt(a[0]);
     sc->alpha = 1.0;
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
 
 // x += alpha ph + omega sh; r = s - omega t; convergence test
 template <class T>
-__global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S, double tol_in, int itmax_in) {
+__global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S) {
   if (S.sc->conv) return;
   using A = typename Acc<T>::type;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -333,8 +335,10 @@ __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S, double tol_in, int it
   }
   double out[2];
   block_sum_t<2, A>(v, out);
-  finish_reduce<2>(S, out, [tol_in, itmax_in] __device__(const Dev<T>& S2, double* a) {
+  finish_reduce<2>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
+    const double tol_in = sc->tol_in;
+    const int itmax_in = sc->itmax_in;
     sc->it = sc->it + 1;
     sc->total_it = sc->total_it + 1;
     const double rel = sc->red[0] > 0.0 ? sqrt(a[1]) / sc->red[0] : 0.0;

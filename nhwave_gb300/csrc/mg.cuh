@@ -1,0 +1,322 @@
+// mg.cuh -- multigrid V-cycle used as the preconditioner of the Poisson solve.
+//
+// The reference preconditions its Krylov solve with HYPRE's semicoarsening
+// multigrid (StructSMG, src/pressure.F:406-415) or with incomplete
+// factorisations in NSPCG.  This is this project's own multigrid for the same
+// operator, built for the GPU:
+//   * coarsening: aggregation of columns in the horizontal only (2 x 2 while a
+//     direction has at least 4 cells), the vertical resolution kept on every
+//     level -- the sigma-layer coupling is usually the strong one;
+//   * coarse operators: Galerkin products P^T A P with piecewise-constant P,
+//     which keep the 15-point pattern, hence the compact form of krylov.cuh
+//     plus explicit in-level couplings (uneven last aggregates make those
+//     non-uniform);
+//   * smoother: red-black ("zebra") vertical-line Gauss-Seidel -- each colour
+//     solves the tridiagonal (C13, C1, C6) system of its columns with the
+//     neighbouring columns (the other colour) fixed; one sweep before and one
+//     after the coarse-grid correction, several on the coarsest level.
+// Every kernel returns at once when the Krylov solve has stopped (sc->conv).
+#pragma once
+#include "krylov.cuh"
+
+namespace nhw {
+
+template <class T>
+struct MGL {
+  int M, N, K, n;
+  const T* coef;        // [7][n] compact operator of this level
+  const T* cxr;         // [n] coupling to i+1 (nullptr: the constant cxx)
+  const T* cyr;         // [n] coupling to j+1 (nullptr: the constant cyy)
+  T cxx, cyy;
+  const T* lcp;         // line factors of (C13, C1, C6)
+  const T* linv;
+  T* x;
+  T* b;
+  int rx, ry;           // aggregation to the next coarser level
+  int Mc, Nc;
+};
+
+template <class T>
+__device__ __forceinline__ T cx_p(const MGL<T>& L, int ic) { return L.cxr ? L.cxr[ic] : L.cxx; }
+template <class T>
+__device__ __forceinline__ T cx_m(const MGL<T>& L, int ic) { return L.cxr ? L.cxr[ic - 1] : L.cxx; }
+template <class T>
+__device__ __forceinline__ T cy_p(const MGL<T>& L, int ic) { return L.cyr ? L.cyr[ic] : L.cyy; }
+template <class T>
+__device__ __forceinline__ T cy_m(const MGL<T>& L, int ic) { return L.cyr ? L.cyr[ic - L.M] : L.cyy; }
+
+// off-column part of (A x) at cell (ii, jj, kk): everything but C1, C6, C13
+template <class T>
+__device__ __forceinline__ T off_column(const MGL<T>& L, const T* __restrict__ x, int ic, int ii, int jj, int kk) {
+  const int M = L.M, MN = L.M * L.N, n = L.n;
+  const bool im = ii > 0, ip = ii < L.M - 1, jm = jj > 0, jp = jj < L.N - 1, km = kk > 0, kp = kk < L.K - 1;
+  T s = (T)0;
+  if (ip) s += cx_p(L, ic) * x[ic + 1];
+  if (im) s += cx_m(L, ic) * x[ic - 1];
+  if (jp) s += cy_p(L, ic) * x[ic + M];
+  if (jm) s += cy_m(L, ic) * x[ic - M];
+  const T c4 = L.coef[3 * n + ic], c5 = L.coef[4 * n + ic], c7 = L.coef[5 * n + ic], c8 = L.coef[6 * n + ic];
+  if (kp) {
+    const int u = ic + MN;
+    if (ip) s += c7 * x[u + 1];
+    if (im) s += c5 * x[u - 1];
+    if (jp) s += c8 * x[u + M];
+    if (jm) s += c4 * x[u - M];
+  }
+  if (km) {
+    const int d = ic - MN;
+    if (ip) s -= c7 * x[d + 1];
+    if (im) s -= c5 * x[d - 1];
+    if (jp) s -= c8 * x[d + M];
+    if (jm) s -= c4 * x[d - M];
+  }
+  return s;
+}
+
+template <class T>
+__device__ __forceinline__ T level_apply(const MGL<T>& L, const T* __restrict__ x, int ic, int ii, int jj, int kk) {
+  const int MN = L.M * L.N;
+  T s = L.coef[ic] * x[ic] + off_column(L, x, ic, ii, jj, kk);
+  if (kk < L.K - 1) s += L.coef[L.n + ic] * x[ic + MN];
+  if (kk > 0) s += L.coef[2 * L.n + ic] * x[ic - MN];
+  return s;
+}
+
+// red-black line Gauss-Seidel half-sweep: columns with (ii+jj)%2 == color
+template <class T>
+__global__ void __launch_bounds__(128) k_mg_smooth(MGL<T> L, const DevScal* sc, int color, int zero_x) {
+  if (sc->conv) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // thread t handles the t-th column of its colour: rows alternate the colour's parity
+  const int half = (L.M + 1 - color) / 2;          // columns of this colour in a row with jj even
+  const int ncol_row0 = half;
+  const int ncol_row1 = (L.M + color) / 2;          // rows with jj odd
+  const int pair = ncol_row0 + ncol_row1;
+  const int jp2 = t / pair, rem = t % pair;
+  int jj, ii;
+  if (rem < ncol_row0) { jj = 2 * jp2; ii = 2 * rem + color; }
+  else { jj = 2 * jp2 + 1; ii = 2 * (rem - ncol_row0) + (1 - color); }
+  if (jj >= L.N || ii >= L.M) return;
+  const int M = L.M, MN = L.M * L.N, K = L.K, n = L.n;
+  const int col = ii + M * jj;
+  const T* __restrict__ a = L.coef + 2 * n;
+  T* __restrict__ x = L.x;
+  if (K <= KREG) {
+    T dp[KREG];
+    T prev = (T)0;
+#pragma unroll
+    for (int k = 0; k < KREG; ++k) {
+      if (k < K) {
+        const int ic = col + MN * k;
+        const T rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, x, ic, ii, jj, k));
+        const T am = k > 0 ? a[ic] : (T)0;
+        prev = (rhs - am * prev) * L.linv[ic];
+        dp[k] = prev;
+      }
+    }
+    T z = (T)0;
+#pragma unroll
+    for (int k = KREG - 1; k >= 0; --k) {
+      if (k < K) {
+        const int ic = col + MN * k;
+        z = (k == K - 1) ? dp[k] : dp[k] - L.lcp[ic] * z;
+        x[ic] = z;
+      }
+    }
+  } else {
+    T prev = (T)0;
+    for (int k = 0; k < K; ++k) {
+      const int ic = col + MN * k;
+      const T rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, x, ic, ii, jj, k));
+      const T am = k > 0 ? a[ic] : (T)0;
+      prev = (rhs - am * prev) * L.linv[ic];
+      x[ic] = prev;
+    }
+    T z = x[col + MN * (K - 1)];
+    for (int k = K - 2; k >= 0; --k) {
+      const int ic = col + MN * k;
+      z = x[ic] - L.lcp[ic] * z;
+      x[ic] = z;
+    }
+  }
+}
+
+// Same half-sweep, block-parallel: a block holds 32 columns of the colour and
+// up to 32 levels (blockDim = 32 x min(K,32)); every thread forms the line
+// right-hand sides of its (column, level) cells -- loads coalesced along the
+// columns -- into shared memory, then one warp runs the Thomas sweeps there.
+template <class T>
+__global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal* sc, int color, int zero_x) {
+  if (sc->conv) return;
+  extern __shared__ unsigned char smem_raw[];
+  T* sh = reinterpret_cast<T*>(smem_raw);
+  const int K = L.K, M = L.M, MN = L.M * L.N, n = L.n;
+  T* s_rhs = sh;                 // [K][32]
+  T* s_a = sh + K * 32;          // C13
+  T* s_inv = sh + 2 * K * 32;    // 1/den
+  T* s_cp = sh + 3 * K * 32;     // c/den
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int t = blockIdx.x * 32 + tx;
+  const int ncol_row0 = (M + 1 - color) / 2, ncol_row1 = (M + color) / 2, pair = ncol_row0 + ncol_row1;
+  const int jp2 = t / pair, rem = t % pair;
+  int jj, ii;
+  if (rem < ncol_row0) { jj = 2 * jp2; ii = 2 * rem + color; }
+  else { jj = 2 * jp2 + 1; ii = 2 * (rem - ncol_row0) + (1 - color); }
+  const bool valid = jj < L.N && ii < M;
+  const int col = ii + M * jj;
+  for (int k = ty; k < K; k += blockDim.y) {
+    T rhs = (T)0, a = (T)0, inv = (T)0, cp = (T)0;
+    if (valid) {
+      const int ic = col + MN * k;
+      rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, L.x, ic, ii, jj, k));
+      a = k > 0 ? L.coef[2 * n + ic] : (T)0;
+      inv = L.linv[ic];
+      cp = L.lcp[ic];
+    }
+    s_rhs[k * 32 + tx] = rhs;
+    s_a[k * 32 + tx] = a;
+    s_inv[k * 32 + tx] = inv;
+    s_cp[k * 32 + tx] = cp;
+  }
+  __syncthreads();
+  if (ty != 0 || !valid) return;
+  T prev = (T)0;
+  for (int k = 0; k < K; ++k) {
+    prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
+    s_rhs[k * 32 + tx] = prev;
+  }
+  T z = prev;
+  L.x[col + MN * (K - 1)] = z;
+  for (int k = K - 2; k >= 0; --k) {
+    z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
+    L.x[col + MN * k] = z;
+  }
+}
+
+// b_c = P^T (b_f - A_f x_f), x_c = 0
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_restrict(MGL<T> F, MGL<T> C, const DevScal* sc) {
+  if (sc->conv) return;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= C.n) return;
+  int I, J, k;
+  decode(ic, C.M, C.N, I, J, k);
+  T acc = (T)0;
+  for (int b = 0; b < F.ry; ++b) {
+    const int j = J * F.ry + b;
+    if (j >= F.N) break;
+    for (int a = 0; a < F.rx; ++a) {
+      const int i = I * F.rx + a;
+      if (i >= F.M) break;
+      const int f = i + F.M * (j + F.N * k);
+      acc += F.b[f] - level_apply(F, F.x, f, i, j, k);
+    }
+  }
+  C.b[ic] = acc;
+  C.x[ic] = (T)0;
+}
+
+// x_f += w * x_c(aggregate)
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_prolong(MGL<T> F, MGL<T> C, const DevScal* sc, T w) {
+  if (sc->conv) return;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F.n) return;
+  int i, j, k;
+  decode(f, F.M, F.N, i, j, k);
+  const int c = i / F.rx + C.M * (j / F.ry + C.N * k);
+  F.x[f] += w * C.x[c];
+}
+
+// Galerkin coarse operator P^T A P (piecewise-constant P), compact form + couplings
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_galerkin(MGL<T> F, T* ccoef, T* ccxr, T* ccyr, int Mc, int Nc) {
+  const int nc = Mc * Nc * F.K;
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= nc) return;
+  int I, J, k;
+  decode(ic, Mc, Nc, I, J, k);
+  const int K = F.K, n = F.n, MN = F.M * F.N;
+  (void)MN;
+  T d = 0, up = 0, dn = 0, xp = 0, yp = 0;
+  T x7u = 0, x5u = 0, y8u = 0, y4u = 0, x7d = 0, x5d = 0, y8d = 0, y4d = 0;
+  for (int b = 0; b < F.ry; ++b) {
+    const int j = J * F.ry + b;
+    if (j >= F.N) break;
+    for (int a = 0; a < F.rx; ++a) {
+      const int i = I * F.rx + a;
+      if (i >= F.M) break;
+      const int f = i + F.M * (j + F.N * k);
+      d += F.coef[f];
+      if (k < K - 1) up += F.coef[n + f];
+      if (k > 0) dn += F.coef[2 * n + f];
+      const T c4 = F.coef[3 * n + f], c5 = F.coef[4 * n + f], c7 = F.coef[5 * n + f], c8 = F.coef[6 * n + f];
+      // in-level neighbours
+      if (i + 1 < F.M) { const T c = cx_p(F, f); if ((i + 1) / F.rx == I) d += c; else xp += c; }
+      if (i - 1 >= 0) { const T c = cx_m(F, f); if ((i - 1) / F.rx == I) d += c; }
+      if (j + 1 < F.N) { const T c = cy_p(F, f); if ((j + 1) / F.ry == J) d += c; else yp += c; }
+      if (j - 1 >= 0) { const T c = cy_m(F, f); if ((j - 1) / F.ry == J) d += c; }
+      // cross terms k+1 (+c) and k-1 (-c)
+      if (k < K - 1) {
+        if (i + 1 < F.M) { if ((i + 1) / F.rx == I) up += c7; else x7u += c7; }
+        if (i - 1 >= 0) { if ((i - 1) / F.rx == I) up += c5; else x5u += c5; }
+        if (j + 1 < F.N) { if ((j + 1) / F.ry == J) up += c8; else y8u += c8; }
+        if (j - 1 >= 0) { if ((j - 1) / F.ry == J) up += c4; else y4u += c4; }
+      }
+      if (k > 0) {
+        if (i + 1 < F.M) { if ((i + 1) / F.rx == I) dn -= c7; else x7d -= c7; }
+        if (i - 1 >= 0) { if ((i - 1) / F.rx == I) dn -= c5; else x5d -= c5; }
+        if (j + 1 < F.N) { if ((j + 1) / F.ry == J) dn -= c8; else y8d -= c8; }
+        if (j - 1 >= 0) { if ((j - 1) / F.ry == J) dn -= c4; else y4d -= c4; }
+      }
+    }
+  }
+  const bool top = (k == K - 1);
+  ccoef[ic] = d;
+  ccoef[nc + ic] = up;
+  ccoef[2 * nc + ic] = dn;
+  ccoef[3 * nc + ic] = top ? -y4d : y4u;
+  ccoef[4 * nc + ic] = top ? -x5d : x5u;
+  ccoef[5 * nc + ic] = top ? -x7d : x7u;
+  ccoef[6 * nc + ic] = top ? -y8d : y8u;
+  ccxr[ic] = xp;
+  ccyr[ic] = yp;
+}
+
+// line factors of one level (C13, C1, C6), one column per thread
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_factor(MGL<T> L, T* lcp, T* linv) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= L.M * L.N) return;
+  const int MN = L.M * L.N, n = L.n;
+  double cpm = 0.0;
+  for (int k = 0; k < L.K; ++k) {
+    const int ic = col + MN * k;
+    const double a = k > 0 ? (double)L.coef[2 * n + ic] : 0.0;
+    const double b = (double)L.coef[ic];
+    const double c = k < L.K - 1 ? (double)L.coef[n + ic] : 0.0;
+    const double inv = 1.0 / (b - a * cpm);
+    cpm = c * inv;
+    lcp[ic] = (T)cpm;
+    linv[ic] = (T)inv;
+  }
+}
+
+// p = r + beta (p - omega v)   /   s = r - alpha v   (cell kernels when MG preconditions)
+template <class T>
+__global__ void __launch_bounds__(256) k_bicg_p_cell(Dev<T> S) {
+  if (S.sc->conv) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.neq) return;
+  const T beta = (T)S.sc->beta, omega = (T)S.sc->omega;
+  S.kp[t] = S.kr[t] + beta * (S.kp[t] - omega * S.kv[t]);
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_bicg_s_cell(Dev<T> S) {
+  if (S.sc->conv) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.neq) return;
+  S.ks[t] = S.kr[t] - (T)S.sc->alpha * S.kv[t];
+}
+
+}  // namespace nhw

@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "krylov.cuh"
+#include "mg.cuh"
 #include "setup_host.h"
 
 namespace nhw {
@@ -116,6 +116,11 @@ class Solver final : public SolverBase {
   std::vector<cudaEvent_t> evpool;
   size_t evused = 0;
   cudaEvent_t ev_run0 = nullptr, ev_run1 = nullptr;
+  // multigrid hierarchy (level 0 is the fine operator)
+  std::vector<MGL<T>> mg;
+  bool use_mg = true;
+  T mg_w = (T)1;
+  int mg_coarse_sweeps = 6;
 
   cudaEvent_t take_event() {
     if (evused == evpool.size()) {
@@ -139,6 +144,7 @@ class Solver final : public SolverBase {
   ~Solver() override {
     if (st) cudaStreamSynchronize(st);
     for (auto e : evpool) cudaEventDestroy(e);
+    for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
     if (ev_run0) cudaEventDestroy(ev_run0);
     if (ev_run1) cudaEventDestroy(ev_run1);
     if (arena) cudaFree(arena);
@@ -200,10 +206,13 @@ class Solver final : public SolverBase {
     add(&S.sigc, sizeof(double) * S.Kloc);
     add(&S.xc, sizeof(double) * S.Mloc);
     add(&S.yc, sizeof(double) * S.Nloc);
+    for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds})
+      add((double**)lv, sizeof(double) * S.Kloc);
     double** d2[] = {&S.D, &S.D0, &S.Eta, &S.Eta0, &S.Hc, &S.Hc0, &S.Ho, &S.Hfx, &S.Hfy, &S.Hfx0, &S.Hfy0,
                      &S.DelxH, &S.DelyH, &S.DeltH, &S.DeltHo, &S.Delt2H, &S.DelxEta, &S.DelyEta, &S.SourceX,
                      &S.SourceY, &S.SourceC, &S.Sponge, &S.R1, &S.Wsx, &S.Wsy, &S.EtaxL, &S.EtaxR, &S.EtayL,
-                     &S.EtayR, &S.zUL, &S.zVL, &S.zWL, &S.zUR, &S.zVR, &S.zWR};
+                     &S.EtayR, &S.zUL, &S.zVL, &S.zWL, &S.zUR, &S.zVR, &S.zWR,
+                     &S.cf_hx, &S.cf_ex, &S.cf_hy, &S.cf_ey, &S.cf_invD};
     for (auto pp : d2) add(pp, sizeof(double) * n2);
     int** i2p[] = {&S.Mask, &S.MaskT, &S.Mask_Struct, &S.Mask9};
     for (auto pp : i2p) add(pp, sizeof(int) * n2);
@@ -219,6 +228,36 @@ class Solver final : public SolverBase {
     T** tk[] = {&S.lcp, &S.linv, &S.kx, &S.kr, &S.kr0, &S.kp, &S.kph, &S.kv, &S.ks, &S.ksh, &S.kt};
     for (auto pp : tk) add(pp, sizeof(T) * neq);
     add(&S.partials, sizeof(double) * 8 * (cdiv((long long)neq, 256) + 8));
+    // multigrid levels: horizontal 2x2 aggregation while a direction has >= 4 cells
+    use_mg = p.precond == 0;
+    mg_w = (T)(p.mg_weight > 0.f ? p.mg_weight : 1.0f);
+    mg.clear();
+    {
+      MGL<T> L0{};
+      L0.M = M; L0.N = N; L0.K = K; L0.n = M * N * K;
+      mg.push_back(L0);
+      while (use_mg && mg.size() < 16) {
+        MGL<T>& f = mg.back();
+        const int rx = f.M >= 4 ? 2 : 1, ry = f.N >= 4 ? 2 : 1;
+        if ((rx == 1 && ry == 1) || f.M * f.N <= 32) break;
+        f.rx = rx; f.ry = ry;
+        f.Mc = (f.M + rx - 1) / rx; f.Nc = (f.N + ry - 1) / ry;
+        MGL<T> c{};
+        c.M = f.Mc; c.N = f.Nc; c.K = K; c.n = c.M * c.N * K;
+        mg.push_back(c);
+      }
+    }
+    std::vector<T**> mgptr;
+    for (size_t l = 1; l < mg.size(); ++l) {
+      const size_t nl = (size_t)mg[l].n;
+      add((T**)&mg[l].coef, sizeof(T) * NCOMPACT * nl);
+      add((T**)&mg[l].cxr, sizeof(T) * nl);
+      add((T**)&mg[l].cyr, sizeof(T) * nl);
+      add((T**)&mg[l].lcp, sizeof(T) * nl);
+      add((T**)&mg[l].linv, sizeof(T) * nl);
+      add(&mg[l].x, sizeof(T) * nl);
+      add(&mg[l].b, sizeof(T) * nl);
+    }
     add(&S.sc, sizeof(DevScal));
     add(&d_out, sizeof(double) * 8);
     stage_elems = std::max(n3, (size_t)(S.Mloc + 1) * (S.Nloc + 1) * (S.Kloc + 1));
@@ -237,6 +276,11 @@ class Solver final : public SolverBase {
     size_t off = 0;
     for (auto& e2 : plan) { *e2.first = arena + off; off += (e2.second + 255) & ~size_t(255); }
     if (!kFP32) S.coefT = (T*)S.coef64;
+    mg[0].coef = S.coefT; mg[0].cxr = nullptr; mg[0].cyr = nullptr;
+    mg[0].lcp = S.lcp; mg[0].linv = S.linv;
+    for (auto& L : mg) { L.cxx = (T)S.cxx; L.cyy = (T)S.cyy; }
+    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(T) * 4 * 32 * 64)));
     NHW_CU(cudaMallocHost((void**)&h_sc, sizeof(DevScal)));
     NHW_CU(cudaMallocHost((void**)&h_out, sizeof(double) * 8));
     std::memset(h_sc, 0, sizeof(DevScal));
@@ -387,6 +431,24 @@ class Solver final : public SolverBase {
     NHW_CU(cudaMemcpyAsync((void*)S.sigc, h.sigc.data(), sizeof(double) * h.sigc.size(), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaMemcpyAsync((void*)S.xc, h.xc.data(), sizeof(double) * h.xc.size(), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaMemcpyAsync((void*)S.yc, h.yc.data(), sizeof(double) * h.yc.size(), cudaMemcpyHostToDevice, st));
+    {  // per-level reciprocals of the Poisson assembly and the projection
+      std::vector<double> lx(S.Kloc, 0.0), ly(S.Kloc, 0.0), lu(S.Kloc, 0.0), ld(S.Kloc, 0.0), lh(S.Kloc, 0.0),
+          lds(S.Kloc, 0.0);
+      for (int k = 1; k < S.Kloc; ++k) {
+        const double dk = h.dsig[k], dm = h.dsig[k - 1], s = dk + dm, hk = 0.5 * (dk + dm);
+        lx[k] = 1.0 / (2. * p.dx * s);
+        ly[k] = 1.0 / (2. * p.dy * s);
+        lu[k] = 1.0 / (hk * dk);
+        ld[k] = 1.0 / (hk * dm);
+        lh[k] = 1.0 / hk;
+        lds[k] = 1.0 / dk;
+      }
+      const std::vector<double>* src[] = {&lx, &ly, &lu, &ld, &lh, &lds};
+      const double* dst[] = {S.lv_x, S.lv_y, S.lv_up, S.lv_dn, S.lv_h, S.lv_ds};
+      for (int q = 0; q < 6; ++q)
+        NHW_CU(cudaMemcpyAsync((void*)dst[q], src[q]->data(), sizeof(double) * S.Kloc, cudaMemcpyHostToDevice, st));
+      NHW_CU(cudaStreamSynchronize(st));
+    }
     struct Up { int f; const void* src; } ups[] = {
         {NHW_F_HC, h.Hc.data()}, {NHW_F_HC0, h.Hc0.data()}, {NHW_F_DELXH, h.DelxH.data()},
         {NHW_F_DELYH, h.DelyH.data()}, {NHW_F_ETA, h.Eta.data()}, {NHW_F_ETA0, h.Eta.data()},
@@ -488,10 +550,20 @@ class Solver final : public SolverBase {
     incols(OpVelBcB{});
   }
   int poisson() {
+    incols(OpColFactors{});
     cells(OpPoissonCoef{});
     if (kFP32) cells(OpCoefToT{});
     incols(OpLineFactor{});
     cells(OpXFromP{});
+    if (use_mg)
+      for (size_t l = 1; l < mg.size(); ++l) {
+        MGL<T> f = mg[l - 1];
+        MGL<T>& c = mg[l];
+        L("mg_galerkin", [&] {
+          k_mg_galerkin<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, (T*)c.coef, (T*)c.cxr, (T*)c.cyr, c.M, c.N);
+        });
+        L("mg_factor", [&] { k_mg_factor<T><<<cdiv((long long)c.M * c.N, 256), 256, 0, st>>>(c, (T*)c.lcp, (T*)c.linv); });
+      }
     const int max_ir = kFP32 ? 12 : 30;
     int inner_total = 0, ir = 0, status = NHW_OK;
     for (ir = 0; ir <= max_ir; ++ir) {
@@ -509,17 +581,11 @@ class Solver final : public SolverBase {
       double tol_in = 0.5 * p.tol / rel;
       if (kFP32 && tol_in < 2e-5) tol_in = 2e-5;
       const int itmax_in = p.itmax - inner_total;
-      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in); });
       int chunk = 4;
       while (true) {
-        for (int c = 0; c < chunk; ++c) {
-          const unsigned cb = cdiv((long long)S.M * S.N, 128);
-          L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
-          L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
-          L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
-          L("bicg_t", [&] { k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S); });
-          L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in); });
-        }
+        rc = run_iterations(chunk);
+        if (rc) return rc;
         rc = pull_scalars();
         if (rc) return rc;
         if (h_sc->conv != 0) break;
@@ -537,6 +603,89 @@ class Solver final : public SolverBase {
     int rc = check();
     return rc ? rc : status;
   }
+  // `chunk` BiCGSTAB iterations; replayed from a captured CUDA graph unless the
+  // per-kernel profiler is on (its events would become graph nodes)
+  struct ChunkGraph { int chunk; cudaGraphExec_t exec; long long kernels; };
+  std::vector<ChunkGraph> graphs;
+  bool use_graphs = true;
+  int run_iterations(int chunk) {
+    if (!use_graphs || prof_on) {
+      for (int c = 0; c < chunk; ++c) one_iteration();
+      return check();
+    }
+    for (auto& g : graphs)
+      if (g.chunk == chunk) {
+        NHW_CU(cudaGraphLaunch(g.exec, st));
+        launches += g.kernels;
+        return NHW_OK;
+      }
+    cudaGraph_t graph;
+    const long long l0 = launches;
+    NHW_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int c = 0; c < chunk; ++c) one_iteration();
+    NHW_CU(cudaStreamEndCapture(st, &graph));
+    cudaGraphExec_t exec;
+    NHW_CU(cudaGraphInstantiate(&exec, graph, 0));
+    cudaGraphDestroy(graph);
+    graphs.push_back({chunk, exec, launches - l0});
+    launches = l0;
+    NHW_CU(cudaGraphLaunch(exec, st));
+    launches += graphs.back().kernels;
+    return NHW_OK;
+  }
+  void one_iteration() {
+    const unsigned cb = cdiv((long long)S.M * S.N, 128);
+    if (use_mg) {
+      L("bicg_p", [&] { k_bicg_p_cell<T><<<red_blocks(), 256, 0, st>>>(S); });
+      vcycle(S.kp, S.kph);
+    } else {
+      L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
+    }
+    L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
+    if (use_mg) {
+      L("bicg_s", [&] { k_bicg_s_cell<T><<<red_blocks(), 256, 0, st>>>(S); });
+      vcycle(S.ks, S.ksh);
+    } else {
+      L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
+    }
+    L("bicg_t", [&] { k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S); });
+    L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S); });
+  }
+  // multigrid V-cycle: x ~= A^-1 b on level 0
+  void smooth(const MGL<T>& Lv, int color, int zero_x, int level = 0) {
+    static const char* names[] = {"mg_smooth_l0", "mg_smooth_l1", "mg_smooth_l2", "mg_smooth_l3",
+                                  "mg_smooth_l4", "mg_smooth_l5", "mg_smooth_l6", "mg_smooth_l7+"};
+    const int pair = (Lv.M + 1 - color) / 2 + (Lv.M + color) / 2;
+    const long long nthr = (long long)pair * ((Lv.N + 1) / 2);
+    const int by = std::min(Lv.K, 32);
+    const size_t shm = sizeof(T) * 4 * 32 * Lv.K;
+    L(names[level < 7 ? level : 7], [&] {
+      k_mg_smooth_blk<T><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x);
+    });
+  }
+  void vcycle(const T* b, T* x) {
+    mg[0].b = (T*)b;
+    mg[0].x = x;
+    const int nl = (int)mg.size();
+    for (int l = 0; l < nl - 1; ++l) {
+      smooth(mg[l], 0, 1, l);
+      smooth(mg[l], 1, 0, l);
+      MGL<T> f = mg[l], c = mg[l + 1];
+      L("mg_restrict", [&] { k_mg_restrict<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, c, S.sc); });
+    }
+    const MGL<T>& cl = mg[nl - 1];
+    for (int s2 = 0; s2 < (nl > 1 ? mg_coarse_sweeps : 1); ++s2) {
+      smooth(cl, 0, s2 == 0 ? 1 : 0, nl - 1);
+      smooth(cl, 1, 0, nl - 1);
+    }
+    for (int l = nl - 2; l >= 0; --l) {
+      MGL<T> f = mg[l], c = mg[l + 1];
+      L("mg_prolong", [&] { k_mg_prolong<T><<<cdiv(f.n, 256), 256, 0, st>>>(f, c, S.sc, mg_w); });
+      smooth(mg[l], 1, 0, l);
+      smooth(mg[l], 0, 0, l);
+    }
+  }
+
   int eval_duvw(int istep) override {
     if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
     const int s = istep - 1;

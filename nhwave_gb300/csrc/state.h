@@ -42,7 +42,8 @@ struct DevScal {
   double rho, alpha, omega, beta;
   double red[8];                    // reduction results
   double bnorm, relres, relres64;
-  int32_t it, conv, ir, pad0;
+  int32_t it, conv, ir, itmax_in;
+  double tol_in;
   unsigned int counter[4];          // last-block-done counters
   int64_t total_it, solves;
 };
@@ -80,6 +81,10 @@ struct Dev {
   double *DelxEta, *DelyEta, *SourceX, *SourceY, *SourceC, *Sponge, *R1, *Wsx, *Wsy;
   double *EtaxL, *EtaxR, *EtayL, *EtayR;
   double *zUL, *zVL, *zWL, *zUR, *zVR, *zWR;   // vel_bc face states at the surface / bed
+  double *cf_hx, *cf_ex, *cf_hy, *cf_ey, *cf_invD;  // per column: DelxH/D, DelxEta/D, ..., 1/D
+  // per sigma level k: 1/(2dx(dsig_k+dsig_k-1)), 1/(2dy(..)), 1/(h_k dsig_k), 1/(h_k dsig_k-1),
+  // 1/h_k with h_k = (dsig_k+dsig_k-1)/2, 1/dsig_k
+  const double *lv_x, *lv_y, *lv_up, *lv_dn, *lv_h, *lv_ds;
   int *Mask, *MaskT, *Mask_Struct, *Mask9;
   // 3-D fields (storage type T); P is FP64 in both forms
   T *U, *V, *W, *DU, *DV, *DW, *DU0, *DV0, *DW0, *Omega;

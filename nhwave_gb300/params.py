@@ -53,7 +53,9 @@ class NhwParams(ctypes.Structure):
         ("slide_ut", ctypes.c_double), ("slide_a0", ctypes.c_double),
         ("precision", ctypes.c_int32),
         ("device", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("precond", ctypes.c_int32),
+        ("mg_weight", ctypes.c_float),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
     def copy(self) -> "NhwParams":
