@@ -25,6 +25,7 @@
 namespace nhw {
 
 constexpr int NCOMPACT = 7;
+constexpr int kCPT = 8;    // cells per thread in the reducing kernels (fewer blocks to combine)
 constexpr int KREG = 32;   // columns up to this height are held in registers
 
 template <class T>
@@ -137,17 +138,20 @@ template <class T>
 __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
   const int M = S.M, N = S.N, K = S.K;
   const size_t n = (size_t)S.neq;
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   double v[2] = {0.0, 0.0};
-  if (ic < S.neq) {
-    int ii, jj, kk;
-    decode(ic, M, N, ii, jj, kk);
-    const double b = S.rhs64[ic];
-    const double r = b - spmv_c<double, double>(S.coef64, S.xsol64, n, ic, ii, jj, kk, M, N, K, S.cxx, S.cyy);
-    S.res64[ic] = r;
-    S.kr0[ic] = (T)r;
-    v[0] = r * r;
-    v[1] = b * b;
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (ic < S.neq) {
+      int ii, jj, kk;
+      decode(ic, M, N, ii, jj, kk);
+      const double b = S.rhs64[ic];
+      const double r = b - spmv_c<double, double>(S.coef64, S.xsol64, n, ic, ii, jj, kk, M, N, K, S.cxx, S.cyy);
+      S.res64[ic] = r;
+      S.kr0[ic] = (T)r;
+      v[0] += r * r;
+      v[1] += b * b;
+    }
   }
   double out[2];
   block_sum_t<2, double>(v, out);
@@ -162,15 +166,18 @@ __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S, double tol_in, int itmax_in) {
   using A = typename Acc<T>::type;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   A v[1] = {(A)0};
-  if (t < S.neq) {
-    const T r = S.kr0[t];
-    S.kr[t] = r;
-    S.kx[t] = (T)0;
-    S.kp[t] = (T)0;
-    S.kv[t] = (T)0;
-    v[0] = (A)r * (A)r;
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int t = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (t < S.neq) {
+      const T r = S.kr0[t];
+      S.kr[t] = r;
+      S.kx[t] = (T)0;
+      S.kp[t] = (T)0;
+      S.kv[t] = (T)0;
+      v[0] += (A)r * (A)r;
+    }
   }
   double out[1];
   block_sum_t<1, A>(v, out);
@@ -277,14 +284,20 @@ template <class T>
 __global__ void __launch_bounds__(256) k_bicg_v(Dev<T> S) {
   if (S.sc->conv) return;
   using A = typename Acc<T>::type;
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   A v[1] = {(A)0};
-  if (ic < S.neq) {
-    int ii, jj, kk;
-    decode(ic, S.M, S.N, ii, jj, kk);
-    const T y = spmv_c<T, T>(S.coefT, S.kph, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
-    S.kv[ic] = y;
-    v[0] = (A)S.kr0[ic] * (A)y;
+  const T* __restrict__ ph = S.kph;
+  const T* __restrict__ r0 = S.kr0;
+  T* __restrict__ vv = S.kv;
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (ic < S.neq) {
+      int ii, jj, kk;
+      decode(ic, S.M, S.N, ii, jj, kk);
+      const T y = spmv_c<T, T>(S.coefT, ph, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
+      vv[ic] = y;
+      v[0] += (A)r0[ic] * (A)y;
+    }
   }
   double out[1];
   block_sum_t<1, A>(v, out);
@@ -300,15 +313,21 @@ template <class T>
 __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
   if (S.sc->conv) return;
   using A = typename Acc<T>::type;
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   A v[2] = {(A)0, (A)0};
-  if (ic < S.neq) {
-    int ii, jj, kk;
-    decode(ic, S.M, S.N, ii, jj, kk);
-    const T y = spmv_c<T, T>(S.coefT, S.ksh, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
-    S.kt[ic] = y;
-    v[0] = (A)y * (A)S.ks[ic];
-    v[1] = (A)y * (A)y;
+  const T* __restrict__ sh = S.ksh;
+  const T* __restrict__ ss = S.ks;
+  T* __restrict__ tt = S.kt;
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (ic < S.neq) {
+      int ii, jj, kk;
+      decode(ic, S.M, S.N, ii, jj, kk);
+      const T y = spmv_c<T, T>(S.coefT, sh, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
+      tt[ic] = y;
+      v[0] += (A)y * (A)ss[ic];
+      v[1] += (A)y * (A)y;
+    }
   }
   double out[2];
   block_sum_t<2, A>(v, out);
@@ -323,15 +342,25 @@ template <class T>
 __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S) {
   if (S.sc->conv) return;
   using A = typename Acc<T>::type;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const T alpha = (T)S.sc->alpha, omega = (T)S.sc->omega;
   A v[2] = {(A)0, (A)0};
-  if (t < S.neq) {
-    S.kx[t] = S.kx[t] + alpha * S.kph[t] + omega * S.ksh[t];
-    const T r = S.ks[t] - omega * S.kt[t];
-    S.kr[t] = r;
-    v[0] = (A)S.kr0[t] * (A)r;
-    v[1] = (A)r * (A)r;
+  T* __restrict__ x = S.kx;
+  T* __restrict__ rr = S.kr;
+  const T* __restrict__ ph = S.kph;
+  const T* __restrict__ sh = S.ksh;
+  const T* __restrict__ ss = S.ks;
+  const T* __restrict__ tt = S.kt;
+  const T* __restrict__ r0 = S.kr0;
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int t = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (t < S.neq) {
+      x[t] = x[t] + alpha * ph[t] + omega * sh[t];
+      const T r = ss[t] - omega * tt[t];
+      rr[t] = r;
+      v[0] += (A)r0[t] * (A)r;
+      v[1] += (A)r * (A)r;
+    }
   }
   double out[2];
   block_sum_t<2, A>(v, out);

@@ -82,6 +82,49 @@ __device__ __forceinline__ T level_apply(const MGL<T>& L, const T* __restrict__ 
   return s;
 }
 
+// Neighbour value for the first post-smoothing half-sweep: x + w * P x_c,
+// the coarse-grid correction applied on the fly (the swept colour recomputes
+// its own columns, the other colour is corrected by the next half-sweep).
+template <class T>
+struct Prolong {
+  const T* xc;    // coarse solution (nullptr: plain x)
+  T w;
+  int rx, ry, Mc, MNc, M, MN;
+  __device__ __forceinline__ T operator()(const T* __restrict__ x, int ic) const {
+    if (!xc) return x[ic];
+    const int kk = ic / MN, r = ic - kk * MN, jj = r / M, ii = r - jj * M;
+    return x[ic] + w * xc[ii / rx + Mc * (jj / ry) + MNc * kk];
+  }
+};
+
+template <class T>
+__device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__ x, const Prolong<T>& P, int ic,
+                                          int ii, int jj, int kk) {
+  const int M = L.M, MN = L.M * L.N, n = L.n;
+  const bool im = ii > 0, ip = ii < L.M - 1, jm = jj > 0, jp = jj < L.N - 1, km = kk > 0, kp = kk < L.K - 1;
+  T s = (T)0;
+  if (ip) s += cx_p(L, ic) * P(x, ic + 1);
+  if (im) s += cx_m(L, ic) * P(x, ic - 1);
+  if (jp) s += cy_p(L, ic) * P(x, ic + M);
+  if (jm) s += cy_m(L, ic) * P(x, ic - M);
+  const T c4 = L.coef[3 * n + ic], c5 = L.coef[4 * n + ic], c7 = L.coef[5 * n + ic], c8 = L.coef[6 * n + ic];
+  if (kp) {
+    const int u = ic + MN;
+    if (ip) s += c7 * P(x, u + 1);
+    if (im) s += c5 * P(x, u - 1);
+    if (jp) s += c8 * P(x, u + M);
+    if (jm) s += c4 * P(x, u - M);
+  }
+  if (km) {
+    const int d = ic - MN;
+    if (ip) s -= c7 * P(x, d + 1);
+    if (im) s -= c5 * P(x, d - 1);
+    if (jp) s -= c8 * P(x, d + M);
+    if (jm) s -= c4 * P(x, d - M);
+  }
+  return s;
+}
+
 // red-black line Gauss-Seidel half-sweep: columns with (ii+jj)%2 == color
 template <class T>
 __global__ void __launch_bounds__(128) k_mg_smooth(MGL<T> L, const DevScal* sc, int color, int zero_x) {
@@ -145,8 +188,9 @@ __global__ void __launch_bounds__(128) k_mg_smooth(MGL<T> L, const DevScal* sc, 
 // up to 32 levels (blockDim = 32 x min(K,32)); every thread forms the line
 // right-hand sides of its (column, level) cells -- loads coalesced along the
 // columns -- into shared memory, then one warp runs the Thomas sweeps there.
-template <class T>
-__global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal* sc, int color, int zero_x) {
+template <class T, bool kProlong>
+__global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal* sc, int color, int zero_x,
+                                                        Prolong<T> P) {
   if (sc->conv) return;
   extern __shared__ unsigned char smem_raw[];
   T* sh = reinterpret_cast<T*>(smem_raw);
@@ -168,7 +212,9 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
     T rhs = (T)0, a = (T)0, inv = (T)0, cp = (T)0;
     if (valid) {
       const int ic = col + MN * k;
-      rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, L.x, ic, ii, jj, k));
+      T off = (T)0;
+      if (!zero_x) off = kProlong ? off_column_p(L, L.x, P, ic, ii, jj, k) : off_column(L, L.x, ic, ii, jj, k);
+      rhs = L.b[ic] - off;
       a = k > 0 ? L.coef[2 * n + ic] : (T)0;
       inv = L.linv[ic];
       cp = L.lcp[ic];
@@ -190,6 +236,113 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
   for (int k = K - 2; k >= 0; --k) {
     z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
     L.x[col + MN * k] = z;
+  }
+}
+
+// One thread block runs the V-cycle over the small coarse levels lo..nl-1
+// (1024 threads = 32 columns x 32 levels per batch; __syncthreads between
+// phases), replacing dozens of tiny launches.
+constexpr int kCtaLevels = 8;
+template <class T>
+struct MGSet { MGL<T> L[kCtaLevels]; };
+
+template <class T>
+__device__ void cta_half_sweep(const MGL<T>& L, int color, int zero_x, const Prolong<T>& P, T* sh) {
+  const int K = L.K, M = L.M, MN = L.M * L.N, n = L.n;
+  T* s_rhs = sh;
+  T* s_a = sh + K * 32;
+  T* s_inv = sh + 2 * K * 32;
+  T* s_cp = sh + 3 * K * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5, by = blockDim.x >> 5;
+  const int ncol_row0 = (M + 1 - color) / 2, ncol_row1 = (M + color) / 2, pair = ncol_row0 + ncol_row1;
+  const int ncols = pair * ((L.N + 1) / 2);
+  for (int base = 0; base < ncols; base += 32) {
+    const int t = base + tx;
+    const int jp2 = t / pair, rem = t % pair;
+    int jj, ii;
+    if (rem < ncol_row0) { jj = 2 * jp2; ii = 2 * rem + color; }
+    else { jj = 2 * jp2 + 1; ii = 2 * (rem - ncol_row0) + (1 - color); }
+    const bool valid = t < ncols && jj < L.N && ii < M;
+    const int col = ii + M * jj;
+    for (int k = ty; k < K; k += by) {
+      T rhs = (T)0, a = (T)0, inv = (T)0, cp = (T)0;
+      if (valid) {
+        const int ic = col + MN * k;
+        rhs = L.b[ic] - (zero_x ? (T)0 : off_column_p(L, L.x, P, ic, ii, jj, k));
+        a = k > 0 ? L.coef[2 * n + ic] : (T)0;
+        inv = L.linv[ic];
+        cp = L.lcp[ic];
+      }
+      s_rhs[k * 32 + tx] = rhs;
+      s_a[k * 32 + tx] = a;
+      s_inv[k * 32 + tx] = inv;
+      s_cp[k * 32 + tx] = cp;
+    }
+    __syncthreads();
+    if (ty == 0 && valid) {
+      T prev = (T)0;
+      for (int k = 0; k < K; ++k) {
+        prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
+        s_rhs[k * 32 + tx] = prev;
+      }
+      T z = prev;
+      L.x[col + MN * (K - 1)] = z;
+      for (int k = K - 2; k >= 0; --k) {
+        z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
+        L.x[col + MN * k] = z;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__device__ void cta_restrict(const MGL<T>& F, const MGL<T>& C) {
+  for (int ic = threadIdx.x; ic < C.n; ic += blockDim.x) {
+    int I, J, k;
+    decode(ic, C.M, C.N, I, J, k);
+    T acc = (T)0;
+    for (int b = 0; b < F.ry; ++b) {
+      const int j = J * F.ry + b;
+      if (j >= F.N) break;
+      for (int a = 0; a < F.rx; ++a) {
+        const int i = I * F.rx + a;
+        if (i >= F.M) break;
+        const int f = i + F.M * (j + F.N * k);
+        acc += F.b[f] - level_apply(F, F.x, f, i, j, k);
+      }
+    }
+    C.b[ic] = acc;
+    C.x[ic] = (T)0;
+  }
+  __syncthreads();
+}
+
+// V-cycle over levels set.L[0..nl-1] (set.L[0] holds its right-hand side in b;
+// its x is the output); `coarse_sweeps` red-black sweeps on the last level.
+template <class T>
+__global__ void __launch_bounds__(1024) k_mg_cta_cycle(MGSet<T> set, int nl, const DevScal* sc, T w,
+                                                       int coarse_sweeps) {
+  if (sc->conv) return;
+  extern __shared__ unsigned char smem_raw[];
+  T* sh = reinterpret_cast<T*>(smem_raw);
+  const Prolong<T> none{nullptr, (T)0, 1, 1, 1, 1, 1, 1};
+  for (int l = 0; l < nl - 1; ++l) {
+    cta_half_sweep(set.L[l], 0, 1, none, sh);
+    cta_half_sweep(set.L[l], 1, 0, none, sh);
+    cta_restrict(set.L[l], set.L[l + 1]);
+  }
+  const MGL<T>& cl = set.L[nl - 1];
+  for (int s = 0; s < coarse_sweeps; ++s) {
+    cta_half_sweep(cl, 0, s == 0 ? 1 : 0, none, sh);
+    cta_half_sweep(cl, 1, 0, none, sh);
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    const MGL<T>& F = set.L[l];
+    const MGL<T>& C = set.L[l + 1];
+    const Prolong<T> pr{C.x, w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N};
+    cta_half_sweep(F, 1, 0, pr, sh);
+    cta_half_sweep(F, 0, 0, none, sh);
   }
 }
 

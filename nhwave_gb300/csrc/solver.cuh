@@ -279,7 +279,11 @@ class Solver final : public SolverBase {
     mg[0].coef = S.coefT; mg[0].cxr = nullptr; mg[0].cyr = nullptr;
     mg[0].lcp = S.lcp; mg[0].linv = S.linv;
     for (auto& L : mg) { L.cxx = (T)S.cxx; L.cyy = (T)S.cyy; }
-    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(T) * 4 * 32 * 64)));
+    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(T) * 4 * 32 * 64)));
+    NHW_CU(cudaFuncSetAttribute(k_mg_cta_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(T) * 4 * 32 * 64)));
     NHW_CU(cudaMallocHost((void**)&h_sc, sizeof(DevScal)));
     NHW_CU(cudaMallocHost((void**)&h_out, sizeof(double) * 8));
@@ -305,7 +309,7 @@ class Solver final : public SolverBase {
     });
   }
   template <class Op> void cells(Op op) { box(op, S.M, S.N, S.K, S.IB, S.JB, S.KB); }
-  unsigned red_blocks() const { return cdiv(S.neq, 256); }
+  unsigned red_blocks() const { return cdiv(S.neq, 256 * kCPT); }
 
   int check() {
     cudaError_t e = cudaGetLastError();
@@ -636,14 +640,14 @@ class Solver final : public SolverBase {
   void one_iteration() {
     const unsigned cb = cdiv((long long)S.M * S.N, 128);
     if (use_mg) {
-      L("bicg_p", [&] { k_bicg_p_cell<T><<<red_blocks(), 256, 0, st>>>(S); });
+      L("bicg_p", [&] { k_bicg_p_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
       vcycle(S.kp, S.kph);
     } else {
       L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
     }
     L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
     if (use_mg) {
-      L("bicg_s", [&] { k_bicg_s_cell<T><<<red_blocks(), 256, 0, st>>>(S); });
+      L("bicg_s", [&] { k_bicg_s_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
       vcycle(S.ks, S.ksh);
     } else {
       L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
@@ -652,7 +656,8 @@ class Solver final : public SolverBase {
     L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S); });
   }
   // multigrid V-cycle: x ~= A^-1 b on level 0
-  void smooth(const MGL<T>& Lv, int color, int zero_x, int level = 0) {
+  static constexpr int kCtaColumns = 64;    // levels up to this many columns run in one block
+  void smooth(const MGL<T>& Lv, int color, int zero_x, int level, const Prolong<T>& P) {
     static const char* names[] = {"mg_smooth_l0", "mg_smooth_l1", "mg_smooth_l2", "mg_smooth_l3",
                                   "mg_smooth_l4", "mg_smooth_l5", "mg_smooth_l6", "mg_smooth_l7+"};
     const int pair = (Lv.M + 1 - color) / 2 + (Lv.M + color) / 2;
@@ -660,29 +665,42 @@ class Solver final : public SolverBase {
     const int by = std::min(Lv.K, 32);
     const size_t shm = sizeof(T) * 4 * 32 * Lv.K;
     L(names[level < 7 ? level : 7], [&] {
-      k_mg_smooth_blk<T><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x);
+      if (P.xc)
+        k_mg_smooth_blk<T, true><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P);
+      else
+        k_mg_smooth_blk<T, false><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P);
     });
   }
   void vcycle(const T* b, T* x) {
     mg[0].b = (T*)b;
     mg[0].x = x;
     const int nl = (int)mg.size();
-    for (int l = 0; l < nl - 1; ++l) {
-      smooth(mg[l], 0, 1, l);
-      smooth(mg[l], 1, 0, l);
+    // first level handled by the single-block cycle
+    int lc = 0;
+    while (lc < nl && (long long)mg[lc].M * mg[lc].N > kCtaColumns) ++lc;
+    if (nl - lc > kCtaLevels) lc = nl - kCtaLevels;
+    const Prolong<T> none{nullptr, (T)0, 1, 1, 1, 1, 1, 1};
+    for (int l = 0; l < lc; ++l) {
+      smooth(mg[l], 0, 1, l, none);
+      smooth(mg[l], 1, 0, l, none);
       MGL<T> f = mg[l], c = mg[l + 1];
       L("mg_restrict", [&] { k_mg_restrict<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, c, S.sc); });
     }
-    const MGL<T>& cl = mg[nl - 1];
-    for (int s2 = 0; s2 < (nl > 1 ? mg_coarse_sweeps : 1); ++s2) {
-      smooth(cl, 0, s2 == 0 ? 1 : 0, nl - 1);
-      smooth(cl, 1, 0, nl - 1);
+    if (lc < nl) {
+      MGSet<T> set{};
+      for (int l = lc; l < nl; ++l) set.L[l - lc] = mg[l];
+      const int cnt = nl - lc;
+      const size_t shm = sizeof(T) * 4 * 32 * S.K;
+      L("mg_coarse_cycle", [&] {
+        k_mg_cta_cycle<T><<<1, 1024, shm, st>>>(set, cnt, S.sc, mg_w, mg_coarse_sweeps);
+      });
     }
-    for (int l = nl - 2; l >= 0; --l) {
-      MGL<T> f = mg[l], c = mg[l + 1];
-      L("mg_prolong", [&] { k_mg_prolong<T><<<cdiv(f.n, 256), 256, 0, st>>>(f, c, S.sc, mg_w); });
-      smooth(mg[l], 1, 0, l);
-      smooth(mg[l], 0, 0, l);
+    for (int l = lc - 1; l >= 0; --l) {
+      const MGL<T>& f = mg[l];
+      const MGL<T>& c = mg[l + 1];
+      const Prolong<T> pr{c.x, mg_w, f.rx, f.ry, c.M, c.M * c.N, f.M, f.M * f.N};
+      smooth(f, 1, 0, l, pr);
+      smooth(f, 0, 0, l, none);
     }
   }
 
