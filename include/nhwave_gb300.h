@@ -188,11 +188,18 @@ int nhw_fluxes(nhw_handle* h);
 int nhw_eval_duvw(nhw_handle* h, int32_t istep);
 int nhw_sponge_damping(nhw_handle* h);
 
-/* One full time step (estimate_dt ... last RK stage), replayed from a CUDA
- * graph after the first call.  Writes TIME, dt and RUN_STEP if non-NULL. */
+/* One full time step (estimate_dt ... last RK stage).  The first call
+ * captures the step into a CUDA graph whose pressure-solve loops run on the
+ * device (conditional nodes); later calls replay it, with one host round trip
+ * per call.  Returns the step's first non-OK pressure status, or DT_MIN.
+ * Writes TIME, dt and RUN_STEP if non-NULL. */
 int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step);
 /* Up to nsteps steps while TIME < TOTAL_TIME and RUN_STEP < SIM_STEPS (the
- * reference's do-while condition, src/nhwave.F:119). */
+ * reference's do-while condition, src/nhwave.F:119).  The test runs on the
+ * device in a gated copy of the step graph, so steps go out in batches
+ * without a host round trip each.  Stops at DT_MIN or at a step whose
+ * pressure solve went non-finite; ITMAX without convergence does not stop
+ * it.  *steps_done counts the steps taken (plus the one that hit DT_MIN). */
 int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done);
 
 /* FP64 device reduction of statistics' MassVolume = sum(D*dx*dy). */

@@ -120,16 +120,8 @@ int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step) {
 
 int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done) {
   NHW_GUARD(h);
-  int done = 0, rc = NHW_OK;
-  nhw_scalars sc;
-  for (; done < nsteps; ++done) {
-    rc = h->s->get_scalars(&sc);
-    if (rc) break;
-    if (!(sc.time < h->s->total_time() && sc.run_step < h->s->sim_steps())) break;
-    rc = h->s->step();
-    if (rc != NHW_OK && rc != NHW_ERR_KRYLOV_NOCONV) { ++done; break; }
-    rc = NHW_OK;
-  }
+  int done = 0;
+  const int rc = nsteps > 0 ? h->s->run(nsteps, &done) : NHW_OK;
   if (steps_done) *steps_done = done;
   return rc;
 }

@@ -746,7 +746,9 @@ struct OpPFromX {
   static constexpr const char* kName = "p_from_x";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
-    S.P[i3(S, i, j, k)] = S.xsol64[ic_of(S, i, j, k)];
+    const int ic = ic_of(S, i, j, k);
+    if (S.sc->zero_x) S.xsol64[ic] = 0.0;   // b = 0: HYPRE returns x = 0
+    S.P[i3(S, i, j, k)] = S.xsol64[ic];
   }
 };
 struct OpXFromP {
@@ -999,18 +1001,34 @@ __global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
   if ((threadIdx.x & 31) == 0) atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
 }
 template <class T>
-__global__ void k_dt_finalize(Dev<T> S) {
+__global__ void k_dt_finalize(Dev<T> S, int gated) {
   DevScal* sc = S.sc;
   const double tmp2 = __longlong_as_double((long long)sc->dtmin_bits);
   sc->dtmin_bits = (unsigned long long)__double_as_longlong(kLarge);
-  sc->dt_old = sc->dt;
-  const double dt_growth = (double)1.05f * sc->dt_old;
-  const double dt_courant = S.cfl * tmp2;
-  double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), kLarge), S.dt_max);
-  sc->dt = dt;
-  if (dt < S.dt_min) { sc->status = 5; return; }
-  sc->time = sc->time + dt;
-  sc->run_step = sc->run_step + 1;
+  // A dt below DT_MIN stops the run for good (src/nhwave.F:3840-3850 stops
+  // the program).  The gated form also holds the step back once the run is
+  // over (the main loop's TIME < TOTAL_TIME and RUN_STEP < SIM_STEPS test,
+  // src/nhwave.F:119) or the previous step's pressure solve went non-finite.
+  bool go = sc->status != 5;
+  if (go && gated)
+    go = sc->time < S.total_time && sc->run_step < S.sim_steps && sc->step_status != 7;
+  if (go) {
+    sc->dt_old = sc->dt;
+    const double dt_growth = (double)1.05f * sc->dt_old;
+    const double dt_courant = S.cfl * tmp2;
+    const double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), kLarge), S.dt_max);
+    sc->dt = dt;
+    if (dt < S.dt_min) {
+      sc->status = 5;
+      if (5 > sc->worst) sc->worst = 5;
+      go = false;
+    } else {
+      sc->time = sc->time + dt;
+      sc->run_step = sc->run_step + 1;
+      sc->step_status = 0;
+    }
+  }
+  if (S.graph_mode) cudaGraphSetConditional(S.h_go, go ? 1u : 0u);
 }
 
 // =========================================================================

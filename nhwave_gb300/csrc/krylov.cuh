@@ -133,8 +133,24 @@ __device__ __forceinline__ void decode(int ic, int M, int N, int& ii, int& jj, i
 }
 
 // ------------------------------------------------------------------ FP64 residual
-// r64 = b - A64 x64; inner right-hand side rT = (T) r64; ||r64||, ||b||
+// Sets the condition of a conditional graph node from the finalising thread;
+// eagerly launched kernels (graph_mode 0) leave handles alone.
 template <class T>
+__device__ __forceinline__ void set_cond(const Dev<T>& S, unsigned long long h, bool v) {
+  if (S.graph_mode) cudaGraphSetConditional(h, v ? 1u : 0u);
+}
+
+// Status codes of the C interface that the device writes.
+constexpr int kStKrylovNoconv = 6, kStNaN = 7;
+
+// r64 = b - A64 x64; inner right-hand side rT = (T) r64; ||r64||, ||b||.
+// The last block then makes the refinement decision of the outer loop (the
+// HYPRE stopping test ||r||/||b|| <= TOL, src/pressure.F:225-258 calls the
+// solver with TOL and ITMAX): stop on convergence, on b = 0 (the solution is
+// then x = 0), on a non-finite residual or an inner breakdown flagged as NaN,
+// or when ITMAX inner iterations or the sweep cap are used up; otherwise it
+// sets the next inner tolerance and iteration budget.  kFirst opens a solve.
+template <class T, bool kFirst>
 __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
   const int M = S.M, N = S.N, K = S.K;
   const size_t n = (size_t)S.neq;
@@ -157,14 +173,45 @@ __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
   block_sum_t<2, double>(v, out);
   finish_reduce<2>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
+    if (kFirst) {
+      sc->ir_count = 0;
+      sc->inner_total = 0;
+      sc->pstat = 0;
+      sc->zero_x = 0;
+      sc->conv = 0;
+      sc->solves = sc->solves + 1;
+    }
     sc->bnorm = sqrt(a[1]);
-    sc->relres64 = sc->bnorm > 0.0 ? sqrt(a[0]) / sc->bnorm : 0.0;
+    const double rel = sc->bnorm > 0.0 ? sqrt(a[0]) / sc->bnorm : 0.0;
+    sc->relres64 = rel;
+    int go = 0, st = 0;
+    if (sc->conv == 5 || !(rel == rel)) st = kStNaN;
+    else if (sc->bnorm == 0.0) sc->zero_x = 1;
+    else if (rel <= S2.tol) {}
+    else if (sc->ir_count >= S2.max_ir || sc->inner_total >= S2.itmax) st = kStKrylovNoconv;
+    else {
+      double tol_in = 0.5 * S2.tol / rel;
+      if (tol_in < S2.tol_floor) tol_in = S2.tol_floor;
+      sc->tol_in = tol_in;
+      sc->itmax_in = S2.itmax - sc->inner_total;
+      sc->ir_count = sc->ir_count + 1;
+      sc->total_ir = sc->total_ir + 1;
+      go = 1;
+    }
+    if (st) {
+      sc->pstat = st;
+      if (sc->step_status == 0) sc->step_status = st;
+      if (st > sc->worst) sc->worst = st;
+    }
+    sc->ir_go = go;
+    set_cond(S2, S2.h_ir, go != 0);
   });
 }
 
 // start of an inner solve from c = 0: r = r0 = rT, p = v = 0, rho = (r, r)
+// (tolerance and iteration budget come from the preceding k_res64)
 template <class T>
-__global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S, double tol_in, int itmax_in) {
+__global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S) {
   using A = typename Acc<T>::type;
   A v[1] = {(A)0};
 #pragma unroll
@@ -181,10 +228,8 @@ __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S, double tol_in, int 
   }
   double out[1];
   block_sum_t<1, A>(v, out);
-  finish_reduce<1>(S, out, [tol_in, itmax_in] __device__(const Dev<T>& S2, double* a) {
+  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
     DevScal* sc = S2.sc;
-    sc->tol_in = tol_in;
-    sc->itmax_in = itmax_in;
     sc->rho = a[0];
     sc->red[0] = sqrt(a[0]);
     sc->alpha = 1.0;
@@ -193,6 +238,7 @@ __global__ void __launch_bounds__(256) k_bicg_init(Dev<T> S, double tol_in, int 
     sc->it = 0;
     sc->relres = 1.0;
     sc->conv = (a[0] == 0.0) ? 1 : 0;
+    set_cond(S2, S2.h_inner, sc->conv == 0);
   });
 }
 
@@ -337,10 +383,15 @@ __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
   });
 }
 
-// x += alpha ph + omega sh; r = s - omega t; convergence test
+// x += alpha ph + omega sh; r = s - omega t; convergence test.  Ends the
+// iteration loop of a captured graph: every path leaves the loop condition
+// set, and `it` grows by one per pass, so the loop stops by itmax_in.
 template <class T>
 __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S) {
-  if (S.sc->conv) return;
+  if (S.sc->conv) {   // stopped earlier in this pass (breakdown in k_bicg_v)
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(S, S.h_inner, false);
+    return;
+  }
   using A = typename Acc<T>::type;
   const T alpha = (T)S.sc->alpha, omega = (T)S.sc->omega;
   A v[2] = {(A)0, (A)0};
@@ -370,14 +421,20 @@ __global__ void __launch_bounds__(256) k_bicg_xr(Dev<T> S) {
     const int itmax_in = sc->itmax_in;
     sc->it = sc->it + 1;
     sc->total_it = sc->total_it + 1;
+    sc->inner_total = sc->inner_total + 1;
     const double rel = sc->red[0] > 0.0 ? sqrt(a[1]) / sc->red[0] : 0.0;
     sc->relres = rel;
-    if (!(rel == rel)) { sc->conv = 5; return; }
-    if (rel <= tol_in) { sc->conv = 1; return; }
-    if (sc->it >= itmax_in) { sc->conv = 4; return; }
-    if (a[0] == 0.0 || sc->omega == 0.0) { sc->conv = 2; return; }
-    sc->beta = (a[0] / sc->rho) * (sc->alpha / sc->omega);
-    sc->rho = a[0];
+    int conv = 0;
+    if (!(rel == rel)) conv = 5;
+    else if (rel <= tol_in) conv = 1;
+    else if (sc->it >= itmax_in) conv = 4;
+    else if (a[0] == 0.0 || sc->omega == 0.0) conv = 2;
+    else {
+      sc->beta = (a[0] / sc->rho) * (sc->alpha / sc->omega);
+      sc->rho = a[0];
+    }
+    sc->conv = conv;
+    set_cond(S2, S2.h_inner, conv == 0);
   });
 }
 

@@ -54,6 +54,7 @@ class SolverBase {
   virtual int sim_steps() const = 0;
   virtual int bind() = 0;
   virtual int run_timed(int nsteps, double* ms) = 0;
+  virtual int run(int nsteps, int* done) = 0;
   virtual int profile(int on) = 0;
   virtual int profile_report(char* buf, int len) = 0;
 };
@@ -104,8 +105,6 @@ class Solver final : public SolverBase {
   size_t stage_elems = 0;
   size_t n2 = 0, n3 = 0;
   bool ready = false;
-  int last_inner = 0, last_refine = 0;
-  int64_t solves = 0;
   int it_order = 3;
   static constexpr bool kFP32 = sizeof(T) == 4;
   // launch accounting and optional per-kernel CUDA-event timing
@@ -133,6 +132,7 @@ class Solver final : public SolverBase {
   template <class F>
   void L(const char* name, F f) {
     ++launches;
+    if (capturing) ++cap_counts[cap_level];
     if (!prof_on) { f(); return; }
     cudaEvent_t a = take_event(), b = take_event();
     cudaEventRecord(a, st);
@@ -145,6 +145,9 @@ class Solver final : public SolverBase {
     if (st) cudaStreamSynchronize(st);
     for (auto e : evpool) cudaEventDestroy(e);
     for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+    drop_step_graphs();
+    for (auto c : cap_st)
+      if (c) cudaStreamDestroy(c);
     if (ev_run0) cudaEventDestroy(ev_run0);
     if (ev_run1) cudaEventDestroy(ev_run1);
     if (arena) cudaFree(arena);
@@ -175,6 +178,11 @@ class Solver final : public SolverBase {
     S.dt_min = p.dt_min; S.dt_max = p.dt_max;
     S.fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);
     S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
+    S.tol = p.tol; S.itmax = p.itmax;
+    S.max_ir = kFP32 ? 12 : 30;
+    S.tol_floor = kFP32 ? 2e-5 : 0.0;   // FP32 inner solves cannot go much below this
+    S.total_time = p.total_time; S.sim_steps = p.sim_steps;
+    S.graph_mode = 0; S.h_go = S.h_ir = S.h_inner = 0;
     S.non_hydro = p.non_hydro; S.sponge_on = p.sponge_on;
     S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
     S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
@@ -417,6 +425,7 @@ class Solver final : public SolverBase {
 
   // ----------------------------------------------------------------- setup
   int setup(const double* depth, const double* eta0, const double* uvw0) override {
+    drop_step_graphs();   // a new set-up changes captured kernel arguments
     HostInit h;
     int rc = host_setup(p, depth, eta0, uvw0, h);
     if (rc) return rc;
@@ -494,9 +503,9 @@ class Solver final : public SolverBase {
     if (rc) return rc;
     std::memset(o, 0, sizeof(*o));
     o->time = h_sc->time; o->dt = h_sc->dt; o->dt_old = h_sc->dt_old; o->run_step = h_sc->run_step;
-    o->last_krylov_iters = last_inner; o->total_krylov_iters = h_sc->total_it;
-    o->poisson_solves = solves; o->last_rel_residual = h_sc->relres64;
-    o->last_refinements = last_refine; o->status = h_sc->status;
+    o->last_krylov_iters = h_sc->inner_total; o->total_krylov_iters = h_sc->total_it;
+    o->poisson_solves = h_sc->solves; o->last_rel_residual = h_sc->relres64;
+    o->last_refinements = h_sc->ir_count; o->status = h_sc->status;
     return NHW_OK;
   }
   int set_time(double t, double dt, int rs) override {
@@ -510,7 +519,7 @@ class Solver final : public SolverBase {
   // -------------------------------------------------- reference subroutines
   int estimate_dt() override {
     L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
-    L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S); });
+    L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, 0); });
     int rc = pull_scalars();
     if (rc) return rc;
     if (h_sc->status == NHW_ERR_DT_MIN) return NHW_ERR_DT_MIN;
@@ -568,24 +577,28 @@ class Solver final : public SolverBase {
         });
         L("mg_factor", [&] { k_mg_factor<T><<<cdiv((long long)c.M * c.N, 256), 256, 0, st>>>(c, (T*)c.lcp, (T*)c.linv); });
       }
-    const int max_ir = kFP32 ? 12 : 30;
-    int inner_total = 0, ir = 0, status = NHW_OK;
-    for (ir = 0; ir <= max_ir; ++ir) {
-      L("res64", [&] { k_res64<T><<<red_blocks(), 256, 0, st>>>(S); });
-      int rc = pull_scalars();
-      if (rc) return rc;
-      const double rel = h_sc->relres64;
-      if (!(rel == rel)) { status = NHW_ERR_NAN; break; }
-      if (h_sc->bnorm == 0.0) {  // HYPRE returns x = 0 for b = 0
-        NHW_CU(cudaMemsetAsync(S.xsol64, 0, sizeof(double) * S.neq, st));
-        break;
-      }
-      if (rel <= p.tol) break;
-      if (ir == max_ir || inner_total >= p.itmax) { status = NHW_ERR_KRYLOV_NOCONV; break; }
-      double tol_in = 0.5 * p.tol / rel;
-      if (kFP32 && tol_in < 2e-5) tol_in = 2e-5;
-      const int itmax_in = p.itmax - inner_total;
-      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S, tol_in, itmax_in); });
+    if (capturing) {
+      ++cap_solves;
+      // device-side loops: refinement sweeps around BiCGSTAB iterations
+      S.h_ir = new_handle();      // before the kernels that set them are captured
+      S.h_inner = new_handle();
+      L("res64", [&] { k_res64<T, true><<<red_blocks(), 256, 0, st>>>(S); });
+      cond_node(S.h_ir, cudaGraphCondTypeWhile, [&] {
+        L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+        cond_node(S.h_inner, cudaGraphCondTypeWhile, [&] { one_iteration(); }, 2);
+        L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+        L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
+      }, 1);
+      cells(OpPFromX{});
+      allcols(OpPGhost{});
+      return NHW_OK;
+    }
+    // host-driven loops over the same device-side decisions
+    L("res64", [&] { k_res64<T, true><<<red_blocks(), 256, 0, st>>>(S); });
+    int rc = pull_scalars();
+    if (rc) return rc;
+    while (h_sc->ir_go) {
+      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
       int chunk = 4;
       while (true) {
         rc = run_iterations(chunk);
@@ -595,16 +608,15 @@ class Solver final : public SolverBase {
         if (h_sc->conv != 0) break;
         if (chunk < 16) chunk *= 2;
       }
-      inner_total += h_sc->it;
       L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
-      if (h_sc->conv == 5) { status = NHW_ERR_NAN; break; }
+      L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
+      rc = pull_scalars();
+      if (rc) return rc;
     }
-    last_inner = inner_total;
-    last_refine = ir;
-    ++solves;
+    const int status = h_sc->pstat;
     cells(OpPFromX{});
     allcols(OpPGhost{});
-    int rc = check();
+    rc = check();
     return rc ? rc : status;
   }
   // `chunk` BiCGSTAB iterations; replayed from a captured CUDA graph unless the
@@ -729,13 +741,11 @@ class Solver final : public SolverBase {
     allcols(OpSponge{});
     return check();
   }
-  int step() override {
-    if (!ready) return NHW_ERR_STATE;
-    int rc = estimate_dt();
-    if (rc) return rc;
+  // everything of one time step after estimate_dt (src/nhwave.F:119-200)
+  int step_body() {
     if (S.slide) update_bathymetry();
     update_mask();
-    rc = update_vars();
+    int rc = update_vars();
     if (rc) return rc;
     int worst = NHW_OK;
     for (int s = 1; s <= it_order; ++s) {
@@ -749,14 +759,223 @@ class Solver final : public SolverBase {
     rc = check();
     return rc ? rc : worst;
   }
+  int step_eager() {
+    int rc = estimate_dt();
+    if (rc) return rc;
+    return step_body();
+  }
+
+  // ------------------------------------------------ whole-step CUDA graphs
+  // A time step is captured once into a graph whose loops run on the device:
+  // an IF node holds the step behind k_dt_finalize's decision, and in each
+  // pressure solve a WHILE node holds the refinement sweeps and a nested
+  // WHILE node the BiCGSTAB iterations; the kernels that end a reduction set
+  // the node conditions.  Stepping then needs no host round trip.
+  // sgraph[0] is the plain step, sgraph[1] the gated step used by run().
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long per_launch = 0, per_step = 0, per_sweep = 0, per_iter = 0;  // kernel launches
+  };
+  StepGraph sgraph[2];
+  bool capturing = false;
+  std::string cap_err;
+  cudaGraph_t cap_root = nullptr;
+  cudaStream_t cap_st[4] = {nullptr, nullptr, nullptr, nullptr};
+  int cap_depth = 0, cap_level = 3, cap_solves = 0;
+  long long cap_counts[4] = {0, 0, 0, 0};   // step body, sweep body, iteration body, outside
+  int64_t acc_step = 0, acc_ir = 0, acc_it = 0;   // counters at the last launch accounting
+
+  bool cap_ok(cudaError_t e, const char* what) {
+    if (e != cudaSuccess && cap_err.empty()) cap_err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  }
+  unsigned long long new_handle() {
+    cudaGraphConditionalHandle h = 0;
+    cap_ok(cudaGraphConditionalHandleCreate(&h, cap_root, 0, cudaGraphCondAssignDefault), "conditional handle");
+    return h;
+  }
+  // Appends a conditional node to the capture on `st` and captures `body`
+  // into its body graph on a stream of its own; `level` says which launch
+  // counter the body's kernels go to.
+  template <class F>
+  void cond_node(unsigned long long h, cudaGraphConditionalNodeType type, F body, int level) {
+    if (!cap_err.empty() || cap_depth >= 4) { cap_ok(cudaErrorNotSupported, "conditional nesting"); return; }
+    cudaStreamCaptureStatus cs;
+    unsigned long long id = 0;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    if (!cap_ok(cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, &ed, &nd), "capture info")) return;
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = type;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (!cap_ok(cudaGraphAddNode(&node, g, deps, ed, nd, &cp), "conditional node")) return;
+    if (!cap_ok(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+                "capture dependencies"))
+      return;
+    cudaStream_t outer = st;
+    const int outer_level = cap_level;
+    st = cap_st[cap_depth++];
+    cap_level = level;
+    if (cap_ok(cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeRelaxed), "body capture")) {
+      body();
+      cudaGraph_t gb = nullptr;
+      cap_ok(cudaStreamEndCapture(st, &gb), "body capture end");
+    }
+    st = outer;
+    --cap_depth;
+    cap_level = outer_level;
+  }
+  int capture_step(int gated) {
+    StepGraph& G = sgraph[gated];
+    if (G.exec) return NHW_OK;
+    if (!cap_st[0])
+      for (auto& c : cap_st) NHW_CU(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    NHW_CU(cudaGraphCreate(&g, 0));
+    cap_err.clear();
+    cap_root = g;
+    for (auto& c : cap_counts) c = 0;
+    cap_level = 3;
+    cap_solves = 0;
+    const Dev<T> saved = S;
+    const long long l0 = launches;
+    capturing = true;
+    S.graph_mode = 1;
+    S.h_go = new_handle();
+    if (cap_ok(cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+               "step capture")) {
+      L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+      L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, gated); });
+      cond_node(S.h_go, cudaGraphCondTypeIf, [&] { step_body(); }, 0);
+      cudaGraph_t gg = nullptr;
+      cap_ok(cudaStreamEndCapture(st, &gg), "step capture end");
+    }
+    capturing = false;
+    S = saved;
+    launches = l0;
+    cudaGetLastError();
+    if (cap_err.empty()) {
+      cudaGraphExec_t ex = nullptr;
+      if (cap_ok(cudaGraphInstantiate(&ex, g, 0), "step graph instantiate")) G.exec = ex;
+    }
+    cudaGraphDestroy(g);
+    if (!cap_err.empty()) {
+      set_last_error(cap_err);
+      return NHW_ERR_CUDA;
+    }
+    const long long ns = std::max(cap_solves, 1);
+    G.per_launch = cap_counts[3];
+    G.per_step = cap_counts[0];
+    G.per_sweep = cap_counts[1] / ns;
+    G.per_iter = cap_counts[2] / ns;
+    return NHW_OK;
+  }
+  void drop_step_graphs() {
+    for (auto& G : sgraph) {
+      if (G.exec) cudaGraphExecDestroy(G.exec);
+      G = StepGraph{};
+    }
+  }
+  // kernel launches of `n` graph launches, from the device counters
+  void account(const StepGraph& G, int n) {
+    launches += G.per_launch * n + G.per_step * (h_sc->run_step - acc_step) +
+                G.per_sweep * (h_sc->total_ir - acc_ir) + G.per_iter * (h_sc->total_it - acc_it);
+    snapshot();
+  }
+  void snapshot() {
+    acc_step = h_sc->run_step;
+    acc_ir = h_sc->total_ir;
+    acc_it = h_sc->total_it;
+  }
+  bool graph_path() const { return use_graphs && !prof_on; }
+
+  int step() override {
+    if (!ready) return NHW_ERR_STATE;
+    if (!graph_path()) return step_eager();
+    int rc = capture_step(0);
+    if (rc) return rc;
+    rc = pull_scalars();
+    if (rc) return rc;
+    snapshot();
+    NHW_CU(cudaGraphLaunch(sgraph[0].exec, st));
+    rc = pull_scalars();
+    if (rc) return rc;
+    account(sgraph[0], 1);
+    rc = check();
+    if (rc) return rc;
+    if (h_sc->status == NHW_ERR_DT_MIN) return NHW_ERR_DT_MIN;
+    return h_sc->step_status;
+  }
+  // nhw_run: steps while TIME < TOTAL_TIME and RUN_STEP < SIM_STEPS, at most
+  // nsteps; stops at DT_MIN or a non-finite pressure solve.  Graph launches
+  // go out in batches with one host round trip per batch.
+  int run(int nsteps, int* done_out) override {
+    if (!ready) return NHW_ERR_STATE;
+    int done = 0, rc = NHW_OK;
+    if (!graph_path()) {
+      for (; done < nsteps; ++done) {
+        rc = pull_scalars();
+        if (rc) break;
+        if (!(h_sc->time < p.total_time && h_sc->run_step < p.sim_steps)) break;
+        rc = step_eager();
+        if (rc != NHW_OK && rc != NHW_ERR_KRYLOV_NOCONV) { ++done; break; }
+        rc = NHW_OK;
+      }
+      if (done_out) *done_out = done;
+      return rc;
+    }
+    rc = capture_step(1);
+    if (rc) return rc;
+    NHW_CU(cudaMemsetAsync(&S.sc->step_status, 0, sizeof(int32_t), st));
+    rc = pull_scalars();
+    if (rc) return rc;
+    snapshot();
+    constexpr int kBatch = 16;
+    while (done < nsteps) {
+      const int64_t rs0 = h_sc->run_step;
+      const int b = std::min(kBatch, nsteps - done);
+      for (int q = 0; q < b; ++q) NHW_CU(cudaGraphLaunch(sgraph[1].exec, st));
+      rc = pull_scalars();
+      if (rc) break;
+      account(sgraph[1], b);
+      rc = check();
+      if (rc) break;
+      const int adv = (int)(h_sc->run_step - rs0);
+      done += adv;
+      if (h_sc->status == NHW_ERR_DT_MIN) { ++done; rc = NHW_ERR_DT_MIN; break; }
+      if (h_sc->step_status == NHW_ERR_NAN) { rc = NHW_ERR_NAN; break; }
+      if (adv < b) break;
+    }
+    if (done_out) *done_out = std::min(done, nsteps);
+    return rc;
+  }
   int run_timed(int nsteps, double* ms) override {
     if (!ready) return NHW_ERR_STATE;
     if (!ev_run0) { NHW_CU(cudaEventCreate(&ev_run0)); NHW_CU(cudaEventCreate(&ev_run1)); }
+    const bool graphs_on = graph_path();
+    if (graphs_on) {
+      int rc = capture_step(0);
+      if (rc) return rc;
+      NHW_CU(cudaMemsetAsync(&S.sc->worst, 0, sizeof(int32_t), st));
+      rc = pull_scalars();
+      if (rc) return rc;
+      snapshot();
+    }
     NHW_CU(cudaStreamSynchronize(st));
     NHW_CU(cudaEventRecord(ev_run0, st));
     int worst = NHW_OK;
     for (int n = 0; n < nsteps; ++n) {
-      int rc = step();
+      if (graphs_on) {
+        NHW_CU(cudaGraphLaunch(sgraph[0].exec, st));
+        continue;
+      }
+      int rc = step_eager();
       if (rc != NHW_OK && rc != NHW_ERR_KRYLOV_NOCONV) return rc;
       if (rc != NHW_OK) worst = rc;
     }
@@ -765,6 +984,15 @@ class Solver final : public SolverBase {
     float f = 0.f;
     NHW_CU(cudaEventElapsedTime(&f, ev_run0, ev_run1));
     *ms = (double)f;
+    if (graphs_on) {
+      int rc = pull_scalars();
+      if (rc) return rc;
+      account(sgraph[0], nsteps);
+      rc = check();
+      if (rc) return rc;
+      if (h_sc->status == NHW_ERR_DT_MIN) return NHW_ERR_DT_MIN;
+      worst = h_sc->worst;
+    }
     return worst;
   }
   int profile(int on) override {

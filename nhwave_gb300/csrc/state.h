@@ -46,6 +46,13 @@ struct DevScal {
   double tol_in;
   unsigned int counter[4];          // last-block-done counters
   int64_t total_it, solves;
+  // Poisson refinement state, decided on the device (so that a captured step
+  // can loop without the host): see k_res64 in krylov.cuh
+  int32_t ir_go, ir_count, inner_total, pstat, zero_x;
+  int32_t step_status;              // first non-OK Poisson status of the current step
+  int32_t worst;                    // largest status code since the host last cleared it
+  int32_t pad_;
+  int64_t total_ir;                 // refinement sweeps, cumulative
 };
 
 template <class T>
@@ -61,6 +68,14 @@ struct Dev {
   double cxx, cyy;                 // Poisson in-level couplings -1/dx^2, -1/dy^2
   int froude_on, non_hydro, sponge_on, it_order;
   int bc_x0, bc_xn, bc_y0, bc_yn;
+  double tol, tol_floor;          // outer Poisson tolerance (TOL); floor of the inner one
+  int itmax, max_ir;               // ITMAX over all inner iterations; refinement sweeps
+  double total_time;               // TOTAL_TIME and SIM_STEPS, for the gated run graph
+  int sim_steps;
+  // conditional-node handles of a captured step graph; graph_mode = 0 in
+  // eagerly launched kernels, which then never touch a handle
+  int graph_mode;
+  unsigned long long h_go, h_ir, h_inner;
   double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt)
   double alpha[3], beta[3];        // SSP-RK coefficients
   // wavemaker (INT_LIN / INT_SOL): host-computed constants

@@ -1,0 +1,100 @@
+"""GPU: the captured step graph (device-side refinement and iteration loops)
+against the same routines launched one by one through the C interface.
+
+Both paths run the same kernels in the same order on the same data, so every
+field must agree bit for bit, in both precisions.  Also checks the device-side
+run gate of nhw_run (TOTAL_TIME / SIM_STEPS) and the solver counters.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["D", "ETA", "HC", "U", "V", "W", "DU", "DV", "DW", "P", "OMEGA", "MASK"]
+
+
+def _scen(name, precision, **kw):
+    from nhwave_gb300 import lib, scenarios as S
+    p, d, e, u = S.make(name, precision=precision, seed=11, **kw)
+    p.tol = 1e-10 if precision == 0 else 1e-8
+    p.itmax = 5000
+    return lib.Scenario(p, d, e, u)
+
+
+def _routines(s):
+    """One time step as the reference's main loop calls it (src/nhwave.F:119-200)."""
+    s.estimate_dt()
+    if s.params.slide_type:
+        s.update_bathymetry()
+    s.update_mask()
+    s.update_vars()
+    for st in range(1, int(s.params.time_order) + 1):
+        s.source_terms()
+        s.fluxes()
+        s.eval_duvw(st)
+        if s.params.sponge_on:
+            s.sponge_damping()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"])
+def test_graph_step_equals_routines(name, precision, gpu_lib):
+    from nhwave_gb300 import fields as F
+    a = _scen(name, precision)
+    b = _scen(name, precision)
+    for n in range(3):
+        a.step()
+        _routines(b)
+        sa, sb = a.scalars(), b.scalars()
+        assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
+        assert sa.total_krylov_iters == sb.total_krylov_iters
+        assert sa.poisson_solves == sb.poisson_solves
+        for f in FIELDS:
+            fid = getattr(F, f)
+            x, y = a.get(fid), b.get(fid)
+            bad = np.argwhere(x != y)
+            assert bad.size == 0, f"step {n}: {f} differs at {bad[:4].tolist()}"
+
+
+def test_run_gate_sim_steps(gpu_lib):
+    from nhwave_gb300 import lib, scenarios as S
+    p, d, e, u = S.make("tiny_c1", precision=1, seed=11)
+    p.sim_steps = 5
+    p.total_time = 1e9
+    s = lib.Scenario(p, d, e, u)
+    assert s.run(40) == 5
+    assert s.scalars().run_step == 5
+    assert s.run(10) == 0          # the gate stays shut
+    assert s.scalars().run_step == 5
+
+
+def test_run_gate_total_time(gpu_lib):
+    from nhwave_gb300 import lib, scenarios as S
+    p, d, e, u = S.make("tiny_c2", precision=1, seed=11)
+    p.sim_steps = 100000
+    s0 = lib.Scenario(p, d, e, u)
+    s0.step()
+    dt = s0.scalars().dt
+    p.total_time = 3.5 * dt        # dt grows at most by 5 % a step
+    s = lib.Scenario(p, d, e, u)
+    done = s.run(50)
+    sc = s.scalars()
+    assert 2 <= done <= 4 and sc.run_step == done
+    assert sc.time >= p.total_time
+    # the same steps one call at a time stop at the same point
+    r = lib.Scenario(p, d, e, u)
+    n = 0
+    while r.scalars().time < p.total_time:
+        r.step()
+        n += 1
+    assert n == done and r.scalars().time == sc.time
+
+
+def test_solver_counters(gpu_lib):
+    s = _scen("tiny_c2", 1)
+    s.step()
+    sc = s.scalars()
+    assert sc.poisson_solves == 3
+    assert sc.last_krylov_iters > 0 and sc.total_krylov_iters >= sc.last_krylov_iters
+    assert sc.last_refinements >= 1
+    assert sc.last_rel_residual <= s.params.tol
