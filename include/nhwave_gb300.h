@@ -229,6 +229,38 @@ int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes);
 const char* nhw_status_string(int status);
 const char* nhw_last_error(void);
 
+/* ------------------------------------------------ allocation-free variant
+ * No counterpart in the reference: an addition for callers that cannot let a
+ * library allocate device memory.  Such a caller -- a host model whose fields
+ * live in device memory owned by the OpenACC / CUDA Fortran runtime or by a
+ * framework's caching allocator -- cannot use nhw_create, which allocates a
+ * scenario arena, because cudaMalloc and cudaFree synchronise the device
+ * (stalling its other streams) and draw on a memory budget it fixes up front.
+ *
+ * nhw_estimate_dt_noalloc computes what nhw_estimate_dt computes, the new
+ * time step dt = min(1.05 dt_old, CFL * Courant bound, DT_MAX), on the
+ * caller's device arrays, and writes it to dt_out[0] (device memory) on
+ * `stream` (a cudaStream_t; NULL = the default stream).  It returns once the
+ * work is queued.  U, V, W are (Mglob+4, Nglob+4, Kglob+4), D is
+ * (Mglob+4, Nglob+4) and dsig (Kglob+4), all FP64 in the reference's ghosted
+ * Fortran layout (column-major, two ghost cells a side).  The caller checks
+ * dt against DT_MIN.
+ *
+ * It allocates nothing.  Its reduction scratch is a fixed 65,792-byte device
+ * array inside the library, present on every GPU that loads the library
+ * until the process exits, which caps a call at Mglob*Nglob*Kglob <=
+ * 16,777,216 interior cells; larger grids are rejected with NHW_ERR_ARG and
+ * an nhw_last_error() message.  All calls share that one array: calls whose
+ * work overlaps on the GPU (different streams, threads or processes sharing
+ * a context) race and give wrong results, so order them, e.g. on one stream.
+ * The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress) and keeps it; make that first call before any
+ * stream capture begins. */
+int nhw_estimate_dt_noalloc(const double* U, const double* V, const double* W, const double* D,
+                            const double* dsig, int32_t Mglob, int32_t Nglob, int32_t Kglob, double dx,
+                            double dy, double cfl, double dt_old, double dt_max, double* dt_out,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,7 @@ Plain nvcc / g++ invocations, compiled in parallel, no build system:
   nhw_fp64.cu      nvcc --fmad=false                     (plain FP64 form)
   nhw_fp32.cu      nvcc --fmad=true                      (FP32+IR form)
   capi.cu          nvcc                                  (C-ABI)
+  noalloc.cu       nvcc --fmad=false                     (allocation-free entry point)
 """
 from __future__ import annotations
 
@@ -50,6 +51,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         ([nvcc, *common, "--fmad=true", "-c", os.path.join(CSRC, "nhw_fp32.cu"),
           "-o", os.path.join(OUT, "nhw_fp32.o")]),
         ([nvcc, *common, "-c", os.path.join(CSRC, "capi.cu"), "-o", os.path.join(OUT, "capi.o")]),
+        ([nvcc, *common, "--fmad=false", "-c", os.path.join(CSRC, "noalloc.cu"),
+          "-o", os.path.join(OUT, "noalloc.o")]),
     ]
     if verbose:
         jobs[1][1:1] = ["-Xptxas", "-v"]
@@ -67,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("libnhw_gpu build failed:\n" + "\n".join(errs))
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.check_call([nvcc, *ARCH, "-shared", "-o", tmp,
-                           *[os.path.join(OUT, o) for o in ("setup_host.o", "nhw_fp64.o", "nhw_fp32.o", "capi.o")]])
+                           *[os.path.join(OUT, o) for o in ("setup_host.o", "nhw_fp64.o", "nhw_fp32.o", "capi.o", "noalloc.o")]])
     os.replace(tmp, LIB)
     return LIB
 

@@ -31,6 +31,7 @@ EXPORTS = [
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
     "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
     "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
+    "nhw_estimate_dt_noalloc",
 ]
 
 
@@ -77,6 +78,7 @@ def load(path: str | None = None):
     L.nhw_run_timed.argtypes = [vp, i32, P(dbl)]
     L.nhw_profile.argtypes = [vp, i32]
     L.nhw_profile_report.argtypes = [vp, ctypes.c_char_p, i32]
+    L.nhw_estimate_dt_noalloc.argtypes = [vp] * 5 + [i32] * 3 + [dbl] * 5 + [vp, vp]
     L.nhw_status_string.argtypes = [ctypes.c_int]
     L.nhw_status_string.restype = ctypes.c_char_p
     L.nhw_last_error.argtypes = []
