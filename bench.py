@@ -187,6 +187,12 @@ ALG_BYTES_PER_CELL = {
     "flux_z": lambda s: 7 * s,       # read U,V,W,Omega; write Fz,Gz,Hz
     "stage_explicit": lambda s: 20 * s,  # read 11 fluxes, DU,DV,DW; write DU,DV,DW (+R1 sum)
     "omega_x": lambda s: 3 * s, "omega_y": lambda s: 3 * s,
+    # multigrid level 0, per unknown of the level: a half-sweep updates the
+    # columns of one colour (half the unknowns), each reading its 7 operator
+    # slots, b and x and writing x; restriction reads operator, x and b of
+    # every fine unknown and writes a quarter as many coarse right-hand sides
+    "mg_smooth_l0": lambda s: 5 * s,
+    "mg_restrict_l0": lambda s: 9.25 * s,
     "projection": lambda s: 7 * s, "ssp_combine": lambda s: 9 * s, "get_uvw": lambda s: 6 * s,
 }
 

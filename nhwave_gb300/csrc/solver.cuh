@@ -696,7 +696,9 @@ class Solver final : public SolverBase {
       smooth(mg[l], 0, 1, l, none);
       smooth(mg[l], 1, 0, l, none);
       MGL<T> f = mg[l], c = mg[l + 1];
-      L("mg_restrict", [&] { k_mg_restrict<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, c, S.sc); });
+      static const char* rnames[] = {"mg_restrict_l0", "mg_restrict_l1", "mg_restrict_l2", "mg_restrict_l3",
+                                     "mg_restrict_l4", "mg_restrict_l5", "mg_restrict_l6", "mg_restrict_l7+"};
+      L(rnames[l < 7 ? l : 7], [&] { k_mg_restrict<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, c, S.sc); });
     }
     if (lc < nl) {
       MGSet<T> set{};
