@@ -109,7 +109,11 @@ typedef struct nhw_params {
   int32_t precond;                         /* Poisson preconditioner: 0 multigrid V-cycle,
                                               1 vertical-line (tridiagonal) only     */
   float   mg_weight;                       /* multigrid coarse-correction weight (0: 1.0) */
-  int32_t reserved[5];
+  int32_t krylov_kernel;                   /* 0: one launch per solver phase, loops in
+                                              graph conditional nodes; 1: the whole solve
+                                              in one persistent cooperative launch (needs
+                                              the multigrid preconditioner)            */
+  int32_t reserved[4];
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

@@ -57,17 +57,26 @@ __device__ __forceinline__ int mirror(int i, int b, int e) {
 }
 
 // ---------------------------------------------------------------- launchers
+// In a captured step graph every kernel of the step body returns at once
+// when k_dt_finalize held the step back.
+template <class T>
+__device__ __forceinline__ bool gated_off(const Dev<T>& S) {
+  return S.graph_mode && !S.sc->step_go;
+}
+
 // work-item decoders
 struct AllCols { template <class T> __device__ static int n(const Dev<T>& S) { return S.Mloc * S.Nloc; } };
 
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_allcols(Dev<T> S, Op op) {
+  if (gated_off(S)) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.Mloc * S.Nloc) return;
   op(S, t % S.Mloc, t / S.Mloc);
 }
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_incols(Dev<T> S, Op op) {
+  if (gated_off(S)) return;
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= S.M * S.N) return;
   op(S, S.IB + t % S.M, S.JB + t / S.M);
@@ -75,6 +84,7 @@ __global__ void __launch_bounds__(256) k_incols(Dev<T> S, Op op) {
 // cells over an (nx x ny x nz) box starting at (ox, oy, oz)
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_box(Dev<T> S, Op op, int nx, int ny, int nz, int ox, int oy, int oz) {
+  if (gated_off(S)) return;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)nx * ny * nz;
   if (t >= n) return;
@@ -87,6 +97,7 @@ __global__ void __launch_bounds__(256) k_box(Dev<T> S, Op op, int nx, int ny, in
 // all cells of the ghosted array
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_allcells(Dev<T> S, Op op) {
+  if (gated_off(S)) return;
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)S.Mloc * S.Nloc * S.Kloc;
   if (t >= n) return;
@@ -1028,7 +1039,8 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
       sc->step_status = 0;
     }
   }
-  if (S.graph_mode) cudaGraphSetConditional(S.h_go, go ? 1u : 0u);
+  sc->step_go = go ? 1 : 0;
+  if (S.graph_mode && S.h_go) cudaGraphSetConditional(S.h_go, go ? 1u : 0u);
 }
 
 // =========================================================================

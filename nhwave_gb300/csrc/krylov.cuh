@@ -137,11 +137,11 @@ __device__ __forceinline__ void decode(int ic, int M, int N, int& ii, int& jj, i
 // eagerly launched kernels (graph_mode 0) leave handles alone.
 template <class T>
 __device__ __forceinline__ void set_cond(const Dev<T>& S, unsigned long long h, bool v) {
-  if (S.graph_mode) cudaGraphSetConditional(h, v ? 1u : 0u);
+  if (S.graph_mode && h) cudaGraphSetConditional(h, v ? 1u : 0u);
 }
 
 // Status codes of the C interface that the device writes.
-constexpr int kStKrylovNoconv = 6, kStNaN = 7;
+constexpr int kStKrylovNoconv = 6, kStNaN = 7, kStTimeout = 8;
 
 // r64 = b - A64 x64; inner right-hand side rT = (T) r64; ||r64||, ||b||.
 // The last block then makes the refinement decision of the outer loop (the

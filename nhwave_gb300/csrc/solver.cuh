@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "mg.cuh"
+#include "psolve.cuh"
 #include "setup_host.h"
 
 namespace nhw {
@@ -87,7 +87,22 @@ __global__ void k_unpack(void* dst, int kind, const double* sd, const int* si, i
 }
 template <class T>
 __global__ void k_single(Dev<T> S, int what) {
+  if (gated_off(S)) return;
   if (what == 0) OpSourceArea{}(S, 0, 0);
+}
+// update_vars: D0 = D, Eta0 = Eta (2-D, FP64), DU0/DV0/DW0 = DU/DV/DW (3-D)
+template <class T>
+__global__ void __launch_bounds__(256) k_update_vars(Dev<T> S, long long n2, long long n3) {
+  if (gated_off(S)) return;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n3; t += (long long)gridDim.x * blockDim.x) {
+    S.DU0[t] = S.DU[t];
+    S.DV0[t] = S.DV[t];
+    S.DW0[t] = S.DW[t];
+    if (t < n2) {
+      S.D0[t] = S.D[t];
+      S.Eta0[t] = S.Eta[t];
+    }
+  }
 }
 
 template <class T>
@@ -120,6 +135,13 @@ class Solver final : public SolverBase {
   bool use_mg = true;
   T mg_w = (T)1;
   int mg_coarse_sweeps = 6;
+  // persistent solve (psolve.cuh): one cooperative launch per pressure solve
+  bool use_persistent = false;
+  int ps_nb = 0;             // blocks of the launch
+  size_t ps_smem = 0;        // dynamic shared memory per block
+  double* ps_part = nullptr; // [2][ps_nb][4] partial sums
+  PsGroup<T>* d_group = nullptr;
+  cudaError_t launch_err = cudaSuccess;
 
   cudaEvent_t take_event() {
     if (evused == evpool.size()) {
@@ -266,6 +288,24 @@ class Solver final : public SolverBase {
       add(&mg[l].x, sizeof(T) * nl);
       add(&mg[l].b, sizeof(T) * nl);
     }
+    // persistent solve: every block resident (cooperative launch), at most
+    // one block per 2048 unknowns
+    use_persistent = use_mg && p.krylov_kernel == 1 && (int)mg.size() <= kPsMaxLevels;
+    if (use_persistent) {
+      ps_smem = sizeof(T) * 4 * 32 * K;
+      NHW_CU(cudaFuncSetAttribute(k_psolve<T, kPsBY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps_smem));
+      int dev = 0, nsm = 0, per_sm = 0;
+      NHW_CU(cudaGetDevice(&dev));
+      NHW_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+      NHW_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_psolve<T, kPsBY>, 32 * kPsBY, ps_smem));
+      if (per_sm < 1) {
+        set_last_error("persistent solve: no block fits on a multiprocessor");
+        return NHW_ERR_CUDA;
+      }
+      ps_nb = std::max(1, std::min(per_sm * nsm, (int)cdiv((long long)neq, 2048)));
+      add(&ps_part, sizeof(double) * 2 * 4 * ps_nb);
+      add(&d_group, sizeof(PsGroup<T>));
+    }
     add(&S.sc, sizeof(DevScal));
     add(&d_out, sizeof(double) * 8);
     stage_elems = std::max(n3, (size_t)(S.Mloc + 1) * (S.Nloc + 1) * (S.Kloc + 1));
@@ -320,8 +360,13 @@ class Solver final : public SolverBase {
   unsigned red_blocks() const { return cdiv(S.neq, 256 * kCPT); }
 
   int check() {
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) { set_last_error(std::string("kernel launch: ") + cudaGetErrorString(e)); return NHW_ERR_CUDA; }
+    cudaError_t e = launch_err != cudaSuccess ? launch_err : cudaGetLastError();
+    launch_err = cudaSuccess;
+    if (e != cudaSuccess) {
+      set_last_error(std::string("kernel launch: ") + cudaGetErrorString(e));
+      if (capturing) cap_ok(e, "kernel launch");
+      return NHW_ERR_CUDA;
+    }
     return NHW_OK;
   }
   int pull_scalars() {
@@ -423,6 +468,30 @@ class Solver final : public SolverBase {
     return NHW_OK;
   }
 
+  // table of the persistent solve: this scenario as one group of ps_nb blocks
+  int upload_group() {
+    if (!use_persistent) return NHW_OK;
+    PsGroup<T> g{};
+    g.S = S;
+    g.S.graph_mode = 0;
+    const int nl = (int)mg.size();
+    int lc = 0;
+    while (lc < nl && (long long)mg[lc].M * mg[lc].N > kCtaColumns) ++lc;
+    if (nl - lc > kCtaLevels) lc = nl - kCtaLevels;
+    if (lc >= nl) lc = nl - 1;   // the first block always solves at least the coarsest level
+    for (int l = 0; l < nl; ++l) g.L[l] = mg[l];
+    g.nl = lc;
+    g.ntot = nl;
+    g.w = mg_w;
+    g.coarse_sweeps = mg_coarse_sweeps;
+    g.b0 = 0;
+    g.nb = ps_nb;
+    g.part = ps_part;
+    NHW_CU(cudaMemcpyAsync(d_group, &g, sizeof(g), cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
+
   // ----------------------------------------------------------------- setup
   int setup(const double* depth, const double* eta0, const double* uvw0) override {
     drop_step_graphs();   // a new set-up changes captured kernel arguments
@@ -494,6 +563,10 @@ class Solver final : public SolverBase {
     });
     rc = sync();
     if (rc) return rc;
+    {
+      const int rg = upload_group();
+      if (rg) return rg;
+    }
     ready = true;
     return NHW_OK;
   }
@@ -538,12 +611,11 @@ class Solver final : public SolverBase {
     return check();
   }
   int update_vars() override {
-    NHW_CU(cudaMemcpyAsync(S.D0, S.D, sizeof(double) * n2, cudaMemcpyDeviceToDevice, st));
-    NHW_CU(cudaMemcpyAsync(S.Eta0, S.Eta, sizeof(double) * n2, cudaMemcpyDeviceToDevice, st));
-    NHW_CU(cudaMemcpyAsync(S.DU0, S.DU, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
-    NHW_CU(cudaMemcpyAsync(S.DV0, S.DV, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
-    NHW_CU(cudaMemcpyAsync(S.DW0, S.DW, sizeof(T) * n3, cudaMemcpyDeviceToDevice, st));
-    return NHW_OK;
+    L("update_vars", [&] {
+      k_update_vars<T><<<std::min<unsigned>(cdiv((long long)n3, 256), 4096), 256, 0, st>>>(S, (long long)n2,
+                                                                                            (long long)n3);
+    });
+    return check();
   }
   int source_terms() override {
     if (S.wavemaker) L("source_area", [&] { k_single<T><<<1, 1, 0, st>>>(S, 0); });
@@ -577,6 +649,37 @@ class Solver final : public SolverBase {
         });
         L("mg_factor", [&] { k_mg_factor<T><<<cdiv((long long)c.M * c.N, 256), 256, 0, st>>>(c, (T*)c.lcp, (T*)c.linv); });
       }
+    if (use_persistent) {
+      // count, generation and error word of the solve's grid barrier start at zero
+      NHW_CU(cudaMemsetAsync(&S.sc->bar_count, 0, 3 * sizeof(unsigned int), st));
+      const int gated = capturing ? 1 : 0;
+      L("psolve", [&] {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)ps_nb);
+        cfg.blockDim = dim3(32, kPsBY);
+        cfg.dynamicSmemBytes = ps_smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_psolve<T, kPsBY>, (const PsGroup<T>*)d_group, 1, gated);
+        if (e != cudaSuccess && launch_err == cudaSuccess) launch_err = e;
+      });
+      if (launch_err != cudaSuccess) {
+        set_last_error(std::string("persistent solve launch: ") + cudaGetErrorString(launch_err));
+        launch_err = cudaSuccess;
+        return NHW_ERR_CUDA;
+      }
+      cells(OpPFromX{});
+      allcols(OpPGhost{});
+      if (capturing) return NHW_OK;
+      int rc = pull_scalars();
+      if (rc) return rc;
+      rc = check();
+      return rc ? rc : h_sc->pstat;
+    }
     if (capturing) {
       ++cap_solves;
       // device-side loops: refinement sweeps around BiCGSTAB iterations
@@ -849,12 +952,15 @@ class Solver final : public SolverBase {
     const long long l0 = launches;
     capturing = true;
     S.graph_mode = 1;
-    S.h_go = new_handle();
+    S.h_go = use_persistent ? 0 : new_handle();
     if (cap_ok(cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
                "step capture")) {
       L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
       L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, gated); });
-      cond_node(S.h_go, cudaGraphCondTypeIf, [&] { step_body(); }, 0);
+      if (use_persistent)
+        step_body();   // every kernel checks sc->step_go; no loops left on the host side
+      else
+        cond_node(S.h_go, cudaGraphCondTypeIf, [&] { step_body(); }, 0);
       cudaGraph_t gg = nullptr;
       cap_ok(cudaStreamEndCapture(st, &gg), "step capture end");
     }

@@ -51,8 +51,11 @@ struct DevScal {
   int32_t ir_go, ir_count, inner_total, pstat, zero_x;
   int32_t step_status;              // first non-OK Poisson status of the current step
   int32_t worst;                    // largest status code since the host last cleared it
-  int32_t pad_;
+  int32_t step_go;                  // set by k_dt_finalize: the step proceeds
   int64_t total_ir;                 // refinement sweeps, cumulative
+  // grid barrier of the persistent solve (psolve.cuh)
+  unsigned int bar_count, bar_gen;
+  int32_t bar_err, pad2_;
 };
 
 template <class T>
@@ -72,8 +75,10 @@ struct Dev {
   int itmax, max_ir;               // ITMAX over all inner iterations; refinement sweeps
   double total_time;               // TOTAL_TIME and SIM_STEPS, for the gated run graph
   int sim_steps;
-  // conditional-node handles of a captured step graph; graph_mode = 0 in
-  // eagerly launched kernels, which then never touch a handle
+  // graph_mode = 1 in kernels captured into a step graph: they do nothing
+  // unless k_dt_finalize let the step proceed (sc->step_go), and the
+  // phase-by-phase solver sets the conditions of its loop nodes through the
+  // handles.  Eagerly launched kernels have graph_mode = 0.
   int graph_mode;
   unsigned long long h_go, h_ir, h_inner;
   double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt)

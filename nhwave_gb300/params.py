@@ -55,7 +55,8 @@ class NhwParams(ctypes.Structure):
         ("device", ctypes.c_int32),
         ("precond", ctypes.c_int32),
         ("mg_weight", ctypes.c_float),
-        ("reserved", ctypes.c_int32 * 5),
+        ("krylov_kernel", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
     def copy(self) -> "NhwParams":

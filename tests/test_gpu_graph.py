@@ -13,11 +13,13 @@ pytestmark = pytest.mark.gpu
 FIELDS = ["D", "ETA", "HC", "U", "V", "W", "DU", "DV", "DW", "P", "OMEGA", "MASK"]
 
 
-def _scen(name, precision, **kw):
+def _scen(name, precision, **attrs):
     from nhwave_gb300 import lib, scenarios as S
-    p, d, e, u = S.make(name, precision=precision, seed=11, **kw)
+    p, d, e, u = S.make(name, precision=precision, seed=11)
     p.tol = 1e-10 if precision == 0 else 1e-8
     p.itmax = 5000
+    for k, v in attrs.items():
+        setattr(p, k, v)
     return lib.Scenario(p, d, e, u)
 
 
@@ -98,3 +100,29 @@ def test_solver_counters(gpu_lib):
     assert sc.last_krylov_iters > 0 and sc.total_krylov_iters >= sc.last_krylov_iters
     assert sc.last_refinements >= 1
     assert sc.last_rel_residual <= s.params.tol
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"])
+def test_persistent_solve_matches_phase_solve(name, precision, gpu_lib):
+    """krylov_kernel = 1 (one cooperative launch per pressure solve) against
+    the phase-by-phase solver: same algorithm and tests, summation order of
+    the dot products differs, so the solutions agree to the solver tolerance."""
+    from nhwave_gb300 import fields as F
+    from conftest import rel_l2
+    a = _scen(name, precision)
+    b = _scen(name, precision, krylov_kernel=1)
+    for _ in range(3):
+        assert a.step() == 0
+        assert b.step() == 0
+    lim = 1e-8 if precision == 0 else 1e-6
+    for f in ("ETA", "P", "U", "W"):
+        fid = getattr(F, f)
+        sl = a.shape.interior(fid)
+        r = rel_l2(b.get(fid)[sl], a.get(fid)[sl])
+        assert r < lim, f"{name} {f}: {r:.3e}"
+    assert np.array_equal(a.get(F.MASK), b.get(F.MASK))
+    sa, sb = a.scalars(), b.scalars()
+    assert sa.poisson_solves == sb.poisson_solves
+    assert abs(sa.total_krylov_iters - sb.total_krylov_iters) <= 3
+    assert sb.last_rel_residual <= b.params.tol

@@ -28,7 +28,12 @@ def vel_err(g, o, name):
     return np.linalg.norm(g.get(fid)[sl] - o.get(fid)[sl]) / ref
 
 
-def _pair(name, oracle_mod, precision=0, tol=1e-14, seed=7, **kw):
+# Poisson TOL of the step tests: 1e-13 sits above the FP64 residual floor
+# (about 1e-14 on these grids), so both solvers stop by convergence
+STEP_TOL = 1e-13
+
+
+def _pair(name, oracle_mod, precision=0, tol=STEP_TOL, seed=7, **kw):
     from nhwave_gb300 import lib, scenarios as S
     p, d, e, u = S.make(name, precision=precision, seed=seed, **kw)
     p.tol = tol
@@ -152,7 +157,7 @@ def test_steps_fp64(name, oracle_mod, gpu_lib):
         assert r < 1e-10, f"{name} {f}: rel L2 {r:.3e}"
     sg, so = g.scalars(), o.scalars()
     assert abs(sg.time - so.time) <= 1e-12 * so.time
-    assert sg.last_rel_residual <= 1e-14
+    assert sg.last_rel_residual <= STEP_TOL
     g.close()
 
 
@@ -195,7 +200,7 @@ def test_golden_fixtures(name, gpu_lib):
     steps = GOLDEN[name]
     ref = np.load(golden_path(name, steps))
     p, d, e, u = S.make(name, seed=7)
-    p.tol = 1e-14
+    p.tol = STEP_TOL
     p.itmax = 20000
     g = lib.Scenario(p, d, e, u)
     for _ in range(steps):
