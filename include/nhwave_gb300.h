@@ -233,6 +233,48 @@ int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes);
 const char* nhw_status_string(int status);
 const char* nhw_last_error(void);
 
+/* --------------------------------------------------------------- ensembles
+ * Many scenarios advanced together.  The reference runs one scenario per
+ * program; an ensemble takes set-up handles (same device, precision,
+ * TIME_ORDER and NON_HYDRO; the multigrid preconditioner) and advances all of
+ * them one step per CUDA graph launch: every member's step kernels on a
+ * branch of their own, and per RK stage the pressure solves of all members in
+ * one persistent cooperative launch (more than one when the members need more
+ * blocks than the GPU holds at once).  A member whose run is over (TIME >=
+ * TOTAL_TIME or RUN_STEP >= SIM_STEPS) or that stopped at DT_MIN is skipped
+ * on the device.  A member's results do not depend on the other members.
+ * Members stay owned by the caller: destroy the ensemble before them, and do
+ * not step a member on its own while it belongs to a live ensemble. */
+typedef struct nhw_ensemble nhw_ensemble;
+typedef struct nhw_ensemble_opts {
+  int32_t cells_per_block;   /* unknowns per block of a member's solve (0: 16384)  */
+  int32_t block_rows;        /* solve blocks are 32 x block_rows threads: 8 or 16  */
+  int32_t coarse_sweeps;     /* red-black sweeps on the coarsest level (0: 6)      */
+  int32_t reserved[5];
+} nhw_ensemble_opts;
+typedef struct nhw_ensemble_info {
+  int32_t members;
+  int32_t solve_launches_per_stage;   /* persistent-solve launches per RK stage  */
+  int32_t blocks_per_launch;          /* blocks of the largest of them           */
+  int32_t max_resident_blocks;        /* blocks the GPU holds at once            */
+  int64_t kernels_per_step;           /* kernel launches in one step's graph     */
+  int64_t cells;                      /* interior cells over all members         */
+  nhw_ensemble_opts opts;             /* settings in use                         */
+} nhw_ensemble_info;
+
+int nhw_ensemble_create(nhw_handle* const* members, int32_t n, const nhw_ensemble_opts* opts,
+                        nhw_ensemble** out);
+/* nsteps ensemble steps; returns the worst member status (DT_MIN, NAN, TIMEOUT) */
+int nhw_ensemble_step(nhw_ensemble* e, int32_t nsteps);
+/* nsteps ensemble steps timed with CUDA events on the ensemble's stream */
+int nhw_ensemble_run_timed(nhw_ensemble* e, int32_t nsteps, double* device_ms);
+/* Autotuner: times candidate settings (cells per block, block height, coarse
+ * sweeps) on real ensemble steps -- the members advance by steps_per_trial
+ * steps per candidate -- and keeps the fastest; writes it to *chosen. */
+int nhw_ensemble_tune(nhw_ensemble* e, int32_t steps_per_trial, nhw_ensemble_opts* chosen);
+int nhw_ensemble_get_info(nhw_ensemble* e, nhw_ensemble_info* out);
+int nhw_ensemble_destroy(nhw_ensemble* e);
+
 /* ------------------------------------------------ allocation-free variant
  * No counterpart in the reference: an addition for callers that cannot let a
  * library allocate device memory.  Such a caller -- a host model whose fields

@@ -2,12 +2,17 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <vector>
 
-#include "solver.cuh"
+#include "ensemble.cuh"
 
 struct nhw_handle {
   nhw::SolverBase* s = nullptr;
   nhw_params p{};
+};
+struct nhw_ensemble {
+  nhw::EnsembleBase* e = nullptr;
+  int device = 0;
 };
 
 namespace nhw {
@@ -124,6 +129,61 @@ int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done) {
   const int rc = nsteps > 0 ? h->s->run(nsteps, &done) : NHW_OK;
   if (steps_done) *steps_done = done;
   return rc;
+}
+
+int nhw_ensemble_create(nhw_handle* const* members, int32_t n, const nhw_ensemble_opts* opts,
+                        nhw_ensemble** out) {
+  if (!members || n < 1 || !out) return NHW_ERR_ARG;
+  *out = nullptr;
+  std::vector<SolverBase*> ss;
+  for (int i = 0; i < n; ++i) {
+    if (!members[i] || !members[i]->s) return NHW_ERR_ARG;
+    if (!members[i]->s->is_setup()) return NHW_ERR_STATE;
+    for (int j = 0; j < i; ++j)
+      if (members[j] == members[i]) return NHW_ERR_ARG;
+    ss.push_back(members[i]->s);
+  }
+  int rc = members[0]->s->bind();
+  if (rc) return rc;
+  int st = NHW_OK;
+  nhw::EnsembleBase* e = members[0]->p.precision == NHW_FP32_IR
+                             ? nhw::make_ensemble_fp32(ss.data(), n, opts, &st)
+                             : nhw::make_ensemble_fp64(ss.data(), n, opts, &st);
+  if (!e) return st ? st : NHW_ERR_NOMEM;
+  *out = new nhw_ensemble{e, members[0]->p.device};
+  return NHW_OK;
+}
+#define NHW_ENS(e)                                            \
+  if (!(e) || !(e)->e) return NHW_ERR_ARG;                    \
+  {                                                           \
+    const cudaError_t de_ = cudaSetDevice((e)->device);      \
+    if (de_ != cudaSuccess) return NHW_ERR_CUDA;              \
+  }
+int nhw_ensemble_step(nhw_ensemble* e, int32_t nsteps) {
+  NHW_ENS(e);
+  if (nsteps < 0) return NHW_ERR_ARG;
+  return e->e->step(nsteps);
+}
+int nhw_ensemble_run_timed(nhw_ensemble* e, int32_t nsteps, double* device_ms) {
+  NHW_ENS(e);
+  if (nsteps < 1 || !device_ms) return NHW_ERR_ARG;
+  return e->e->run_timed(nsteps, device_ms);
+}
+int nhw_ensemble_tune(nhw_ensemble* e, int32_t steps_per_trial, nhw_ensemble_opts* chosen) {
+  NHW_ENS(e);
+  return e->e->tune(steps_per_trial, chosen);
+}
+int nhw_ensemble_get_info(nhw_ensemble* e, nhw_ensemble_info* out) {
+  NHW_ENS(e);
+  if (!out) return NHW_ERR_ARG;
+  return e->e->info(out);
+}
+int nhw_ensemble_destroy(nhw_ensemble* e) {
+  if (!e) return NHW_ERR_ARG;
+  cudaSetDevice(e->device);
+  delete e->e;
+  delete e;
+  return NHW_OK;
 }
 
 int nhw_mass(nhw_handle* h, double* mass) {

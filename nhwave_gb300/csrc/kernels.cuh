@@ -1037,6 +1037,8 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
       sc->time = sc->time + dt;
       sc->run_step = sc->run_step + 1;
       sc->step_status = 0;
+      sc->bar_count = 0u;   // grid barrier of this step's persistent solves
+      sc->bar_err = 0;
     }
   }
   sc->step_go = go ? 1 : 0;

@@ -1,8 +1,11 @@
 // nhw_fp64.cu -- plain FP64 form: every kernel instantiated for double.
 // Built with --fmad=false so that products and sums round exactly as the
 // reference's double build does (no fused multiply-add).
-#include "solver.cuh"
+#include "ensemble.cuh"
 
 namespace nhw {
 SolverBase* make_solver_fp64(const nhw_params& p, int* status) { return make_solver_t<double>(p, status); }
+EnsembleBase* make_ensemble_fp64(SolverBase* const* members, int n, const nhw_ensemble_opts* o, int* status) {
+  return make_ensemble_t<double>(members, n, o, status);
+}
 }  // namespace nhw

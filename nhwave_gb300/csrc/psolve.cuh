@@ -35,6 +35,7 @@ namespace nhw {
 constexpr int kPsBY = 16;                          // block = 32 x kPsBY threads (one scenario)
 constexpr int kPsBYEnsemble = 8;                   // 32 x 8 when many scenarios share a launch
 constexpr int kPsMaxLevels = 16;
+constexpr int kPsMaxBlocks = 1024;                 // blocks of one group at most
 constexpr long long kPsSpinLimit = 1ll << 22;      // polls of ~64 ns: well under a second
 
 template <class T>

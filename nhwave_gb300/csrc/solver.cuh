@@ -291,6 +291,8 @@ class Solver final : public SolverBase {
     // persistent solve: every block resident (cooperative launch), at most
     // one block per 2048 unknowns
     use_persistent = use_mg && p.krylov_kernel == 1 && (int)mg.size() <= kPsMaxLevels;
+    if (use_mg && (int)mg.size() <= kPsMaxLevels)   // partial sums of the scenario's group, up to kPsMaxBlocks
+      add(&ps_part, sizeof(double) * 2 * 4 * kPsMaxBlocks);
     if (use_persistent) {
       ps_smem = sizeof(T) * 4 * 32 * K;
       NHW_CU(cudaFuncSetAttribute(k_psolve<T, kPsBY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps_smem));
@@ -302,8 +304,7 @@ class Solver final : public SolverBase {
         set_last_error("persistent solve: no block fits on a multiprocessor");
         return NHW_ERR_CUDA;
       }
-      ps_nb = std::max(1, std::min(per_sm * nsm, (int)cdiv((long long)neq, 2048)));
-      add(&ps_part, sizeof(double) * 2 * 4 * ps_nb);
+      ps_nb = std::max(1, std::min(std::min(per_sm * nsm, kPsMaxBlocks), (int)cdiv((long long)neq, 2048)));
       add(&d_group, sizeof(PsGroup<T>));
     }
     add(&S.sc, sizeof(DevScal));
@@ -468,9 +469,8 @@ class Solver final : public SolverBase {
     return NHW_OK;
   }
 
-  // table of the persistent solve: this scenario as one group of ps_nb blocks
-  int upload_group() {
-    if (!use_persistent) return NHW_OK;
+  // this scenario as one group of the persistent solve: nb blocks from b0
+  PsGroup<T> make_group(int nb, int b0, int coarse_sweeps) const {
     PsGroup<T> g{};
     g.S = S;
     g.S.graph_mode = 0;
@@ -483,14 +483,65 @@ class Solver final : public SolverBase {
     g.nl = lc;
     g.ntot = nl;
     g.w = mg_w;
-    g.coarse_sweeps = mg_coarse_sweeps;
-    g.b0 = 0;
-    g.nb = ps_nb;
+    g.coarse_sweeps = coarse_sweeps;
+    g.b0 = b0;
+    g.nb = nb;
     g.part = ps_part;
+    return g;
+  }
+  int upload_group() {
+    if (!use_persistent) return NHW_OK;
+    const PsGroup<T> g = make_group(ps_nb, 0, mg_coarse_sweeps);
     NHW_CU(cudaMemcpyAsync(d_group, &g, sizeof(g), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaStreamSynchronize(st));
     return NHW_OK;
   }
+  bool persistent_capable() const { return use_mg && (int)mg.size() <= kPsMaxLevels; }
+
+  // ---------------------------------------------- capture into an ensemble
+  // The ensemble captures this scenario's kernels on a branch stream of its
+  // own; every kernel is gated by sc->step_go, which k_dt_finalize sets.
+  cudaStream_t ens_saved_st = nullptr;
+  void ens_begin(cudaStream_t s) {
+    ens_saved_st = st;
+    st = s;
+    capturing = true;
+    cap_level = 3;
+    cap_err.clear();
+    S.graph_mode = 1;
+    S.h_go = 0;
+  }
+  int ens_end() {
+    st = ens_saved_st;
+    capturing = false;
+    S.graph_mode = 0;
+    if (!cap_err.empty()) {
+      set_last_error(cap_err);
+      return NHW_ERR_CUDA;
+    }
+    return NHW_OK;
+  }
+  void ens_prefix() {   // estimate_dt (gated), bathymetry, mask, update_vars
+    L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+    L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, 1); });
+    if (S.slide) update_bathymetry();
+    update_mask();
+    update_vars();
+  }
+  void ens_stage_head(int s) {   // source_terms, fluxes, eval_duvw up to the solve
+    source_terms();
+    fluxes();
+    stage_pre(s);
+  }
+  void ens_stage_tail(int s) {   // eval_duvw after the solve, sponge
+    stage_post(s);
+    if (S.sponge_on) sponge_damping();
+  }
+  int pull() { return pull_scalars(); }
+  const DevScal& scal() const { return *h_sc; }
+  int order() const { return it_order; }
+  const Dev<T>& dev() const { return S; }
+  const nhw_params& params() const { return p; }
 
   // ----------------------------------------------------------------- setup
   int setup(const double* depth, const double* eta0, const double* uvw0) override {
@@ -634,7 +685,9 @@ class Solver final : public SolverBase {
     allcols(OpVelBcA{});
     incols(OpVelBcB{});
   }
-  int poisson() {
+  // generate_coef_rhs (src/pressure.F:475-840), line factors, initial guess
+  // and the multigrid coarse operators
+  void poisson_setup() {
     incols(OpColFactors{});
     cells(OpPoissonCoef{});
     if (kFP32) cells(OpCoefToT{});
@@ -649,6 +702,13 @@ class Solver final : public SolverBase {
         });
         L("mg_factor", [&] { k_mg_factor<T><<<cdiv((long long)c.M * c.N, 256), 256, 0, st>>>(c, (T*)c.lcp, (T*)c.linv); });
       }
+  }
+  // P from the solution, ghosts mirrored (src/pressure.F:185-239)
+  void poisson_finish() {
+    cells(OpPFromX{});
+    allcols(OpPGhost{});
+  }
+  int poisson_solve() {
     if (use_persistent) {
       // count, generation and error word of the solve's grid barrier start at zero
       NHW_CU(cudaMemsetAsync(&S.sc->bar_count, 0, 3 * sizeof(unsigned int), st));
@@ -672,8 +732,6 @@ class Solver final : public SolverBase {
         launch_err = cudaSuccess;
         return NHW_ERR_CUDA;
       }
-      cells(OpPFromX{});
-      allcols(OpPGhost{});
       if (capturing) return NHW_OK;
       int rc = pull_scalars();
       if (rc) return rc;
@@ -692,8 +750,6 @@ class Solver final : public SolverBase {
         L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
         L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
       }, 1);
-      cells(OpPFromX{});
-      allcols(OpPGhost{});
       return NHW_OK;
     }
     // host-driven loops over the same device-side decisions
@@ -716,11 +772,8 @@ class Solver final : public SolverBase {
       rc = pull_scalars();
       if (rc) return rc;
     }
-    const int status = h_sc->pstat;
-    cells(OpPFromX{});
-    allcols(OpPGhost{});
     rc = check();
-    return rc ? rc : status;
+    return rc ? rc : h_sc->pstat;
   }
   // `chunk` BiCGSTAB iterations; replayed from a captured CUDA graph unless the
   // per-kernel profiler is on (its events would become graph nodes)
@@ -821,17 +874,22 @@ class Solver final : public SolverBase {
     }
   }
 
-  int eval_duvw(int istep) override {
-    if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
-    const int s = istep - 1;
+  // eval_duvw up to the pressure solve: explicit stage update, surface BC,
+  // slopes, velocities and the Poisson system
+  void stage_pre(int s) {
     incols(OpExplicit{s});
     allcols(OpWlBcEta{});
     allcols(OpSlopeEta{});
-    int status = NHW_OK;
     if (S.non_hydro) {
       get_uvw();
-      status = poisson();
-      if (status == NHW_ERR_CUDA) return status;
+      poisson_setup();
+    }
+  }
+  // eval_duvw after the pressure solve: projection, SSP-RK combination,
+  // velocities and Omega
+  void stage_post(int s) {
+    if (S.non_hydro) {
+      poisson_finish();
       cells(OpProjection{});
     }
     cells(OpSSP{s});
@@ -839,6 +897,17 @@ class Solver final : public SolverBase {
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});
+  }
+  int eval_duvw(int istep) override {
+    if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
+    const int s = istep - 1;
+    stage_pre(s);
+    int status = NHW_OK;
+    if (S.non_hydro) {
+      status = poisson_solve();
+      if (status == NHW_ERR_CUDA) return status;
+    }
+    stage_post(s);
     int rc = check();
     return rc ? rc : status;
   }

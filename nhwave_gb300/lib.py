@@ -32,7 +32,22 @@ EXPORTS = [
     "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
     "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
     "nhw_estimate_dt_noalloc",
+    "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
+    "nhw_ensemble_get_info", "nhw_ensemble_destroy",
 ]
+
+
+class EnsembleOpts(ctypes.Structure):
+    """nhw_ensemble_opts (include/nhwave_gb300.h)."""
+    _fields_ = [("cells_per_block", ctypes.c_int32), ("block_rows", ctypes.c_int32),
+                ("coarse_sweeps", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+
+
+class EnsembleInfo(ctypes.Structure):
+    """nhw_ensemble_info (include/nhwave_gb300.h)."""
+    _fields_ = [("members", ctypes.c_int32), ("solve_launches_per_stage", ctypes.c_int32),
+                ("blocks_per_launch", ctypes.c_int32), ("max_resident_blocks", ctypes.c_int32),
+                ("kernels_per_step", ctypes.c_int64), ("cells", ctypes.c_int64), ("opts", EnsembleOpts)]
 
 
 class NhwError(RuntimeError):
@@ -79,6 +94,12 @@ def load(path: str | None = None):
     L.nhw_profile.argtypes = [vp, i32]
     L.nhw_profile_report.argtypes = [vp, ctypes.c_char_p, i32]
     L.nhw_estimate_dt_noalloc.argtypes = [vp] * 5 + [i32] * 3 + [dbl] * 5 + [vp, vp]
+    L.nhw_ensemble_create.argtypes = [P(vp), i32, P(EnsembleOpts), P(vp)]
+    L.nhw_ensemble_step.argtypes = [vp, i32]
+    L.nhw_ensemble_run_timed.argtypes = [vp, i32, P(dbl)]
+    L.nhw_ensemble_tune.argtypes = [vp, i32, P(EnsembleOpts)]
+    L.nhw_ensemble_get_info.argtypes = [vp, P(EnsembleInfo)]
+    L.nhw_ensemble_destroy.argtypes = [vp]
     L.nhw_status_string.argtypes = [ctypes.c_int]
     L.nhw_status_string.restype = ctypes.c_char_p
     L.nhw_last_error.argtypes = []
@@ -236,3 +257,52 @@ class Scenario:
         if a.size != int(np.prod(shp)):
             raise ValueError(f"field {F.NAMES[field]} wants {shp}, got {a.size} elements")
         _chk(load().nhw_set_field(self._h, field, _ptr(a)), "nhw_set_field")
+
+
+class Ensemble:
+    """Many scenarios advanced together: one CUDA graph launch per ensemble
+    step (nhw_ensemble_*).  ``members`` are set-up ``Scenario`` objects; they
+    stay usable for field access, and must outlive the ensemble."""
+
+    def __init__(self, members, cells_per_block: int = 0, block_rows: int = 0, coarse_sweeps: int = 0):
+        self.members = list(members)
+        arr = (ctypes.c_void_p * len(self.members))(*[m._h for m in self.members])
+        o = EnsembleOpts(cells_per_block, block_rows, coarse_sweeps)
+        self._e = ctypes.c_void_p()
+        _chk(load().nhw_ensemble_create(arr, len(self.members), ctypes.byref(o), ctypes.byref(self._e)),
+             "nhw_ensemble_create")
+
+    def step(self, n: int = 1) -> int:
+        return _chk(load().nhw_ensemble_step(self._e, n), "nhw_ensemble_step")
+
+    def run_timed(self, n: int) -> float:
+        ms = ctypes.c_double(0.0)
+        _chk(load().nhw_ensemble_run_timed(self._e, n, ctypes.byref(ms)), "nhw_ensemble_run_timed")
+        return ms.value
+
+    def tune(self, steps_per_trial: int = 1) -> EnsembleOpts:
+        o = EnsembleOpts()
+        _chk(load().nhw_ensemble_tune(self._e, steps_per_trial, ctypes.byref(o)), "nhw_ensemble_tune")
+        return o
+
+    def info(self) -> EnsembleInfo:
+        out = EnsembleInfo()
+        _chk(load().nhw_ensemble_get_info(self._e, ctypes.byref(out)), "nhw_ensemble_get_info")
+        return out
+
+    def close(self):
+        if getattr(self, "_e", None) and self._e.value:
+            load().nhw_ensemble_destroy(self._e)
+            self._e = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
