@@ -250,16 +250,22 @@ typedef struct nhw_ensemble_opts {
   int32_t cells_per_block;   /* unknowns per block of a member's solve (0: 16384)  */
   int32_t block_rows;        /* solve blocks are 32 x block_rows threads: 8 or 16  */
   int32_t coarse_sweeps;     /* red-black sweeps on the coarsest level (0: 6)      */
-  int32_t reserved[5];
+  int32_t solver;            /* 0: every member's phase-by-phase solve on its own
+                                branch, loops in conditional nodes; 1: the solves
+                                of all members as groups of persistent launches */
+  int32_t reserved[4];
 } nhw_ensemble_opts;
 typedef struct nhw_ensemble_info {
   int32_t members;
   int32_t solve_launches_per_stage;   /* persistent-solve launches per RK stage  */
   int32_t blocks_per_launch;          /* blocks of the largest of them           */
   int32_t max_resident_blocks;        /* blocks the GPU holds at once            */
-  int64_t kernels_per_step;           /* kernel launches in one step's graph     */
+  int64_t kernels_per_step;           /* kernel launches of a step outside the
+                                         members' own solver loops               */
   int64_t cells;                      /* interior cells over all members         */
   nhw_ensemble_opts opts;             /* settings in use                         */
+  int64_t kernels_launched;           /* all kernel launches so far, loops
+                                         counted from the device's counters      */
 } nhw_ensemble_info;
 
 int nhw_ensemble_create(nhw_handle* const* members, int32_t n, const nhw_ensemble_opts* opts,

@@ -48,6 +48,12 @@ class Ensemble final : public EnsembleBase {
   int max_blocks = 0, device = 0, order = 3, non_hydro = 1;
   size_t smem_max = 0;
   cudaError_t lerr = cudaSuccess;
+  // kernel launches: per graph launch outside loops, and per refinement sweep
+  // and per BiCGSTAB iteration of each member's own solver loops
+  long long per_launch = 0;
+  std::vector<long long> per_sweep, per_iter;
+  std::vector<int64_t> acc_ir, acc_it;
+  long long launches = 0;
 
   ~Ensemble() override {
     cudaSetDevice(device);
@@ -66,6 +72,7 @@ class Ensemble final : public EnsembleBase {
     if (o->cells_per_block <= 0) o->cells_per_block = 16384;
     if (o->block_rows != 8 && o->block_rows != 16) o->block_rows = kPsBYEnsemble;
     if (o->coarse_sweeps <= 0) o->coarse_sweeps = 6;
+    if (o->solver != 1) o->solver = 0;
   }
 
   int create(const std::vector<Solver<T>*>& members, const nhw_ensemble_opts* o) {
@@ -164,8 +171,15 @@ class Ensemble final : public EnsembleBase {
     // ---- capture
     kernels = 0;
     lerr = cudaSuccess;
-    cudaGraph_t g = nullptr;
+    cudaGraph_t g = nullptr, root = nullptr;
+    for (auto* s : m) s->ens_reset_counts();
     NHW_CU(cudaStreamBeginCapture(st0, cudaStreamCaptureModeThreadLocal));
+    {
+      cudaStreamCaptureStatus cs;
+      unsigned long long id = 0;
+      const cudaError_t e = cudaStreamGetCaptureInfo(st0, &cs, &id, &root, nullptr, nullptr, nullptr);
+      if (e != cudaSuccess) lerr = e;
+    }
     auto fork = [&] {
       cudaEventRecord(ev_fork, st0);
       for (auto s : br) cudaStreamWaitEvent(s, ev_fork, 0);
@@ -179,13 +193,14 @@ class Ensemble final : public EnsembleBase {
     int err = NHW_OK;
     auto member = [&](size_t i, auto fn) {
       const long long l0 = m[i]->launches;
-      m[i]->ens_begin(br[i]);
-      fn(m[i]);
-      const int r = m[i]->ens_end();
-      kernels += m[i]->launches - l0;
+      int r = m[i]->ens_begin(br[i], root, opts.coarse_sweeps);
+      if (!r) fn(m[i]);
+      const int r2 = m[i]->ens_end();
       m[i]->launches = l0;
+      if (!r) r = r2;
       if (r && !err) err = r;
     };
+    const bool groups_solve = non_hydro && opts.solver == 1;
     fork();
     for (size_t i = 0; i < m.size(); ++i)
       member(i, [&](Solver<T>* s) {
@@ -193,7 +208,7 @@ class Ensemble final : public EnsembleBase {
         s->ens_stage_head(0);
       });
     for (int st = 0; st < order; ++st) {
-      if (non_hydro) {
+      if (groups_solve) {
         join();
         if (opts.block_rows == 16) launch_solves<16>();
         else launch_solves<8>();
@@ -201,11 +216,22 @@ class Ensemble final : public EnsembleBase {
       }
       for (size_t i = 0; i < m.size(); ++i)
         member(i, [&](Solver<T>* s) {
+          if (non_hydro && !groups_solve) s->ens_solve();
           s->ens_stage_tail(st);
           if (st + 1 < order) s->ens_stage_head(st + 1);
         });
     }
     join();
+    per_launch = kernels;   // the persistent solves
+    per_sweep.assign(m.size(), 0);
+    per_iter.assign(m.size(), 0);
+    for (size_t i = 0; i < m.size(); ++i) {
+      const long long ns = std::max(1, m[i]->cap_solves);
+      per_launch += m[i]->cap_counts[3] + m[i]->cap_counts[0];
+      per_sweep[i] = m[i]->cap_counts[1] / ns;
+      per_iter[i] = m[i]->cap_counts[2] / ns;
+    }
+    kernels = per_launch;
     cudaError_t ce = cudaStreamEndCapture(st0, &g);
     if (ce == cudaSuccess && lerr != cudaSuccess) ce = lerr;
     if (ce != cudaSuccess || err) {
@@ -224,13 +250,33 @@ class Ensemble final : public EnsembleBase {
   }
 
   // worst member status after a batch of steps (DT_MIN or a non-finite solve)
-  int collect() {
+  // pull every member's scalars; remember the loop counters for accounting
+  int snapshot() {
+    NHW_CU(cudaStreamSynchronize(st0));
+    acc_ir.resize(m.size());
+    acc_it.resize(m.size());
+    for (size_t i = 0; i < m.size(); ++i) {
+      const int rc = m[i]->pull();
+      if (rc) return rc;
+      acc_ir[i] = m[i]->scal().total_ir;
+      acc_it[i] = m[i]->scal().total_it;
+    }
+    return NHW_OK;
+  }
+  int collect(int nlaunch) {
     NHW_CU(cudaStreamSynchronize(st0));
     int worst = NHW_OK;
-    for (auto* s : m) {
+    launches += per_launch * nlaunch;
+    for (size_t ii = 0; ii < m.size(); ++ii) {
+      auto* s = m[ii];
       int rc = s->pull();
       if (rc) return rc;
       const DevScal& sc = s->scal();
+      if (ii < acc_ir.size()) {
+        launches += per_sweep[ii] * (sc.total_ir - acc_ir[ii]) + per_iter[ii] * (sc.total_it - acc_it[ii]);
+        acc_ir[ii] = sc.total_ir;
+        acc_it[ii] = sc.total_it;
+      }
       if (sc.status == NHW_ERR_DT_MIN) worst = std::max(worst, (int)NHW_ERR_DT_MIN);
       if (sc.bar_err) worst = std::max(worst, (int)NHW_ERR_TIMEOUT);
       if (sc.step_status == NHW_ERR_NAN) worst = std::max(worst, (int)NHW_ERR_NAN);
@@ -240,14 +286,16 @@ class Ensemble final : public EnsembleBase {
 
   int step(int nsteps) override {
     NHW_CU(cudaSetDevice(device));
+    int rc = snapshot();
+    if (rc) return rc;
     for (int q = 0; q < nsteps; ++q) NHW_CU(cudaGraphLaunch(exec, st0));
-    for (auto* s : m) s->launches += kernels * nsteps / (long long)m.size();
-    return collect();
+    return collect(nsteps);
   }
 
   int run_timed(int nsteps, double* ms) override {
     NHW_CU(cudaSetDevice(device));
-    NHW_CU(cudaStreamSynchronize(st0));
+    int rc = snapshot();
+    if (rc) return rc;
     NHW_CU(cudaEventRecord(ev0, st0));
     for (int q = 0; q < nsteps; ++q) NHW_CU(cudaGraphLaunch(exec, st0));
     NHW_CU(cudaEventRecord(ev1, st0));
@@ -255,34 +303,45 @@ class Ensemble final : public EnsembleBase {
     float f = 0.f;
     NHW_CU(cudaEventElapsedTime(&f, ev0, ev1));
     *ms = (double)f;
-    return collect();
+    return collect(nsteps);
   }
 
   // Autotuner: times every candidate setting on real ensemble steps (the
   // members advance) and keeps the fastest.
   int tune(int steps_per_trial, nhw_ensemble_opts* chosen) override {
     if (steps_per_trial < 1) steps_per_trial = 1;
-    const int cpb[] = {4096, 16384, 65536};
-    const int rows[] = {8, 16};
-    const int sweeps[] = {4, 6};
+    std::vector<nhw_ensemble_opts> cand;
+    for (int w : {4, 6}) {
+      nhw_ensemble_opts o{};
+      o.solver = 0;
+      o.coarse_sweeps = w;
+      cand.push_back(o);
+      if (!non_hydro) break;
+      for (int c : {4096, 16384, 65536})
+        for (int r : {8, 16}) {
+          nhw_ensemble_opts q{};
+          q.solver = 1;
+          q.cells_per_block = c;
+          q.block_rows = r;
+          q.coarse_sweeps = w;
+          cand.push_back(q);
+        }
+    }
     nhw_ensemble_opts best = opts;
     double best_ms = 1e300;
-    for (int c : cpb)
-      for (int r : rows)
-        for (int w : sweeps) {
-          opts.cells_per_block = c;
-          opts.block_rows = r;
-          opts.coarse_sweeps = w;
-          int rc = build();
-          if (rc) return rc;
-          double ms = 0.0;
-          rc = run_timed(steps_per_trial, &ms);
-          if (rc) return rc;
-          if (ms < best_ms) {
-            best_ms = ms;
-            best = opts;
-          }
-        }
+    for (auto o : cand) {
+      defaults(&o);
+      opts = o;
+      int rc = build();
+      if (rc) return rc;
+      double ms = 0.0;
+      rc = run_timed(steps_per_trial, &ms);
+      if (rc) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = opts;
+      }
+    }
     opts = best;
     if (chosen) *chosen = best;
     return build();
@@ -291,7 +350,8 @@ class Ensemble final : public EnsembleBase {
   int info(nhw_ensemble_info* out) override {
     std::memset(out, 0, sizeof(*out));
     out->members = (int32_t)m.size();
-    out->kernels_per_step = kernels;
+    out->kernels_per_step = per_launch;
+    out->kernels_launched = launches;
     out->solve_launches_per_stage = (int32_t)waves.size();
     int blocks = 0;
     for (const Wave& w : waves) blocks = std::max(blocks, w.blocks);

@@ -152,6 +152,9 @@ constexpr int kStKrylovNoconv = 6, kStNaN = 7, kStTimeout = 8;
 // sets the next inner tolerance and iteration budget.  kFirst opens a solve.
 template <class T, bool kFirst>
 __global__ void __launch_bounds__(256) k_res64(Dev<T> S) {
+  // a step held back by k_dt_finalize: the loop conditions keep their
+  // launch default (0), so no sweep runs
+  if (gated_off(S)) return;
   const int M = S.M, N = S.N, K = S.K;
   const size_t n = (size_t)S.neq;
   double v[2] = {0.0, 0.0};

@@ -502,17 +502,27 @@ class Solver final : public SolverBase {
   // The ensemble captures this scenario's kernels on a branch stream of its
   // own; every kernel is gated by sc->step_go, which k_dt_finalize sets.
   cudaStream_t ens_saved_st = nullptr;
-  void ens_begin(cudaStream_t s) {
+  int ens_saved_sweeps = 0;
+  // root: the ensemble's capture graph (conditional handles belong to it)
+  int ens_begin(cudaStream_t s, cudaGraph_t root, int coarse_sweeps) {
+    if (!cap_st[0])
+      for (auto& c : cap_st) NHW_CU(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking));
     ens_saved_st = st;
+    ens_saved_sweeps = mg_coarse_sweeps;
+    mg_coarse_sweeps = coarse_sweeps;
     st = s;
     capturing = true;
+    cap_root = root;
+    cap_depth = 0;
     cap_level = 3;
     cap_err.clear();
     S.graph_mode = 1;
     S.h_go = 0;
+    return NHW_OK;
   }
   int ens_end() {
     st = ens_saved_st;
+    mg_coarse_sweeps = ens_saved_sweeps;
     capturing = false;
     S.graph_mode = 0;
     if (!cap_err.empty()) {
@@ -532,6 +542,11 @@ class Solver final : public SolverBase {
     source_terms();
     fluxes();
     stage_pre(s);
+  }
+  int ens_solve() { return poisson_solve(); }   // phase-by-phase, loops in conditional nodes
+  void ens_reset_counts() {
+    for (auto& c : cap_counts) c = 0;
+    cap_solves = 0;
   }
   void ens_stage_tail(int s) {   // eval_duvw after the solve, sponge
     stage_post(s);

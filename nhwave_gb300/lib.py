@@ -40,14 +40,15 @@ EXPORTS = [
 class EnsembleOpts(ctypes.Structure):
     """nhw_ensemble_opts (include/nhwave_gb300.h)."""
     _fields_ = [("cells_per_block", ctypes.c_int32), ("block_rows", ctypes.c_int32),
-                ("coarse_sweeps", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("coarse_sweeps", ctypes.c_int32), ("solver", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class EnsembleInfo(ctypes.Structure):
     """nhw_ensemble_info (include/nhwave_gb300.h)."""
     _fields_ = [("members", ctypes.c_int32), ("solve_launches_per_stage", ctypes.c_int32),
                 ("blocks_per_launch", ctypes.c_int32), ("max_resident_blocks", ctypes.c_int32),
-                ("kernels_per_step", ctypes.c_int64), ("cells", ctypes.c_int64), ("opts", EnsembleOpts)]
+                ("kernels_per_step", ctypes.c_int64), ("cells", ctypes.c_int64), ("opts", EnsembleOpts),
+                ("kernels_launched", ctypes.c_int64)]
 
 
 class NhwError(RuntimeError):
@@ -264,10 +265,11 @@ class Ensemble:
     step (nhw_ensemble_*).  ``members`` are set-up ``Scenario`` objects; they
     stay usable for field access, and must outlive the ensemble."""
 
-    def __init__(self, members, cells_per_block: int = 0, block_rows: int = 0, coarse_sweeps: int = 0):
+    def __init__(self, members, cells_per_block: int = 0, block_rows: int = 0, coarse_sweeps: int = 0,
+                 solver: int = 0):
         self.members = list(members)
         arr = (ctypes.c_void_p * len(self.members))(*[m._h for m in self.members])
-        o = EnsembleOpts(cells_per_block, block_rows, coarse_sweeps)
+        o = EnsembleOpts(cells_per_block, block_rows, coarse_sweeps, solver)
         self._e = ctypes.c_void_p()
         _chk(load().nhw_ensemble_create(arr, len(self.members), ctypes.byref(o), ctypes.byref(self._e)),
              "nhw_ensemble_create")

@@ -1,10 +1,13 @@
 """GPU: ensembles -- many scenarios advanced by one graph launch per step,
 their pressure solves sharing persistent cooperative launches.
 
-* a member's results are the same bits alone and in a mix (its solve group's
-  block count depends only on its own size);
+* a member's results are the same bits alone and in a mix, with either
+  solver (the persistent groups' block counts depend only on a member's own
+  size);
 * ensemble steps agree with the same scenarios stepped one by one through
-  nhw_step (the phase-by-phase solver), to the solver tolerance;
+  nhw_step: bit for bit with the phase-by-phase solver on every member's
+  branch (the same kernels in the same order), to the solver tolerance with
+  the persistent groups;
 * members whose run is over are skipped on the device, each at its own
   SIM_STEPS;
 * the autotuner returns one of its candidate settings and the ensemble
@@ -48,13 +51,14 @@ def _mk(spec):
     return lib.Scenario(p, d, e, u)
 
 
+@pytest.mark.parametrize("solver", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_member_alone_equals_member_in_mix(precision, gpu_lib):
+def test_member_alone_equals_member_in_mix(precision, solver, gpu_lib):
     from nhwave_gb300 import fields as F, lib
     specs = _ensemble_members(precision)
     mix = [_mk(s) for s in specs]
     alone = _mk(specs[1])
-    opts = dict(cells_per_block=4096, block_rows=8, coarse_sweeps=6)
+    opts = dict(cells_per_block=4096, block_rows=8, coarse_sweeps=6, solver=solver)
     with lib.Ensemble(mix, **opts) as em, lib.Ensemble([alone], **opts) as ea:
         assert em.step(3) == 0
         assert ea.step(3) == 0
@@ -65,13 +69,14 @@ def test_member_alone_equals_member_in_mix(precision, gpu_lib):
         assert mix[1].scalars().total_krylov_iters == alone.scalars().total_krylov_iters
 
 
+@pytest.mark.parametrize("solver", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_ensemble_matches_single_steps(precision, gpu_lib):
+def test_ensemble_matches_single_steps(precision, solver, gpu_lib):
     from nhwave_gb300 import fields as F, lib
     names = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
     ens = [_member(n, precision) for n in names]
     ref = [_member(n, precision) for n in names]
-    with lib.Ensemble(ens) as e:
+    with lib.Ensemble(ens, solver=solver) as e:
         info = e.info()
         assert info.members == 4 and info.kernels_per_step > 0
         for _ in range(3):
@@ -87,8 +92,11 @@ def test_ensemble_matches_single_steps(precision, gpu_lib):
         for f in ("ETA", "P", "U"):
             fid = getattr(F, f)
             sl = a.shape.interior(fid)
-            r = rel_l2(a.get(fid)[sl], b.get(fid)[sl])
-            assert r < lim, f"{n} {f}: {r:.3e}"
+            if solver == 0:
+                assert np.array_equal(a.get(fid), b.get(fid)), f"{n} {f} differs"
+            else:
+                r = rel_l2(a.get(fid)[sl], b.get(fid)[sl])
+                assert r < lim, f"{n} {f}: {r:.3e}"
 
 
 def test_members_stop_at_their_own_sim_steps(gpu_lib):
@@ -97,6 +105,8 @@ def test_members_stop_at_their_own_sim_steps(gpu_lib):
     b = _member("tiny_c4", 1, sim_steps=5, total_time=1e9)
     with lib.Ensemble([a, b]) as e:
         assert e.step(8) == 0
+        launched = e.info().kernels_launched
+    assert launched > 0
     assert a.scalars().run_step == 2
     assert b.scalars().run_step == 5
 
@@ -107,6 +117,7 @@ def test_autotuner_picks_a_candidate(gpu_lib):
     ms = [_mk(s) for s in specs]
     with lib.Ensemble(ms) as e:
         o = e.tune(1)
+        assert o.solver in (0, 1)
         assert o.cells_per_block in (4096, 16384, 65536)
         assert o.block_rows in (8, 16)
         assert o.coarse_sweeps in (4, 6)
