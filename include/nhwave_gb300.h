@@ -165,6 +165,10 @@ typedef struct nhw_handle nhw_handle;
  * handle; one host thread per handle. */
 int nhw_create(const nhw_params* params, nhw_handle** out);
 int nhw_destroy(nhw_handle* h);
+/* Device memory (bytes) a handle created with these parameters holds, found
+ * without allocating: the admission test of a memory-budgeted request loop.
+ * Needs the CUDA device (kernel occupancy is part of the plan). */
+int nhw_device_bytes(const nhw_params* params, int64_t* bytes);
 
 /* Set-up without the Fortran driver: generate_grid + read_bathymetry (from
  * `depth`, Mglob x Nglob for CELL_CENTER, (Mglob+1) x (Nglob+1) for

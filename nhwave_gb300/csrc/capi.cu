@@ -53,6 +53,15 @@ int nhw_create(const nhw_params* params, nhw_handle** out) {
   return NHW_OK;
 }
 
+int nhw_device_bytes(const nhw_params* params, int64_t* bytes) {
+  if (!params || !bytes) return NHW_ERR_ARG;
+  size_t b = 0;
+  const int rc = params->precision == NHW_FP32_IR ? nhw::device_bytes_fp32(*params, &b)
+                                                  : nhw::device_bytes_fp64(*params, &b);
+  *bytes = (int64_t)b;
+  return rc;
+}
+
 int nhw_destroy(nhw_handle* h) {
   if (!h) return NHW_ERR_ARG;
   if (h->s) h->s->bind();

@@ -5,6 +5,7 @@
 
 namespace nhw {
 SolverBase* make_solver_fp32(const nhw_params& p, int* status) { return make_solver_t<float>(p, status); }
+int device_bytes_fp32(const nhw_params& p, size_t* bytes) { return device_bytes_t<float>(p, bytes); }
 EnsembleBase* make_ensemble_fp32(SolverBase* const* members, int n, const nhw_ensemble_opts* o, int* status) {
   return make_ensemble_t<float>(members, n, o, status);
 }

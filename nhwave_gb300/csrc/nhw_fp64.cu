@@ -5,6 +5,7 @@
 
 namespace nhw {
 SolverBase* make_solver_fp64(const nhw_params& p, int* status) { return make_solver_t<double>(p, status); }
+int device_bytes_fp64(const nhw_params& p, size_t* bytes) { return device_bytes_t<double>(p, bytes); }
 EnsembleBase* make_ensemble_fp64(SolverBase* const* members, int n, const nhw_ensemble_opts* o, int* status) {
   return make_ensemble_t<double>(members, n, o, status);
 }

@@ -113,6 +113,7 @@ class Solver final : public SolverBase {
   cudaStream_t st = nullptr;
   char* arena = nullptr;
   size_t arena_bytes = 0;
+  bool estimate_only = false;
   DevScal* h_sc = nullptr;     // pinned mirror of S.sc
   double* d_out = nullptr;     // small device output
   double* h_out = nullptr;
@@ -313,6 +314,10 @@ class Solver final : public SolverBase {
     add(&d_stage, sizeof(double) * stage_elems);
     size_t total = 0;
     for (auto& e : plan) total += (e.second + 255) & ~size_t(255);
+    if (estimate_only) {   // device bytes a scenario would hold, nothing allocated
+      arena_bytes = total;
+      return NHW_OK;
+    }
     NHW_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     cudaError_t e = cudaMalloc((void**)&arena, total);
     if (e != cudaSuccess) {
@@ -1231,6 +1236,18 @@ class Solver final : public SolverBase {
 
 SolverBase* make_solver_fp64(const nhw_params& p, int* status);
 SolverBase* make_solver_fp32(const nhw_params& p, int* status);
+int device_bytes_fp64(const nhw_params& p, size_t* bytes);
+int device_bytes_fp32(const nhw_params& p, size_t* bytes);
+
+// device memory a scenario's handle holds (its arena), computed without allocating
+template <class T>
+int device_bytes_t(const nhw_params& p, size_t* bytes) {
+  Solver<T> s;
+  s.estimate_only = true;
+  const int rc = s.create(p);
+  *bytes = s.arena_bytes;
+  return rc;
+}
 
 template <class T>
 SolverBase* make_solver_t(const nhw_params& p, int* status) {

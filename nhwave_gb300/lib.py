@@ -33,7 +33,7 @@ EXPORTS = [
     "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
     "nhw_estimate_dt_noalloc",
     "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
-    "nhw_ensemble_get_info", "nhw_ensemble_destroy",
+    "nhw_ensemble_get_info", "nhw_ensemble_destroy", "nhw_device_bytes",
 ]
 
 
@@ -101,6 +101,7 @@ def load(path: str | None = None):
     L.nhw_ensemble_tune.argtypes = [vp, i32, P(EnsembleOpts)]
     L.nhw_ensemble_get_info.argtypes = [vp, P(EnsembleInfo)]
     L.nhw_ensemble_destroy.argtypes = [vp]
+    L.nhw_device_bytes.argtypes = [P(NhwParams), P(ctypes.c_int64)]
     L.nhw_status_string.argtypes = [ctypes.c_int]
     L.nhw_status_string.restype = ctypes.c_char_p
     L.nhw_last_error.argtypes = []
@@ -258,6 +259,13 @@ class Scenario:
         if a.size != int(np.prod(shp)):
             raise ValueError(f"field {F.NAMES[field]} wants {shp}, got {a.size} elements")
         _chk(load().nhw_set_field(self._h, field, _ptr(a)), "nhw_set_field")
+
+
+def device_bytes(params: NhwParams) -> int:
+    """Device memory a Scenario with these parameters would hold (nhw_device_bytes)."""
+    b = ctypes.c_int64(0)
+    _chk(load().nhw_device_bytes(ctypes.byref(params), ctypes.byref(b)), "nhw_device_bytes")
+    return b.value
 
 
 class Ensemble:
