@@ -16,6 +16,15 @@ sponge).  The metric is cell-updates/s = M*N*K*steps / device time.
   fp64    the plain FP64 drop-in on the same workload and steps; the FP32+IR
           eta is compared with it (relative L2)
 
+  ensemble  config 4: 256 scenarios of uneven size (the C4 generator) advanced
+          together, one CUDA graph launch per ensemble step; device-timed
+          over a few steps (the full 500-step run is out of a bench's reach)
+  serving   config 5: Poisson arrivals at 50 requests/s replayed in real time
+          through the continuous-batching loop under a 150 GB HBM budget;
+          p50/p99 time-to-solution and cell-updates/s, FP32+IR and FP64; each
+          request runs a bounded number of steps instead of 60 s of
+          simulated time (stated in the line)
+
 ``--impl reference`` times the CPU restatement of the reference (the oracle;
 the Fortran reference cannot be compiled on this machine) on the host cores.
 Multi-GPU (``--gpus N`` under torchrun): independent replicas, one per GPU.
@@ -234,6 +243,86 @@ def roofline(prof, cells, elem_bytes):
             "launches": launches, "kernel_time_shares": shares}
 
 
+# ---------------------------------------------------------------- replicas
+def replica_throughput(ms_local: float, cells: int, steps: int, world: int, device: str = "cpu"):
+    """Whole-job throughput of `world` independent replicas (one per GPU, no
+    data-path collective): every rank advanced `cells` cells `steps` steps;
+    the elapsed time is the maximum over ranks.  Returns (max ms, cell-updates/s)."""
+    t_max = ms_local
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        tt = torch.tensor([ms_local], device=device, dtype=torch.float64)
+        td.all_reduce(tt, op=td.ReduceOp.MAX)
+        t_max = float(tt.item())
+    return t_max, cells * steps * world / (t_max / 1000.0)
+
+
+# --------------------------------------------------------- C4 and C5 legs
+ENSEMBLE_MEMBERS = 256
+SERVE_RATE, SERVE_WINDOW_S, SERVE_STEPS, SERVE_BUDGET = 50.0, 2.0, 8, 150 << 30
+
+
+def run_ensemble(local, steps=3, warmup=2):
+    """Config 4: 256 seeded members, FP32+IR, one ensemble graph per step."""
+    from nhwave_gb300 import lib, scenarios as S
+    from nhwave_gb300.params import NHW_FP32_IR
+    specs = S.ensemble(ENSEMBLE_MEMBERS, seed=2024)
+    ms = []
+    for (p, d, e, u) in specs:
+        p.precision = NHW_FP32_IR
+        p.device = local
+        ms.append(lib.Scenario(p, d, e, u))
+    cells = sum(m.params.Mglob * m.params.Nglob * m.params.Kglob for m in ms)
+    with lib.Ensemble(ms) as E:
+        E.step(warmup)
+        l0 = E.info().kernels_launched
+        ms_dev = E.run_timed(steps)
+        info = E.info()
+    its = [m.scalars().total_krylov_iters / max(1, m.scalars().poisson_solves) for m in ms]
+    for m in ms:
+        m.close()
+    return {"members": ENSEMBLE_MEMBERS, "cells": cells, "steps": steps, "warmup": warmup,
+            "value": cells * steps / (ms_dev / 1000.0), "unit": UNIT, "ms_per_step": ms_dev / steps,
+            "gpu_launches": int(info.kernels_launched - l0), "solver": int(info.opts.solver),
+            "krylov_iters_per_solve_mean": round(float(sum(its) / len(its)), 1),
+            "precision": "FP32+IR", "generator": "scenarios.ensemble(256, seed=2024)"}
+
+
+def run_serving(local):
+    """Config 5 (bounded): the request loop on a replayed Poisson stream, FP32+IR then FP64."""
+    import numpy as np
+    from nhwave_gb300 import scenarios as S, serve
+    from nhwave_gb300.params import NHW_FP32_IR, NHW_FP64
+    rng = np.random.default_rng(77)
+    t, arr = 0.0, []
+    gen = np.random.default_rng(2025)
+    while True:
+        t += float(rng.exponential(1.0 / SERVE_RATE))
+        if t > SERVE_WINDOW_S:
+            break
+        p, d, e, u = S.ensemble_member(gen)
+        p.sim_steps = SERVE_STEPS
+        p.total_time = 1e30
+        p.device = local
+        arr.append((t, p, d, e, u))
+    out = {"rate_per_s": SERVE_RATE, "window_s": SERVE_WINDOW_S, "requests": len(arr),
+           "steps_per_request": SERVE_STEPS, "hbm_budget_bytes": SERVE_BUDGET,
+           "note": "each request runs SERVE_STEPS steps (not 60 s of simulated time) so that the run stays bounded"}
+    eta = {}
+    for name, prec in (("fp32ir", NHW_FP32_IR), ("fp64", NHW_FP64)):
+        srv = serve.Server(SERVE_BUDGET, precision=prec, steps_per_round=4)
+        st = srv.serve(arr)
+        first = min(srv.finished, key=lambda r: r.id)
+        eta[name] = first.result["ETA"]
+        srv.close()
+        out[name] = {k: st[k] for k in ("p50_s", "p99_s", "cell_updates_per_s", "wall_s", "rounds",
+                                        "ensemble_rebuilds") if k in st}
+    a, b = eta["fp32ir"], eta["fp64"]
+    out["eta_rel_l2_fp32ir_vs_fp64_first_request"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return out
+
+
 # --------------------------------------------------------------- GPU arm
 def run_gpu_arm(args):
     rank, world, local = dist_env()
@@ -250,6 +339,7 @@ def run_gpu_arm(args):
     def make(prec):
         p, d, e, u = S.make("c2", precision=prec, seed=rank)
         p.device = local
+        p.krylov_kernel = args.krylov_kernel
         return p, d, e, u
 
     # ---- FP32+IR, device-timed (value)
@@ -268,12 +358,7 @@ def run_gpu_arm(args):
     clocks = clk.summary()
     sc = g.scalars()
     iters_per_solve = sc.total_krylov_iters / max(1, sc.poisson_solves)
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        td.all_reduce(tt, op=td.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = cells * args.steps * world / (t_max / 1000.0)
+    t_max, value = replica_throughput(ms, cells, args.steps, world, device="cuda")
     eta32 = g.get(F.ETA)[g.shape.interior(F.ETA)]
     # ---- profile pass: per-kernel CUDA events over the same number of steps
     g.profile(True)
@@ -326,6 +411,9 @@ def run_gpu_arm(args):
     g.close()
     e2e_val = cells * args.steps * world / e2e_s
 
+    ens = run_ensemble(local) if not args.no_ensemble else None
+    srv = run_serving(local) if not args.no_serving else None
+
     line = None
     if rank == 0:
         rl = roofline(prof, cells, 4)
@@ -348,6 +436,10 @@ def run_gpu_arm(args):
             "roofline": rl,
             "clocks": clocks,
         }
+        if ens:
+            line["ensemble"] = ens
+        if srv:
+            line["serving"] = srv
     if world > 1:
         td.barrier()
     if rank == 0:
@@ -367,6 +459,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="FP32+IR timed region and profile pass only")
+    ap.add_argument("--krylov-kernel", type=int, default=0, choices=[0, 1],
+                    help="pressure solver of the C2 legs: 0 phase by phase, 1 one persistent launch per solve")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the config-4 ensemble leg")
+    ap.add_argument("--no-serving", action="store_true", help="skip the config-5 serving leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -113,7 +113,10 @@ typedef struct nhw_params {
                                               graph conditional nodes; 1: the whole solve
                                               in one persistent cooperative launch (needs
                                               the multigrid preconditioner)            */
-  int32_t reserved[4];
+  int32_t mg_coarse_sweeps;                /* red-black sweeps on the coarsest level (0: 2) */
+  int32_t mg_cta_columns;                  /* levels with at most this many columns run in
+                                              one thread block (0: 64)                */
+  int32_t reserved[2];
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */
@@ -253,7 +256,7 @@ typedef struct nhw_ensemble nhw_ensemble;
 typedef struct nhw_ensemble_opts {
   int32_t cells_per_block;   /* unknowns per block of a member's solve (0: 16384)  */
   int32_t block_rows;        /* solve blocks are 32 x block_rows threads: 8 or 16  */
-  int32_t coarse_sweeps;     /* red-black sweeps on the coarsest level (0: 6)      */
+  int32_t coarse_sweeps;     /* red-black sweeps on the coarsest level (0: 2)      */
   int32_t solver;            /* 0: every member's phase-by-phase solve on its own
                                 branch, loops in conditional nodes; 1: the solves
                                 of all members as groups of persistent launches */
@@ -278,8 +281,8 @@ int nhw_ensemble_create(nhw_handle* const* members, int32_t n, const nhw_ensembl
 int nhw_ensemble_step(nhw_ensemble* e, int32_t nsteps);
 /* nsteps ensemble steps timed with CUDA events on the ensemble's stream */
 int nhw_ensemble_run_timed(nhw_ensemble* e, int32_t nsteps, double* device_ms);
-/* Autotuner: times candidate settings (cells per block, block height, coarse
- * sweeps) on real ensemble steps -- the members advance by steps_per_trial
+/* Autotuner: times candidate settings (solver form, cells per block, block
+ * height, coarse sweeps) on real ensemble steps -- the members advance by steps_per_trial
  * steps per candidate -- and keeps the fastest; writes it to *chosen. */
 int nhw_ensemble_tune(nhw_ensemble* e, int32_t steps_per_trial, nhw_ensemble_opts* chosen);
 int nhw_ensemble_get_info(nhw_ensemble* e, nhw_ensemble_info* out);

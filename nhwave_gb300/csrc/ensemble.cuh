@@ -14,9 +14,9 @@
 // tuning options, never on the other members: a member's results are the same
 // bits alone and in any mix.
 //
-// Tuning: blocks per group (cells per block), block height and coarse-level
-// sweeps are chosen by timing candidate settings on real ensemble steps
-// (Ensemble::tune).
+// Tuning: the solver form, blocks per group (cells per block), block height
+// and coarse-level sweeps are chosen by timing candidate settings on real
+// ensemble steps (Ensemble::tune).
 #pragma once
 #include "solver.cuh"
 
@@ -71,7 +71,7 @@ class Ensemble final : public EnsembleBase {
   static void defaults(nhw_ensemble_opts* o) {
     if (o->cells_per_block <= 0) o->cells_per_block = 16384;
     if (o->block_rows != 8 && o->block_rows != 16) o->block_rows = kPsBYEnsemble;
-    if (o->coarse_sweeps <= 0) o->coarse_sweeps = 6;
+    if (o->coarse_sweeps <= 0) o->coarse_sweeps = 2;
     if (o->solver != 1) o->solver = 0;
   }
 
@@ -311,7 +311,7 @@ class Ensemble final : public EnsembleBase {
   int tune(int steps_per_trial, nhw_ensemble_opts* chosen) override {
     if (steps_per_trial < 1) steps_per_trial = 1;
     std::vector<nhw_ensemble_opts> cand;
-    for (int w : {4, 6}) {
+    for (int w : {2, 4, 6}) {
       nhw_ensemble_opts o{};
       o.solver = 0;
       o.coarse_sweeps = w;

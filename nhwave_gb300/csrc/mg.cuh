@@ -184,13 +184,47 @@ __global__ void __launch_bounds__(128) k_mg_smooth(MGL<T> L, const DevScal* sc, 
   }
 }
 
+// Right-hand sides of a half-sweep:
+//   MgB            b as stored;
+//   MgInP / MgInS  the BiCGSTAB vectors p = r + beta (p - omega v) and
+//                  s = r - alpha v, formed on the fine level by the sweep that
+//                  owns each column (colour 0 in the first half-sweep, colour 1
+//                  in the second) and stored -- no launch of their own.
+template <class T>
+struct MgB {
+  const T* b;
+  __device__ __forceinline__ T operator()(const DevScal*, int ic, int, int, int) const { return b[ic]; }
+};
+template <class T>
+struct MgInP {
+  T* p;
+  const T* r;
+  const T* v;
+  __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
+    const T val = r[ic] + (T)sc->beta * (p[ic] - (T)sc->omega * v[ic]);
+    p[ic] = val;
+    return val;
+  }
+};
+template <class T>
+struct MgInS {
+  T* s;
+  const T* r;
+  const T* v;
+  __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
+    const T val = r[ic] - (T)sc->alpha * v[ic];
+    s[ic] = val;
+    return val;
+  }
+};
+
 // Same half-sweep, block-parallel: a block holds 32 columns of the colour and
 // up to 32 levels (blockDim = 32 x min(K,32)); every thread forms the line
 // right-hand sides of its (column, level) cells -- loads coalesced along the
 // columns -- into shared memory, then one warp runs the Thomas sweeps there.
-template <class T, bool kProlong>
+template <class T, bool kProlong, class In>
 __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal* sc, int color, int zero_x,
-                                                        Prolong<T> P) {
+                                                        Prolong<T> P, In in) {
   if (sc->conv) return;
   extern __shared__ unsigned char smem_raw[];
   T* sh = reinterpret_cast<T*>(smem_raw);
@@ -214,7 +248,7 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
       const int ic = col + MN * k;
       T off = (T)0;
       if (!zero_x) off = kProlong ? off_column_p(L, L.x, P, ic, ii, jj, k) : off_column(L, L.x, ic, ii, jj, k);
-      rhs = L.b[ic] - off;
+      rhs = in(sc, ic, ii, jj, k) - off;
       a = k > 0 ? L.coef[2 * n + ic] : (T)0;
       inv = L.linv[ic];
       cp = L.lcp[ic];

@@ -135,7 +135,7 @@ class Solver final : public SolverBase {
   std::vector<MGL<T>> mg;
   bool use_mg = true;
   T mg_w = (T)1;
-  int mg_coarse_sweeps = 6;
+  int mg_coarse_sweeps = 2;   // red-black sweeps on the coarsest level (fastest of 2, 4, 6 on C2)
   // persistent solve (psolve.cuh): one cooperative launch per pressure solve
   bool use_persistent = false;
   int ps_nb = 0;             // blocks of the launch
@@ -262,6 +262,8 @@ class Solver final : public SolverBase {
     // multigrid levels: horizontal 2x2 aggregation while a direction has >= 4 cells
     use_mg = p.precond == 0;
     mg_w = (T)(p.mg_weight > 0.f ? p.mg_weight : 1.0f);
+    if (p.mg_coarse_sweeps > 0) mg_coarse_sweeps = p.mg_coarse_sweeps;
+    if (p.mg_cta_columns > 0) cta_columns = p.mg_cta_columns;
     mg.clear();
     {
       MGL<T> L0{};
@@ -333,10 +335,13 @@ class Solver final : public SolverBase {
     mg[0].coef = S.coefT; mg[0].cxr = nullptr; mg[0].cyr = nullptr;
     mg[0].lcp = S.lcp; mg[0].linv = S.linv;
     for (auto& L : mg) { L.cxx = (T)S.cxx; L.cyy = (T)S.cyy; }
-    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(T) * 4 * 32 * 64)));
-    NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(sizeof(T) * 4 * 32 * 64)));
+    {
+      const int shm = (int)(sizeof(T) * 4 * 32 * 64);
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, true, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+    }
     NHW_CU(cudaFuncSetAttribute(k_mg_cta_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(T) * 4 * 32 * 64)));
     NHW_CU(cudaMallocHost((void**)&h_sc, sizeof(DevScal)));
@@ -481,7 +486,7 @@ class Solver final : public SolverBase {
     g.S.graph_mode = 0;
     const int nl = (int)mg.size();
     int lc = 0;
-    while (lc < nl && (long long)mg[lc].M * mg[lc].N > kCtaColumns) ++lc;
+    while (lc < nl && (long long)mg[lc].M * mg[lc].N > cta_columns) ++lc;
     if (nl - lc > kCtaLevels) lc = nl - kCtaLevels;
     if (lc >= nl) lc = nl - 1;   // the first block always solves at least the coarsest level
     for (int l = 0; l < nl; ++l) g.L[l] = mg[l];
@@ -828,15 +833,13 @@ class Solver final : public SolverBase {
   void one_iteration() {
     const unsigned cb = cdiv((long long)S.M * S.N, 128);
     if (use_mg) {
-      L("bicg_p", [&] { k_bicg_p_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
-      vcycle(S.kp, S.kph);
+      vcycle(S.kp, S.kph, 1);   // p is formed by the fine level's first sweeps
     } else {
       L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
     }
     L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
     if (use_mg) {
-      L("bicg_s", [&] { k_bicg_s_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
-      vcycle(S.ks, S.ksh);
+      vcycle(S.ks, S.ksh, 2);   // s likewise
     } else {
       L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
     }
@@ -844,8 +847,9 @@ class Solver final : public SolverBase {
     L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S); });
   }
   // multigrid V-cycle: x ~= A^-1 b on level 0
-  static constexpr int kCtaColumns = 64;    // levels up to this many columns run in one block
-  void smooth(const MGL<T>& Lv, int color, int zero_x, int level, const Prolong<T>& P) {
+  int cta_columns = 64;    // levels up to this many columns run in one block (mg_cta_columns)
+  template <class In>
+  void smooth(const MGL<T>& Lv, int color, int zero_x, int level, const Prolong<T>& P, In in) {
     static const char* names[] = {"mg_smooth_l0", "mg_smooth_l1", "mg_smooth_l2", "mg_smooth_l3",
                                   "mg_smooth_l4", "mg_smooth_l5", "mg_smooth_l6", "mg_smooth_l7+"};
     const int pair = (Lv.M + 1 - color) / 2 + (Lv.M + color) / 2;
@@ -854,26 +858,35 @@ class Solver final : public SolverBase {
     const size_t shm = sizeof(T) * 4 * 32 * Lv.K;
     L(names[level < 7 ? level : 7], [&] {
       if (P.xc)
-        k_mg_smooth_blk<T, true><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P);
+        k_mg_smooth_blk<T, true, In><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
       else
-        k_mg_smooth_blk<T, false><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P);
+        k_mg_smooth_blk<T, false, In><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
     });
   }
-  void vcycle(const T* b, T* x) {
-    mg[0].b = (T*)b;
+  // fine_in: 0 b as given; 1 b = p formed on the fly; 2 b = s formed on the fly
+  void vcycle(T* b, T* x, int fine_in) {
+    mg[0].b = b;
     mg[0].x = x;
     const int nl = (int)mg.size();
     // first level handled by the single-block cycle
     int lc = 0;
-    while (lc < nl && (long long)mg[lc].M * mg[lc].N > kCtaColumns) ++lc;
+    while (lc < nl && (long long)mg[lc].M * mg[lc].N > cta_columns) ++lc;
     if (nl - lc > kCtaLevels) lc = nl - kCtaLevels;
     const Prolong<T> none{nullptr, (T)0, 1, 1, 1, 1, 1, 1};
+    if (lc == 0 && fine_in != 0) {   // the whole hierarchy in one block: form b first
+      if (fine_in == 1) L("bicg_p", [&] { k_bicg_p_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+      else L("bicg_s", [&] { k_bicg_s_cell<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+    }
+    static const char* rnames[] = {"mg_restrict_l0", "mg_restrict_l1", "mg_restrict_l2", "mg_restrict_l3",
+                                   "mg_restrict_l4", "mg_restrict_l5", "mg_restrict_l6", "mg_restrict_l7+"};
     for (int l = 0; l < lc; ++l) {
-      smooth(mg[l], 0, 1, l, none);
-      smooth(mg[l], 1, 0, l, none);
+      for (int color = 0; color < 2; ++color) {
+        const int zx = color == 0 ? 1 : 0;
+        if (l == 0 && fine_in == 1) smooth(mg[0], color, zx, 0, none, MgInP<T>{S.kp, S.kr, S.kv});
+        else if (l == 0 && fine_in == 2) smooth(mg[0], color, zx, 0, none, MgInS<T>{S.ks, S.kr, S.kv});
+        else smooth(mg[l], color, zx, l, none, MgB<T>{mg[l].b});
+      }
       MGL<T> f = mg[l], c = mg[l + 1];
-      static const char* rnames[] = {"mg_restrict_l0", "mg_restrict_l1", "mg_restrict_l2", "mg_restrict_l3",
-                                     "mg_restrict_l4", "mg_restrict_l5", "mg_restrict_l6", "mg_restrict_l7+"};
       L(rnames[l < 7 ? l : 7], [&] { k_mg_restrict<T><<<cdiv(c.n, 256), 256, 0, st>>>(f, c, S.sc); });
     }
     if (lc < nl) {
@@ -889,8 +902,8 @@ class Solver final : public SolverBase {
       const MGL<T>& f = mg[l];
       const MGL<T>& c = mg[l + 1];
       const Prolong<T> pr{c.x, mg_w, f.rx, f.ry, c.M, c.M * c.N, f.M, f.M * f.N};
-      smooth(f, 1, 0, l, pr);
-      smooth(f, 0, 0, l, none);
+      smooth(f, 1, 0, l, pr, MgB<T>{f.b});
+      smooth(f, 0, 0, l, none, MgB<T>{f.b});
     }
   }
 

@@ -56,7 +56,9 @@ class NhwParams(ctypes.Structure):
         ("precond", ctypes.c_int32),
         ("mg_weight", ctypes.c_float),
         ("krylov_kernel", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("mg_coarse_sweeps", ctypes.c_int32),
+        ("mg_cta_columns", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
     def copy(self) -> "NhwParams":
