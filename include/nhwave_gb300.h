@@ -116,7 +116,8 @@ typedef struct nhw_params {
   int32_t mg_coarse_sweeps;                /* red-black sweeps on the coarsest level (0: 2) */
   int32_t mg_cta_columns;                  /* levels with at most this many columns run in
                                               one thread block (0: 64)                */
-  int32_t reserved[2];
+  int32_t mg_aggregate;                    /* multigrid aggregates of n x n columns (0: 2) */
+  int32_t reserved[1];
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

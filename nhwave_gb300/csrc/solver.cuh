@@ -271,7 +271,10 @@ class Solver final : public SolverBase {
       mg.push_back(L0);
       while (use_mg && mg.size() < 16) {
         MGL<T>& f = mg.back();
-        const int rx = f.M >= 4 ? 2 : 1, ry = f.N >= 4 ? 2 : 1;
+        // aggregates of agg x agg columns (agg = 2 by default) while a direction
+        // keeps at least two aggregates
+        const int agg = p.mg_aggregate > 1 ? p.mg_aggregate : 2;
+        const int rx = f.M >= 2 * agg ? agg : (f.M >= 4 ? 2 : 1), ry = f.N >= 2 * agg ? agg : (f.N >= 4 ? 2 : 1);
         if ((rx == 1 && ry == 1) || f.M * f.N <= 32) break;
         f.rx = rx; f.ry = ry;
         f.Mc = (f.M + rx - 1) / rx; f.Nc = (f.N + ry - 1) / ry;

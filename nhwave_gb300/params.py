@@ -58,7 +58,8 @@ class NhwParams(ctypes.Structure):
         ("krylov_kernel", ctypes.c_int32),
         ("mg_coarse_sweeps", ctypes.c_int32),
         ("mg_cta_columns", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("mg_aggregate", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 1),
     ]
 
     def copy(self) -> "NhwParams":
