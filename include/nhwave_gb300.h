@@ -214,6 +214,20 @@ int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step);
  * it.  *steps_done counts the steps taken (plus the one that hit DT_MIN). */
 int nhw_run(nhw_handle* h, int32_t nsteps, int32_t* steps_done);
 
+/* Checkpoint / resume.  The reference's hot start rereads f15.6 text files
+ * written at output intervals (src/nhwave.F:3513-3690), which loses bits;
+ * these three calls save and restore a scenario's complete state instead, so
+ * a resumed run continues bit for bit: every array a step reads before it
+ * writes it (grids, 2-D fields, masks, 3-D fields, P) and the device scalars
+ * (TIME, dt, RUN_STEP, solver counters).  The buffer is host memory of
+ * nhw_checkpoint_bytes bytes.  nhw_load_state needs a handle created with the
+ * same parameters and set up from the same inputs (nhw_setup), as the
+ * reference's hot start rereads input.txt and the depth file; a checkpoint of
+ * another grid, precision or library build is rejected with NHW_ERR_ARG. */
+int nhw_checkpoint_bytes(nhw_handle* h, int64_t* bytes);
+int nhw_save_state(nhw_handle* h, void* host, int64_t bytes);
+int nhw_load_state(nhw_handle* h, const void* host, int64_t bytes);
+
 /* FP64 device reduction of statistics' MassVolume = sum(D*dx*dy). */
 int nhw_mass(nhw_handle* h, double* mass);
 

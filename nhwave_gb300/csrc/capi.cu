@@ -195,6 +195,25 @@ int nhw_ensemble_destroy(nhw_ensemble* e) {
   return NHW_OK;
 }
 
+int nhw_checkpoint_bytes(nhw_handle* h, int64_t* bytes) {
+  NHW_GUARD(h);
+  if (!bytes) return NHW_ERR_ARG;
+  size_t b = 0;
+  const int rc = h->s->checkpoint_bytes(&b);
+  *bytes = (int64_t)b;
+  return rc;
+}
+int nhw_save_state(nhw_handle* h, void* host, int64_t bytes) {
+  NHW_GUARD(h);
+  if (bytes < 0) return NHW_ERR_ARG;
+  return h->s->save_state(host, (size_t)bytes);
+}
+int nhw_load_state(nhw_handle* h, const void* host, int64_t bytes) {
+  NHW_GUARD(h);
+  if (bytes < 0) return NHW_ERR_ARG;
+  return h->s->load_state(host, (size_t)bytes);
+}
+
 int nhw_mass(nhw_handle* h, double* mass) {
   NHW_GUARD(h);
   if (!mass) return NHW_ERR_ARG;

@@ -57,6 +57,9 @@ class SolverBase {
   virtual int run(int nsteps, int* done) = 0;
   virtual int profile(int on) = 0;
   virtual int profile_report(char* buf, int len) = 0;
+  virtual int checkpoint_bytes(size_t* bytes) = 0;
+  virtual int save_state(void* host, size_t bytes) = 0;
+  virtual int load_state(const void* host, size_t bytes) = 0;
 };
 
 template <class T>
@@ -114,6 +117,7 @@ class Solver final : public SolverBase {
   char* arena = nullptr;
   size_t arena_bytes = 0;
   bool estimate_only = false;
+  size_t state_bytes = 0;   // arena prefix that holds the prognostic state (grids .. P)
   DevScal* h_sc = nullptr;     // pinned mirror of S.sc
   double* d_out = nullptr;     // small device output
   double* h_out = nullptr;
@@ -334,6 +338,8 @@ class Solver final : public SolverBase {
     NHW_CU(cudaMemsetAsync(arena, 0, total, st));
     size_t off = 0;
     for (auto& e2 : plan) { *e2.first = arena + off; off += (e2.second + 255) & ~size_t(255); }
+    // everything a step carries to the next lies in front of the Poisson scratch
+    state_bytes = (size_t)((char*)(S.P + n3) - arena);
     if (!kFP32) S.coefT = (T*)S.coef64;
     mg[0].coef = S.coefT; mg[0].cxr = nullptr; mg[0].cyr = nullptr;
     mg[0].lcp = S.lcp; mg[0].linv = S.linv;
@@ -1241,6 +1247,59 @@ class Solver final : public SolverBase {
     }
     return (int)out.size();
   }
+  // ------------------------------------------------------ checkpoint/resume
+  // A snapshot is a header, the device scalars (TIME, dt, RUN_STEP, solver
+  // counters) and the arena prefix from the grids through P: every array a
+  // step reads before writing it.  The Poisson and Krylov arrays after it are
+  // rebuilt by every solve and are not saved.
+  struct CkptHeader {
+    char magic[8];
+    int32_t version, precision, M, N, K, reserved;
+    uint64_t state_bytes, scal_bytes;
+  };
+  size_t ckpt_size() const { return sizeof(CkptHeader) + sizeof(DevScal) + state_bytes; }
+  int checkpoint_bytes(size_t* bytes) override {
+    *bytes = ckpt_size();
+    return NHW_OK;
+  }
+  int save_state(void* host, size_t bytes) override {
+    if (!ready) return NHW_ERR_STATE;
+    if (!host || bytes < ckpt_size()) return NHW_ERR_ARG;
+    CkptHeader h{};
+    std::memcpy(h.magic, "NHWCKPT1", 8);
+    h.version = 1;
+    h.precision = kFP32 ? NHW_FP32_IR : NHW_FP64;
+    h.M = S.M; h.N = S.N; h.K = S.K;
+    h.state_bytes = state_bytes;
+    h.scal_bytes = sizeof(DevScal);
+    char* out = static_cast<char*>(host);
+    std::memcpy(out, &h, sizeof(h));
+    NHW_CU(cudaStreamSynchronize(st));
+    NHW_CU(cudaMemcpy(out + sizeof(h), S.sc, sizeof(DevScal), cudaMemcpyDeviceToHost));
+    NHW_CU(cudaMemcpy(out + sizeof(h) + sizeof(DevScal), arena, state_bytes, cudaMemcpyDeviceToHost));
+    return NHW_OK;
+  }
+  int load_state(const void* host, size_t bytes) override {
+    if (!ready) return NHW_ERR_STATE;
+    if (!host || bytes < sizeof(CkptHeader)) return NHW_ERR_ARG;
+    CkptHeader h{};
+    std::memcpy(&h, host, sizeof(h));
+    if (std::memcmp(h.magic, "NHWCKPT1", 8) != 0 || h.version != 1) {
+      set_last_error("nhw_load_state: not a checkpoint of this library");
+      return NHW_ERR_ARG;
+    }
+    if (h.precision != (kFP32 ? NHW_FP32_IR : NHW_FP64) || h.M != S.M || h.N != S.N || h.K != S.K ||
+        h.state_bytes != state_bytes || h.scal_bytes != sizeof(DevScal) || bytes < ckpt_size()) {
+      set_last_error("nhw_load_state: checkpoint of a different grid, precision or build");
+      return NHW_ERR_ARG;
+    }
+    const char* in = static_cast<const char*>(host);
+    NHW_CU(cudaStreamSynchronize(st));
+    NHW_CU(cudaMemcpy(S.sc, in + sizeof(h), sizeof(DevScal), cudaMemcpyHostToDevice));
+    NHW_CU(cudaMemcpy(arena, in + sizeof(h) + sizeof(DevScal), state_bytes, cudaMemcpyHostToDevice));
+    return pull_scalars();
+  }
+
   int mass(double* m) override {
     L("mass", [&] { k_mass<T><<<1, 1, 0, st>>>(S, d_out); });
     NHW_CU(cudaMemcpyAsync(h_out, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));

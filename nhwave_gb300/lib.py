@@ -34,6 +34,7 @@ EXPORTS = [
     "nhw_estimate_dt_noalloc",
     "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
     "nhw_ensemble_get_info", "nhw_ensemble_destroy", "nhw_device_bytes",
+    "nhw_checkpoint_bytes", "nhw_save_state", "nhw_load_state",
 ]
 
 
@@ -102,6 +103,9 @@ def load(path: str | None = None):
     L.nhw_ensemble_get_info.argtypes = [vp, P(EnsembleInfo)]
     L.nhw_ensemble_destroy.argtypes = [vp]
     L.nhw_device_bytes.argtypes = [P(NhwParams), P(ctypes.c_int64)]
+    L.nhw_checkpoint_bytes.argtypes = [vp, P(ctypes.c_int64)]
+    L.nhw_save_state.argtypes = [vp, vp, ctypes.c_int64]
+    L.nhw_load_state.argtypes = [vp, vp, ctypes.c_int64]
     L.nhw_status_string.argtypes = [ctypes.c_int]
     L.nhw_status_string.restype = ctypes.c_char_p
     L.nhw_last_error.argtypes = []
@@ -202,6 +206,18 @@ class Scenario:
         done = ctypes.c_int32(0)
         _chk(load().nhw_run(self._h, n, ctypes.byref(done)), "nhw_run")
         return done.value
+
+    def save_state(self) -> np.ndarray:
+        """Complete state as a byte array (nhw_save_state); resume with load_state."""
+        n = ctypes.c_int64(0)
+        _chk(load().nhw_checkpoint_bytes(self._h, ctypes.byref(n)), "nhw_checkpoint_bytes")
+        buf = np.empty(n.value, dtype=np.uint8)
+        _chk(load().nhw_save_state(self._h, buf.ctypes.data, buf.size), "nhw_save_state")
+        return buf
+
+    def load_state(self, buf: np.ndarray):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        _chk(load().nhw_load_state(self._h, buf.ctypes.data, buf.size), "nhw_load_state")
 
     def run_timed(self, n: int) -> float:
         """Run n steps; device milliseconds from CUDA events on the handle's stream."""

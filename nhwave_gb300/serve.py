@@ -12,7 +12,10 @@ initial state) to integrate until its own TOTAL_TIME / SIM_STEPS.  The loop
   gate, so each result is exactly its scenario's own end state;
 * between rounds retires finished requests (their result fields are copied
   out, their memory freed) and admits newly arrived ones -- requests that
-  arrive while others are on the GPU join the batch as memory frees up.
+  arrive while others are on the GPU join the batch as memory frees up;
+* can preempt a running request (``preempt``): its state is checkpointed to
+  host memory and its device memory freed, and it resumes bit for bit when
+  it is admitted again.
 
 Time-to-solution of a request = the wall time from its arrival to the end of
 the round in which it finished.  ``stats()`` reports p50/p99 and throughput in
@@ -49,6 +52,8 @@ class Request:
     status: int = lib.OK
     steps: int = 0
     scenario: "lib.Scenario | None" = None
+    saved: "np.ndarray | None" = None      # checkpoint while preempted
+    preemptions: int = 0
     result: dict = dataclasses.field(default_factory=dict)
 
     @property
@@ -110,7 +115,11 @@ class Server:
                 break
             self.pending.popleft()
             r.scenario = lib.Scenario(r.params, r.depth, r.eta0, r.uvw0)
-            r.admitted = now
+            if r.saved is not None:          # a preempted request resumes where it stopped
+                r.scenario.load_state(r.saved)
+                r.saved = None
+            if r.admitted is None:
+                r.admitted = now
             self.used += r.bytes
             self.active.append(r)
 
@@ -176,6 +185,28 @@ class Server:
                     self.used -= r.bytes
             self.active = keep
         return done_ids
+
+    def preempt(self, rid: int) -> bool:
+        """Take an admitted request off the GPU between rounds: its complete
+        state goes to host memory (nhw_save_state), its device memory is freed
+        and it returns to the front of the queue; when it is admitted again it
+        resumes bit for bit (nhw_load_state).  Returns False if `rid` is not
+        on the GPU."""
+        for r in self.active:
+            if r.id == rid:
+                r.saved = r.scenario.save_state()
+                r.preemptions += 1
+                if self._ens is not None:
+                    self._ens.close()
+                    self._ens = None
+                    self._ens_key = ()
+                r.scenario.close()
+                r.scenario = None
+                self.used -= r.bytes
+                self.active.remove(r)
+                self.pending.appendleft(r)
+                return True
+        return False
 
     def drain(self):
         """Rounds until nothing is queued or active."""
