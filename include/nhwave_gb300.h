@@ -17,6 +17,7 @@
  *
  *   nhw_estimate_dt        <- estimate_dt          src/nhwave.F:3694-3874
  *   nhw_update_bathymetry  <- update_bathymetry    src/nhwave.F:5755-6071 (RIGID_3D)
+ *   nhw_update_wave_bc     <- update_wave_bc       src/nhwave.F:5514-5565 (LEF_LIN, LEF_SOL)
  *   nhw_update_mask        <- update_mask          src/nhwave.F:5403-5456
  *   nhw_update_vars        <- update_vars          src/nhwave.F:5459-5511
  *   nhw_source_terms       <- source_terms         src/source_terms.F:1-455 (INT_LIN + bed slope)
@@ -65,7 +66,10 @@ enum nhw_precision {
                        depth/eta/mask fields, FP64 Poisson residual + refinement     */
 };
 
-enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2 };
+/* INT_*: internal source strip (src/source_terms.F); LEF_*: waves fed through
+ * the west boundary, which then needs BC_X0 = 3 (src/waves.F:808-903) */
+enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
+                     NHW_WM_LEF_SOL = 4 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 
@@ -89,7 +93,9 @@ typedef struct nhw_params {
   int32_t viscous_flow;                    /* VISCOUS_FLOW (must be 0)                */
   int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
   int32_t itmax; double tol;               /* ITMAX TOL                               */
-  int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn (1 or 2)        */
+  int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
+                                              2 no-slip wall; BC_X0 = 3 wave inflow
+                                              with a LEF_* wavemaker                  */
   int32_t bc_z0;                           /* BC_Z0 (1)                               */
   double  visc;                            /* VISCOSITY (initial Cmu)                 */
   double  slat;                            /* slat -> fcor                            */
@@ -193,6 +199,7 @@ int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step);
 /* ------------------------------------------- the reference's subroutines */
 int nhw_estimate_dt(nhw_handle* h);
 int nhw_update_bathymetry(nhw_handle* h);
+int nhw_update_wave_bc(nhw_handle* h);
 int nhw_update_mask(nhw_handle* h);
 int nhw_update_vars(nhw_handle* h);
 int nhw_source_terms(nhw_handle* h);

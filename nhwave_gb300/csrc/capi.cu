@@ -105,6 +105,7 @@ int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step) {
 
 int nhw_estimate_dt(nhw_handle* h) { NHW_GUARD(h); return h->s->estimate_dt(); }
 int nhw_update_bathymetry(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_bathymetry(); return rc ? rc : h->s->sync(); }
+int nhw_update_wave_bc(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_wave_bc(); return rc ? rc : h->s->sync(); }
 int nhw_update_mask(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_mask(); return rc ? rc : h->s->sync(); }
 int nhw_update_vars(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_vars(); return rc ? rc : h->s->sync(); }
 int nhw_source_terms(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->source_terms(); return rc ? rc : h->s->sync(); }

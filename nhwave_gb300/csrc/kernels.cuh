@@ -156,6 +156,65 @@ __device__ __forceinline__ void reduce_finalize(const Dev<T>& S, double (&v)[NV]
 }
 
 // =========================================================================
+//   update_wave_bc: waves fed through the west boundary (BC_X0 = 3)
+//   (src/nhwave.F:5514-5565; LEF_LIN src/waves.F:808-855, LEF_SOL 869-903)
+// =========================================================================
+// one thread per row j (all Nloc rows for Ein/Din, interior rows for the
+// velocities), evaluated at the step's new TIME
+struct OpWaveBC {
+  static constexpr const char* kName = "wave_bc";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int, int j, int) const {
+    const double TIME = S.sc->time;
+    const double hfx = S.Hfx[i2(S, S.IB, j)];
+    const bool inner = j >= S.JB && j <= S.JE;
+    const int Nl = S.Nloc;
+    if (S.lef == 3) {   // LEF_LIN
+      const double A = S.lef_amp;
+      const double phs = S.yc[j] * S.lef_sinth * S.lef_wn;
+      const double arg = kPi / 2 - S.lef_segma * TIME + phs;
+      const double cs = cos(arg), sn = sin(arg);
+      const double E = 0.5 * A * cs;
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        const double ch = cosh(S.lef_wn * Zlev), sh = sinh(S.lef_wn * Zlev);
+        const double u = 0.5 * A * S.lef_segma * ch / S.lef_shd * cs - S.lef_stokes * 1.0;
+        S.Uin[j + Nl * k] = u * S.lef_costh;
+        S.Win[j + Nl * k] = 0.5 * A * S.lef_segma * sh / S.lef_shd * sn;
+        S.Vin[j + Nl * k] = u * S.lef_sinth;
+      }
+    } else if (S.lef == 4) {   // LEF_SOL
+      const double A = S.lef_amp, Dep = S.lef_dep, Atmp = S.lef_atmp;
+      const double Xc = S.lef_xstart - S.lef_cel * TIME;
+      const double ch = cosh(Atmp * Xc), sh = sinh(Atmp * Xc);
+      const double ch2 = ch * ch, ch3 = ch * ch2, ch4 = ch2 * ch2, ch5 = ch * ch4;
+      const double E = A / ch2;
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      const double C2 = S.lef_c2;
+      const double D2 = 2.0 * A * (Atmp * Atmp) * (2.0 * ch2 - 3.) / ch4;
+      const double D1 = -2.0 * A * sh * Atmp / ch3;
+      const double D3 = -8.0 * A * sh * (Atmp * Atmp * Atmp) * (ch2 - 3.) / ch5;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        S.Uin[j + Nl * k] =
+            C2 * E / Dep * (1.0 - 0.25 * E / Dep + Dep / 3.0 * (Dep / E) * (1.0 - 1.5 * (Zlev * Zlev) / (Dep * Dep)) * D2);
+        S.Win[j + Nl * k] = -C2 * Zlev / Dep *
+                            ((1.0 - 0.5 * E / Dep) * D1 +
+                             (double)(1.0f / 3.0f) * (Dep * Dep) * (1.0 - 0.5 * (Zlev * Zlev) / (Dep * Dep)) * D3);
+        S.Vin[j + Nl * k] = 0.0;
+      }
+    }
+  }
+};
+
+// =========================================================================
 //                        2-D slopes of eta (delx/yFun_2D)
 // =========================================================================
 struct OpSlopeEta {
@@ -295,7 +354,18 @@ struct OpFluxX {
     R Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
     R Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
     // flux_bc: walls, then dry cells (src/nhwave.F:2366-2434, 2508-2549)
-    if (f == S.IB) { Ex = (R)0; Fx = hydro<R>(reR, rh0); Gx = (R)0; Hx = (R)0; }
+    if (f == S.IB) {
+      if (S.bc_x0 == 3) {   // inflow (src/nhwave.F:2381-2387)
+        const double dn = S.Din[j], un = S.Uin[j + S.Nloc * k];
+        const double vn = S.Vin[j + S.Nloc * k], wn = S.Win[j + S.Nloc * k], en = S.Ein[j];
+        Ex = (R)(dn * un);
+        Fx = (R)(dn * un * un + 0.5 * kGrav * (en * en + 2.0 * en * h0));
+        Gx = (R)(dn * un * vn);
+        Hx = (R)(dn * un * wn);
+      } else {
+        Ex = (R)0; Fx = hydro<R>(reR, rh0); Gx = (R)0; Hx = (R)0;
+      }
+    }
     if (f == S.IE + 1) { Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0; }
     if (mR == 0) {
       Ex = (R)0; Gx = (R)0; Hx = (R)0;
@@ -476,7 +546,10 @@ struct OpWlBcEta {
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
     const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
-    if (mi != i || mj != j) S.D[c] = S.D[i2(S, mi, mj)];
+    if (i < S.IB && S.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157); corners copy their row's value
+      S.D[c] = 2.0 * S.Din[mj] - S.D[i2(S, mi, mj)];
+    else if (mi != i || mj != j)
+      S.D[c] = S.D[i2(S, mi, mj)];
     S.Eta[c] = S.D[c] - S.Hc[c];
   }
 };
@@ -526,7 +599,20 @@ struct OpVelBcA {
       S.zUR[c] = uR; S.zVR[c] = vR; S.zWR[c] = wR;
       return;
     }
-    if (!ii && jj) {  // west/east ghost columns of interior rows
+    if (!ii && jj && i < S.IB && S.bc_x0 == 3) {  // inflow ghosts (src/nhwave.F:4468-4476)
+      const int src = mirror(i, S.IB, S.IE);
+      const double dn = S.Din[j];
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const long long o = i3(S, i, j, k), q = i3(S, src, j, k);
+        const double un = S.Uin[j + S.Nloc * k], vn = S.Vin[j + S.Nloc * k], wn = S.Win[j + S.Nloc * k];
+        S.U[o] = (T)(2.0 * un - (double)S.U[q]);
+        S.V[o] = (T)(2.0 * vn - (double)S.V[q]);
+        S.W[o] = (T)(2.0 * wn - (double)S.W[q]);
+        S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
+        S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
+        S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
+      }
+    } else if (!ii && jj) {  // west/east ghost columns of interior rows
       const int src = mirror(i, S.IB, S.IE);
       const T s = (T)((i < S.IB ? S.bc_x0 : S.bc_xn) == 1 ? 1 : -1);
       for (int k = S.KB; k <= S.KE; ++k) {
@@ -883,6 +969,7 @@ struct OpOmegaX {
     }
     R Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
     if (f == S.IB || f == S.IE + 1) Ex = (R)0;
+    if (f == S.IB && S.bc_x0 == 3) Ex = (R)(S.Din[j] * S.Uin[j + S.Nloc * k]);   // src/nhwave.F:1564-1566
     S.Ex[i3(S, f, j, k)] = Ex;
   }
 };

@@ -23,10 +23,13 @@ int check_params(const nhw_params& p) {
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
   if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
-  for (int b : {p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn})
+  for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+  const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
+  // west inflow (BC_X0 = 3) only with a wave fed through it
+  if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
-  if (p.wavemaker < 0 || p.wavemaker > 2) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > 4) return NHW_ERR_UNSUPPORTED;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
@@ -248,6 +251,21 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     h.wm_celerity = std::sqrt(kGravH * Dep * (1.0 + A / Dep));
     h.wm_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
     h.wm_xstart = 4.0 * Dep / std::sqrt(A / Dep);
+  } else if (p.wavemaker == NHW_WM_LEF_LIN) {   // src/waves.F:820-829
+    h.lef_segma = 2.0 * kPiH / p.per_wave;
+    h.lef_wn = wave_number(h.lef_segma, p.dep_wave);
+    const double wl = 2.0 * kPiH / h.lef_wn;
+    h.lef_stokes = kGravH * (p.amp_wave * p.amp_wave) / (wl / p.per_wave) / p.dep_wave / 8.0;
+    const double th = p.theta_wave * kPiH / 180.;
+    h.lef_sinth = std::sin(th);
+    h.lef_costh = std::cos(th);
+    h.lef_shd = std::sinh(h.lef_wn * p.dep_wave);
+  } else if (p.wavemaker == NHW_WM_LEF_SOL) {   // src/waves.F:879-886
+    const double A = p.amp_wave, Dep = p.dep_wave;
+    h.lef_cel = std::sqrt(kGravH * Dep * (1.0 + A / Dep));
+    h.lef_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
+    h.lef_xstart = 4.0 * Dep / std::sqrt(A / Dep);
+    h.lef_c2 = std::sqrt(kGravH * Dep);
   }
   return NHW_OK;
 }

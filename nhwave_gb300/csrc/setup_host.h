@@ -19,6 +19,9 @@ struct HostInit {
   int it_order = 1;
   // host-computed wavemaker constants
   double wm_segma = 0, wm_celerity = 0, wm_wnumy = 0, wm_atmp = 0, wm_xstart = 0;
+  // LEF_* boundary waves (src/waves.F:808-903)
+  double lef_segma = 0, lef_wn = 0, lef_shd = 0, lef_stokes = 0, lef_sinth = 0, lef_costh = 0;
+  double lef_cel = 0, lef_atmp = 0, lef_xstart = 0, lef_c2 = 0;
 };
 
 // Validate parameters against the path's scope; NHW_OK or an error code.

@@ -40,6 +40,7 @@ class SolverBase {
   virtual int set_time(double t, double dt, int rs) = 0;
   virtual int estimate_dt() = 0;
   virtual int update_bathymetry() = 0;
+  virtual int update_wave_bc() = 0;
   virtual int update_mask() = 0;
   virtual int update_vars() = 0;
   virtual int source_terms() = 0;
@@ -255,6 +256,10 @@ class Solver final : public SolverBase {
                 &S.Ex, &S.Fx, &S.Gx, &S.Hx, &S.Ey, &S.Fy, &S.Gy, &S.Hy, &S.Fz, &S.Gz, &S.Hz};
     for (auto pp : t3) add(pp, sizeof(T) * n3);
     add(&S.P, sizeof(double) * n3);
+    // west-boundary wave values, recomputed every step (after the checkpointed state)
+    add(&S.Ein, sizeof(double) * S.Nloc);
+    add(&S.Din, sizeof(double) * S.Nloc);
+    for (double** pp : {&S.Uin, &S.Vin, &S.Win}) add(pp, sizeof(double) * S.Nloc * S.Kloc);
     add(&S.coef64, sizeof(double) * NCOMPACT * neq);
     add(&S.rhs64, sizeof(double) * neq);
     add(&S.xsol64, sizeof(double) * neq);
@@ -554,6 +559,7 @@ class Solver final : public SolverBase {
     L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
     L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, 1); });
     if (S.slide) update_bathymetry();
+    update_wave_bc();
     update_mask();
     update_vars();
   }
@@ -587,6 +593,11 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
+    S.lef = (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL) ? p.wavemaker : 0;
+    S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave;
+    S.lef_segma = h.lef_segma; S.lef_wn = h.lef_wn; S.lef_shd = h.lef_shd; S.lef_stokes = h.lef_stokes;
+    S.lef_sinth = h.lef_sinth; S.lef_costh = h.lef_costh;
+    S.lef_cel = h.lef_cel; S.lef_atmp = h.lef_atmp; S.lef_xstart = h.lef_xstart; S.lef_c2 = h.lef_c2;
     S.wm_i0 = S.IB; S.wm_i1 = S.IB - 1;   // empty unless a source column exists
     for (int i = S.IB; i <= S.IE; ++i)
       if (h.xc[i] >= p.xsource_west && h.xc[i] <= p.xsource_east) {
@@ -688,6 +699,11 @@ class Solver final : public SolverBase {
     allcols(OpSlideA{});
     allcols(OpSlideB{});
     box(OpSlideC{}, S.Mloc + 1, S.Nloc + 1, 1, 0, 0, 0);
+    return check();
+  }
+  int update_wave_bc() override {
+    if (!S.lef) return NHW_OK;
+    box(OpWaveBC{}, 1, S.Nloc, 1, 0, 0, 0);
     return check();
   }
   int update_mask() override {
@@ -960,6 +976,7 @@ class Solver final : public SolverBase {
   // everything of one time step after estimate_dt (src/nhwave.F:119-200)
   int step_body() {
     if (S.slide) update_bathymetry();
+    update_wave_bc();
     update_mask();
     int rc = update_vars();
     if (rc) return rc;

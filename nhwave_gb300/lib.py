@@ -27,7 +27,8 @@ OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_DT_MIN, ERR_KRYLOV_NOCONV
 # every entry point declared in include/nhwave_gb300.h
 EXPORTS = [
     "nhw_create", "nhw_destroy", "nhw_setup", "nhw_get_field", "nhw_set_field", "nhw_field_shape",
-    "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_mask",
+    "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc",
+    "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
     "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
     "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
@@ -84,7 +85,7 @@ def load(path: str | None = None):
     L.nhw_field_shape.argtypes = [vp, i32, P(i32 * 3), P(i32)]
     L.nhw_get_scalars.argtypes = [vp, P(NhwScalars)]
     L.nhw_set_time.argtypes = [vp, dbl, dbl, i32]
-    for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_mask", "nhw_update_vars",
+    for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc", "nhw_update_mask", "nhw_update_vars",
               "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_synchronize"):
         getattr(L, n).argtypes = [vp]
     L.nhw_eval_duvw.argtypes = [vp, i32]
@@ -180,6 +181,9 @@ class Scenario:
 
     def update_bathymetry(self):
         return _chk(load().nhw_update_bathymetry(self._h), "update_bathymetry")
+
+    def update_wave_bc(self):
+        return _chk(load().nhw_update_wave_bc(self._h), "update_wave_bc")
 
     def update_mask(self):
         return _chk(load().nhw_update_mask(self._h), "update_mask")

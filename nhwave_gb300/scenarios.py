@@ -142,6 +142,27 @@ def ensemble(n: int, seed: int = 2024, **kw):
     return [ensemble_member(rng, **kw) for _ in range(n)]
 
 
+# --------------------------------------------------------- wave flume
+def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5, amp=0.02, per=1.5,
+               sponge=2.0, **kw):
+    """Flat flume fed through its west boundary (BC_X0 = 3): a linear wave
+    (LEF_LIN, amplitude `amp`, period `per`) or a solitary wave (LEF_SOL,
+    height `amp`); sponge layer and wall at the east end, walls along the
+    sides; at rest initially."""
+    from .params import WM_LEF_LIN, WM_LEF_SOL
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
+                       dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, total_time=20.0)
+    p.bc_x0 = 3
+    p.wavemaker = WM_LEF_LIN if kind == "LIN" else WM_LEF_SOL
+    p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
+    p.sponge_on = 1
+    p.sponge_east_width = sponge
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, np.full(M * N, depth), None, None
+
+
 # ------------------------------------------------------------ registry
 def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
     """Return ``(params, depth, eta0, uvw0)`` for a named scenario."""
@@ -161,6 +182,10 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         out = landslide_beach(M=48, N=40, K=5, dx=2.0 * 1024 / 48 / 2, **kw)
     elif name == "tiny_c4":
         out = ensemble_member(np.random.default_rng(seed), Kchoices=(4, 5), side=(24, 48), **kw)
+    elif name == "tiny_flume_lin":
+        out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
+    elif name == "tiny_flume_sol":
+        out = wave_flume("SOL", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.05, sponge=1.5, **kw)
     else:
         raise KeyError(name)
     p = out[0]

@@ -121,6 +121,9 @@ struct Model {
   A2 D, D0, Eta, Eta0, SourceX, SourceY, SourceC, DxL, DxR, DyL, DyR;
   A2 EtaxL, EtaxR, EtayL, EtayR, DelxEta, DelyEta, Sponge, Wsx, Wsy, R1s;
   I2 Mask, Mask_Struct, Mask9;
+  // west-boundary inflow (Ein_X0, Din_X0, Uin_X0, Vin_X0, Win_X0; src/mod_global.F)
+  A1 Ein_X0, Din_X0;
+  A2 Uin_X0, Vin_X0, Win_X0;
   A3 U, V, W, DU, DV, DW, DU0, DV0, DW0, P, Omega, Uf, Vf, Wf;
   A3 UxL, UxR, VxL, VxR, WxL, WxR, DUxL, DUxR, DVxL, DVxR, DWxL, DWxR;
   A3 UyL, UyR, VyL, VyR, WyL, WyR, DUyL, DUyR, DVyL, DVyR, DWyL, DWyR;
@@ -141,8 +144,10 @@ struct Model {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
     if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
-    for (int b : {p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn})
+    for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+    const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
+    if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
     // index (src/initialize.F:1339-1419), serial build
     Mloc = p.Mglob + 2 * Nghost; Nloc = p.Nglob + 2 * Nghost; Kloc = p.Kglob + 2 * Nghost;
@@ -153,6 +158,8 @@ struct Model {
     dx = p.dx; dy = p.dy; MinDep = p.min_dep;
     fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);  // src/initialize.F:494
     x.init(Mloc1); xc.init(Mloc); y.init(Nloc1); yc.init(Nloc);
+    Ein_X0.init(Nloc); Din_X0.init(Nloc);
+    for (A2* a : {&Uin_X0, &Vin_X0, &Win_X0}) a->init(Nloc, Kloc);
     sig.init(Kloc1); dsig.init(Kloc); sigc.init(Kloc);
     for (A2* a : {&Hc, &Hc0, &Ho, &DeltH, &DeltHo, &Delt2H, &DelxH, &DelyH, &D, &D0, &Eta, &Eta0,
                   &SourceX, &SourceY, &SourceC, &DelxEta, &DelyEta, &Sponge, &Wsx, &Wsy, &R1s})
@@ -503,6 +510,67 @@ struct Model {
       Wn = Wn_new;
     }
     return Wn;
+  }
+
+  // ------------------------------------------------------ update_wave_bc
+  // Linear (LEF_LIN, src/waves.F:808-855) and solitary (LEF_SOL,
+  // src/waves.F:869-903) waves fed through the west boundary
+  // (src/nhwave.F:5514-5565), evaluated at the new TIME once per step.
+  void update_wave_bc() {
+    if (p.wavemaker == NHW_WM_LEF_LIN) {
+      const double Segma = 2.0 * pi / p.per_wave;
+      const double Wave_Number = wave_dispersion(Segma);
+      const double Wave_Length = 2.0 * pi / Wave_Number;
+      const double Stokes_Drift = Grav * (p.amp_wave * p.amp_wave) / (Wave_Length / p.per_wave) / p.dep_wave / 8.0;
+      const double Fact = 1.0;
+      const double th = p.theta_wave * pi / 180.;
+      for (int j = 1; j <= Nloc; ++j) {
+        const double Phs_Lag = yc(j) * std::sin(th) * Wave_Number;
+        Ein_X0(j) = 0.5 * p.amp_wave * std::cos(pi / 2 - Segma * TIME + Phs_Lag);
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+      }
+      const double shd = std::sinh(Wave_Number * p.dep_wave);
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j) {
+          const double Phs_Lag = yc(j) * std::sin(th) * Wave_Number;
+          const double Zlev = sigc(k) * Din_X0(j);
+          const double cs = std::cos(pi / 2 - Segma * TIME + Phs_Lag);
+          const double sn = std::sin(pi / 2 - Segma * TIME + Phs_Lag);
+          Uin_X0(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+                         std::cos(th);
+          Win_X0(j, k) = 0.5 * p.amp_wave * Segma * std::sinh(Wave_Number * Zlev) / shd * sn;
+          Vin_X0(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+                         std::sin(th);
+        }
+    } else if (p.wavemaker == NHW_WM_LEF_SOL) {
+      Uin_X0.fill(0.0); Vin_X0.fill(0.0); Win_X0.fill(0.0);
+      const double A = p.amp_wave, Dep = p.dep_wave;
+      const double Celerity = std::sqrt(Grav * Dep * (1.0 + A / Dep));
+      for (int j = 1; j <= Nloc; ++j) {
+        const double Atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
+        const double Xstart = 4.0 * Dep / std::sqrt(A / Dep);
+        const double Xc = Xstart - Celerity * TIME;
+        const double ch = std::cosh(Atmp * Xc), sh = std::sinh(Atmp * Xc);
+        const double ch2 = ch * ch, ch3 = ch * ch2, ch4 = ch2 * ch2, ch5 = ch * ch4;
+        Ein_X0(j) = A / ch2;
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+        const double C2 = std::sqrt(Grav * Dep);
+        const double D2 = 2.0 * A * (Atmp * Atmp) * (2.0 * ch2 - 3.) / ch4;
+        const double D1 = -2.0 * A * sh * Atmp / ch3;
+        const double D3 = -8.0 * A * sh * (Atmp * Atmp * Atmp) * (ch2 - 3.) / ch5;
+        if (j < Jbeg || j > Jend) continue;
+        for (int k = Kbeg; k <= Kend; ++k) {
+          const double Zlev = sigc(k) * Din_X0(j);
+          const double E = Ein_X0(j);
+          Uin_X0(j, k) = C2 * E / Dep *
+                         (1.0 - 0.25 * E / Dep + Dep / 3.0 * (Dep / E) * (1.0 - 1.5 * (Zlev * Zlev) / (Dep * Dep)) * D2);
+          Win_X0(j, k) = -C2 * Zlev / Dep *
+                         ((1.0 - 0.5 * E / Dep) * D1 +
+                          (double)(1.0f / 3.0f) * (Dep * Dep) * (1.0 - 0.5 * (Zlev * Zlev) / (Dep * Dep)) * D3);
+          Vin_X0(j, k) = 0.0;
+        }
+      }
+    }
   }
 
   double source_area() {
@@ -876,9 +944,16 @@ struct Model {
 
   void flux_bc() {
     for (int j = Jbeg; j <= Jend; ++j)
-      for (int k = Kbeg; k <= Kend; ++k) {  // walls: Bc 1, 2 (5)
-        Ex(Ibeg, j, k) = Zero; Fx(Ibeg, j, k) = hydro(EtaxR(Ibeg, j), Hfx0(Ibeg, j));
-        Gx(Ibeg, j, k) = Zero; Hx(Ibeg, j, k) = Zero;
+      for (int k = Kbeg; k <= Kend; ++k) {  // walls: Bc 1, 2 (5); inflow: Bc 3 (src/nhwave.F:2375-2387)
+        if (p.bc_x0 == 3) {
+          Ex(Ibeg, j, k) = Din_X0(j) * Uin_X0(j, k);
+          Fx(Ibeg, j, k) = Din_X0(j) * Uin_X0(j, k) * Uin_X0(j, k) + hydro(Ein_X0(j), Hfx0(Ibeg, j));
+          Gx(Ibeg, j, k) = Din_X0(j) * Uin_X0(j, k) * Vin_X0(j, k);
+          Hx(Ibeg, j, k) = Din_X0(j) * Uin_X0(j, k) * Win_X0(j, k);
+        } else {
+          Ex(Ibeg, j, k) = Zero; Fx(Ibeg, j, k) = hydro(EtaxR(Ibeg, j), Hfx0(Ibeg, j));
+          Gx(Ibeg, j, k) = Zero; Hx(Ibeg, j, k) = Zero;
+        }
         Ex(Iend1, j, k) = Zero; Fx(Iend1, j, k) = hydro(EtaxL(Iend1, j), Hfx0(Iend1, j));
         Gx(Iend1, j, k) = Zero; Hx(Iend1, j, k) = Zero;
       }
@@ -924,7 +999,10 @@ struct Model {
   // -------------------------------------------------------------- wl_bc
   void wl_bc() {
     for (int j = Jbeg; j <= Jend; ++j) {
-      for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);
+      if (p.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157)
+        for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = 2.0 * Din_X0(j) - D(Ibeg + i - 1, j);
+      else
+        for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);
       for (int i = 1; i <= Nghost; ++i) D(Iend + i, j) = D(Iend - i + 1, j);
     }
     for (int i = 1; i <= Mloc; ++i)
@@ -949,6 +1027,15 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = 1; i <= Nghost; ++i) {
+          if (p.bc_x0 == 3) {   // inflow (src/nhwave.F:4468-4476)
+            U(Ibeg - i, j, k) = 2.0 * Uin_X0(j, k) - U(Ibeg + i - 1, j, k);
+            V(Ibeg - i, j, k) = 2.0 * Vin_X0(j, k) - V(Ibeg + i - 1, j, k);
+            W(Ibeg - i, j, k) = 2.0 * Win_X0(j, k) - W(Ibeg + i - 1, j, k);
+            DU(Ibeg - i, j, k) = 2.0 * Din_X0(j) * Uin_X0(j, k) - DU(Ibeg + i - 1, j, k);
+            DV(Ibeg - i, j, k) = 2.0 * Din_X0(j) * Vin_X0(j, k) - DV(Ibeg + i - 1, j, k);
+            DW(Ibeg - i, j, k) = 2.0 * Din_X0(j) * Win_X0(j, k) - DW(Ibeg + i - 1, j, k);
+            continue;
+          }
           U(Ibeg - i, j, k) = -U(Ibeg + i - 1, j, k);
           V(Ibeg - i, j, k) = sx0 * V(Ibeg + i - 1, j, k);
           W(Ibeg - i, j, k) = sx0 * W(Ibeg + i - 1, j, k);
@@ -1373,7 +1460,10 @@ struct Model {
     HLL(SxL, SxR, ExL, ExR, nullptr, nullptr, &DxL, &DxR, Ex);
     HLL(SyL, SyR, EyL, EyR, nullptr, nullptr, &DyL, &DyR, Ey);
     for (int j = Jbeg; j <= Jend; ++j)
-      for (int k = Kbeg; k <= Kend; ++k) { Ex(Ibeg, j, k) = Zero; Ex(Iend1, j, k) = Zero; }
+      for (int k = Kbeg; k <= Kend; ++k) {   // src/nhwave.F:1558-1580
+        Ex(Ibeg, j, k) = p.bc_x0 == 3 ? Din_X0(j) * Uin_X0(j, k) : Zero;
+        Ex(Iend1, j, k) = Zero;
+      }
     for (int i = Ibeg; i <= Iend; ++i)
       for (int k = Kbeg; k <= Kend; ++k) { Ey(i, Jbeg, k) = Zero; Ey(i, Jend1, k) = Zero; }
     Omega.fill(0.0);
@@ -1495,6 +1585,7 @@ struct Model {
     int st = estimate_dt();
     if (st) return status = st;
     if (p.slide_type != NHW_SLIDE_NONE) update_bathymetry();
+    update_wave_bc();
     update_mask();
     update_wind();
     update_vars();
@@ -1577,6 +1668,7 @@ int orc_setup(void* o, const double* depth, const double* eta0, const double* uv
 int orc_estimate_dt(void* o) { return static_cast<Model*>(o)->estimate_dt(); }
 void orc_update_bathymetry(void* o) { static_cast<Model*>(o)->update_bathymetry(); }
 void orc_update_mask(void* o) { static_cast<Model*>(o)->update_mask(); }
+void orc_update_wave_bc(void* o) { static_cast<Model*>(o)->update_wave_bc(); }
 void orc_update_vars(void* o) { Model* m = static_cast<Model*>(o); m->update_wind(); m->update_vars(); }
 void orc_source_terms(void* o) { static_cast<Model*>(o)->source_terms(); }
 void orc_fluxes(void* o) { static_cast<Model*>(o)->fluxes(); }

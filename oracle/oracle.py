@@ -54,7 +54,7 @@ def lib():
         for name in ("orc_estimate_dt", "orc_step"):
             getattr(L, name).argtypes = [vp]
         L.orc_eval_duvw.argtypes = [vp, i32]
-        for name in ("orc_update_bathymetry", "orc_update_mask", "orc_update_vars",
+        for name in ("orc_update_bathymetry", "orc_update_wave_bc", "orc_update_mask", "orc_update_vars",
                      "orc_source_terms", "orc_fluxes", "orc_sponge_damping",
                      "orc_generate_coef_rhs"):
             getattr(L, name).argtypes = [vp]
@@ -115,6 +115,9 @@ class Oracle:
 
     def update_bathymetry(self):
         lib().orc_update_bathymetry(self._h)
+
+    def update_wave_bc(self):
+        lib().orc_update_wave_bc(self._h)
 
     def update_mask(self):
         lib().orc_update_mask(self._h)

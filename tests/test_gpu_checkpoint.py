@@ -23,7 +23,7 @@ def _scen(name, precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("name", ["tiny_c2", "tiny_c3", "tiny_c4"])
+@pytest.mark.parametrize("name", ["tiny_c2", "tiny_c3", "tiny_c4", "tiny_flume_lin"])
 def test_resume_continues_bit_for_bit(name, precision, gpu_lib):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision)

@@ -28,6 +28,7 @@ def _routines(s):
     s.estimate_dt()
     if s.params.slide_type:
         s.update_bathymetry()
+    s.update_wave_bc()
     s.update_mask()
     s.update_vars()
     for st in range(1, int(s.params.time_order) + 1):
@@ -39,7 +40,7 @@ def _routines(s):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"])
+@pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4", "tiny_flume_lin", "tiny_flume_sol"])
 def test_graph_step_equals_routines(name, precision, gpu_lib):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision)

@@ -215,3 +215,40 @@ def test_golden_fixtures(name, gpu_lib):
         assert r < lim, f"{name} {f}: rel L2 {r:.3e}"
     assert np.array_equal(g.get(F.MASK)[g.shape.interior(F.MASK)], ref["MASK"])
     g.close()
+
+
+FLUMES = ["tiny_flume_lin", "tiny_flume_sol"]
+
+
+@pytest.mark.parametrize("name", FLUMES)
+def test_flume_steps_fp64(name, oracle_mod, gpu_lib):
+    """Waves fed through the west boundary (BC_X0 = 3, LEF_LIN / LEF_SOL):
+    FP64 steps against the oracle.  The boundary values use cos/cosh/sinh,
+    whose CUDA and host results may differ in the last bit, hence 1e-9."""
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod)
+    for n in range(20):
+        assert g.step() == 0 and o.step() == 0
+        assert np.array_equal(g.get(F.MASK), o.get(F.MASK)), f"mask differs after step {n}"
+    sl = o.shape.interior
+    for f in ("ETA", "P"):
+        fid = getattr(F, f)
+        r = rel_l2(g.get(fid)[sl(fid)], o.get(fid)[sl(fid)])
+        assert r < 1e-9, f"{name} {f}: rel L2 {r:.3e}"
+    for f in ("U", "W"):
+        r = vel_err(g, o, f)
+        assert r < 1e-9, f"{name} {f}: {r:.3e}"
+    g.close()
+
+
+@pytest.mark.parametrize("name", FLUMES)
+def test_flume_steps_fp32_ir(name, oracle_mod, gpu_lib):
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod, precision=1, tol=1e-10)
+    for _ in range(20):
+        assert g.step() == 0 and o.step() == 0
+    sl = o.shape.interior
+    assert np.array_equal(g.get(F.MASK), o.get(F.MASK))
+    r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
+    assert r < 1e-6, f"{name} eta rel L2 {r:.3e}"
+    g.close()

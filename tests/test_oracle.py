@@ -135,3 +135,42 @@ def test_wet_dry_front_exists_in_slide_case(oracle_mod):
     ref = np.load(golden_path("tiny_c3", GOLDEN["tiny_c3"]))
     mask = ref["MASK"]
     assert 0 < (mask == 0).sum() < mask.size
+
+
+def test_flume_linear_inflow_follows_the_boundary_wave(oracle_mod):
+    """LEF_LIN through BC_X0 = 3 (src/waves.F:808-855): eta in the first
+    interior column follows the imposed boundary elevation 0.5*A*sin(sigma t)."""
+    import math
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_flume_lin")
+    p.tol, p.itmax = 1e-10, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    ts, e0 = [], []
+    for _ in range(150):
+        assert o.step() == 0
+        ts.append(o.scalars().time)
+        e0.append(o.get(F.ETA)[o.shape.interior(F.ETA)][:, 0].mean())
+    ts, e0 = np.array(ts), np.array(e0)
+    ref = 0.5 * p.amp_wave * np.sin(2 * math.pi / p.per_wave * ts)
+    assert np.corrcoef(e0, ref)[0, 1] > 0.97
+    assert 0.85 < e0.std() / ref.std() < 1.1
+
+
+def test_flume_solitary_inflow_arrives_with_its_height(oracle_mod):
+    """LEF_SOL (src/waves.F:869-903): the boundary elevation peaks at about
+    the wave height when the crest, started 4h/sqrt(A/h) upstream, arrives."""
+    import math
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_flume_sol")
+    p.tol, p.itmax = 1e-10, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    A, h = p.amp_wave, p.dep_wave
+    arrival = 4 * h / math.sqrt(A / h) / math.sqrt(9.81 * h * (1 + A / h))
+    peak, t_peak = 0.0, 0.0
+    while o.scalars().time < arrival + 0.5:
+        assert o.step() == 0
+        v = o.get(F.ETA)[o.shape.interior(F.ETA)][:, 0].mean()
+        if v > peak:
+            peak, t_peak = v, o.scalars().time
+    assert abs(peak - A) < 0.15 * A
+    assert abs(t_peak - arrival) < 0.15
