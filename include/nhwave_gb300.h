@@ -123,7 +123,10 @@ typedef struct nhw_params {
   int32_t mg_cta_columns;                  /* levels with at most this many columns run in
                                               one thread block (0: 64)                */
   int32_t mg_aggregate;                    /* multigrid aggregates of n x n columns (0: 2) */
-  int32_t reserved[1];
+  int32_t test_barrier_extra;              /* test hook, 0 in use: the persistent solve's
+                                              grid barrier also waits for this many blocks
+                                              that do not exist, so its bounded wait runs
+                                              out and the solve reports NHW_ERR_TIMEOUT */
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

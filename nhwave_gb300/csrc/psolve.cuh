@@ -36,7 +36,7 @@ constexpr int kPsBY = 16;                          // block = 32 x kPsBY threads
 constexpr int kPsBYEnsemble = 8;                   // 32 x 8 when many scenarios share a launch
 constexpr int kPsMaxLevels = 16;
 constexpr int kPsMaxBlocks = 1024;                 // blocks of one group at most
-constexpr long long kPsSpinLimit = 1ll << 22;      // polls of ~64 ns: well under a second
+constexpr long long kPsSpinLimit = 1ll << 20;      // about a second of polling (L2 round trip + 64 ns sleep)
 
 template <class T>
 struct PsGroup {
@@ -47,6 +47,7 @@ struct PsGroup {
   T w;                      // coarse-correction weight
   int coarse_sweeps;
   int b0, nb;               // the group's blocks: [b0, b0 + nb)
+  int bar_nb;               // arrivals a barrier waits for (nb; more only in the timeout test)
   double* part;             // [2][nb][4] partial sums
 };
 
@@ -100,7 +101,7 @@ __device__ __forceinline__ void ps_reduce(const PsGroup<T>& G, int lb, int& rid,
     for (int w = 0; w < nw; ++w) x += s_w[tid][w];
     part[(size_t)lb * 4 + tid] = x;
   }
-  ps_sync(G.S.sc, G.nb);
+  ps_sync(G.S.sc, G.bar_nb);
   if (warp == 0) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
@@ -347,36 +348,36 @@ __device__ void ps_vcycle(const PsGroup<T>& G, const MGL<T>* Ls, In in0, T* sh, 
   DevScal* sc = G.S.sc;
   if (G.nl == 0) {   // the whole hierarchy fits one block: form b first
     for (int ic = lb * nt + tid; ic < Ls[0].n; ic += G.nb * nt) (void)in0(ic);
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
     if (lb == 0) ps_cta_cycle(Ls, 0, G.ntot, G.w, G.coarse_sweeps, sh);
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
     return;
   }
   for (int l = 0; l < G.nl; ++l) {
     const MGL<T>& Lv = Ls[l];
     if (l == 0) {
       ps_sweep(Lv, 0, true, in0, none, sh, lb, G.nb);
-      ps_sync(sc, G.nb);
+      ps_sync(sc, G.bar_nb);
       ps_sweep(Lv, 1, false, in0, none, sh, lb, G.nb);
     } else {
       ps_sweep(Lv, 0, true, PsPlainB<T>{Lv.b}, none, sh, lb, G.nb);
-      ps_sync(sc, G.nb);
+      ps_sync(sc, G.bar_nb);
       ps_sweep(Lv, 1, false, PsPlainB<T>{Lv.b}, none, sh, lb, G.nb);
     }
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
     ps_restrict(Lv, Ls[l + 1], lb * nt + tid, G.nb * nt);
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
   }
   if (lb == 0) ps_cta_cycle(Ls, G.nl, G.ntot, G.w, G.coarse_sweeps, sh);
-  ps_sync(sc, G.nb);
+  ps_sync(sc, G.bar_nb);
   for (int l = G.nl - 1; l >= 0; --l) {
     const MGL<T>& F = Ls[l];
     const MGL<T>& C = Ls[l + 1];
     const Prolong<T> pr{C.x, G.w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N};
     ps_sweep(F, 1, false, PsPlainB<T>{F.b}, pr, sh, lb, G.nb);
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
     ps_sweep(F, 0, false, PsPlainB<T>{F.b}, none, sh, lb, G.nb);
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
   }
 }
 
@@ -550,7 +551,7 @@ __global__ void __launch_bounds__(32 * BY, BY >= 16 ? 1 : 2) k_psolve(const PsGr
     }
     // x64 += c
     for (int ic = c0; ic < n; ic += cstep) S.xsol64[ic] = S.xsol64[ic] + (double)S.kx[ic];
-    ps_sync(sc, G.nb);
+    ps_sync(sc, G.bar_nb);
   }
   if (reporter) {
     if (sc->bar_err) pstat = kStTimeout;

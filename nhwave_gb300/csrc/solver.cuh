@@ -510,6 +510,7 @@ class Solver final : public SolverBase {
     g.coarse_sweeps = coarse_sweeps;
     g.b0 = b0;
     g.nb = nb;
+    g.bar_nb = nb + (p.test_barrier_extra > 0 ? p.test_barrier_extra : 0);
     g.part = ps_part;
     return g;
   }

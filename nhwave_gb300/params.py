@@ -59,7 +59,7 @@ class NhwParams(ctypes.Structure):
         ("mg_coarse_sweeps", ctypes.c_int32),
         ("mg_cta_columns", ctypes.c_int32),
         ("mg_aggregate", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 1),
+        ("test_barrier_extra", ctypes.c_int32),
     ]
 
     def copy(self) -> "NhwParams":
