@@ -125,65 +125,9 @@ __device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__
   return s;
 }
 
-// red-black line Gauss-Seidel half-sweep: columns with (ii+jj)%2 == color
-template <class T>
-__global__ void __launch_bounds__(128) k_mg_smooth(MGL<T> L, const DevScal* sc, int color, int zero_x) {
-  if (sc->conv) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  // thread t handles the t-th column of its colour: rows alternate the colour's parity
-  const int half = (L.M + 1 - color) / 2;          // columns of this colour in a row with jj even
-  const int ncol_row0 = half;
-  const int ncol_row1 = (L.M + color) / 2;          // rows with jj odd
-  const int pair = ncol_row0 + ncol_row1;
-  const int jp2 = t / pair, rem = t % pair;
-  int jj, ii;
-  if (rem < ncol_row0) { jj = 2 * jp2; ii = 2 * rem + color; }
-  else { jj = 2 * jp2 + 1; ii = 2 * (rem - ncol_row0) + (1 - color); }
-  if (jj >= L.N || ii >= L.M) return;
-  const int M = L.M, MN = L.M * L.N, K = L.K, n = L.n;
-  const int col = ii + M * jj;
-  const T* __restrict__ a = L.coef + 2 * n;
-  T* __restrict__ x = L.x;
-  if (K <= KREG) {
-    T dp[KREG];
-    T prev = (T)0;
-#pragma unroll
-    for (int k = 0; k < KREG; ++k) {
-      if (k < K) {
-        const int ic = col + MN * k;
-        const T rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, x, ic, ii, jj, k));
-        const T am = k > 0 ? a[ic] : (T)0;
-        prev = (rhs - am * prev) * L.linv[ic];
-        dp[k] = prev;
-      }
-    }
-    T z = (T)0;
-#pragma unroll
-    for (int k = KREG - 1; k >= 0; --k) {
-      if (k < K) {
-        const int ic = col + MN * k;
-        z = (k == K - 1) ? dp[k] : dp[k] - L.lcp[ic] * z;
-        x[ic] = z;
-      }
-    }
-  } else {
-    T prev = (T)0;
-    for (int k = 0; k < K; ++k) {
-      const int ic = col + MN * k;
-      const T rhs = L.b[ic] - (zero_x ? (T)0 : off_column(L, x, ic, ii, jj, k));
-      const T am = k > 0 ? a[ic] : (T)0;
-      prev = (rhs - am * prev) * L.linv[ic];
-      x[ic] = prev;
-    }
-    T z = x[col + MN * (K - 1)];
-    for (int k = K - 2; k >= 0; --k) {
-      const int ic = col + MN * k;
-      z = x[ic] - L.lcp[ic] * z;
-      x[ic] = z;
-    }
-  }
-}
-
+// Red-black line Gauss-Seidel: a half-sweep solves the columns with
+// (ii + jj) % 2 == color.
+//
 // Right-hand sides of a half-sweep:
 //   MgB            b as stored;
 //   MgInP / MgInS  the BiCGSTAB vectors p = r + beta (p - omega v) and
@@ -401,18 +345,6 @@ __global__ void __launch_bounds__(256) k_mg_restrict(MGL<T> F, MGL<T> C, const D
   }
   C.b[ic] = acc;
   C.x[ic] = (T)0;
-}
-
-// x_f += w * x_c(aggregate)
-template <class T>
-__global__ void __launch_bounds__(256) k_mg_prolong(MGL<T> F, MGL<T> C, const DevScal* sc, T w) {
-  if (sc->conv) return;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= F.n) return;
-  int i, j, k;
-  decode(f, F.M, F.N, i, j, k);
-  const int c = i / F.rx + C.M * (j / F.ry + C.N * k);
-  F.x[f] += w * C.x[c];
 }
 
 // Galerkin coarse operator P^T A P (piecewise-constant P), compact form + couplings
