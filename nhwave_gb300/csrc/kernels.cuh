@@ -751,16 +751,16 @@ struct OpPoissonCoef {
     const double lx = S.lv_x[k], ly = S.lv_y[k], ih = S.lv_h[k];
     // Rhs (src/pressure.F:521-525); Uf/Vf: linear interpolation to sig(k) (src/nhwave.F:1346-1355)
     const double dsk = S.dsig[k], dskm = S.dsig[k - 1];
-    const double fint = dsk / (dsk + dskm);
+    const double fint = S.lv_fint[k];   // dsk / (dsk + dskm)
     const long long o = i3(S, i, j, k);
     auto uf = [&](const T* A, long long e) -> double {
       return (1.0 - fint) * (double)A[e] + fint * (double)A[e - sz];
     };
-    const double i2dx = 0.5 / S.dx, i2dy = 0.5 / S.dy;
+    const double i2dx = S.i2dx, i2dy = S.i2dy;
     double rhs = -((uf(S.U, o + 1) - uf(S.U, o - 1)) * i2dx + ((double)S.U[o] - (double)S.U[o - sz]) * ih * DelxS +
                    (uf(S.V, o + sy) - uf(S.V, o - sy)) * i2dy + ((double)S.V[o] - (double)S.V[o - sz]) * ih * DelyS +
                    ((double)S.W[o] - (double)S.W[o - sz]) * ih * DelzS - S.SourceC[q]) *
-                 (kRho0 / S.sc->dt);
+                 S.sc->rho_dt;
     double C[NCOEF + 1];
     const double cxx = S.cxx, cyy = S.cyy;
     C[1] = -2. * cxx - 2. * cyy + A1 * S.lv_up[k] + A1 * S.lv_dn[k];
@@ -875,14 +875,14 @@ struct OpProjection {
     if (S.Mask[q] == 0) return;
     const long long o = i3(S, i, j, k), sy = S.sy, sz = S.sz;
     const double* P = S.P;
-    const double i2dx = 0.5 / S.dx, i2dy = 0.5 / S.dy;
+    const double i2dx = S.i2dx, i2dy = S.i2dy;
     const double DelxP = 0.5 * ((P[o + 1] - P[o - 1]) * i2dx + (P[o + 1 + sz] - P[o - 1 + sz]) * i2dx);
     const double DelyP = 0.5 * ((P[o + sy] - P[o - sy]) * i2dy + (P[o + sy + sz] - P[o - sy + sz]) * i2dy);
     const double DelzP = (P[o + sz] - P[o]) * S.lv_ds[k];
     const double sc = S.sigc[k], omc = 1.0 - sc;
     const double DelxSc = omc * S.cf_hx[q] - sc * S.cf_ex[q];
     const double DelySc = omc * S.cf_hy[q] - sc * S.cf_ey[q];
-    const double f = S.D[q] * (S.sc->dt / kRho0), g = S.sc->dt / kRho0;
+    const double g = S.sc->dt_rho, f = S.D[q] * g;   // dt / Rho0
     S.DU[o] = (T)((double)S.DU[o] - f * (DelxP + DelzP * DelxSc));
     S.DV[o] = (T)((double)S.DV[o] - f * (DelyP + DelzP * DelySc));
     S.DW[o] = (T)((double)S.DW[o] - g * DelzP);
@@ -1116,6 +1116,8 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
     const double dt_courant = S.cfl * tmp2;
     const double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), kLarge), S.dt_max);
     sc->dt = dt;
+    sc->rho_dt = kRho0 / dt;
+    sc->dt_rho = dt / kRho0;
     if (dt < S.dt_min) {
       sc->status = 5;
       if (5 > sc->worst) sc->worst = 5;

@@ -203,6 +203,7 @@ class Solver final : public SolverBase {
     S.neq = M * N * K;
     S.dx = p.dx; S.dy = p.dy; S.min_dep = p.min_dep; S.cfl = p.cfl;
     S.cxx = -1. / (p.dx * p.dx); S.cyy = -1. / (p.dy * p.dy);
+    S.i2dx = 0.5 / p.dx; S.i2dy = 0.5 / p.dy;
     S.dt_min = p.dt_min; S.dt_max = p.dt_max;
     S.fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);
     S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
@@ -242,7 +243,7 @@ class Solver final : public SolverBase {
     add(&S.sigc, sizeof(double) * S.Kloc);
     add(&S.xc, sizeof(double) * S.Mloc);
     add(&S.yc, sizeof(double) * S.Nloc);
-    for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds})
+    for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds, &S.lv_fint})
       add((double**)lv, sizeof(double) * S.Kloc);
     double** d2[] = {&S.D, &S.D0, &S.Eta, &S.Eta0, &S.Hc, &S.Hc0, &S.Ho, &S.Hfx, &S.Hfy, &S.Hfx0, &S.Hfy0,
                      &S.DelxH, &S.DelyH, &S.DeltH, &S.DeltHo, &S.Delt2H, &S.DelxEta, &S.DelyEta, &S.SourceX,
@@ -362,6 +363,7 @@ class Solver final : public SolverBase {
     NHW_CU(cudaMallocHost((void**)&h_out, sizeof(double) * 8));
     std::memset(h_sc, 0, sizeof(DevScal));
     h_sc->dt = p.dt_ini;
+    h_sc->rho_dt = kRho0 / p.dt_ini; h_sc->dt_rho = p.dt_ini / kRho0;
     h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
     NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
     NHW_CU(cudaStreamSynchronize(st));
@@ -612,7 +614,7 @@ class Solver final : public SolverBase {
     NHW_CU(cudaMemcpyAsync((void*)S.yc, h.yc.data(), sizeof(double) * h.yc.size(), cudaMemcpyHostToDevice, st));
     {  // per-level reciprocals of the Poisson assembly and the projection
       std::vector<double> lx(S.Kloc, 0.0), ly(S.Kloc, 0.0), lu(S.Kloc, 0.0), ld(S.Kloc, 0.0), lh(S.Kloc, 0.0),
-          lds(S.Kloc, 0.0);
+          lds(S.Kloc, 0.0), lf(S.Kloc, 0.0);
       for (int k = 1; k < S.Kloc; ++k) {
         const double dk = h.dsig[k], dm = h.dsig[k - 1], s = dk + dm, hk = 0.5 * (dk + dm);
         lx[k] = 1.0 / (2. * p.dx * s);
@@ -621,10 +623,11 @@ class Solver final : public SolverBase {
         ld[k] = 1.0 / (hk * dm);
         lh[k] = 1.0 / hk;
         lds[k] = 1.0 / dk;
+        lf[k] = dk / (dk + dm);
       }
-      const std::vector<double>* src[] = {&lx, &ly, &lu, &ld, &lh, &lds};
-      const double* dst[] = {S.lv_x, S.lv_y, S.lv_up, S.lv_dn, S.lv_h, S.lv_ds};
-      for (int q = 0; q < 6; ++q)
+      const std::vector<double>* src[] = {&lx, &ly, &lu, &ld, &lh, &lds, &lf};
+      const double* dst[] = {S.lv_x, S.lv_y, S.lv_up, S.lv_dn, S.lv_h, S.lv_ds, S.lv_fint};
+      for (int q = 0; q < 7; ++q)
         NHW_CU(cudaMemcpyAsync((void*)dst[q], src[q]->data(), sizeof(double) * S.Kloc, cudaMemcpyHostToDevice, st));
       NHW_CU(cudaStreamSynchronize(st));
     }
@@ -650,6 +653,7 @@ class Solver final : public SolverBase {
     }
     std::memset(h_sc, 0, sizeof(DevScal));
     h_sc->time = 0.0; h_sc->dt = p.dt_ini; h_sc->run_step = 0;
+    h_sc->rho_dt = kRho0 / p.dt_ini; h_sc->dt_rho = p.dt_ini / kRho0;
     h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
     NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
     // initial: vel_bc on the initial velocities, then DU = D*U*Mask
@@ -682,6 +686,7 @@ class Solver final : public SolverBase {
     int rc = pull_scalars();
     if (rc) return rc;
     h_sc->time = t; h_sc->dt = dt; h_sc->run_step = rs;
+    h_sc->rho_dt = kRho0 / dt; h_sc->dt_rho = dt / kRho0;
     NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
     return sync();
   }

@@ -44,6 +44,7 @@ struct DevScal {
   double bnorm, relres, relres64;
   int32_t it, conv, ir, itmax_in;
   double tol_in;
+  double rho_dt, dt_rho;            // Rho0/dt and dt/Rho0 of the current dt (set where dt is set)
   unsigned int counter[4];          // last-block-done counters
   int64_t total_it, solves;
   // Poisson refinement state, decided on the device (so that a captured step
@@ -112,6 +113,8 @@ struct Dev {
   // per sigma level k: 1/(2dx(dsig_k+dsig_k-1)), 1/(2dy(..)), 1/(h_k dsig_k), 1/(h_k dsig_k-1),
   // 1/h_k with h_k = (dsig_k+dsig_k-1)/2, 1/dsig_k
   const double *lv_x, *lv_y, *lv_up, *lv_dn, *lv_h, *lv_ds;
+  const double* lv_fint;   // dsig_k / (dsig_k + dsig_k-1): weight of level k-1 at face k
+  double i2dx, i2dy;       // 0.5/dx, 0.5/dy
   int *Mask, *MaskT, *Mask_Struct, *Mask9;
   // 3-D fields (storage type T); P is FP64 in both forms
   T *U, *V, *W, *DU, *DV, *DW, *DU0, *DV0, *DW0, *Omega;
