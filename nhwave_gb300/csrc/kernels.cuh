@@ -11,6 +11,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
+#include <type_traits>
 #include "state.h"
 
 namespace nhw {
@@ -575,20 +576,23 @@ struct OpVelBcA {
   static constexpr const char* kName = "vel_bc_a";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
-    const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
+    // interior columns: surface and bed face states (the lateral ghost cells
+    // are filled per cell by OpVelBcLat)
     const long long c = i2(S, i, j);
-    if (ii && jj) {
+    {
       const long long sz = S.sz;
+      // arithmetic of the face states: FP64 in the FP64 form, FP32 in FP32+IR
+      using R = typename std::conditional<sizeof(T) == 4, float, double>::type;
       auto zface = [&](const T* A, double& top, double& bot) {
         // top: UzL(Kend1) = U(Kend) + 0.5 dsig(Kend) DelzU(Kend)
         const int kt = S.KE, kb = S.KB;
         const long long ot = i3(S, i, j, kt), ob = i3(S, i, j, kb);
-        double s_t = lim_slope<double>((double)A[ot - sz], (double)A[ot], (double)A[ot + sz],
-                                       S.sigc[kt] - S.sigc[kt - 1], S.sigc[kt + 1] - S.sigc[kt]);
-        double s_b = lim_slope<double>((double)A[ob - sz], (double)A[ob], (double)A[ob + sz],
-                                       S.sigc[kb] - S.sigc[kb - 1], S.sigc[kb + 1] - S.sigc[kb]);
-        top = (double)A[ot] + 0.5 * S.dsig[kt] * s_t;
-        bot = (double)A[ob] - 0.5 * S.dsig[kb] * s_b;
+        R s_t = lim_slope<R>((R)A[ot - sz], (R)A[ot], (R)A[ot + sz], (R)(S.sigc[kt] - S.sigc[kt - 1]),
+                             (R)(S.sigc[kt + 1] - S.sigc[kt]));
+        R s_b = lim_slope<R>((R)A[ob - sz], (R)A[ob], (R)A[ob + sz], (R)(S.sigc[kb] - S.sigc[kb - 1]),
+                             (R)(S.sigc[kb + 1] - S.sigc[kb]));
+        top = (double)((R)A[ot] + (R)0.5 * (R)S.dsig[kt] * s_t);
+        bot = (double)((R)A[ob] - (R)0.5 * (R)S.dsig[kb] * s_b);
       };
       double uL, uR, vL, vR, wL, wR;
       zface(S.U, uL, uR); zface(S.V, vL, vR); zface(S.W, wL, wR);
@@ -597,43 +601,44 @@ struct OpVelBcA {
       wR = -S.DeltH[c] - S.DelxH[c] * uR - S.DelyH[c] * vR;
       S.zUL[c] = uL; S.zVL[c] = vL; S.zWL[c] = wL;
       S.zUR[c] = uR; S.zVR[c] = vR; S.zWR[c] = wR;
-      return;
-    }
-    if (!ii && jj && i < S.IB && S.bc_x0 == 3) {  // inflow ghosts (src/nhwave.F:4468-4476)
-      const int src = mirror(i, S.IB, S.IE);
-      const double dn = S.Din[j];
-      for (int k = S.KB; k <= S.KE; ++k) {
-        const long long o = i3(S, i, j, k), q = i3(S, src, j, k);
-        const double un = S.Uin[j + S.Nloc * k], vn = S.Vin[j + S.Nloc * k], wn = S.Win[j + S.Nloc * k];
-        S.U[o] = (T)(2.0 * un - (double)S.U[q]);
-        S.V[o] = (T)(2.0 * vn - (double)S.V[q]);
-        S.W[o] = (T)(2.0 * wn - (double)S.W[q]);
-        S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
-        S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
-        S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
-      }
-    } else if (!ii && jj) {  // west/east ghost columns of interior rows
-      const int src = mirror(i, S.IB, S.IE);
-      const T s = (T)((i < S.IB ? S.bc_x0 : S.bc_xn) == 1 ? 1 : -1);
-      for (int k = S.KB; k <= S.KE; ++k) {
-        const long long o = i3(S, i, j, k), q = i3(S, src, j, k);
-        S.U[o] = -S.U[q]; S.V[o] = s * S.V[q]; S.W[o] = s * S.W[q];
-        S.DU[o] = -S.DU[q]; S.DV[o] = s * S.DV[q]; S.DW[o] = s * S.DW[q];
-      }
-    } else if (ii && !jj) {  // south/north ghost rows of interior columns
-      const int src = mirror(j, S.JB, S.JE);
-      const T s = (T)((j < S.JB ? S.bc_y0 : S.bc_yn) == 1 ? 1 : -1);
-      for (int k = S.KB; k <= S.KE; ++k) {
-        const long long o = i3(S, i, j, k), q = i3(S, i, src, k);
-        S.U[o] = s * S.U[q]; S.V[o] = -S.V[q]; S.W[o] = s * S.W[q];
-        S.DU[o] = s * S.DU[q]; S.DV[o] = -S.DV[q]; S.DW[o] = s * S.DW[q];
-      }
     }
   }
 };
-
-// vel_bc, part B: bed and surface ghosts of interior columns
-// (free-slip bed; Derakhti et al. stress condition at the surface)
+// lateral ghost cells of U, V, W, DU, DV, DW (src/nhwave.F:4416-4621): one
+// thread per (ghost column or ghost row, level); corner columns stay untouched
+struct OpVelBcLat {
+  static constexpr const char* kName = "vel_bc_lat";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const bool ii = (i >= S.IB && i <= S.IE), jj = (j >= S.JB && j <= S.JE);
+    if (ii == jj) return;
+    const long long o = i3(S, i, j, k);
+    if (jj && i < S.IB && S.bc_x0 == 3) {  // inflow ghosts (src/nhwave.F:4468-4476)
+      const int src = mirror(i, S.IB, S.IE);
+      const long long q = i3(S, src, j, k);
+      const double dn = S.Din[j];
+      const double un = S.Uin[j + S.Nloc * k], vn = S.Vin[j + S.Nloc * k], wn = S.Win[j + S.Nloc * k];
+      S.U[o] = (T)(2.0 * un - (double)S.U[q]);
+      S.V[o] = (T)(2.0 * vn - (double)S.V[q]);
+      S.W[o] = (T)(2.0 * wn - (double)S.W[q]);
+      S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
+      S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
+      S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
+    } else if (jj) {  // west/east ghost columns of interior rows
+      const int src = mirror(i, S.IB, S.IE);
+      const T s = (T)((i < S.IB ? S.bc_x0 : S.bc_xn) == 1 ? 1 : -1);
+      const long long q = i3(S, src, j, k);
+      S.U[o] = -S.U[q]; S.V[o] = s * S.V[q]; S.W[o] = s * S.W[q];
+      S.DU[o] = -S.DU[q]; S.DV[o] = s * S.DV[q]; S.DW[o] = s * S.DW[q];
+    } else {  // south/north ghost rows of interior columns
+      const int src = mirror(j, S.JB, S.JE);
+      const T s = (T)((j < S.JB ? S.bc_y0 : S.bc_yn) == 1 ? 1 : -1);
+      const long long q = i3(S, i, src, k);
+      S.U[o] = s * S.U[q]; S.V[o] = -S.V[q]; S.W[o] = s * S.W[q];
+      S.DU[o] = s * S.DU[q]; S.DV[o] = -S.DV[q]; S.DW[o] = s * S.DW[q];
+    }
+  }
+};
 struct OpVelBcB {
   static constexpr const char* kName = "vel_bc_b";
   template <class T>
@@ -643,47 +648,50 @@ struct OpVelBcB {
       return (x >= S.IB && x <= S.IE && y >= S.JB && y <= S.JE) ? a[i2(S, x, y)] : 0.0;
     };
     const bool wet = S.Mask[c] != 0;
-    auto dx_ = [&](const double* a) -> double {
-      return wet ? lim_slope<double>(zl(a, i - 1, j), a[c], zl(a, i + 1, j), S.dx, S.dx) : 0.0;
+    // arithmetic of the surface stress ghosts: FP64 in the FP64 form, FP32 in FP32+IR
+    using R = typename std::conditional<sizeof(T) == 4, float, double>::type;
+    auto dx_ = [&](const double* a) -> R {
+      return wet ? lim_slope<R>((R)zl(a, i - 1, j), (R)a[c], (R)zl(a, i + 1, j), (R)S.dx, (R)S.dx) : (R)0;
     };
-    auto dy_ = [&](const double* a) -> double {
-      return wet ? lim_slope<double>(zl(a, i, j - 1), a[c], zl(a, i, j + 1), S.dy, S.dy) : 0.0;
+    auto dy_ = [&](const double* a) -> R {
+      return wet ? lim_slope<R>((R)zl(a, i, j - 1), (R)a[c], (R)zl(a, i, j + 1), (R)S.dy, (R)S.dy) : (R)0;
     };
-    const double DelxUzL = dx_(S.zUL), DelxVzL = dx_(S.zVL), DelxWzL = dx_(S.zWL);
-    const double DelyUzL = dy_(S.zUL), DelyVzL = dy_(S.zVL), DelyWzL = dy_(S.zWL);
-    const double dxe = S.DelxEta[c], dye = S.DelyEta[c], Dij = S.D[c];
-    const double Atop = sqrt(1.0 + dxe * dxe + dye * dye);
-    const double Fext_Wind1 = 1.0 / Atop * ((1 - dxe * dxe) * S.Wsx[c] - dxe * dye * S.Wsy[c]);
-    const double Fext_Wind2 = 1.0 / Atop * ((1 - dye * dye) * S.Wsy[c] - dxe * dye * S.Wsx[c]);
-    const double MinDepBC = (double)0.01f;
-    const double WzLt = S.zWL[c], WzRb = S.zWR[c], UzLt = S.zUL[c], VzLt = S.zVL[c];
+    const R DelxUzL = dx_(S.zUL), DelxVzL = dx_(S.zVL), DelxWzL = dx_(S.zWL);
+    const R DelyUzL = dy_(S.zUL), DelyVzL = dy_(S.zVL), DelyWzL = dy_(S.zWL);
+    const R dxe = (R)S.DelxEta[c], dye = (R)S.DelyEta[c], Dij = (R)S.D[c];
+    const R Atop = sqrt((R)1.0 + dxe * dxe + dye * dye);
+    const R Fext_Wind1 = (R)1.0 / Atop * (((R)1 - dxe * dxe) * (R)S.Wsx[c] - dxe * dye * (R)S.Wsy[c]);
+    const R Fext_Wind2 = (R)1.0 / Atop * (((R)1 - dye * dye) * (R)S.Wsy[c] - dxe * dye * (R)S.Wsx[c]);
+    const R MinDepBC = (R)(double)0.01f;
+    const R WzLt = (R)S.zWL[c], WzRb = (R)S.zWR[c], UzLt = (R)S.zUL[c], VzLt = (R)S.zVL[c];
+    const R vtop = (R)S.visc_top;
     const int KB = S.KB, KE = S.KE;
     for (int k = 1; k <= NG; ++k) {
       const long long ob = i3(S, i, j, KB - k), oi = i3(S, i, j, KB + k - 1);
       const long long ot = i3(S, i, j, KE + k), os = i3(S, i, j, KE - k + 1);
-      S.DW[ob] = (T)(2.0 * Dij * WzRb - (double)S.DW[oi]);
+      S.DW[ob] = (T)((R)2.0 * Dij * WzRb - (R)S.DW[oi]);
       S.DU[ob] = S.DU[oi];
       S.DV[ob] = S.DV[oi];
-      const double dsg = S.sigc[KE + k] - S.sigc[KE - k + 1];
-      const double DWs = (double)S.DW[os], DUs = (double)S.DU[os], DVs = (double)S.DV[os];
-      S.DW[ot] = (T)(2.0 * Dij * WzLt - DWs);
-      double du = DUs + dsg * (Fext_Wind1 * (Dij * Dij / Atop / S.visc_top) -
-                               dxe * (Dij * WzLt - DWs) / (dsg / 2.0) +
-                               Dij * Dij / (Atop * Atop) *
-                                   (+2.0 * dxe * DelxUzL - (1.0 - dxe * dxe) * DelxWzL +
-                                    dye * (DelyUzL + DelxVzL + dxe * DelyWzL)));
-      const double DUtop_old = 2.0 * Dij * UzLt - DUs;
-      if (DUtop_old > 0.) du = dmin_(3.0 * DUtop_old, dmax_(-1.0 * DUtop_old, du));
-      else if (DUtop_old < 0.) du = dmax_(3.0 * DUtop_old, dmin_(-1.0 * DUtop_old, du));
+      const R dsg = (R)(S.sigc[KE + k] - S.sigc[KE - k + 1]);
+      const R DWs = (R)S.DW[os], DUs = (R)S.DU[os], DVs = (R)S.DV[os];
+      S.DW[ot] = (T)((R)2.0 * Dij * WzLt - DWs);
+      R du = DUs + dsg * (Fext_Wind1 * (Dij * Dij / Atop / vtop) -
+                          dxe * (Dij * WzLt - DWs) / (dsg / (R)2.0) +
+                          Dij * Dij / (Atop * Atop) *
+                              (+(R)2.0 * dxe * DelxUzL - ((R)1.0 - dxe * dxe) * DelxWzL +
+                               dye * (DelyUzL + DelxVzL + dxe * DelyWzL)));
+      const R DUtop_old = (R)2.0 * Dij * UzLt - DUs;
+      if (DUtop_old > (R)0) du = rmin<R>((R)3.0 * DUtop_old, rmax<R>((R)-1.0 * DUtop_old, du));
+      else if (DUtop_old < (R)0) du = rmax<R>((R)3.0 * DUtop_old, rmin<R>((R)-1.0 * DUtop_old, du));
       if (Dij < MinDepBC) du = DUs;
-      double dv = DVs + dsg * (Fext_Wind2 * (Dij * Dij / Atop / S.visc_top) -
-                               dye * (Dij * WzLt - DWs) / (dsg / 2.0) +
-                               Dij * Dij / (Atop * Atop) *
-                                   (+2.0 * dye * DelyVzL - (1.0 - dye * dye) * DelyWzL +
-                                    dxe * (DelxVzL + DelyUzL + dye * DelxWzL)));
-      const double DVtop_old = 2.0 * Dij * VzLt - DVs;
-      if (DVtop_old > 0.) dv = dmin_(3.0 * DVtop_old, dmax_(-1.0 * DVtop_old, dv));
-      else if (DVtop_old < 0.) dv = dmax_(3.0 * DVtop_old, dmin_(-1.0 * DVtop_old, dv));
+      R dv = DVs + dsg * (Fext_Wind2 * (Dij * Dij / Atop / vtop) -
+                          dye * (Dij * WzLt - DWs) / (dsg / (R)2.0) +
+                          Dij * Dij / (Atop * Atop) *
+                              (+(R)2.0 * dye * DelyVzL - ((R)1.0 - dye * dye) * DelyWzL +
+                               dxe * (DelxVzL + DelyUzL + dye * DelxWzL)));
+      const R DVtop_old = (R)2.0 * Dij * VzLt - DVs;
+      if (DVtop_old > (R)0) dv = rmin<R>((R)3.0 * DVtop_old, rmax<R>((R)-1.0 * DVtop_old, dv));
+      else if (DVtop_old < (R)0) dv = rmax<R>((R)3.0 * DVtop_old, rmin<R>((R)-1.0 * DVtop_old, dv));
       if (Dij < MinDepBC) dv = DVs;
       S.DU[ot] = (T)du;
       S.DV[ot] = (T)dv;

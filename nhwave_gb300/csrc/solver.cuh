@@ -657,7 +657,8 @@ class Solver final : public SolverBase {
     h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
     NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
     // initial: vel_bc on the initial velocities, then DU = D*U*Mask
-    allcols(OpVelBcA{});
+    incols(OpVelBcA{});
+    box(OpVelBcLat{}, S.Mloc, S.Nloc, S.K, 0, 0, S.KB);
     incols(OpVelBcB{});
     L(OpInitDU::kName, [&] {
       k_allcells<T, OpInitDU><<<cdiv((long long)S.Mloc * S.Nloc * S.Kloc, 256), 256, 0, st>>>(S, OpInitDU{});
@@ -738,7 +739,8 @@ class Solver final : public SolverBase {
   }
   void get_uvw() {
     cells(OpGetUVW{});
-    allcols(OpVelBcA{});
+    incols(OpVelBcA{});
+    box(OpVelBcLat{}, S.Mloc, S.Nloc, S.K, 0, 0, S.KB);
     incols(OpVelBcB{});
   }
   // generate_coef_rhs (src/pressure.F:475-840), line factors, initial guess
