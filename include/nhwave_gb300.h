@@ -47,7 +47,7 @@ extern "C" {
 enum nhw_status {
   NHW_OK = 0,
   NHW_ERR_ARG = 1,           /* null pointer, bad size or bad field id            */
-  NHW_ERR_UNSUPPORTED = 2,   /* option outside this path (HLLC, viscous, open BC) */
+  NHW_ERR_UNSUPPORTED = 2,   /* option outside this path (viscous, open BC)       */
   NHW_ERR_CUDA = 3,          /* CUDA runtime error (message: nhw_last_error)      */
   NHW_ERR_NOMEM = 4,         /* device allocation failed                          */
   NHW_ERR_DT_MIN = 5,        /* dt < DT_MIN: the reference stops here             */
@@ -89,7 +89,7 @@ typedef struct nhw_params {
   double  min_dep;                         /* MinDep                                  */
   int32_t non_hydro;                       /* NON_HYDRO                               */
   int32_t time_order;                      /* 1,2,3 <- TIME_ORDER FIRST/SECOND/THIRD  */
-  int32_t hllc;                            /* HLLC (must be 0)                        */
+  int32_t hllc;                            /* HLLC: 1 HLLC face fluxes, 0 HLL          */
   int32_t viscous_flow;                    /* VISCOUS_FLOW (must be 0)                */
   int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
   int32_t itmax; double tol;               /* ITMAX TOL                               */

@@ -52,6 +52,24 @@ template <class R>
 __device__ __forceinline__ R hll(R sl, R sr, R fl, R fr, R ul, R ur) {
   return hll_d<R>(sl, sr, fl, fr, ur - ul);
 }
+// Contact speed of a wet/wet face for HLLC in FP32: (uL+uR)/2 + sqrt(g dL) -
+// sqrt(g dR) (src/nhwave.F:2835), the difference of the two roots formed as
+// g (dL - dR) / (sqrt(g dL) + sqrt(g dR)) with dL - dR in FP64.  The plain
+// difference of two FP32 roots of about 1-10 m/s cancels to an absolute error
+// of a few 1e-7 m/s, which the HLLC mass flux carries in full (HLL takes
+// dR - dL in FP64 and never forms it).
+__device__ __forceinline__ float contact_speed_f32(float uL, float uR, float pL, float pR, double dL,
+                                                   double dR) {
+  return 0.5f * (uL + uR) + (float)(dL - dR) * (float)kGrav / (pL + pR);
+}
+// HLLC (src/nhwave.F:2779-2810): uls/urs are the star states of the face
+template <class R>
+__device__ __forceinline__ R hllc(R sl, R sr, R ss, R fl, R fr, R ul, R uls, R ur, R urs) {
+  if (sl >= (R)0) return fl;
+  if (sr <= (R)0) return fr;
+  if (ss >= (R)0) return fl + sl * (uls - ul);
+  return fr + sr * (urs - ur);
+}
 
 __device__ __forceinline__ int mirror(int i, int b, int e) {
   return i < b ? 2 * b - 1 - i : (i > e ? 2 * e + 1 - i : i);
@@ -334,26 +352,44 @@ struct OpFluxX {
     const R GxL = rdL * uL * vL, GxR = rdR * uR * vR;
     const R HxL = rdL * uL * wL, HxR = rdR * uR * wR;
     // wave speeds (src/nhwave.F:2813-2849)
-    R SL = (R)0, SR = (R)0;
+    R SL = (R)0, SR = (R)0, SS = (R)0;
     if (mL == 1 && mR == 1) {
       R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
       R pS = (R)0.5 * (pL + pR) + (R)0.25 * (uL - uR);
       R uS = (R)0.5 * (uL + uR) + pL - pR;
       SL = rmin<R>(uL - pL, uS - pS);
       SR = rmax<R>(uR + pR, uS + pS);
+      SS = uS;
+      if constexpr (sizeof(R) == 4) {
+        if (S.hllc) SS = contact_speed_f32(uL, uR, pL, pR, dL, dR);
+      }
     } else if (mL == 0 && mR == 1) {
       R pR = sqrt((R)kGrav * fabs(rdR));
       SL = uR - (R)2.0 * pR;
       SR = uR + pR;
+      SS = SL;
     } else if (mL == 1 && mR == 0) {
       R pL = sqrt((R)kGrav * fabs(rdL));
       SL = uL - pL;
       SR = uL + (R)2.0 * pL;
+      SS = SR;
     }
-    R Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
-    R Fx = hll<R>(SL, SR, FxL, FxR, duL, duR);
-    R Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
-    R Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
+    R Ex, Fx, Gx, Hx;
+    if (S.hllc) {   // HLLC (src/nhwave.F:2555-2670); the mass-flux star state in FP64
+      const double sl = SL, sr = SR, ss = SS;
+      const double ls = dL * (sl - (double)uL + kSmall) / (sl - ss + kSmall);
+      const double rs = dR * (sr - (double)uR + kSmall) / (sr - ss + kSmall);
+      Ex = (R)hllc<double>(sl, sr, ss, (double)duL, (double)duR, dL, ls, dR, rs);
+      const R lsR = (R)ls, rsR = (R)rs;
+      Fx = hllc<R>(SL, SR, SS, FxL, FxR, duL, lsR * SS, duR, rsR * SS);
+      Gx = hllc<R>(SL, SR, SS, GxL, GxR, dvL, lsR * vL, dvR, rsR * vR);
+      Hx = hllc<R>(SL, SR, SS, HxL, HxR, dwL, lsR * wL, dwR, rsR * wR);
+    } else {
+      Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
+      Fx = hll<R>(SL, SR, FxL, FxR, duL, duR);
+      Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
+      Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
+    }
     // flux_bc: walls, then dry cells (src/nhwave.F:2366-2434, 2508-2549)
     if (f == S.IB) {
       if (S.bc_x0 == 3) {   // inflow (src/nhwave.F:2381-2387)
@@ -432,26 +468,44 @@ struct OpFluxY {
     const R FyL = rdL * uL * vL, FyR = rdR * uR * vR;
     const R GyL = dvL * vL + hydro<R>(reL, rh0), GyR = dvR * vR + hydro<R>(reR, rh0);
     const R HyL = rdL * vL * wL, HyR = rdR * vR * wR;
-    R SL = (R)0, SR = (R)0;
+    R SL = (R)0, SR = (R)0, SS = (R)0;
     if (mL == 1 && mR == 1) {
       R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
       R pS = (R)0.5 * (pL + pR) + (R)0.25 * (vL - vR);
       R uS = (R)0.5 * (vL + vR) + pL - pR;
       SL = rmin<R>(vL - pL, uS - pS);
       SR = rmax<R>(vR + pR, uS + pS);
+      SS = uS;
+      if constexpr (sizeof(R) == 4) {
+        if (S.hllc) SS = contact_speed_f32(vL, vR, pL, pR, dL, dR);
+      }
     } else if (mL == 0 && mR == 1) {
       R pR = sqrt((R)kGrav * fabs(rdR));
       SL = vR - (R)2.0 * pR;
       SR = vR + pR;
+      SS = SL;
     } else if (mL == 1 && mR == 0) {
       R pL = sqrt((R)kGrav * fabs(rdL));
       SL = vL - pL;
       SR = vL + (R)2.0 * pL;
+      SS = SR;
     }
-    R Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
-    R Fy = hll<R>(SL, SR, FyL, FyR, duL, duR);
-    R Gy = hll<R>(SL, SR, GyL, GyR, dvL, dvR);
-    R Hy = hll<R>(SL, SR, HyL, HyR, dwL, dwR);
+    R Ey, Fy, Gy, Hy;
+    if (S.hllc) {   // HLLC (src/nhwave.F:2555-2670); the mass-flux star state in FP64
+      const double sl = SL, sr = SR, ss = SS;
+      const double ls = dL * (sl - (double)vL + kSmall) / (sl - ss + kSmall);
+      const double rs = dR * (sr - (double)vR + kSmall) / (sr - ss + kSmall);
+      Ey = (R)hllc<double>(sl, sr, ss, (double)dvL, (double)dvR, dL, ls, dR, rs);
+      const R lsR = (R)ls, rsR = (R)rs;
+      Fy = hllc<R>(SL, SR, SS, FyL, FyR, duL, lsR * uL, duR, rsR * uR);
+      Gy = hllc<R>(SL, SR, SS, GyL, GyR, dvL, lsR * SS, dvR, rsR * SS);
+      Hy = hllc<R>(SL, SR, SS, HyL, HyR, dwL, lsR * wL, dwR, rsR * wR);
+    } else {
+      Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
+      Fy = hll<R>(SL, SR, FyL, FyR, duL, duR);
+      Gy = hll<R>(SL, SR, GyL, GyR, dvL, dvR);
+      Hy = hll<R>(SL, SR, HyL, HyR, dwL, dwR);
+    }
     if (g == S.JB) { Ey = (R)0; Fy = (R)0; Gy = hydro<R>(reR, rh0); Hy = (R)0; }
     if (g == S.JE + 1) { Ey = (R)0; Fy = (R)0; Gy = hydro<R>(reL, rh0); Hy = (R)0; }
     if (mR == 0) {

@@ -22,7 +22,7 @@ int check_params(const nhw_params& p) {
   if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1) return NHW_ERR_ARG;
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
-  if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+  if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
   for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
   const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;

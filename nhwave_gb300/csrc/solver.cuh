@@ -213,6 +213,7 @@ class Solver final : public SolverBase {
     S.total_time = p.total_time; S.sim_steps = p.sim_steps;
     S.graph_mode = 0; S.h_go = S.h_ir = S.h_inner = 0;
     S.non_hydro = p.non_hydro; S.sponge_on = p.sponge_on;
+    S.hllc = p.hllc ? 1 : 0;
     S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
     S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
     S.wavemaker = p.wavemaker;

@@ -71,6 +71,7 @@ struct Dev {
   double dx, dy, min_dep, cfl, dt_min, dt_max, fcor, froude_cap;
   double cxx, cyy;                 // Poisson in-level couplings -1/dx^2, -1/dy^2
   int froude_on, non_hydro, sponge_on, it_order;
+  int hllc;                        // HLLC face fluxes (ADV_HLLC) instead of HLL
   int bc_x0, bc_xn, bc_y0, bc_yn;
   double tol, tol_floor;          // outer Poisson tolerance (TOL); floor of the inner one
   int itmax, max_ir;               // ITMAX over all inner iterations; refinement sweeps

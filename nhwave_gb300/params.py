@@ -198,8 +198,6 @@ def read_input(path: str) -> NhwParams:
 
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
-    if p.hllc:
-        return "HLLC=T (HLLC fluxes are outside the GPU path)"
     if p.viscous_flow:
         return "VISCOUS_FLOW=T (viscous/turbulent terms are outside the GPU path)"
     if not p.barotropic:

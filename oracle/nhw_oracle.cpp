@@ -143,7 +143,7 @@ struct Model {
   int create(const nhw_params& q) {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
-    if (p.hllc || p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
     for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
     const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
@@ -942,6 +942,57 @@ struct Model {
         }
   }
 
+  // HLLC (src/nhwave.F:2779-2810): left/right/star states of one face
+  static double HLLC(double sl, double sr, double ss, double fl, double fr, double ul, double uls, double ur,
+                     double urs) {
+    if (sl >= Zero) return fl;
+    if (sr <= Zero) return fr;
+    if (ss >= Zero) return fl + sl * (uls - ul);
+    return fr + sr * (urs - ur);
+  }
+  // fluxes_at_faces_HLLC (src/nhwave.F:2555-2670).  The reference forms every
+  // star state as DxL*(SxL-UxL+Small)/(SxL-SxS+Small) times a factor; the
+  // common product is formed once here, with the same operations in the same
+  // order.
+  void fluxes_at_faces_HLLC() {
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc1; ++i) {
+          const double sl = SxL(i, j, k), sr = SxR(i, j, k), ss = SxS(i, j, k);
+          const double dl = DxL(i, j), dr = DxR(i, j);
+          const double ls = dl * (sl - UxL(i, j, k) + Small) / (sl - ss + Small);
+          const double rs = dr * (sr - UxR(i, j, k) + Small) / (sr - ss + Small);
+          Ex(i, j, k) = HLLC(sl, sr, ss, ExL(i, j, k), ExR(i, j, k), dl, ls, dr, rs);
+          Fx(i, j, k) = HLLC(sl, sr, ss, FxL(i, j, k), FxR(i, j, k), DUxL(i, j, k), ls * ss, DUxR(i, j, k), rs * ss);
+          Gx(i, j, k) = HLLC(sl, sr, ss, GxL(i, j, k), GxR(i, j, k), DVxL(i, j, k), ls * VxL(i, j, k), DVxR(i, j, k),
+                             rs * VxR(i, j, k));
+          Hx(i, j, k) = HLLC(sl, sr, ss, HxL(i, j, k), HxR(i, j, k), DWxL(i, j, k), ls * WxL(i, j, k), DWxR(i, j, k),
+                             rs * WxR(i, j, k));
+        }
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc1; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          const double sl = SyL(i, j, k), sr = SyR(i, j, k), ss = SyS(i, j, k);
+          const double dl = DyL(i, j), dr = DyR(i, j);
+          const double ls = dl * (sl - VyL(i, j, k) + Small) / (sl - ss + Small);
+          const double rs = dr * (sr - VyR(i, j, k) + Small) / (sr - ss + Small);
+          Ey(i, j, k) = HLLC(sl, sr, ss, EyL(i, j, k), EyR(i, j, k), dl, ls, dr, rs);
+          Fy(i, j, k) = HLLC(sl, sr, ss, FyL(i, j, k), FyR(i, j, k), DUyL(i, j, k), ls * UyL(i, j, k), DUyR(i, j, k),
+                             rs * UyR(i, j, k));
+          Gy(i, j, k) = HLLC(sl, sr, ss, GyL(i, j, k), GyR(i, j, k), DVyL(i, j, k), ls * ss, DVyR(i, j, k), rs * ss);
+          Hy(i, j, k) = HLLC(sl, sr, ss, HyL(i, j, k), HyR(i, j, k), DWyL(i, j, k), ls * WyL(i, j, k), DWyR(i, j, k),
+                             rs * WyR(i, j, k));
+        }
+    for (int k = Kbeg + 1; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          double om = Omega(i, j, k);
+          Fz(i, j, k) = 0.5 * (om * (UzL(i, j, k) + UzR(i, j, k)) - std::fabs(om) * (UzR(i, j, k) - UzL(i, j, k)));
+          Gz(i, j, k) = 0.5 * (om * (VzL(i, j, k) + VzR(i, j, k)) - std::fabs(om) * (VzR(i, j, k) - VzL(i, j, k)));
+          Hz(i, j, k) = 0.5 * (om * (WzL(i, j, k) + WzR(i, j, k)) - std::fabs(om) * (WzR(i, j, k) - WzL(i, j, k)));
+        }
+  }
+
   void flux_bc() {
     for (int j = Jbeg; j <= Jend; ++j)
       for (int k = Kbeg; k <= Kend; ++k) {  // walls: Bc 1, 2 (5); inflow: Bc 3 (src/nhwave.F:2375-2387)
@@ -992,7 +1043,8 @@ struct Model {
     delxyzFun();
     construction();
     wave_speed();
-    fluxes_at_faces_HLL();
+    if (p.hllc) fluxes_at_faces_HLLC();   // src/nhwave.F:1705-1709
+    else fluxes_at_faces_HLL();
     flux_bc();
   }
 

@@ -41,10 +41,10 @@ def _routines(s):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4", "tiny_flume_lin", "tiny_flume_sol"])
-def test_graph_step_equals_routines(name, precision, gpu_lib):
+def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
     from nhwave_gb300 import fields as F
-    a = _scen(name, precision)
-    b = _scen(name, precision)
+    a = _scen(name, precision, hllc=hllc)
+    b = _scen(name, precision, hllc=hllc)
     for n in range(3):
         a.step()
         _routines(b)
@@ -57,6 +57,13 @@ def test_graph_step_equals_routines(name, precision, gpu_lib):
             x, y = a.get(fid), b.get(fid)
             bad = np.argwhere(x != y)
             assert bad.size == 0, f"step {n}: {f} differs at {bad[:4].tolist()}"
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", ["tiny_c2", "tiny_c3"])
+def test_graph_step_equals_routines_hllc(name, precision, gpu_lib):
+    """The same with HLLC=T face fluxes."""
+    test_graph_step_equals_routines(name, precision, gpu_lib, hllc=1)
 
 
 def test_run_gate_sim_steps(gpu_lib):

@@ -61,11 +61,13 @@ def test_setup_bit_exact(name, oracle_mod, gpu_lib):
     _cmp_exact(g, o, ["MASK", "MASK_STRUCT", "MASK9"] + STATE2D + ["SPONGE"] + STATE3D, "setup")
 
 
+@pytest.mark.parametrize("hllc", [0, 1])
 @pytest.mark.parametrize("name", CASES)
-def test_explicit_routines_bit_exact(name, oracle_mod, gpu_lib):
-    """estimate_dt .. fluxes, and a hydrostatic eval_duvw, match operation for operation."""
+def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
+    """estimate_dt .. fluxes, and a hydrostatic eval_duvw, match operation for
+    operation, with HLL and with HLLC face fluxes (src/nhwave.F:1705-1709)."""
     from nhwave_gb300 import fields as F
-    g, o = _pair(name, oracle_mod, non_hydro=0)
+    g, o = _pair(name, oracle_mod, non_hydro=0, hllc=hllc)
     for rnd in range(2):
         for obj in (g, o):
             assert obj.estimate_dt() == 0
@@ -251,4 +253,33 @@ def test_flume_steps_fp32_ir(name, oracle_mod, gpu_lib):
     assert np.array_equal(g.get(F.MASK), o.get(F.MASK))
     r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
     assert r < 1e-6, f"{name} eta rel L2 {r:.3e}"
+    g.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", CASES)
+def test_hllc_steps(name, precision, oracle_mod, gpu_lib):
+    """Whole non-hydrostatic steps with HLLC=T: FP64 within 1e-10 of the
+    oracle (eta and P), FP32+IR eta within 1e-6; the mask bit for bit (the
+    landslide case has a moving wet/dry front, where the dry-side star
+    speeds of src/nhwave.F:2842-2853 are used).  FP64 steps the slide case
+    with the oracle's bathymetry pinned, as test_steps_fp64 does."""
+    from nhwave_gb300 import fields as F
+    g, o = _pair(name, oracle_mod, precision=precision, hllc=1)
+    for n in range(6):
+        if precision == 0 and g.params.slide_type:
+            step_pinned(g, o)
+        else:
+            assert g.step() == 0 and o.step() == 0
+        assert np.array_equal(g.get(F.MASK), o.get(F.MASK)), f"mask differs after step {n}"
+    sl = o.shape.interior
+    lim = 1e-10 if precision == 0 else 1e-6
+    r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
+    assert r < lim, f"{name} eta rel L2 {r:.3e}"
+    if precision == 0:
+        r = rel_l2(g.get(F.P)[sl(F.P)], o.get(F.P)[sl(F.P)])
+        assert r < 1e-10, f"{name} P rel L2 {r:.3e}"
+        for f in ("U", "V", "W"):
+            r = vel_err(g, o, f)
+            assert r < 1e-10, f"{name} {f}: rel L2 {r:.3e}"
     g.close()

@@ -64,13 +64,14 @@ def test_flat_bed_poisson_coefficients(oracle_mod):
     assert np.all(coef[[3, 4, 5, 6, 7], top] == 0.0)                 # Dirichlet P = 0 above
 
 
-def test_lake_at_rest(oracle_mod):
+@pytest.mark.parametrize("hllc", [0, 1])
+def test_lake_at_rest(hllc, oracle_mod):
     """A lake at rest stays at rest but for the SSP-RK3 coefficient sum: each step
     scales D by ALPHA(3)+BETA(3) = 1 + 2.98e-8, lifting eta by Hc*(g^n - 1)."""
     from nhwave_gb300 import default_params, fields as F
     rng = np.random.default_rng(3)
     M, N, K = 24, 10, 4
-    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=1.0, dy=1.0, tol=1e-12, dt_ini=0.05)
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=1.0, dy=1.0, tol=1e-12, dt_ini=0.05, hllc=hllc)
     depth = 5.0 + rng.uniform(0.0, 2.0, size=M * N)
     o = oracle_mod.Oracle(p, depth)
     n = 4
@@ -86,9 +87,10 @@ def test_lake_at_rest(oracle_mod):
     assert np.abs(o.get(F.U)[sl(F.U)]).max() < 1e-6
 
 
-def test_mass_grows_by_rk_coefficient_sum(oracle_mod):
+@pytest.mark.parametrize("hllc", [0, 1])
+def test_mass_grows_by_rk_coefficient_sum(hllc, oracle_mod):
     from nhwave_gb300 import scenarios as S
-    p, d, e, u = S.make("tiny_c1")
+    p, d, e, u = S.make("tiny_c1", hllc=hllc)
     p.tol = 1e-12
     o = oracle_mod.Oracle(p, d, e, u)
     m0 = o.mass()
@@ -99,17 +101,44 @@ def test_mass_grows_by_rk_coefficient_sum(oracle_mod):
     assert o.mass() / m0 == pytest.approx(growth ** n, abs=1e-13)
 
 
-def test_mirror_symmetry(oracle_mod):
+@pytest.mark.parametrize("hllc", [0, 1])
+def test_mirror_symmetry(hllc, oracle_mod):
     from nhwave_gb300 import default_params, fields as F
     M, N, K = 30, 6, 4
-    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.5, tol=1e-13, dt_ini=0.01)
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.5, tol=1e-13, dt_ini=0.01, hllc=hllc)
     x = (np.arange(M) + 0.5) * 0.5
     eta = 0.05 * np.exp(-((x - 7.5) / 2.0) ** 2)
     o = oracle_mod.Oracle(p, np.full(M * N, 2.0), np.tile(eta, N))
     for _ in range(4):
         assert o.step() == 0
     e2 = o.get(F.ETA)[o.shape.interior(F.ETA)]
-    assert np.abs(e2 - e2[:, ::-1]).max() < 1e-12 * np.abs(e2).max()
+    # HLLC's left mass flux is DUxL + SxL*(DxL*(SxL-UxL)/(SxL-SxS) - DxL)
+    # (src/nhwave.F:1792, 2585, 2799): at SxS = 0 it is DUxL - DxL*UxL, the
+    # gap between the reconstructed D*U and the product of the reconstructed
+    # D and U, and the right one is its mirror image.  The branch SxS >= 0
+    # takes the left one, so on the symmetry plane (SxS = 0) the mass flux is
+    # that second-order gap instead of zero: the mirror image holds to
+    # O(dx^2 * slope products) only
+    lim = 1e-12 if not hllc else 1e-6
+    assert np.abs(e2 - e2[:, ::-1]).max() < lim * np.abs(e2).max()
+
+
+def test_hllc_close_to_hll_on_a_smooth_wave(oracle_mod):
+    """HLLC (src/nhwave.F:2555-2670) differs from HLL only by the contact
+    wave's star state: on a smooth, subcritical wave both agree to the
+    truncation error, the mass is the same to rounding, and they differ."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    out = []
+    for hllc in (0, 1):
+        p, d, e, u = S.make("tiny_c2", hllc=hllc)
+        p.tol = 1e-12
+        o = oracle_mod.Oracle(p, d, e, u)
+        for _ in range(6):
+            assert o.step() == 0
+        out.append((o.get(F.ETA)[o.shape.interior(F.ETA)], o.mass()))
+    r = rel_l2(out[1][0], out[0][0])
+    assert 0.0 < r < 1e-2
+    assert out[1][1] == pytest.approx(out[0][1], rel=1e-13)
 
 
 @pytest.mark.parametrize("name", list(GOLDEN))

@@ -74,4 +74,7 @@ def test_out_of_scope_reason(tmp_path):
     from nhwave_gb300 import params as P
     f = tmp_path / "input.txt"
     f.write_text(SAMPLE.replace("HLLC = F", "HLLC = T"))
-    assert "HLLC" in P.unsupported_reason(P.read_input(str(f)))
+    p = P.read_input(str(f))
+    assert p.hllc == 1 and P.unsupported_reason(p) is None
+    f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 2"))
+    assert "BC_Z0" in P.unsupported_reason(P.read_input(str(f)))
