@@ -85,43 +85,82 @@ __device__ __forceinline__ T level_apply(const MGL<T>& L, const T* __restrict__ 
 // Neighbour value for the first post-smoothing half-sweep: x + w * P x_c,
 // the coarse-grid correction applied on the fly (the swept colour recomputes
 // its own columns, the other colour is corrected by the next half-sweep).
+//
+// P interpolates bilinearly in the horizontal between the centres of the
+// aggregates (weights 3/4, 1/4 for 2 x 2 aggregates; the aggregate's own value
+// at the walls), level by level in the vertical.  Restriction stays the
+// aggregate sum P0^T and the coarse operator the rescaled product of P0
+// (k_mg_galerkin): the piecewise-constant P0 leaves a saw-tooth in every
+// corrected smooth error, which the bilinear form does not.
 template <class T>
 struct Prolong {
   const T* xc;    // coarse solution (nullptr: plain x)
   T w;
-  int rx, ry, Mc, MNc, M, MN;
+  int rx, ry, Mc, MNc, M, MN, Nc;
+  T hx, hy;       // 1 / (2 rx), 1 / (2 ry)
+  __device__ __forceinline__ T coarse(int ic) const {
+    const int kk = ic / MN, r = ic - kk * MN, jj = r / M, ii = r - jj * M;
+    const int I = ii / rx, J = jj / ry;
+    // fine-cell centre relative to its aggregate's centre, in coarse cells
+    const T ox = (T)(2 * (ii - I * rx) + 1 - rx) * hx, oy = (T)(2 * (jj - J * ry) + 1 - ry) * hy;
+    int I2 = ox < (T)0 ? I - 1 : I + 1, J2 = oy < (T)0 ? J - 1 : J + 1;
+    T wx = ox < (T)0 ? -ox : ox, wy = oy < (T)0 ? -oy : oy;
+    if (I2 < 0 || I2 >= Mc) { I2 = I; wx = (T)0; }
+    if (J2 < 0 || J2 >= Nc) { J2 = J; wy = (T)0; }
+    const T* c = xc + MNc * kk;
+    return ((T)1 - wy) * (((T)1 - wx) * c[I + Mc * J] + wx * c[I2 + Mc * J]) +
+           wy * (((T)1 - wx) * c[I + Mc * J2] + wx * c[I2 + Mc * J2]);
+  }
   __device__ __forceinline__ T operator()(const T* __restrict__ x, int ic) const {
     if (!xc) return x[ic];
-    const int kk = ic / MN, r = ic - kk * MN, jj = r / M, ii = r - jj * M;
-    return x[ic] + w * xc[ii / rx + Mc * (jj / ry) + MNc * kk];
+    return x[ic] + w * coarse(ic);
+  }
+  // the horizontal part of coarse(): four offsets into a level plane of xc
+  // and their weights, shared by the three levels of a neighbouring column
+  struct Stencil {
+    int c00, c10, c01, c11;
+    T w00, w10, w01, w11;
+  };
+  __device__ __forceinline__ Stencil stencil(int ii, int jj) const {
+    const int I = rx == 2 ? ii >> 1 : ii / rx, J = ry == 2 ? jj >> 1 : jj / ry;
+    const T ox = (T)(2 * (ii - I * rx) + 1 - rx) * hx, oy = (T)(2 * (jj - J * ry) + 1 - ry) * hy;
+    int I2 = ox < (T)0 ? I - 1 : I + 1, J2 = oy < (T)0 ? J - 1 : J + 1;
+    T wx = ox < (T)0 ? -ox : ox, wy = oy < (T)0 ? -oy : oy;
+    if (I2 < 0 || I2 >= Mc) { I2 = I; wx = (T)0; }
+    if (J2 < 0 || J2 >= Nc) { J2 = J; wy = (T)0; }
+    return Stencil{I + Mc * J, I2 + Mc * J, I + Mc * J2, I2 + Mc * J2,
+                   ((T)1 - wx) * ((T)1 - wy), wx * ((T)1 - wy), ((T)1 - wx) * wy, wx * wy};
+  }
+  // x + w P x_c at fine cell ic of level kk, whose column's stencil is st
+  __device__ __forceinline__ T at(const T* __restrict__ x, int ic, const Stencil& st, int kk) const {
+    const T* c = xc + MNc * kk;
+    return x[ic] + w * (st.w00 * c[st.c00] + st.w10 * c[st.c10] + st.w01 * c[st.c01] + st.w11 * c[st.c11]);
   }
 };
+template <class T>
+__host__ __device__ inline Prolong<T> prolong_from(const MGL<T>& F, const MGL<T>& C, T w) {
+  return Prolong<T>{C.x, w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N, C.N, (T)0.5 / (T)F.rx, (T)0.5 / (T)F.ry};
+}
 
 template <class T>
 __device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__ x, const Prolong<T>& P, int ic,
                                           int ii, int jj, int kk) {
+  if (!P.xc) return off_column(L, x, ic, ii, jj, kk);
   const int M = L.M, MN = L.M * L.N, n = L.n;
   const bool im = ii > 0, ip = ii < L.M - 1, jm = jj > 0, jp = jj < L.N - 1, km = kk > 0, kp = kk < L.K - 1;
-  T s = (T)0;
-  if (ip) s += cx_p(L, ic) * P(x, ic + 1);
-  if (im) s += cx_m(L, ic) * P(x, ic - 1);
-  if (jp) s += cy_p(L, ic) * P(x, ic + M);
-  if (jm) s += cy_m(L, ic) * P(x, ic - M);
   const T c4 = L.coef[3 * n + ic], c5 = L.coef[4 * n + ic], c7 = L.coef[5 * n + ic], c8 = L.coef[6 * n + ic];
-  if (kp) {
-    const int u = ic + MN;
-    if (ip) s += c7 * P(x, u + 1);
-    if (im) s += c5 * P(x, u - 1);
-    if (jp) s += c8 * P(x, u + M);
-    if (jm) s += c4 * P(x, u - M);
-  }
-  if (km) {
-    const int d = ic - MN;
-    if (ip) s -= c7 * P(x, d + 1);
-    if (im) s -= c5 * P(x, d - 1);
-    if (jp) s -= c8 * P(x, d + M);
-    if (jm) s -= c4 * P(x, d - M);
-  }
+  T s = (T)0;
+  // each neighbouring column: its in-level coupling, then the cross terms at k+1 and k-1
+  auto column = [&](int off, T c, T cross, int ci, int cj) {
+    const typename Prolong<T>::Stencil st = P.stencil(ci, cj);
+    s += c * P.at(x, ic + off, st, kk);
+    if (kp) s += cross * P.at(x, ic + off + MN, st, kk + 1);
+    if (km) s -= cross * P.at(x, ic + off - MN, st, kk - 1);
+  };
+  if (ip) column(1, cx_p(L, ic), c7, ii + 1, jj);
+  if (im) column(-1, cx_m(L, ic), c5, ii - 1, jj);
+  if (jp) column(M, cy_p(L, ic), c8, ii, jj + 1);
+  if (jm) column(-M, cy_m(L, ic), c4, ii, jj - 1);
   return s;
 }
 
@@ -318,7 +357,7 @@ __global__ void __launch_bounds__(1024) k_mg_cta_cycle(MGSet<T> set, int nl, con
   for (int l = nl - 2; l >= 0; --l) {
     const MGL<T>& F = set.L[l];
     const MGL<T>& C = set.L[l + 1];
-    const Prolong<T> pr{C.x, w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N};
+    const Prolong<T> pr = prolong_from(F, C, w);
     cta_half_sweep(F, 1, 0, pr, sh);
     cta_half_sweep(F, 0, 0, none, sh);
   }
@@ -357,7 +396,7 @@ __global__ void __launch_bounds__(256) k_mg_galerkin(MGL<T> F, T* ccoef, T* ccxr
   decode(ic, Mc, Nc, I, J, k);
   const int K = F.K, n = F.n, MN = F.M * F.N;
   (void)MN;
-  T d = 0, up = 0, dn = 0, xp = 0, yp = 0;
+  T d = 0, up = 0, dn = 0, xp = 0, yp = 0, xm = 0, ym = 0;
   T x7u = 0, x5u = 0, y8u = 0, y4u = 0, x7d = 0, x5d = 0, y8d = 0, y4d = 0;
   for (int b = 0; b < F.ry; ++b) {
     const int j = J * F.ry + b;
@@ -372,9 +411,9 @@ __global__ void __launch_bounds__(256) k_mg_galerkin(MGL<T> F, T* ccoef, T* ccxr
       const T c4 = F.coef[3 * n + f], c5 = F.coef[4 * n + f], c7 = F.coef[5 * n + f], c8 = F.coef[6 * n + f];
       // in-level neighbours
       if (i + 1 < F.M) { const T c = cx_p(F, f); if ((i + 1) / F.rx == I) d += c; else xp += c; }
-      if (i - 1 >= 0) { const T c = cx_m(F, f); if ((i - 1) / F.rx == I) d += c; }
+      if (i - 1 >= 0) { const T c = cx_m(F, f); if ((i - 1) / F.rx == I) d += c; else xm += c; }
       if (j + 1 < F.N) { const T c = cy_p(F, f); if ((j + 1) / F.ry == J) d += c; else yp += c; }
-      if (j - 1 >= 0) { const T c = cy_m(F, f); if ((j - 1) / F.ry == J) d += c; }
+      if (j - 1 >= 0) { const T c = cy_m(F, f); if ((j - 1) / F.ry == J) d += c; else ym += c; }
       // cross terms k+1 (+c) and k-1 (-c)
       if (k < K - 1) {
         if (i + 1 < F.M) { if ((i + 1) / F.rx == I) up += c7; else x7u += c7; }
@@ -390,6 +429,20 @@ __global__ void __launch_bounds__(256) k_mg_galerkin(MGL<T> F, T* ccoef, T* ccxr
       }
     }
   }
+  // Rescaled horizontal couplings.  Across an aggregate boundary the product
+  // sums ry (x faces) or rx (y faces) fine couplings, each ~ h_y dz / h_x, so
+  // the coarse x coupling comes out rx times what the same operator
+  // discretised on the coarse cells has (2 h_y dz / (2 h_x) for 2 x 2); the
+  // vertical couplings and the x-z / y-z cross terms come out at the coarse
+  // discretisation's scale.  Too-strong horizontal couplings halve the
+  // correction of horizontally smooth errors on every level, which a uniform
+  // correction weight cannot undo without over-correcting the vertical.  So
+  // the in-level couplings are scaled by 1/rx and 1/ry, and the removed part
+  // goes to the diagonal: the row sums stay those of the product.
+  const T sx = (T)1 / (T)F.rx, sy = (T)1 / (T)F.ry;
+  d += ((T)1 - sx) * (xp + xm) + ((T)1 - sy) * (yp + ym);
+  xp *= sx;
+  yp *= sy;
   const bool top = (k == K - 1);
   ccoef[ic] = d;
   ccoef[nc + ic] = up;

@@ -122,8 +122,7 @@ __device__ __forceinline__ void ps_reduce(const PsGroup<T>& G, int lb, int& rid,
 template <class T>
 __device__ __forceinline__ T ps_xval(const T* x, const Prolong<T>& P, int ic) {
   if (!P.xc) return x[ic];
-  const int kk = ic / P.MN, r = ic - kk * P.MN, jj = r / P.M, ii = r - jj * P.M;
-  return x[ic] + P.w * P.xc[ii / P.rx + P.Mc * (jj / P.ry) + P.MNc * kk];
+  return x[ic] + P.w * P.coarse(ic);
 }
 
 // off-column part of (A x): everything but C1, C6, C13
@@ -333,7 +332,7 @@ __device__ void ps_cta_cycle(const MGL<T>* Ls, int lo, int hi, T w, int coarse_s
   for (int l = hi - 2; l >= lo; --l) {
     const MGL<T>& F = Ls[l];
     const MGL<T>& C = Ls[l + 1];
-    const Prolong<T> pr{C.x, w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N};
+    const Prolong<T> pr = prolong_from(F, C, w);
     ps_sweep(F, 1, false, PsPlainB<T>{F.b}, pr, sh, 0, 1);
     ps_sweep(F, 0, false, PsPlainB<T>{F.b}, none, sh, 0, 1);
   }
@@ -373,7 +372,7 @@ __device__ void ps_vcycle(const PsGroup<T>& G, const MGL<T>* Ls, In in0, T* sh, 
   for (int l = G.nl - 1; l >= 0; --l) {
     const MGL<T>& F = Ls[l];
     const MGL<T>& C = Ls[l + 1];
-    const Prolong<T> pr{C.x, G.w, F.rx, F.ry, C.M, C.M * C.N, F.M, F.M * F.N};
+    const Prolong<T> pr = prolong_from(F, C, G.w);
     ps_sweep(F, 1, false, PsPlainB<T>{F.b}, pr, sh, lb, G.nb);
     ps_sync(sc, G.bar_nb);
     ps_sweep(F, 0, false, PsPlainB<T>{F.b}, none, sh, lb, G.nb);

@@ -935,7 +935,7 @@ class Solver final : public SolverBase {
     for (int l = lc - 1; l >= 0; --l) {
       const MGL<T>& f = mg[l];
       const MGL<T>& c = mg[l + 1];
-      const Prolong<T> pr{c.x, mg_w, f.rx, f.ry, c.M, c.M * c.N, f.M, f.M * f.N};
+      const Prolong<T> pr = prolong_from(f, c, mg_w);
       smooth(f, 1, 0, l, pr, MgB<T>{f.b});
       smooth(f, 0, 0, l, none, MgB<T>{f.b});
     }
