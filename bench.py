@@ -198,10 +198,12 @@ ALG_BYTES_PER_CELL = {
     "omega_x": lambda s: 3 * s, "omega_y": lambda s: 3 * s,
     # multigrid level 0, per unknown of the level: a half-sweep updates the
     # columns of one colour (half the unknowns), each reading its 7 operator
-    # slots, b and x and writing x; restriction reads operator, x and b of
-    # every fine unknown and writes a quarter as many coarse right-hand sides
+    # slots, b and x and writing x; restriction reads the 4 cross terms of the
+    # colour-0 half and the colour-1 x, and writes b and x of a quarter as many
+    # coarse unknowns; the correction pass reads and writes x of colour 0
     "mg_smooth_l0": lambda s: 5 * s,
-    "mg_restrict_l0": lambda s: 9.25 * s,
+    "mg_restrict_l0": lambda s: 3 * s,
+    "mg_prolong_l0": lambda s: 1 * s,
     "projection": lambda s: 7 * s, "ssp_combine": lambda s: 9 * s, "get_uvw": lambda s: 6 * s,
 }
 

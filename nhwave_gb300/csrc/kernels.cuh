@@ -896,6 +896,18 @@ struct OpLineFactor {
       cpm = c * inv;
       S.lcp[ic] = (T)cpm;
       S.linv[ic] = (T)inv;
+      if (S.sp0) {   // colour-split copy for the level-0 half-sweeps (layout in mg.cuh, MGL::sp)
+        const int ii = i - S.IB, jj = j - S.JB, Mh = (S.M + 1) >> 1;
+        const size_t nmh = (size_t)Mh * S.N, cs = nmh * S.K;
+        T* e = S.sp0 + (size_t)((ii + jj) & 1) * cs + nmh * k + (size_t)Mh * jj + (ii >> 1);
+        e[0] = (T)a;
+        e[2 * cs] = (T)inv;
+        e[4 * cs] = (T)cpm;
+        e[6 * cs] = (T)S.coef64[3 * n + ic];
+        e[8 * cs] = (T)S.coef64[4 * n + ic];
+        e[10 * cs] = (T)S.coef64[5 * n + ic];
+        e[12 * cs] = (T)S.coef64[6 * n + ic];
+      }
     }
   }
 };

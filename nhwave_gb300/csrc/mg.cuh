@@ -34,6 +34,11 @@ struct MGL {
   T* b;
   int rx, ry;           // aggregation to the next coarser level
   int Mc, Nc;
+  // Level 0 only (else nullptr): C13, 1/den, c/den, C4, C5, C7, C8 of the
+  // half-sweeps again, split by colour.  Slot s of colour c starts at
+  // sp + (2 s + c) * K * N * Mh, Mh = (M + 1) / 2, and holds level k, row jj,
+  // column ii of that colour at k * N * Mh + jj * Mh + ii / 2.
+  const T* sp;
 };
 
 template <class T>
@@ -45,17 +50,18 @@ __device__ __forceinline__ T cy_p(const MGL<T>& L, int ic) { return L.cyr ? L.cy
 template <class T>
 __device__ __forceinline__ T cy_m(const MGL<T>& L, int ic) { return L.cyr ? L.cyr[ic - L.M] : L.cyy; }
 
-// off-column part of (A x) at cell (ii, jj, kk): everything but C1, C6, C13
+// off-column part of (A x) at cell (ii, jj, kk): everything but C1, C6, C13;
+// c4, c5, c7, c8 are the cell's cross terms
 template <class T>
-__device__ __forceinline__ T off_column(const MGL<T>& L, const T* __restrict__ x, int ic, int ii, int jj, int kk) {
-  const int M = L.M, MN = L.M * L.N, n = L.n;
+__device__ __forceinline__ T off_column_c(const MGL<T>& L, const T* __restrict__ x, int ic, int ii, int jj, int kk,
+                                          T c4, T c5, T c7, T c8) {
+  const int M = L.M, MN = L.M * L.N;
   const bool im = ii > 0, ip = ii < L.M - 1, jm = jj > 0, jp = jj < L.N - 1, km = kk > 0, kp = kk < L.K - 1;
   T s = (T)0;
   if (ip) s += cx_p(L, ic) * x[ic + 1];
   if (im) s += cx_m(L, ic) * x[ic - 1];
   if (jp) s += cy_p(L, ic) * x[ic + M];
   if (jm) s += cy_m(L, ic) * x[ic - M];
-  const T c4 = L.coef[3 * n + ic], c5 = L.coef[4 * n + ic], c7 = L.coef[5 * n + ic], c8 = L.coef[6 * n + ic];
   if (kp) {
     const int u = ic + MN;
     if (ip) s += c7 * x[u + 1];
@@ -71,6 +77,12 @@ __device__ __forceinline__ T off_column(const MGL<T>& L, const T* __restrict__ x
     if (jm) s -= c4 * x[d - M];
   }
   return s;
+}
+template <class T>
+__device__ __forceinline__ T off_column(const MGL<T>& L, const T* __restrict__ x, int ic, int ii, int jj, int kk) {
+  const int n = L.n;
+  return off_column_c(L, x, ic, ii, jj, kk, L.coef[3 * n + ic], L.coef[4 * n + ic], L.coef[5 * n + ic],
+                      L.coef[6 * n + ic]);
 }
 
 template <class T>
@@ -131,10 +143,14 @@ struct Prolong {
     return Stencil{I + Mc * J, I2 + Mc * J, I + Mc * J2, I2 + Mc * J2,
                    ((T)1 - wx) * ((T)1 - wy), wx * ((T)1 - wy), ((T)1 - wx) * wy, wx * wy};
   }
+  // (P x_c) at level kk of the column whose stencil is st
+  __device__ __forceinline__ T at_coarse(const Stencil& st, int kk) const {
+    const T* c = xc + MNc * kk;
+    return st.w00 * c[st.c00] + st.w10 * c[st.c10] + st.w01 * c[st.c01] + st.w11 * c[st.c11];
+  }
   // x + w P x_c at fine cell ic of level kk, whose column's stencil is st
   __device__ __forceinline__ T at(const T* __restrict__ x, int ic, const Stencil& st, int kk) const {
-    const T* c = xc + MNc * kk;
-    return x[ic] + w * (st.w00 * c[st.c00] + st.w10 * c[st.c10] + st.w01 * c[st.c01] + st.w11 * c[st.c11]);
+    return x[ic] + w * at_coarse(st, kk);
   }
 };
 template <class T>
@@ -143,12 +159,11 @@ __host__ __device__ inline Prolong<T> prolong_from(const MGL<T>& F, const MGL<T>
 }
 
 template <class T>
-__device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__ x, const Prolong<T>& P, int ic,
-                                          int ii, int jj, int kk) {
-  if (!P.xc) return off_column(L, x, ic, ii, jj, kk);
-  const int M = L.M, MN = L.M * L.N, n = L.n;
+__device__ __forceinline__ T off_column_pc(const MGL<T>& L, const T* __restrict__ x, const Prolong<T>& P, int ic,
+                                           int ii, int jj, int kk, T c4, T c5, T c7, T c8) {
+  if (!P.xc) return off_column_c(L, x, ic, ii, jj, kk, c4, c5, c7, c8);
+  const int M = L.M, MN = L.M * L.N;
   const bool im = ii > 0, ip = ii < L.M - 1, jm = jj > 0, jp = jj < L.N - 1, km = kk > 0, kp = kk < L.K - 1;
-  const T c4 = L.coef[3 * n + ic], c5 = L.coef[4 * n + ic], c7 = L.coef[5 * n + ic], c8 = L.coef[6 * n + ic];
   T s = (T)0;
   // each neighbouring column: its in-level coupling, then the cross terms at k+1 and k-1
   auto column = [&](int off, T c, T cross, int ci, int cj) {
@@ -162,6 +177,13 @@ __device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__
   if (jp) column(M, cy_p(L, ic), c8, ii, jj + 1);
   if (jm) column(-M, cy_m(L, ic), c4, ii, jj - 1);
   return s;
+}
+template <class T>
+__device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__ x, const Prolong<T>& P, int ic,
+                                          int ii, int jj, int kk) {
+  const int n = L.n;
+  return off_column_pc(L, x, P, ic, ii, jj, kk, L.coef[3 * n + ic], L.coef[4 * n + ic], L.coef[5 * n + ic],
+                       L.coef[6 * n + ic]);
 }
 
 // Red-black line Gauss-Seidel: a half-sweep solves the columns with
@@ -254,6 +276,85 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
     z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
     L.x[col + MN * k] = z;
   }
+}
+
+// Level-0 half-sweep on the colour-split operator (MGL::sp).  A block holds
+// 32 consecutive columns of the colour in that layout, so its loads of C13,
+// the line factors and the cross terms are contiguous; in the natural layout
+// every other column of a row belongs to the other colour and half of each
+// sector read would be the other colour's.  Otherwise as k_mg_smooth_blk.
+template <class T, bool kProlong, class In>
+__global__ void __launch_bounds__(1024, 2) k_mg_smooth_split(MGL<T> L, const DevScal* sc, int color, int zero_x,
+                                                          Prolong<T> P, In in) {
+  if (sc->conv) return;
+  extern __shared__ unsigned char smem_raw[];
+  T* sh = reinterpret_cast<T*>(smem_raw);
+  const int K = L.K, M = L.M, MN = L.M * L.N;
+  T* s_rhs = sh;
+  T* s_a = sh + K * 32;
+  T* s_inv = sh + 2 * K * 32;
+  T* s_cp = sh + 3 * K * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int Mh = (M + 1) >> 1, nmh = Mh * L.N;
+  const int q = blockIdx.x * 32 + tx;
+  const int jj = q / Mh, r = q - jj * Mh, ii = 2 * r + ((color + jj) & 1);
+  const bool valid = jj < L.N && ii < M;
+  const int col = ii + M * jj;
+  const size_t cs = (size_t)K * nmh;
+  const T* sp = L.sp + (size_t)color * cs + q;
+  for (int k = ty; k < K; k += blockDim.y) {
+    T rhs = (T)0, a = (T)0, inv = (T)0, cp = (T)0;
+    if (valid) {
+      const int ic = col + MN * k;
+      const T* e = sp + (size_t)nmh * k;
+      a = e[0];
+      inv = e[2 * cs];
+      cp = e[4 * cs];
+      T off = (T)0;
+      if (!zero_x) {
+        const T c4 = e[6 * cs], c5 = e[8 * cs], c7 = e[10 * cs], c8 = e[12 * cs];
+        off = kProlong ? off_column_pc(L, L.x, P, ic, ii, jj, k, c4, c5, c7, c8)
+                       : off_column_c(L, L.x, ic, ii, jj, k, c4, c5, c7, c8);
+      }
+      rhs = in(sc, ic, ii, jj, k) - off;
+    }
+    s_rhs[k * 32 + tx] = rhs;
+    s_a[k * 32 + tx] = a;
+    s_inv[k * 32 + tx] = inv;
+    s_cp[k * 32 + tx] = cp;
+  }
+  __syncthreads();
+  if (ty != 0 || !valid) return;
+  T prev = (T)0;
+  for (int k = 0; k < K; ++k) {
+    prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
+    s_rhs[k * 32 + tx] = prev;
+  }
+  T z = prev;
+  L.x[col + MN * (K - 1)] = z;
+  for (int k = K - 2; k >= 0; --k) {
+    z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
+    L.x[col + MN * k] = z;
+  }
+}
+
+// Coarse-grid correction of the colour-0 cells of a level, in place:
+// x += w P x_c, one thread per cell.  The first post-smoothing half-sweep
+// (colour 1) re-solves its own columns from their colour-0 neighbours and the
+// second one re-solves colour 0 from those, so only colour 0 needs the
+// corrected values -- each of which the half-sweep would otherwise
+// interpolate once for every one of the 12 off-column couplings that read it.
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_prolong0(MGL<T> F, Prolong<T> P, const DevScal* sc) {
+  if (sc->conv) return;
+  const int Mh = (F.M + 1) >> 1, nq = Mh * F.N;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nq * F.K) return;
+  const int k = (int)(t / nq), q = (int)(t - (long long)k * nq);
+  const int jj = q / Mh, ii = 2 * (q - jj * Mh) + (jj & 1);
+  if (ii >= F.M) return;
+  const int ic = ii + F.M * (jj + F.N * k);
+  F.x[ic] += P.w * P.at_coarse(P.stencil(ii, jj), k);
 }
 
 // One thread block runs the V-cycle over the small coarse levels lo..nl-1
@@ -363,14 +464,22 @@ __global__ void __launch_bounds__(1024) k_mg_cta_cycle(MGSet<T> set, int nl, con
   }
 }
 
-// b_c = P^T (b_f - A_f x_f), x_c = 0
+// b_c = P^T (b_f - A_f x_f), x_c = 0, right after the pre-smoothing sweep.
+// That sweep starts from x = 0: colour 0 solves T0 x0 = b0 (no neighbours
+// yet), then colour 1 solves its lines exactly against the new colour-0
+// values.  So the residual is zero on colour 1, and on colour 0 it is minus
+// the off-column part of A x, all of whose neighbours are colour 1.  The sum
+// runs over the aggregate's colour-0 cells and reads neither b nor C1, C6, C13
+// (the colour-split copy of the cross terms on level 0).
 template <class T>
-__global__ void __launch_bounds__(256) k_mg_restrict(MGL<T> F, MGL<T> C, const DevScal* sc) {
+__global__ void __launch_bounds__(256) k_mg_restrict_c0(MGL<T> F, MGL<T> C, const DevScal* sc) {
   if (sc->conv) return;
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= C.n) return;
   int I, J, k;
   decode(ic, C.M, C.N, I, J, k);
+  const int n = F.n, Mh = (F.M + 1) >> 1;
+  const size_t nmh = (size_t)Mh * F.N, cs = nmh * F.K;
   T acc = (T)0;
   for (int b = 0; b < F.ry; ++b) {
     const int j = J * F.ry + b;
@@ -378,8 +487,16 @@ __global__ void __launch_bounds__(256) k_mg_restrict(MGL<T> F, MGL<T> C, const D
     for (int a = 0; a < F.rx; ++a) {
       const int i = I * F.rx + a;
       if (i >= F.M) break;
+      if ((i + j) & 1) continue;
       const int f = i + F.M * (j + F.N * k);
-      acc += F.b[f] - level_apply(F, F.x, f, i, j, k);
+      T c4, c5, c7, c8;
+      if (F.sp) {
+        const T* e = F.sp + nmh * k + (size_t)Mh * j + (i >> 1);
+        c4 = e[6 * cs]; c5 = e[8 * cs]; c7 = e[10 * cs]; c8 = e[12 * cs];
+      } else {
+        c4 = F.coef[3 * n + f]; c5 = F.coef[4 * n + f]; c7 = F.coef[5 * n + f]; c8 = F.coef[6 * n + f];
+      }
+      acc -= off_column_c(F, F.x, f, i, j, k, c4, c5, c7, c8);
     }
   }
   C.b[ic] = acc;

@@ -129,6 +129,7 @@ struct Dev {
   // Krylov working vectors in the inner precision T (compact interior order)
   T* coefT;           // [7][neq] (aliases coef64 when T == double)
   T *lcp, *linv;      // line preconditioner factors [neq]
+  T* sp0;             // colour-split copy of the level-0 smoother's operator (MGL::sp), or nullptr
   T *kx, *kr, *kr0, *kp, *kph, *kv, *ks, *ksh, *kt;
   double* partials;   // reduction partials [nblocks * 8]
   DevScal* sc;
