@@ -34,6 +34,20 @@ __device__ __forceinline__ R lim_slope(R am, R a0, R ap, R dm, R dp) {
   R t2 = (a0 - am) / dm;
   return (fabs(t1) + fabs(t2)) < (R)kSmall ? (R)0 : limiter(t1, t2);
 }
+// the same with the reciprocals of the spacings (FP32 form: products for divisions)
+template <class R>
+__device__ __forceinline__ R lim_slope_r(R am, R a0, R ap, R rdm, R rdp) {
+  R t1 = (ap - a0) * rdp;
+  R t2 = (a0 - am) * rdm;
+  return (fabs(t1) + fabs(t2)) < (R)kSmall ? (R)0 : limiter(t1, t2);
+}
+// lim_slope over a uniform spacing d (1/d = rd): FP64 divides as the reference
+// does, FP32 multiplies by the reciprocal
+template <class R>
+__device__ __forceinline__ R lim_slope_u(R am, R a0, R ap, R d, R rd) {
+  if constexpr (sizeof(R) == 4) return lim_slope_r<R>(am, a0, ap, rd, rd);
+  else return lim_slope<R>(am, a0, ap, d, d);
+}
 // 0.5*Grav*(eta*eta + 2*eta*h0): hydrostatic part of the momentum flux
 template <class R>
 __device__ __forceinline__ R hydro(R eta, R h0) {
@@ -242,14 +256,17 @@ struct OpSlopeEta {
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const double* E = S.Eta;
     const long long c = i2(S, i, j);
+    const double rdx = 2.0 * S.i2dx, rdy = 2.0 * S.i2dy;   // 1/dx, 1/dy (FP32 form: products)
     double sx, sy;
     if (i == 0) sx = (E[c + 1] - E[c]) / S.dx;
     else if (i == S.Mloc - 1) sx = (E[c] - E[c - 1]) / S.dx;
     else if (S.Mask[c] == 0) sx = 0.0;
+    else if constexpr (sizeof(T) == 4) sx = lim_slope_r<double>(E[c - 1], E[c], E[c + 1], rdx, rdx);
     else sx = lim_slope<double>(E[c - 1], E[c], E[c + 1], S.dx, S.dx);
     if (j == 0) sy = (E[c + S.sy] - E[c]) / S.dy;
     else if (j == S.Nloc - 1) sy = (E[c] - E[c - S.sy]) / S.dy;
     else if (S.Mask[c] == 0) sy = 0.0;
+    else if constexpr (sizeof(T) == 4) sy = lim_slope_r<double>(E[c - S.sy], E[c], E[c + S.sy], rdy, rdy);
     else sy = lim_slope<double>(E[c - S.sy], E[c], E[c + S.sy], S.dy, S.dy);
     S.DelxEta[c] = sx;
     S.DelyEta[c] = sy;
@@ -306,10 +323,10 @@ struct OpFluxX {
     const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
     const long long q0 = i2(S, c0, j), q1 = q0 + 1;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx;
+    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx, irdx = (R)(1.0 / S.dx);
     // limited x slopes of the two cells (zero in dry cells)
     auto sl = [&](const T* A, long long e, int m) -> R {
-      return m == 0 ? (R)0 : lim_slope<R>(A[e - 1], A[e], A[e + 1], rdx, rdx);
+      return m == 0 ? (R)0 : lim_slope_u<R>(A[e - 1], A[e], A[e + 1], rdx, irdx);
     };
     R uL = S.U[e0] + hdx * sl(S.U, e0, mL), uR = S.U[e1] - hdx * sl(S.U, e1, mR);
     R vL = S.V[e0] + hdx * sl(S.V, e0, mL), vR = S.V[e1] - hdx * sl(S.V, e1, mR);
@@ -427,9 +444,9 @@ struct OpFluxY {
     const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
     const long long q0 = i2(S, i, c0), q1 = q0 + sy;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy;
+    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy, irdy = (R)(1.0 / S.dy);
     auto sl = [&](const T* A, long long e, int m) -> R {
-      return m == 0 ? (R)0 : lim_slope<R>(A[e - sy], A[e], A[e + sy], rdy, rdy);
+      return m == 0 ? (R)0 : lim_slope_u<R>(A[e - sy], A[e], A[e + sy], rdy, irdy);
     };
     R uL = S.U[e0] + hdy * sl(S.U, e0, mL), uR = S.U[e1] - hdy * sl(S.U, e1, mR);
     R vL = S.V[e0] + hdy * sl(S.V, e0, mL), vR = S.V[e1] - hdy * sl(S.V, e1, mR);
@@ -529,9 +546,10 @@ struct OpFluxZ {
     const long long o = i3(S, i, j, k);
     if (k == S.KB || k == S.KE + 1) { S.Fz[o] = (R)0; S.Gz[o] = (R)0; S.Hz[o] = (R)0; return; }
     const long long sz = S.sz;
-    const R dm = (R)(S.sigc[k - 1] - S.sigc[k - 2]), d0 = (R)(S.sigc[k] - S.sigc[k - 1]),
-            dp = (R)(S.sigc[k + 1] - S.sigc[k]);
-    const R hm = (R)(0.5 * S.dsig[k - 1]), h0 = (R)(0.5 * S.dsig[k]);
+    const T* dsc = S.lvT + S.Kloc;       // sigc_k - sigc_k-1
+    const T* hds = S.lvT + 2 * S.Kloc;   // dsig_k / 2
+    const R dm = dsc[k - 1], d0 = dsc[k], dp = dsc[k + 1];
+    const R hm = hds[k - 1], h0 = hds[k];
     auto face = [&](const T* A, R& L, R& Rr) {
       const R am = A[o - 2 * sz], a0 = A[o - sz], a1 = A[o], a2 = A[o + sz];
       L = a0 + hm * lim_slope<R>(am, a0, a1, dm, d0);
@@ -571,7 +589,7 @@ struct OpExplicit {
       const R sx = (R)S.SourceX[c], syy = (R)S.SourceY[c];
       for (int k = S.KB; k <= S.KE; ++k) {
         const long long o = i3(S, i, j, k);
-        const R rds = (R)(1.0 / S.dsig[k]);
+        const R rds = S.lvT[k];   // (R)(1.0 / dsig_k)
         const R du = S.DU[o], dv = S.DV[o], dw = S.DW[o];
         const R R2 = -rdx * (S.Fx[o + 1] - S.Fx[o]) - rdy * (S.Fy[o + S.sy] - S.Fy[o]) -
                      rds * (S.Fz[o + S.sz] - S.Fz[o]) + fc * dv + sx;
@@ -1005,9 +1023,9 @@ struct OpOmegaX {
     const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
     const long long q0 = i2(S, c0, j), q1 = q0 + 1;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx;
+    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx, irdx = (R)(1.0 / S.dx);
     auto sl = [&](const T* A, long long e, int m) -> R {
-      return m == 0 ? (R)0 : lim_slope<R>(A[e - 1], A[e], A[e + 1], rdx, rdx);
+      return m == 0 ? (R)0 : lim_slope_u<R>(A[e - 1], A[e], A[e + 1], rdx, irdx);
     };
     const R uL = S.U[e0] + hdx * sl(S.U, e0, mL), uR = S.U[e1] - hdx * sl(S.U, e1, mR);
     R duL = S.DU[e0] + hdx * sl(S.DU, e0, mL), duR = S.DU[e1] - hdx * sl(S.DU, e1, mR);
@@ -1057,9 +1075,9 @@ struct OpOmegaY {
     const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
     const long long q0 = i2(S, i, c0), q1 = q0 + sy;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy;
+    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy, irdy = (R)(1.0 / S.dy);
     auto sl = [&](const T* A, long long e, int m) -> R {
-      return m == 0 ? (R)0 : lim_slope<R>(A[e - sy], A[e], A[e + sy], rdy, rdy);
+      return m == 0 ? (R)0 : lim_slope_u<R>(A[e - sy], A[e], A[e + sy], rdy, irdy);
     };
     const R vL = S.V[e0] + hdy * sl(S.V, e0, mL), vR = S.V[e1] - hdy * sl(S.V, e1, mR);
     R dvL = S.DV[e0] + hdy * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdy * sl(S.DV, e1, mR);
@@ -1106,13 +1124,16 @@ struct OpOmegaScan {
     const long long q = i2(S, i, j);
     const bool wet = S.Mask[q] != 0;
     const double r1 = S.R1[q];
+    const double rdx = 2.0 * S.i2dx, rdy = 2.0 * S.i2dy;   // 1/dx, 1/dy
     double om = 0.0;
     S.Omega[i3(S, i, j, S.KB)] = (T)0;
     for (int k = S.KB + 1; k <= S.KE + 1; ++k) {
       const long long o = i3(S, i, j, k - 1);
       const double dEx = (double)S.Ex[o + 1] - (double)S.Ex[o];
       const double dEy = (double)S.Ey[o + S.sy] - (double)S.Ey[o];
-      double v = om - S.dsig[k - 1] * (r1 + dEx / S.dx + dEy / S.dy);
+      double v;
+      if constexpr (sizeof(T) == 4) v = om - S.dsig[k - 1] * (r1 + dEx * rdx + dEy * rdy);   // FP32 form: products
+      else v = om - S.dsig[k - 1] * (r1 + dEx / S.dx + dEy / S.dy);
       if (!wet) v = 0.0;
       S.Omega[i3(S, i, j, k)] = (T)v;
       om = (double)(T)v;
@@ -1134,6 +1155,18 @@ struct OpSponge {
     S.Eta[c] = S.Eta[c] * sp;
     S.D[c] = S.Eta[c] + S.Hc[c];
     const double d = S.D[c];
+    if constexpr (sizeof(T) == 4) {   // FP32 form: the 3-D part in FP32
+      const T rsp = (T)sp, ruc = (T)Ucur, rd = (T)d;
+      for (int k = 0; k < S.Kloc; ++k) {
+        const long long o = i3(S, i, j, k);
+        const T u = (S.U[o] - ruc) * rsp + ruc, v = S.V[o] * rsp;
+        S.U[o] = u;
+        S.V[o] = v;
+        S.DU[o] = rd * u;
+        S.DV[o] = rd * v;
+      }
+      return;
+    }
     for (int k = 0; k < S.Kloc; ++k) {
       const long long o = i3(S, i, j, k);
       const double u = ((double)S.U[o] - Ucur) * sp + Ucur;

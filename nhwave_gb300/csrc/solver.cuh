@@ -246,6 +246,7 @@ class Solver final : public SolverBase {
     add(&S.yc, sizeof(double) * S.Nloc);
     for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds, &S.lv_fint})
       add((double**)lv, sizeof(double) * S.Kloc);
+    add((T**)&S.lvT, sizeof(T) * 3 * S.Kloc);
     double** d2[] = {&S.D, &S.D0, &S.Eta, &S.Eta0, &S.Hc, &S.Hc0, &S.Ho, &S.Hfx, &S.Hfy, &S.Hfx0, &S.Hfy0,
                      &S.DelxH, &S.DelyH, &S.DeltH, &S.DeltHo, &S.Delt2H, &S.DelxEta, &S.DelyEta, &S.SourceX,
                      &S.SourceY, &S.SourceC, &S.Sponge, &S.R1, &S.Wsx, &S.Wsy, &S.EtaxL, &S.EtaxR, &S.EtayL,
@@ -637,6 +638,13 @@ class Solver final : public SolverBase {
       const double* dst[] = {S.lv_x, S.lv_y, S.lv_up, S.lv_dn, S.lv_h, S.lv_ds, S.lv_fint};
       for (int q = 0; q < 7; ++q)
         NHW_CU(cudaMemcpyAsync((void*)dst[q], src[q]->data(), sizeof(double) * S.Kloc, cudaMemcpyHostToDevice, st));
+      std::vector<T> lt(3 * (size_t)S.Kloc, (T)0);
+      for (int k = 0; k < S.Kloc; ++k) {
+        lt[k] = (T)(1.0 / h.dsig[k]);
+        if (k > 0) lt[S.Kloc + k] = (T)(h.sigc[k] - h.sigc[k - 1]);
+        lt[2 * S.Kloc + k] = (T)(0.5 * h.dsig[k]);
+      }
+      NHW_CU(cudaMemcpyAsync((void*)S.lvT, lt.data(), sizeof(T) * lt.size(), cudaMemcpyHostToDevice, st));
       NHW_CU(cudaStreamSynchronize(st));
     }
     struct Up { int f; const void* src; } ups[] = {

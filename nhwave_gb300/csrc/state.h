@@ -115,6 +115,10 @@ struct Dev {
   // 1/h_k with h_k = (dsig_k+dsig_k-1)/2, 1/dsig_k
   const double *lv_x, *lv_y, *lv_up, *lv_dn, *lv_h, *lv_ds;
   const double* lv_fint;   // dsig_k / (dsig_k + dsig_k-1): weight of level k-1 at face k
+  // per sigma level k in the storage type T, [3][Kloc]: 1/dsig_k, sigc_k - sigc_k-1,
+  // dsig_k / 2 -- each formed in FP64 on the host and rounded once, as the
+  // kernels formed them per cell before
+  const T* lvT;
   double i2dx, i2dy;       // 0.5/dx, 0.5/dy
   int *Mask, *MaskT, *Mask_Struct, *Mask9;
   // 3-D fields (storage type T); P is FP64 in both forms
