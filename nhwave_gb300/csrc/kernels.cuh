@@ -248,6 +248,106 @@ struct OpWaveBC {
 };
 
 // =========================================================================
+//   2-D face states shared by flux_x/y and omega_x/y
+// =========================================================================
+// State of the face between cells q0 and q1 = q0 + step (x faces: step 1, y
+// faces: sy): eta and D reconstructed from the eta slopes (hd = dx/2 or dy/2),
+// the face bed height h0 (Hfx0 / Hfy0), with the wet/dry front fix of
+// src/nhwave.F:1745-1788.  inL / inR: cell q0 / q1 is an interior cell of its
+// row (x) or column (y).
+struct Face2D {
+  double etaL, etaR, dL, dR, h0;
+  bool wrote_h0;   // the fix replaced h0 by a cell's Hc
+  bool zl, zr;     // the fix zeroes the 3-D states on the left / right side
+};
+template <class T>
+__device__ __forceinline__ void face_flags(const Dev<T>& S, long long q0, long long step, bool inL, bool inR,
+                                           bool& zl, bool& zr) {
+  const long long q1 = q0 + step;
+  const int mL = S.Mask[q0], mR = S.Mask[q1];
+  zl = inL && ((mL == 1 && mR == 0) || mL == 0);
+  zr = false;
+  if (inR) {
+    const int mRR = S.Mask[q1 + step];
+    zr = !(mR == 1 && mRR == 0) && ((mR == 1 && mL == 0) || mR == 0);
+  }
+}
+template <class T>
+__device__ __forceinline__ Face2D face_2d(const Dev<T>& S, long long q0, long long step, bool inL, bool inR,
+                                          double hd, const double* Delt, const double* Hf, const double* Hf0) {
+  const long long q1 = q0 + step;
+  const int mL = S.Mask[q0], mR = S.Mask[q1];
+  Face2D F;
+  F.etaL = S.Eta[q0] + hd * Delt[q0];
+  F.etaR = S.Eta[q1] - hd * Delt[q1];
+  const double hf = Hf[q1];
+  F.dL = dmax_(F.etaL + hf, S.min_dep);
+  F.dR = dmax_(F.etaR + hf, S.min_dep);
+  F.h0 = Hf0[q1];
+  F.wrote_h0 = F.zl = F.zr = false;
+  if (inL) {
+    if (mL == 1 && mR == 0) {
+      F.etaL = S.Eta[q0]; F.dL = S.D[q0]; F.h0 = S.Hc[q0]; F.wrote_h0 = true; F.zl = true;
+    } else if (mL == 0) {
+      F.etaL = S.Eta[q0]; F.dL = S.D[q0]; F.zl = true;
+    }
+  }
+  if (inR) {
+    const int mRR = S.Mask[q1 + step];
+    if (mR == 1 && mRR == 0) {
+    } else if (mR == 1 && mL == 0) {
+      F.etaR = S.Eta[q1]; F.dR = S.D[q1]; F.h0 = S.Hc[q1]; F.wrote_h0 = true; F.zr = true;
+    } else if (mR == 0) {
+      F.etaR = S.Eta[q1]; F.dR = S.D[q1]; F.zr = true;
+    }
+  }
+  return F;
+}
+// The FP32+IR form with HLL reads the 2-D face states from Dev::fxT / fyT,
+// formed once per face by OpFacePrep, instead of forming them in FP64 on
+// every level of the face (the FP64 pipe runs at 1/58 of the FP32 rate).
+template <class R, class T>
+__device__ __forceinline__ bool face_table(const Dev<T>& S) {
+  if constexpr (sizeof(R) == 4) return S.fxT != nullptr && !S.hllc;
+  else return false;
+}
+// table slots: eta, D on each side and h0 rounded to T, then (T)(dR - dL)
+struct FaceT {
+  template <class T>
+  __device__ __forceinline__ static void put(T* tab, long long q1, long long n2, const Face2D& F) {
+    tab[q1] = (T)F.etaL; tab[n2 + q1] = (T)F.etaR; tab[2 * n2 + q1] = (T)F.dL; tab[3 * n2 + q1] = (T)F.dR;
+    tab[4 * n2 + q1] = (T)F.h0; tab[5 * n2 + q1] = (T)(F.dR - F.dL);
+  }
+};
+// one x face (f, j) and one y face (i, g) per thread over (M+1) x (N+1): the
+// face states at the start of a stage (flux; writes Hfx0/Hfy0 where the fix
+// replaced h0) or after it (omega; writes EtaxL/R, EtayL/R for source_terms)
+struct OpFacePrep {
+  static constexpr const char* kName = "face_prep";
+  int omega;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int) const {
+    const long long n2 = (long long)S.Mloc * S.Nloc;
+    if (j <= S.JE) {   // x face f = i between cells i-1 and i
+      const long long q0 = i2(S, i - 1, j);
+      const Face2D F = face_2d(S, q0, 1, i - 1 >= S.IB && i - 1 <= S.IE, i >= S.IB && i <= S.IE, 0.5 * S.dx,
+                               S.DelxEta, S.Hfx, S.Hfx0);
+      if (omega) { S.EtaxL[q0 + 1] = F.etaL; S.EtaxR[q0 + 1] = F.etaR; }
+      else if (F.wrote_h0) S.Hfx0[q0 + 1] = F.h0;
+      FaceT::put(S.fxT, q0 + 1, n2, F);
+    }
+    if (i <= S.IE) {   // y face g = j between cells j-1 and j
+      const long long q0 = i2(S, i, j - 1);
+      const Face2D F = face_2d(S, q0, S.sy, j - 1 >= S.JB && j - 1 <= S.JE, j >= S.JB && j <= S.JE, 0.5 * S.dy,
+                               S.DelyEta, S.Hfy, S.Hfy0);
+      if (omega) { S.EtayL[q0 + S.sy] = F.etaL; S.EtayR[q0 + S.sy] = F.etaR; }
+      else if (F.wrote_h0) S.Hfy0[q0 + S.sy] = F.h0;
+      FaceT::put(S.fyT, q0 + S.sy, n2, F);
+    }
+  }
+};
+
+// =========================================================================
 //                        2-D slopes of eta (delx/yFun_2D)
 // =========================================================================
 struct OpSlopeEta {
@@ -323,7 +423,7 @@ struct OpFluxX {
     const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
     const long long q0 = i2(S, c0, j), q1 = q0 + 1;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx, irdx = (R)(1.0 / S.dx);
+    const R hdx = S.hdxT, rdx = S.dxT, irdx = S.idxT;
     // limited x slopes of the two cells (zero in dry cells)
     auto sl = [&](const T* A, long long e, int m) -> R {
       return m == 0 ? (R)0 : lim_slope_u<R>(A[e - 1], A[e], A[e + 1], rdx, irdx);
@@ -334,36 +434,25 @@ struct OpFluxX {
     R duL = S.DU[e0] + hdx * sl(S.DU, e0, mL), duR = S.DU[e1] - hdx * sl(S.DU, e1, mR);
     R dvL = S.DV[e0] + hdx * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdx * sl(S.DV, e1, mR);
     R dwL = S.DW[e0] + hdx * sl(S.DW, e0, mL), dwR = S.DW[e1] - hdx * sl(S.DW, e1, mR);
-    double etaL = S.Eta[q0] + 0.5 * S.dx * S.DelxEta[q0];
-    double etaR = S.Eta[q1] - 0.5 * S.dx * S.DelxEta[q1];
-    const double hf = S.Hfx[q1];
-    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
-    double h0 = S.Hfx0[q1];
-    bool wrote_h0 = false;
-    // wet/dry front fix (src/nhwave.F:1745-1788)
-    if (c0 >= S.IB && c0 <= S.IE) {
-      if (mL == 1 && mR == 0) {
-        etaL = S.Eta[q0]; dL = S.D[q0]; h0 = S.Hc[q0]; wrote_h0 = true;
-        uL = vL = wL = duL = dvL = dwL = (R)0;
-      } else if (mL == 0) {
-        etaL = S.Eta[q0]; dL = S.D[q0];
-        uL = vL = wL = duL = dvL = dwL = (R)0;
-      }
+    // 2-D face state with the wet/dry front fix (src/nhwave.F:1745-1788)
+    R reL, reR, rh0, rdL, rdR, rdd;
+    double dL = 0.0, dR = 0.0, h0;   // FP64 face depths (HLLC) and bed height
+    bool zl, zr;
+    const bool inL = c0 >= S.IB && c0 <= S.IE, inR = c1 >= S.IB && c1 <= S.IE;
+    if (face_table<R>(S)) {
+      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const T* ft = S.fxT + q1;
+      reL = ft[0]; reR = ft[n2]; rdL = ft[2 * n2]; rdR = ft[3 * n2]; rh0 = ft[4 * n2]; rdd = ft[5 * n2];
+      h0 = (double)rh0;
+      face_flags(S, q0, 1, inL, inR, zl, zr);
+    } else {
+      const Face2D F = face_2d(S, q0, 1, inL, inR, 0.5 * S.dx, S.DelxEta, S.Hfx, S.Hfx0);
+      if (F.wrote_h0 && k == S.KB) S.Hfx0[q1] = F.h0;
+      dL = F.dL; dR = F.dR; h0 = F.h0; zl = F.zl; zr = F.zr;
+      reL = (R)F.etaL; reR = (R)F.etaR; rh0 = (R)F.h0; rdL = (R)F.dL; rdR = (R)F.dR; rdd = (R)(F.dR - F.dL);
     }
-    if (c1 >= S.IB && c1 <= S.IE) {
-      const int mRR = S.Mask[q1 + 1];
-      if (mR == 1 && mRR == 0) {
-        // case 1 of cell c1 concerns face c1+1
-      } else if (mR == 1 && mL == 0) {
-        etaR = S.Eta[q1]; dR = S.D[q1]; h0 = S.Hc[q1]; wrote_h0 = true;
-        uR = vR = wR = duR = dvR = dwR = (R)0;
-      } else if (mR == 0) {
-        etaR = S.Eta[q1]; dR = S.D[q1];
-        uR = vR = wR = duR = dvR = dwR = (R)0;
-      }
-    }
-    if (wrote_h0 && k == S.KB) S.Hfx0[q1] = h0;
-    const R reL = (R)etaL, reR = (R)etaR, rh0 = (R)h0, rdL = (R)dL, rdR = (R)dR;
+    if (zl) uL = vL = wL = duL = dvL = dwL = (R)0;
+    if (zr) uR = vR = wR = duR = dvR = dwR = (R)0;
     // physical fluxes at the faces
     const R FxL = duL * uL + hydro<R>(reL, rh0), FxR = duR * uR + hydro<R>(reR, rh0);
     const R GxL = rdL * uL * vL, GxR = rdR * uR * vR;
@@ -402,7 +491,7 @@ struct OpFluxX {
       Gx = hllc<R>(SL, SR, SS, GxL, GxR, dvL, lsR * vL, dvR, rsR * vR);
       Hx = hllc<R>(SL, SR, SS, HxL, HxR, dwL, lsR * wL, dwR, rsR * wR);
     } else {
-      Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
+      Ex = hll_d<R>(SL, SR, duL, duR, rdd);
       Fx = hll<R>(SL, SR, FxL, FxR, duL, duR);
       Gx = hll<R>(SL, SR, GxL, GxR, dvL, dvR);
       Hx = hll<R>(SL, SR, HxL, HxR, dwL, dwR);
@@ -444,7 +533,7 @@ struct OpFluxY {
     const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
     const long long q0 = i2(S, i, c0), q1 = q0 + sy;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy, irdy = (R)(1.0 / S.dy);
+    const R hdy = S.hdyT, rdy = S.dyT, irdy = S.idyT;
     auto sl = [&](const T* A, long long e, int m) -> R {
       return m == 0 ? (R)0 : lim_slope_u<R>(A[e - sy], A[e], A[e + sy], rdy, irdy);
     };
@@ -454,34 +543,23 @@ struct OpFluxY {
     R duL = S.DU[e0] + hdy * sl(S.DU, e0, mL), duR = S.DU[e1] - hdy * sl(S.DU, e1, mR);
     R dvL = S.DV[e0] + hdy * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdy * sl(S.DV, e1, mR);
     R dwL = S.DW[e0] + hdy * sl(S.DW, e0, mL), dwR = S.DW[e1] - hdy * sl(S.DW, e1, mR);
-    double etaL = S.Eta[q0] + 0.5 * S.dy * S.DelyEta[q0];
-    double etaR = S.Eta[q1] - 0.5 * S.dy * S.DelyEta[q1];
-    const double hf = S.Hfy[q1];
-    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
-    double h0 = S.Hfy0[q1];
-    bool wrote_h0 = false;
-    if (c0 >= S.JB && c0 <= S.JE) {
-      if (mL == 1 && mR == 0) {
-        etaL = S.Eta[q0]; dL = S.D[q0]; h0 = S.Hc[q0]; wrote_h0 = true;
-        uL = vL = wL = duL = dvL = dwL = (R)0;
-      } else if (mL == 0) {
-        etaL = S.Eta[q0]; dL = S.D[q0];
-        uL = vL = wL = duL = dvL = dwL = (R)0;
-      }
+    R reL, reR, rh0, rdL, rdR, rdd;
+    double dL = 0.0, dR = 0.0;   // FP64 face depths (HLLC)
+    bool zl, zr;
+    const bool inL = c0 >= S.JB && c0 <= S.JE, inR = c1 >= S.JB && c1 <= S.JE;
+    if (face_table<R>(S)) {
+      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const T* ft = S.fyT + q1;
+      reL = ft[0]; reR = ft[n2]; rdL = ft[2 * n2]; rdR = ft[3 * n2]; rh0 = ft[4 * n2]; rdd = ft[5 * n2];
+      face_flags(S, q0, sy, inL, inR, zl, zr);
+    } else {
+      const Face2D F = face_2d(S, q0, sy, inL, inR, 0.5 * S.dy, S.DelyEta, S.Hfy, S.Hfy0);
+      if (F.wrote_h0 && k == S.KB) S.Hfy0[q1] = F.h0;
+      dL = F.dL; dR = F.dR; zl = F.zl; zr = F.zr;
+      reL = (R)F.etaL; reR = (R)F.etaR; rh0 = (R)F.h0; rdL = (R)F.dL; rdR = (R)F.dR; rdd = (R)(F.dR - F.dL);
     }
-    if (c1 >= S.JB && c1 <= S.JE) {
-      const int mRR = S.Mask[q1 + sy];
-      if (mR == 1 && mRR == 0) {
-      } else if (mR == 1 && mL == 0) {
-        etaR = S.Eta[q1]; dR = S.D[q1]; h0 = S.Hc[q1]; wrote_h0 = true;
-        uR = vR = wR = duR = dvR = dwR = (R)0;
-      } else if (mR == 0) {
-        etaR = S.Eta[q1]; dR = S.D[q1];
-        uR = vR = wR = duR = dvR = dwR = (R)0;
-      }
-    }
-    if (wrote_h0 && k == S.KB) S.Hfy0[q1] = h0;
-    const R reL = (R)etaL, reR = (R)etaR, rh0 = (R)h0, rdL = (R)dL, rdR = (R)dR;
+    if (zl) uL = vL = wL = duL = dvL = dwL = (R)0;
+    if (zr) uR = vR = wR = duR = dvR = dwR = (R)0;
     const R FyL = rdL * uL * vL, FyR = rdR * uR * vR;
     const R GyL = dvL * vL + hydro<R>(reL, rh0), GyR = dvR * vR + hydro<R>(reR, rh0);
     const R HyL = rdL * vL * wL, HyR = rdR * vR * wR;
@@ -518,7 +596,7 @@ struct OpFluxY {
       Gy = hllc<R>(SL, SR, SS, GyL, GyR, dvL, lsR * SS, dvR, rsR * SS);
       Hy = hllc<R>(SL, SR, SS, HyL, HyR, dwL, lsR * wL, dwR, rsR * wR);
     } else {
-      Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
+      Ey = hll_d<R>(SL, SR, dvL, dvR, rdd);
       Fy = hll<R>(SL, SR, FyL, FyR, duL, duR);
       Gy = hll<R>(SL, SR, GyL, GyR, dvL, dvR);
       Hy = hll<R>(SL, SR, HyL, HyR, dwL, dwR);
@@ -585,7 +663,7 @@ struct OpExplicit {
       }
       r1 = r1 + S.D[c] * S.SourceC[c];
       S.D[c] = S.alpha[istep] * S.D0[c] + S.beta[istep] * (S.D[c] + dt * r1);
-      const R rdx = (R)(1.0 / S.dx), rdy = (R)(1.0 / S.dy), rdt = (R)dt, fc = (R)S.fcor;
+      const R rdx = S.idxT, rdy = S.idyT, rdt = (R)dt, fc = (R)S.fcor;
       const R sx = (R)S.SourceX[c], syy = (R)S.SourceY[c];
       for (int k = S.KB; k <= S.KE; ++k) {
         const long long o = i3(S, i, j, k);
@@ -723,10 +801,10 @@ struct OpVelBcB {
     // arithmetic of the surface stress ghosts: FP64 in the FP64 form, FP32 in FP32+IR
     using R = typename std::conditional<sizeof(T) == 4, float, double>::type;
     auto dx_ = [&](const double* a) -> R {
-      return wet ? lim_slope<R>((R)zl(a, i - 1, j), (R)a[c], (R)zl(a, i + 1, j), (R)S.dx, (R)S.dx) : (R)0;
+      return wet ? lim_slope<R>((R)zl(a, i - 1, j), (R)a[c], (R)zl(a, i + 1, j), S.dxT, S.dxT) : (R)0;
     };
     auto dy_ = [&](const double* a) -> R {
-      return wet ? lim_slope<R>((R)zl(a, i, j - 1), (R)a[c], (R)zl(a, i, j + 1), (R)S.dy, (R)S.dy) : (R)0;
+      return wet ? lim_slope<R>((R)zl(a, i, j - 1), (R)a[c], (R)zl(a, i, j + 1), S.dyT, S.dyT) : (R)0;
     };
     const R DelxUzL = dx_(S.zUL), DelxVzL = dx_(S.zVL), DelxWzL = dx_(S.zWL);
     const R DelyUzL = dy_(S.zUL), DelyVzL = dy_(S.zVL), DelyWzL = dy_(S.zWL);
@@ -1023,26 +1101,27 @@ struct OpOmegaX {
     const long long e0 = i3(S, c0, j, k), e1 = e0 + 1;
     const long long q0 = i2(S, c0, j), q1 = q0 + 1;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdx = (R)(0.5 * S.dx), rdx = (R)S.dx, irdx = (R)(1.0 / S.dx);
+    const R hdx = S.hdxT, rdx = S.dxT, irdx = S.idxT;
     auto sl = [&](const T* A, long long e, int m) -> R {
       return m == 0 ? (R)0 : lim_slope_u<R>(A[e - 1], A[e], A[e + 1], rdx, irdx);
     };
     const R uL = S.U[e0] + hdx * sl(S.U, e0, mL), uR = S.U[e1] - hdx * sl(S.U, e1, mR);
     R duL = S.DU[e0] + hdx * sl(S.DU, e0, mL), duR = S.DU[e1] - hdx * sl(S.DU, e1, mR);
-    double etaL = S.Eta[q0] + 0.5 * S.dx * S.DelxEta[q0];
-    double etaR = S.Eta[q1] - 0.5 * S.dx * S.DelxEta[q1];
-    const double hf = S.Hfx[q1];
-    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
-    if (c0 >= S.IB && c0 <= S.IE) {
-      if ((mL == 1 && mR == 0) || mL == 0) { etaL = S.Eta[q0]; dL = S.D[q0]; duL = (R)0; }
+    R rdL, rdR, rdd;
+    bool zl, zr;
+    const bool inL = c0 >= S.IB && c0 <= S.IE, inR = c1 >= S.IB && c1 <= S.IE;
+    if (face_table<R>(S)) {
+      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const T* ft = S.fxT + q1;
+      rdL = ft[2 * n2]; rdR = ft[3 * n2]; rdd = ft[5 * n2];
+      face_flags(S, q0, 1, inL, inR, zl, zr);
+    } else {
+      const Face2D F = face_2d(S, q0, 1, inL, inR, 0.5 * S.dx, S.DelxEta, S.Hfx, S.Hfx0);
+      if (k == S.KB) { S.EtaxL[q1] = F.etaL; S.EtaxR[q1] = F.etaR; }
+      rdL = (R)F.dL; rdR = (R)F.dR; rdd = (R)(F.dR - F.dL); zl = F.zl; zr = F.zr;
     }
-    if (c1 >= S.IB && c1 <= S.IE) {
-      const int mRR = S.Mask[q1 + 1];
-      if (mR == 1 && mRR == 0) {
-      } else if ((mR == 1 && mL == 0) || mR == 0) { etaR = S.Eta[q1]; dR = S.D[q1]; duR = (R)0; }
-    }
-    if (k == S.KB) { S.EtaxL[q1] = etaL; S.EtaxR[q1] = etaR; }
-    const R rdL = (R)dL, rdR = (R)dR;
+    if (zl) duL = (R)0;
+    if (zr) duR = (R)0;
     R SL = (R)0, SR = (R)0;
     if (mL == 1 && mR == 1) {
       R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
@@ -1059,7 +1138,7 @@ struct OpOmegaX {
       SL = uL - pL;
       SR = uL + (R)2.0 * pL;
     }
-    R Ex = hll_d<R>(SL, SR, duL, duR, (R)(dR - dL));
+    R Ex = hll_d<R>(SL, SR, duL, duR, rdd);
     if (f == S.IB || f == S.IE + 1) Ex = (R)0;
     if (f == S.IB && S.bc_x0 == 3) Ex = (R)(S.Din[j] * S.Uin[j + S.Nloc * k]);   // src/nhwave.F:1564-1566
     S.Ex[i3(S, f, j, k)] = Ex;
@@ -1075,26 +1154,27 @@ struct OpOmegaY {
     const long long e0 = i3(S, i, c0, k), e1 = e0 + sy;
     const long long q0 = i2(S, i, c0), q1 = q0 + sy;
     const int mL = S.Mask[q0], mR = S.Mask[q1];
-    const R hdy = (R)(0.5 * S.dy), rdy = (R)S.dy, irdy = (R)(1.0 / S.dy);
+    const R hdy = S.hdyT, rdy = S.dyT, irdy = S.idyT;
     auto sl = [&](const T* A, long long e, int m) -> R {
       return m == 0 ? (R)0 : lim_slope_u<R>(A[e - sy], A[e], A[e + sy], rdy, irdy);
     };
     const R vL = S.V[e0] + hdy * sl(S.V, e0, mL), vR = S.V[e1] - hdy * sl(S.V, e1, mR);
     R dvL = S.DV[e0] + hdy * sl(S.DV, e0, mL), dvR = S.DV[e1] - hdy * sl(S.DV, e1, mR);
-    double etaL = S.Eta[q0] + 0.5 * S.dy * S.DelyEta[q0];
-    double etaR = S.Eta[q1] - 0.5 * S.dy * S.DelyEta[q1];
-    const double hf = S.Hfy[q1];
-    double dL = dmax_(etaL + hf, S.min_dep), dR = dmax_(etaR + hf, S.min_dep);
-    if (c0 >= S.JB && c0 <= S.JE) {
-      if ((mL == 1 && mR == 0) || mL == 0) { etaL = S.Eta[q0]; dL = S.D[q0]; dvL = (R)0; }
+    R rdL, rdR, rdd;
+    bool zl, zr;
+    const bool inL = c0 >= S.JB && c0 <= S.JE, inR = c1 >= S.JB && c1 <= S.JE;
+    if (face_table<R>(S)) {
+      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const T* ft = S.fyT + q1;
+      rdL = ft[2 * n2]; rdR = ft[3 * n2]; rdd = ft[5 * n2];
+      face_flags(S, q0, sy, inL, inR, zl, zr);
+    } else {
+      const Face2D F = face_2d(S, q0, sy, inL, inR, 0.5 * S.dy, S.DelyEta, S.Hfy, S.Hfy0);
+      if (k == S.KB) { S.EtayL[q1] = F.etaL; S.EtayR[q1] = F.etaR; }
+      rdL = (R)F.dL; rdR = (R)F.dR; rdd = (R)(F.dR - F.dL); zl = F.zl; zr = F.zr;
     }
-    if (c1 >= S.JB && c1 <= S.JE) {
-      const int mRR = S.Mask[q1 + sy];
-      if (mR == 1 && mRR == 0) {
-      } else if ((mR == 1 && mL == 0) || mR == 0) { etaR = S.Eta[q1]; dR = S.D[q1]; dvR = (R)0; }
-    }
-    if (k == S.KB) { S.EtayL[q1] = etaL; S.EtayR[q1] = etaR; }
-    const R rdL = (R)dL, rdR = (R)dR;
+    if (zl) dvL = (R)0;
+    if (zr) dvR = (R)0;
     R SL = (R)0, SR = (R)0;
     if (mL == 1 && mR == 1) {
       R pL = sqrt((R)kGrav * fabs(rdL)), pR = sqrt((R)kGrav * fabs(rdR));
@@ -1111,7 +1191,7 @@ struct OpOmegaY {
       SL = vL - pL;
       SR = vL + (R)2.0 * pL;
     }
-    R Ey = hll_d<R>(SL, SR, dvL, dvR, (R)(dR - dL));
+    R Ey = hll_d<R>(SL, SR, dvL, dvR, rdd);
     if (g == S.JB || g == S.JE + 1) Ey = (R)0;
     S.Ey[i3(S, i, g, k)] = Ey;
   }

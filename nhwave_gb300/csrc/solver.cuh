@@ -204,6 +204,8 @@ class Solver final : public SolverBase {
     S.dx = p.dx; S.dy = p.dy; S.min_dep = p.min_dep; S.cfl = p.cfl;
     S.cxx = -1. / (p.dx * p.dx); S.cyy = -1. / (p.dy * p.dy);
     S.i2dx = 0.5 / p.dx; S.i2dy = 0.5 / p.dy;
+    S.dxT = (T)p.dx; S.hdxT = (T)(0.5 * p.dx); S.idxT = (T)(1.0 / p.dx);
+    S.dyT = (T)p.dy; S.hdyT = (T)(0.5 * p.dy); S.idyT = (T)(1.0 / p.dy);
     S.dt_min = p.dt_min; S.dt_max = p.dt_max;
     S.fcor = 2.0 * (double)7.29e-5f * std::sin(p.slat);
     S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
@@ -299,6 +301,8 @@ class Solver final : public SolverBase {
     }
     std::vector<T**> mgptr;
     if (use_mg) add(&S.sp0, sizeof(T) * 7 * 2 * (size_t)K * N * ((M + 1) / 2));
+    if (kFP32 && !p.hllc)   // 2-D face states (scratch of one stage)
+      for (T** ft : {&S.fxT, &S.fyT}) add(ft, sizeof(T) * 6 * (size_t)S.Mloc * S.Nloc);
     for (size_t l = 1; l < mg.size(); ++l) {
       const size_t nl = (size_t)mg[l].n;
       add((T**)&mg[l].coef, sizeof(T) * NCOMPACT * nl);
@@ -748,6 +752,7 @@ class Solver final : public SolverBase {
   }
   int fluxes() override {
     allcols(OpSlopeEta{});
+    if (S.fxT) box(OpFacePrep{0}, S.M + 1, S.N + 1, 1, S.IB, S.JB, 0);
     box(OpFluxX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpFluxY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     box(OpFluxZ{}, S.M, S.N, S.K + 1, S.IB, S.JB, S.KB);
@@ -993,6 +998,7 @@ class Solver final : public SolverBase {
     }
     cells(OpSSP{s});
     get_uvw();
+    if (S.fxT) box(OpFacePrep{1}, S.M + 1, S.N + 1, 1, S.IB, S.JB, 0);
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});

@@ -120,6 +120,11 @@ struct Dev {
   // kernels formed them per cell before
   const T* lvT;
   double i2dx, i2dy;       // 0.5/dx, 0.5/dy
+  // the spacings in the storage type, rounded once: dx, dx/2, 1/dx (and y)
+  T dxT, hdxT, idxT, dyT, hdyT, idyT;
+  // FP32+IR form with HLL: 2-D face states of the x / y faces in the storage
+  // type, [6][Mloc*Nloc] at the face's right cell (OpFacePrep), else nullptr
+  T *fxT, *fyT;
   int *Mask, *MaskT, *Mask_Struct, *Mask9;
   // 3-D fields (storage type T); P is FP64 in both forms
   T *U, *V, *W, *DU, *DV, *DW, *DU0, *DV0, *DW0, *Omega;
