@@ -311,6 +311,9 @@ __device__ __forceinline__ bool face_table(const Dev<T>& S) {
   if constexpr (sizeof(R) == 4) return S.fxT != nullptr && !S.hllc;
   else return false;
 }
+// elements of one slot of fxT / fyT: the size of a 2-D field, sy * (Nloc + 1)
+template <class T>
+__device__ __forceinline__ long long face_slot(const Dev<T>& S) { return (long long)S.sy * (S.Nloc + 1); }
 // table slots: eta, D on each side and h0 rounded to T, then (T)(dR - dL)
 struct FaceT {
   template <class T>
@@ -327,7 +330,7 @@ struct OpFacePrep {
   int omega;
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j, int) const {
-    const long long n2 = (long long)S.Mloc * S.Nloc;
+    const long long n2 = face_slot(S);
     if (j <= S.JE) {   // x face f = i between cells i-1 and i
       const long long q0 = i2(S, i - 1, j);
       const Face2D F = face_2d(S, q0, 1, i - 1 >= S.IB && i - 1 <= S.IE, i >= S.IB && i <= S.IE, 0.5 * S.dx,
@@ -440,7 +443,7 @@ struct OpFluxX {
     bool zl, zr;
     const bool inL = c0 >= S.IB && c0 <= S.IE, inR = c1 >= S.IB && c1 <= S.IE;
     if (face_table<R>(S)) {
-      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const long long n2 = face_slot(S);
       const T* ft = S.fxT + q1;
       reL = ft[0]; reR = ft[n2]; rdL = ft[2 * n2]; rdR = ft[3 * n2]; rh0 = ft[4 * n2]; rdd = ft[5 * n2];
       h0 = (double)rh0;
@@ -548,7 +551,7 @@ struct OpFluxY {
     bool zl, zr;
     const bool inL = c0 >= S.JB && c0 <= S.JE, inR = c1 >= S.JB && c1 <= S.JE;
     if (face_table<R>(S)) {
-      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const long long n2 = face_slot(S);
       const T* ft = S.fyT + q1;
       reL = ft[0]; reR = ft[n2]; rdL = ft[2 * n2]; rdR = ft[3 * n2]; rh0 = ft[4 * n2]; rdd = ft[5 * n2];
       face_flags(S, q0, sy, inL, inR, zl, zr);
@@ -1111,7 +1114,7 @@ struct OpOmegaX {
     bool zl, zr;
     const bool inL = c0 >= S.IB && c0 <= S.IE, inR = c1 >= S.IB && c1 <= S.IE;
     if (face_table<R>(S)) {
-      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const long long n2 = face_slot(S);
       const T* ft = S.fxT + q1;
       rdL = ft[2 * n2]; rdR = ft[3 * n2]; rdd = ft[5 * n2];
       face_flags(S, q0, 1, inL, inR, zl, zr);
@@ -1164,7 +1167,7 @@ struct OpOmegaY {
     bool zl, zr;
     const bool inL = c0 >= S.JB && c0 <= S.JE, inR = c1 >= S.JB && c1 <= S.JE;
     if (face_table<R>(S)) {
-      const long long n2 = (long long)S.Mloc * S.Nloc;
+      const long long n2 = face_slot(S);
       const T* ft = S.fyT + q1;
       rdL = ft[2 * n2]; rdR = ft[3 * n2]; rdd = ft[5 * n2];
       face_flags(S, q0, sy, inL, inR, zl, zr);

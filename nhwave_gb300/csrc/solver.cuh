@@ -302,7 +302,7 @@ class Solver final : public SolverBase {
     std::vector<T**> mgptr;
     if (use_mg) add(&S.sp0, sizeof(T) * 7 * 2 * (size_t)K * N * ((M + 1) / 2));
     if (kFP32 && !p.hllc)   // 2-D face states (scratch of one stage)
-      for (T** ft : {&S.fxT, &S.fyT}) add(ft, sizeof(T) * 6 * (size_t)S.Mloc * S.Nloc);
+      for (T** ft : {&S.fxT, &S.fyT}) add(ft, sizeof(T) * 6 * n2);
     for (size_t l = 1; l < mg.size(); ++l) {
       const size_t nl = (size_t)mg[l].n;
       add((T**)&mg[l].coef, sizeof(T) * NCOMPACT * nl);

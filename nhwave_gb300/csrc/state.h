@@ -123,7 +123,8 @@ struct Dev {
   // the spacings in the storage type, rounded once: dx, dx/2, 1/dx (and y)
   T dxT, hdxT, idxT, dyT, hdyT, idyT;
   // FP32+IR form with HLL: 2-D face states of the x / y faces in the storage
-  // type, [6][Mloc*Nloc] at the face's right cell (OpFacePrep), else nullptr
+  // type, [6][sy*(Nloc+1)] (the size of a 2-D field) at the face's right cell
+  // (OpFacePrep), else nullptr
   T *fxT, *fyT;
   int *Mask, *MaskT, *Mask_Struct, *Mask9;
   // 3-D fields (storage type T); P is FP64 in both forms

@@ -78,3 +78,29 @@ def test_out_of_scope_reason(tmp_path):
     assert p.hllc == 1 and P.unsupported_reason(p) is None
     f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 2"))
     assert "BC_Z0" in P.unsupported_reason(P.read_input(str(f)))
+
+
+def test_reference_example_inputs_where_present():
+    """The reference's own example input files, read by the host reader: the
+    non-viscous, barotropic ones fall inside the GPU path, the viscous ones
+    (3-D k-epsilon, bottom friction) and the baroclinic default are rejected
+    with their reason.  Reads the reference checkout when one is mounted."""
+    import glob
+    import os
+    from nhwave_gb300 import params as P
+    root = os.environ.get("NHWAVE_REFERENCE", "/root/reference")
+    files = sorted(glob.glob(os.path.join(root, "**", "input*.txt"), recursive=True))
+    if not files:
+        pytest.skip("no reference checkout")
+    inside = 0
+    for f in files:
+        p = P.read_input(f)
+        reason = P.unsupported_reason(p)
+        if p.viscous_flow:
+            assert reason and "VISCOUS_FLOW" in reason, f
+        elif not p.barotropic:
+            assert reason and "BAROTROPIC" in reason, f
+        else:
+            assert reason is None, (f, reason)
+            inside += 1
+    assert inside >= 4
