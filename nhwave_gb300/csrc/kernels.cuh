@@ -984,17 +984,19 @@ struct OpLineFactor {
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const size_t n = (size_t)S.neq, mn = (size_t)S.M * S.N;
     const size_t base = (size_t)(i - S.IB) + (size_t)S.M * (j - S.JB);
-    double cpm = 0.0;
+    // in the storage type: FP64 as before, FP32 in the FP32+IR form (the
+    // factors are stored in FP32 there anyway)
+    T cpm = (T)0;
     for (int k = 0; k < S.K; ++k) {
       const size_t ic = base + mn * k;
-      const double a = k > 0 ? S.coef64[2 * n + ic] : 0.0;
-      const double b = S.coef64[ic];
-      const double c = k < S.K - 1 ? S.coef64[n + ic] : 0.0;
-      const double den = b - a * cpm;
-      const double inv = 1.0 / den;
+      const T a = k > 0 ? (T)S.coef64[2 * n + ic] : (T)0;
+      const T b = (T)S.coef64[ic];
+      const T c = k < S.K - 1 ? (T)S.coef64[n + ic] : (T)0;
+      const T den = b - a * cpm;
+      const T inv = (T)1 / den;
       cpm = c * inv;
-      S.lcp[ic] = (T)cpm;
-      S.linv[ic] = (T)inv;
+      S.lcp[ic] = cpm;
+      S.linv[ic] = inv;
       if (S.sp0) {   // colour-split copy for the level-0 half-sweeps (layout in mg.cuh, MGL::sp)
         const int ii = i - S.IB, jj = j - S.JB, Mh = (S.M + 1) >> 1;
         const size_t nmh = (size_t)Mh * S.N, cs = nmh * S.K;
@@ -1061,6 +1063,30 @@ struct OpProjection {
     S.DW[o] = (T)((double)S.DW[o] - g * DelzP);
   }
 };
+// The same in the FP32+IR form: the pressure differences in FP64 (P is FP64),
+// each rounded once, and the rest in FP32
+struct OpProjection32 {
+  static constexpr const char* kName = "projection";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j);
+    if (S.Mask[q] == 0) return;
+    const long long o = i3(S, i, j, k), sy = S.sy, sz = S.sz;
+    const double* P = S.P;
+    const T hx = (T)S.i2dx, hy = (T)S.i2dy;
+    const T dx0 = (T)(P[o + 1] - P[o - 1]), dx1 = (T)(P[o + 1 + sz] - P[o - 1 + sz]);
+    const T dy0 = (T)(P[o + sy] - P[o - sy]), dy1 = (T)(P[o + sy + sz] - P[o - sy + sz]);
+    const T DelxP = (T)0.5 * (dx0 * hx + dx1 * hx), DelyP = (T)0.5 * (dy0 * hy + dy1 * hy);
+    const T DelzP = (T)(P[o + sz] - P[o]) * S.lvT[k];
+    const T sc = (T)S.sigc[k], omc = (T)1 - sc;
+    const T DelxSc = omc * (T)S.cf_hx[q] - sc * (T)S.cf_ex[q];
+    const T DelySc = omc * (T)S.cf_hy[q] - sc * (T)S.cf_ey[q];
+    const T g = (T)S.sc->dt_rho, f = (T)S.D[q] * g;
+    S.DU[o] = S.DU[o] - f * (DelxP + DelzP * DelxSc);
+    S.DV[o] = S.DV[o] - f * (DelyP + DelzP * DelySc);
+    S.DW[o] = S.DW[o] - g * DelzP;
+  }
+};
 
 // SSP-RK combination, mask and Froude cap (src/nhwave.F:1227-1261)
 struct OpSSP {
@@ -1078,11 +1104,19 @@ struct OpSSP {
     if (m == 0) { du = (R)0; dv = (R)0; dw = (R)0; }
     if (S.froude_on && m > 0) {
       const double Dq = S.D[q];
-      const double FroudeU = sqrt(kGrav * Dq) * S.froude_cap * Dq;
-      const double a = (double)du, b = (double)dv, cc = (double)dw;
-      const double DUU = sqrt(a * a + b * b + cc * cc);
-      if (DUU > FroudeU) {
-        const double ang = atan2(b, a);
+      bool over;
+      double FroudeU = 0.0;
+      if constexpr (sizeof(R) == 4) {   // FP32+IR form: the test in FP32, the cap itself in FP64
+        const R rD = (R)Dq;
+        over = sqrt(du * du + dv * dv + dw * dw) > sqrt((R)kGrav * rD) * (R)S.froude_cap * rD;
+        if (over) FroudeU = sqrt(kGrav * Dq) * S.froude_cap * Dq;
+      } else {
+        FroudeU = sqrt(kGrav * Dq) * S.froude_cap * Dq;
+        const double a = (double)du, b = (double)dv, cc = (double)dw;
+        over = sqrt(a * a + b * b + cc * cc) > FroudeU;
+      }
+      if (over) {
+        const double ang = atan2((double)dv, (double)du);
         du = (R)(FroudeU * cos(ang));
         dv = (R)(FroudeU * sin(ang));
         dw = (R)0;

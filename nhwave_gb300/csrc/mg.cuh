@@ -578,16 +578,16 @@ __global__ void __launch_bounds__(256) k_mg_factor(MGL<T> L, T* lcp, T* linv) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= L.M * L.N) return;
   const int MN = L.M * L.N, n = L.n;
-  double cpm = 0.0;
+  T cpm = (T)0;   // in the storage type, as the factors are stored
   for (int k = 0; k < L.K; ++k) {
     const int ic = col + MN * k;
-    const double a = k > 0 ? (double)L.coef[2 * n + ic] : 0.0;
-    const double b = (double)L.coef[ic];
-    const double c = k < L.K - 1 ? (double)L.coef[n + ic] : 0.0;
-    const double inv = 1.0 / (b - a * cpm);
+    const T a = k > 0 ? L.coef[2 * n + ic] : (T)0;
+    const T b = L.coef[ic];
+    const T c = k < L.K - 1 ? L.coef[n + ic] : (T)0;
+    const T inv = (T)1 / (b - a * cpm);
     cpm = c * inv;
-    lcp[ic] = (T)cpm;
-    linv[ic] = (T)inv;
+    lcp[ic] = cpm;
+    linv[ic] = inv;
   }
 }
 

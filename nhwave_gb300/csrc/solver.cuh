@@ -994,7 +994,8 @@ class Solver final : public SolverBase {
   void stage_post(int s) {
     if (S.non_hydro) {
       poisson_finish();
-      cells(OpProjection{});
+      if (kFP32) cells(OpProjection32{});
+      else cells(OpProjection{});
     }
     cells(OpSSP{s});
     get_uvw();
