@@ -78,6 +78,10 @@ def test_out_of_scope_reason(tmp_path):
     assert p.hllc == 1 and P.unsupported_reason(p) is None
     f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 2"))
     assert "BC_Z0" in P.unsupported_reason(P.read_input(str(f)))
+    # a generator of the reference that the path does not build is rejected, not run as NONE
+    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_CON"))
+    p = P.read_input(str(f))
+    assert p.wavemaker == P.WM_OTHER and "WAVEMAKER" in P.unsupported_reason(p)
 
 
 def test_reference_example_inputs_where_present():
