@@ -191,6 +191,12 @@ def read_input(path: str) -> NhwParams:
         p.sponge_south_width = f("Sponge_South_Width", 0.0)
         p.sponge_north_width = f("Sponge_North_Width", 0.0)
     p.tramp = f("TRAMP", 0.0)
+    # The reference reads SlideType only in a build with its landslide option
+    # (src/initialize.F:1033-1045), and its example inputs carry the key as a
+    # template line (TWOLAYER in the submerged bar, berkhoff and breaking
+    # cases, which have no slide).  RIGID_3D, the slide this path builds,
+    # turns the slide on; any other value reads as no slide, as in a build
+    # without that option.
     st = s("SlideType", "").upper()
     if st.startswith("RIGID_3D"):
         p.slide_type = SLIDE_RIGID_3D
