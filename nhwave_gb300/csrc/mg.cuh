@@ -480,23 +480,38 @@ __global__ void __launch_bounds__(256) k_mg_restrict_c0(MGL<T> F, MGL<T> C, cons
   decode(ic, C.M, C.N, I, J, k);
   const int n = F.n, Mh = (F.M + 1) >> 1;
   const size_t nmh = (size_t)Mh * F.N, cs = nmh * F.K;
+  // minus the off-column part of A x at colour-0 cell (i, j) of level k
+  auto cell = [&](int i, int j) -> T {
+    const int f = i + F.M * (j + F.N * k);
+    T c4, c5, c7, c8;
+    if (F.sp) {
+      const T* e = F.sp + nmh * k + (size_t)Mh * j + (i >> 1);
+      c4 = e[6 * cs]; c5 = e[8 * cs]; c7 = e[10 * cs]; c8 = e[12 * cs];
+    } else {
+      c4 = F.coef[3 * n + f]; c5 = F.coef[4 * n + f]; c7 = F.coef[5 * n + f]; c8 = F.coef[6 * n + f];
+    }
+    return off_column_c(F, F.x, f, i, j, k, c4, c5, c7, c8);
+  };
   T acc = (T)0;
-  for (int b = 0; b < F.ry; ++b) {
-    const int j = J * F.ry + b;
-    if (j >= F.N) break;
-    for (int a = 0; a < F.rx; ++a) {
-      const int i = I * F.rx + a;
-      if (i >= F.M) break;
-      if ((i + j) & 1) continue;
-      const int f = i + F.M * (j + F.N * k);
-      T c4, c5, c7, c8;
-      if (F.sp) {
-        const T* e = F.sp + nmh * k + (size_t)Mh * j + (i >> 1);
-        c4 = e[6 * cs]; c5 = e[8 * cs]; c7 = e[10 * cs]; c8 = e[12 * cs];
-      } else {
-        c4 = F.coef[3 * n + f]; c5 = F.coef[4 * n + f]; c7 = F.coef[5 * n + f]; c8 = F.coef[6 * n + f];
+  if (F.rx == 2 && F.ry == 2) {
+    // 2 x 2: the colour-0 cells are (2I, 2J) and (2I+1, 2J+1), in the order
+    // of the general loop below, written out so that both cells' loads issue
+    // together
+    const int i0 = 2 * I, j0 = 2 * J;
+    const bool c0 = i0 < F.M && j0 < F.N, c1 = i0 + 1 < F.M && j0 + 1 < F.N;
+    const T r0 = c0 ? cell(i0, j0) : (T)0, r1 = c1 ? cell(i0 + 1, j0 + 1) : (T)0;
+    if (c0) acc -= r0;
+    if (c1) acc -= r1;
+  } else {
+    for (int b = 0; b < F.ry; ++b) {
+      const int j = J * F.ry + b;
+      if (j >= F.N) break;
+      for (int a = 0; a < F.rx; ++a) {
+        const int i = I * F.rx + a;
+        if (i >= F.M) break;
+        if ((i + j) & 1) continue;
+        acc -= cell(i, j);
       }
-      acc -= off_column_c(F, F.x, f, i, j, k, c4, c5, c7, c8);
     }
   }
   C.b[ic] = acc;
