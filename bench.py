@@ -461,8 +461,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="FP32+IR timed region and profile pass only")
-    ap.add_argument("--krylov-kernel", type=int, default=0, choices=[0, 1],
-                    help="pressure solver of the C2 legs: 0 phase by phase, 1 one persistent launch per solve")
+    ap.add_argument("--krylov-kernel", type=int, default=0, choices=[0, 1, 2],
+                    help="pressure solver of the C2 legs: 0 BiCGSTAB phase by phase, 1 BiCGSTAB in one "
+                         "persistent launch per solve, 2 GMRES phase by phase")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the config-4 ensemble leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the config-5 serving leg")
     args = ap.parse_args()

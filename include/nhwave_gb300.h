@@ -115,10 +115,16 @@ typedef struct nhw_params {
   int32_t precond;                         /* Poisson preconditioner: 0 multigrid V-cycle,
                                               1 vertical-line (tridiagonal) only     */
   float   mg_weight;                       /* multigrid coarse-correction weight (0: 1.0) */
-  int32_t krylov_kernel;                   /* 0: one launch per solver phase, loops in
-                                              graph conditional nodes; 1: the whole solve
-                                              in one persistent cooperative launch (needs
-                                              the multigrid preconditioner)            */
+  int32_t krylov_kernel;                   /* inner Krylov solver of the pressure solve:
+                                              0: BiCGSTAB, one launch per phase, loops
+                                              in graph conditional nodes (fastest);
+                                              1: BiCGSTAB, the whole solve in one
+                                              persistent cooperative launch;
+                                              2: GMRES as in the reference's HYPRE
+                                              path (cycles of up to 16 iterations,
+                                              one V-cycle each), one launch per phase.
+                                              1 and 2 need the multigrid preconditioner;
+                                              without it BiCGSTAB runs phase by phase */
   int32_t mg_coarse_sweeps;                /* red-black sweeps on the coarsest level (0: 2) */
   int32_t mg_cta_columns;                  /* levels with at most this many columns run in
                                               one thread block (0: 64)                */

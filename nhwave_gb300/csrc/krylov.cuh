@@ -89,14 +89,16 @@ __device__ __forceinline__ void block_sum_t(A (&v)[NV], double (&out)[NV]) {
   }
 }
 
-// partials + last-block finalisation (fixed order)
+// partials + last-block finalisation (fixed order); `part` holds `stride`
+// doubles per block
 template <int NV, class T, class Fin>
-__device__ __forceinline__ void finish_reduce(const Dev<T>& S, double (&v)[NV], Fin fin) {
+__device__ __forceinline__ void finish_reduce_at(const Dev<T>& S, double* part, int stride, double (&v)[NV],
+                                                 Fin fin) {
   __shared__ bool last;
   __shared__ double sh2[NV * 32];
   const int nb = gridDim.x;
   if (threadIdx.x == 0) {
-    for (int q = 0; q < NV; ++q) S.partials[(size_t)blockIdx.x * 8 + q] = v[q];
+    for (int q = 0; q < NV; ++q) part[(size_t)blockIdx.x * stride + q] = v[q];
     __threadfence();
     const unsigned prev = atomicAdd(&S.sc->counter[0], 1u);
     last = (prev == (unsigned)nb - 1);
@@ -107,7 +109,7 @@ __device__ __forceinline__ void finish_reduce(const Dev<T>& S, double (&v)[NV], 
   double acc[NV];
   for (int q = 0; q < NV; ++q) acc[q] = 0.0;
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
-    for (int q = 0; q < NV; ++q) acc[q] += ((volatile double*)S.partials)[(size_t)b * 8 + q];
+    for (int q = 0; q < NV; ++q) acc[q] += ((volatile double*)part)[(size_t)b * stride + q];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   for (int q = 0; q < NV; ++q)
     for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
@@ -123,6 +125,10 @@ __device__ __forceinline__ void finish_reduce(const Dev<T>& S, double (&v)[NV], 
     S.sc->counter[0] = 0u;
     fin(S, tot);
   }
+}
+template <int NV, class T, class Fin>
+__device__ __forceinline__ void finish_reduce(const Dev<T>& S, double (&v)[NV], Fin fin) {
+  finish_reduce_at<NV>(S, S.partials, 8, v, fin);
 }
 
 __device__ __forceinline__ void decode(int ic, int M, int N, int& ii, int& jj, int& kk) {
@@ -446,6 +452,188 @@ template <class T>
 __global__ void __launch_bounds__(256) k_xupd(Dev<T> S) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < S.neq) S.xsol64[t] = S.xsol64[t] + (double)S.kx[t];
+}
+
+// ------------------------------------------------------------------ GMRES
+// Right-preconditioned GMRES: one cycle of at most kGmMax iterations per
+// refinement sweep, so the sweeps of k_res64 are its restarts.  It is the
+// method of the reference's parallel build, HYPRE StructGMRES preconditioned
+// by one SMG cycle (src/pressure.F:399-423); the preconditioner here is the
+// V-cycle of mg.cuh.  Iteration j:
+//   z_j = M^-1 v_j          the V-cycle, whose first half-sweeps form
+//                           v_j = w / ||w|| (MgInV) and store it;
+//   w = A z_j, h_ij = (w, v_i), i <= j                      k_gm_arnoldi;
+//   w -= sum_i h_ij v_i, h_j+1,j = ||w||                     k_gm_orth
+//     (classical Gram-Schmidt; its last block rotates column j of H with the
+//     Givens rotations so far, updates the residual norm |g_j+1| and decides
+//     the loop, and at the end solves R y = g);
+// after the loop k_gm_xupd adds sum_i y_i z_i to the FP64 solution.  One
+// iteration is one preconditioner application (BiCGSTAB takes two).
+constexpr int kGmMax = 16;
+constexpr int kGmM1 = kGmMax + 1;
+// FP64 state in Dev::gm: H column-major (h_ij at j * kGmM1 + i), cosines,
+// sines, g, y
+constexpr int kGmH = 0, kGmCs = kGmM1 * kGmMax, kGmSn = kGmCs + kGmMax, kGmG = kGmSn + kGmMax,
+              kGmY = kGmG + kGmM1, kGmSize = kGmY + kGmMax;
+// T copies in Dev::gmT: column j of H, y, 1/||w||
+constexpr int kGmTH = 0, kGmTY = kGmMax, kGmTInv = 2 * kGmMax, kGmTSize = 2 * kGmMax + 1;
+
+// start of a cycle from c = 0: w = r0 (the inner right-hand side), beta = ||w||
+template <class T>
+__global__ void __launch_bounds__(256) k_gm_init(Dev<T> S) {
+  using A = typename Acc<T>::type;
+  A v[1] = {(A)0};
+#pragma unroll
+  for (int q = 0; q < kCPT; ++q) {
+    const int t = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (t < S.neq) {
+      const T r = S.kr0[t];
+      S.kt[t] = r;
+      v[0] += (A)r * (A)r;
+    }
+  }
+  double out[1];
+  block_sum_t<1, A>(v, out);
+  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
+    DevScal* sc = S2.sc;
+    double* gm = S2.gm;
+    const double beta = sqrt(a[0]);
+    sc->red[0] = beta;
+    sc->it = 0;
+    sc->relres = 1.0;
+    for (int i = 0; i < kGmM1; ++i) gm[kGmG + i] = 0.0;
+    gm[kGmG] = beta;
+    sc->gm_inv = beta > 0.0 ? 1.0 / beta : 0.0;
+    S2.gmT[kGmTInv] = (T)sc->gm_inv;
+    sc->conv = !(beta == beta) ? 5 : (beta == 0.0 ? 1 : 0);
+    set_cond(S2, S2.h_inner, sc->conv == 0);
+  });
+}
+
+// w = A z_j (z_j = the V-cycle's output in kph, kept as column j of Z);
+// h_ij = (w, v_i) for i <= j
+template <class T>
+__global__ void __launch_bounds__(256) k_gm_arnoldi(Dev<T> S) {
+  if (S.sc->conv) return;
+  using A = typename Acc<T>::type;
+  const int j = S.sc->it;
+  const size_t n = (size_t)S.neq;
+  const T* __restrict__ z = S.kph;
+  T* __restrict__ zj = S.gmZ + (size_t)j * n;
+  A v[kGmMax];
+#pragma unroll
+  for (int i = 0; i < kGmMax; ++i) v[i] = (A)0;
+  for (int q = 0; q < kCPT; ++q) {
+    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (ic < S.neq) {
+      int ii, jj, kk;
+      decode(ic, S.M, S.N, ii, jj, kk);
+      const T y = spmv_c<T, T>(S.coefT, z, n, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
+      S.kt[ic] = y;
+      zj[ic] = z[ic];
+#pragma unroll
+      for (int i = 0; i < kGmMax; ++i)
+        if (i <= j) v[i] += (A)y * (A)S.gmV[(size_t)i * n + ic];
+    }
+  }
+  double out[kGmMax];
+  block_sum_t<kGmMax, A>(v, out);
+  finish_reduce_at<kGmMax>(S, S.gm_part, kGmMax, out, [] __device__(const Dev<T>& S2, double* a) {
+    const int j2 = S2.sc->it;
+    for (int i = 0; i <= j2; ++i) {
+      S2.gm[kGmH + j2 * kGmM1 + i] = a[i];
+      S2.gmT[kGmTH + i] = (T)a[i];
+    }
+  });
+}
+
+// w -= sum_i h_ij v_i; ||w||; rotations, residual estimate, loop decision
+template <class T>
+__global__ void __launch_bounds__(256) k_gm_orth(Dev<T> S) {
+  if (S.sc->conv) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_cond(S, S.h_inner, false);
+    return;
+  }
+  using A = typename Acc<T>::type;
+  const int j = S.sc->it;
+  const size_t n = (size_t)S.neq;
+  T h[kGmMax];
+#pragma unroll
+  for (int i = 0; i < kGmMax; ++i) h[i] = i <= j ? S.gmT[kGmTH + i] : (T)0;
+  A v[1] = {(A)0};
+  for (int q = 0; q < kCPT; ++q) {
+    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+    if (ic < S.neq) {
+      T w = S.kt[ic];
+#pragma unroll
+      for (int i = 0; i < kGmMax; ++i)
+        if (i <= j) w -= h[i] * S.gmV[(size_t)i * n + ic];
+      S.kt[ic] = w;
+      v[0] += (A)w * (A)w;
+    }
+  }
+  double out[1];
+  block_sum_t<1, A>(v, out);
+  finish_reduce<1>(S, out, [] __device__(const Dev<T>& S2, double* a) {
+    DevScal* sc = S2.sc;
+    double* gm = S2.gm;
+    const int j2 = sc->it;
+    const double hn = sqrt(a[0]);
+    double* Hj = gm + kGmH + j2 * kGmM1;
+    Hj[j2 + 1] = hn;
+    for (int i = 0; i < j2; ++i) {   // earlier rotations on column j
+      const double c = gm[kGmCs + i], s = gm[kGmSn + i];
+      const double t0 = c * Hj[i] + s * Hj[i + 1];
+      Hj[i + 1] = -s * Hj[i] + c * Hj[i + 1];
+      Hj[i] = t0;
+    }
+    const double a0 = Hj[j2], b0 = Hj[j2 + 1], rr = sqrt(a0 * a0 + b0 * b0);
+    const double c = rr > 0.0 ? a0 / rr : 1.0, s = rr > 0.0 ? b0 / rr : 0.0;
+    gm[kGmCs + j2] = c;
+    gm[kGmSn + j2] = s;
+    Hj[j2] = rr;
+    Hj[j2 + 1] = 0.0;
+    const double gj = gm[kGmG + j2];
+    gm[kGmG + j2] = c * gj;
+    gm[kGmG + j2 + 1] = -s * gj;
+    sc->it = j2 + 1;
+    sc->total_it = sc->total_it + 1;
+    sc->inner_total = sc->inner_total + 1;
+    const double rel = sc->red[0] > 0.0 ? fabs(gm[kGmG + j2 + 1]) / sc->red[0] : 0.0;
+    sc->relres = rel;
+    int conv = 0;
+    if (!(rel == rel) || !(hn == hn)) conv = 5;
+    else if (rel <= sc->tol_in || hn == 0.0) conv = 1;   // hn = 0: exact within the Krylov space
+    else if (sc->it >= kGmMax || sc->it >= sc->itmax_in) conv = 4;
+    else {
+      sc->gm_inv = 1.0 / hn;
+      S2.gmT[kGmTInv] = (T)sc->gm_inv;
+    }
+    if (conv) {   // R y = g over the iterations of this cycle
+      const int m = sc->it;
+      for (int k = m - 1; k >= 0; --k) {
+        double acc = gm[kGmG + k];
+        for (int l = k + 1; l < m; ++l) acc -= gm[kGmH + l * kGmM1 + k] * gm[kGmY + l];
+        const double d = gm[kGmH + k * kGmM1 + k];
+        gm[kGmY + k] = d != 0.0 ? acc / d : 0.0;
+        S2.gmT[kGmTY + k] = (T)gm[kGmY + k];
+      }
+    }
+    sc->conv = conv;
+    set_cond(S2, S2.h_inner, conv == 0);
+  });
+}
+
+// x64 += sum_i y_i z_i over the cycle's iterations
+template <class T>
+__global__ void __launch_bounds__(256) k_gm_xupd(Dev<T> S) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= S.neq) return;
+  const int m = S.sc->it;
+  const size_t n = (size_t)S.neq;
+  T acc = (T)0;
+  for (int i = 0; i < m; ++i) acc += S.gmT[kGmTY + i] * S.gmZ[(size_t)i * n + t];
+  S.xsol64[t] = S.xsol64[t] + (double)acc;
 }
 
 }  // namespace nhw

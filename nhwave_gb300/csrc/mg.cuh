@@ -223,6 +223,25 @@ struct MgInS {
   }
 };
 
+// GMRES: v_j = w / ||w||, formed by the sweep that owns each column and stored
+// both as column j of the basis (j = sc->it, read on the device, so a
+// captured iteration serves every j) and in `b`, which the post-smoothing
+// half-sweeps read as the level's right-hand side
+template <class T>
+struct MgInV {
+  const T* w;
+  T* b;
+  T* V;
+  const T* inv;   // (T)(1 / ||w||)
+  size_t n;
+  __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
+    const T val = w[ic] * *inv;
+    V[(size_t)sc->it * n + ic] = val;
+    b[ic] = val;
+    return val;
+  }
+};
+
 // Same half-sweep, block-parallel: a block holds 32 columns of the colour and
 // up to 32 levels (blockDim = 32 x min(K,32)); every thread forms the line
 // right-hand sides of its (column, level) cells -- loads coalesced along the

@@ -30,6 +30,7 @@ int check_params(const nhw_params& p) {
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
   if (p.wavemaker < 0 || p.wavemaker > 4) return NHW_ERR_UNSUPPORTED;
+  if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;

@@ -143,6 +143,7 @@ class Solver final : public SolverBase {
   int mg_coarse_sweeps = 2;   // red-black sweeps on the coarsest level (fastest of 2, 4, 6 on C2)
   // persistent solve (psolve.cuh): one cooperative launch per pressure solve
   bool use_persistent = false;
+  bool use_gmres = false;   // krylov_kernel 2 with multigrid: GMRES (krylov.cuh); else BiCGSTAB
   int ps_nb = 0;             // blocks of the launch
   size_t ps_smem = 0;        // dynamic shared memory per block
   double* ps_part = nullptr; // [2][ps_nb][4] partial sums
@@ -316,6 +317,14 @@ class Solver final : public SolverBase {
     // persistent solve: every block resident (cooperative launch), at most
     // one block per 2048 unknowns
     use_persistent = use_mg && p.krylov_kernel == 1 && (int)mg.size() <= kPsMaxLevels;
+    use_gmres = use_mg && p.krylov_kernel == 2;
+    if (use_gmres) {
+      add(&S.gmV, sizeof(T) * (kGmMax + 1) * (size_t)neq);
+      add(&S.gmZ, sizeof(T) * kGmMax * (size_t)neq);
+      add(&S.gmT, sizeof(T) * kGmTSize);
+      add(&S.gm, sizeof(double) * kGmSize);
+      add(&S.gm_part, sizeof(double) * kGmMax * (size_t)cdiv((long long)neq, 256 * kCPT));
+    }
     if (use_mg && (int)mg.size() <= kPsMaxLevels)   // partial sums of the scenario's group, up to kPsMaxBlocks
       add(&ps_part, sizeof(double) * 2 * 4 * kPsMaxBlocks);
     if (use_persistent) {
@@ -369,6 +378,8 @@ class Solver final : public SolverBase {
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
     }
     NHW_CU(cudaFuncSetAttribute(k_mg_cta_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(sizeof(T) * 4 * 32 * 64)));
@@ -824,9 +835,9 @@ class Solver final : public SolverBase {
       S.h_inner = new_handle();
       L("res64", [&] { k_res64<T, true><<<red_blocks(), 256, 0, st>>>(S); });
       cond_node(S.h_ir, cudaGraphCondTypeWhile, [&] {
-        L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+        inner_init();
         cond_node(S.h_inner, cudaGraphCondTypeWhile, [&] { one_iteration(); }, 2);
-        L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+        inner_finish();
         L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
       }, 1);
       return NHW_OK;
@@ -836,7 +847,7 @@ class Solver final : public SolverBase {
     int rc = pull_scalars();
     if (rc) return rc;
     while (h_sc->ir_go) {
-      L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+      inner_init();
       int chunk = 4;
       while (true) {
         rc = run_iterations(chunk);
@@ -846,7 +857,7 @@ class Solver final : public SolverBase {
         if (h_sc->conv != 0) break;
         if (chunk < 16) chunk *= 2;
       }
-      L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+      inner_finish();
       L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
       rc = pull_scalars();
       if (rc) return rc;
@@ -854,7 +865,16 @@ class Solver final : public SolverBase {
     rc = check();
     return rc ? rc : h_sc->pstat;
   }
-  // `chunk` BiCGSTAB iterations; replayed from a captured CUDA graph unless the
+  // start and end of one inner solve (one refinement sweep)
+  void inner_init() {
+    if (use_gmres) L("gm_init", [&] { k_gm_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+    else L("bicg_init", [&] { k_bicg_init<T><<<red_blocks(), 256, 0, st>>>(S); });
+  }
+  void inner_finish() {
+    if (use_gmres) L("x_update", [&] { k_gm_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+    else L("x_update", [&] { k_xupd<T><<<cdiv(S.neq, 256), 256, 0, st>>>(S); });
+  }
+  // `chunk` Krylov iterations; replayed from a captured CUDA graph unless the
   // per-kernel profiler is on (its events would become graph nodes)
   struct ChunkGraph { int chunk; cudaGraphExec_t exec; long long kernels; };
   std::vector<ChunkGraph> graphs;
@@ -885,6 +905,12 @@ class Solver final : public SolverBase {
     return NHW_OK;
   }
   void one_iteration() {
+    if (use_gmres) {   // z_j = M^-1 v_j (v_j formed by the first sweeps), then Arnoldi
+      vcycle(S.kp, S.kph, 3);
+      L("gm_arnoldi", [&] { k_gm_arnoldi<T><<<red_blocks(), 256, 0, st>>>(S); });
+      L("gm_orth", [&] { k_gm_orth<T><<<red_blocks(), 256, 0, st>>>(S); });
+      return;
+    }
     const unsigned cb = cdiv((long long)S.M * S.N, 128);
     if (use_mg) {
       vcycle(S.kp, S.kph, 1);   // p is formed by the fine level's first sweeps
@@ -949,6 +975,8 @@ class Solver final : public SolverBase {
         const int zx = color == 0 ? 1 : 0;
         if (l == 0 && fine_in == 1) smooth(mg[0], color, zx, 0, none, MgInP<T>{S.kp, S.kr, S.kv});
         else if (l == 0 && fine_in == 2) smooth(mg[0], color, zx, 0, none, MgInS<T>{S.ks, S.kr, S.kv});
+        else if (l == 0 && fine_in == 3)
+          smooth(mg[0], color, zx, 0, none, MgInV<T>{S.kt, S.kp, S.gmV, S.gmT + kGmTInv, (size_t)S.neq});
         else smooth(mg[l], color, zx, l, none, MgB<T>{mg[l].b});
       }
       MGL<T> f = mg[l], c = mg[l + 1];

@@ -57,6 +57,7 @@ struct DevScal {
   // grid barrier of the persistent solve (psolve.cuh)
   unsigned int bar_count, bar_gen;
   int32_t bar_err, pad2_;
+  double gm_inv;                    // GMRES: 1 / ||w|| of the vector the next iteration normalises
 };
 
 template <class T>
@@ -141,6 +142,12 @@ struct Dev {
   T *lcp, *linv;      // line preconditioner factors [neq]
   T* sp0;             // colour-split copy of the level-0 smoother's operator (MGL::sp), or nullptr
   T *kx, *kr, *kr0, *kp, *kph, *kv, *ks, *ksh, *kt;
+  // GMRES (krylov.cuh): basis V [kGmMax+1][neq], preconditioned basis Z
+  // [kGmMax][neq], Hessenberg / rotations / g / y in FP64 (gm), the current
+  // column, y and 1/||w|| in T (gmT), wide reduction partials; nullptr unless
+  // the GMRES solver is on
+  T *gmV, *gmZ, *gmT;
+  double *gm, *gm_part;
   double* partials;   // reduction partials [nblocks * 8]
   DevScal* sc;
 };

@@ -54,7 +54,8 @@ def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     assert st == lib.ERR_UNSUPPORTED and not h.value
 
 
-@pytest.mark.parametrize("field,value", [("Mglob", 0), ("dx", 0.0), ("precision", 7), ("time_order", 4)])
+@pytest.mark.parametrize("field,value", [("Mglob", 0), ("dx", 0.0), ("precision", 7), ("time_order", 4),
+                                         ("krylov_kernel", 3)])
 def test_bad_arguments_rejected(field, value, gpu_lib):
     from nhwave_gb300 import default_params, lib
     p = default_params(**{field: value})

@@ -136,3 +136,30 @@ def test_persistent_solve_matches_phase_solve(name, precision, gpu_lib):
     # products are summed in another order: the counts agree to about 10 %
     assert abs(sa.total_krylov_iters - sb.total_krylov_iters) <= max(3, 0.1 * sa.total_krylov_iters)
     assert sb.last_rel_residual <= b.params.tol
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"])
+def test_gmres_matches_bicgstab(name, precision, gpu_lib):
+    """GMRES (krylov_kernel = 2) against BiCGSTAB (the default) with the same
+    multigrid preconditioner and refinement loop: both solve each step's
+    pressure system to TOL, so the fields agree to the solver tolerance, and
+    GMRES applies the preconditioner at most as often."""
+    from nhwave_gb300 import fields as F
+    from conftest import rel_l2
+    a = _scen(name, precision)
+    b = _scen(name, precision, krylov_kernel=2)
+    for _ in range(3):
+        assert a.step() == 0
+        assert b.step() == 0
+    lim = 1e-8 if precision == 0 else 1e-6
+    for f in ("ETA", "P", "U", "W"):
+        fid = getattr(F, f)
+        sl = a.shape.interior(fid)
+        r = rel_l2(b.get(fid)[sl], a.get(fid)[sl])
+        assert r < lim, f"{name} {f}: {r:.3e}"
+    assert np.array_equal(a.get(F.MASK), b.get(F.MASK))
+    sa, sb = a.scalars(), b.scalars()
+    assert sb.last_rel_residual <= b.params.tol
+    # one GMRES iteration is one V-cycle, one BiCGSTAB iteration two
+    assert sb.total_krylov_iters <= 2 * sa.total_krylov_iters
