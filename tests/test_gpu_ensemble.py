@@ -126,3 +126,24 @@ def test_autotuner_picks_a_candidate(gpu_lib):
         assert [m.scalars().run_step for m in ms] == [x + 2 for x in n0]
         info = e.info()
         assert info.opts.cells_per_block == o.cells_per_block
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ensemble_of_gmres_members_matches_single_steps(precision, gpu_lib):
+    """Members on the GMRES solver (krylov_kernel = 2) inside one ensemble
+    graph: each member's branch runs the kernels its own step would, so the
+    fields agree bit for bit with the members stepped one by one."""
+    from nhwave_gb300 import fields as F, lib
+    names = ["tiny_c1", "tiny_c3", "tiny_c4"]
+    ens = [_member(n, precision, krylov_kernel=2) for n in names]
+    ref = [_member(n, precision, krylov_kernel=2) for n in names]
+    with lib.Ensemble(ens, solver=0) as e:
+        for _ in range(2):
+            assert e.step(1) == 0
+            for r in ref:
+                assert r.step() == 0
+    for n, a, b in zip(names, ens, ref):
+        assert a.scalars().total_krylov_iters == b.scalars().total_krylov_iters, n
+        for f in ("ETA", "P", "U", "MASK"):
+            fid = getattr(F, f)
+            assert np.array_equal(a.get(fid), b.get(fid)), f"{n} {f} differs"
