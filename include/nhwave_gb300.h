@@ -28,6 +28,7 @@
  *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
  *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
  *   nhw_mass               <- statistics' MassVolume  src/nhwave.F:3139-3148
+ *   nhw_statistics         <- statistics               src/nhwave.F:3118-3160
  *
  * Set-up (the work of read_bathymetry src/initialize.F:1734-2175, generate_grid
  * src/initialize.F:1647-1729 and initial src/initialize.F:2502-3408) is offered
@@ -246,6 +247,17 @@ int nhw_load_state(nhw_handle* h, const void* host, int64_t bytes);
 
 /* FP64 device reduction of statistics' MassVolume = sum(D*dx*dy). */
 int nhw_mass(nhw_handle* h, double* mass);
+
+/* The figures statistics prints (src/nhwave.F:3118-3160) over the interior,
+ * reduced on the device in FP64: MassVolume = sum D dx dy; Energy = sum over
+ * cells of CellMass (g (D sigc_k - Hc) + |u|^2 / 2), CellMass =
+ * Rho0 dsig_k D dx dy (potential energy measured from z = 0); MaxEta, MinEta;
+ * the largest |U|, |V|, |W|.  The sums are taken in a fixed block order, not
+ * the reference's loop order. */
+typedef struct nhw_stats {
+  double mass_volume, energy, max_eta, min_eta, max_u, max_v, max_w;
+} nhw_stats;
+int nhw_statistics(nhw_handle* h, nhw_stats* out);
 
 /* Wait for the handle's stream. */
 int nhw_synchronize(nhw_handle* h);

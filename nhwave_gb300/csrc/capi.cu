@@ -220,6 +220,16 @@ int nhw_mass(nhw_handle* h, double* mass) {
   if (!mass) return NHW_ERR_ARG;
   return h->s->mass(mass);
 }
+int nhw_statistics(nhw_handle* h, nhw_stats* out) {
+  NHW_GUARD(h);
+  if (!out) return NHW_ERR_ARG;
+  double v[7];
+  const int rc = h->s->statistics(v);
+  if (rc) return rc;
+  out->mass_volume = v[0]; out->energy = v[1]; out->max_eta = v[2]; out->min_eta = v[3];
+  out->max_u = v[4]; out->max_v = v[5]; out->max_w = v[6];
+  return NHW_OK;
+}
 int nhw_synchronize(nhw_handle* h) {
   NHW_BIND(h);
   return h->s->sync();

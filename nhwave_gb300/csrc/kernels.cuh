@@ -1473,6 +1473,74 @@ struct OpMaskB {
 // =========================================================================
 //                             diagnostics
 // =========================================================================
+// statistics (src/nhwave.F:3118-3160), per interior column: MassVolume's
+// D dx dy; Energy's sum over the column's levels, in k order, of
+// CellMass (g (D sigc_k - Hc) + (U^2 + V^2 + W^2) / 2) with
+// CellMass = Rho0 dsig_k D dx dy; eta; the largest |U|, |V|, |W|.  Slots of a
+// block's partial (stride 8 in S.partials): sums 0-1, maxima 2-6 (slot 3
+// holds -eta, so that MinEta is minus its maximum).  k_stats_final combines
+// the partials in block order.
+constexpr int kStatN = 7;
+template <class T>
+__global__ void __launch_bounds__(256) k_stats(Dev<T> S) {
+  __shared__ double sh[kStatN][256];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[kStatN] = {0.0, 0.0, -1.0e308, -1.0e308, 0.0, 0.0, 0.0};
+  if (t < S.M * S.N) {
+    const int i = S.IB + t % S.M, j = S.JB + t / S.M;
+    const long long q = i2(S, i, j);
+    const double D = S.D[q], hc = S.Hc[q];
+    v[0] = D * S.dx * S.dy;
+    double e = 0.0;
+    for (int k = S.KB; k <= S.KE; ++k) {
+      const long long o = i3(S, i, j, k);
+      const double cm = kRho0 * S.dsig[k] * D * S.dx * S.dy;
+      const double u = (double)S.U[o], w1 = (double)S.V[o], w2 = (double)S.W[o];
+      e = e + cm * kGrav * (D * S.sigc[k] - hc) + 0.5 * cm * (u * u + w1 * w1 + w2 * w2);
+      v[4] = dmax_(v[4], fabs(u));
+      v[5] = dmax_(v[5], fabs(w1));
+      v[6] = dmax_(v[6], fabs(w2));
+    }
+    v[1] = e;
+    v[2] = S.Eta[q];
+    v[3] = -S.Eta[q];
+  }
+  for (int m = 0; m < kStatN; ++m) sh[m][threadIdx.x] = v[m];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int m = 0; m < kStatN; ++m)
+        sh[m][threadIdx.x] = m < 2 ? sh[m][threadIdx.x] + sh[m][threadIdx.x + w]
+                                   : dmax_(sh[m][threadIdx.x], sh[m][threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int m = 0; m < kStatN; ++m) S.partials[(size_t)blockIdx.x * 8 + m] = sh[m][0];
+}
+template <class T>
+__global__ void __launch_bounds__(256) k_stats_final(Dev<T> S, int nb, double* out) {
+  __shared__ double sh[kStatN][256];
+  double v[kStatN] = {0.0, 0.0, -1.0e308, -1.0e308, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    for (int m = 0; m < kStatN; ++m) {
+      const double x = S.partials[(size_t)b * 8 + m];
+      v[m] = m < 2 ? v[m] + x : dmax_(v[m], x);
+    }
+  for (int m = 0; m < kStatN; ++m) sh[m][threadIdx.x] = v[m];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int m = 0; m < kStatN; ++m)
+        sh[m][threadIdx.x] = m < 2 ? sh[m][threadIdx.x] + sh[m][threadIdx.x + w]
+                                   : dmax_(sh[m][threadIdx.x], sh[m][threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int m = 0; m < kStatN; ++m) out[m] = sh[m][0];
+    out[3] = -out[3];
+  }
+}
+
 template <class T>
 __global__ void k_mass(Dev<T> S, double* out) {
   // MassVolume = sum over interior (j outer, i inner) of D*dx*dy, FP64, in order

@@ -49,6 +49,7 @@ class SolverBase {
   virtual int sponge_damping() = 0;
   virtual int step() = 0;
   virtual int mass(double* m) = 0;
+  virtual int statistics(double* out7) = 0;
   virtual int sync() = 0;
   virtual bool is_setup() const = 0;
   virtual double total_time() const = 0;
@@ -1403,6 +1404,18 @@ class Solver final : public SolverBase {
     NHW_CU(cudaMemcpyAsync(h_out, d_out, sizeof(double), cudaMemcpyDeviceToHost, st));
     NHW_CU(cudaStreamSynchronize(st));
     *m = h_out[0];
+    return check();
+  }
+  // MassVolume, Energy, MaxEta, MinEta, MaxU, MaxV, MaxW
+  int statistics(double* out7) override {
+    const int nb = (int)cdiv((long long)S.M * S.N, 256);
+    L("statistics", [&] {
+      k_stats<T><<<nb, 256, 0, st>>>(S);
+      k_stats_final<T><<<1, 256, 0, st>>>(S, nb, d_out);
+    });
+    NHW_CU(cudaMemcpyAsync(h_out, d_out, sizeof(double) * kStatN, cudaMemcpyDeviceToHost, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    for (int m = 0; m < kStatN; ++m) out7[m] = h_out[m];
     return check();
   }
 };

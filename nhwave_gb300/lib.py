@@ -30,13 +30,19 @@ EXPORTS = [
     "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc",
     "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
-    "nhw_step", "nhw_run", "nhw_mass", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
+    "nhw_step", "nhw_run", "nhw_mass", "nhw_statistics", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
     "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
     "nhw_estimate_dt_noalloc",
     "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
     "nhw_ensemble_get_info", "nhw_ensemble_destroy", "nhw_device_bytes",
     "nhw_checkpoint_bytes", "nhw_save_state", "nhw_load_state",
 ]
+
+
+class NhwStats(ctypes.Structure):
+    """nhw_stats: the figures of the reference's statistics."""
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("mass_volume", "energy", "max_eta", "min_eta", "max_u", "max_v", "max_w")]
 
 
 class EnsembleOpts(ctypes.Structure):
@@ -92,6 +98,7 @@ def load(path: str | None = None):
     L.nhw_step.argtypes = [vp, P(dbl), P(dbl), P(i32)]
     L.nhw_run.argtypes = [vp, i32, P(i32)]
     L.nhw_mass.argtypes = [vp, P(dbl)]
+    L.nhw_statistics.argtypes = [vp, P(NhwStats)]
     L.nhw_abi_sizes.argtypes = [P(i32), P(i32)]
     L.nhw_run_timed.argtypes = [vp, i32, P(dbl)]
     L.nhw_profile.argtypes = [vp, i32]
@@ -252,6 +259,12 @@ class Scenario:
         m = ctypes.c_double(0.0)
         _chk(load().nhw_mass(self._h, ctypes.byref(m)), "nhw_mass")
         return m.value
+
+    def statistics(self) -> dict:
+        """nhw_statistics: MassVolume, Energy, MaxEta, MinEta, MaxU, MaxV, MaxW."""
+        st = NhwStats()
+        _chk(load().nhw_statistics(self._h, ctypes.byref(st)), "nhw_statistics")
+        return {n: getattr(st, n) for n, _ in NhwStats._fields_}
 
     def scalars(self) -> NhwScalars:
         s = NhwScalars()

@@ -1659,6 +1659,33 @@ struct Model {
       for (int i = Ibeg; i <= Iend; ++i) MassVolume = MassVolume + D(i, j) * dx * dy;
     return MassVolume;
   }
+  // statistics (src/nhwave.F:3118-3160): MassVolume, Energy, MaxEta, MinEta,
+  // MaxU, MaxV, MaxW, in the reference's loop order
+  void statistics(double* out) {
+    double MassVolume = Zero, Energy = Zero;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        MassVolume = MassVolume + D(i, j) * dx * dy;
+        for (int k = Kbeg; k <= Kend; ++k) {
+          const double CellMass = Rho0 * dsig(k) * D(i, j) * dx * dy;
+          Energy = Energy + CellMass * Grav * (D(i, j) * sigc(k) - Hc(i, j)) +
+                   0.5 * CellMass * (U(i, j, k) * U(i, j, k) + V(i, j, k) * V(i, j, k) + W(i, j, k) * W(i, j, k));
+        }
+      }
+    double MaxEta = -1e308, MinEta = 1e308, MaxU = 0.0, MaxV = 0.0, MaxW = 0.0;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        MaxEta = std::max(MaxEta, Eta(i, j));
+        MinEta = std::min(MinEta, Eta(i, j));
+        for (int k = Kbeg; k <= Kend; ++k) {
+          MaxU = std::max(MaxU, std::fabs(U(i, j, k)));
+          MaxV = std::max(MaxV, std::fabs(V(i, j, k)));
+          MaxW = std::max(MaxW, std::fabs(W(i, j, k)));
+        }
+      }
+    out[0] = MassVolume; out[1] = Energy; out[2] = MaxEta; out[3] = MinEta;
+    out[4] = MaxU; out[5] = MaxV; out[6] = MaxW;
+  }
 
   // ------------------------------------------------------- field access
   struct FieldRef { double* d = nullptr; int32_t* i = nullptr; size_t n = 0; };
@@ -1728,6 +1755,7 @@ int orc_eval_duvw(void* o, int istep) { return static_cast<Model*>(o)->eval_duvw
 void orc_sponge_damping(void* o) { static_cast<Model*>(o)->sponge_damping(); }
 int orc_step(void* o) { return static_cast<Model*>(o)->step(); }
 double orc_mass(void* o) { return static_cast<Model*>(o)->mass(); }
+void orc_statistics(void* o, double* out) { static_cast<Model*>(o)->statistics(out); }
 int orc_get_field(void* o, int f, void* out) {
   auto r = static_cast<Model*>(o)->field(f);
   if (!out || r.n == 0) return NHW_ERR_ARG;

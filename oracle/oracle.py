@@ -61,6 +61,8 @@ def lib():
             getattr(L, name).restype = None
         L.orc_mass.argtypes = [vp]
         L.orc_mass.restype = dbl
+        L.orc_statistics.argtypes = [vp, ctypes.c_void_p]
+        L.orc_statistics.restype = None
         L.orc_get_field.argtypes = [vp, i32, vp]
         L.orc_set_field.argtypes = [vp, i32, vp]
         L.orc_get_scalars.argtypes = [vp, ctypes.POINTER(NhwScalars)]
@@ -79,6 +81,9 @@ def lib():
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+STAT_KEYS = ("mass_volume", "energy", "max_eta", "min_eta", "max_u", "max_v", "max_w")
 
 
 class Oracle:
@@ -149,6 +154,12 @@ class Oracle:
 
     def mass(self) -> float:
         return lib().orc_mass(self._h)
+
+    def statistics(self) -> dict:
+        """statistics' figures (src/nhwave.F:3118-3160), in the reference's loop order."""
+        out = np.zeros(7)
+        lib().orc_statistics(self._h, out.ctypes.data)
+        return dict(zip(STAT_KEYS, out.tolist()))
 
     def scalars(self) -> NhwScalars:
         s = NhwScalars()

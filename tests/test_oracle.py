@@ -203,3 +203,22 @@ def test_flume_solitary_inflow_arrives_with_its_height(oracle_mod):
             peak, t_peak = v, o.scalars().time
     assert abs(peak - A) < 0.15 * A
     assert abs(t_peak - arrival) < 0.15
+
+
+def test_statistics_of_a_lake_at_rest(oracle_mod):
+    """statistics (src/nhwave.F:3118-3160) of a flat lake: with eta = 0 and
+    uniform sigma levels the potential energy from z = 0 is
+    -Rho0 g dx dy sum D^2 * sum_k dsig_k (1 - sigc_k) = -Rho0 g dx dy sum D^2 / 2,
+    the kinetic energy is zero, and MassVolume is sum D dx dy."""
+    from nhwave_gb300 import default_params
+    rng = np.random.default_rng(4)
+    M, N, K = 12, 7, 5
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.25, tol=1e-12, dt_ini=0.05)
+    depth = 2.0 + rng.uniform(0.0, 1.0, size=M * N)
+    o = oracle_mod.Oracle(p, depth)
+    st = o.statistics()
+    g = float(np.float32(9.81))
+    assert st["mass_volume"] == pytest.approx(depth.sum() * 0.5 * 0.25, rel=1e-14)
+    assert st["energy"] == pytest.approx(-0.5 * 1000.0 * g * 0.5 * 0.25 * (depth ** 2).sum(), rel=1e-6)
+    assert st["max_eta"] == 0.0 and st["min_eta"] == 0.0
+    assert st["max_u"] == st["max_v"] == st["max_w"] == 0.0
