@@ -209,6 +209,8 @@ class Ensemble final : public EnsembleBase {
       });
     for (int st = 0; st < order; ++st) {
       if (groups_solve) {
+        // each member's coarse operators (formed on its side stream) before the solves
+        for (size_t i = 0; i < m.size(); ++i) member(i, [&](Solver<T>* s) { s->ens_join_mg(); });
         join();
         if (opts.block_rows == 16) launch_solves<16>();
         else launch_solves<8>();

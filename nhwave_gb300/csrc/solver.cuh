@@ -183,6 +183,9 @@ class Solver final : public SolverBase {
     if (arena) cudaFree(arena);
     if (h_sc) cudaFreeHost(h_sc);
     if (h_out) cudaFreeHost(h_out);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (mg_st) cudaStreamDestroy(mg_st);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -353,6 +356,9 @@ class Solver final : public SolverBase {
       return NHW_OK;
     }
     NHW_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    NHW_CU(cudaStreamCreateWithFlags(&mg_st, cudaStreamNonBlocking));
+    NHW_CU(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    NHW_CU(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     cudaError_t e = cudaMalloc((void**)&arena, total);
     if (e != cudaSuccess) {
       set_last_error(std::string("cudaMalloc arena: ") + cudaGetErrorString(e));
@@ -597,6 +603,7 @@ class Solver final : public SolverBase {
     stage_pre(s);
   }
   int ens_solve() { return poisson_solve(); }   // phase-by-phase, loops in conditional nodes
+  void ens_join_mg() { join_mg(); }   // before the ensemble's own solve (persistent groups)
   void ens_reset_counts() {
     for (auto& c : cap_counts) c = 0;
     cap_solves = 0;
@@ -778,13 +785,29 @@ class Solver final : public SolverBase {
   }
   // generate_coef_rhs (src/pressure.F:475-840), line factors, initial guess
   // and the multigrid coarse operators
+  // The coarse multigrid operators (Galerkin products and line factors)
+  // depend on level 0's operator alone: they are formed on a second stream,
+  // forked after the assembly, while level 0's line factors, the initial
+  // guess and the first FP64 residual run on the main one; join_mg() merges
+  // the streams before the first V-cycle.  In a captured graph the fork and
+  // join are edges of the graph.
+  cudaStream_t mg_st = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool mg_forked = false;
+  void join_mg() {
+    if (!mg_forked) return;
+    cudaStreamWaitEvent(st, ev_join, 0);
+    mg_forked = false;
+  }
   void poisson_setup() {
     incols(OpColFactors{});
     cells(OpPoissonCoef{});
     if (kFP32) cells(OpCoefToT{});
-    incols(OpLineFactor{});
-    cells(OpXFromP{});
-    if (use_mg)
+    if (use_mg && mg.size() > 1) {
+      cudaEventRecord(ev_fork, st);
+      cudaStreamWaitEvent(mg_st, ev_fork, 0);
+      cudaStream_t main_st = st;
+      st = mg_st;
       for (size_t l = 1; l < mg.size(); ++l) {
         MGL<T> f = mg[l - 1];
         MGL<T>& c = mg[l];
@@ -793,6 +816,12 @@ class Solver final : public SolverBase {
         });
         L("mg_factor", [&] { k_mg_factor<T><<<cdiv((long long)c.M * c.N, 256), 256, 0, st>>>(c, (T*)c.lcp, (T*)c.linv); });
       }
+      cudaEventRecord(ev_join, st);
+      st = main_st;
+      mg_forked = true;
+    }
+    incols(OpLineFactor{});
+    cells(OpXFromP{});
   }
   // P from the solution, ghosts mirrored (src/pressure.F:185-239)
   void poisson_finish() {
@@ -801,6 +830,7 @@ class Solver final : public SolverBase {
   }
   int poisson_solve() {
     if (use_persistent) {
+      join_mg();
       // count, generation and error word of the solve's grid barrier start at zero
       NHW_CU(cudaMemsetAsync(&S.sc->bar_count, 0, 3 * sizeof(unsigned int), st));
       const int gated = capturing ? 1 : 0;
@@ -835,6 +865,7 @@ class Solver final : public SolverBase {
       S.h_ir = new_handle();      // before the kernels that set them are captured
       S.h_inner = new_handle();
       L("res64", [&] { k_res64<T, true><<<red_blocks(), 256, 0, st>>>(S); });
+      join_mg();
       cond_node(S.h_ir, cudaGraphCondTypeWhile, [&] {
         inner_init();
         cond_node(S.h_inner, cudaGraphCondTypeWhile, [&] { one_iteration(); }, 2);
@@ -845,6 +876,7 @@ class Solver final : public SolverBase {
     }
     // host-driven loops over the same device-side decisions
     L("res64", [&] { k_res64<T, true><<<red_blocks(), 256, 0, st>>>(S); });
+    join_mg();
     int rc = pull_scalars();
     if (rc) return rc;
     while (h_sc->ir_go) {
