@@ -96,7 +96,8 @@ typedef struct nhw_params {
   int32_t itmax; double tol;               /* ITMAX TOL                               */
   int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
                                               2 no-slip wall; BC_X0 = 3 wave inflow
-                                              with a LEF_* wavemaker                  */
+                                              with a LEF_* wavemaker; BC_Xn = 6
+                                              Orlanski radiation (open east side)     */
   int32_t bc_z0;                           /* BC_Z0 (1)                               */
   double  visc;                            /* VISCOSITY (initial Cmu)                 */
   double  slat;                            /* slat -> fcor                            */

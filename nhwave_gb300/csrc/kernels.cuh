@@ -512,7 +512,8 @@ struct OpFluxX {
         Ex = (R)0; Fx = hydro<R>(reR, rh0); Gx = (R)0; Hx = (R)0;
       }
     }
-    if (f == S.IE + 1) { Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0; }
+    // east wall; an open (Orlanski) east face keeps its Riemann fluxes
+    if (f == S.IE + 1 && S.bc_xn != 6) { Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0; }
     if (mR == 0) {
       Ex = (R)0; Gx = (R)0; Hx = (R)0;
       Fx = (f == S.IB) ? (R)0 : hydro<R>(reL, rh0) * (R)mL;
@@ -702,7 +703,15 @@ struct OpWlBcEta {
     const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
     if (i < S.IB && S.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157); corners copy their row's value
       S.D[c] = 2.0 * S.Din[mj] - S.D[i2(S, mi, mj)];
-    else if (mi != i || mj != j)
+    else if (i > S.IE && S.bc_xn == 6) {
+      // Orlanski radiation (src/nhwave.F:5197-5206) from the last two steps'
+      // eta; corner rows copy their mirrored row's value, as the y pass does
+      const long long a = i2(S, i - 1, mj), b = i2(S, i - 2, mj), g = i2(S, i, mj);
+      double Cg = -(S.Eta0[a] - S.Eta00[a] + kOrlSmall) / (S.Eta00[a] - S.Eta00[b] + kOrlSmall);
+      Cg = dmax_(dmin_(Cg, 1.0), 0.0);
+      const double eta = Cg * S.Eta0[a] + (1.0 - Cg) * S.Eta0[g];
+      S.D[c] = S.Hc[g] + eta;
+    } else if (mi != i || mj != j)
       S.D[c] = S.D[i2(S, mi, mj)];
     S.Eta[c] = S.D[c] - S.Hc[c];
   }
@@ -777,6 +786,17 @@ struct OpVelBcLat {
       S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
       S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
       S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
+    } else if (jj && i > S.IE && S.bc_xn == 6) {  // Orlanski radiation (src/nhwave.F:4599-4621)
+      const long long a = i3(S, i - 1, j, k), b = i3(S, i - 2, j, k);
+      auto orl = [&](const T* X0, const T* X00) -> double {
+        double Cg = -((double)X0[a] - (double)X00[a] + kOrlSmall) / ((double)X00[a] - (double)X00[b] + kOrlSmall);
+        Cg = dmax_(dmin_(Cg, 1.0), 0.0);
+        return Cg * (double)X0[a] + (1.0 - Cg) * (double)X0[o];
+      };
+      const T u = (T)orl(S.U0, S.U00), v = (T)orl(S.V0, S.V00), w = (T)orl(S.W0, S.W00);
+      const double d = S.D[i2(S, i, j)];
+      S.U[o] = u; S.V[o] = v; S.W[o] = w;
+      S.DU[o] = (T)(d * (double)u); S.DV[o] = (T)(d * (double)v); S.DW[o] = (T)(d * (double)w);
     } else if (jj) {  // west/east ghost columns of interior rows
       const int src = mirror(i, S.IB, S.IE);
       const T s = (T)((i < S.IB ? S.bc_x0 : S.bc_xn) == 1 ? 1 : -1);
@@ -1176,7 +1196,7 @@ struct OpOmegaX {
       SR = uL + (R)2.0 * pL;
     }
     R Ex = hll_d<R>(SL, SR, duL, duR, rdd);
-    if (f == S.IB || f == S.IE + 1) Ex = (R)0;
+    if (f == S.IB || (f == S.IE + 1 && S.bc_xn != 6)) Ex = (R)0;
     if (f == S.IB && S.bc_x0 == 3) Ex = (R)(S.Din[j] * S.Uin[j + S.Nloc * k]);   // src/nhwave.F:1564-1566
     S.Ex[i3(S, f, j, k)] = Ex;
   }

@@ -23,8 +23,9 @@ int check_params(const nhw_params& p) {
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
-  for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
+  for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+  if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
   const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;

@@ -103,7 +103,12 @@ __global__ void __launch_bounds__(256) k_update_vars(Dev<T> S, long long n2, lon
     S.DU0[t] = S.DU[t];
     S.DV0[t] = S.DV[t];
     S.DW0[t] = S.DW[t];
+    if (S.U0) {   // Orlanski boundary: the previous step's velocities move back one level
+      S.U00[t] = S.U0[t]; S.V00[t] = S.V0[t]; S.W00[t] = S.W0[t];
+      S.U0[t] = S.U[t]; S.V0[t] = S.V[t]; S.W0[t] = S.W[t];
+    }
     if (t < n2) {
+      if (S.Eta00) S.Eta00[t] = S.Eta0[t];
       S.D0[t] = S.D[t];
       S.Eta0[t] = S.Eta[t];
     }
@@ -265,6 +270,10 @@ class Solver final : public SolverBase {
     T** t3[] = {&S.U, &S.V, &S.W, &S.DU, &S.DV, &S.DW, &S.DU0, &S.DV0, &S.DW0, &S.Omega,
                 &S.Ex, &S.Fx, &S.Gx, &S.Hx, &S.Ey, &S.Fy, &S.Gy, &S.Hy, &S.Fz, &S.Gz, &S.Hz};
     for (auto pp : t3) add(pp, sizeof(T) * n3);
+    if (p.bc_xn == 6) {   // Orlanski boundary: two earlier time levels (checkpointed state)
+      add(&S.Eta00, sizeof(double) * n2);
+      for (T** pp : {&S.U0, &S.V0, &S.W0, &S.U00, &S.V00, &S.W00}) add(pp, sizeof(T) * n3);
+    }
     add(&S.P, sizeof(double) * n3);
     // west-boundary wave values, recomputed every step (after the checkpointed state)
     add(&S.Ein, sizeof(double) * S.Nloc);

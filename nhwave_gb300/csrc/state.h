@@ -28,6 +28,7 @@ constexpr int NCOEF = 15;      // Poisson stencil entries (src/pressure.F:276-27
 // i.e. rounded to single precision then widened.
 constexpr double kPi = (double)3.141592653f;
 constexpr double kSmall = (double)1.0e-16f;
+constexpr double kOrlSmall = (double)1.e-16f;   // the Orlanski boundary's 1.e-16 (default real)
 constexpr double kLarge = 10000000.0;
 constexpr double kGrav = (double)9.81f;
 constexpr double kRho0 = 1000.0;
@@ -107,6 +108,7 @@ struct Dev {
   const double *sig, *dsig, *sigc, *xc, *yc;
   // 2-D FP64 fields
   double *D, *D0, *Eta, *Eta0, *Hc, *Hc0, *Ho;
+  double* Eta00;               // Orlanski boundary (BC_Xn = 6) only, else nullptr
   double *Hfx, *Hfy, *Hfx0, *Hfy0, *DelxH, *DelyH, *DeltH, *DeltHo, *Delt2H;
   double *DelxEta, *DelyEta, *SourceX, *SourceY, *SourceC, *Sponge, *R1, *Wsx, *Wsy;
   double *EtaxL, *EtaxR, *EtayL, *EtayR;
@@ -142,6 +144,9 @@ struct Dev {
   T *lcp, *linv;      // line preconditioner factors [neq]
   T* sp0;             // colour-split copy of the level-0 smoother's operator (MGL::sp), or nullptr
   T *kx, *kr, *kr0, *kp, *kph, *kv, *ks, *ksh, *kt;
+  // velocities of the last two steps, read by the Orlanski boundary
+  // (BC_Xn = 6) only, else nullptr
+  T *U0, *V0, *W0, *U00, *V00, *W00;
   // GMRES (krylov.cuh): basis V [kGmMax+1][neq], preconditioned basis Z
   // [kGmMax][neq], Hessenberg / rotations / g / y in FP64 (gm), the current
   // column, y and 1/||w|| in T (gmT), wide reduction partials; nullptr unless

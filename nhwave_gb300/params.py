@@ -218,9 +218,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if p.bc_x0 == 3 and p.wavemaker not in (WM_LEF_LIN, WM_LEF_SOL):
         return "BC_X0=3 needs a LEF_LIN or LEF_SOL wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
-        ok = (1, 2, 3) if name == "bc_x0" else (1, 2)
+        ok = {"bc_x0": (1, 2, 3), "bc_xn": (1, 2, 6)}.get(name, (1, 2))
         if getattr(p, name) not in ok:
-            return f"{name.upper()}={getattr(p, name)} (walls 1/2 and the west inflow 3 are on the GPU path)"
+            return (f"{name.upper()}={getattr(p, name)} (walls 1/2, the west inflow 3 and the east "
+                    "Orlanski boundary 6 are on the GPU path)")
     if p.bc_z0 != 1:
         return "BC_Z0 must be 1 (free slip)"
     return None

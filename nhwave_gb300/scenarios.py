@@ -186,6 +186,12 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
     elif name == "tiny_flume_sol":
         out = wave_flume("SOL", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.05, sponge=1.5, **kw)
+    elif name == "tiny_open":
+        # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
+        out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)
+    elif name == "tiny_flume_open":
+        # linear wave fed in at the west and let out through an Orlanski east side, no sponge
+        out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, bc_xn=6, sponge_on=0, **kw)
     else:
         raise KeyError(name)
     p = out[0]

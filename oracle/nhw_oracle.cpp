@@ -66,6 +66,7 @@ const double Large = 10000000.0;
 const double Grav = (double)9.81f;
 const double Zero = 0.0;
 const double Rho0 = 1000.0;
+const double kOrlSmall = (double)1.e-16f;   // the Orlanski boundary's 1.e-16 (default real)
 const int Nghost = 2;
 
 inline double dmax(double a, double b) { return a > b ? a : b; }
@@ -118,13 +119,14 @@ struct Model {
 
   A1 x, xc, y, yc, sig, dsig, sigc;
   A2 Hc, Hc0, Ho, Hfx, Hfy, Hfx0, Hfy0, DeltH, DeltHo, Delt2H, DelxH, DelyH;
-  A2 D, D0, Eta, Eta0, SourceX, SourceY, SourceC, DxL, DxR, DyL, DyR;
+  A2 D, D0, Eta, Eta0, Eta00, SourceX, SourceY, SourceC, DxL, DxR, DyL, DyR;
   A2 EtaxL, EtaxR, EtayL, EtayR, DelxEta, DelyEta, Sponge, Wsx, Wsy, R1s;
   I2 Mask, Mask_Struct, Mask9;
   // west-boundary inflow (Ein_X0, Din_X0, Uin_X0, Vin_X0, Win_X0; src/mod_global.F)
   A1 Ein_X0, Din_X0;
   A2 Uin_X0, Vin_X0, Win_X0;
   A3 U, V, W, DU, DV, DW, DU0, DV0, DW0, P, Omega, Uf, Vf, Wf;
+  A3 U0, V0, W0, U00, V00, W00;   // earlier time levels, read by the Orlanski boundary
   A3 UxL, UxR, VxL, VxR, WxL, WxR, DUxL, DUxR, DVxL, DVxR, DWxL, DWxR;
   A3 UyL, UyR, VyL, VyR, WyL, WyR, DUyL, DUyR, DVyL, DVyR, DWyL, DWyR;
   A3 UzL, UzR, VzL, VzR, WzL, WzR;
@@ -144,8 +146,9 @@ struct Model {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
     if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
-    for (int b : {p.bc_xn, p.bc_y0, p.bc_yn})
+    for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
+    if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
     const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
@@ -161,13 +164,14 @@ struct Model {
     Ein_X0.init(Nloc); Din_X0.init(Nloc);
     for (A2* a : {&Uin_X0, &Vin_X0, &Win_X0}) a->init(Nloc, Kloc);
     sig.init(Kloc1); dsig.init(Kloc); sigc.init(Kloc);
-    for (A2* a : {&Hc, &Hc0, &Ho, &DeltH, &DeltHo, &Delt2H, &DelxH, &DelyH, &D, &D0, &Eta, &Eta0,
+    for (A2* a : {&Hc, &Hc0, &Ho, &DeltH, &DeltHo, &Delt2H, &DelxH, &DelyH, &D, &D0, &Eta, &Eta0, &Eta00,
                   &SourceX, &SourceY, &SourceC, &DelxEta, &DelyEta, &Sponge, &Wsx, &Wsy, &R1s})
       a->init(Mloc, Nloc);
     for (A2* a : {&Hfx, &Hfx0, &DxL, &DxR, &EtaxL, &EtaxR}) a->init(Mloc1, Nloc);
     for (A2* a : {&Hfy, &Hfy0, &DyL, &DyR, &EtayL, &EtayR}) a->init(Mloc, Nloc1);
     Mask.init(Mloc, Nloc); Mask_Struct.init(Mloc, Nloc); Mask9.init(Mloc, Nloc);
-    for (A3* a : {&U, &V, &W, &DU, &DV, &DW, &DU0, &DV0, &DW0, &P, &DelxU, &DelyU, &DelzU, &DelxV,
+    for (A3* a : {&U, &V, &W, &DU, &DV, &DW, &DU0, &DV0, &DW0, &U0, &V0, &W0, &U00, &V00, &W00, &P, &DelxU,
+                  &DelyU, &DelzU, &DelxV,
                   &DelyV, &DelzV, &DelxW, &DelyW, &DelzW, &DelxDU, &DelyDU, &DelxDV, &DelyDV,
                   &DelxDW, &DelyDW, &DelxSc, &DelySc})
       a->init(Mloc, Nloc, Kloc);
@@ -494,7 +498,13 @@ struct Model {
     compute_mask9();
   }
 
-  void update_vars() { D0 = D; Eta0 = Eta; DU0 = DU; DV0 = DV; DW0 = DW; }
+  // update_vars (src/nhwave.F:5459-5511): the time levels the step reads.
+  // Eta00, U00/V00/W00 and U0/V0/W0 feed only the Orlanski boundary, and
+  // start as zero (the reference never initialises them)
+  void update_vars() {
+    Eta00 = Eta0; U00 = U0; V00 = V0; W00 = W0;
+    D0 = D; Eta0 = Eta; U0 = U; V0 = V; W0 = W; DU0 = DU; DV0 = DV; DW0 = DW;
+  }
 
   // --------------------------------------------------------- source_terms
   double wave_dispersion(double Segma) {
@@ -1005,8 +1015,10 @@ struct Model {
           Ex(Ibeg, j, k) = Zero; Fx(Ibeg, j, k) = hydro(EtaxR(Ibeg, j), Hfx0(Ibeg, j));
           Gx(Ibeg, j, k) = Zero; Hx(Ibeg, j, k) = Zero;
         }
-        Ex(Iend1, j, k) = Zero; Fx(Iend1, j, k) = hydro(EtaxL(Iend1, j), Hfx0(Iend1, j));
-        Gx(Iend1, j, k) = Zero; Hx(Iend1, j, k) = Zero;
+        if (p.bc_xn != 6) {   // an open (Orlanski) east face keeps its Riemann fluxes
+          Ex(Iend1, j, k) = Zero; Fx(Iend1, j, k) = hydro(EtaxL(Iend1, j), Hfx0(Iend1, j));
+          Gx(Iend1, j, k) = Zero; Hx(Iend1, j, k) = Zero;
+        }
       }
     for (int i = Ibeg; i <= Iend; ++i)
       for (int k = Kbeg; k <= Kend; ++k) {
@@ -1055,7 +1067,16 @@ struct Model {
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = 2.0 * Din_X0(j) - D(Ibeg + i - 1, j);
       else
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);
-      for (int i = 1; i <= Nghost; ++i) D(Iend + i, j) = D(Iend - i + 1, j);
+      if (p.bc_xn == 6)   // Orlanski radiation (src/nhwave.F:5197-5206)
+        for (int i = 1; i <= Nghost; ++i) {
+          double Cg = -(Eta0(Iend + i - 1, j) - Eta00(Iend + i - 1, j) + kOrlSmall) /
+                      (Eta00(Iend + i - 1, j) - Eta00(Iend + i - 2, j) + kOrlSmall);
+          Cg = dmax(dmin(Cg, 1.0), 0.0);
+          Eta(Iend + i, j) = Cg * Eta0(Iend + i - 1, j) + (1.0 - Cg) * Eta0(Iend + i, j);
+          D(Iend + i, j) = Hc(Iend + i, j) + Eta(Iend + i, j);
+        }
+      else
+        for (int i = 1; i <= Nghost; ++i) D(Iend + i, j) = D(Iend - i + 1, j);
     }
     for (int i = 1; i <= Mloc; ++i)
       for (int j = 1; j <= Nghost; ++j) D(i, j) = D(i, Jbeg + Nghost - j);
@@ -1098,6 +1119,21 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = 1; i <= Nghost; ++i) {
+          if (p.bc_xn == 6) {   // Orlanski radiation (src/nhwave.F:4599-4621)
+            auto orl = [&](A3& X0, A3& X00) {
+              double Cg = -(X0(Iend + i - 1, j, k) - X00(Iend + i - 1, j, k) + kOrlSmall) /
+                          (X00(Iend + i - 1, j, k) - X00(Iend + i - 2, j, k) + kOrlSmall);
+              Cg = dmax(dmin(Cg, 1.0), 0.0);
+              return Cg * X0(Iend + i - 1, j, k) + (1.0 - Cg) * X0(Iend + i, j, k);
+            };
+            U(Iend + i, j, k) = orl(U0, U00);
+            V(Iend + i, j, k) = orl(V0, V00);
+            W(Iend + i, j, k) = orl(W0, W00);
+            DU(Iend + i, j, k) = D(Iend + i, j) * U(Iend + i, j, k);
+            DV(Iend + i, j, k) = D(Iend + i, j) * V(Iend + i, j, k);
+            DW(Iend + i, j, k) = D(Iend + i, j) * W(Iend + i, j, k);
+            continue;
+          }
           U(Iend + i, j, k) = -U(Iend - i + 1, j, k);
           V(Iend + i, j, k) = sxn * V(Iend - i + 1, j, k);
           W(Iend + i, j, k) = sxn * W(Iend - i + 1, j, k);
@@ -1514,7 +1550,7 @@ struct Model {
     for (int j = Jbeg; j <= Jend; ++j)
       for (int k = Kbeg; k <= Kend; ++k) {   // src/nhwave.F:1558-1580
         Ex(Ibeg, j, k) = p.bc_x0 == 3 ? Din_X0(j) * Uin_X0(j, k) : Zero;
-        Ex(Iend1, j, k) = Zero;
+        if (p.bc_xn != 6) Ex(Iend1, j, k) = Zero;
       }
     for (int i = Ibeg; i <= Iend; ++i)
       for (int k = Kbeg; k <= Kend; ++k) { Ey(i, Jbeg, k) = Zero; Ey(i, Jend1, k) = Zero; }

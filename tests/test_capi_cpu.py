@@ -44,7 +44,7 @@ def test_status_strings(gpu_lib):
 
 
 @pytest.mark.parametrize("field,value", [("viscous_flow", 1), ("barotropic", 0),
-                                         ("bc_x0", 3), ("bc_yn", 6), ("bc_z0", 2), ("Kglob", 65),
+                                         ("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 2), ("Kglob", 65),
                                          ("wavemaker", -1)])
 def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     from nhwave_gb300 import default_params, lib

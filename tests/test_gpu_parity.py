@@ -14,6 +14,8 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
+# plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east side
+OPEN_CASES = CASES + ["tiny_open"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -62,7 +64,7 @@ def test_setup_bit_exact(name, oracle_mod, gpu_lib):
 
 
 @pytest.mark.parametrize("hllc", [0, 1])
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", OPEN_CASES)
 def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
     """estimate_dt .. fluxes, and a hydrostatic eval_duvw, match operation for
     operation, with HLL and with HLLC face fluxes (src/nhwave.F:1705-1709)."""
@@ -138,7 +140,7 @@ def step_pinned(g, o):
                 obj.sponge_damping()
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", OPEN_CASES)
 def test_steps_fp64(name, oracle_mod, gpu_lib):
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod)
@@ -178,7 +180,7 @@ def test_slide_free_running(oracle_mod, gpu_lib):
     g.close()
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", OPEN_CASES)
 def test_steps_fp32_ir(name, oracle_mod, gpu_lib):
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod, precision=1, tol=1e-10)
@@ -219,13 +221,15 @@ def test_golden_fixtures(name, gpu_lib):
     g.close()
 
 
-FLUMES = ["tiny_flume_lin", "tiny_flume_sol"]
+# tiny_flume_open: LEF_LIN in at the west, out through an Orlanski east side
+FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_open"]
 
 
 @pytest.mark.parametrize("name", FLUMES)
 def test_flume_steps_fp64(name, oracle_mod, gpu_lib):
-    """Waves fed through the west boundary (BC_X0 = 3, LEF_LIN / LEF_SOL):
-    FP64 steps against the oracle.  The boundary values use cos/cosh/sinh,
+    """Waves fed through the west boundary (BC_X0 = 3, LEF_LIN / LEF_SOL),
+    one of them leaving through an open east side (BC_Xn = 6): FP64 steps
+    against the oracle.  The boundary values use cos/cosh/sinh,
     whose CUDA and host results may differ in the last bit, hence 1e-9."""
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod)

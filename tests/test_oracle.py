@@ -222,3 +222,31 @@ def test_statistics_of_a_lake_at_rest(oracle_mod):
     assert st["energy"] == pytest.approx(-0.5 * 1000.0 * g * 0.5 * 0.25 * (depth ** 2).sum(), rel=1e-6)
     assert st["max_eta"] == 0.0 and st["min_eta"] == 0.0
     assert st["max_u"] == st["max_v"] == st["max_w"] == 0.0
+
+
+def test_orlanski_east_side_lets_a_solitary_wave_out(oracle_mod):
+    """BC_Xn = 6 (Orlanski radiation, src/nhwave.F:4599-4621 and 5197-5206):
+    a solitary wave running into the east side leaves through it.  After the
+    crest reaches the side (t > 3 s) a wall reflects it at full height; the
+    open side keeps well under that (the radiation speed is estimated from
+    the last two steps' values, so part of the wave still comes back), and
+    water leaves the domain."""
+    from nhwave_gb300 import fields as F, scenarios as S
+
+    def run(bc_xn):
+        p, d, e, u = S.solitary_channel(M=80, N=3, K=4, dx=0.1, h=0.5, amp=0.05, x0=4.0, bc_xn=bc_xn)
+        p.tol, p.itmax = 1e-8, 5000
+        o = oracle_mod.Oracle(p, d, e, u)
+        m0, late = o.mass(), 0.0
+        while o.scalars().time < 4.0:
+            assert o.step() == 0
+            if o.scalars().time > 3.0:
+                late = max(late, np.abs(o.get(F.ETA)[o.shape.interior(F.ETA)]).max())
+        return late, o.mass() / m0
+
+    wall, wall_mass = run(1)
+    open_, open_mass = run(6)
+    assert wall > 0.9 * 0.05
+    assert open_ < 0.75 * wall
+    assert wall_mass == pytest.approx(1.0, abs=1e-4)
+    assert open_mass < wall_mass - 1e-3
