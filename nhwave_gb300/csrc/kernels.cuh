@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <type_traits>
+#include "cnoidal.h"
 #include "state.h"
 
 namespace nhw {
@@ -190,7 +191,8 @@ __device__ __forceinline__ void reduce_finalize(const Dev<T>& S, double (&v)[NV]
 
 // =========================================================================
 //   update_wave_bc: waves fed through the west boundary (BC_X0 = 3)
-//   (src/nhwave.F:5514-5565; LEF_LIN src/waves.F:808-855, LEF_SOL 869-903)
+//   (src/nhwave.F:5514-5565; LEF_LIN src/waves.F:808-855, LEF_SOL 869-903,
+//   LEF_STK 518-560, LEF_CON 92-170)
 // =========================================================================
 // one thread per row j (all Nloc rows for Ein/Din, interior rows for the
 // velocities), evaluated at the step's new TIME
@@ -241,6 +243,50 @@ struct OpWaveBC {
         S.Win[j + Nl * k] = -C2 * Zlev / Dep *
                             ((1.0 - 0.5 * E / Dep) * D1 +
                              (double)(1.0f / 3.0f) * (Dep * Dep) * (1.0 - 0.5 * (Zlev * Zlev) / (Dep * Dep)) * D3);
+        S.Vin[j + Nl * k] = 0.0;
+      }
+    } else if (S.lef == 5) {   // LEF_STK: second-order Stokes wave
+      const double A = S.lef_amp, Sg = S.lef_segma, wk = S.lef_wn, sh = S.lef_shd;
+      const double ph = kPi / 2 - Sg * TIME;
+      const double cs = cos(ph), sn = sin(ph), cs2 = cos(2. * ph), sn2 = sin(2. * ph);
+      const double E = 0.5 * A * cs + S.lef_e2 * cs2;
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      const double sh4 = (sh * sh) * (sh * sh);
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        S.Uin[j + Nl * k] = 0.5 * A * Sg * cosh(wk * Zlev) / sh * cs + S.lef_u2 * cosh(2. * wk * Zlev) / sh4 * cs2;
+        S.Win[j + Nl * k] = 0.5 * A * Sg * sinh(wk * Zlev) / sh * sn + S.lef_u2 * sinh(2. * wk * Zlev) / sh4 * sn2;
+        S.Vin[j + Nl * k] = 0.0;
+      }
+    } else if (S.lef == 6) {   // LEF_CON: cnoidal wave
+      const double A = S.lef_amp, Dep = S.lef_dep, m = S.con_mod, ck = S.con_ck, L = S.con_len, Yt = S.con_ytr;
+      const double Xcn = cnoidal_cn(S.con_x0 + 2.0 * ck * (-(TIME / S.lef_per)), m);
+      const double cn2 = Xcn * Xcn;
+      const double E = Yt + A * cn2;
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      const double Xsn = sqrt(1.0 - cn2), Xdn = sqrt(1.0 - m * (1.0 - cn2));
+      const double sn2 = Xsn * Xsn, dn2 = Xdn * Xdn, DY = Dep + Yt;
+      const double c0 = sqrt(kGrav * Dep);
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        const double Z2 = Zlev * Zlev;
+        S.Uin[j + Nl * k] =
+            c0 * (-5. / 4. + 3. * DY / 2.0 / Dep - (DY * DY) / 4. / (Dep * Dep) +
+                  (3. * A / 2. / Dep - DY * A / 2. / (Dep * Dep)) * cn2 - (A * A) / 4. / (Dep * Dep) * (cn2 * cn2) -
+                  8.0 * A * (ck * ck) / (L * L) * (Dep / 3 - Z2 / 2 / Dep) *
+                      (-((m * m) * sn2 * cn2) + cn2 * dn2 - sn2 * dn2)) -
+            S.lef_stokes * 1.0;
+        S.Win[j + Nl * k] = c0 * Zlev * 2 * A * ck / L / Dep *
+                            (1 + DY / Dep + A / Dep * cn2 +
+                             32 * (ck * ck) / 3 / (L * L) * ((Dep * Dep) - Z2 / 2) *
+                                 ((m * m) * sn2 - (m * m) * cn2 - dn2)) *
+                            Xsn * Xcn * Xdn;
         S.Vin[j + Nl * k] = 0.0;
       }
     }

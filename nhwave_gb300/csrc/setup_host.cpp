@@ -10,6 +10,8 @@
 #include <cmath>
 #include <cstring>
 
+#include "cnoidal.h"
+
 namespace nhw {
 namespace {
 const double kPiH = (double)3.141592653f;
@@ -26,18 +28,63 @@ int check_params(const nhw_params& p) {
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-  const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
+  const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL ||
+                   p.wavemaker == NHW_WM_LEF_STK || p.wavemaker == NHW_WM_LEF_CON;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
-  if (p.wavemaker < 0 || p.wavemaker > 4) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_CON) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
   if (p.wavemaker && !(p.per_wave > 0 && p.dep_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker == NHW_WM_LEF_CON && !(p.amp_wave > 0)) return NHW_ERR_ARG;
   return NHW_OK;
 }
+
+namespace {
+// cnoidal (src/waves.F:184-220): Newton iteration for the elliptic parameter
+// m of a cnoidal wave of height H in depth d with period T, then its length
+// L and trough level x2.  Returns false when m leaves (0, 1].
+bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m) {
+  m = 0.99999999;
+  for (int n = 1;; ++n) {
+    if (!(m > 0.0 && m <= 1.0)) return false;
+    const double ck = cnoidal_ck(m), ce = cnoidal_ce(m);
+    const double xa = m * d + 2.0 * H - m * H - 3.0 * H * ce / ck -
+                      16.0 * (d * d * d) * (m * m) * (ck * ck) / 3.0 / kGravH / H / (T * T);
+    if (std::fabs(xa) <= (double)1.0e-8f || n > 1000) break;
+    const double xb = d - H + 3.0 * H / 2.0 / m / (1.0 - m) / (ck * ck) *
+                                  ((1.0 - m) * (ck * ck) + ce * ce - 2.0 * (1.0 - m) * ck * ce) -
+                      16.0 * (d * d * d) * m * ck / 3.0 / kGravH / (1.0 - m) / H / (T * T) *
+                          ((1.0 - m) * ck + ce);
+    m = m - xa / xb;
+  }
+  if (!(m > 0.0 && m <= 1.0)) return false;
+  const double ck = cnoidal_ck(m), ce = cnoidal_ce(m);
+  L = 4.0 * ck * d * std::sqrt(m * d / H / 3.0);
+  x2 = H / m * (1.0 - m - ce / ck);
+  return std::isfinite(L) && std::isfinite(x2);
+}
+
+// Start phase of the cnoidal boundary wave (src/waves.F:106-130): bisection
+// for the phase in [0, 1] where the elevation crosses zero, to 1e-6.
+bool cnoidal_start(double Ytrough, double A, double m, double& Xstart) {
+  const double ck = cnoidal_ck(m);
+  double Zup = 1.0, Zlow = 0.0, Zmid = (Zup + Zlow) / 2.0;
+  for (int nn = 1;; ++nn) {
+    const double cn = cnoidal_cn(Zmid * 0.5 * ck, m);
+    const double Zero1 = Ytrough + A * (cn * cn);
+    if (std::fabs(Zero1) <= (double)1.0e-6f) break;
+    if (nn > 1000) return false;   // the reference stops the run here
+    if (Zero1 < 0.0) Zup = Zmid; else Zlow = Zmid;
+    Zmid = (Zup + Zlow) / 2.0;
+  }
+  Xstart = Zmid;
+  return true;
+}
+}  // namespace
 
 double wave_number(double Segma, double Dep) {
   double Wn = (Segma * Segma) / (kGravH * std::pow(std::tanh(Segma * Segma * Dep / kGravH), 0.5));
@@ -268,6 +315,30 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     h.lef_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
     h.lef_xstart = 4.0 * Dep / std::sqrt(A / Dep);
     h.lef_c2 = std::sqrt(kGravH * Dep);
+  } else if (p.wavemaker == NHW_WM_LEF_STK) {   // src/waves.F:531-540
+    const double A = p.amp_wave;
+    h.lef_segma = 2.0 * kPiH / p.per_wave;
+    h.lef_wn = wave_number(h.lef_segma, p.dep_wave);
+    const double wk = h.lef_wn, Dep = p.dep_wave;
+    h.lef_shd = std::sinh(wk * Dep);
+    const double sh = h.lef_shd;
+    // second-order elevation and velocity amplitudes, in the reference's
+    // left-to-right order up to the trigonometric factor of the step
+    h.lef_e2 = (A * A) * wk / 16. * std::cosh(wk * Dep) / (sh * sh * sh) * (2.0 + std::cosh(2. * wk * Dep));
+    h.lef_u2 = (double)(3.f / 16.f) * (A * A) * h.lef_segma * wk;
+  } else if (p.wavemaker == NHW_WM_LEF_CON) {   // src/waves.F:100-140
+    const double A = p.amp_wave, Dep = p.dep_wave;
+    double L = 0, Yt = 0, m = 0, Xstart = 0;
+    if (!cnoidal_params(A, Dep, p.per_wave, L, Yt, m)) return NHW_ERR_ARG;
+    if (!cnoidal_start(Yt, A, m, Xstart)) return NHW_ERR_ARG;
+    double a[kCnMax], c[kCnMax];
+    if (!(std::fabs(c[cn_agm(m, a, c)]) < kCnEps)) return NHW_ERR_ARG;   // sequence must fit kCnMax
+    h.con_mod = m;
+    h.con_len = L;
+    h.con_ytr = Yt;
+    h.con_ck = cnoidal_ck(m);
+    h.con_x0 = Xstart * 0.5 * h.con_ck;
+    h.lef_stokes = kGravH * (A * A) / (L / p.per_wave) / Dep / 8.0;
   }
   return NHW_OK;
 }

@@ -19,9 +19,11 @@ struct HostInit {
   int it_order = 1;
   // host-computed wavemaker constants
   double wm_segma = 0, wm_celerity = 0, wm_wnumy = 0, wm_atmp = 0, wm_xstart = 0;
-  // LEF_* boundary waves (src/waves.F:808-903)
+  // LEF_* boundary waves (src/waves.F:92-170, 518-560, 808-903)
   double lef_segma = 0, lef_wn = 0, lef_shd = 0, lef_stokes = 0, lef_sinth = 0, lef_costh = 0;
   double lef_cel = 0, lef_atmp = 0, lef_xstart = 0, lef_c2 = 0;
+  double lef_e2 = 0, lef_u2 = 0;                          // LEF_STK second-order amplitudes
+  double con_mod = 0, con_len = 0, con_ytr = 0, con_ck = 0, con_x0 = 0;   // LEF_CON
 };
 
 // Validate parameters against the path's scope; NHW_OK or an error code.

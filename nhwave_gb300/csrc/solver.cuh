@@ -637,8 +637,10 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL) ? p.wavemaker : 0;
-    S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave;
+    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON) ? p.wavemaker : 0;
+    S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave; S.lef_per = p.per_wave;
+    S.lef_e2 = h.lef_e2; S.lef_u2 = h.lef_u2;
+    S.con_mod = h.con_mod; S.con_len = h.con_len; S.con_ytr = h.con_ytr; S.con_ck = h.con_ck; S.con_x0 = h.con_x0;
     S.lef_segma = h.lef_segma; S.lef_wn = h.lef_wn; S.lef_shd = h.lef_shd; S.lef_stokes = h.lef_stokes;
     S.lef_sinth = h.lef_sinth; S.lef_costh = h.lef_costh;
     S.lef_cel = h.lef_cel; S.lef_atmp = h.lef_atmp; S.lef_xstart = h.lef_xstart; S.lef_c2 = h.lef_c2;

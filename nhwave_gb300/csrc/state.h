@@ -92,11 +92,14 @@ struct Dev {
   double wm_segma, wm_celerity, wm_amp, wm_wnumy, wm_xw, wm_xe, wm_ys, wm_yn;
   double wm_atmp, wm_xstart;
   int wm_i0, wm_i1;                // interior i range of the source strip (xc is monotonic)
-  // waves through the west boundary (BC_X0 = 3): LEF_LIN / LEF_SOL constants
-  // (host-computed, src/waves.F:808-903) and the boundary values of the step
-  int lef;                         // 0 none, 3 LEF_LIN, 4 LEF_SOL (nhw_wavemaker)
-  double lef_amp, lef_dep, lef_segma, lef_wn, lef_shd, lef_stokes, lef_sinth, lef_costh;
+  // waves through the west boundary (BC_X0 = 3): LEF_LIN / LEF_SOL /
+  // LEF_STK / LEF_CON constants (host-computed, src/waves.F:92-170,
+  // 518-560, 808-903) and the boundary values of the step
+  int lef;                         // 0 none, else the nhw_wavemaker (3 .. 6)
+  double lef_amp, lef_dep, lef_per, lef_segma, lef_wn, lef_shd, lef_stokes, lef_sinth, lef_costh;
   double lef_cel, lef_atmp, lef_xstart, lef_c2;
+  double lef_e2, lef_u2;                           // LEF_STK second-order amplitudes
+  double con_mod, con_len, con_ytr, con_ck, con_x0;   // LEF_CON: m, L, trough, K(m), start phase
   double *Ein, *Din;               // [Nloc] Ein_X0, Din_X0
   double *Uin, *Vin, *Win;         // [Kloc][Nloc] Uin_X0 .. (index j + Nloc*k)
   // sponge current

@@ -146,15 +146,16 @@ def ensemble(n: int, seed: int = 2024, **kw):
 def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5, amp=0.02, per=1.5,
                sponge=2.0, **kw):
     """Flat flume fed through its west boundary (BC_X0 = 3): a linear wave
-    (LEF_LIN, amplitude `amp`, period `per`) or a solitary wave (LEF_SOL,
-    height `amp`); sponge layer and wall at the east end, walls along the
-    sides; at rest initially."""
-    from .params import WM_LEF_LIN, WM_LEF_SOL
+    (LEF_LIN, amplitude `amp`, period `per`), a solitary wave (LEF_SOL,
+    height `amp`), a second-order Stokes wave (LEF_STK, amplitude `amp`) or a
+    cnoidal wave (LEF_CON, height `amp`); sponge layer and wall at the east
+    end, walls along the sides; at rest initially."""
+    from .params import WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK
     p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
                        dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
                        tol=1e-8, itmax=1000, total_time=20.0)
     p.bc_x0 = 3
-    p.wavemaker = WM_LEF_LIN if kind == "LIN" else WM_LEF_SOL
+    p.wavemaker = {"LIN": WM_LEF_LIN, "SOL": WM_LEF_SOL, "STK": WM_LEF_STK, "CON": WM_LEF_CON}[kind]
     p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
     p.sponge_on = 1
     p.sponge_east_width = sponge
@@ -186,6 +187,11 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
     elif name == "tiny_flume_sol":
         out = wave_flume("SOL", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.05, sponge=1.5, **kw)
+    elif name == "tiny_flume_stk":
+        out = wave_flume("STK", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.04, per=1.5, sponge=1.5, **kw)
+    elif name == "tiny_flume_con":
+        # Ursell number H L^2 / h^3 of about 34: elliptic parameter m = 0.91
+        out = wave_flume("CON", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.1, per=3.0, sponge=1.5, **kw)
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)

@@ -69,6 +69,73 @@ const double Rho0 = 1000.0;
 const double kOrlSmall = (double)1.e-16f;   // the Orlanski boundary's 1.e-16 (default real)
 const int Nghost = 2;
 
+// ---------------------------------------------------------------- cnoidal
+// cnoidal_cn, cnoidal_ck, cnoidal_ce (src/waves.F:225-370): the AGM
+// sequence of the parameter m, stopped when |c| < 1.0e-15 (default real) or
+// after 1000 terms; K = (pi/2)/a_N with a default-real pi literal;
+// E = K (1 - sum 2^(n-2) c_n^2); cn by descending Landen steps from
+// phi_N = 2^(N-1) a_N u.
+const double CnPi = (double)3.1415926535897932384626f;
+int agm_terms(double mod, double* a, double* c) {
+  double a0 = 1.0, b0 = std::sqrt(1.0 - mod), c0 = std::sqrt(mod);
+  int n = 1;
+  a[n] = a0; c[n] = c0;
+  while (!(std::fabs(c0) < (double)1.0e-15f || n > 1000)) {
+    n = n + 1;
+    const double a1 = (a0 + b0) / 2.0, b1 = std::sqrt(a0 * b0), c1 = (a0 - b0) / 2.0;
+    a0 = a1; b0 = b1; c0 = c1;
+    a[n] = a0; c[n] = c0;
+  }
+  return n;
+}
+double cnoidal_cn(double u, double mod) {
+  std::vector<double> a(1002), c(1002), y(1002);
+  const int n = agm_terms(mod, a.data(), c.data());
+  y[n] = std::pow(2.0, n - 1) * a[n] * u;
+  for (int i = n - 1; i >= 1; --i) y[i] = (y[i + 1] + std::asin(c[i + 1] / a[i + 1] * std::sin(y[i + 1]))) / 2.0;
+  return std::cos(y[1]);
+}
+double cnoidal_ck(double mod) {
+  std::vector<double> a(1002), c(1002);
+  const int n = agm_terms(mod, a.data(), c.data());
+  return CnPi / 2.0 / a[n];
+}
+double cnoidal_ce(double mod) {
+  std::vector<double> a(1002), c(1002);
+  const int n = agm_terms(mod, a.data(), c.data());
+  const double ck = CnPi / 2.0 / a[n];
+  double sum = 0.0;
+  for (int k1 = 1; k1 <= n; ++k1) sum = sum + std::pow(2.0, k1 - 2) * (c[k1] * c[k1]);
+  return ck * (1.0 - sum);
+}
+// cnoidal (src/waves.F:184-220): Newton iteration for m from 0.99999999,
+// then the wave length l and the trough level x2 (c, the celerity, is unused
+// by the boundary).  False when m leaves (0, 1], where the reference's
+// square roots turn to NaN.
+bool cnoidal(double height, double depth, double period, double& l, double& x2, double& mod) {
+  mod = 0.99999999;
+  int n = 0;
+  while (true) {
+    n = n + 1;
+    if (!(mod > 0.0 && mod <= 1.0)) return false;
+    const double xa = mod * depth + 2.0 * height - mod * height - 3.0 * height * cnoidal_ce(mod) / cnoidal_ck(mod) -
+                      16.0 * (depth * depth * depth) * (mod * mod) * (cnoidal_ck(mod) * cnoidal_ck(mod)) / 3.0 / Grav /
+                          height / (period * period);
+    if (std::fabs(xa) <= (double)1.0e-8f || n > 1000) break;
+    const double ck = cnoidal_ck(mod), ce = cnoidal_ce(mod);
+    const double xb = depth - height +
+                      3.0 * height / 2.0 / mod / (1.0 - mod) / (ck * ck) *
+                          ((1.0 - mod) * (ck * ck) + ce * ce - 2.0 * (1.0 - mod) * ck * ce) -
+                      16.0 * (depth * depth * depth) * mod * ck / 3.0 / Grav / (1.0 - mod) / height /
+                          (period * period) * ((1.0 - mod) * ck + ce);
+    mod = mod - xa / xb;
+  }
+  if (!(mod > 0.0 && mod <= 1.0)) return false;
+  l = 4.0 * cnoidal_ck(mod) * depth * std::sqrt(mod * depth / height / 3.0);
+  x2 = height / mod * (1.0 - mod - cnoidal_ce(mod) / cnoidal_ck(mod));
+  return std::isfinite(l) && std::isfinite(x2);
+}
+
 inline double dmax(double a, double b) { return a > b ? a : b; }
 inline double dmin(double a, double b) { return a < b ? a : b; }
 
@@ -149,8 +216,14 @@ struct Model {
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-    const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL;
+    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+    if (p.wavemaker == NHW_WM_LEF_CON) {   // the reference stops when these fail
+      double l, x2, m, xs;
+      if (!(p.amp_wave > 0) || !cnoidal(p.amp_wave, p.dep_wave, p.per_wave, l, x2, m) ||
+          !cnoidal_start(x2, m, xs))
+        return NHW_ERR_ARG;
+    }
     if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
     // index (src/initialize.F:1339-1419), serial build
     Mloc = p.Mglob + 2 * Nghost; Nloc = p.Nglob + 2 * Nghost; Kloc = p.Kglob + 2 * Nghost;
@@ -522,10 +595,34 @@ struct Model {
     return Wn;
   }
 
+  // Start phase of the cnoidal boundary wave (src/waves.F:106-130):
+  // bisection on [0, 1] for the zero crossing of the elevation.
+  bool cnoidal_start(double Ytrough, double Mod1, double& Xstart) {
+    double Zup = 1.0, Zlow = 0.0, Zmid = (Zup + Zlow) / 2.0;
+    int nn = 0;
+    while (true) {
+      nn = nn + 1;
+      const double cn = cnoidal_cn(Zmid * 0.5 * cnoidal_ck(Mod1), Mod1);
+      const double Zero1 = Ytrough + p.amp_wave * (cn * cn);
+      if (std::fabs(Zero1) <= (double)1.0e-6f) break;
+      if (nn > 1000) return false;
+      if (Zero1 < 0.0) {
+        Zup = Zmid;
+        Zmid = (Zup + Zlow) / 2.0;
+      } else {
+        Zlow = Zmid;
+        Zmid = (Zup + Zlow) / 2.0;
+      }
+    }
+    Xstart = Zmid;
+    return true;
+  }
+
   // ------------------------------------------------------ update_wave_bc
-  // Linear (LEF_LIN, src/waves.F:808-855) and solitary (LEF_SOL,
-  // src/waves.F:869-903) waves fed through the west boundary
-  // (src/nhwave.F:5514-5565), evaluated at the new TIME once per step.
+  // Linear (LEF_LIN, src/waves.F:808-855), solitary (LEF_SOL, :869-903),
+  // second-order Stokes (LEF_STK, :518-560) and cnoidal (LEF_CON, :92-170)
+  // waves fed through the west boundary (src/nhwave.F:5514-5565), evaluated
+  // at the new TIME once per step.
   void update_wave_bc() {
     if (p.wavemaker == NHW_WM_LEF_LIN) {
       const double Segma = 2.0 * pi / p.per_wave;
@@ -580,6 +677,64 @@ struct Model {
           Vin_X0(j, k) = 0.0;
         }
       }
+    } else if (p.wavemaker == NHW_WM_LEF_STK) {
+      const double A = p.amp_wave, Dep = p.dep_wave;
+      const double Segma = 2.0 * pi / p.per_wave;
+      const double Wave_Number = wave_dispersion(Segma);
+      const double sh = std::sinh(Wave_Number * Dep);
+      for (int j = 1; j <= Nloc; ++j) {
+        Ein_X0(j) = 0.5 * A * std::cos(pi / 2 - Segma * TIME) +
+                    (A * A) * Wave_Number / 16. * std::cosh(Wave_Number * Dep) / (sh * sh * sh) *
+                        (2.0 + std::cosh(2. * Wave_Number * Dep)) * std::cos(2. * (pi / 2 - Segma * TIME));
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+      }
+      const double sh4 = (sh * sh) * (sh * sh);
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j) {
+          const double Zlev = sigc(k) * Din_X0(j);
+          Uin_X0(j, k) = 0.5 * A * Segma * std::cosh(Wave_Number * Zlev) / sh * std::cos(pi / 2 - Segma * TIME) +
+                         3. / 16. * (A * A) * Segma * Wave_Number * std::cosh(2. * Wave_Number * Zlev) / sh4 *
+                             std::cos(2. * (pi / 2 - Segma * TIME));
+          Win_X0(j, k) = 0.5 * A * Segma * std::sinh(Wave_Number * Zlev) / sh * std::sin(pi / 2 - Segma * TIME) +
+                         3. / 16. * (A * A) * Segma * Wave_Number * std::sinh(2. * Wave_Number * Zlev) / sh4 *
+                             std::sin(2. * (pi / 2 - Segma * TIME));
+          Vin_X0(j, k) = 0.0;
+        }
+    } else if (p.wavemaker == NHW_WM_LEF_CON) {
+      const double A = p.amp_wave, Dep = p.dep_wave;
+      double Wave_Length = 0, Ytrough = 0, Mod1 = 0, Xstart = 0;
+      cnoidal(A, Dep, p.per_wave, Wave_Length, Ytrough, Mod1);   // checked at create
+      cnoidal_start(Ytrough, Mod1, Xstart);
+      const double ck = cnoidal_ck(Mod1);
+      for (int j = 1; j <= Nloc; ++j) {
+        const double cn = cnoidal_cn(Xstart * 0.5 * ck + 2.0 * ck * (-(TIME / p.per_wave)), Mod1);
+        Ein_X0(j) = Ytrough + A * (cn * cn);
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+      }
+      const double Stokes_Drift = Grav * (A * A) / (Wave_Length / p.per_wave) / Dep / 8.0;
+      const double Fact = 1.0;
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j) {
+          const double Zlev = sigc(k) * Din_X0(j);
+          const double Xcn = cnoidal_cn(Xstart * 0.5 * ck + 2.0 * ck * (-(TIME / p.per_wave)), Mod1);
+          const double Xsn = std::sqrt(1.0 - Xcn * Xcn);
+          const double Xdn = std::sqrt(1.0 - Mod1 * (1.0 - Xcn * Xcn));
+          const double c2 = Xcn * Xcn, s2 = Xsn * Xsn, d2 = Xdn * Xdn, m2 = Mod1 * Mod1;
+          Uin_X0(j, k) = std::sqrt(Grav * Dep) *
+                             (-5. / 4. + 3. * (Dep + Ytrough) / 2.0 / Dep -
+                              ((Dep + Ytrough) * (Dep + Ytrough)) / 4. / (Dep * Dep) +
+                              (3. * A / 2. / Dep - (Dep + Ytrough) * A / 2. / (Dep * Dep)) * c2 -
+                              (A * A) / 4. / (Dep * Dep) * (c2 * c2) -
+                              8.0 * A * (ck * ck) / (Wave_Length * Wave_Length) * (Dep / 3 - (Zlev * Zlev) / 2 / Dep) *
+                                  (-(m2 * s2 * c2) + c2 * d2 - s2 * d2)) -
+                         Stokes_Drift * Fact;
+          Win_X0(j, k) = std::sqrt(Grav * Dep) * Zlev * 2 * A * ck / Wave_Length / Dep *
+                         (1 + (Dep + Ytrough) / Dep + A / Dep * c2 +
+                          32 * (ck * ck) / 3 / (Wave_Length * Wave_Length) * ((Dep * Dep) - (Zlev * Zlev) / 2) *
+                              (m2 * s2 - m2 * c2 - d2)) *
+                         Xsn * Xcn * Xdn;
+          Vin_X0(j, k) = 0.0;
+        }
     }
   }
 
@@ -1835,5 +1990,14 @@ int orc_get_coef(void* o, double* coef15, double* rhs) {
 void orc_generate_coef_rhs(void* o) { static_cast<Model*>(o)->generate_coef_rhs(); }
 double orc_limiter(double a, double b) { return LIMITER(a, b); }
 double orc_wave_number(void* o, double segma) { return static_cast<Model*>(o)->wave_dispersion(segma); }
+// the AGM elliptic functions of the cnoidal boundary wave: 0 cn(u|m), 1 K(m), 2 E(m)
+double orc_elliptic(int what, double u, double m) {
+  return what == 0 ? cnoidal_cn(u, m) : what == 1 ? cnoidal_ck(m) : cnoidal_ce(m);
+}
+// cnoidal (src/waves.F:184-220): out[0..2] = wave length, trough level, m;
+// returns 0, or -1 when the iteration leaves (0, 1]
+int orc_cnoidal_wave(double height, double depth, double period, double* out) {
+  return cnoidal(height, depth, period, out[0], out[1], out[2]) ? 0 : -1;
+}
 
 }  // extern "C"

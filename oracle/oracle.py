@@ -75,6 +75,10 @@ def lib():
         L.orc_limiter.restype = dbl
         L.orc_wave_number.argtypes = [vp, dbl]
         L.orc_wave_number.restype = dbl
+        L.orc_elliptic.argtypes = [i32, dbl, dbl]
+        L.orc_elliptic.restype = dbl
+        L.orc_cnoidal_wave.argtypes = [dbl, dbl, dbl, vp]
+        L.orc_cnoidal_wave.restype = i32
         _lib = L
     return _lib
 

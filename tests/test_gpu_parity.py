@@ -221,16 +221,18 @@ def test_golden_fixtures(name, gpu_lib):
     g.close()
 
 
-# tiny_flume_open: LEF_LIN in at the west, out through an Orlanski east side
-FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_open"]
+# tiny_flume_open: LEF_LIN in at the west, out through an Orlanski east side;
+# tiny_flume_stk / _con: second-order Stokes and cnoidal waves fed in
+FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open"]
 
 
 @pytest.mark.parametrize("name", FLUMES)
 def test_flume_steps_fp64(name, oracle_mod, gpu_lib):
-    """Waves fed through the west boundary (BC_X0 = 3, LEF_LIN / LEF_SOL),
-    one of them leaving through an open east side (BC_Xn = 6): FP64 steps
-    against the oracle.  The boundary values use cos/cosh/sinh,
-    whose CUDA and host results may differ in the last bit, hence 1e-9."""
+    """Waves fed through the west boundary (BC_X0 = 3, LEF_LIN / LEF_SOL /
+    LEF_STK / LEF_CON), one of them leaving through an open east side
+    (BC_Xn = 6): FP64 steps against the oracle.  The boundary values use
+    cos/sin/cosh/sinh/asin, whose CUDA and host results may differ in the
+    last bit, hence 1e-9."""
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod)
     for n in range(20):

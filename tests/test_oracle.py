@@ -250,3 +250,86 @@ def test_orlanski_east_side_lets_a_solitary_wave_out(oracle_mod):
     assert open_ < 0.75 * wall
     assert wall_mass == pytest.approx(1.0, abs=1e-4)
     assert open_mass < wall_mass - 1e-3
+
+
+def _west_boundary_eta(o):
+    """Ein_X0 recovered from the west ghost column: wl_bc sets D there to
+    2 Din - D(Ibeg), so on a flat bed the mean of eta over the first ghost and
+    first interior column is Ein (row-averaged over the interior rows)."""
+    from nhwave_gb300 import fields as F
+    e = o.get(F.ETA)
+    return 0.5 * (e[2:-2, 1] + e[2:-2, 2]).mean()
+
+
+def test_elliptic_functions_against_scipy(oracle_mod):
+    """cnoidal_cn / cnoidal_ck / cnoidal_ce (src/waves.F:225-370) against
+    scipy's Jacobi cn and complete elliptic integrals (parameter m).  K and E
+    carry the single-precision pi literal of the reference (2.8e-8 relative)."""
+    sp = pytest.importorskip("scipy.special")
+    L = oracle_mod.lib()
+    for m in (0.1, 0.5, 0.9135, 0.999, 1.0 - 1e-8):
+        K, E = L.orc_elliptic(1, 0.0, m), L.orc_elliptic(2, 0.0, m)
+        assert K == pytest.approx(sp.ellipk(m), rel=1e-7), m
+        assert E == pytest.approx(sp.ellipe(m), rel=1e-7), m
+        for u in (0.0, 0.3, 1.1, -2.0, 0.5 * K, K):
+            assert L.orc_elliptic(0, u, m) == pytest.approx(sp.ellipj(u, m)[1], abs=1e-12), (u, m)
+
+
+def test_cnoidal_wave_parameters(oracle_mod):
+    """cnoidal (src/waves.F:184-220) for H = 0.1 m, h = 0.5 m, T = 3 s: the
+    trough level makes the mean elevation over a wave length zero, and the
+    length is the period times the celerity of the reference's formula."""
+    import ctypes
+    sp = pytest.importorskip("scipy.special")
+    out = (ctypes.c_double * 3)()
+    H, h, T = 0.1, 0.5, 3.0
+    assert oracle_mod.lib().orc_cnoidal_wave(H, h, T, out) == 0
+    L, yt, m = out
+    assert 0.85 < m < 0.95 and -H < yt < 0
+    K, E = sp.ellipk(m), sp.ellipe(m)
+    u = np.linspace(0.0, 2 * K, 20001)[:-1]
+    assert abs((yt + H * sp.ellipj(u, m)[1] ** 2).mean()) < 1e-6 * H
+    g = float(np.float32(9.81))
+    c = math.sqrt(g * h * (1.0 + H / h / m * (-m + 2.0 - 3.0 * E / K)))
+    assert L == pytest.approx(c * T, rel=0.02)
+    assert oracle_mod.lib().orc_cnoidal_wave(0.02, 0.5, 1.5, out) != 0   # deep water: m leaves (0, 1]
+
+
+def test_flume_cnoidal_inflow_over_one_period(oracle_mod):
+    """LEF_CON (src/waves.F:92-170): the boundary elevation starts at its
+    zero crossing and over one period spans the wave height, trough to
+    crest, with zero mean."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_flume_con")
+    p.tol, p.itmax = 1e-8, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    ts, ein = [], []
+    while o.scalars().time < p.per_wave:
+        assert o.step() == 0
+        ts.append(o.scalars().time)
+        ein.append(_west_boundary_eta(o))
+    ts, ein = np.array(ts), np.array(ein)
+    H = p.amp_wave
+    assert abs(ein[0]) < 0.1 * H
+    assert (ein.max() - ein.min()) == pytest.approx(H, rel=0.02)
+    w = np.gradient(ts)
+    assert abs((ein * w).sum() / w.sum()) < 0.03 * H
+
+
+def test_flume_stokes_inflow_follows_the_formula(oracle_mod):
+    """LEF_STK (src/waves.F:518-560): the boundary elevation is the
+    second-order Stokes wave 0.5 A cos(phi) + A^2 k/16 cosh(kh)/sinh^3(kh)
+    (2 + cosh 2kh) cos(2 phi), phi = pi/2 - sigma t."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_flume_stk")
+    p.tol, p.itmax = 1e-8, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    pi = float(np.float32(3.141592653))
+    sigma = 2.0 * pi / p.per_wave
+    k = oracle_mod.lib().orc_wave_number(o._h, sigma)
+    h, A = p.dep_wave, p.amp_wave
+    e2 = A * A * k / 16.0 * math.cosh(k * h) / math.sinh(k * h) ** 3 * (2.0 + math.cosh(2.0 * k * h))
+    for _ in range(40):
+        assert o.step() == 0
+        ph = pi / 2 - sigma * o.scalars().time
+        assert _west_boundary_eta(o) == pytest.approx(0.5 * A * math.cos(ph) + e2 * math.cos(2 * ph), abs=1e-12)

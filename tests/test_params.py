@@ -79,9 +79,16 @@ def test_out_of_scope_reason(tmp_path):
     f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 2"))
     assert "BC_Z0" in P.unsupported_reason(P.read_input(str(f)))
     # a generator of the reference that the path does not build is rejected, not run as NONE
-    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_CON"))
+    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_JON"))
     p = P.read_input(str(f))
     assert p.wavemaker == P.WM_OTHER and "WAVEMAKER" in P.unsupported_reason(p)
+    # the cnoidal and Stokes boundary waves are on the path, through BC_X0 = 3
+    for name, wm in (("LEF_CON", P.WM_LEF_CON), ("LEF_STK", P.WM_LEF_STK)):
+        f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = " + name))
+        p = P.read_input(str(f))
+        assert p.wavemaker == wm
+        p.bc_x0 = 3
+        assert P.unsupported_reason(p) is None
 
 
 def test_reference_example_inputs_where_present():
