@@ -92,7 +92,8 @@ typedef struct nhw_params {
   int32_t non_hydro;                       /* NON_HYDRO                               */
   int32_t time_order;                      /* 1,2,3 <- TIME_ORDER FIRST/SECOND/THIRD  */
   int32_t hllc;                            /* HLLC: 1 HLLC face fluxes, 0 HLL          */
-  int32_t viscous_flow;                    /* VISCOUS_FLOW (must be 0)                */
+  int32_t viscous_flow;                    /* VISCOUS_FLOW: 1 needs IVTURB = IHTURB = 1
+                                              (constant eddy viscosities) and BC_Z0 = 1 */
   int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
   int32_t itmax; double tol;               /* ITMAX TOL                               */
   int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
@@ -136,6 +137,14 @@ typedef struct nhw_params {
                                               grid barrier also waits for this many blocks
                                               that do not exist, so its bounded wait runs
                                               out and the solve reports NHW_ERR_TIMEOUT */
+  /* viscous flow (read when viscous_flow = 1; src/initialize.F:357, 385-392) */
+  int32_t ivturb, ihturb;                  /* IVTURB IHTURB: 1 constant viscosity       */
+  int32_t rng;                             /* RNG: seeding viscosity of the first stage */
+  double  cvs, chs;                        /* Cvs Chs: vertical / horizontal eddy
+                                              viscosity of IVTURB = 1 / IHTURB = 1      */
+  double  schmidt;                         /* Schmidt                                 */
+  double  viscous_number;                  /* VISCOUS_NUMBER: dt limit of the explicit
+                                              horizontal viscous terms                */
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

@@ -401,6 +401,9 @@ struct OpFacePrep {
 // =========================================================================
 struct OpSlopeEta {
   static constexpr const char* kName = "slope_eta";
+  // eval_duvw's call (snap = true) is followed by sigma_transform, whose
+  // inputs the viscous flow keeps; the call at the start of fluxes is not
+  bool snap = false;
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const double* E = S.Eta;
@@ -419,6 +422,14 @@ struct OpSlopeEta {
     else sy = lim_slope<double>(E[c - S.sy], E[c], E[c + S.sy], S.dy, S.dy);
     S.DelxEta[c] = sx;
     S.DelyEta[c] = sy;
+    if (snap && S.scD) {   // viscous flow: sigma_transform's inputs, kept for the next stage's diffusion
+      S.scD[c] = S.D[c];
+      S.scEx[c] = sx;
+      S.scEy[c] = sy;
+      S.scHx[c] = S.DelxH[c];
+      S.scHy[c] = S.DelyH[c];
+      if (c == 0) S.sc->sig_set = 1;
+    }
   }
 };
 
@@ -719,12 +730,18 @@ struct OpExplicit {
         const long long o = i3(S, i, j, k);
         const R rds = S.lvT[k];   // (R)(1.0 / dsig_k)
         const R du = S.DU[o], dv = S.DV[o], dw = S.DW[o];
-        const R R2 = -rdx * (S.Fx[o + 1] - S.Fx[o]) - rdy * (S.Fy[o + S.sy] - S.Fy[o]) -
-                     rds * (S.Fz[o + S.sz] - S.Fz[o]) + fc * dv + sx;
-        const R R3 = -rdx * (S.Gx[o + 1] - S.Gx[o]) - rdy * (S.Gy[o + S.sy] - S.Gy[o]) -
-                     rds * (S.Gz[o + S.sz] - S.Gz[o]) - fc * du + syy;
-        const R R4 = -rdx * (S.Hx[o + 1] - S.Hx[o]) - rdy * (S.Hy[o + S.sy] - S.Hy[o]) -
-                     rds * (S.Hz[o + S.sz] - S.Hz[o]);
+        R R2 = -rdx * (S.Fx[o + 1] - S.Fx[o]) - rdy * (S.Fy[o + S.sy] - S.Fy[o]) -
+               rds * (S.Fz[o + S.sz] - S.Fz[o]) + fc * dv + sx;
+        R R3 = -rdx * (S.Gx[o + 1] - S.Gx[o]) - rdy * (S.Gy[o + S.sy] - S.Gy[o]) -
+               rds * (S.Gz[o + S.sz] - S.Gz[o]) - fc * du + syy;
+        R R4 = -rdx * (S.Hx[o + 1] - S.Hx[o]) - rdy * (S.Hy[o + S.sy] - S.Hy[o]) -
+               rds * (S.Hz[o + S.sz] - S.Hz[o]);
+        if (S.Dxx) {   // viscous terms of diffusion (src/nhwave.F:642-679)
+          R2 = R2 + S.Dxx[o] + S.Dxy[o];
+          R3 = R3 + S.Dyx[o] + S.Dyy[o];
+          R4 = R4 + S.Dzx[o] + S.Dzy[o];
+        }
+        // viscous flow: DU + dt R2 is the right-hand side of OpVertVisc
         S.DU[o] = du + rdt * R2;
         S.DV[o] = dv + rdt * R3;
         S.DW[o] = dw + rdt * R4;
@@ -883,7 +900,7 @@ struct OpVelBcB {
     const R Fext_Wind2 = (R)1.0 / Atop * (((R)1 - dye * dye) * (R)S.Wsy[c] - dxe * dye * (R)S.Wsx[c]);
     const R MinDepBC = (R)(double)0.01f;
     const R WzLt = (R)S.zWL[c], WzRb = (R)S.zWR[c], UzLt = (R)S.zUL[c], VzLt = (R)S.zVL[c];
-    const R vtop = (R)S.visc_top;
+    const R vtop = (R)(S.sc->turb ? S.visc_top_t : S.visc_top);
     const int KB = S.KB, KE = S.KE;
     for (int k = 1; k <= NG; ++k) {
       const long long ob = i3(S, i, j, KB - k), oi = i3(S, i, j, KB + k - 1);
@@ -917,6 +934,192 @@ struct OpVelBcB {
       const T d = (T)Dij;
       S.U[ob] = S.DU[ob] / d; S.V[ob] = S.DV[ob] / d; S.W[ob] = S.DW[ob] / d;
       S.U[ot] = S.DU[ot] / d; S.V[ot] = S.DV[ot] / d; S.W[ot] = S.DW[ot] / d;
+    }
+  }
+};
+
+// =========================================================================
+//   viscous flow with constant viscosities (IVTURB = IHTURB = 1)
+// =========================================================================
+// diffusion (src/nhwave.F:6785-7141): the explicit viscous terms of R2-R4,
+// one thread per interior cell, from the stage's starting DU/DV/DW and the
+// sigma slopes of the last sigma_transform (zero before the first one).
+// Cmu = Visc; CmuHt = Cmut_min until eval_turb, then Chs.  Each bracket
+// keeps the reference's evaluation order (bit-exact in the FP64 form).
+struct OpDiffusion {
+  static constexpr const char* kName = "diffusion";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    using R = T;
+    const long long c = i2(S, i, j), o = i3(S, i, j, k);
+    if (S.Mask[c] == 0) {
+      S.Dxx[o] = (T)0; S.Dxy[o] = (T)0; S.Dyx[o] = (T)0; S.Dyy[o] = (T)0; S.Dzx[o] = (T)0; S.Dzy[o] = (T)0;
+      return;
+    }
+    const bool set = S.sc->sig_set != 0;
+    // DelxSc / DelySc at level kk (sigc) and DelxSl / DelySl at face kk (sig)
+    auto slope = [&](const double* lev, const double* H, const double* E, int ii, int jj, int kk) -> R {
+      if (!set) return (R)0;
+      const long long q = i2(S, ii, jj);
+      return (R)((1.0 - lev[kk]) / S.scD[q] * H[q] - lev[kk] / S.scD[q] * E[q]);
+    };
+    auto Scx = [&](int ii, int jj, int kk) { return slope(S.sigc, S.scHx, S.scEx, ii, jj, kk); };
+    auto Scy = [&](int ii, int jj, int kk) { return slope(S.sigc, S.scHy, S.scEy, ii, jj, kk); };
+    const T* DU = S.DU;
+    const T* DV = S.DV;
+    const T* DW = S.DW;
+    auto F = [&](const T* a, int ii, int jj, int kk) -> R { return a[i3(S, ii, jj, kk)]; };
+    const R dx = (R)S.dx, dy = (R)S.dy;
+    const R cmu = (R)S.v_cmu, cmh = (R)(S.sc->turb ? S.v_chs : S.v_cmut0), sch = (R)S.v_schmidt;
+    const R nuF = (R)0.5 * (cmu + cmu) + (R)0.5 * (cmh + cmh) / sch;
+    const R nuC = cmu + cmh / sch;
+    const double* dsg = S.dsig;
+    const double L1top = dsg[k + 1] / (dsg[k] + dsg[k + 1]), L2top = dsg[k] / (dsg[k] + dsg[k + 1]);
+    const double L1bot = dsg[k] / (dsg[k] + dsg[k - 1]), L2bot = dsg[k - 1] / (dsg[k] + dsg[k - 1]);
+    const double ck = (dsg[k] + dsg[k + 1]) / 2.0, ck1 = (dsg[k - 1] + dsg[k]) / 2.0;
+    const R ac = (R)(-ck / (ck + ck1) / ck1), bc = (R)((ck - ck1) / (ck * ck1)), gc = (R)(ck1 / (ck + ck1) / ck);
+    const R nuH_top = ((R)L1top * cmu + (R)L2top * cmu) + ((R)L1top * cmh + (R)L2top * cmh) / sch;
+    const R nuH_bot = ((R)L1bot * cmu + (R)L2bot * cmu) + ((R)L1bot * cmh + (R)L2bot * cmh) / sch;
+    const R Dc = (R)S.D[c], dsk = (R)dsg[k], rck = (R)ck, rck1 = (R)ck1;
+    auto s3 = [&](const T* a, bool y, int ii, int jj) -> R {   // a F(k-1) Sc(k-1) + b .. + c ..
+      auto sc = [&](int kk) { return y ? Scy(ii, jj, kk) : Scx(ii, jj, kk); };
+      return ac * F(a, ii, jj, k - 1) * sc(k - 1) + bc * F(a, ii, jj, k) * sc(k) + gc * F(a, ii, jj, k + 1) * sc(k + 1);
+    };
+    auto s3x = [&](R lead, int ii, int jj) -> R {   // lead + a (Sx DV + Sy DU)(k-1) + ..
+      return lead + ac * (Scx(ii, jj, k - 1) * F(DV, ii, jj, k - 1) + Scy(ii, jj, k - 1) * F(DU, ii, jj, k - 1)) +
+             bc * (Scx(ii, jj, k) * F(DV, ii, jj, k) + Scy(ii, jj, k) * F(DU, ii, jj, k)) +
+             gc * (Scx(ii, jj, k + 1) * F(DV, ii, jj, k + 1) + Scy(ii, jj, k + 1) * F(DU, ii, jj, k + 1));
+    };
+    auto s3w = [&](bool y, const T* a, int ii, int jj) -> R {   // a (W Sc + F/D)(k-1) + ..
+      auto sc = [&](int kk) { return y ? Scy(ii, jj, kk) : Scx(ii, jj, kk); };
+      return ac * (F(DW, ii, jj, k - 1) * sc(k - 1) + F(a, ii, jj, k - 1) / Dc) +
+             bc * (F(DW, ii, jj, k) * sc(k) + F(a, ii, jj, k) / Dc) +
+             gc * (F(DW, ii, jj, k + 1) * sc(k + 1) + F(a, ii, jj, k + 1) / Dc);
+    };
+    auto vco = [&](bool y, R& cA, R& cB, R& cC) {   // coefficients of d/dsigma[nu Sl d/dsigma]
+      const R st = slope(S.sig, y ? S.scHy : S.scHx, y ? S.scEy : S.scEx, i, j, k + 1);
+      const R sb = slope(S.sig, y ? S.scHy : S.scHx, y ? S.scEy : S.scEx, i, j, k);
+      const R Pq = nuH_top * st - nuH_bot * sb, Sq = nuH_top * st + nuH_bot * sb;
+      cA = Pq * ac / dsk + Sq / rck1 / (rck + rck1);
+      cB = Pq * bc / dsk - Sq / rck1 / rck;
+      cC = Pq * gc / dsk + Sq / rck / (rck + rck1);
+    };
+    R xA, xB, xC, yA, yB, yC;
+    vco(false, xA, xB, xC);
+    vco(true, yA, yB, yC);
+    auto mixed = [&](int kk) -> R {   // d/dy DU + d/dx DV at level kk
+      return (F(DU, i, j + 1, kk) - F(DU, i, j - 1, kk)) / (R)2.0 / dy +
+             (F(DV, i + 1, j, kk) - F(DV, i - 1, j, kk)) / (R)2.0 / dx;
+    };
+    const R two = (R)2.0;
+    S.Dxx[o] =
+        (two * nuF * (F(DU, i + 1, j, k) - F(DU, i, j, k)) / dx - two * nuF * (F(DU, i, j, k) - F(DU, i - 1, j, k)) / dx) / dx +
+        (two * nuC * s3(DU, false, i + 1, j) - two * nuC * s3(DU, false, i - 1, j)) / two / dx +
+        (ac * two * nuC * Scx(i, j, k - 1) * (F(DU, i + 1, j, k - 1) - F(DU, i - 1, j, k - 1)) / two / dx +
+         bc * two * nuC * Scx(i, j, k) * (F(DU, i + 1, j, k) - F(DU, i - 1, j, k)) / two / dx +
+         gc * two * nuC * Scx(i, j, k + 1) * (F(DU, i + 1, j, k + 1) - F(DU, i - 1, j, k + 1)) / two / dx);
+    S.Dxy[o] =
+        (nuF * (F(DU, i, j + 1, k) - F(DU, i, j, k)) / dy - nuF * (F(DU, i, j, k) - F(DU, i, j - 1, k)) / dy) / dy +
+        (nuC * s3x((F(DV, i + 1, j + 1, k) - F(DV, i - 1, j + 1, k)) / two / dx, i, j + 1) -
+         nuC * s3x((F(DV, i + 1, j - 1, k) - F(DV, i - 1, j - 1, k)) / two / dx, i, j - 1)) / two / dy +
+        (ac * nuC * Scy(i, j, k - 1) * mixed(k - 1) + bc * nuC * Scy(i, j, k) * mixed(k) +
+         gc * nuC * Scy(i, j, k + 1) * mixed(k + 1)) +
+        (yA * Scx(i, j, k - 1) * F(DV, i, j, k - 1) + yB * Scx(i, j, k) * F(DV, i, j, k) +
+         yC * Scx(i, j, k + 1) * F(DV, i, j, k + 1));
+    S.Dyx[o] =
+        (nuF * (F(DV, i + 1, j, k) - F(DV, i, j, k)) / dx - nuF * (F(DV, i, j, k) - F(DV, i - 1, j, k)) / dx) / dx +
+        (nuC * s3x((F(DU, i + 1, j + 1, k) - F(DU, i + 1, j - 1, k)) / two / dy, i + 1, j) -
+         nuC * s3x((F(DU, i - 1, j + 1, k) - F(DU, i - 1, j - 1, k)) / two / dy, i - 1, j)) / two / dx +
+        (ac * nuC * Scx(i, j, k - 1) * mixed(k - 1) + bc * nuC * Scx(i, j, k) * mixed(k) +
+         gc * nuC * Scx(i, j, k + 1) * mixed(k + 1)) +
+        (xA * Scy(i, j, k - 1) * F(DU, i, j, k - 1) + xB * Scy(i, j, k) * F(DU, i, j, k) +
+         xC * Scy(i, j, k + 1) * F(DU, i, j, k + 1));
+    S.Dyy[o] =
+        (two * nuF * (F(DV, i, j + 1, k) - F(DV, i, j, k)) / dy - two * nuF * (F(DV, i, j, k) - F(DV, i, j - 1, k)) / dy) / dy +
+        (two * nuC * s3(DV, true, i, j + 1) - two * nuC * s3(DV, true, i, j - 1)) / two / dy +
+        (ac * two * nuC * Scy(i, j, k - 1) * (F(DV, i, j + 1, k - 1) - F(DV, i, j - 1, k - 1)) / two / dy +
+         bc * two * nuC * Scy(i, j, k) * (F(DV, i, j + 1, k) - F(DV, i, j - 1, k)) / two / dy +
+         gc * two * nuC * Scy(i, j, k + 1) * (F(DV, i, j + 1, k + 1) - F(DV, i, j - 1, k + 1)) / two / dy);
+    S.Dzx[o] =
+        (nuF * (F(DW, i + 1, j, k) - F(DW, i, j, k)) / dx - nuF * (F(DW, i, j, k) - F(DW, i - 1, j, k)) / dx) / dx +
+        (nuC * s3w(false, DU, i + 1, j) - nuC * s3w(false, DU, i - 1, j)) / two / dx +
+        (ac * nuC * Scx(i, j, k - 1) * (F(DW, i + 1, j, k - 1) - F(DW, i - 1, j, k - 1)) / two / dx +
+         bc * nuC * Scx(i, j, k) * (F(DW, i + 1, j, k) - F(DW, i - 1, j, k)) / two / dx +
+         gc * nuC * Scx(i, j, k + 1) * (F(DW, i + 1, j, k + 1) - F(DW, i - 1, j, k + 1)) / two / dx) +
+        (xA * F(DU, i, j, k - 1) / Dc + xB * F(DU, i, j, k) / Dc + xC * F(DU, i, j, k + 1) / Dc);
+    S.Dzy[o] =
+        (nuF * (F(DW, i, j + 1, k) - F(DW, i, j, k)) / dy - nuF * (F(DW, i, j, k) - F(DW, i, j - 1, k)) / dy) / dy +
+        (nuC * s3w(true, DV, i, j + 1) - nuC * s3w(true, DV, i, j - 1)) / two / dy +
+        (ac * nuC * Scy(i, j, k - 1) * (F(DW, i, j + 1, k - 1) - F(DW, i, j - 1, k - 1)) / two / dy +
+         bc * nuC * Scy(i, j, k) * (F(DW, i, j + 1, k) - F(DW, i, j - 1, k)) / two / dy +
+         gc * nuC * Scy(i, j, k + 1) * (F(DW, i, j + 1, k + 1) - F(DW, i, j - 1, k + 1)) / two / dy) +
+        (yA * F(DV, i, j, k - 1) / Dc + yB * F(DV, i, j, k) / Dc + yC * F(DV, i, j, k + 1) / Dc);
+  }
+};
+
+// Implicit vertical viscous step of eval_duvw (src/nhwave.F:690-822 DU,
+// 850-1010 DV, 1012-1182 DW, BC_Z0 = 1), one thread per wet interior column,
+// after the new D, Eta and eta slopes: DU/DV/DW hold the explicit update
+// DU + dt R2 on entry.  The tridiagonal systems are solved by trig's
+// elimination (src/nhwave.F:13182-13224) in FP64, with the eliminated
+// right-hand side kept in place (in T); the coefficients depend on the level
+// only, so they are recomputed rather than stored.
+struct OpVertVisc {
+  static constexpr const char* kName = "vertical_viscous";
+  static constexpr int kMaxK = 64;   // Kglob <= 64 (nhw_create)
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long c = i2(S, i, j);
+    if (S.Mask[c] == 0) return;
+    const int KB = S.KB, KE = S.KE, n = KE - KB + 1;
+    const double dt = S.sc->dt, Dc = S.D[c];
+    const double cvt = S.sc->turb ? S.v_cvs : S.v_cmut0;
+    const double nuz = 0.5 * (S.v_cmu + S.v_cmu) + 0.5 * (cvt + cvt) / S.v_schmidt;
+    const double* dsg = S.dsig;
+    auto A = [&](int k) { return k == KB ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsg[k] * (dsg[k] + dsg[k - 1])); };
+    auto C = [&](int k) { return k == KE ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsg[k] * (dsg[k] + dsg[k + 1])); };
+    const double Wbot = -S.DeltH[c] - (double)S.U[i3(S, i, j, KB)] * S.DelxH[c] - (double)S.V[i3(S, i, j, KB)] * S.DelyH[c];
+    const double Wtop = (S.Eta[c] - S.Eta0[c]) / dt + (double)S.U[i3(S, i, j, KE)] * S.DelxEta[c] +
+                        (double)S.V[i3(S, i, j, KE)] * S.DelyEta[c];
+    double bp[kMaxK];   // eliminated diagonal; the eliminated right-hand side goes in place
+    for (int which = 0; which < 3; ++which) {
+      T* Fv = which == 0 ? S.DU : which == 1 ? S.DV : S.DW;
+      auto coefs = [&](int k, double& b, double& r) {
+        const double f = (double)Fv[i3(S, i, j, k)];
+        if (which < 2) {
+          b = 1.0 - A(k) - C(k);
+          r = f;
+          if (k == KE) r = r + dt * (which == 0 ? S.Wsx[c] : S.Wsy[c]) / dsg[k];
+        } else if (k == KB) {
+          const double q = 0.25 * dsg[k] * (dsg[k] + dsg[k - 1]);
+          b = 1.0 - C(k) + dt / (Dc * Dc) * nuz / q;
+          r = f + dt / Dc * nuz / q * Wbot;
+        } else if (k == KE) {
+          const double q = 0.25 * dsg[k] * (dsg[k] + dsg[k + 1]);
+          b = 1.0 - A(k) + dt / (Dc * Dc) * nuz / q;
+          r = f + dt / Dc * nuz / q * Wtop;
+        } else {
+          b = 1.0 - A(k) - C(k);
+          r = f;
+        }
+      };
+      double rprev;
+      coefs(KB, bp[0], rprev);
+      Fv[i3(S, i, j, KB)] = (T)rprev;
+      for (int q = 1; q < n; ++q) {
+        double b, r;
+        coefs(KB + q, b, r);
+        const double coeff = A(KB + q) / bp[q - 1];
+        bp[q] = b - coeff * C(KB + q - 1);
+        rprev = r - coeff * rprev;
+        Fv[i3(S, i, j, KB + q)] = (T)rprev;
+      }
+      double x = rprev / bp[n - 1];
+      Fv[i3(S, i, j, KE)] = (T)x;
+      for (int q = n - 2; q >= 0; --q) {
+        x = ((double)Fv[i3(S, i, j, KB + q)] - C(KB + q) * x) / bp[q];
+        Fv[i3(S, i, j, KB + q)] = (T)x;
+      }
     }
   }
 };
@@ -1404,7 +1607,18 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
     sc->dt_old = sc->dt;
     const double dt_growth = (double)1.05f * sc->dt_old;
     const double dt_courant = S.cfl * tmp2;
-    const double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), kLarge), S.dt_max);
+    // limit of the explicit viscous terms (src/nhwave.F:3812-3832); the
+    // horizontal viscosity is the same in every cell
+    double dt_viscous = kLarge;
+    if (S.viscous) {
+      const double ch = fabs(sc->turb ? S.v_chs : S.v_cmut0) + (double)1.e-16f;
+      double t2 = kLarge;
+      const double ax = S.dx * S.dx / ch, ay = S.dy * S.dy / ch;
+      if (ax < t2) t2 = ax;
+      if (ay < t2) t2 = ay;
+      dt_viscous = S.v_number * t2;
+    }
+    const double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), dt_viscous), S.dt_max);
     sc->dt = dt;
     sc->rho_dt = kRho0 / dt;
     sc->dt_rho = dt / kRho0;

@@ -24,7 +24,10 @@ int check_params(const nhw_params& p) {
   if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1) return NHW_ERR_ARG;
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
-  if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+  if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
+  // viscous flow with constant viscosities only (no k-epsilon / LES), free-slip bed
+  if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1 || p.bc_z0 != 1)) return NHW_ERR_UNSUPPORTED;
+  if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski

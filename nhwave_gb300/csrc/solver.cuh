@@ -94,6 +94,7 @@ template <class T>
 __global__ void k_single(Dev<T> S, int what) {
   if (gated_off(S)) return;
   if (what == 0) OpSourceArea{}(S, 0, 0);
+  else if (what == 1) S.sc->turb = 1;
 }
 // update_vars: D0 = D, Eta0 = Eta (2-D, FP64), DU0/DV0/DW0 = DU/DV/DW (3-D)
 template <class T>
@@ -228,6 +229,16 @@ class Solver final : public SolverBase {
     S.hllc = p.hllc ? 1 : 0;
     S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
     S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
+    S.visc_top_t = S.visc_top;
+    S.viscous = p.viscous_flow ? 1 : 0;
+    if (S.viscous) {   // seeding viscosity of initial (src/initialize.F:3172-3195)
+      const double tke = (double)1.e-9f, eps = (double)1.e-9f;
+      S.v_cmut0 = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (tke * tke) / eps;
+      S.v_cmu = p.visc; S.v_cvs = p.cvs; S.v_chs = p.chs;
+      S.v_schmidt = p.schmidt; S.v_number = p.viscous_number;
+      S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + S.v_cmut0 + p.visc + 0.0 + S.v_cmut0);
+      S.visc_top_t = kSmall + 0.5 * (p.visc + 0.0 + p.cvs + p.visc + 0.0 + p.cvs);
+    }
     S.wavemaker = p.wavemaker;
     S.wm_amp = p.amp_wave; S.wm_xw = p.xsource_west; S.wm_xe = p.xsource_east;
     S.wm_ys = p.ysource_suth; S.wm_yn = p.ysource_nrth;
@@ -274,7 +285,11 @@ class Solver final : public SolverBase {
       add(&S.Eta00, sizeof(double) * n2);
       for (T** pp : {&S.U0, &S.V0, &S.W0, &S.U00, &S.V00, &S.W00}) add(pp, sizeof(T) * n3);
     }
+    if (p.viscous_flow)   // sigma_transform's inputs, read by the next stage (checkpointed state)
+      for (double** pp : {&S.scD, &S.scEx, &S.scEy, &S.scHx, &S.scHy}) add(pp, sizeof(double) * n2);
     add(&S.P, sizeof(double) * n3);
+    if (p.viscous_flow)   // explicit viscous terms of the stage
+      for (T** pp : {&S.Dxx, &S.Dxy, &S.Dyx, &S.Dyy, &S.Dzx, &S.Dzy}) add(pp, sizeof(T) * n3);
     // west-boundary wave values, recomputed every step (after the checkpointed state)
     add(&S.Ein, sizeof(double) * S.Nloc);
     add(&S.Din, sizeof(double) * S.Nloc);
@@ -1058,9 +1073,11 @@ class Solver final : public SolverBase {
   // eval_duvw up to the pressure solve: explicit stage update, surface BC,
   // slopes, velocities and the Poisson system
   void stage_pre(int s) {
+    if (S.viscous) cells(OpDiffusion{});
     incols(OpExplicit{s});
     allcols(OpWlBcEta{});
-    allcols(OpSlopeEta{});
+    allcols(OpSlopeEta{true});
+    if (S.viscous) incols(OpVertVisc{});
     if (S.non_hydro) {
       get_uvw();
       poisson_setup();
@@ -1080,6 +1097,10 @@ class Solver final : public SolverBase {
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});
+    // eval_turb with IVTURB = IHTURB = 1 (src/nhwave.F:6544-6686): from now
+    // on CmuVt = Cvs, CmuHt = Chs.  The reference calls it after
+    // sponge_damping, which reads no viscosity.
+    if (S.viscous) L("eval_turb", [&] { k_single<T><<<1, 1, 0, st>>>(S, 1); });
   }
   int eval_duvw(int istep) override {
     if (istep < 1 || istep > it_order) return NHW_ERR_ARG;

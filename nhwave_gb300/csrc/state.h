@@ -57,7 +57,9 @@ struct DevScal {
   int64_t total_ir;                 // refinement sweeps, cumulative
   // grid barrier of the persistent solve (psolve.cuh)
   unsigned int bar_count, bar_gen;
-  int32_t bar_err, pad2_;
+  int32_t bar_err;
+  int32_t turb;                     // viscous flow: eval_turb has set CmuVt = Cvs, CmuHt = Chs
+  int32_t sig_set, pad3_;           // viscous flow: the sigma slopes have been formed once
   double gm_inv;                    // GMRES: 1 / ||w|| of the vector the next iteration normalises
 };
 
@@ -85,7 +87,13 @@ struct Dev {
   // handles.  Eagerly launched kernels have graph_mode = 0.
   int graph_mode;
   unsigned long long h_go, h_ir, h_inner;
-  double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt)
+  double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt) before eval_turb
+  double visc_top_t;               // the same after it (viscous flow: CmuVt = Cvs)
+  // viscous flow with constant viscosities (IVTURB = IHTURB = 1): Cmu = Visc;
+  // CmuVt = CmuHt = Cmut_min until eval_turb, then Cvs / Chs; Schmidt;
+  // VISCOUS_NUMBER.  viscous = 0 on the inviscid path.
+  int viscous;
+  double v_cmu, v_cmut0, v_cvs, v_chs, v_schmidt, v_number;
   double alpha[3], beta[3];        // SSP-RK coefficients
   // wavemaker (INT_LIN / INT_SOL): host-computed constants
   int wavemaker;
@@ -112,6 +120,10 @@ struct Dev {
   // 2-D FP64 fields
   double *D, *D0, *Eta, *Eta0, *Hc, *Hc0, *Ho;
   double* Eta00;               // Orlanski boundary (BC_Xn = 6) only, else nullptr
+  // viscous flow only, else nullptr: D, DelxEta, DelyEta, DelxH, DelyH as of
+  // the last sigma_transform, from which the viscous terms form DelxSc /
+  // DelySc (cell levels) and DelxSl / DelySl (faces) of that moment
+  double *scD, *scEx, *scEy, *scHx, *scHy;
   double *Hfx, *Hfy, *Hfx0, *Hfy0, *DelxH, *DelyH, *DeltH, *DeltHo, *Delt2H;
   double *DelxEta, *DelyEta, *SourceX, *SourceY, *SourceC, *Sponge, *R1, *Wsx, *Wsy;
   double *EtaxL, *EtaxR, *EtayL, *EtayR;
@@ -150,6 +162,9 @@ struct Dev {
   // velocities of the last two steps, read by the Orlanski boundary
   // (BC_Xn = 6) only, else nullptr
   T *U0, *V0, *W0, *U00, *V00, *W00;
+  // explicit viscous terms of the stage (viscous flow only, else nullptr):
+  // Diffxx, Diffxy (into R2), Diffyx, Diffyy (R3), Diffzx, Diffzy (R4)
+  T *Dxx, *Dxy, *Dyx, *Dyy, *Dzx, *Dzy;
   // GMRES (krylov.cuh): basis V [kGmMax+1][neq], preconditioned basis Z
   // [kGmMax][neq], Hessenberg / rotations / g / y in FP64 (gm), the current
   // column, y and 1/||w|| in T (gmT), wide reduction partials; nullptr unless

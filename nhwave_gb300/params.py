@@ -62,6 +62,9 @@ class NhwParams(ctypes.Structure):
         ("mg_cta_columns", ctypes.c_int32),
         ("mg_aggregate", ctypes.c_int32),
         ("test_barrier_extra", ctypes.c_int32),
+        ("ivturb", ctypes.c_int32), ("ihturb", ctypes.c_int32), ("rng", ctypes.c_int32),
+        ("cvs", ctypes.c_double), ("chs", ctypes.c_double), ("schmidt", ctypes.c_double),
+        ("viscous_number", ctypes.c_double),
     ]
 
     def copy(self) -> "NhwParams":
@@ -104,6 +107,9 @@ def default_params(**kw) -> NhwParams:
     p.sponge_on = 0
     p.slide_type = SLIDE_NONE
     p.precision = NHW_FP64
+    p.ivturb = p.ihturb = 1
+    p.cvs = p.chs = 0.0
+    p.schmidt, p.viscous_number = 1.0, 1.0 / 6.0
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(f"unknown nhw_params field {k!r}")
@@ -169,6 +175,10 @@ def read_input(path: str) -> NhwParams:
     p.bc_y0, p.bc_yn = i("BC_Y0", 1), i("BC_Yn", 1)
     p.bc_z0 = i("BC_Z0", 1)
     p.visc, p.slat = f("VISCOSITY", 1e-6), f("slat", 0.0)
+    if p.viscous_flow:
+        p.ivturb, p.ihturb, p.rng = i("IVTURB", 1), i("IHTURB", 1), _logical(kv.get("RNG", "F"))
+        p.cvs, p.chs, p.schmidt = f("Cvs", 0.0), f("Chs", 0.0), f("Schmidt", 1.0)
+        p.viscous_number = f("VISCOUS_NUMBER", 1.0 / 6.0)
     p.wind_u, p.wind_v = f("WindU", 0.0), f("WindV", 0.0)
     dt_ = s("DEPTH_TYPE", "CELL_CENTER").upper()
     p.depth_type = DEPTH_CELL_GRID if dt_ == "CELL_GRID" else DEPTH_CELL_CENTER
@@ -210,8 +220,9 @@ def read_input(path: str) -> NhwParams:
 
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
-    if p.viscous_flow:
-        return "VISCOUS_FLOW=T (viscous/turbulent terms are outside the GPU path)"
+    if p.viscous_flow and (p.ivturb != 1 or p.ihturb != 1):
+        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (only constant viscosities, "
+                "IVTURB = IHTURB = 1, are on the GPU path; the k-epsilon and LES models are not)")
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF:

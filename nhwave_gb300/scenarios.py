@@ -192,6 +192,14 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
     elif name == "tiny_flume_con":
         # Ursell number H L^2 / h^3 of about 34: elliptic parameter m = 0.91
         out = wave_flume("CON", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.1, per=3.0, sponge=1.5, **kw)
+    elif name == "tiny_visc":
+        # the small submerged bar with constant viscosities (VISCOUS_FLOW, IVTURB = IHTURB = 1)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_visc_dt":
+        # as tiny_visc, with a horizontal viscosity large enough that VISCOUS_NUMBER limits dt
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.05, chs=20.0), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)

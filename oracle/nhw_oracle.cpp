@@ -205,14 +205,23 @@ struct Model {
   // Poisson system (Coef(neqns,15), Rhs(neqns); src/mod_global.F:239-243)
   int neqns = 0;
   std::vector<double> Coef, Rhs;
-  // Cmu = Visc, CmuR = CmuVt = 0 on the inviscid path (src/initialize.F:2663-2666)
-  double Cmu = 0, CmuR = 0, CmuVt = 0;
+  // Cmu = Visc, CmuR = CmuVt = 0 on the inviscid path (src/initialize.F:2663-2666).
+  // With VISCOUS_FLOW and IVTURB = IHTURB = 1 every cell holds the same
+  // viscosities, so they are scalars here: CmuVt = CmuHt = Cmut_min from
+  // initial (src/initialize.F:3172-3195) until the first eval_turb sets
+  // CmuVt = Cvs, CmuHt = Chs (src/nhwave.F:6650-6686).
+  double Cmu = 0, CmuR = 0, CmuVt = 0, CmuHt = 0;
+  // viscous flow: face sigma slopes (sigma_transform) and the explicit
+  // viscous terms of diffusion (src/nhwave.F:6785-7141)
+  A3 DelxSl, DelySl, Diffxx, Diffxy, Diffyx, Diffyy, Diffzx, Diffzy;
 
   // ------------------------------------------------------------ index/alloc
   int create(const nhw_params& q) {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
-    if (p.viscous_flow || !p.barotropic) return NHW_ERR_UNSUPPORTED;
+    if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1 || p.bc_z0 != 1)) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
@@ -250,6 +259,10 @@ struct Model {
       a->init(Mloc, Nloc, Kloc);
     for (A3* a : {&Omega, &Uf, &Vf, &Wf, &UzL, &UzR, &VzL, &VzR, &WzL, &WzR, &Fz, &Gz, &Hz})
       a->init(Mloc, Nloc, Kloc1);
+    if (p.viscous_flow) {
+      DelxSl.init(Mloc, Nloc, Kloc1); DelySl.init(Mloc, Nloc, Kloc1);
+      for (A3* a : {&Diffxx, &Diffxy, &Diffyx, &Diffyy, &Diffzx, &Diffzy}) a->init(Mloc, Nloc, Kloc);
+    }
     for (A3* a : {&UxL, &UxR, &VxL, &VxR, &WxL, &WxR, &DUxL, &DUxR, &DVxL, &DVxR, &DWxL, &DWxR,
                   &SxL, &SxR, &SxS, &ExL, &ExR, &FxL, &FxR, &GxL, &GxR, &HxL, &HxR, &Ex, &Fx,
                   &Gx, &Hx})
@@ -410,7 +423,13 @@ struct Model {
   void initial(const double* eta0, const double* uvw0) {
     TIME = Zero; RUN_STEP = 0; dt = p.dt_ini;
     Sponge.fill(1.0);
-    Cmu = p.visc; CmuR = 0.0; CmuVt = 0.0;
+    Cmu = p.visc; CmuR = 0.0; CmuVt = 0.0; CmuHt = 0.0;
+    if (p.viscous_flow) {   // seeding values (src/initialize.F:3172-3195)
+      const double Tke_min = (double)1.e-9f, Eps_min = (double)1.e-9f;
+      const double Cmut_min = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (Tke_min * Tke_min) / Eps_min;
+      CmuHt = Cmut_min;
+      CmuVt = Cmut_min;
+    }
     Eta.fill(0.0);
     const int Mg = p.Mglob, Ng = p.Nglob, Kg = p.Kglob;
     if (eta0 || uvw0) {
@@ -489,7 +508,20 @@ struct Model {
           if (dzonw < tmp2) tmp2 = dzonw;
         }
     const double dt_courant = p.cfl * tmp2;
-    const double dt_viscous = Large;
+    // limit of the explicit viscous terms (src/nhwave.F:3812-3832)
+    double dt_viscous = Large;
+    if (p.viscous_flow) {
+      tmp2 = Large;
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j)
+          for (int i = Ibeg; i <= Iend; ++i) {
+            double tmp1 = dx * dx / (std::fabs(CmuHt) + (double)1.e-16f);
+            if (tmp1 < tmp2) tmp2 = tmp1;
+            tmp1 = dy * dy / (std::fabs(CmuHt) + (double)1.e-16f);
+            if (tmp1 < tmp2) tmp2 = tmp1;
+          }
+      dt_viscous = p.viscous_number * tmp2;
+    }
     dt = dmin(dmin(dmin(dt_growth, dt_courant), dt_viscous), p.dt_max);
     if (dt < p.dt_min) return NHW_ERR_DT_MIN;
     TIME = TIME + dt;
@@ -1246,6 +1278,171 @@ struct Model {
           DelxSc(i, j, k) = (1.0 - sigc(k)) / D(i, j) * DelxH(i, j) - sigc(k) / D(i, j) * DelxEta(i, j);
           DelySc(i, j, k) = (1.0 - sigc(k)) / D(i, j) * DelyH(i, j) - sigc(k) / D(i, j) * DelyEta(i, j);
         }
+    if (!p.viscous_flow) return;   // DelxSl / DelySl feed only the viscous terms
+    for (int k = 1; k <= Kloc1; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          DelxSl(i, j, k) = (1.0 - sig(k)) / D(i, j) * DelxH(i, j) - sig(k) / D(i, j) * DelxEta(i, j);
+          DelySl(i, j, k) = (1.0 - sig(k)) / D(i, j) * DelyH(i, j) - sig(k) / D(i, j) * DelyEta(i, j);
+        }
+  }
+
+  // -------------------------------------------------------------- diffusion
+  // Explicit part of the viscous terms (src/nhwave.F:6785-7141) for uniform
+  // viscosities: Diffxx/Diffxy enter R2, Diffyx/Diffyy R3, Diffzx/Diffzy
+  // R4 (the reference also forms Diffxz/Diffyz, which nothing reads).
+  // The sigma slopes are those of the last sigma_transform; D is the
+  // current one.  Every bracket keeps the reference's evaluation order.
+  void diffusion() {
+    for (A3* a : {&Diffxx, &Diffxy, &Diffyx, &Diffyy, &Diffzx, &Diffzy}) a->fill(0.0);
+    const double Schmidt = p.schmidt;
+    // face and cell viscosities of uniform Cmu / CmuHt
+    const double nuF = 0.5 * (Cmu + Cmu) + 0.5 * (CmuHt + CmuHt) / Schmidt;
+    const double nuC = Cmu + CmuHt / Schmidt;
+    for (int k = Kbeg; k <= Kend; ++k) {
+      const double L1top = dsig(k + 1) / (dsig(k) + dsig(k + 1)), L2top = dsig(k) / (dsig(k) + dsig(k + 1));
+      const double L1bot = dsig(k) / (dsig(k) + dsig(k - 1)), L2bot = dsig(k - 1) / (dsig(k) + dsig(k - 1));
+      const double dsigck = (dsig(k) + dsig(k + 1)) / 2.0, dsigck1 = (dsig(k - 1) + dsig(k)) / 2.0;
+      const double ac = -dsigck / (dsigck + dsigck1) / dsigck1;
+      const double bc = (dsigck - dsigck1) / (dsigck * dsigck1);
+      const double gc = dsigck1 / (dsigck + dsigck1) / dsigck;
+      const double nuH_top = (L1top * Cmu + L2top * Cmu) + (L1top * CmuHt + L2top * CmuHt) / Schmidt;
+      const double nuH_bot = (L1bot * Cmu + L2bot * Cmu) + (L1bot * CmuHt + L2bot * CmuHt) / Schmidt;
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 0) continue;
+          const double Dc = D(i, j);
+          // three-level sums  a F(k-1) G(k-1) + b F(k) G(k) + c F(k+1) G(k+1)
+          auto s3 = [&](A3& F, A3& G, int ii, int jj) {
+            return ac * F(ii, jj, k - 1) * G(ii, jj, k - 1) + bc * F(ii, jj, k) * G(ii, jj, k) +
+                   gc * F(ii, jj, k + 1) * G(ii, jj, k + 1);
+          };
+          // lead + a (Sx DV + Sy DU)(k-1) + ..., summed left to right: the
+          // cross-slope sums of Diffxy / Diffyx
+          auto s3x = [&](double lead, int ii, int jj) {
+            return lead + ac * (DelxSc(ii, jj, k - 1) * DV(ii, jj, k - 1) + DelySc(ii, jj, k - 1) * DU(ii, jj, k - 1)) +
+                   bc * (DelxSc(ii, jj, k) * DV(ii, jj, k) + DelySc(ii, jj, k) * DU(ii, jj, k)) +
+                   gc * (DelxSc(ii, jj, k + 1) * DV(ii, jj, k + 1) + DelySc(ii, jj, k + 1) * DU(ii, jj, k + 1));
+          };
+          // a (W Sx + F/D)(k-1) + ...: Diffzx / Diffzy
+          auto s3w = [&](A3& Sl, A3& F, int ii, int jj) {
+            return ac * (DW(ii, jj, k - 1) * Sl(ii, jj, k - 1) + F(ii, jj, k - 1) / Dc) +
+                   bc * (DW(ii, jj, k) * Sl(ii, jj, k) + F(ii, jj, k) / Dc) +
+                   gc * (DW(ii, jj, k + 1) * Sl(ii, jj, k + 1) + F(ii, jj, k + 1) / Dc);
+          };
+          // vertical coefficients of the d/dsigma[nu Sl d/dsigma] terms
+          auto vco = [&](A3& Sl, double& cA, double& cB, double& cC) {
+            const double Pq = nuH_top * Sl(i, j, k + 1) - nuH_bot * Sl(i, j, k);
+            const double Sq = nuH_top * Sl(i, j, k + 1) + nuH_bot * Sl(i, j, k);
+            cA = Pq * ac / dsig(k) + Sq / dsigck1 / (dsigck + dsigck1);
+            cB = Pq * bc / dsig(k) - Sq / dsigck1 / dsigck;
+            cC = Pq * gc / dsig(k) + Sq / dsigck / (dsigck + dsigck1);
+          };
+          double xA, xB, xC, yA, yB, yC;
+          vco(DelxSl, xA, xB, xC);
+          vco(DelySl, yA, yB, yC);
+          // d/dx[2 nu d/dx DU] + d/dx[2 nu d/dsigma(DU Sx)] + d/dsigma[2 nu Sx d/dx DU]
+          Diffxx(i, j, k) =
+              (2.0 * nuF * (DU(i + 1, j, k) - DU(i, j, k)) / dx - 2.0 * nuF * (DU(i, j, k) - DU(i - 1, j, k)) / dx) / dx +
+              (2.0 * nuC * s3(DU, DelxSc, i + 1, j) - 2.0 * nuC * s3(DU, DelxSc, i - 1, j)) / 2.0 / dx +
+              (ac * 2.0 * nuC * DelxSc(i, j, k - 1) * (DU(i + 1, j, k - 1) - DU(i - 1, j, k - 1)) / 2.0 / dx +
+               bc * 2.0 * nuC * DelxSc(i, j, k) * (DU(i + 1, j, k) - DU(i - 1, j, k)) / 2.0 / dx +
+               gc * 2.0 * nuC * DelxSc(i, j, k + 1) * (DU(i + 1, j, k + 1) - DU(i - 1, j, k + 1)) / 2.0 / dx);
+          auto mixed = [&](int kk) {   // d/dy DU + d/dx DV at level kk
+            return (DU(i, j + 1, kk) - DU(i, j - 1, kk)) / 2.0 / dy + (DV(i + 1, j, kk) - DV(i - 1, j, kk)) / 2.0 / dx;
+          };
+          Diffxy(i, j, k) =
+              (nuF * (DU(i, j + 1, k) - DU(i, j, k)) / dy - nuF * (DU(i, j, k) - DU(i, j - 1, k)) / dy) / dy +
+              (nuC * s3x((DV(i + 1, j + 1, k) - DV(i - 1, j + 1, k)) / 2.0 / dx, i, j + 1) -
+               nuC * s3x((DV(i + 1, j - 1, k) - DV(i - 1, j - 1, k)) / 2.0 / dx, i, j - 1)) /
+                  2.0 / dy +
+              (ac * nuC * DelySc(i, j, k - 1) * mixed(k - 1) + bc * nuC * DelySc(i, j, k) * mixed(k) +
+               gc * nuC * DelySc(i, j, k + 1) * mixed(k + 1)) +
+              (yA * DelxSc(i, j, k - 1) * DV(i, j, k - 1) + yB * DelxSc(i, j, k) * DV(i, j, k) +
+               yC * DelxSc(i, j, k + 1) * DV(i, j, k + 1));
+          Diffyx(i, j, k) =
+              (nuF * (DV(i + 1, j, k) - DV(i, j, k)) / dx - nuF * (DV(i, j, k) - DV(i - 1, j, k)) / dx) / dx +
+              (nuC * s3x((DU(i + 1, j + 1, k) - DU(i + 1, j - 1, k)) / 2.0 / dy, i + 1, j) -
+               nuC * s3x((DU(i - 1, j + 1, k) - DU(i - 1, j - 1, k)) / 2.0 / dy, i - 1, j)) /
+                  2.0 / dx +
+              (ac * nuC * DelxSc(i, j, k - 1) * mixed(k - 1) + bc * nuC * DelxSc(i, j, k) * mixed(k) +
+               gc * nuC * DelxSc(i, j, k + 1) * mixed(k + 1)) +
+              (xA * DelySc(i, j, k - 1) * DU(i, j, k - 1) + xB * DelySc(i, j, k) * DU(i, j, k) +
+               xC * DelySc(i, j, k + 1) * DU(i, j, k + 1));
+          Diffyy(i, j, k) =
+              (2.0 * nuF * (DV(i, j + 1, k) - DV(i, j, k)) / dy - 2.0 * nuF * (DV(i, j, k) - DV(i, j - 1, k)) / dy) / dy +
+              (2.0 * nuC * s3(DV, DelySc, i, j + 1) - 2.0 * nuC * s3(DV, DelySc, i, j - 1)) / 2.0 / dy +
+              (ac * 2.0 * nuC * DelySc(i, j, k - 1) * (DV(i, j + 1, k - 1) - DV(i, j - 1, k - 1)) / 2.0 / dy +
+               bc * 2.0 * nuC * DelySc(i, j, k) * (DV(i, j + 1, k) - DV(i, j - 1, k)) / 2.0 / dy +
+               gc * 2.0 * nuC * DelySc(i, j, k + 1) * (DV(i, j + 1, k + 1) - DV(i, j - 1, k + 1)) / 2.0 / dy);
+          Diffzx(i, j, k) =
+              (nuF * (DW(i + 1, j, k) - DW(i, j, k)) / dx - nuF * (DW(i, j, k) - DW(i - 1, j, k)) / dx) / dx +
+              (nuC * s3w(DelxSc, DU, i + 1, j) - nuC * s3w(DelxSc, DU, i - 1, j)) / 2.0 / dx +
+              (ac * nuC * DelxSc(i, j, k - 1) * (DW(i + 1, j, k - 1) - DW(i - 1, j, k - 1)) / 2.0 / dx +
+               bc * nuC * DelxSc(i, j, k) * (DW(i + 1, j, k) - DW(i - 1, j, k)) / 2.0 / dx +
+               gc * nuC * DelxSc(i, j, k + 1) * (DW(i + 1, j, k + 1) - DW(i - 1, j, k + 1)) / 2.0 / dx) +
+              (xA * DU(i, j, k - 1) / Dc + xB * DU(i, j, k) / Dc + xC * DU(i, j, k + 1) / Dc);
+          Diffzy(i, j, k) =
+              (nuF * (DW(i, j + 1, k) - DW(i, j, k)) / dy - nuF * (DW(i, j, k) - DW(i, j - 1, k)) / dy) / dy +
+              (nuC * s3w(DelySc, DV, i, j + 1) - nuC * s3w(DelySc, DV, i, j - 1)) / 2.0 / dy +
+              (ac * nuC * DelySc(i, j, k - 1) * (DW(i, j + 1, k - 1) - DW(i, j - 1, k - 1)) / 2.0 / dy +
+               bc * nuC * DelySc(i, j, k) * (DW(i, j + 1, k) - DW(i, j - 1, k)) / 2.0 / dy +
+               gc * nuC * DelySc(i, j, k + 1) * (DW(i, j + 1, k + 1) - DW(i, j - 1, k + 1)) / 2.0 / dy) +
+              (yA * DV(i, j, k - 1) / Dc + yB * DV(i, j, k) / Dc + yC * DV(i, j, k + 1) / Dc);
+        }
+    }
+  }
+
+  // trig (src/nhwave.F:13182-13224): tridiagonal solve by forward
+  // elimination and back substitution
+  static void trig(const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& c,
+                   const std::vector<double>& r, std::vector<double>& x, int n) {
+    std::vector<double> bp(n), rp(n);
+    bp[0] = b[0];
+    rp[0] = r[0];
+    for (int q = 1; q < n; ++q) {
+      const double coeff = a[q] / bp[q - 1];
+      bp[q] = b[q] - coeff * c[q - 1];
+      rp[q] = r[q] - coeff * rp[q - 1];
+    }
+    x[n - 1] = rp[n - 1] / bp[n - 1];
+    for (int q = n - 2; q >= 0; --q) x[q] = (rp[q] - c[q] * x[q + 1]) / bp[q];
+  }
+
+  // Implicit vertical viscous step of eval_duvw for one column
+  // (src/nhwave.F:690-822 DU, 850-1010 DV, 1012-1182 DW) with BC_Z0 = 1:
+  // on entry F holds DU + dt R2 (the explicit update), on exit the solution.
+  // which = 0 DU, 1 DV, 2 DW.
+  void vertical_viscous(int i, int j, int which) {
+    const int n = Kend - Kbeg + 1;
+    std::vector<double> A(n), B(n), C(n), Rhs(n), X(n);
+    const double Schmidt = p.schmidt, Dc = D(i, j);
+    // face viscosity between levels k1 and k2 (uniform Cmu, CmuR, CmuVt)
+    const double nuz = 0.5 * (((Cmu + Cmu) + CmuR) + CmuR) + 0.5 * (CmuVt + CmuVt) / Schmidt;
+    A3& F = which == 0 ? DU : which == 1 ? DV : DW;
+    for (int k = Kbeg; k <= Kend; ++k) {
+      const int q = k - Kbeg;
+      A[q] = k == Kbeg ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k - 1)));
+      C[q] = k == Kend ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k + 1)));
+      if (which < 2) {
+        B[q] = 1.0 - A[q] - C[q];
+        Rhs[q] = F(i, j, k);
+        if (k == Kend) Rhs[q] = Rhs[q] + dt * (which == 0 ? Wsx(i, j) : Wsy(i, j)) / dsig(k);
+      } else if (k == Kbeg) {
+        B[q] = 1.0 - C[q] + dt / (Dc * Dc) * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1)));
+        const double Wbot = -DeltH(i, j) - U(i, j, Kbeg) * DelxH(i, j) - V(i, j, Kbeg) * DelyH(i, j);
+        Rhs[q] = F(i, j, k) + dt / Dc * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1))) * Wbot;
+      } else if (k == Kend) {
+        B[q] = 1.0 - A[q] + dt / (Dc * Dc) * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1)));
+        const double Wtop = (Eta(i, j) - Eta0(i, j)) / dt + U(i, j, Kend) * DelxEta(i, j) + V(i, j, Kend) * DelyEta(i, j);
+        Rhs[q] = F(i, j, k) + dt / Dc * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1))) * Wtop;
+      } else {
+        B[q] = 1.0 - A[q] - C[q];
+        Rhs[q] = F(i, j, k);
+      }
+    }
+    trig(A, B, C, Rhs, X, n);
+    for (int k = Kbeg; k <= Kend; ++k) F(i, j, k) = X[k - Kbeg];
   }
 
   // ------------------------------------------------------- get_UVW/vel_bc
@@ -1723,6 +1920,7 @@ struct Model {
   int eval_duvw(int ISTEP) {
     const double al = ALPHA[ISTEP - 1], be = BETA[ISTEP - 1];
     int st = NHW_OK;
+    if (p.viscous_flow) diffusion();
     R1s.fill(0.0);
     for (int j = Jbeg; j <= Jend; ++j)
       for (int i = Ibeg; i <= Iend; ++i) {
@@ -1752,6 +1950,11 @@ struct Model {
                         1.0 / dsig(k) * (Gz(i, j, k + 1) - Gz(i, j, k)) - fcor * DU(i, j, k) + SourceY(i, j);
           R4(i, j, k) = -1.0 / dx * (Hx(i + 1, j, k) - Hx(i, j, k)) - 1.0 / dy * (Hy(i, j + 1, k) - Hy(i, j, k)) -
                         1.0 / dsig(k) * (Hz(i, j, k + 1) - Hz(i, j, k));
+          if (p.viscous_flow) {   // + Diffxx + Diffxy etc. (src/nhwave.F:642-679)
+            R2(i, j, k) = R2(i, j, k) + Diffxx(i, j, k) + Diffxy(i, j, k);
+            R3(i, j, k) = R3(i, j, k) + Diffyx(i, j, k) + Diffyy(i, j, k);
+            R4(i, j, k) = R4(i, j, k) + Diffzx(i, j, k) + Diffzy(i, j, k);
+          }
         }
       }
     for (int i = Ibeg; i <= Iend; ++i)
@@ -1769,6 +1972,11 @@ struct Model {
         if (Mask(i, j) == 0) continue;
         for (int k = Kbeg; k <= Kend; ++k) DW(i, j, k) = DW(i, j, k) + dt * R4(i, j, k);
       }
+    if (p.viscous_flow)   // DU, DV, DW in turn, implicit in the vertical
+      for (int which = 0; which < 3; ++which)
+        for (int i = Ibeg; i <= Iend; ++i)
+          for (int j = Jbeg; j <= Jend; ++j)
+            if (Mask(i, j) != 0) vertical_viscous(i, j, which);
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = Ibeg; i <= Iend; ++i)
@@ -1804,6 +2012,12 @@ struct Model {
         }
     get_UVW();
     get_Omega();
+    // eval_turb (src/nhwave.F:6544-6686) with IVTURB = IHTURB = 1.  The
+    // reference calls it after sponge_damping, which reads no viscosity.
+    if (p.viscous_flow) {
+      CmuVt = p.cvs;
+      CmuHt = p.chs;
+    }
     return st;
   }
 

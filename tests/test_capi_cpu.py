@@ -43,7 +43,7 @@ def test_status_strings(gpu_lib):
     assert "DT_MIN" in lib.status_string(lib.ERR_DT_MIN)
 
 
-@pytest.mark.parametrize("field,value", [("viscous_flow", 1), ("barotropic", 0),
+@pytest.mark.parametrize("field,value", [("barotropic", 0),
                                          ("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 2), ("Kglob", 65),
                                          ("wavemaker", -1)])
 def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
@@ -52,6 +52,20 @@ def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     h = ctypes.c_void_p()
     st = gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h))
     assert st == lib.ERR_UNSUPPORTED and not h.value
+
+
+@pytest.mark.parametrize("fields", [dict(ivturb=10), dict(ihturb=2), dict(ivturb=3, ihturb=10), dict(bc_z0=5)])
+def test_viscous_models_other_than_constant_rejected(fields, gpu_lib):
+    """VISCOUS_FLOW = T runs with IVTURB = IHTURB = 1 (constant viscosities) on
+    a free-slip bed only; the k-epsilon / LES models and bed friction are
+    rejected on the host."""
+    from nhwave_gb300 import default_params, lib
+    p = default_params(viscous_flow=1, **fields)
+    h = ctypes.c_void_p()
+    assert gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h)) == lib.ERR_UNSUPPORTED and not h.value
+    for bad in (dict(schmidt=0.0), dict(viscous_number=0.0)):
+        p = default_params(viscous_flow=1, **bad)
+        assert gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h)) == lib.ERR_ARG and not h.value
 
 
 @pytest.mark.parametrize("field,value", [("Mglob", 0), ("dx", 0.0), ("precision", 7), ("time_order", 4),

@@ -14,8 +14,10 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
-# plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east side
-OPEN_CASES = CASES + ["tiny_open"]
+# plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east
+# side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
+# in tiny_visc_dt the viscous limit sets dt)
+MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -64,7 +66,7 @@ def test_setup_bit_exact(name, oracle_mod, gpu_lib):
 
 
 @pytest.mark.parametrize("hllc", [0, 1])
-@pytest.mark.parametrize("name", OPEN_CASES)
+@pytest.mark.parametrize("name", MORE_CASES)
 def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
     """estimate_dt .. fluxes, and a hydrostatic eval_duvw, match operation for
     operation, with HLL and with HLLC face fluxes (src/nhwave.F:1705-1709)."""
@@ -140,7 +142,7 @@ def step_pinned(g, o):
                 obj.sponge_damping()
 
 
-@pytest.mark.parametrize("name", OPEN_CASES)
+@pytest.mark.parametrize("name", MORE_CASES)
 def test_steps_fp64(name, oracle_mod, gpu_lib):
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod)
@@ -180,7 +182,7 @@ def test_slide_free_running(oracle_mod, gpu_lib):
     g.close()
 
 
-@pytest.mark.parametrize("name", OPEN_CASES)
+@pytest.mark.parametrize("name", MORE_CASES)
 def test_steps_fp32_ir(name, oracle_mod, gpu_lib):
     from nhwave_gb300 import fields as F
     g, o = _pair(name, oracle_mod, precision=1, tol=1e-10)

@@ -333,3 +333,65 @@ def test_flume_stokes_inflow_follows_the_formula(oracle_mod):
         assert o.step() == 0
         ph = pi / 2 - sigma * o.scalars().time
         assert _west_boundary_eta(o) == pytest.approx(0.5 * A * math.cos(ph) + e2 * math.cos(2 * ph), abs=1e-12)
+
+
+def _viscous_channel(oracle_mod, M, N, K, u_profile, T, **kw):
+    """Flat 1 m deep channel started from a velocity profile U (K, N); runs to
+    time T and returns (time, U interior (K, N, M))."""
+    from nhwave_gb300 import default_params, fields as F
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.2, dy=0.2, dt_ini=0.01, dt_max=0.02, tol=1e-10,
+                       itmax=2000, viscous_flow=1, visc=1e-6, **kw)
+    uvw = np.zeros((3, K, N, M))
+    uvw[0] = u_profile[:, :, None]
+    o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
+    while o.scalars().time < T:
+        assert o.step() == 0
+    return o.scalars().time, o.get(F.U)[o.shape.interior(F.U)]
+
+
+def test_viscous_vertical_mode_decays_at_the_diffusion_rate(oracle_mod):
+    """Implicit vertical viscous step (src/nhwave.F:690-1182, trig :13182-13224)
+    with IVTURB = 1: a depth-mean-free shear U = U0 cos(pi sigma) in a flat
+    channel decays as exp(-nu lambda t), lambda = (2 - 2 cos(pi/K)) / (D dsig)^2
+    the discrete Neumann eigenvalue, nu = VISCOSITY + Cvs / Schmidt."""
+    K = 10
+    sig = (np.arange(K) + 0.5) / K
+    prof = 0.01 * np.cos(np.pi * sig)[:, None] * np.ones((1, 3))
+    t, u = _viscous_channel(oracle_mod, 80, 3, K, prof, 2.0, cvs=0.01, chs=0.0)
+    amp = 2 * np.mean(u[:, 1, 40] * np.cos(np.pi * sig)) / 0.01
+    nu = 1e-6 + 0.01
+    lam = (2 - 2 * math.cos(math.pi / K)) * K * K
+    assert amp == pytest.approx(math.exp(-nu * lam * t), rel=2e-3)
+
+
+def test_viscous_horizontal_mode_decays_at_the_diffusion_rate(oracle_mod):
+    """Explicit horizontal viscous terms (diffusion, src/nhwave.F:6785-7141)
+    with IHTURB = 1: a cross-channel profile U = U0 cos(pi y / W) decays by
+    exp(-nu lambda t) more than the same run without viscosity (whose decay
+    is the flux scheme's own), lambda = (2 - 2 cos(pi/N)) / dy^2."""
+    N, K = 10, 4
+    y = (np.arange(N) + 0.5) * 0.2
+    prof = 0.01 * np.ones((K, 1)) * np.cos(np.pi * y / (N * 0.2))[None, :]
+    amps = []
+    for chs in (0.0, 0.05):
+        t, u = _viscous_channel(oracle_mod, 40, N, K, prof, 1.5, cvs=0.0, chs=chs)
+        amps.append(2 * np.mean(u[2, :, 20] * np.cos(np.pi * y / (N * 0.2))) / 0.01)
+    lam = (2 - 2 * math.cos(math.pi / N)) / 0.04
+    assert amps[1] / amps[0] == pytest.approx(math.exp(-0.05 * lam * t), rel=0.01)
+
+
+def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):
+    """VISCOUS_FLOW = T with zero viscosities: the tridiagonal systems are the
+    identity and the explicit terms vanish, so the run equals the inviscid
+    one up to the seeding viscosity of the first stage (9e-11 m^2/s)."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    outs = []
+    for vf in (0, 1):
+        p, d, e, u = S.make("tiny_c2")
+        p.tol, p.itmax = 1e-12, 5000
+        p.viscous_flow, p.visc, p.cvs, p.chs = vf, 0.0, 0.0, 0.0
+        o = oracle_mod.Oracle(p, d, e, u)
+        for _ in range(5):
+            assert o.step() == 0
+        outs.append(o.get(F.ETA)[o.shape.interior(F.ETA)])
+    assert rel_l2(outs[1], outs[0]) < 1e-9
