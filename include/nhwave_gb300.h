@@ -93,14 +93,15 @@ typedef struct nhw_params {
   int32_t time_order;                      /* 1,2,3 <- TIME_ORDER FIRST/SECOND/THIRD  */
   int32_t hllc;                            /* HLLC: 1 HLLC face fluxes, 0 HLL          */
   int32_t viscous_flow;                    /* VISCOUS_FLOW: 1 needs IVTURB = IHTURB = 1
-                                              (constant eddy viscosities) and BC_Z0 = 1 */
+                                              (constant eddy viscosities)             */
   int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
   int32_t itmax; double tol;               /* ITMAX TOL                               */
   int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
                                               2 no-slip wall; BC_X0 = 3 wave inflow
                                               with a LEF_* wavemaker; BC_Xn = 6
                                               Orlanski radiation (open east side)     */
-  int32_t bc_z0;                           /* BC_Z0 (1)                               */
+  int32_t bc_z0;                           /* BC_Z0: 1 free-slip bed, 2 no-slip,
+                                              5 friction law (Ibot, Cd0, Zob)          */
   double  visc;                            /* VISCOSITY (initial Cmu)                 */
   double  slat;                            /* slat -> fcor                            */
   double  wind_u, wind_v;                  /* WindU WindV (Iws = 1)                   */
@@ -145,6 +146,9 @@ typedef struct nhw_params {
   double  schmidt;                         /* Schmidt                                 */
   double  viscous_number;                  /* VISCOUS_NUMBER: dt limit of the explicit
                                               horizontal viscous terms                */
+  /* bed friction of BC_Z0 = 5 (src/initialize.F:466-468) */
+  int32_t ibot;                            /* Ibot: 1 drag coefficient Cd0, 2 roughness Zob */
+  double  cd0, zob;                        /* Cd0 Zob                                 */
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

@@ -902,12 +902,72 @@ struct OpVelBcB {
     const R WzLt = (R)S.zWL[c], WzRb = (R)S.zWR[c], UzLt = (R)S.zUL[c], VzLt = (R)S.zVL[c];
     const R vtop = (R)(S.sc->turb ? S.visc_top_t : S.visc_top);
     const int KB = S.KB, KE = S.KE;
+    // bed stress (src/nhwave.F:4806-4847) for BC_Z0 = 2 (no slip) and 5 (friction)
+    const R dxh = (R)S.DelxH[c], dyh = (R)S.DelyH[c];
+    const R Abot = sqrt((R)1.0 + dxh * dxh + dyh * dyh), Bbot = sqrt((R)1.0 + dxh * dxh);
+    // Cmu + CmuR + CmuVt at the bed level (CmuR = 0)
+    const R nub = (R)(S.v_cmu + 0.0 + (S.viscous ? (S.sc->turb ? S.v_cvs : S.v_cmut0) : 0.0));
+    R Fext_Bot1 = (R)0, Fext_Bot2 = (R)0;
+    R DelxUzR = (R)0, DelxVzR = (R)0, DelxWzR = (R)0, DelyUzR = (R)0, DelyVzR = (R)0, DelyWzR = (R)0;
+    if (S.bc_z0 != 1) {
+      DelxUzR = dx_(S.zUR); DelxVzR = dx_(S.zVR); DelxWzR = dx_(S.zWR);
+      DelyUzR = dy_(S.zUR); DelyVzR = dy_(S.zVR); DelyWzR = dy_(S.zWR);
+      const long long ok = i3(S, i, j, KB);
+      const R du0 = (R)S.DU[ok], dv0 = (R)S.DV[ok], dw0 = (R)S.DW[ok];
+      const R DUprime = (du0 - dxh * dw0) / Bbot;
+      // "DU(i,j,Kbeg)* +(1.0+DelxH**2)*DV(i,j,Kbeg)" in the reference multiplies
+      // the two terms, so on a flat bed DVprime is 0
+      const R DVprime = (-(dxh * dyh * du0 * (((R)1.0 + dxh * dxh) * dv0)) - dyh * dw0) / Abot / Bbot;
+      const R DUmag = sqrt(DUprime * DUprime + DVprime * DVprime);
+      const R Dz1 = (R)0.5 * Dij * (R)S.dsig[KB] / Abot;
+      R Cdrag = (R)S.cd0;
+      if (S.ibot != 1) {
+        const R lg = (R)kKappa / log(Dz1 / (R)(S.zob / 30.0));
+        Cdrag = lg * lg;
+      }
+      Cdrag = rmin<R>(Cdrag, nub / Dz1 / (DUmag + (R)kSmall) * Dij);
+      R TauBot1 = (R)0, TauBot2 = (R)0;
+      if (S.bc_z0 == 2) {
+        TauBot1 = DUprime / Dij / Dz1 * nub;
+        TauBot2 = DVprime / Dij / Dz1 * nub;
+      } else {
+        TauBot1 = Cdrag * DUprime * DUmag / (Dij * Dij);
+        TauBot2 = Cdrag * DVprime * DUmag / (Dij * Dij);
+      }
+      Fext_Bot1 = Bbot * TauBot1;
+      Fext_Bot2 = (dxh * dyh * TauBot1 + Abot * TauBot2) / Bbot;
+    }
+    const R vbot = (R)(kSmall + S.v_cmu + 0.0 + (S.viscous ? (S.sc->turb ? S.v_cvs : S.v_cmut0) : 0.0));
+    const R UzRb = (R)S.zUR[c], VzRb = (R)S.zVR[c];
     for (int k = 1; k <= NG; ++k) {
       const long long ob = i3(S, i, j, KB - k), oi = i3(S, i, j, KB + k - 1);
       const long long ot = i3(S, i, j, KE + k), os = i3(S, i, j, KE - k + 1);
       S.DW[ob] = (T)((R)2.0 * Dij * WzRb - (R)S.DW[oi]);
-      S.DU[ob] = S.DU[oi];
-      S.DV[ob] = S.DV[oi];
+      if (S.bc_z0 == 1) {
+        S.DU[ob] = S.DU[oi];
+        S.DV[ob] = S.DV[oi];
+      } else {   // stress ghosts (src/nhwave.F:4869-4903)
+        const R dsb = (R)(S.sigc[KB + k - 1] - S.sigc[KB - k]);
+        const R DUi = (R)S.DU[oi], DVi = (R)S.DV[oi], DWi = (R)S.DW[oi];
+        R du = DUi - dsb * (Fext_Bot1 * (Dij * Dij / Abot / vbot) + dxh * (DWi - Dij * WzRb) / (dsb / (R)2.0) +
+                            Dij * Dij / (Abot * Abot) *
+                                (-(R)2.0 * dxh * DelxUzR - ((R)1.0 - dxh * dxh) * DelxWzR -
+                                 dyh * (DelyUzR + DelxVzR - dxh * DelyWzR)));
+        const R DUbot_old = (R)2.0 * Dij * UzRb - DUi;
+        if (DUbot_old > (R)0) du = rmin<R>((R)3.0 * DUbot_old, rmax<R>((R)-1.0 * DUbot_old, du));
+        else if (DUbot_old < (R)0) du = rmax<R>((R)3.0 * DUbot_old, rmin<R>((R)-1.0 * DUbot_old, du));
+        if (Dij < MinDepBC) du = DUi;
+        R dv = DVi - dsb * (Fext_Bot2 * (Dij * Dij / Abot / vbot) + dyh * (DWi - Dij * WzRb) / (dsb / (R)2.0) +
+                            Dij * Dij / (Abot * Abot) *
+                                (-(R)2.0 * dyh * DelyVzR - ((R)1.0 - dyh * dyh) * DelyWzR -
+                                 dxh * (DelxVzR + DelyUzR - dyh * DelxWzR)));
+        const R DVbot_old = (R)2.0 * Dij * VzRb - DVi;
+        if (DVbot_old > (R)0) dv = rmin<R>((R)3.0 * DVbot_old, rmax<R>((R)-1.0 * DVbot_old, dv));
+        else if (DVbot_old < (R)0) dv = rmax<R>((R)3.0 * DVbot_old, rmin<R>((R)-1.0 * DVbot_old, dv));
+        if (Dij < MinDepBC) dv = DVi;
+        S.DU[ob] = (T)du;
+        S.DV[ob] = (T)dv;
+      }
       const R dsg = (R)(S.sigc[KE + k] - S.sigc[KE - k + 1]);
       const R DWs = (R)S.DW[os], DUs = (R)S.DU[os], DVs = (R)S.DV[os];
       S.DW[ot] = (T)((R)2.0 * Dij * WzLt - DWs);
@@ -1058,7 +1118,7 @@ struct OpDiffusion {
 };
 
 // Implicit vertical viscous step of eval_duvw (src/nhwave.F:690-822 DU,
-// 850-1010 DV, 1012-1182 DW, BC_Z0 = 1), one thread per wet interior column,
+// 850-1010 DV, 1012-1182 DW), one thread per wet interior column,
 // after the new D, Eta and eta slopes: DU/DV/DW hold the explicit update
 // DU + dt R2 on entry.  The tridiagonal systems are solved by trig's
 // elimination (src/nhwave.F:13182-13224) in FP64, with the eliminated
@@ -1087,9 +1147,25 @@ struct OpVertVisc {
       auto coefs = [&](int k, double& b, double& r) {
         const double f = (double)Fv[i3(S, i, j, k)];
         if (which < 2) {
-          b = 1.0 - A(k) - C(k);
-          r = f;
-          if (k == KE) r = r + dt * (which == 0 ? S.Wsx[c] : S.Wsy[c]) / dsg[k];
+          if (k == KB && S.bc_z0 == 2)   // no-slip bed
+            b = 1.0 - C(k) + dt / (Dc * Dc) * (S.v_cmu + 0.0 + cvt / S.v_schmidt) / (0.5 * dsg[k] * dsg[k]);
+          else
+            b = 1.0 - A(k) - C(k);
+          if (k == KB && S.bc_z0 == 5) {   // friction law: bed stress in the first right-hand side
+            const double Dz1 = 0.5 * Dc * dsg[KB];
+            double Cdrag = S.cd0;
+            if (S.ibot != 1) {
+              const double lg = 1. / kKappa * log(30.0 * Dz1 / S.zob);
+              Cdrag = 1. / (lg * lg);
+            }
+            const double u = (double)S.U[i3(S, i, j, k)], v = (double)S.V[i3(S, i, j, k)];
+            const double Ustar2 = Cdrag * sqrt(u * u + v * v) * (which == 0 ? u : v);
+            r = f - dt * Ustar2 / dsg[k];
+          } else if (k == KE) {
+            r = f + dt * (which == 0 ? S.Wsx[c] : S.Wsy[c]) / dsg[k];
+          } else {
+            r = f;
+          }
         } else if (k == KB) {
           const double q = 0.25 * dsg[k] * (dsg[k] + dsg[k - 1]);
           b = 1.0 - C(k) + dt / (Dc * Dc) * nuz / q;

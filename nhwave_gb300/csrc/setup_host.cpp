@@ -26,7 +26,7 @@ int check_params(const nhw_params& p) {
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
   if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
   // viscous flow with constant viscosities only (no k-epsilon / LES), free-slip bed
-  if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1 || p.bc_z0 != 1)) return NHW_ERR_UNSUPPORTED;
+  if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
@@ -35,7 +35,10 @@ int check_params(const nhw_params& p) {
                    p.wavemaker == NHW_WM_LEF_STK || p.wavemaker == NHW_WM_LEF_CON;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
-  if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
+  // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
+  if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
+  if (p.bc_z0 == 5 && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
+  if (p.bc_z0 == 5 && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
   if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_CON) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;

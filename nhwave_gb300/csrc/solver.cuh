@@ -230,6 +230,8 @@ class Solver final : public SolverBase {
     S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
     S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
     S.visc_top_t = S.visc_top;
+    S.v_cmu = p.visc;
+    S.bc_z0 = p.bc_z0; S.ibot = p.ibot; S.cd0 = p.cd0; S.zob = p.zob;
     S.viscous = p.viscous_flow ? 1 : 0;
     if (S.viscous) {   // seeding viscosity of initial (src/initialize.F:3172-3195)
       const double tke = (double)1.e-9f, eps = (double)1.e-9f;

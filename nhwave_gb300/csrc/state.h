@@ -29,6 +29,7 @@ constexpr int NCOEF = 15;      // Poisson stencil entries (src/pressure.F:276-27
 constexpr double kPi = (double)3.141592653f;
 constexpr double kSmall = (double)1.0e-16f;
 constexpr double kOrlSmall = (double)1.e-16f;   // the Orlanski boundary's 1.e-16 (default real)
+constexpr double kKappa = (double)0.41f;        // von Karman constant (default real parameter)
 constexpr double kLarge = 10000000.0;
 constexpr double kGrav = (double)9.81f;
 constexpr double kRho0 = 1000.0;
@@ -94,6 +95,9 @@ struct Dev {
   // VISCOUS_NUMBER.  viscous = 0 on the inviscid path.
   int viscous;
   double v_cmu, v_cmut0, v_cvs, v_chs, v_schmidt, v_number;
+  // bed (BC_Z0): 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
+  int bc_z0, ibot;
+  double cd0, zob;
   double alpha[3], beta[3];        // SSP-RK coefficients
   // wavemaker (INT_LIN / INT_SOL): host-computed constants
   int wavemaker;

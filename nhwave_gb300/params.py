@@ -65,6 +65,7 @@ class NhwParams(ctypes.Structure):
         ("ivturb", ctypes.c_int32), ("ihturb", ctypes.c_int32), ("rng", ctypes.c_int32),
         ("cvs", ctypes.c_double), ("chs", ctypes.c_double), ("schmidt", ctypes.c_double),
         ("viscous_number", ctypes.c_double),
+        ("ibot", ctypes.c_int32), ("cd0", ctypes.c_double), ("zob", ctypes.c_double),
     ]
 
     def copy(self) -> "NhwParams":
@@ -110,6 +111,7 @@ def default_params(**kw) -> NhwParams:
     p.ivturb = p.ihturb = 1
     p.cvs = p.chs = 0.0
     p.schmidt, p.viscous_number = 1.0, 1.0 / 6.0
+    p.ibot, p.cd0, p.zob = 1, 0.0, 1e-4
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(f"unknown nhw_params field {k!r}")
@@ -174,6 +176,7 @@ def read_input(path: str) -> NhwParams:
     p.bc_x0, p.bc_xn = i("BC_X0", 1), i("BC_Xn", 1)
     p.bc_y0, p.bc_yn = i("BC_Y0", 1), i("BC_Yn", 1)
     p.bc_z0 = i("BC_Z0", 1)
+    p.ibot, p.cd0, p.zob = i("Ibot", 1), f("Cd0", 0.0), f("Zob", 1e-4)
     p.visc, p.slat = f("VISCOSITY", 1e-6), f("slat", 0.0)
     if p.viscous_flow:
         p.ivturb, p.ihturb, p.rng = i("IVTURB", 1), i("IHTURB", 1), _logical(kv.get("RNG", "F"))
@@ -234,8 +237,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
         if getattr(p, name) not in ok:
             return (f"{name.upper()}={getattr(p, name)} (walls 1/2, the west inflow 3 and the east "
                     "Orlanski boundary 6 are on the GPU path)")
-    if p.bc_z0 != 1:
-        return "BC_Z0 must be 1 (free slip)"
+    if p.bc_z0 not in (1, 2, 5):
+        return f"BC_Z0={p.bc_z0} (free slip 1, no slip 2 and the friction law 5 are on the GPU path)"
+    if p.bc_z0 == 5 and p.ibot not in (1, 2):
+        return f"Ibot={p.ibot} (1 drag coefficient, 2 roughness height)"
     return None
 
 

@@ -200,6 +200,18 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         # as tiny_visc, with a horizontal viscosity large enough that VISCOUS_NUMBER limits dt
         kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.05, chs=20.0), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_visc_noslip":
+        # tiny_visc on a no-slip bed (BC_Z0 = 2)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=2), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_visc_fric":
+        # tiny_visc with the bed friction law (BC_Z0 = 5) and a drag coefficient (Ibot = 1)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=5, ibot=1, cd0=0.006), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_fric_log":
+        # the inviscid small bar with the friction law from a roughness height (Ibot = 2)
+        kw = dict(dict(bc_z0=5, ibot=2, zob=1e-3), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)

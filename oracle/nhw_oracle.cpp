@@ -67,6 +67,7 @@ const double Grav = (double)9.81f;
 const double Zero = 0.0;
 const double Rho0 = 1000.0;
 const double kOrlSmall = (double)1.e-16f;   // the Orlanski boundary's 1.e-16 (default real)
+const double Kappa = (double)0.41f;         // von Karman constant (default real parameter)
 const int Nghost = 2;
 
 // ---------------------------------------------------------------- cnoidal
@@ -220,7 +221,7 @@ struct Model {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
     if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
-    if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1 || p.bc_z0 != 1)) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
@@ -233,7 +234,10 @@ struct Model {
           !cnoidal_start(x2, m, xs))
         return NHW_ERR_ARG;
     }
-    if (p.bc_z0 != 1) return NHW_ERR_UNSUPPORTED;
+    // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
+    if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
+    if (p.bc_z0 == 5 && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
+    if (p.bc_z0 == 5 && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
     // index (src/initialize.F:1339-1419), serial build
     Mloc = p.Mglob + 2 * Nghost; Nloc = p.Nglob + 2 * Nghost; Kloc = p.Kglob + 2 * Nghost;
     Mloc1 = Mloc + 1; Nloc1 = Nloc + 1; Kloc1 = Kloc + 1;
@@ -1410,9 +1414,10 @@ struct Model {
   }
 
   // Implicit vertical viscous step of eval_duvw for one column
-  // (src/nhwave.F:690-822 DU, 850-1010 DV, 1012-1182 DW) with BC_Z0 = 1:
-  // on entry F holds DU + dt R2 (the explicit update), on exit the solution.
-  // which = 0 DU, 1 DV, 2 DW.
+  // (src/nhwave.F:690-822 DU, 850-1010 DV, 1012-1182 DW): on entry F holds
+  // DU + dt R2 (the explicit update), on exit the solution.  which = 0 DU,
+  // 1 DV, 2 DW.  The bed enters DU and DV: no slip (BC_Z0 = 2) in the first
+  // diagonal, the friction law (5) in the first right-hand side.
   void vertical_viscous(int i, int j, int which) {
     const int n = Kend - Kbeg + 1;
     std::vector<double> A(n), B(n), C(n), Rhs(n), X(n);
@@ -1425,9 +1430,25 @@ struct Model {
       A[q] = k == Kbeg ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k - 1)));
       C[q] = k == Kend ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k + 1)));
       if (which < 2) {
-        B[q] = 1.0 - A[q] - C[q];
-        Rhs[q] = F(i, j, k);
-        if (k == Kend) Rhs[q] = Rhs[q] + dt * (which == 0 ? Wsx(i, j) : Wsy(i, j)) / dsig(k);
+        if (k == Kbeg && p.bc_z0 == 2)
+          B[q] = 1.0 - C[q] + dt / (Dc * Dc) * (Cmu + CmuR + CmuVt / Schmidt) / (0.5 * dsig(k) * dsig(k));
+        else
+          B[q] = 1.0 - A[q] - C[q];
+        if (k == Kbeg && p.bc_z0 == 5) {
+          const double Dz1 = 0.5 * Dc * dsig(Kbeg);
+          double Cdrag = p.cd0;
+          if (p.ibot != 1) {
+            const double lg = 1. / Kappa * std::log(30.0 * Dz1 / p.zob);
+            Cdrag = 1. / (lg * lg);
+          }
+          const double Ustar2 = Cdrag * std::sqrt(U(i, j, k) * U(i, j, k) + V(i, j, k) * V(i, j, k)) *
+                                (which == 0 ? U(i, j, k) : V(i, j, k));
+          Rhs[q] = F(i, j, k) - dt * Ustar2 / dsig(k);
+        } else if (k == Kend) {
+          Rhs[q] = F(i, j, k) + dt * (which == 0 ? Wsx(i, j) : Wsy(i, j)) / dsig(k);
+        } else {
+          Rhs[q] = F(i, j, k);
+        }
       } else if (k == Kbeg) {
         B[q] = 1.0 - C[q] + dt / (Dc * Dc) * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1)));
         const double Wbot = -DeltH(i, j) - U(i, j, Kbeg) * DelxH(i, j) - V(i, j, Kbeg) * DelyH(i, j);
@@ -1522,6 +1543,13 @@ struct Model {
     KBC_bottom();
     delxFun_3D(UzL, DelxUzL); delxFun_3D(VzL, DelxVzL); delxFun_3D(WzL, DelxWzL);
     delyFun_3D(UzL, DelyUzL); delyFun_3D(VzL, DelyVzL); delyFun_3D(WzL, DelyWzL);
+    // bed-face slopes, read by the stress ghosts of BC_Z0 = 2, 5
+    A3 DelxUzR, DelxVzR, DelxWzR, DelyUzR, DelyVzR, DelyWzR;
+    if (p.bc_z0 != 1) {
+      for (A3* a : {&DelxUzR, &DelxVzR, &DelxWzR, &DelyUzR, &DelyVzR, &DelyWzR}) a->init(Mloc, Nloc, Kloc1);
+      delxFun_3D(UzR, DelxUzR); delxFun_3D(VzR, DelxVzR); delxFun_3D(WzR, DelxWzR);
+      delyFun_3D(UzR, DelyUzR); delyFun_3D(VzR, DelyVzR); delyFun_3D(WzR, DelyWzR);
+    }
     const double MinDepBC = (double)0.01f;
     const double visc_top = Small + 0.5 * (Cmu + CmuR + CmuVt + Cmu + CmuR + CmuVt);
     for (int j = Jbeg; j <= Jend; ++j)
@@ -1530,11 +1558,62 @@ struct Model {
         const double Atop = std::sqrt(1.0 + dxe * dxe + dye * dye);
         const double Fext_Wind1 = 1.0 / Atop * ((1 - dxe * dxe) * Wsx(i, j) - dxe * dye * Wsy(i, j));
         const double Fext_Wind2 = 1.0 / Atop * ((1 - dye * dye) * Wsy(i, j) - dxe * dye * Wsx(i, j));
+        // bed stress (src/nhwave.F:4806-4847)
+        const double dxh = DelxH(i, j), dyh = DelyH(i, j);
+        const double Abot = std::sqrt(1.0 + dxh * dxh + dyh * dyh), Bbot = std::sqrt(1.0 + dxh * dxh);
+        double Fext_Bot1 = 0.0, Fext_Bot2 = 0.0;
+        if (p.bc_z0 != 1) {
+          const double DUprime = (DU(i, j, Kbeg) - dxh * DW(i, j, Kbeg)) / Bbot;
+          // the reference's "DU(i,j,Kbeg)* +(1.0+DelxH**2)*DV(i,j,Kbeg)" multiplies
+          // the two terms (a unary plus after '*'), so on a flat bed DVprime is 0
+          const double DVprime =
+              (-(dxh * dyh * DU(i, j, Kbeg) * ((1.0 + dxh * dxh) * DV(i, j, Kbeg))) - dyh * DW(i, j, Kbeg)) / Abot / Bbot;
+          const double DUmag = std::sqrt(DUprime * DUprime + DVprime * DVprime);
+          const double Dz1 = 0.5 * Dij * dsig(Kbeg) / Abot;
+          const double Z0 = p.zob / 30.0;
+          double Cdrag = p.ibot == 1 ? p.cd0 : (Kappa / std::log(Dz1 / Z0)) * (Kappa / std::log(Dz1 / Z0));
+          Cdrag = dmin(Cdrag, (Cmu + CmuR + CmuVt) / Dz1 / (DUmag + Small) * Dij);
+          double TauBot1 = Zero, TauBot2 = Zero;
+          if (p.bc_z0 == 2) {
+            TauBot1 = DUprime / Dij / Dz1 * (Cmu + CmuR + CmuVt);
+            TauBot2 = DVprime / Dij / Dz1 * (Cmu + CmuR + CmuVt);
+          } else if (p.bc_z0 == 5) {
+            TauBot1 = Cdrag * DUprime * DUmag / (Dij * Dij);
+            TauBot2 = Cdrag * DVprime * DUmag / (Dij * Dij);
+          }
+          Fext_Bot1 = Bbot * TauBot1;
+          Fext_Bot2 = (dxh * dyh * TauBot1 + Abot * TauBot2) / Bbot;
+        }
         for (int k = 1; k <= Nghost; ++k) {
-          // bottom, free slip (Bc_Z0 = 1)
+          // bottom
           DW(i, j, Kbeg - k) = 2.0 * Dij * WzR(i, j, Kbeg) - DW(i, j, Kbeg + k - 1);
-          DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1);
-          DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1);
+          if (p.bc_z0 == 1) {   // free slip
+            DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1);
+            DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1);
+          } else {   // stress ghosts (src/nhwave.F:4869-4903)
+            const double dsb = sigc(Kbeg + k - 1) - sigc(Kbeg - k);
+            const double vb = Small + Cmu + CmuR + CmuVt;
+            DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1) -
+                dsb * (Fext_Bot1 * (Dij * Dij / Abot / vb) +
+                       dxh * (DW(i, j, Kbeg + k - 1) - Dij * WzR(i, j, Kbeg)) / (dsb / 2.0) +
+                       Dij * Dij / (Abot * Abot) *
+                           (-2.0 * dxh * DelxUzR(i, j, Kbeg) - (1.0 - dxh * dxh) * DelxWzR(i, j, Kbeg) -
+                            dyh * (DelyUzR(i, j, Kbeg) + DelxVzR(i, j, Kbeg) - dxh * DelyWzR(i, j, Kbeg))));
+            const double DUbot_old = 2.0 * Dij * UzR(i, j, Kbeg) - DU(i, j, Kbeg + k - 1);
+            if (DUbot_old > 0.) DU(i, j, Kbeg - k) = dmin(3.0 * DUbot_old, dmax(-1.0 * DUbot_old, DU(i, j, Kbeg - k)));
+            else if (DUbot_old < 0.) DU(i, j, Kbeg - k) = dmax(3.0 * DUbot_old, dmin(-1.0 * DUbot_old, DU(i, j, Kbeg - k)));
+            if (Dij < MinDepBC) DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1);
+            DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1) -
+                dsb * (Fext_Bot2 * (Dij * Dij / Abot / vb) +
+                       dyh * (DW(i, j, Kbeg + k - 1) - Dij * WzR(i, j, Kbeg)) / (dsb / 2.0) +
+                       Dij * Dij / (Abot * Abot) *
+                           (-2.0 * dyh * DelyVzR(i, j, Kbeg) - (1.0 - dyh * dyh) * DelyWzR(i, j, Kbeg) -
+                            dxh * (DelxVzR(i, j, Kbeg) + DelyUzR(i, j, Kbeg) - dyh * DelxWzR(i, j, Kbeg))));
+            const double DVbot_old = 2.0 * Dij * VzR(i, j, Kbeg) - DV(i, j, Kbeg + k - 1);
+            if (DVbot_old > 0.) DV(i, j, Kbeg - k) = dmin(3.0 * DVbot_old, dmax(-1.0 * DVbot_old, DV(i, j, Kbeg - k)));
+            else if (DVbot_old < 0.) DV(i, j, Kbeg - k) = dmax(3.0 * DVbot_old, dmin(-1.0 * DVbot_old, DV(i, j, Kbeg - k)));
+            if (Dij < MinDepBC) DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1);
+          }
           // surface
           const double dsg = sigc(Kend + k) - sigc(Kend - k + 1);
           DW(i, j, Kend + k) = 2.0 * Dij * WzL(i, j, Kend1) - DW(i, j, Kend - k + 1);

@@ -44,7 +44,7 @@ def test_status_strings(gpu_lib):
 
 
 @pytest.mark.parametrize("field,value", [("barotropic", 0),
-                                         ("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 2), ("Kglob", 65),
+                                         ("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 3), ("Kglob", 65),
                                          ("wavemaker", -1)])
 def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     from nhwave_gb300 import default_params, lib
@@ -54,11 +54,10 @@ def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     assert st == lib.ERR_UNSUPPORTED and not h.value
 
 
-@pytest.mark.parametrize("fields", [dict(ivturb=10), dict(ihturb=2), dict(ivturb=3, ihturb=10), dict(bc_z0=5)])
+@pytest.mark.parametrize("fields", [dict(ivturb=10), dict(ihturb=2), dict(ivturb=3, ihturb=10)])
 def test_viscous_models_other_than_constant_rejected(fields, gpu_lib):
-    """VISCOUS_FLOW = T runs with IVTURB = IHTURB = 1 (constant viscosities) on
-    a free-slip bed only; the k-epsilon / LES models and bed friction are
-    rejected on the host."""
+    """VISCOUS_FLOW = T runs with IVTURB = IHTURB = 1 (constant viscosities)
+    only; the k-epsilon / LES models are rejected on the host."""
     from nhwave_gb300 import default_params, lib
     p = default_params(viscous_flow=1, **fields)
     h = ctypes.c_void_p()

@@ -16,8 +16,8 @@ pytestmark = pytest.mark.gpu
 CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east
 # side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
-# in tiny_visc_dt the viscous limit sets dt)
-MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt"]
+# in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds)
+MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -225,7 +225,8 @@ def test_golden_fixtures(name, gpu_lib):
 
 # tiny_flume_open: LEF_LIN in at the west, out through an Orlanski east side;
 # tiny_flume_stk / _con: second-order Stokes and cnoidal waves fed in
-FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open"]
+FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open",
+          "tiny_fric_log"]   # and the friction law from a roughness height: log() of CUDA and libm
 
 
 @pytest.mark.parametrize("name", FLUMES)

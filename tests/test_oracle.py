@@ -395,3 +395,21 @@ def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):
             assert o.step() == 0
         outs.append(o.get(F.ETA)[o.shape.interior(F.ETA)])
     assert rel_l2(outs[1], outs[0]) < 1e-9
+
+
+def test_bed_stress_slows_the_near_bed_flow(oracle_mod):
+    """BC_Z0 = 2 (no slip) and 5 (friction law, src/nhwave.F:4806-4903 and
+    the first rows of the implicit vertical step): the shear mode
+    U = U0 cos(pi sigma), whose bed value is +U0, loses more of its amplitude
+    over a no-slip or frictional bed than over a free-slip one."""
+    K = 10
+    sig = (np.arange(K) + 0.5) / K
+    prof = 0.05 * np.cos(np.pi * sig)[:, None] * np.ones((1, 3))
+    amps = {}
+    for key, kw in (("free", dict(bc_z0=1)), ("noslip", dict(bc_z0=2)),
+                    ("fric", dict(bc_z0=5, ibot=1, cd0=0.05))):
+        t, u = _viscous_channel(oracle_mod, 40, 3, K, prof, 1.0, cvs=0.01, chs=0.0, **kw)
+        amps[key] = 2 * np.mean(u[:, 1, 20] * np.cos(np.pi * sig)) / 0.05
+        assert np.isfinite(u).all()
+    assert amps["noslip"] < amps["free"] - 0.01
+    assert amps["fric"] < amps["free"] - 0.002

@@ -76,8 +76,11 @@ def test_out_of_scope_reason(tmp_path):
     f.write_text(SAMPLE.replace("HLLC = F", "HLLC = T"))
     p = P.read_input(str(f))
     assert p.hllc == 1 and P.unsupported_reason(p) is None
-    f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 2"))
+    f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 3"))
     assert "BC_Z0" in P.unsupported_reason(P.read_input(str(f)))
+    f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 5"))
+    p = P.read_input(str(f))
+    assert p.bc_z0 == 5 and P.unsupported_reason(p) is None
     # a generator of the reference that the path does not build is rejected, not run as NONE
     f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_JON"))
     p = P.read_input(str(f))
