@@ -67,11 +67,12 @@ enum nhw_precision {
                        depth/eta/mask fields, FP64 Poisson residual + refinement     */
 };
 
-/* INT_*: internal source strip (src/source_terms.F); LEF_*: waves fed through
- * the west boundary, which then needs BC_X0 = 3: linear, solitary,
- * second-order Stokes and cnoidal (src/waves.F:92-170, 518-560, 808-903) */
+/* INT_*: internal source strip (src/source_terms.F); LEF_* and WAV_CUR:
+ * waves fed through the west boundary, which then needs BC_X0 = 3: linear,
+ * solitary, second-order Stokes, cnoidal, and linear on a current ramped up
+ * over TRAMP (src/waves.F:92-170, 518-560, 706-756, 808-903) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
-                     NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6 };
+                     NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 

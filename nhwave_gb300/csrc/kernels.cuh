@@ -204,8 +204,10 @@ struct OpWaveBC {
     const double hfx = S.Hfx[i2(S, S.IB, j)];
     const bool inner = j >= S.JB && j <= S.JE;
     const int Nl = S.Nloc;
-    if (S.lef == 3) {   // LEF_LIN
+    if (S.lef == 3 || S.lef == 7) {   // LEF_LIN; WAV_CUR adds the ramped current (src/waves.F:706-756)
       const double A = S.lef_amp;
+      double Ucur = 0.0;
+      if (S.lef == 7) Ucur = (S.tramp > 0.0 ? tanh(TIME / S.tramp) : 1.0) * S.cur_wave;
       const double phs = S.yc[j] * S.lef_sinth * S.lef_wn;
       const double arg = kPi / 2 - S.lef_segma * TIME + phs;
       const double cs = cos(arg), sn = sin(arg);
@@ -217,7 +219,7 @@ struct OpWaveBC {
       for (int k = S.KB; k <= S.KE; ++k) {
         const double Zlev = S.sigc[k] * Dn;
         const double ch = cosh(S.lef_wn * Zlev), sh = sinh(S.lef_wn * Zlev);
-        const double u = 0.5 * A * S.lef_segma * ch / S.lef_shd * cs - S.lef_stokes * 1.0;
+        const double u = Ucur + 0.5 * A * S.lef_segma * ch / S.lef_shd * cs - S.lef_stokes * 1.0;
         S.Uin[j + Nl * k] = u * S.lef_costh;
         S.Win[j + Nl * k] = 0.5 * A * S.lef_segma * sh / S.lef_shd * sn;
         S.Vin[j + Nl * k] = u * S.lef_sinth;

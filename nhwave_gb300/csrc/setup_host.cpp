@@ -31,15 +31,14 @@ int check_params(const nhw_params& p) {
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-  const bool lef = p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_LEF_SOL ||
-                   p.wavemaker == NHW_WM_LEF_STK || p.wavemaker == NHW_WM_LEF_CON;
+  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
   if (p.bc_z0 == 5 && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (p.bc_z0 == 5 && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_CON) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_WAV_CUR) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
@@ -306,7 +305,7 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     h.wm_celerity = std::sqrt(kGravH * Dep * (1.0 + A / Dep));
     h.wm_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
     h.wm_xstart = 4.0 * Dep / std::sqrt(A / Dep);
-  } else if (p.wavemaker == NHW_WM_LEF_LIN) {   // src/waves.F:820-829
+  } else if (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_WAV_CUR) {   // src/waves.F:720-730, 820-829
     h.lef_segma = 2.0 * kPiH / p.per_wave;
     h.lef_wn = wave_number(h.lef_segma, p.dep_wave);
     const double wl = 2.0 * kPiH / h.lef_wn;

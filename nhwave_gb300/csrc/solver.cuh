@@ -654,7 +654,7 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON) ? p.wavemaker : 0;
+    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR) ? p.wavemaker : 0;
     S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave; S.lef_per = p.per_wave;
     S.lef_e2 = h.lef_e2; S.lef_u2 = h.lef_u2;
     S.con_mod = h.con_mod; S.con_len = h.con_len; S.con_ytr = h.con_ytr; S.con_ck = h.con_ck; S.con_x0 = h.con_x0;

@@ -13,8 +13,9 @@ import ctypes
 
 NHW_FP64 = 0
 NHW_FP32_IR = 1
-WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON = 0, 1, 2, 3, 4, 5, 6
-WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON)   # fed through the west boundary (BC_X0 = 3)
+WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR = range(8)
+# fed through the west boundary (BC_X0 = 3)
+WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
 SLIDE_NONE, SLIDE_RIGID_3D = 0, 1
 DEPTH_CELL_CENTER, DEPTH_CELL_GRID = 0, 1
@@ -190,7 +191,7 @@ def read_input(path: str) -> NhwParams:
     # LEF_JON, INT_IRR, FLUX_LR, ...) is kept as WM_OTHER and rejected, not run
     # as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
-             "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON}
+             "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
@@ -229,9 +230,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF:
-        return "WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK and LEF_CON are on the GPU path)"
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON and WAV_CUR "
+                "are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
-        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK or LEF_CON wavemaker"
+        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON or WAV_CUR wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
         ok = {"bc_x0": (1, 2, 3), "bc_xn": (1, 2, 6)}.get(name, (1, 2))
         if getattr(p, name) not in ok:
@@ -251,7 +253,7 @@ def cells(p: NhwParams) -> int:
 __all__ = [
     "NhwParams", "NhwScalars", "default_params", "read_input", "unsupported_reason", "cells",
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
-    "WM_LEF_STK", "WM_LEF_CON", "WM_LEF", "WM_OTHER",
+    "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_LEF", "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",
 ]

@@ -147,15 +147,17 @@ def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5,
                sponge=2.0, **kw):
     """Flat flume fed through its west boundary (BC_X0 = 3): a linear wave
     (LEF_LIN, amplitude `amp`, period `per`), a solitary wave (LEF_SOL,
-    height `amp`), a second-order Stokes wave (LEF_STK, amplitude `amp`) or a
-    cnoidal wave (LEF_CON, height `amp`); sponge layer and wall at the east
-    end, walls along the sides; at rest initially."""
-    from .params import WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK
+    height `amp`), a second-order Stokes wave (LEF_STK, amplitude `amp`), a
+    cnoidal wave (LEF_CON, height `amp`) or a linear wave on a current
+    (WAV_CUR, `cur_wave`, `tramp`); sponge layer and wall at the east end,
+    walls along the sides; at rest initially."""
+    from .params import WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_WAV_CUR
     p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
                        dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
                        tol=1e-8, itmax=1000, total_time=20.0)
     p.bc_x0 = 3
-    p.wavemaker = {"LIN": WM_LEF_LIN, "SOL": WM_LEF_SOL, "STK": WM_LEF_STK, "CON": WM_LEF_CON}[kind]
+    p.wavemaker = {"LIN": WM_LEF_LIN, "SOL": WM_LEF_SOL, "STK": WM_LEF_STK, "CON": WM_LEF_CON,
+                   "CUR": WM_WAV_CUR}[kind]
     p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
     p.sponge_on = 1
     p.sponge_east_width = sponge
@@ -212,6 +214,10 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         # the inviscid small bar with the friction law from a roughness height (Ibot = 2)
         kw = dict(dict(bc_z0=5, ibot=2, zob=1e-3), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_flume_cur":
+        # LEF_LIN on a current of 0.05 m/s ramped up over TRAMP = 0.5 s (WAV_CUR), out at an Orlanski east side
+        kw = dict(dict(cur_wave=0.05, tramp=0.5, bc_xn=6, sponge_on=0), **kw)
+        out = wave_flume("CUR", M=64, N=4, K=5, dx=0.1, dy=0.1, **kw)
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)

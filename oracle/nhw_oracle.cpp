@@ -226,7 +226,7 @@ struct Model {
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON;
+    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.wavemaker == NHW_WM_LEF_CON) {   // the reference stops when these fail
       double l, x2, m, xs;
@@ -660,7 +660,11 @@ struct Model {
   // waves fed through the west boundary (src/nhwave.F:5514-5565), evaluated
   // at the new TIME once per step.
   void update_wave_bc() {
-    if (p.wavemaker == NHW_WM_LEF_LIN) {
+    if (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_WAV_CUR) {
+      // WAV_CUR (src/waves.F:706-756) is LEF_LIN plus the current
+      // Ucur = tanh(TIME/TRamp) Cur_Wave in the horizontal velocities
+      double Ucur = 0.0;
+      if (p.wavemaker == NHW_WM_WAV_CUR) Ucur = (p.tramp > 0.0 ? std::tanh(TIME / p.tramp) : 1.0) * p.cur_wave;
       const double Segma = 2.0 * pi / p.per_wave;
       const double Wave_Number = wave_dispersion(Segma);
       const double Wave_Length = 2.0 * pi / Wave_Number;
@@ -679,10 +683,10 @@ struct Model {
           const double Zlev = sigc(k) * Din_X0(j);
           const double cs = std::cos(pi / 2 - Segma * TIME + Phs_Lag);
           const double sn = std::sin(pi / 2 - Segma * TIME + Phs_Lag);
-          Uin_X0(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+          Uin_X0(j, k) = (Ucur + 0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
                          std::cos(th);
           Win_X0(j, k) = 0.5 * p.amp_wave * Segma * std::sinh(Wave_Number * Zlev) / shd * sn;
-          Vin_X0(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+          Vin_X0(j, k) = (Ucur + 0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
                          std::sin(th);
         }
     } else if (p.wavemaker == NHW_WM_LEF_SOL) {

@@ -413,3 +413,25 @@ def test_bed_stress_slows_the_near_bed_flow(oracle_mod):
         assert np.isfinite(u).all()
     assert amps["noslip"] < amps["free"] - 0.01
     assert amps["fric"] < amps["free"] - 0.002
+
+
+def test_wave_current_inflow_carries_the_current(oracle_mod):
+    """WAV_CUR (src/waves.F:706-756): the linear boundary wave of LEF_LIN on a
+    current Cur_Wave ramped up as tanh(t/TRamp).  Until the current reaches
+    the far side, the domain gains, over the plain LEF_LIN run, the volume
+    the current carries in: Cur_Wave TRamp ln cosh(t/TRamp) h W."""
+    from nhwave_gb300 import params as P, scenarios as S
+    gain = []
+    for wm in (P.WM_WAV_CUR, P.WM_LEF_LIN):
+        p, d, e, u = S.make("tiny_flume_cur")
+        p.wavemaker = wm
+        p.tol, p.itmax = 1e-8, 5000
+        o = oracle_mod.Oracle(p, d, e, u)
+        m0 = o.mass()
+        while o.scalars().time < 3.0:
+            assert o.step() == 0
+        gain.append(o.mass() - m0)
+        t = o.scalars().time
+    width = p.Nglob * p.dy
+    expect = p.cur_wave * p.tramp * math.log(math.cosh(t / p.tramp)) * p.dep_wave * width
+    assert gain[0] - gain[1] == pytest.approx(expect, rel=0.05)
