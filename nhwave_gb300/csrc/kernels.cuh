@@ -833,6 +833,20 @@ struct OpVelBcA {
 };
 // lateral ghost cells of U, V, W, DU, DV, DW (src/nhwave.F:4416-4621): one
 // thread per (ghost column or ghost row, level); corner columns stay untouched
+// Wall friction factor of a BC = 5 side (src/nhwave.F:4486-4493): h the
+// spacing across the wall, a and b the first interior cell's tangential
+// velocities; Cmu + CmuHt of the cell
+template <class T>
+__device__ __forceinline__ double wall_phi(const Dev<T>& S, double h, double a, double b) {
+  double Cdrag = S.cd0;
+  if (S.ibot != 1) {
+    const double lg = 1. / kKappa * log(30.0 * h / 2.0 / S.zob);
+    Cdrag = 1. / (lg * lg);
+  }
+  const double cmh = S.viscous ? (S.sc->turb ? S.v_chs : S.v_cmut0) : 0.0;
+  const double Phi = h * Cdrag * sqrt(a * a + b * b) / (S.v_cmu + cmh);
+  return dmin_(Phi, 2.0);
+}
 struct OpVelBcLat {
   static constexpr const char* kName = "vel_bc_lat";
   template <class T>
@@ -860,6 +874,24 @@ struct OpVelBcLat {
       };
       const T u = (T)orl(S.U0, S.U00), v = (T)orl(S.V0, S.V00), w = (T)orl(S.W0, S.W00);
       const double d = S.D[i2(S, i, j)];
+      S.U[o] = u; S.V[o] = v; S.W[o] = w;
+      S.DU[o] = (T)(d * (double)u); S.DV[o] = (T)(d * (double)v); S.DW[o] = (T)(d * (double)w);
+    } else if (jj && (i < S.IB ? S.bc_x0 : S.bc_xn) == 5) {  // wall friction (src/nhwave.F:4486-4500, 4583-4598)
+      const bool west = i < S.IB;
+      const int g = west ? S.IB - i : i - S.IE;   // ghost offset 1, 2
+      const long long q = i3(S, mirror(i, S.IB, S.IE), j, k), e = i3(S, west ? S.IB : S.IE, j, k);
+      const double Phi = wall_phi(S, S.dx, (double)S.V[e], (double)S.W[e]);
+      const double d = S.D[i2(S, g - 1, j)];   // the reference's D(i,j) with i the ghost offset
+      const T u = -S.U[q], v = (T)((1.0 - Phi) * (double)S.V[q]), w = (T)((1.0 - Phi) * (double)S.W[q]);
+      S.U[o] = u; S.V[o] = v; S.W[o] = w;
+      S.DU[o] = (T)(d * (double)u); S.DV[o] = (T)(d * (double)v); S.DW[o] = (T)(d * (double)w);
+    } else if (!jj && (j < S.JB ? S.bc_y0 : S.bc_yn) == 5) {  // wall friction (src/nhwave.F:4676-4691, 4737-4752)
+      const bool south = j < S.JB;
+      const int g = south ? S.JB - j : j - S.JE;
+      const long long q = i3(S, i, mirror(j, S.JB, S.JE), k), e = i3(S, i, south ? S.JB : S.JE, k);
+      const double Phi = wall_phi(S, S.dy, (double)S.U[e], (double)S.W[e]);
+      const double d = S.D[i2(S, i, g - 1)];   // D(i,j) with j the ghost offset
+      const T u = (T)((1.0 - Phi) * (double)S.U[q]), v = -S.V[q], w = (T)((1.0 - Phi) * (double)S.W[q]);
       S.U[o] = u; S.V[o] = v; S.W[o] = w;
       S.DU[o] = (T)(d * (double)u); S.DV[o] = (T)(d * (double)v); S.DW[o] = (T)(d * (double)w);
     } else if (jj) {  // west/east ghost columns of interior rows

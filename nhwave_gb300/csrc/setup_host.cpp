@@ -28,16 +28,18 @@ int check_params(const nhw_params& p) {
   // viscous flow with constant viscosities only (no k-epsilon / LES), free-slip bed
   if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
+  // lateral sides: 1 free slip, 2 no slip, 5 wall friction; BC_Xn = 6 Orlanski
   for (int b : {p.bc_y0, p.bc_yn})
-    if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
-  if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
+    if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
+  if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;
   const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
   // west inflow (BC_X0 = 3) only with a wave fed through it
-  if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+  if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
-  if (p.bc_z0 == 5 && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
-  if (p.bc_z0 == 5 && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
+  const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
+  if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
+  if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
   if (p.wavemaker < 0 || p.wavemaker > NHW_WM_WAV_CUR) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;

@@ -235,13 +235,13 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
         return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON or WAV_CUR wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
-        ok = {"bc_x0": (1, 2, 3), "bc_xn": (1, 2, 6)}.get(name, (1, 2))
+        ok = {"bc_x0": (1, 2, 3, 5), "bc_xn": (1, 2, 5, 6)}.get(name, (1, 2, 5))
         if getattr(p, name) not in ok:
-            return (f"{name.upper()}={getattr(p, name)} (walls 1/2, the west inflow 3 and the east "
-                    "Orlanski boundary 6 are on the GPU path)")
+            return (f"{name.upper()}={getattr(p, name)} (walls 1/2, wall friction 5, the west inflow 3 "
+                    "and the east Orlanski boundary 6 are on the GPU path)")
     if p.bc_z0 not in (1, 2, 5):
         return f"BC_Z0={p.bc_z0} (free slip 1, no slip 2 and the friction law 5 are on the GPU path)"
-    if p.bc_z0 == 5 and p.ibot not in (1, 2):
+    if 5 in (p.bc_z0, p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn) and p.ibot not in (1, 2):
         return f"Ibot={p.ibot} (1 drag coefficient, 2 roughness height)"
     return None
 

@@ -207,12 +207,19 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=2), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_visc_fric":
-        # tiny_visc with the bed friction law (BC_Z0 = 5) and a drag coefficient (Ibot = 1)
-        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=5, ibot=1, cd0=0.006), **kw)
+        # tiny_visc with the friction law on the bed (BC_Z0 = 5) and on the south, north and east
+        # walls (BC = 5), from a drag coefficient (Ibot = 1)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=5, bc_y0=5, bc_yn=5, bc_xn=5,
+                       ibot=1, cd0=0.006), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_fric_log":
-        # the inviscid small bar with the friction law from a roughness height (Ibot = 2)
-        kw = dict(dict(bc_z0=5, ibot=2, zob=1e-3), **kw)
+        # the inviscid small bar with the friction law on the bed and the side walls, from a
+        # roughness height (Ibot = 2)
+        kw = dict(dict(bc_z0=5, bc_y0=5, bc_yn=5, bc_xn=5, ibot=2, zob=1e-3), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_wallfric":
+        # the inviscid small bar with wall friction (BC = 5) on every side, drag coefficient 0.01
+        kw = dict(dict(bc_x0=5, bc_xn=5, bc_y0=5, bc_yn=5, ibot=1, cd0=0.01), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_flume_cur":
         # LEF_LIN on a current of 0.05 m/s ramped up over TRAMP = 0.5 s (WAV_CUR), out at an Orlanski east side

@@ -224,10 +224,10 @@ struct Model {
     if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
-      if (b != 1 && b != 2) return NHW_ERR_UNSUPPORTED;
-    if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
+      if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
+    if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
     const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
-    if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+    if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.wavemaker == NHW_WM_LEF_CON) {   // the reference stops when these fail
       double l, x2, m, xs;
       if (!(p.amp_wave > 0) || !cnoidal(p.amp_wave, p.dep_wave, p.per_wave, l, x2, m) ||
@@ -236,8 +236,9 @@ struct Model {
     }
     // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
     if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
-    if (p.bc_z0 == 5 && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
-    if (p.bc_z0 == 5 && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
+    const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
+    if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
+    if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
     // index (src/initialize.F:1339-1419), serial build
     Mloc = p.Mglob + 2 * Nghost; Nloc = p.Nglob + 2 * Nghost; Kloc = p.Kglob + 2 * Nghost;
     Mloc1 = Mloc + 1; Nloc1 = Nloc + 1; Kloc1 = Kloc + 1;
@@ -1471,12 +1472,80 @@ struct Model {
   }
 
   // ------------------------------------------------------- get_UVW/vel_bc
+  // Wall friction factor of a BC = 5 side (src/nhwave.F:4486-4493): h is the
+  // grid spacing across the wall, a and b the tangential velocities of the
+  // first interior cell
+  double wall_phi(double h, double a, double b) const {
+    double Cdrag = p.cd0;
+    if (p.ibot != 1) {
+      const double lg = 1. / Kappa * std::log(30.0 * h / 2.0 / p.zob);
+      Cdrag = 1. / (lg * lg);
+    }
+    const double Phi = h * Cdrag * std::sqrt(a * a + b * b) / (Cmu + CmuHt);
+    return dmin(Phi, 2.0);
+  }
+
   void vel_bc() {
     const int sx0 = p.bc_x0 == 1 ? 1 : -1, sxn = p.bc_xn == 1 ? 1 : -1;
     const int sy0 = p.bc_y0 == 1 ? 1 : -1, syn = p.bc_yn == 1 ? 1 : -1;
+    // Wall friction (BC = 5): tangential ghosts (1 - Phi) times the mirror;
+    // the ghost momenta take D(i,j) with the ghost offset for i (x sides) or j
+    // (y sides), as the reference writes them (src/nhwave.F:4486-4500,
+    // 4583-4598, 4676-4691, 4737-4752)
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (p.bc_x0 == 5) {
+          const double Phi = wall_phi(dx, V(Ibeg, j, k), W(Ibeg, j, k));
+          for (int i = 1; i <= Nghost; ++i) {
+            U(Ibeg - i, j, k) = -U(Ibeg + i - 1, j, k);
+            V(Ibeg - i, j, k) = (1.0 - Phi) * V(Ibeg + i - 1, j, k);
+            W(Ibeg - i, j, k) = (1.0 - Phi) * W(Ibeg + i - 1, j, k);
+            DU(Ibeg - i, j, k) = D(i, j) * U(Ibeg - i, j, k);
+            DV(Ibeg - i, j, k) = D(i, j) * V(Ibeg - i, j, k);
+            DW(Ibeg - i, j, k) = D(i, j) * W(Ibeg - i, j, k);
+          }
+        }
+        if (p.bc_xn == 5) {
+          const double Phi = wall_phi(dx, V(Iend, j, k), W(Iend, j, k));
+          for (int i = 1; i <= Nghost; ++i) {
+            U(Iend + i, j, k) = -U(Iend - i + 1, j, k);
+            V(Iend + i, j, k) = (1.0 - Phi) * V(Iend - i + 1, j, k);
+            W(Iend + i, j, k) = (1.0 - Phi) * W(Iend - i + 1, j, k);
+            DU(Iend + i, j, k) = D(i, j) * U(Iend + i, j, k);
+            DV(Iend + i, j, k) = D(i, j) * V(Iend + i, j, k);
+            DW(Iend + i, j, k) = D(i, j) * W(Iend + i, j, k);
+          }
+        }
+      }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        if (p.bc_y0 == 5) {
+          const double Phi = wall_phi(dy, U(i, Jbeg, k), W(i, Jbeg, k));
+          for (int j = 1; j <= Nghost; ++j) {
+            U(i, Jbeg - j, k) = (1.0 - Phi) * U(i, Jbeg + j - 1, k);
+            V(i, Jbeg - j, k) = -V(i, Jbeg + j - 1, k);
+            W(i, Jbeg - j, k) = (1.0 - Phi) * W(i, Jbeg + j - 1, k);
+            DU(i, Jbeg - j, k) = D(i, j) * U(i, Jbeg - j, k);
+            DV(i, Jbeg - j, k) = D(i, j) * V(i, Jbeg - j, k);
+            DW(i, Jbeg - j, k) = D(i, j) * W(i, Jbeg - j, k);
+          }
+        }
+        if (p.bc_yn == 5) {
+          const double Phi = wall_phi(dy, U(i, Jend, k), W(i, Jend, k));
+          for (int j = 1; j <= Nghost; ++j) {
+            U(i, Jend + j, k) = (1.0 - Phi) * U(i, Jend - j + 1, k);
+            V(i, Jend + j, k) = -V(i, Jend - j + 1, k);
+            W(i, Jend + j, k) = (1.0 - Phi) * W(i, Jend - j + 1, k);
+            DU(i, Jend + j, k) = D(i, j) * U(i, Jend + j, k);
+            DV(i, Jend + j, k) = D(i, j) * V(i, Jend + j, k);
+            DW(i, Jend + j, k) = D(i, j) * W(i, Jend + j, k);
+          }
+        }
+      }
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = 1; i <= Nghost; ++i) {
+          if (p.bc_x0 == 5) break;
           if (p.bc_x0 == 3) {   // inflow (src/nhwave.F:4468-4476)
             U(Ibeg - i, j, k) = 2.0 * Uin_X0(j, k) - U(Ibeg + i - 1, j, k);
             V(Ibeg - i, j, k) = 2.0 * Vin_X0(j, k) - V(Ibeg + i - 1, j, k);
@@ -1496,6 +1565,7 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = 1; i <= Nghost; ++i) {
+          if (p.bc_xn == 5) break;
           if (p.bc_xn == 6) {   // Orlanski radiation (src/nhwave.F:4599-4621)
             auto orl = [&](A3& X0, A3& X00) {
               double Cg = -(X0(Iend + i - 1, j, k) - X00(Iend + i - 1, j, k) + kOrlSmall) /
@@ -1521,6 +1591,7 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int i = Ibeg; i <= Iend; ++i)
         for (int j = 1; j <= Nghost; ++j) {
+          if (p.bc_y0 == 5) break;
           U(i, Jbeg - j, k) = sy0 * U(i, Jbeg + j - 1, k);
           V(i, Jbeg - j, k) = -V(i, Jbeg + j - 1, k);
           W(i, Jbeg - j, k) = sy0 * W(i, Jbeg + j - 1, k);
@@ -1531,6 +1602,7 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int i = Ibeg; i <= Iend; ++i)
         for (int j = 1; j <= Nghost; ++j) {
+          if (p.bc_yn == 5) break;
           U(i, Jend + j, k) = syn * U(i, Jend - j + 1, k);
           V(i, Jend + j, k) = -V(i, Jend - j + 1, k);
           W(i, Jend + j, k) = syn * W(i, Jend - j + 1, k);

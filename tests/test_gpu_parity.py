@@ -16,8 +16,10 @@ pytestmark = pytest.mark.gpu
 CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east
 # side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
-# in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds)
-MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric"]
+# in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds),
+# and wall friction (BC = 5) on the sides
+MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric",
+                      "tiny_wallfric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 

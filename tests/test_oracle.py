@@ -435,3 +435,19 @@ def test_wave_current_inflow_carries_the_current(oracle_mod):
     width = p.Nglob * p.dy
     expect = p.cur_wave * p.tramp * math.log(math.cosh(t / p.tramp)) * p.dep_wave * width
     assert gain[0] - gain[1] == pytest.approx(expect, rel=0.05)
+
+
+def test_wall_friction_slows_the_flow_along_the_walls(oracle_mod):
+    """BC_Y0 = BC_Yn = 5 (src/nhwave.F:4676-4691, 4737-4752): the ghosts
+    along a wall take (1 - Phi) times the mirrored tangential velocity, Phi
+    growing with the drag, so a flow along the channel loses more at the
+    walls than between free-slip walls (Phi = 0)."""
+    N, K = 10, 4
+    y = (np.arange(N) + 0.5) * 0.2
+    prof = 0.01 * np.ones((K, 1)) * np.cos(np.pi * y / (N * 0.2))[None, :]
+    edge = {}
+    for bc in (1, 5):
+        t, u = _viscous_channel(oracle_mod, 40, N, K, prof, 1.0, cvs=0.0, chs=0.05, bc_y0=bc, bc_yn=bc,
+                                ibot=1, cd0=5.0)
+        edge[bc] = abs(u[2, 0, 20])
+    assert edge[5] < 0.97 * edge[1]
