@@ -67,12 +67,14 @@ enum nhw_precision {
                        depth/eta/mask fields, FP64 Poisson residual + refinement     */
 };
 
-/* INT_*: internal source strip (src/source_terms.F); LEF_* and WAV_CUR:
- * waves fed through the west boundary, which then needs BC_X0 = 3: linear,
- * solitary, second-order Stokes, cnoidal, and linear on a current ramped up
- * over TRAMP (src/waves.F:92-170, 518-560, 706-756, 808-903) */
+/* INT_*: internal source strip (src/source_terms.F); LEF_*, WAV_CUR and
+ * FOCUSED: waves fed through the west boundary, which then needs BC_X0 = 3:
+ * linear, solitary, second-order Stokes, cnoidal, linear on a current ramped
+ * up over TRAMP, and a focused group of NWAVE linear components
+ * (src/waves.F:92-170, 518-560, 638-756, 808-903) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
-                     NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7 };
+                     NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7,
+                     NHW_WM_FOCUSED = 8 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 
@@ -150,6 +152,14 @@ typedef struct nhw_params {
   /* bed friction of BC_Z0 = 5 (src/initialize.F:466-468) */
   int32_t ibot;                            /* Ibot: 1 drag coefficient Cd0, 2 roughness Zob */
   double  cd0, zob;                        /* Cd0 Zob                                 */
+  /* FOCUSED wave group (src/initialize.F:709-781): NWAVE >= 2 components of
+     frequencies spread over normalized_delta_f around f_center, focusing at
+     x_breaking, t_breaking; amplitude Slope_group/NWAVE/k (k_center when
+     Component_Amp_Type = 1); depth_comp; sd_return (read with AMP for the
+     LEF_ / WAV_ makers only, so 0 for FOCUSED inputs) */
+  int32_t nwave, component_amp_type;
+  double  k_center, f_center, x_breaking, t_breaking, slope_group, normalized_delta_f, depth_comp;
+  double  sd_return;
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */

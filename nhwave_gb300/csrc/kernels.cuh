@@ -263,6 +263,32 @@ struct OpWaveBC {
         S.Win[j + Nl * k] = 0.5 * A * Sg * sinh(wk * Zlev) / sh * sn + S.lef_u2 * sinh(2. * wk * Zlev) / sh4 * sn2;
         S.Vin[j + Nl * k] = 0.0;
       }
+    } else if (S.lef == 8) {   // FOCUSED: a group of NWAVE linear components (src/waves.F:638-692)
+      const int nw = S.nwave;
+      const double *Ai = S.foc, *ki = S.foc + nw, *fi = S.foc + 2 * nw;
+      const double tc = TIME - (double)(int)(TIME / 20.0) * 20.0;   // the group repeats every 20 s
+      const double dc = S.foc_dc;
+      double E = 0.0;
+      for (int n = 0; n < nw; ++n) E = E + Ai[n] * cos(-ki[n] * S.foc_xb - 2. * kPi * fi[n] * (tc - S.foc_tb));
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        double u = 0.0, w = 0.0;
+        for (int n = 0; n < nw; ++n) {
+          const double sg = 2. * kPi * fi[n], c = sg / ki[n];
+          const double ph = -ki[n] * S.foc_xb - sg * (tc - S.foc_tb);
+          const double sd = kGrav * (Ai[n] * Ai[n]) / c / dc / 2.;
+          u = u + kGrav * Ai[n] * ki[n] / sg * cosh(ki[n] * Zlev) / cosh(ki[n] * (dc + E)) * cos(ph) -
+              sd * (2 * ki[n] * dc) / sinh(2 * ki[n] * (dc + E)) * cosh(2 * ki[n] * Zlev) * S.foc_sd;
+          w = w + kGrav * Ai[n] * ki[n] / sg * sinh(ki[n] * Zlev) / cosh(ki[n] * (dc + E)) * sin(ph);
+        }
+        S.Uin[j + Nl * k] = u;
+        S.Win[j + Nl * k] = w;
+        S.Vin[j + Nl * k] = 0.0;
+      }
     } else if (S.lef == 6) {   // LEF_CON: cnoidal wave
       const double A = S.lef_amp, Dep = S.lef_dep, m = S.con_mod, ck = S.con_ck, L = S.con_len, Yt = S.con_ytr;
       const double Xcn = cnoidal_cn(S.con_x0 + 2.0 * ck * (-(TIME / S.lef_per)), m);

@@ -32,7 +32,7 @@ int check_params(const nhw_params& p) {
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;
-  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
+  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
@@ -40,12 +40,18 @@ int check_params(const nhw_params& p) {
   const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
   if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_WAV_CUR) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_FOCUSED) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
-  if (p.wavemaker && !(p.per_wave > 0 && p.dep_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && !(p.per_wave > 0 && p.dep_wave > 0)) return NHW_ERR_ARG;
+  // FOCUSED: at least two components (the frequency spacing divides by
+  // NWAVE - 1), at most the reference's 12000
+  if (p.wavemaker == NHW_WM_FOCUSED &&
+      (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0) ||
+       (p.component_amp_type == 1 && !(p.k_center > 0))))
+    return NHW_ERR_ARG;
   if (p.wavemaker == NHW_WM_LEF_CON && !(p.amp_wave > 0)) return NHW_ERR_ARG;
   return NHW_OK;
 }
@@ -333,6 +339,29 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     // left-to-right order up to the trigonometric factor of the step
     h.lef_e2 = (A * A) * wk / 16. * std::cosh(wk * Dep) / (sh * sh * sh) * (2.0 + std::cosh(2. * wk * Dep));
     h.lef_u2 = (double)(3.f / 16.f) * (A * A) * h.lef_segma * wk;
+  } else if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
+    const int nw = p.nwave;
+    const double dc = p.depth_comp;
+    h.foc.assign(3 * (size_t)nw, 0.0);
+    for (int n = 1; n <= nw; ++n) {
+      const double fi = p.f_center - 0.5 * p.normalized_delta_f * p.f_center +
+                        (n - 1.0) * p.normalized_delta_f * p.f_center / (nw - 1.0);
+      const double period = 1.0 / fi;
+      // wave number by Newton's method from the shallow-water guess, to |F| <= 1e-6
+      const double sq = 2.0 * kPiH / period, segmasqr = sq * sq;
+      const double ctmp = std::sqrt(kGravH * dc), xltmp = ctmp * period;
+      double xxk = 2.0 * kPiH / xltmp;
+      for (int it = 0;; ++it) {
+        const double Fk = kGravH * xxk * std::tanh(xxk * dc) - segmasqr;
+        if (std::fabs(Fk) <= (double)1.0e-6f || it > 1000) break;
+        const double th = std::tanh(xxk * dc);
+        const double Fkdif = kGravH * xxk * dc * (1.0 - th * th) + kGravH * std::tanh(xxk * dc);
+        xxk = xxk - Fk / Fkdif;
+      }
+      h.foc[n - 1] = p.component_amp_type == 1 ? p.slope_group / nw / p.k_center : p.slope_group / nw / xxk;
+      h.foc[nw + n - 1] = xxk;
+      h.foc[2 * nw + n - 1] = fi;
+    }
   } else if (p.wavemaker == NHW_WM_LEF_CON) {   // src/waves.F:100-140
     const double A = p.amp_wave, Dep = p.dep_wave;
     double L = 0, Yt = 0, m = 0, Xstart = 0;

@@ -24,6 +24,7 @@ struct HostInit {
   double lef_cel = 0, lef_atmp = 0, lef_xstart = 0, lef_c2 = 0;
   double lef_e2 = 0, lef_u2 = 0;                          // LEF_STK second-order amplitudes
   double con_mod = 0, con_len = 0, con_ytr = 0, con_ck = 0, con_x0 = 0;   // LEF_CON
+  std::vector<double> foc;   // FOCUSED: Amp_i [nwave], k_i [nwave], f_i [nwave]
 };
 
 // Validate parameters against the path's scope; NHW_OK or an error code.

@@ -269,6 +269,9 @@ class Solver final : public SolverBase {
     add(&S.sigc, sizeof(double) * S.Kloc);
     add(&S.xc, sizeof(double) * S.Mloc);
     add(&S.yc, sizeof(double) * S.Nloc);
+    S.nwave = p.wavemaker == NHW_WM_FOCUSED ? p.nwave : 0;
+    S.foc_xb = p.x_breaking; S.foc_tb = p.t_breaking; S.foc_dc = p.depth_comp; S.foc_sd = p.sd_return;
+    if (S.nwave) add((double**)&S.foc, sizeof(double) * 3 * S.nwave);
     for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds, &S.lv_fint})
       add((double**)lv, sizeof(double) * S.Kloc);
     add((T**)&S.lvT, sizeof(T) * 3 * S.Kloc);
@@ -654,7 +657,9 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR) ? p.wavemaker : 0;
+    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED) ? p.wavemaker : 0;
+    if (S.lef == NHW_WM_FOCUSED)
+      NHW_CU(cudaMemcpyAsync((void*)S.foc, h.foc.data(), sizeof(double) * h.foc.size(), cudaMemcpyHostToDevice, st));
     S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave; S.lef_per = p.per_wave;
     S.lef_e2 = h.lef_e2; S.lef_u2 = h.lef_u2;
     S.con_mod = h.con_mod; S.con_len = h.con_len; S.con_ytr = h.con_ytr; S.con_ck = h.con_ck; S.con_x0 = h.con_x0;

@@ -112,6 +112,11 @@ struct Dev {
   double lef_cel, lef_atmp, lef_xstart, lef_c2;
   double lef_e2, lef_u2;                           // LEF_STK second-order amplitudes
   double con_mod, con_len, con_ytr, con_ck, con_x0;   // LEF_CON: m, L, trough, K(m), start phase
+  // FOCUSED: components Amp_i, k_i, f_i ([nwave] each, host-computed), focus
+  // point and time, depth_comp, sd_return
+  const double* foc;
+  int nwave;
+  double foc_xb, foc_tb, foc_dc, foc_sd;
   double *Ein, *Din;               // [Nloc] Ein_X0, Din_X0
   double *Uin, *Vin, *Win;         // [Kloc][Nloc] Uin_X0 .. (index j + Nloc*k)
   // sponge current

@@ -13,9 +13,9 @@ import ctypes
 
 NHW_FP64 = 0
 NHW_FP32_IR = 1
-WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR = range(8)
+WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED = range(9)
 # fed through the west boundary (BC_X0 = 3)
-WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR)
+WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
 SLIDE_NONE, SLIDE_RIGID_3D = 0, 1
 DEPTH_CELL_CENTER, DEPTH_CELL_GRID = 0, 1
@@ -67,6 +67,11 @@ class NhwParams(ctypes.Structure):
         ("cvs", ctypes.c_double), ("chs", ctypes.c_double), ("schmidt", ctypes.c_double),
         ("viscous_number", ctypes.c_double),
         ("ibot", ctypes.c_int32), ("cd0", ctypes.c_double), ("zob", ctypes.c_double),
+        ("nwave", ctypes.c_int32), ("component_amp_type", ctypes.c_int32),
+        ("k_center", ctypes.c_double), ("f_center", ctypes.c_double), ("x_breaking", ctypes.c_double),
+        ("t_breaking", ctypes.c_double), ("slope_group", ctypes.c_double),
+        ("normalized_delta_f", ctypes.c_double), ("depth_comp", ctypes.c_double),
+        ("sd_return", ctypes.c_double),
     ]
 
     def copy(self) -> "NhwParams":
@@ -191,14 +196,22 @@ def read_input(path: str) -> NhwParams:
     # LEF_JON, INT_IRR, FLUX_LR, ...) is kept as WM_OTHER and rejected, not run
     # as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
-             "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR}
+             "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR,
+             "FOCUSED": WM_FOCUSED}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
         p.theta_wave, p.cur_wave = f("THETA", 0.0), f("CUR", 0.0)
+        p.sd_return = f("sd_return", 0.0)
         if wm[:3] == "INT":
             p.xsource_west, p.xsource_east = f("Xsource_West", 0.0), f("Xsource_East", 0.0)
             p.ysource_suth, p.ysource_nrth = f("Ysource_Suth", 0.0), f("Ysource_Nrth", 0.0)
+    if wm[:3] == "FOC":   # src/initialize.F:709-719
+        p.nwave, p.component_amp_type = i("nwave", 0), i("Component_Amp_Type", 1)
+        p.k_center, p.f_center = f("k_center", 0.0), f("f_center", 0.0)
+        p.x_breaking, p.t_breaking = f("x_breaking", 0.0), f("t_breaking", 0.0)
+        p.slope_group, p.normalized_delta_f = f("Slope_group", 0.0), f("normalized_delta_f", 0.0)
+        p.depth_comp = f("depth_comp", 0.0)
     p.sponge_on = _logical(kv.get("SPONGE_ON", "F"))
     if p.sponge_on:
         p.sponge_west_width = f("Sponge_West_Width", 0.0)
@@ -230,10 +243,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF:
-        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON and WAV_CUR "
-                "are on the GPU path)")
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, WAV_CUR and "
+                "FOCUSED are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
-        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON or WAV_CUR wavemaker"
+        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, WAV_CUR or FOCUSED wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
         ok = {"bc_x0": (1, 2, 3, 5), "bc_xn": (1, 2, 5, 6)}.get(name, (1, 2, 5))
         if getattr(p, name) not in ok:
@@ -253,7 +266,8 @@ def cells(p: NhwParams) -> int:
 __all__ = [
     "NhwParams", "NhwScalars", "default_params", "read_input", "unsupported_reason", "cells",
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
-    "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_LEF", "WM_OTHER",
+    "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF",
+    "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",
 ]

@@ -226,8 +226,35 @@ struct Model {
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_WAV_CUR;
+    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+    if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
+      if (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0)) return NHW_ERR_ARG;
+      const int nw = p.nwave;
+      Amp_i.assign(nw, 0.0); k_i.assign(nw, 0.0); f_i.assign(nw, 0.0);
+      for (int n = 1; n <= nw; ++n) {
+        f_i[n - 1] = p.f_center - 0.5 * p.normalized_delta_f * p.f_center +
+                     (n - 1.0) * p.normalized_delta_f * p.f_center / (nw - 1.0);
+        const double period_i = 1.0 / f_i[n - 1];
+        const double segmasqr = (2.0 * pi / period_i) * (2.0 * pi / period_i);
+        const double ctmp = std::sqrt(Grav * p.depth_comp);
+        const double xltmp = ctmp * period_i;
+        double xxk = 2.0 * pi / xltmp;
+        int it = 0;
+        while (true) {
+          const double Fk = Grav * xxk * std::tanh(xxk * p.depth_comp) - segmasqr;
+          if (std::fabs(Fk) <= (double)1.0e-6f || it > 1000) break;
+          const double Fkdif = Grav * xxk * p.depth_comp *
+                                   (1.0 - std::tanh(xxk * p.depth_comp) * std::tanh(xxk * p.depth_comp)) +
+                               Grav * std::tanh(xxk * p.depth_comp);
+          xxk = xxk - Fk / Fkdif;
+          it = it + 1;
+        }
+        k_i[n - 1] = xxk;
+      }
+      for (int n = 0; n < nw; ++n)
+        Amp_i[n] = p.component_amp_type == 1 ? p.slope_group / nw / p.k_center : p.slope_group / nw / k_i[n];
+    }
     if (p.wavemaker == NHW_WM_LEF_CON) {   // the reference stops when these fail
       double l, x2, m, xs;
       if (!(p.amp_wave > 0) || !cnoidal(p.amp_wave, p.dep_wave, p.per_wave, l, x2, m) ||
@@ -632,6 +659,9 @@ struct Model {
     return Wn;
   }
 
+  // FOCUSED wave group components (src/initialize.F:742-781)
+  std::vector<double> Amp_i, k_i, f_i;
+
   // Start phase of the cnoidal boundary wave (src/waves.F:106-130):
   // bisection on [0, 1] for the zero crossing of the elevation.
   bool cnoidal_start(double Ytrough, double Mod1, double& Xstart) {
@@ -740,6 +770,39 @@ struct Model {
                          3. / 16. * (A * A) * Segma * Wave_Number * std::sinh(2. * Wave_Number * Zlev) / sh4 *
                              std::sin(2. * (pi / 2 - Segma * TIME));
           Vin_X0(j, k) = 0.0;
+        }
+    } else if (p.wavemaker == NHW_WM_FOCUSED) {   // src/waves.F:638-692
+      const int nw = p.nwave;
+      const double tc = TIME - (double)(int)(TIME / 20.0) * 20.0;
+      std::vector<double> Segma_i(nw), c_i(nw), eta_i(nw), Stokes_Drift_i(nw);
+      for (int n = 0; n < nw; ++n) {
+        Segma_i[n] = 2. * pi * f_i[n];
+        c_i[n] = Segma_i[n] / k_i[n];
+        eta_i[n] = Amp_i[n] * std::cos(-k_i[n] * p.x_breaking - Segma_i[n] * (tc - p.t_breaking));
+        Stokes_Drift_i[n] = Grav * (Amp_i[n] * Amp_i[n]) / c_i[n] / p.depth_comp / 2.;
+      }
+      for (int j = 1; j <= Nloc; ++j) {
+        Ein_X0(j) = Zero;
+        for (int n = 0; n < nw; ++n) Ein_X0(j) = Ein_X0(j) + eta_i[n];
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+      }
+      const double dc = p.depth_comp;
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j) {
+          const double Zlev = sigc(k) * Din_X0(j);
+          Uin_X0(j, k) = Zero;
+          Win_X0(j, k) = Zero;
+          for (int n = 0; n < nw; ++n) {
+            const double ph = -k_i[n] * p.x_breaking - Segma_i[n] * (tc - p.t_breaking);
+            Uin_X0(j, k) = Uin_X0(j, k) +
+                           Grav * Amp_i[n] * k_i[n] / Segma_i[n] * std::cosh(k_i[n] * Zlev) /
+                               std::cosh(k_i[n] * (dc + Ein_X0(j))) * std::cos(ph) -
+                           Stokes_Drift_i[n] * (2 * k_i[n] * dc) / std::sinh(2 * k_i[n] * (dc + Ein_X0(j))) *
+                               std::cosh(2 * k_i[n] * Zlev) * p.sd_return;
+            Win_X0(j, k) = Win_X0(j, k) + Grav * Amp_i[n] * k_i[n] / Segma_i[n] * std::sinh(k_i[n] * Zlev) /
+                                              std::cosh(k_i[n] * (dc + Ein_X0(j))) * std::sin(ph);
+          }
+          Vin_X0(j, k) = Zero;
         }
     } else if (p.wavemaker == NHW_WM_LEF_CON) {
       const double A = p.amp_wave, Dep = p.dep_wave;

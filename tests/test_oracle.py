@@ -451,3 +451,32 @@ def test_wall_friction_slows_the_flow_along_the_walls(oracle_mod):
                                 ibot=1, cd0=5.0)
         edge[bc] = abs(u[2, 0, 20])
     assert edge[5] < 0.97 * edge[1]
+
+
+def test_focused_group_boundary_elevation(oracle_mod):
+    """FOCUSED (src/waves.F:638-692, components src/initialize.F:742-781):
+    the boundary elevation is the sum of NWAVE linear components
+    a_n cos(-k_n x_b - 2 pi f_n (t - t_b)), frequencies evenly spread over
+    normalized_delta_f f_center, k_n from linear dispersion, a_n =
+    Slope_group / NWAVE / k_n; recomputed here independently."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_flume_foc")
+    p.tol, p.itmax = 1e-8, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    pi = float(np.float32(3.141592653))
+    g = float(np.float32(9.81))
+    nw, h = p.nwave, p.depth_comp
+    f = p.f_center - 0.5 * p.normalized_delta_f * p.f_center + np.arange(nw) * p.normalized_delta_f * p.f_center / (nw - 1)
+    k = np.empty(nw)
+    for n in range(nw):   # linear dispersion, to full precision
+        sig2 = (2 * pi * f[n]) ** 2
+        kk = 2 * pi / (math.sqrt(g * h) / f[n])
+        for _ in range(60):
+            kk -= (g * kk * math.tanh(kk * h) - sig2) / (g * kk * h * (1 - math.tanh(kk * h) ** 2) + g * math.tanh(kk * h))
+        k[n] = kk
+    a = p.slope_group / nw / k
+    for _ in range(30):
+        assert o.step() == 0
+        t = o.scalars().time
+        expect = np.sum(a * np.cos(-k * p.x_breaking - 2 * pi * f * (t - p.t_breaking)))
+        assert _west_boundary_eta(o) == pytest.approx(expect, abs=1e-8)
