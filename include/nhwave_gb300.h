@@ -372,7 +372,9 @@ int nhw_ensemble_destroy(nhw_ensemble* e);
  * work is queued.  U, V, W are (Mglob+4, Nglob+4, Kglob+4), D is
  * (Mglob+4, Nglob+4) and dsig (Kglob+4), all FP64 in the reference's ghosted
  * Fortran layout (column-major, two ghost cells a side).  The caller checks
- * dt against DT_MIN.
+ * dt against DT_MIN.  A viscous run (VISCOUS_FLOW) also takes the minimum
+ * with VISCOUS_NUMBER * min(dx^2, dy^2) / (|CmuHt| + 1e-16), which this call
+ * leaves to the caller (src/nhwave.F:3812-3832).
  *
  * It allocates nothing.  Its reduction scratch is a fixed 65,792-byte device
  * array inside the library, present on every GPU that loads the library
