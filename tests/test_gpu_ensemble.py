@@ -147,3 +147,33 @@ def test_ensemble_of_gmres_members_matches_single_steps(precision, gpu_lib):
         for f in ("ETA", "P", "U", "MASK"):
             fid = getattr(F, f)
             assert np.array_equal(a.get(fid), b.get(fid)), f"{n} {f} differs"
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ensemble_of_the_added_boundaries_and_viscous_flow(precision, solver, gpu_lib):
+    """Members that use the later rows -- viscous flow on a friction bed with
+    friction walls, an Orlanski east side, cnoidal and focused inflow -- step in
+    one ensemble as they step alone (bit for bit with solver 0)."""
+    from nhwave_gb300 import fields as F, lib
+    names = ["tiny_visc_fric", "tiny_open", "tiny_flume_con", "tiny_flume_foc"]
+    ens = [_member(n, precision) for n in names]
+    ref = [_member(n, precision) for n in names]
+    with lib.Ensemble(ens, solver=solver) as e:
+        for _ in range(3):
+            assert e.step(1) == 0
+            for r in ref:
+                assert r.step() == 0
+    lim = 1e-8 if precision == 0 else 1e-6
+    for n, a, b in zip(names, ens, ref):
+        assert a.scalars().run_step == b.scalars().run_step == 3
+        assert np.array_equal(a.get(F.MASK), b.get(F.MASK)), n
+        for f in ("ETA", "P", "U", "W"):
+            fid = getattr(F, f)
+            if solver == 0:
+                assert np.array_equal(a.get(fid), b.get(fid)), f"{n} {f} differs"
+            else:
+                sl = a.shape.interior(fid)
+                den = max(np.linalg.norm(b.get(fid)[sl]), 1e-30)
+                r = np.linalg.norm(a.get(fid)[sl] - b.get(fid)[sl]) / den
+                assert r < lim, f"{n} {f}: {r:.3e}"

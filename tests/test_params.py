@@ -118,3 +118,49 @@ def test_reference_example_inputs_where_present():
             assert reason is None, (f, reason)
             inside += 1
     assert inside >= 4
+
+
+def test_reader_takes_the_added_keys(tmp_path):
+    """The keys of the viscous, bed, wall and FOCUSED options reach nhw_params
+    (src/initialize.F:357, 385-392, 466-468, 614, 709-719)."""
+    from nhwave_gb300 import params as P
+    f = tmp_path / "input.txt"
+    extra = """
+IVTURB = 1
+IHTURB = 1
+VISCOSITY = 2.e-6
+Schmidt = 0.7
+Cvs = 0.003
+Chs = 0.02
+RNG = T
+VISCOUS_NUMBER = 0.2
+Ibot = 2
+Cd0 = 0.004
+Zob = 2.e-4
+"""
+    text = (SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 5").replace("BC_Y0 = 1", "BC_Y0 = 5")
+            .replace("VISCOUS_FLOW = F", "VISCOUS_FLOW = T") + extra)
+    f.write_text(text)
+    p = P.read_input(str(f))
+    assert p.viscous_flow == 1 and p.ivturb == 1 and p.ihturb == 1 and p.rng == 1
+    assert (p.visc, p.schmidt, p.cvs, p.chs, p.viscous_number) == (2e-6, 0.7, 0.003, 0.02, 0.2)
+    assert (p.bc_z0, p.bc_y0, p.ibot, p.cd0, p.zob) == (5, 5, 2, 0.004, 2e-4)
+    assert P.unsupported_reason(p) is None
+    f.write_text(text.replace("IVTURB = 1", "IVTURB = 10"))
+    assert "IVTURB" in P.unsupported_reason(P.read_input(str(f)))
+    foc = SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = FOCUSED") + """
+nwave = 12
+Component_Amp_Type = 1
+k_center = 4.0
+f_center = 1.1
+x_breaking = 6.0
+t_breaking = 9.0
+Slope_group = 0.3
+normalized_delta_f = 0.75
+depth_comp = 0.6
+"""
+    f.write_text(foc)
+    p = P.read_input(str(f))
+    assert p.wavemaker == P.WM_FOCUSED and p.nwave == 12 and p.component_amp_type == 1
+    assert (p.k_center, p.f_center, p.x_breaking, p.t_breaking) == (4.0, 1.1, 6.0, 9.0)
+    assert (p.slope_group, p.normalized_delta_f, p.depth_comp) == (0.3, 0.75, 0.6)
