@@ -70,11 +70,11 @@ enum nhw_precision {
 /* INT_*: internal source strip (src/source_terms.F); LEF_*, WAV_CUR and
  * FOCUSED: waves fed through the west boundary, which then needs BC_X0 = 3:
  * linear, solitary, second-order Stokes, cnoidal, linear on a current ramped
- * up over TRAMP, and a focused group of NWAVE linear components
- * (src/waves.F:92-170, 518-560, 638-756, 808-903) */
+ * up over TRAMP, a focused group of NWAVE linear components, and the S2 tide
+ * (src/waves.F:92-170, 518-560, 638-756, 808-903; src/nhwave.F:5715-5750) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
                      NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7,
-                     NHW_WM_FOCUSED = 8 };
+                     NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 

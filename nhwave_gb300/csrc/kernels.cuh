@@ -263,6 +263,16 @@ struct OpWaveBC {
         S.Win[j + Nl * k] = 0.5 * A * Sg * sinh(wk * Zlev) / sh * sn + S.lef_u2 * sinh(2. * wk * Zlev) / sh4 * sn2;
         S.Vin[j + Nl * k] = 0.0;
       }
+    } else if (S.lef == 9) {   // LEF_TID: the S2 tide, period 43200 s (src/nhwave.F:5715-5750)
+      const double E = 0.5 * S.lef_amp * cos(2.0 * kPi / 43200. * TIME - kPi / 2.0);
+      S.Ein[j] = E;
+      S.Din[j] = E + hfx;
+      if (!inner) return;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        S.Uin[j + Nl * k] = sqrt(kGrav / hfx) * E;
+        S.Vin[j + Nl * k] = 0.0;
+        S.Win[j + Nl * k] = 0.0;
+      }
     } else if (S.lef == 8) {   // FOCUSED: a group of NWAVE linear components (src/waves.F:638-692)
       const int nw = S.nwave;
       const double *Ai = S.foc, *ki = S.foc + nw, *fi = S.foc + 2 * nw;
@@ -792,7 +802,11 @@ struct OpWlBcEta {
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
     const int mi = mirror(i, S.IB, S.IE), mj = mirror(j, S.JB, S.JE);
-    if (i < S.IB && S.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157); corners copy their row's value
+    if (i <= S.IB && S.bc_x0 == 3 && S.lef == 9)
+      // tide (src/nhwave.F:5145-5148): D = Din in the ghosts and the first
+      // interior column; ghost rows copy their mirrored row's value
+      S.D[c] = S.Din[mj];
+    else if (i < S.IB && S.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157); corners copy their row's value
       S.D[c] = 2.0 * S.Din[mj] - S.D[i2(S, mi, mj)];
     else if (i > S.IE && S.bc_xn == 6) {
       // Orlanski radiation (src/nhwave.F:5197-5206) from the last two steps'

@@ -32,7 +32,7 @@ int check_params(const nhw_params& p) {
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;
-  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED;
+  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID;
   // west inflow (BC_X0 = 3) only with a wave fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
@@ -40,7 +40,7 @@ int check_params(const nhw_params& p) {
   const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
   if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_FOCUSED) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_TID) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;

@@ -657,7 +657,7 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED) ? p.wavemaker : 0;
+    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ? p.wavemaker : 0;
     if (S.lef == NHW_WM_FOCUSED)
       NHW_CU(cudaMemcpyAsync((void*)S.foc, h.foc.data(), sizeof(double) * h.foc.size(), cudaMemcpyHostToDevice, st));
     S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave; S.lef_per = p.per_wave;

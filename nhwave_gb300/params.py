@@ -13,9 +13,10 @@ import ctypes
 
 NHW_FP64 = 0
 NHW_FP32_IR = 1
-WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED = range(9)
+(WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED,
+ WM_LEF_TID) = range(10)
 # fed through the west boundary (BC_X0 = 3)
-WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED)
+WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
 SLIDE_NONE, SLIDE_RIGID_3D = 0, 1
 DEPTH_CELL_CENTER, DEPTH_CELL_GRID = 0, 1
@@ -197,7 +198,7 @@ def read_input(path: str) -> NhwParams:
     # as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
              "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR,
-             "FOCUSED": WM_FOCUSED}
+             "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
@@ -243,10 +244,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF:
-        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, WAV_CUR and "
-                "FOCUSED are on the GPU path)")
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR "
+                "and FOCUSED are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
-        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, WAV_CUR or FOCUSED wavemaker"
+        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR or FOCUSED wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
         ok = {"bc_x0": (1, 2, 3, 5), "bc_xn": (1, 2, 5, 6)}.get(name, (1, 2, 5))
         if getattr(p, name) not in ok:
@@ -266,7 +267,7 @@ def cells(p: NhwParams) -> int:
 __all__ = [
     "NhwParams", "NhwScalars", "default_params", "read_input", "unsupported_reason", "cells",
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
-    "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF",
+    "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF_TID", "WM_LEF",
     "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",

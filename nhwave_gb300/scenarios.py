@@ -152,13 +152,13 @@ def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5,
     (WAV_CUR, `cur_wave`, `tramp`) or a focused group (FOCUSED, `nwave` ...);
     sponge layer and wall at the east end,
     walls along the sides; at rest initially."""
-    from .params import WM_FOCUSED, WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_WAV_CUR
+    from .params import WM_FOCUSED, WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_TID, WM_WAV_CUR
     p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
                        dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
                        tol=1e-8, itmax=1000, total_time=20.0)
     p.bc_x0 = 3
     p.wavemaker = {"LIN": WM_LEF_LIN, "SOL": WM_LEF_SOL, "STK": WM_LEF_STK, "CON": WM_LEF_CON,
-                   "CUR": WM_WAV_CUR, "FOC": WM_FOCUSED}[kind]
+                   "CUR": WM_WAV_CUR, "FOC": WM_FOCUSED, "TID": WM_LEF_TID}[kind]
     p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
     p.sponge_on = 1
     p.sponge_east_width = sponge
@@ -222,6 +222,9 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         # the inviscid small bar with wall friction (BC = 5) on every side, drag coefficient 0.01
         kw = dict(dict(bc_x0=5, bc_xn=5, bc_y0=5, bc_yn=5, ibot=1, cd0=0.01), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_flume_tid":
+        # the S2 tide (LEF_TID) of 0.1 m amplitude from its zero crossing
+        out = wave_flume("TID", M=64, N=4, K=5, dx=0.1, dy=0.1, amp=0.1, sponge=1.5, **kw)
     elif name == "tiny_flume_foc":
         # a focused group of 8 components around 1 Hz (FOCUSED), focusing 3 m in at t = 4 s
         kw = dict(dict(nwave=8, component_amp_type=2, f_center=1.0, normalized_delta_f=0.6, x_breaking=3.0,

@@ -226,7 +226,7 @@ struct Model {
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_FOCUSED;
+    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
       if (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0)) return NHW_ERR_ARG;
@@ -770,6 +770,18 @@ struct Model {
                          3. / 16. * (A * A) * Segma * Wave_Number * std::sinh(2. * Wave_Number * Zlev) / sh4 *
                              std::sin(2. * (pi / 2 - Segma * TIME));
           Vin_X0(j, k) = 0.0;
+        }
+    } else if (p.wavemaker == NHW_WM_LEF_TID) {   // tidal_wave_left_boundary (src/nhwave.F:5715-5750)
+      const double period1 = 43200.;   // S2 (the first of the routine's eight periods)
+      for (int j = 1; j <= Nloc; ++j) {
+        Ein_X0(j) = 0.5 * p.amp_wave * std::cos(2.0 * pi / period1 * TIME - pi / 2.0);
+        Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+      }
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = Jbeg; j <= Jend; ++j) {
+          Uin_X0(j, k) = std::sqrt(Grav / Hfx(Ibeg, j)) * Ein_X0(j);
+          Vin_X0(j, k) = 0.0;
+          Win_X0(j, k) = 0.0;
         }
     } else if (p.wavemaker == NHW_WM_FOCUSED) {   // src/waves.F:638-692
       const int nw = p.nwave;
@@ -1322,7 +1334,9 @@ struct Model {
   // -------------------------------------------------------------- wl_bc
   void wl_bc() {
     for (int j = Jbeg; j <= Jend; ++j) {
-      if (p.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157)
+      if (p.bc_x0 == 3 && p.wavemaker == NHW_WM_LEF_TID)   // tide: D = Din from the first interior column out (src/nhwave.F:5145-5148)
+        for (int i = 0; i <= Nghost; ++i) D(Ibeg - i, j) = Din_X0(j);
+      else if (p.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157)
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = 2.0 * Din_X0(j) - D(Ibeg + i - 1, j);
       else
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);

@@ -480,3 +480,20 @@ def test_focused_group_boundary_elevation(oracle_mod):
         t = o.scalars().time
         expect = np.sum(a * np.cos(-k * p.x_breaking - 2 * pi * f * (t - p.t_breaking)))
         assert _west_boundary_eta(o) == pytest.approx(expect, abs=1e-8)
+
+
+def test_tide_sets_the_first_column_depth(oracle_mod):
+    """LEF_TID (src/nhwave.F:5715-5750 with wl_bc :5145-5148): the boundary
+    elevation is 0.5 A cos(2 pi t / 43200 - pi/2), and wl_bc sets D to
+    Din = Hfx + Ein in the ghosts and the first interior column alike."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_flume_tid")
+    p.tol, p.itmax = 1e-8, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    pi = float(np.float32(3.141592653))
+    for _ in range(10):
+        assert o.step() == 0
+    t = o.scalars().time
+    ein = 0.5 * p.amp_wave * math.cos(2.0 * pi / 43200.0 * t - pi / 2.0)
+    D = o.get(F.D)
+    assert np.allclose(D[2:-2, 0:3], p.dep_wave + ein, rtol=0, atol=1e-14)
