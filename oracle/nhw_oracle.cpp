@@ -10,7 +10,8 @@
 // restatement is therefore "parity unpinned" against the reference binary.  It
 // is pinned instead by known-answer tests (lake at rest, mass conservation,
 // mirror symmetry, linear dispersion, hand-computed limiter / HLL / Poisson
-// coefficients) in tests/test_oracle_*.py.
+// coefficients, boundary-wave formulas, elliptic functions against scipy,
+// viscous decay rates) in tests/test_oracle.py.
 //
 // Reference routines restated here (file:line in the reference project):
 //   generate_grid              src/initialize.F:1647-1729
@@ -23,8 +24,14 @@
 //   update_wind (Iws=1)        src/nhwave.F:5333-5400
 //   source_terms               src/source_terms.F:1-67, 418-455; wave_dispersion src/waves.F:61-91
 //   fluxes & co.               src/nhwave.F:1686-2351, 2354-2552, 2673-2776, 2813-2906
-//   eval_duvw (inviscid)       src/nhwave.F:539-1300
-//   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117
+//   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
+//   diffusion                  src/nhwave.F:6785-7141
+//   trig                       src/nhwave.F:13182-13224
+//   eval_turb (IVTURB=IHTURB=1) src/nhwave.F:6544-6686
+//   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
+//                              Orlanski east side, bed stress)
+//   update_wave_bc             src/nhwave.F:5514-5565, 5715-5750; src/waves.F:92-370,
+//                              518-560, 638-756, 808-903; components src/initialize.F:709-781
 //   interpolate_velocity_to_faces src/nhwave.F:1332-1368
 //   get_Omega                  src/nhwave.F:1411-1648
 //   wl_bc / phi_2D_coll        src/nhwave.F:5119-5330
@@ -33,7 +40,7 @@
 //   generate_coef_rhs          src/pressure.F:475-840
 //   sponge_damping             src/nhwave.F:6463-6502
 //   sigma_transform            src/nhwave.F:6505-6541
-//   statistics (MassVolume)    src/nhwave.F:3139-3148
+//   statistics                 src/nhwave.F:3118-3160
 //
 // Arithmetic: IEEE FP64 with the reference's evaluation order written out
 // (left-to-right products and quotients, explicit parentheses) and built with
