@@ -18,6 +18,8 @@ const double kPiH = (double)3.141592653f;
 const double kGravH = (double)9.81f;
 inline double dmx(double a, double b) { return a > b ? a : b; }
 inline double dmn(double a, double b) { return a < b ? a : b; }
+bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m);
+bool cnoidal_start(double Ytrough, double A, double m, double& Xstart);
 }  // namespace
 
 int check_params(const nhw_params& p) {
@@ -52,7 +54,12 @@ int check_params(const nhw_params& p) {
       (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0) ||
        (p.component_amp_type == 1 && !(p.k_center > 0))))
     return NHW_ERR_ARG;
-  if (p.wavemaker == NHW_WM_LEF_CON && !(p.amp_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker == NHW_WM_LEF_CON) {   // the cnoidal parameter and start phase must exist
+    double L = 0, Yt = 0, m = 0, Xstart = 0;
+    if (!(p.amp_wave > 0) || !cnoidal_params(p.amp_wave, p.dep_wave, p.per_wave, L, Yt, m) ||
+        !cnoidal_start(Yt, p.amp_wave, m, Xstart))
+      return NHW_ERR_ARG;
+  }
   return NHW_OK;
 }
 

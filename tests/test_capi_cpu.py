@@ -81,3 +81,23 @@ def test_null_arguments(gpu_lib):
     assert gpu_lib.nhw_create(None, None) == lib.ERR_ARG
     assert gpu_lib.nhw_step(None, None, None, None) == lib.ERR_ARG
     assert gpu_lib.nhw_destroy(None) == lib.ERR_ARG
+
+
+@pytest.mark.parametrize("fields,status", [
+    (dict(bc_x0=3, wavemaker=8, nwave=1, f_center=1.0, depth_comp=0.5), "ERR_ARG"),      # FOCUSED, one component
+    (dict(bc_x0=3, wavemaker=8, nwave=4, f_center=0.0, depth_comp=0.5), "ERR_ARG"),      # no centre frequency
+    (dict(bc_x0=3, wavemaker=6, amp_wave=0.0), "ERR_ARG"),                                # cnoidal of zero height
+    (dict(bc_x0=3, wavemaker=6, amp_wave=0.02, per_wave=1.5, dep_wave=0.5), "ERR_ARG"),  # cnoidal in deep water
+    (dict(bc_y0=5, ibot=3), "ERR_UNSUPPORTED"),                                           # unknown Ibot
+    (dict(bc_z0=5, ibot=2, zob=0.0), "ERR_ARG"),                                          # roughness height 0
+    (dict(bc_x0=3, wavemaker=1), "ERR_UNSUPPORTED"),                                      # inflow without a LEF_ maker
+    (dict(bc_xn=3), "ERR_UNSUPPORTED"),                                                   # east inflow
+])
+def test_added_options_checked_on_host(fields, status, gpu_lib):
+    """The boundary-wave, wall/bed and FOCUSED options are checked on the host
+    before any device work: impossible values are NHW_ERR_ARG (the reference
+    would stop or run with NaN), options outside the path NHW_ERR_UNSUPPORTED."""
+    from nhwave_gb300 import default_params, lib
+    p = default_params(**fields)
+    h = ctypes.c_void_p()
+    assert gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h)) == getattr(lib, status) and not h.value
