@@ -101,3 +101,28 @@ def test_added_options_checked_on_host(fields, status, gpu_lib):
     p = default_params(**fields)
     h = ctypes.c_void_p()
     assert gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h)) == getattr(lib, status) and not h.value
+
+
+def test_reference_example_inputs_pass_the_host_checks(gpu_lib):
+    """Every example input of the reference that the Python reader places
+    inside the path also passes nhw_create's host checks: on a machine
+    without a GPU the call gets as far as the device and fails there
+    (NHW_ERR_CUDA), never with NHW_ERR_UNSUPPORTED or NHW_ERR_ARG.  The
+    others are rejected as unsupported.  Reads the reference checkout when
+    one is mounted."""
+    import glob
+    from nhwave_gb300 import lib, params as P
+    root = os.environ.get("NHWAVE_REFERENCE", "/root/reference")
+    files = sorted(glob.glob(os.path.join(root, "**", "input*.txt"), recursive=True))
+    if not files:
+        pytest.skip("no reference checkout")
+    for f in files:
+        p = P.read_input(f)
+        h = ctypes.c_void_p()
+        st = gpu_lib.nhw_create(ctypes.byref(p), ctypes.byref(h))
+        if P.unsupported_reason(p) is None:
+            assert st not in (lib.ERR_UNSUPPORTED, lib.ERR_ARG), (f, st)
+            if st == 0:
+                gpu_lib.nhw_destroy(h)
+        else:
+            assert st == lib.ERR_UNSUPPORTED, (f, st)
