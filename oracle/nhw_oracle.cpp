@@ -5,10 +5,10 @@
 // checked against its source lines.  Only tests/, __graft_entry__.smoke() and
 // bench.py's CPU-baseline leg load it, and only as the checker / CPU baseline.
 //
-// Parity status: the reference is Fortran and no Fortran compiler exists in
-// this build environment, and the reference ships no golden outputs; this
-// restatement is therefore "parity unpinned" against the reference binary.  It
-// is pinned instead by known-answer tests (lake at rest, mass conservation,
+// Parity status: the reference is Fortran, no Fortran compiler is installed
+// where this file is compiled and run, and the reference ships no golden
+// outputs; this restatement is therefore "parity unpinned" against the
+// reference binary.  It is pinned instead by known-answer tests (lake at rest, mass conservation,
 // mirror symmetry, linear dispersion, hand-computed limiter / HLL / Poisson
 // coefficients, boundary-wave formulas, elliptic functions against scipy,
 // viscous decay rates) in tests/test_oracle.py.
