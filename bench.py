@@ -361,7 +361,8 @@ def run_gpu_arm(args):
     sc = g.scalars()
     iters_per_solve = sc.total_krylov_iters / max(1, sc.poisson_solves)
     t_max, value = replica_throughput(ms, cells, args.steps, world, device="cuda")
-    eta32 = g.get(F.ETA)[g.shape.interior(F.ETA)]
+    ERR_FIELDS = {"eta": F.ETA, "u": F.U, "v": F.V, "w": F.W, "p": F.P}
+    end32 = {k: g.get(f)[g.shape.interior(f)].astype(np.float64) for k, f in ERR_FIELDS.items()}
     # ---- profile pass: per-kernel CUDA events over the same number of steps
     g.profile(True)
     g.run_timed(max(1, min(args.steps, 5)))
@@ -383,11 +384,17 @@ def run_gpu_arm(args):
     g64 = lib.Scenario(p64, d, e, u)
     g64.run_timed(args.warmup)
     ms64 = g64.run_timed(args.steps)
-    eta64 = g64.get(F.ETA)[g64.shape.interior(F.ETA)]
+    end64 = {k: g64.get(f)[g64.shape.interior(f)] for k, f in ERR_FIELDS.items()}
     iters64 = g64.scalars().total_krylov_iters / max(1, g64.scalars().poisson_solves)
     g64.close()
     value64 = cells * args.steps / (ms64 / 1000.0)
-    eta_err = float(np.linalg.norm(eta32 - eta64) / np.linalg.norm(eta64))
+    # FP32+IR against FP64 after the same warm-up + timed steps: relative L2 of
+    # eta and P; u, v, w relative to the whole FP64 velocity field
+    vnorm = math.sqrt(sum(float(np.linalg.norm(end64[c])) ** 2 for c in ("u", "v", "w")))
+    fp32_err = {k: float(np.linalg.norm(end32[k] - end64[k]) /
+                         (vnorm if k in ("u", "v", "w") else np.linalg.norm(end64[k])))
+                for k in ERR_FIELDS}
+    eta_err = fp32_err["eta"]
 
     # ---- e2e through the C-ABI with host buffers
     p, d, e, u = make(NHW_FP32_IR)
@@ -431,6 +438,7 @@ def run_gpu_arm(args):
                      "krylov_iters_per_solve": round(iters64, 1)},
             "fp32ir_over_fp64": value / world / value64,
             "eta_rel_l2_vs_fp64": eta_err,
+            "fp32ir_rel_l2_vs_fp64": {"steps": args.warmup + args.steps, **fp32_err},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                     "d2h_bytes_per_step": int(d2h_step + d2h_end / args.steps),
                     "note": "state uploaded once from pinned host memory, eta read back every step"},

@@ -371,7 +371,10 @@ int nhw_ensemble_destroy(nhw_ensemble* e);
  * `stream` (a cudaStream_t; NULL = the default stream).  It returns once the
  * work is queued.  U, V, W are (Mglob+4, Nglob+4, Kglob+4), D is
  * (Mglob+4, Nglob+4) and dsig (Kglob+4), all FP64 in the reference's ghosted
- * Fortran layout (column-major, two ghost cells a side).  The caller checks
+ * Fortran layout (column-major, two ghost cells a side).  Every array must be
+ * device memory of the current device, or managed memory; host memory and
+ * another GPU's memory are refused with NHW_ERR_ARG.  A NaN candidate is
+ * skipped, as the reference's `if (x < tmp2) tmp2 = x` skips it.  The caller checks
  * dt against DT_MIN.  A viscous run (VISCOUS_FLOW) also takes the minimum
  * with VISCOUS_NUMBER * min(dx^2, dy^2) / (|CmuHt| + 1e-16), which this call
  * leaves to the caller (src/nhwave.F:3812-3832).

@@ -1729,14 +1729,20 @@ __global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
     const int j = S.JB + (int)(r % S.N), k = S.KB + (int)(r / S.N);
     const long long q = i2(S, i, j), o = i3(S, i, j, k);
     const double Dq = S.D[q];
+    // each candidate replaces m only if it is smaller, as the reference's
+    // `if(dxonu<tmp2) tmp2=dxonu` (src/nhwave.F:3730-3746): a NaN candidate
+    // leaves m unchanged
     double tmp1 = fabs((double)S.U[o]) + sqrt(kGrav * Dq);
     tmp1 = dmax_(tmp1, kSmall);
-    m = dmin_(m, S.dx / tmp1);
+    double x = S.dx / tmp1;
+    if (x < m) m = x;
     tmp1 = fabs((double)S.V[o]) + sqrt(kGrav * Dq);
     tmp1 = dmax_(tmp1, kSmall);
-    m = dmin_(m, S.dy / tmp1);
+    x = S.dy / tmp1;
+    if (x < m) m = x;
     tmp1 = dmax_(fabs((double)S.W[o]), kSmall);
-    m = dmin_(m, S.dsig[k] * Dq / tmp1);
+    x = S.dsig[k] * Dq / tmp1;
+    if (x < m) m = x;
   }
   for (int o = 16; o > 0; o >>= 1) m = dmin_(m, __shfl_down_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));

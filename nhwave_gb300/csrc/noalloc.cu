@@ -39,7 +39,10 @@ constexpr int kNaCounter = kNaMaxBlocks;                                        
 // cudaGetSymbolAddress (scratch_on_current_device).
 static __device__ __align__(256) double g_dt_scratch[kNaMaxBlocks + 32];
 
-__device__ __forceinline__ double na_min(double a, double b) { return a < b ? a : b; }
+// Running minimum m updated by a candidate x the way the reference does
+// (src/nhwave.F:3730-3746, `if(dxonu<tmp2) tmp2=dxonu`): a NaN candidate fails
+// the comparison and leaves m as it was.
+__device__ __forceinline__ double na_min(double m, double x) { return x < m ? x : m; }
 __device__ __forceinline__ double na_max(double a, double b) { return a > b ? a : b; }
 
 __device__ __forceinline__ double block_min(double m) {
@@ -133,13 +136,16 @@ int scratch_on_current_device(double** out) {
   return NHW_OK;
 }
 
-bool on_device(const void* p) {
+// Device memory of the current device, or managed memory.  Device memory of
+// another GPU is refused: without peer access the kernel's loads would fault.
+bool on_device(const void* p, int dev) {
   cudaPointerAttributes a{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -165,10 +171,17 @@ extern "C" int nhw_estimate_dt_noalloc(const double* U, const double* V, const d
                    " that its static device scratch holds");
     return NHW_ERR_ARG;
   }
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    set_last_error("nhw_estimate_dt_noalloc: no current CUDA device");
+    return NHW_ERR_CUDA;
+  }
   for (const void* p : {(const void*)U, (const void*)V, (const void*)W, (const void*)D, (const void*)dsig,
                         (const void*)dt_out})
-    if (!on_device(p)) {
-      set_last_error("nhw_estimate_dt_noalloc: every array must be device (or managed) memory");
+    if (!on_device(p, dev)) {
+      set_last_error("nhw_estimate_dt_noalloc: every array must be device memory of the current device "
+                     "(device " + std::to_string(dev) + ") or managed memory");
       return NHW_ERR_ARG;
     }
   double* scratch = nullptr;

@@ -204,3 +204,49 @@ class Oracle:
 
 def limiter(a: float, b: float) -> float:
     return lib().orc_limiter(a, b)
+
+
+BATHY_FIELDS = ("HC", "HFX", "HFY", "HFX0", "HFY0", "DELXH", "DELYH", "DELTH", "DELT2H")
+
+
+def run_scenario(name: str, steps: int, tol: float = 1e-13, pinned: bool = False, seed: int = 7,
+                 fields=("ETA", "D", "U", "V", "W", "P", "MASK"), **kw) -> dict:
+    """Run the seeded scenario ``name`` (``nhwave_gb300.scenarios.make``) for
+    ``steps`` FP64 steps and return plain arrays, so that a process pool can
+    run it beside the GPU: the end ``fields`` (whole ghosted arrays), the
+    mask after every step, the scalars, and -- with ``pinned`` -- each step's
+    bathymetry right after update_bathymetry (the step is then taken routine
+    by routine in the main loop's order, src/nhwave.F:127-258), for a GPU run
+    that copies it in."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make(name, seed=seed, **kw)
+    p.tol, p.itmax, p.precision = tol, 20000, 0
+    o = Oracle(p, d, e, u)
+    masks, bathy = [], []
+    for _ in range(steps):
+        if pinned:
+            rc = o.estimate_dt()
+            if rc:
+                raise RuntimeError(f"oracle estimate_dt: {rc}")
+            o.update_bathymetry()
+            bathy.append({n: o.get(getattr(F, n)).copy() for n in BATHY_FIELDS})
+            o.update_mask()
+            o.update_vars()
+            for s in (1, 2, 3):
+                o.source_terms()
+                o.fluxes()
+                rc = o.eval_duvw(s)
+                if rc:
+                    raise RuntimeError(f"oracle eval_duvw: {rc}")
+                if o.params.sponge_on:
+                    o.sponge_damping()
+        else:
+            rc = o.step()
+            if rc:
+                raise RuntimeError(f"oracle step: {rc}")
+        masks.append(o.get(F.MASK).copy())
+    sc = o.scalars()
+    out = {"fields": {f: o.get(getattr(F, f)).copy() for f in fields}, "masks": masks, "bathy": bathy,
+           "time": sc.time, "dt": sc.dt, "run_step": sc.run_step}
+    o.close()
+    return out

@@ -184,6 +184,14 @@ def test_slide_free_running(oracle_mod, gpu_lib):
     g.close()
 
 
+# FP32+IR against the FP64 oracle after 6 steps of the small cases, per field:
+# eta relative L2, P relative L2, U/V/W relative to the whole velocity field.
+# Largest values measured on a GB300 over these cases: eta 1.5e-8, P 4.1e-6
+# (tiny_open), U 1.5e-6 and V 1.5e-6 (tiny_c4), W 2.0e-7; the bounds leave a
+# factor of about 5, and eta is held to the 1e-6 the FP32+IR form is built for.
+FP32IR_BOUNDS = {"ETA": 1e-6, "P": 2e-5, "U": 1e-5, "V": 1e-5, "W": 2e-6}
+
+
 @pytest.mark.parametrize("name", MORE_CASES)
 def test_steps_fp32_ir(name, oracle_mod, gpu_lib):
     from nhwave_gb300 import fields as F
@@ -194,8 +202,12 @@ def test_steps_fp32_ir(name, oracle_mod, gpu_lib):
         assert o.step() == 0
     sl = o.shape.interior
     assert np.array_equal(g.get(F.MASK), o.get(F.MASK))
-    r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
-    assert r < 1e-6, f"{name} eta rel L2 {r:.3e} (|eta| {np.abs(eta0).max():.3e})"
+    err = {f: rel_l2(g.get(getattr(F, f))[sl(getattr(F, f))], o.get(getattr(F, f))[sl(getattr(F, f))])
+           for f in ("ETA", "P")}
+    err.update({f: vel_err(g, o, f) for f in ("U", "V", "W")})
+    print(f"\n{name} FP32+IR vs FP64 oracle, 6 steps: " + ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
+    for f, r in err.items():
+        assert r < FP32IR_BOUNDS[f], f"{name} {f} rel L2 {r:.3e} (|eta0| {np.abs(eta0).max():.3e})"
     assert g.scalars().last_rel_residual <= 1e-10
     g.close()
 

@@ -25,13 +25,13 @@ def _dsig(K):
     return np.full(K + 4, np.float64(np.float32(1.0) / np.float32(K)))
 
 
-def _noalloc_dt(L, torch, g, dt_old, out):
+def _noalloc_dt(L, torch, g, dt_old, out, device="cuda"):
     """Upload U, V, W, D and dsig as the caller's device arrays; one call."""
     from nhwave_gb300 import fields as F
     p = g.params
-    arrs = [torch.from_numpy(np.ascontiguousarray(g.get(getattr(F, n)), dtype=np.float64)).to("cuda")
+    arrs = [torch.from_numpy(np.ascontiguousarray(g.get(getattr(F, n)), dtype=np.float64)).to(device)
             for n in ("U", "V", "W", "D")]
-    arrs.append(torch.from_numpy(_dsig(p.Kglob)).to("cuda"))
+    arrs.append(torch.from_numpy(_dsig(p.Kglob)).to(device))
     torch.cuda.synchronize()
     st = L.nhw_estimate_dt_noalloc(*[a.data_ptr() for a in arrs], p.Mglob, p.Nglob, p.Kglob,
                                    p.dx, p.dy, p.cfl, dt_old, p.dt_max, out.data_ptr(), None)
@@ -81,3 +81,45 @@ def test_noalloc_rejects_oversize_and_host_arrays(gpu_lib):
     st = L.nhw_estimate_dt_noalloc(None, ptr, ptr, ptr, ptr, 4, 4, 2, 1.0, 1.0, 0.5, 1.0, 1.0,
                                    out.data_ptr(), None)
     assert st == lib.ERR_ARG
+
+
+def test_noalloc_skips_nan_like_estimate_dt(gpu_lib):
+    """A NaN depth in one cell gives NaN candidates there; both entry points
+    skip them, as the reference's `if (dzonw < tmp2) tmp2 = dzonw` does, and
+    return the same dt from the other cells."""
+    torch = pytest.importorskip("torch")
+    from nhwave_gb300 import fields as F, lib, scenarios as S
+    p, d, e, u = S.make("tiny_c1", precision=0, seed=5)
+    g = lib.Scenario(p, d, e, u)
+    L = lib.load()
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    assert g.step() == lib.OK
+    for cell in [(3, 7), (4, 20)]:          # interior (j, i) of the ghosted 2-D array
+        dt_old = g.scalars().dt
+        D = g.get(F.D).copy()
+        D[cell] = np.nan
+        g.set(F.D, D)
+        st, got = _noalloc_dt(L, torch, g, dt_old, out)
+        assert st == lib.OK, lib.last_error()
+        assert np.isfinite(got)
+        assert g.estimate_dt() == lib.OK     # takes dt_old from the handle's dt
+        assert got == g.scalars().dt
+    g.close()
+
+
+def test_noalloc_rejects_another_devices_arrays(gpu_lib):
+    """Arrays on a GPU other than the current one are refused (their loads
+    would fault without peer access); needs two visible GPUs."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("one GPU visible")
+    from nhwave_gb300 import lib
+    L = lib.load()
+    other = torch.zeros(1024, dtype=torch.float64, device="cuda:1")
+    ptr = torch.zeros(1024, dtype=torch.float64, device="cuda:0").data_ptr()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    torch.cuda.set_device(0)
+    st = L.nhw_estimate_dt_noalloc(other.data_ptr(), ptr, ptr, ptr, ptr, 4, 4, 2, 1.0, 1.0, 0.5, 1.0, 1.0,
+                                   out.data_ptr(), None)
+    assert st == lib.ERR_ARG
+    assert "current device" in lib.last_error()
