@@ -19,6 +19,9 @@ sponge).  The metric is cell-updates/s = M*N*K*steps / device time.
   ensemble  config 4: 256 scenarios of uneven size (the C4 generator) advanced
           together, one CUDA graph launch per ensemble step; device-timed
           over a few steps (the full 500-step run is out of a bench's reach)
+  c3_landslide  config 3: the rigid landslide on the wet/dry beach at
+          512 x 512 x 10, FP32+IR and FP64 device-timed over the same steps,
+          the wet/dry masks compared and the fields' errors
   serving   config 5: Poisson arrivals at 50 requests/s replayed in real time
           through the continuous-batching loop under a 150 GB HBM budget;
           p50/p99 time-to-solution and cell-updates/s, FP32+IR and FP64; each
@@ -28,6 +31,8 @@ sponge).  The metric is cell-updates/s = M*N*K*steps / device time.
 ``--impl reference`` times the CPU restatement of the reference (the oracle;
 the Fortran reference cannot be compiled on this machine) on the host cores.
 Multi-GPU (``--gpus N`` under torchrun): independent replicas, one per GPU.
+``--horizon c2|c3`` runs FP32+IR against FP64 over a whole simulated run
+instead (masks after every step, the five fields' errors along the run).
 """
 from __future__ import annotations
 
@@ -325,6 +330,106 @@ def run_serving(local):
     return out
 
 
+# ------------------------------------------------------------- C3 leg
+def _end_state(g, F):
+    import numpy as np
+    return {"mask": g.get(F.MASK).copy(),
+            **{k: g.get(f)[g.shape.interior(f)].astype(np.float64) for k, f in
+               (("eta", F.ETA), ("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P))}}
+
+
+def _field_errors(a, b):
+    """FP32+IR end state `a` against FP64 `b`: relative L2 of eta and p; u, v,
+    w relative to the whole FP64 velocity field."""
+    import numpy as np
+    vnorm = math.sqrt(sum(float(np.linalg.norm(b[c])) ** 2 for c in ("u", "v", "w")))
+    return {k: float(np.linalg.norm(a[k] - b[k]) / (vnorm if k in ("u", "v", "w") else np.linalg.norm(b[k])))
+            for k in ("eta", "u", "v", "w", "p")}
+
+
+def run_c3(local, steps=10, warmup=3):
+    """Config 3: the rigid landslide on the wet/dry plane beach, 512 x 512 x 10,
+    TOL 1e-8; FP32+IR and FP64 from the same state over the same steps, each
+    device-timed, then the wet/dry masks compared and the fields' errors."""
+    import numpy as np
+    from nhwave_gb300 import fields as F, lib, scenarios as S
+    from nhwave_gb300.params import NHW_FP32_IR, NHW_FP64
+    out, ends = {"workload": "rigid landslide, plane beach 1:15, 512x512x10, dx=dy=2 m, TOL=1e-8",
+                 "steps": steps, "warmup": warmup}, {}
+    for name, prec in (("fp32ir", NHW_FP32_IR), ("fp64", NHW_FP64)):
+        p, d, e, u = S.make("c3", precision=prec)
+        p.device = local
+        cells = p.Mglob * p.Nglob * p.Kglob
+        g = lib.Scenario(p, d, e, u)
+        g.run_timed(warmup)
+        ms = g.run_timed(steps)
+        sc = g.scalars()
+        ends[name] = _end_state(g, F)
+        out[name] = {"value": cells * steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / steps,
+                     "krylov_iters_per_solve": round(sc.total_krylov_iters / max(1, sc.poisson_solves), 1),
+                     "sim_time_s": sc.time}
+        if prec == NHW_FP32_IR:
+            g.profile(True)
+            g.run_timed(3)
+            out[name]["roofline"] = roofline(g.profile_report(), cells, 4)
+            g.profile(False)
+        g.close()
+    a, b = ends["fp32ir"], ends["fp64"]
+    sl = (slice(2, -2), slice(2, -2))
+    out["mask_equal"] = bool(np.array_equal(a["mask"], b["mask"]))
+    out["dry_cells"] = int((b["mask"][sl] == 0).sum())
+    out["fp32ir_rel_l2_vs_fp64"] = _field_errors(a, b)
+    out["fp32ir_over_fp64"] = out["fp32ir"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def run_horizon(args):
+    """FP32+IR against FP64 over a whole simulated run (``--horizon c2``: the
+    submerged bar's 20 s; ``c3``: the landslide's 200 s), both on the GPU
+    from the same state: the wet/dry masks compared after every step, and the
+    five fields' errors every ``--sample-every`` steps.  One JSON line."""
+    import numpy as np
+    from nhwave_gb300 import build as B, fields as F, lib, scenarios as S
+    from nhwave_gb300.params import NHW_FP32_IR, NHW_FP64
+    B.build()
+    gs = {}
+    for name, prec in (("fp32ir", NHW_FP32_IR), ("fp64", NHW_FP64)):
+        p, d, e, u = S.make(args.horizon, precision=prec)
+        gs[name] = lib.Scenario(p, d, e, u)
+    total = gs["fp64"].params.total_time
+    if args.max_steps:
+        total = 1e30
+    g32, g64 = gs["fp32ir"], gs["fp64"]
+    m0 = g64.get(F.MASK).copy()
+    ever_changed = np.zeros(m0.shape, dtype=bool)
+    mask_diff_steps, first_diff, samples, n = 0, None, [], 0
+    t0 = time.perf_counter()
+    while True:
+        assert g64.step() == 0 and g32.step() == 0
+        n += 1
+        m64, m32 = g64.get(F.MASK), g32.get(F.MASK)
+        ever_changed |= m64 != m0
+        if not np.array_equal(m64, m32):
+            mask_diff_steps += 1
+            if first_diff is None:
+                first_diff = {"step": n, "cells": int((m64 != m32).sum())}
+        t64 = g64.scalars().time
+        done = t64 >= total or (args.max_steps and n >= args.max_steps)
+        if n % args.sample_every == 0 or done:
+            err = _field_errors(_end_state(g32, F), _end_state(g64, F))
+            samples.append({"step": n, "time_s": round(t64, 4), "time_fp32ir_s": round(g32.scalars().time, 4),
+                            "cells_changed_wet_dry": int(ever_changed.sum()),
+                            **{k: float(f"{v:.3e}") for k, v in err.items()}})
+        if done:
+            break
+    line = {"horizon": args.horizon, "steps": n, "sim_time_s": t64, "wall_s": round(time.perf_counter() - t0, 1),
+            "mask_equal_every_step": mask_diff_steps == 0, "mask_differing_steps": mask_diff_steps,
+            "first_mask_difference": first_diff, "cells_changed_wet_dry": int(ever_changed.sum()),
+            "samples": samples}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 # --------------------------------------------------------------- GPU arm
 def run_gpu_arm(args):
     rank, world, local = dist_env()
@@ -420,6 +525,7 @@ def run_gpu_arm(args):
     g.close()
     e2e_val = cells * args.steps * world / e2e_s
 
+    c3 = run_c3(local) if not args.no_c3 else None
     ens = run_ensemble(local) if not args.no_ensemble else None
     srv = run_serving(local) if not args.no_serving else None
 
@@ -446,6 +552,8 @@ def run_gpu_arm(args):
             "roofline": rl,
             "clocks": clocks,
         }
+        if c3:
+            line["c3_landslide"] = c3
         if ens:
             line["ensemble"] = ens
         if srv:
@@ -474,11 +582,18 @@ def main():
                          "persistent launch per solve, 2 GMRES phase by phase")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the config-4 ensemble leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the config-5 serving leg")
+    ap.add_argument("--no-c3", action="store_true", help="skip the config-3 landslide leg")
+    ap.add_argument("--horizon", choices=["c2", "c3"],
+                    help="instead of the bench line: FP32+IR against FP64 over the whole simulated run")
+    ap.add_argument("--sample-every", type=int, default=200)
+    ap.add_argument("--max-steps", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.horizon:
+        return run_horizon(args)
     return run_gpu_arm(args)
 
 
