@@ -267,10 +267,10 @@ def replica_throughput(ms_local: float, cells: int, steps: int, world: int, devi
 
 # --------------------------------------------------------- C4 and C5 legs
 ENSEMBLE_MEMBERS = 256
-SERVE_RATE, SERVE_WINDOW_S, SERVE_STEPS, SERVE_BUDGET = 50.0, 2.0, 8, 150 << 30
+SERVE_RATE, SERVE_WINDOW_S, SERVE_STEPS, SERVE_BUDGET = 50.0, 1.0, 100, 150 << 30
 
 
-def run_ensemble(local, steps=3, warmup=2):
+def run_ensemble(local, steps=10, warmup=3):
     """Config 4: 256 seeded members, FP32+IR, one ensemble graph per step."""
     from nhwave_gb300 import lib, scenarios as S
     from nhwave_gb300.params import NHW_FP32_IR
@@ -315,16 +315,18 @@ def run_serving(local):
         arr.append((t, p, d, e, u))
     out = {"rate_per_s": SERVE_RATE, "window_s": SERVE_WINDOW_S, "requests": len(arr),
            "steps_per_request": SERVE_STEPS, "hbm_budget_bytes": SERVE_BUDGET,
-           "note": "each request runs SERVE_STEPS steps (not 60 s of simulated time) so that the run stays bounded"}
+           "note": f"each request runs {SERVE_STEPS} steps (not 60 s of simulated time, about 1200 steps of a "
+                   f"C4 scenario) so that the run stays bounded"}
     eta = {}
     for name, prec in (("fp32ir", NHW_FP32_IR), ("fp64", NHW_FP64)):
-        srv = serve.Server(SERVE_BUDGET, precision=prec, steps_per_round=4)
+        srv = serve.Server(SERVE_BUDGET, precision=prec, steps_per_round=10)
         st = srv.serve(arr)
         first = min(srv.finished, key=lambda r: r.id)
         eta[name] = first.result["ETA"]
         srv.close()
         out[name] = {k: st[k] for k in ("p50_s", "p99_s", "cell_updates_per_s", "wall_s", "rounds",
-                                        "ensemble_rebuilds") if k in st}
+                                        "ensemble_rebuilds", "capture_s", "capture_share", "admit_s",
+                                        "retire_s", "busy_s") if k in st}
     a, b = eta["fp32ir"], eta["fp64"]
     out["eta_rel_l2_fp32ir_vs_fp64_first_request"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
     return out
@@ -387,14 +389,22 @@ def run_horizon(args):
     """FP32+IR against FP64 over a whole simulated run (``--horizon c2``: the
     submerged bar's 20 s; ``c3``: the landslide's 200 s), both on the GPU
     from the same state: the wet/dry masks compared after every step, and the
-    five fields' errors every ``--sample-every`` steps.  One JSON line."""
+    five fields' errors every ``--sample-every`` steps (also printed to stderr
+    as they come).  ``--horizon-pair gmres64`` compares two FP64 runs instead,
+    GMRES against BiCGSTAB: the spread that the Poisson stopping tolerance
+    alone leaves between two solvers.  ``--horizon-tol`` overrides TOL.  One
+    JSON line."""
     import numpy as np
     from nhwave_gb300 import build as B, fields as F, lib, scenarios as S
     from nhwave_gb300.params import NHW_FP32_IR, NHW_FP64
     B.build()
     gs = {}
-    for name, prec in (("fp32ir", NHW_FP32_IR), ("fp64", NHW_FP64)):
+    first = (NHW_FP64, 2) if args.horizon_pair == "gmres64" else (NHW_FP32_IR, 0)
+    for name, (prec, kk) in (("fp32ir", first), ("fp64", (NHW_FP64, 0))):
         p, d, e, u = S.make(args.horizon, precision=prec)
+        p.krylov_kernel = kk
+        if args.horizon_tol:
+            p.tol = args.horizon_tol
         gs[name] = lib.Scenario(p, d, e, u)
     total = gs["fp64"].params.total_time
     if args.max_steps:
@@ -418,11 +428,13 @@ def run_horizon(args):
         if n % args.sample_every == 0 or done:
             err = _field_errors(_end_state(g32, F), _end_state(g64, F))
             samples.append({"step": n, "time_s": round(t64, 4), "time_fp32ir_s": round(g32.scalars().time, 4),
-                            "cells_changed_wet_dry": int(ever_changed.sum()),
+                            "cells_changed_wet_dry": int(ever_changed.sum()), "mask_differing_steps": mask_diff_steps,
+                            "wall_s": round(time.perf_counter() - t0, 1),
                             **{k: float(f"{v:.3e}") for k, v in err.items()}})
+            print("# " + json.dumps(samples[-1]), file=sys.stderr, flush=True)
         if done:
             break
-    line = {"horizon": args.horizon, "steps": n, "sim_time_s": t64, "wall_s": round(time.perf_counter() - t0, 1),
+    line = {"horizon": args.horizon, "pair": args.horizon_pair, "tol": g64.params.tol, "steps": n, "sim_time_s": t64, "wall_s": round(time.perf_counter() - t0, 1),
             "mask_equal_every_step": mask_diff_steps == 0, "mask_differing_steps": mask_diff_steps,
             "first_mask_difference": first_diff, "cells_changed_wet_dry": int(ever_changed.sum()),
             "samples": samples}
@@ -586,6 +598,9 @@ def main():
     ap.add_argument("--horizon", choices=["c2", "c3"],
                     help="instead of the bench line: FP32+IR against FP64 over the whole simulated run")
     ap.add_argument("--sample-every", type=int, default=200)
+    ap.add_argument("--horizon-pair", choices=["fp32ir", "gmres64"], default="fp32ir",
+                    help="FP32+IR against FP64 (default), or FP64 GMRES against FP64 BiCGSTAB")
+    ap.add_argument("--horizon-tol", type=float, default=0.0, help="Poisson TOL of both runs (0: the config's)")
     ap.add_argument("--max-steps", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
