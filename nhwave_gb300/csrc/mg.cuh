@@ -284,13 +284,17 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
   }
   __syncthreads();
   if (ty != 0 || !valid) return;
+  // the Thomas sweeps, unrolled so that the shared-memory loads of several
+  // levels issue ahead of the dependent chain
   T prev = (T)0;
+#pragma unroll 4
   for (int k = 0; k < K; ++k) {
     prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
     s_rhs[k * 32 + tx] = prev;
   }
   T z = prev;
   L.x[col + MN * (K - 1)] = z;
+#pragma unroll 4
   for (int k = K - 2; k >= 0; --k) {
     z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
     L.x[col + MN * k] = z;
@@ -344,13 +348,17 @@ __global__ void __launch_bounds__(1024, 2) k_mg_smooth_split(MGL<T> L, const Dev
   }
   __syncthreads();
   if (ty != 0 || !valid) return;
+  // the Thomas sweeps, unrolled so that the shared-memory loads of several
+  // levels issue ahead of the dependent chain
   T prev = (T)0;
+#pragma unroll 4
   for (int k = 0; k < K; ++k) {
     prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
     s_rhs[k * 32 + tx] = prev;
   }
   T z = prev;
   L.x[col + MN * (K - 1)] = z;
+#pragma unroll 4
   for (int k = K - 2; k >= 0; --k) {
     z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
     L.x[col + MN * k] = z;
@@ -418,12 +426,14 @@ __device__ void cta_half_sweep(const MGL<T>& L, int color, int zero_x, const Pro
     __syncthreads();
     if (ty == 0 && valid) {
       T prev = (T)0;
+#pragma unroll 4
       for (int k = 0; k < K; ++k) {
         prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
         s_rhs[k * 32 + tx] = prev;
       }
       T z = prev;
       L.x[col + MN * (K - 1)] = z;
+#pragma unroll 4
       for (int k = K - 2; k >= 0; --k) {
         z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
         L.x[col + MN * k] = z;
