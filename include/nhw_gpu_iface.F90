@@ -49,6 +49,8 @@ module nhw_gpu_iface
   integer(c_int), parameter :: NHW_WM_WAV_CUR = 7
   integer(c_int), parameter :: NHW_WM_FOCUSED = 8
   integer(c_int), parameter :: NHW_WM_LEF_TID = 9
+  integer(c_int), parameter :: NHW_WM_RIG_LIN = 10
+  integer(c_int), parameter :: NHW_WM_FLUX_LR = 11
 
   ! ------------------------------------------- enum nhw_slide, nhw_depth_type
   integer(c_int), parameter :: NHW_SLIDE_NONE = 0

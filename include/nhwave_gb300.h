@@ -71,10 +71,16 @@ enum nhw_precision {
  * FOCUSED: waves fed through the west boundary, which then needs BC_X0 = 3:
  * linear, solitary, second-order Stokes, cnoidal, linear on a current ramped
  * up over TRAMP, a focused group of NWAVE linear components, and the S2 tide
- * (src/waves.F:92-170, 518-560, 638-756, 808-903; src/nhwave.F:5715-5750) */
+ * (src/waves.F:92-170, 518-560, 638-756, 808-903; src/nhwave.F:5715-5750).
+ * RIG_LIN: a linear wave fed through the east boundary, which then needs
+ * BC_Xn = 3 (src/waves.F:762-803).  FLUX_LR: a log-profile current in through
+ * the west side (BC_X0 = 3) and out through the east side (BC_Xn = 3) at the
+ * same volume flux, with the east values radiated as in the Orlanski
+ * condition (flux_left_right_boundary, src/nhwave.F:5566-5712; it uses Zob
+ * and TRAMP) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
                      NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7,
-                     NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9 };
+                     NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9, NHW_WM_RIG_LIN = 10, NHW_WM_FLUX_LR = 11 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 
@@ -100,9 +106,11 @@ typedef struct nhw_params {
   int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
   int32_t itmax; double tol;               /* ITMAX TOL                               */
   int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
-                                              2 no-slip wall; BC_X0 = 3 wave inflow
-                                              with a LEF_* wavemaker; BC_Xn = 6
-                                              Orlanski radiation (open east side)     */
+                                              2 no-slip wall, 5 wall friction; BC_X0 = 3
+                                              inflow with a LEF_* wavemaker or FLUX_LR;
+                                              BC_Xn = 3 inflow/outflow with RIG_LIN or
+                                              FLUX_LR; BC_Xn = 6 Orlanski radiation
+                                              (open east side)                        */
   int32_t bc_z0;                           /* BC_Z0: 1 free-slip bed, 2 no-slip,
                                               5 friction law (Ibot, Cd0, Zob)          */
   double  visc;                            /* VISCOSITY (initial Cmu)                 */

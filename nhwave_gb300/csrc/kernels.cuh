@@ -331,6 +331,100 @@ struct OpWaveBC {
   }
 };
 
+// linear_wave_right_boundary (src/waves.F:762-803): the LEF_LIN wave given to
+// the east side (BC_Xn = 3) at the step's new TIME, with the reference's
+// phase and sign convention; one thread per row j
+struct OpWaveBCEast {
+  static constexpr const char* kName = "wave_bc_east";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int, int j, int) const {
+    const double TIME = S.sc->time;
+    const double hfx = S.Hfx[i2(S, S.IE + 1, j)];
+    const int Nl = S.Nloc;
+    const double A = S.lef_amp;
+    const double phs = S.yc[j] * S.lef_sinth * S.lef_wn;
+    const double arg = kPi / 2 - S.lef_segma * TIME + phs;
+    const double cs = cos(arg), sn = sin(arg);
+    const double E = 0.5 * A * cs;
+    const double Dn = E + hfx;
+    S.Ein_xn[j] = E;
+    S.Din_xn[j] = Dn;
+    if (j < S.JB || j > S.JE) return;
+    for (int k = S.KB; k <= S.KE; ++k) {
+      const double Zlev = S.sigc[k] * Dn;
+      const double ch = cosh(S.lef_wn * Zlev), sh = sinh(S.lef_wn * Zlev);
+      const double u = 0.5 * A * S.lef_segma * ch / S.lef_shd * cs - S.lef_stokes * 1.0;
+      S.Uin_xn[j + Nl * k] = u * S.lef_costh;
+      S.Win_xn[j + Nl * k] = 0.5 * A * S.lef_segma * sh / S.lef_shd * sn;
+      S.Vin_xn[j + Nl * k] = u * S.lef_sinth;
+    }
+  }
+};
+
+// flux_left_right_boundary (src/nhwave.F:5566-5712; its sediment and
+// salinity parts are outside this path), one block: the logarithmic current
+// of depth-mean 0.115 m/s into the west side at eta = 0, ramped up by
+// tanh(TIME/TRamp), and its volume flux FluxL, summed by one thread in the
+// reference's loop order (k outer, j inner); then the east side's eta, V and
+// W radiated from the last two steps and its U mixed with the outflow
+// velocity FluxL/(Din_Xn dy Nglob) of this step and of the previous one.
+template <class T>
+__global__ void __launch_bounds__(256) k_flux_lr(Dev<T> S) {
+  if (gated_off(S)) return;
+  __shared__ double s_flux;
+  const double TIME = S.sc->time;
+  const double Ramp = S.tramp > 0.0 ? tanh(TIME / S.tramp) : 1.0;
+  const int Nl = S.Nloc, nj = S.JE - S.JB + 1, nk = S.KE - S.KB + 1;
+  for (int j = threadIdx.x; j < Nl; j += blockDim.x) {
+    S.Ein[j] = 0.0;
+    S.Din[j] = S.Ein[j] + S.Hfx[i2(S, S.IB, j)];
+  }
+  __syncthreads();
+  const double Ufric = (double)0.115f * kKappa / (log(30. * S.Din[S.JB] / S.zob));
+  for (int t = threadIdx.x; t < nj * nk; t += blockDim.x) {
+    const int j = S.JB + t % nj, k = S.KB + t / nj;
+    const double Zlev1 = S.sigc[k] * S.Din[j];
+    S.Uin[j + Nl * k] = Ufric / kKappa * log(30. * Zlev1 / S.zob) * Ramp;
+    S.Win[j + Nl * k] = 0.0;
+    S.Vin[j + Nl * k] = 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double FluxL = 0.0;
+    for (int k = S.KB; k <= S.KE; ++k)
+      for (int j = S.JB; j <= S.JE; ++j) FluxL = FluxL + S.dsig[k] * S.Din[j] * S.dy * S.Uin[j + Nl * k];
+    s_flux = FluxL;
+  }
+  auto cg = [](double a, double b, double c) {
+    const double Cg = -(a - b + kOrlSmall) / (b - c + kOrlSmall);
+    return dmax_(dmin_(Cg, 1.0), 0.0);
+  };
+  for (int j = threadIdx.x; j < Nl; j += blockDim.x) {
+    const long long e = i2(S, S.IE, j), w = i2(S, S.IE - 1, j), g = i2(S, S.IE + 1, j);
+    const double Cg = cg(S.Eta0[e], S.Eta00[e], S.Eta00[w]);
+    S.Ein_xn[j] = (Cg * S.Eta0[e] + (1.0 - Cg) * S.Eta0[g] + S.Eta[e]) / 2.0;
+    S.Din_xn[j] = S.Hfx[g] + S.Ein_xn[j];
+  }
+  __syncthreads();
+  const double FluxL = s_flux;
+  for (int t = threadIdx.x; t < Nl * S.Kloc; t += blockDim.x) {
+    const int j = t % Nl, k = t / Nl;
+    const double prev = S.Uxni[t];
+    S.Uxni0[t] = prev;
+    if (j < S.JB || j > S.JE || k < S.KB || k > S.KE) continue;
+    const double ni = FluxL / (S.Din_xn[j] * S.dy * (double)(float)S.N);
+    S.Uxni[t] = ni;
+    const long long e = i3(S, S.IE, j, k), w = i3(S, S.IE - 1, j, k), g = i3(S, S.IE + 1, j, k);
+    double Cg = cg((double)S.U0[e], (double)S.U00[e], (double)S.U00[w]);
+    const double ue = (double)S.U[e];
+    S.Uin_xn[t] = (Cg * ue + prev - Cg * ni + ue) / 2.0;
+    Cg = cg((double)S.V0[e], (double)S.V00[e], (double)S.V00[w]);
+    S.Vin_xn[t] = (Cg * (double)S.V0[e] + (1.0 - Cg) * (double)S.V0[g] + (double)S.V[e]) / 2.0;
+    Cg = cg((double)S.W0[e], (double)S.W00[e], (double)S.W00[w]);
+    S.Win_xn[t] = (Cg * (double)S.W0[e] + (1.0 - Cg) * (double)S.W0[g] + (double)S.W[e]) / 2.0;
+  }
+}
+
 // =========================================================================
 //   2-D face states shared by flux_x/y and omega_x/y
 // =========================================================================
@@ -608,7 +702,16 @@ struct OpFluxX {
       }
     }
     // east wall; an open (Orlanski) east face keeps its Riemann fluxes
-    if (f == S.IE + 1 && S.bc_xn != 6) { Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0; }
+    if (f == S.IE + 1 && S.bc_xn == 3) {   // inflow/outflow (src/nhwave.F:2411-2416)
+      const double dn = S.Din_xn[j], un = S.Uin_xn[j + S.Nloc * k];
+      const double vn = S.Vin_xn[j + S.Nloc * k], wn = S.Win_xn[j + S.Nloc * k], en = S.Ein_xn[j];
+      Ex = (R)(dn * un);
+      Fx = (R)(dn * un * un + 0.5 * kGrav * (en * en + 2.0 * en * h0));
+      Gx = (R)(dn * un * vn);
+      Hx = (R)(dn * un * wn);
+    } else if (f == S.IE + 1 && S.bc_xn != 6) {
+      Ex = (R)0; Fx = hydro<R>(reL, rh0); Gx = (R)0; Hx = (R)0;
+    }
     if (mR == 0) {
       Ex = (R)0; Gx = (R)0; Hx = (R)0;
       Fx = (f == S.IB) ? (R)0 : hydro<R>(reL, rh0) * (R)mL;
@@ -808,9 +911,10 @@ struct OpWlBcEta {
       S.D[c] = S.Din[mj];
     else if (i < S.IB && S.bc_x0 == 3)   // inflow (src/nhwave.F:5148-5157); corners copy their row's value
       S.D[c] = 2.0 * S.Din[mj] - S.D[i2(S, mi, mj)];
-    else if (i > S.IE && S.bc_xn == 6) {
-      // Orlanski radiation (src/nhwave.F:5197-5206) from the last two steps'
-      // eta; corner rows copy their mirrored row's value, as the y pass does
+    else if (i > S.IE && (S.bc_xn == 6 || S.bc_xn == 3)) {
+      // Orlanski radiation (src/nhwave.F:5182-5206, the same for the open and
+      // the inflow/outflow east side) from the last two steps' eta; corner
+      // rows copy their mirrored row's value, as the y pass does
       const long long a = i2(S, i - 1, mj), b = i2(S, i - 2, mj), g = i2(S, i, mj);
       double Cg = -(S.Eta0[a] - S.Eta00[a] + kOrlSmall) / (S.Eta00[a] - S.Eta00[b] + kOrlSmall);
       Cg = dmax_(dmin_(Cg, 1.0), 0.0);
@@ -902,6 +1006,35 @@ struct OpVelBcLat {
       S.U[o] = (T)(2.0 * un - (double)S.U[q]);
       S.V[o] = (T)(2.0 * vn - (double)S.V[q]);
       S.W[o] = (T)(2.0 * wn - (double)S.W[q]);
+      S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
+      S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
+      S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
+    } else if (jj && i > S.IE && S.bc_xn == 3) {  // inflow/outflow (src/nhwave.F:4547-4572)
+      // U(Iend+1) = Cg U(Iend) + Uin_Xni0 - Cg Uin_Xni and U(Iend+2) = Cg U(Iend+1)
+      // + (1 - Cg) U(Iend+2), U(Iend+2) as it was before this call: the second
+      // ghost's thread forms the first ghost's new value itself
+      auto cgf = [&](const T* X0, const T* X00, int ii) -> double {
+        const long long a = i3(S, ii - 1, j, k), b = i3(S, ii - 2, j, k);
+        const double Cg = -((double)X0[a] - (double)X00[a] + kOrlSmall) / ((double)X00[a] - (double)X00[b] + kOrlSmall);
+        return dmax_(dmin_(Cg, 1.0), 0.0);
+      };
+      const int jk = j + S.Nloc * k;
+      const double c1 = cgf(S.U0, S.U00, S.IE + 1);
+      double u = c1 * (double)S.U[i3(S, S.IE, j, k)] + S.Uxni0[jk] - c1 * S.Uxni[jk];
+      if (i == S.IE + 2) {
+        const T u1 = (T)u;
+        const double c2 = cgf(S.U0, S.U00, i);
+        u = c2 * (double)u1 + (1.0 - c2) * (double)S.U[o];
+      }
+      const long long a = i3(S, i - 1, j, k);
+      double Cg = cgf(S.V0, S.V00, i);
+      const double v = Cg * (double)S.V0[a] + (1.0 - Cg) * (double)S.V0[o];
+      Cg = cgf(S.W0, S.W00, i);
+      const double w = Cg * (double)S.W0[a] + (1.0 - Cg) * (double)S.W0[o];
+      const long long q = i3(S, mirror(i, S.IB, S.IE), j, k);
+      const double dn = S.Din_xn[j];
+      const double un = S.Uin_xn[jk], vn = S.Vin_xn[jk], wn = S.Win_xn[jk];
+      S.U[o] = (T)u; S.V[o] = (T)v; S.W[o] = (T)w;
       S.DU[o] = (T)(2.0 * dn * un - (double)S.DU[q]);
       S.DV[o] = (T)(2.0 * dn * vn - (double)S.DV[q]);
       S.DW[o] = (T)(2.0 * dn * wn - (double)S.DW[q]);
@@ -1597,6 +1730,7 @@ struct OpOmegaX {
     R Ex = hll_d<R>(SL, SR, duL, duR, rdd);
     if (f == S.IB || (f == S.IE + 1 && S.bc_xn != 6)) Ex = (R)0;
     if (f == S.IB && S.bc_x0 == 3) Ex = (R)(S.Din[j] * S.Uin[j + S.Nloc * k]);   // src/nhwave.F:1564-1566
+    if (f == S.IE + 1 && S.bc_xn == 3) Ex = (R)(S.Din_xn[j] * S.Uin_xn[j + S.Nloc * k]);   // :1580-1581
     S.Ex[i3(S, f, j, k)] = Ex;
   }
 };

@@ -68,6 +68,78 @@ __device__ __forceinline__ V spmv_c(const C* __restrict__ cf, const V* __restric
   return s;
 }
 
+// y = A x walked up a water column: thread t takes column t % (M N) and the
+// levels [k0, k1) of chunk t / (M N) (chunks of kc levels).  x at the
+// column and its four horizontal neighbours is loaded once per level and kept
+// in registers for the levels above and below, so a level costs five loads of
+// x instead of the fifteen of spmv_c; each level's sum is formed in spmv_c's
+// order, so y is the same bit for bit.  f(ic, y) takes each result.
+// The BiCGSTAB matvecs of the FP32+IR form walk columns (C2: 30.9 -> 23.6 us
+// for v = A ph); in FP64 the walk's registers (58-80) cost more than the
+// reloads it saves, so the FP64 operator keeps one cell per thread.
+template <class T>
+constexpr bool kColumnWalk = sizeof(T) == 4;
+
+template <class V>
+struct Xcol {
+  V c, e, w, nn, s;
+};
+template <class C, class V, class F>
+__device__ __forceinline__ void spmv_column(const C* __restrict__ cf, const V* __restrict__ x, size_t n, int t,
+                                            int kc, int M, int N, int K, V cxx, V cyy, F f) {
+  const int MN = M * N;
+  const int col = t % MN, chunk = t / MN;
+  const int ii = col % M, jj = col / M;
+  const int k0 = chunk * kc, k1 = min(K, k0 + kc);
+  if (k0 >= K) return;
+  const bool im = ii > 0, ip = ii < M - 1, jm = jj > 0, jp = jj < N - 1;
+  auto load = [&](int k) {
+    const int ic = col + MN * k;
+    Xcol<V> r;
+    r.c = x[ic];
+    r.e = ip ? x[ic + 1] : (V)0;
+    r.w = im ? x[ic - 1] : (V)0;
+    r.nn = jp ? x[ic + M] : (V)0;
+    r.s = jm ? x[ic - M] : (V)0;
+    return r;
+  };
+  Xcol<V> lo{}, mid = load(k0), hi{};
+  if (k0 > 0) lo = load(k0 - 1);
+#pragma unroll 2
+  for (int k = k0; k < k1; ++k) {
+    const int ic = col + MN * k;
+    const bool kp = k < K - 1, km = k > 0;
+    if (kp) hi = load(k + 1);
+    V s = (V)cf[ic] * mid.c;
+    V h = (V)0;
+    if (ip) h += mid.e;
+    if (im) h += mid.w;
+    s += cxx * h;
+    h = (V)0;
+    if (jp) h += mid.nn;
+    if (jm) h += mid.s;
+    s += cyy * h;
+    const V c4 = (V)cf[3 * n + ic], c5 = (V)cf[4 * n + ic], c7 = (V)cf[5 * n + ic], c8 = (V)cf[6 * n + ic];
+    if (kp) {
+      s += (V)cf[n + ic] * hi.c;
+      if (ip) s += c7 * hi.e;
+      if (im) s += c5 * hi.w;
+      if (jp) s += c8 * hi.nn;
+      if (jm) s += c4 * hi.s;
+    }
+    if (km) {
+      s += (V)cf[2 * n + ic] * lo.c;
+      if (ip) s -= c7 * lo.e;
+      if (im) s -= c5 * lo.w;
+      if (jp) s -= c8 * lo.nn;
+      if (jm) s -= c4 * lo.s;
+    }
+    f(ic, s);
+    lo = mid;
+    mid = hi;
+  }
+}
+
 // block-wide sum of NV accumulators (A = float or double), result in lane 0 of warp 0
 template <int NV, class A>
 __device__ __forceinline__ void block_sum_t(A (&v)[NV], double (&out)[NV]) {
@@ -343,15 +415,25 @@ __global__ void __launch_bounds__(256) k_bicg_v(Dev<T> S) {
   const T* __restrict__ ph = S.kph;
   const T* __restrict__ r0 = S.kr0;
   T* __restrict__ vv = S.kv;
+  if constexpr (kColumnWalk<T>) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < S.M * S.N * S.col_chunks)
+      spmv_column<T, T>(S.coefT, ph, (size_t)S.neq, t, S.col_kc, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy,
+                        [&](int ic, T y) {
+                          vv[ic] = y;
+                          v[0] += (A)r0[ic] * (A)y;
+                        });
+  } else {
 #pragma unroll
-  for (int q = 0; q < kCPT; ++q) {
-    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
-    if (ic < S.neq) {
-      int ii, jj, kk;
-      decode(ic, S.M, S.N, ii, jj, kk);
-      const T y = spmv_c<T, T>(S.coefT, ph, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
-      vv[ic] = y;
-      v[0] += (A)r0[ic] * (A)y;
+    for (int q = 0; q < kCPT; ++q) {
+      const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+      if (ic < S.neq) {
+        int ii, jj, kk;
+        decode(ic, S.M, S.N, ii, jj, kk);
+        const T y = spmv_c<T, T>(S.coefT, ph, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
+        vv[ic] = y;
+        v[0] += (A)r0[ic] * (A)y;
+      }
     }
   }
   double out[1];
@@ -372,16 +454,27 @@ __global__ void __launch_bounds__(256) k_bicg_t(Dev<T> S) {
   const T* __restrict__ sh = S.ksh;
   const T* __restrict__ ss = S.ks;
   T* __restrict__ tt = S.kt;
+  if constexpr (kColumnWalk<T>) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < S.M * S.N * S.col_chunks)
+      spmv_column<T, T>(S.coefT, sh, (size_t)S.neq, t, S.col_kc, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy,
+                        [&](int ic, T y) {
+                          tt[ic] = y;
+                          v[0] += (A)y * (A)ss[ic];
+                          v[1] += (A)y * (A)y;
+                        });
+  } else {
 #pragma unroll
-  for (int q = 0; q < kCPT; ++q) {
-    const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
-    if (ic < S.neq) {
-      int ii, jj, kk;
-      decode(ic, S.M, S.N, ii, jj, kk);
-      const T y = spmv_c<T, T>(S.coefT, sh, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
-      tt[ic] = y;
-      v[0] += (A)y * (A)ss[ic];
-      v[1] += (A)y * (A)y;
+    for (int q = 0; q < kCPT; ++q) {
+      const int ic = (blockIdx.x * kCPT + q) * blockDim.x + threadIdx.x;
+      if (ic < S.neq) {
+        int ii, jj, kk;
+        decode(ic, S.M, S.N, ii, jj, kk);
+        const T y = spmv_c<T, T>(S.coefT, sh, (size_t)S.neq, ic, ii, jj, kk, S.M, S.N, S.K, (T)S.cxx, (T)S.cyy);
+        tt[ic] = y;
+        v[0] += (A)y * (A)ss[ic];
+        v[1] += (A)y * (A)y;
+      }
     }
   }
   double out[2];

@@ -33,21 +33,28 @@ int check_params(const nhw_params& p) {
   // lateral sides: 1 free slip, 2 no slip, 5 wall friction; BC_Xn = 6 Orlanski
   for (int b : {p.bc_y0, p.bc_yn})
     if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
-  if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;
-  const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID;
-  // west inflow (BC_X0 = 3) only with a wave fed through it
+  // east side: BC_Xn = 3 only with RIG_LIN or FLUX_LR, which feed it
+  const bool east_in = p.wavemaker == NHW_WM_RIG_LIN || p.wavemaker == NHW_WM_FLUX_LR;
+  if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6 && !(p.bc_xn == 3 && east_in))
+    return NHW_ERR_UNSUPPORTED;
+  const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ||
+                   p.wavemaker == NHW_WM_FLUX_LR;
+  // west inflow (BC_X0 = 3) only with a wave or current fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker == NHW_WM_FLUX_LR && !(p.zob > 0.0)) return NHW_ERR_ARG;   // log-profile inflow
   // bed: 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   if (p.bc_z0 != 1 && p.bc_z0 != 2 && p.bc_z0 != 5) return NHW_ERR_UNSUPPORTED;
   const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
   if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_TID) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_FLUX_LR) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
-  if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && !(p.per_wave > 0 && p.dep_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && p.wavemaker != NHW_WM_FLUX_LR &&
+      !(p.per_wave > 0 && p.dep_wave > 0))
+    return NHW_ERR_ARG;
   // FOCUSED: at least two components (the frequency spacing divides by
   // NWAVE - 1), at most the reference's 12000
   if (p.wavemaker == NHW_WM_FOCUSED &&
@@ -320,7 +327,8 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     h.wm_celerity = std::sqrt(kGravH * Dep * (1.0 + A / Dep));
     h.wm_atmp = std::sqrt((double)0.75f * A / (Dep * Dep * Dep));
     h.wm_xstart = 4.0 * Dep / std::sqrt(A / Dep);
-  } else if (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_WAV_CUR) {   // src/waves.F:720-730, 820-829
+  } else if (p.wavemaker == NHW_WM_LEF_LIN || p.wavemaker == NHW_WM_WAV_CUR ||
+             p.wavemaker == NHW_WM_RIG_LIN) {   // src/waves.F:720-730, 774-784, 820-829
     h.lef_segma = 2.0 * kPiH / p.per_wave;
     h.lef_wn = wave_number(h.lef_segma, p.dep_wave);
     const double wl = 2.0 * kPiH / h.lef_wn;

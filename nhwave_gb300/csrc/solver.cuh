@@ -212,6 +212,10 @@ class Solver final : public SolverBase {
     S.sz = (long long)S.sy * (S.Nloc + 1);
     S.IB = NG; S.IE = M + NG - 1; S.JB = NG; S.JE = N + NG - 1; S.KB = NG; S.KE = K + NG - 1;
     S.neq = M * N * K;
+    // column-walk matvecs: two chunks of levels per column on tall grids
+    // (twice the threads; each chunk reloads one level above and below)
+    S.col_chunks = K >= 16 ? 2 : 1;
+    S.col_kc = (K + S.col_chunks - 1) / S.col_chunks;
     S.dx = p.dx; S.dy = p.dy; S.min_dep = p.min_dep; S.cfl = p.cfl;
     S.cxx = -1. / (p.dx * p.dx); S.cyy = -1. / (p.dy * p.dy);
     S.i2dx = 0.5 / p.dx; S.i2dy = 0.5 / p.dy;
@@ -286,10 +290,12 @@ class Solver final : public SolverBase {
     T** t3[] = {&S.U, &S.V, &S.W, &S.DU, &S.DV, &S.DW, &S.DU0, &S.DV0, &S.DW0, &S.Omega,
                 &S.Ex, &S.Fx, &S.Gx, &S.Hx, &S.Ey, &S.Fy, &S.Gy, &S.Hy, &S.Fz, &S.Gz, &S.Hz};
     for (auto pp : t3) add(pp, sizeof(T) * n3);
-    if (p.bc_xn == 6) {   // Orlanski boundary: two earlier time levels (checkpointed state)
+    if (p.bc_xn == 6 || p.bc_xn == 3) {   // east boundary: two earlier time levels (checkpointed state)
       add(&S.Eta00, sizeof(double) * n2);
       for (T** pp : {&S.U0, &S.V0, &S.W0, &S.U00, &S.V00, &S.W00}) add(pp, sizeof(T) * n3);
     }
+    if (p.bc_xn == 3)   // FLUX_LR's outflow velocities of this and the previous step (checkpointed state)
+      for (double** pp : {&S.Uxni, &S.Uxni0}) add(pp, sizeof(double) * S.Nloc * S.Kloc);
     if (p.viscous_flow)   // sigma_transform's inputs, read by the next stage (checkpointed state)
       for (double** pp : {&S.scD, &S.scEx, &S.scEy, &S.scHx, &S.scHy}) add(pp, sizeof(double) * n2);
     add(&S.P, sizeof(double) * n3);
@@ -299,6 +305,10 @@ class Solver final : public SolverBase {
     add(&S.Ein, sizeof(double) * S.Nloc);
     add(&S.Din, sizeof(double) * S.Nloc);
     for (double** pp : {&S.Uin, &S.Vin, &S.Win}) add(pp, sizeof(double) * S.Nloc * S.Kloc);
+    if (p.bc_xn == 3) {   // east-boundary values, recomputed every step
+      for (double** pp : {&S.Ein_xn, &S.Din_xn}) add(pp, sizeof(double) * S.Nloc);
+      for (double** pp : {&S.Uin_xn, &S.Vin_xn, &S.Win_xn}) add(pp, sizeof(double) * S.Nloc * S.Kloc);
+    }
     add(&S.coef64, sizeof(double) * NCOMPACT * neq);
     add(&S.rhs64, sizeof(double) * neq);
     add(&S.xsol64, sizeof(double) * neq);
@@ -445,6 +455,9 @@ class Solver final : public SolverBase {
   }
   template <class Op> void cells(Op op) { box(op, S.M, S.N, S.K, S.IB, S.JB, S.KB); }
   unsigned red_blocks() const { return cdiv(S.neq, 256 * kCPT); }
+  // the column-walk matvec kernels: one thread per column and chunk of levels
+  unsigned col_blocks() const { return cdiv((long long)S.M * S.N * S.col_chunks, 256); }
+  unsigned matvec_blocks() const { return kColumnWalk<T> ? col_blocks() : red_blocks(); }
 
   int check() {
     cudaError_t e = launch_err != cudaSuccess ? launch_err : cudaGetLastError();
@@ -658,6 +671,7 @@ class Solver final : public SolverBase {
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
     S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ? p.wavemaker : 0;
+    S.east = p.bc_xn == 3 ? p.wavemaker : 0;   // RIG_LIN or FLUX_LR (check_params)
     if (S.lef == NHW_WM_FOCUSED)
       NHW_CU(cudaMemcpyAsync((void*)S.foc, h.foc.data(), sizeof(double) * h.foc.size(), cudaMemcpyHostToDevice, st));
     S.lef_amp = p.amp_wave; S.lef_dep = p.dep_wave; S.lef_per = p.per_wave;
@@ -781,8 +795,10 @@ class Solver final : public SolverBase {
     return check();
   }
   int update_wave_bc() override {
-    if (!S.lef) return NHW_OK;
-    box(OpWaveBC{}, 1, S.Nloc, 1, 0, 0, 0);
+    if (!S.lef && !S.east) return NHW_OK;
+    if (S.lef) box(OpWaveBC{}, 1, S.Nloc, 1, 0, 0, 0);
+    if (S.east == NHW_WM_RIG_LIN) box(OpWaveBCEast{}, 1, S.Nloc, 1, 0, 0, 0);
+    if (S.east == NHW_WM_FLUX_LR) L("flux_lr", [&] { k_flux_lr<T><<<1, 256, 0, st>>>(S); });
     return check();
   }
   int update_mask() override {
@@ -983,13 +999,13 @@ class Solver final : public SolverBase {
     } else {
       L("bicg_p", [&] { k_bicg_p<T><<<cb, 128, 0, st>>>(S); });
     }
-    L("bicg_v", [&] { k_bicg_v<T><<<red_blocks(), 256, 0, st>>>(S); });
+    L("bicg_v", [&] { k_bicg_v<T><<<matvec_blocks(), 256, 0, st>>>(S); });
     if (use_mg) {
       vcycle(S.ks, S.ksh, 2);   // s likewise
     } else {
       L("bicg_s", [&] { k_bicg_s<T><<<cb, 128, 0, st>>>(S); });
     }
-    L("bicg_t", [&] { k_bicg_t<T><<<red_blocks(), 256, 0, st>>>(S); });
+    L("bicg_t", [&] { k_bicg_t<T><<<matvec_blocks(), 256, 0, st>>>(S); });
     L("bicg_xr", [&] { k_bicg_xr<T><<<red_blocks(), 256, 0, st>>>(S); });
   }
   // multigrid V-cycle: x ~= A^-1 b on level 0

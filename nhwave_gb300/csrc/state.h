@@ -72,6 +72,7 @@ struct Dev {
   long long sz;      // k stride
   int IB, IE, JB, JE, KB, KE;   // interior bounds (inclusive), 0-based
   int neq;           // M*N*K
+  int col_chunks, col_kc;   // column-walk matvecs: chunks per column, levels per chunk
   // parameters
   double dx, dy, min_dep, cfl, dt_min, dt_max, fcor, froude_cap;
   double cxx, cyy;                 // Poisson in-level couplings -1/dx^2, -1/dy^2
@@ -119,6 +120,13 @@ struct Dev {
   double foc_xb, foc_tb, foc_dc, foc_sd;
   double *Ein, *Din;               // [Nloc] Ein_X0, Din_X0
   double *Uin, *Vin, *Win;         // [Kloc][Nloc] Uin_X0 .. (index j + Nloc*k)
+  // the east side open to a boundary condition (BC_Xn = 3): RIG_LIN or
+  // FLUX_LR (0: none); its values of the step (src/nhwave.F:5514-5712), and
+  // FLUX_LR's outflow velocity of this and the previous step (checkpointed)
+  int east;
+  double *Ein_xn, *Din_xn;         // [Nloc] Ein_Xn, Din_Xn
+  double *Uin_xn, *Vin_xn, *Win_xn;  // [Kloc][Nloc] Uin_Xn ..
+  double *Uxni, *Uxni0;            // [Kloc][Nloc] Uin_Xni, Uin_Xni0
   // sponge current
   double cur_wave, tramp;
   // rigid slide (RIGID_3D)
@@ -128,7 +136,7 @@ struct Dev {
   const double *sig, *dsig, *sigc, *xc, *yc;
   // 2-D FP64 fields
   double *D, *D0, *Eta, *Eta0, *Hc, *Hc0, *Ho;
-  double* Eta00;               // Orlanski boundary (BC_Xn = 6) only, else nullptr
+  double* Eta00;               // east boundary of BC_Xn = 6 or 3 only, else nullptr
   // viscous flow only, else nullptr: D, DelxEta, DelyEta, DelxH, DelyH as of
   // the last sigma_transform, from which the viscous terms form DelxSc /
   // DelySc (cell levels) and DelxSl / DelySl (faces) of that moment

@@ -14,9 +14,11 @@ import ctypes
 NHW_FP64 = 0
 NHW_FP32_IR = 1
 (WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED,
- WM_LEF_TID) = range(10)
+ WM_LEF_TID, WM_RIG_LIN, WM_FLUX_LR) = range(12)
 # fed through the west boundary (BC_X0 = 3)
-WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID)
+WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID, WM_FLUX_LR)
+# fed through the east boundary (BC_Xn = 3)
+WM_EAST = (WM_RIG_LIN, WM_FLUX_LR)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
 SLIDE_NONE, SLIDE_RIGID_3D = 0, 1
 DEPTH_CELL_CENTER, DEPTH_CELL_GRID = 0, 1
@@ -194,11 +196,10 @@ def read_input(path: str) -> NhwParams:
     p.depth_type = DEPTH_CELL_GRID if dt_ == "CELL_GRID" else DEPTH_CELL_CENTER
     wm = s("WAVEMAKER", "NONE").upper()
     # a generator of the reference that this path does not build (LEF_SPC,
-    # LEF_JON, INT_IRR, FLUX_LR, ...) is kept as WM_OTHER and rejected, not run
-    # as NONE
+    # LEF_JON, INT_IRR, ...) is kept as WM_OTHER and rejected, not run as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
              "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR,
-             "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID}
+             "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID, "RIG_LIN": WM_RIG_LIN, "FLUX_LR": WM_FLUX_LR}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
@@ -243,16 +244,20 @@ def unsupported_reason(p: NhwParams) -> str | None:
                 "IVTURB = IHTURB = 1, are on the GPU path; the k-epsilon and LES models are not)")
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
-    if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF:
-        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR "
-                "and FOCUSED are on the GPU path)")
+    if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF + WM_EAST:
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR, "
+                "FOCUSED, RIG_LIN and FLUX_LR are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
-        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR or FOCUSED wavemaker"
+        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR, FOCUSED or FLUX_LR wavemaker"
+    if p.bc_xn == 3 and p.wavemaker not in WM_EAST:
+        return "BC_Xn=3 needs the RIG_LIN or FLUX_LR wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
-        ok = {"bc_x0": (1, 2, 3, 5), "bc_xn": (1, 2, 5, 6)}.get(name, (1, 2, 5))
+        ok = {"bc_x0": (1, 2, 3, 5), "bc_xn": (1, 2, 3, 5, 6)}.get(name, (1, 2, 5))
         if getattr(p, name) not in ok:
-            return (f"{name.upper()}={getattr(p, name)} (walls 1/2, wall friction 5, the west inflow 3 "
+            return (f"{name.upper()}={getattr(p, name)} (walls 1/2, wall friction 5, the inflows 3 "
                     "and the east Orlanski boundary 6 are on the GPU path)")
+    if p.wavemaker == WM_FLUX_LR and not p.zob > 0:
+        return "FLUX_LR needs Zob > 0 (its inflow has a logarithmic profile)"
     if p.bc_z0 not in (1, 2, 5):
         return f"BC_Z0={p.bc_z0} (free slip 1, no slip 2 and the friction law 5 are on the GPU path)"
     if 5 in (p.bc_z0, p.bc_x0, p.bc_xn, p.bc_y0, p.bc_yn) and p.ibot not in (1, 2):
@@ -268,6 +273,7 @@ __all__ = [
     "NhwParams", "NhwScalars", "default_params", "read_input", "unsupported_reason", "cells",
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
     "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF_TID", "WM_LEF",
+    "WM_RIG_LIN", "WM_FLUX_LR", "WM_EAST",
     "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",

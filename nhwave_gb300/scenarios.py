@@ -167,6 +167,37 @@ def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5,
     return p, np.full(M * N, depth), None, None
 
 
+# ------------------------------------------------------- east inflows
+def east_flume(kind: str = "RIG", M=64, N=4, K=5, dx=0.1, dy=0.1, depth=0.5, amp=0.02, per=1.5, **kw):
+    """Flumes whose east side is open to a boundary condition (BC_Xn = 3).
+    ``RIG``: a linear wave given to the east side (RIG_LIN, amplitude `amp`,
+    period `per`), wall and a 1.5 m sponge at the west end.  ``FLR``: the
+    FLUX_LR current, in through the west side (BC_X0 = 3) over a smooth bump
+    of a fifth of the depth, out through the east side, ramped up over TRAMP
+    = 1 s, roughness Zob = 1 mm.  At rest initially."""
+    from .params import WM_FLUX_LR, WM_RIG_LIN
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
+                       dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, total_time=20.0)
+    p.bc_xn = 3
+    p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
+    xs = _xc(p)
+    h = np.full(M, depth)
+    if kind == "RIG":
+        p.wavemaker = WM_RIG_LIN
+        p.sponge_on = 1
+        p.sponge_west_width = 1.5
+    else:
+        p.wavemaker = WM_FLUX_LR
+        p.bc_x0 = 3
+        p.tramp = 1.0
+        p.zob = 1e-3
+        h = depth - 0.2 * depth * np.exp(-((xs - 0.5 * M * dx) / (0.1 * M * dx)) ** 2)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, np.broadcast_to(h, (N, M)).copy().ravel(), None, None
+
+
 # ------------------------------------------------------------ registry
 def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
     """Return ``(params, depth, eta0, uvw0)`` for a named scenario."""
@@ -237,6 +268,12 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)
+    elif name == "tiny_flume_rig":
+        # a linear wave given to the east side (RIG_LIN through BC_Xn = 3), wall and sponge at the west
+        out = east_flume("RIG", **kw)
+    elif name == "tiny_flux_lr":
+        # the FLUX_LR current through the west (BC_X0 = 3) and east (BC_Xn = 3) sides, over a bump
+        out = east_flume("FLR", depth=0.3, **kw)
     elif name == "tiny_flume_open":
         # linear wave fed in at the west and let out through an Orlanski east side, no sponge
         out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, bc_xn=6, sponge_on=0, **kw)

@@ -200,6 +200,11 @@ struct Model {
   // west-boundary inflow (Ein_X0, Din_X0, Uin_X0, Vin_X0, Win_X0; src/mod_global.F)
   A1 Ein_X0, Din_X0;
   A2 Uin_X0, Vin_X0, Win_X0;
+  // east-boundary inflow/outflow (Ein_Xn ... Win_Xn) and the FLUX_LR outflow
+  // velocities of this and the previous call (Uin_Xni, Uin_Xni0; zero at
+  // start, src/initialize.F:2688-2689)
+  A1 Ein_Xn, Din_Xn;
+  A2 Uin_Xn, Vin_Xn, Win_Xn, Uin_Xni, Uin_Xni0;
   A3 U, V, W, DU, DV, DW, DU0, DV0, DW0, P, Omega, Uf, Vf, Wf;
   A3 U0, V0, W0, U00, V00, W00;   // earlier time levels, read by the Orlanski boundary
   A3 UxL, UxR, VxL, VxR, WxL, WxR, DUxL, DUxR, DVxL, DVxR, DWxL, DWxR;
@@ -232,9 +237,14 @@ struct Model {
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
-    if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6) return NHW_ERR_UNSUPPORTED;   // 6: Orlanski
-    const bool lef = p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID;
+    const bool east_in = p.wavemaker == NHW_WM_RIG_LIN || p.wavemaker == NHW_WM_FLUX_LR;
+    // 6: Orlanski; 3: inflow/outflow of RIG_LIN and FLUX_LR
+    if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6 && !(p.bc_xn == 3 && east_in))
+      return NHW_ERR_UNSUPPORTED;
+    const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ||
+                     p.wavemaker == NHW_WM_FLUX_LR;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
+    if (p.wavemaker == NHW_WM_FLUX_LR && !(p.zob > 0.0)) return NHW_ERR_ARG;
     if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
       if (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0)) return NHW_ERR_ARG;
       const int nw = p.nwave;
@@ -284,6 +294,8 @@ struct Model {
     x.init(Mloc1); xc.init(Mloc); y.init(Nloc1); yc.init(Nloc);
     Ein_X0.init(Nloc); Din_X0.init(Nloc);
     for (A2* a : {&Uin_X0, &Vin_X0, &Win_X0}) a->init(Nloc, Kloc);
+    Ein_Xn.init(Nloc); Din_Xn.init(Nloc);
+    for (A2* a : {&Uin_Xn, &Vin_Xn, &Win_Xn, &Uin_Xni, &Uin_Xni0}) a->init(Nloc, Kloc);
     sig.init(Kloc1); dsig.init(Kloc); sigc.init(Kloc);
     for (A2* a : {&Hc, &Hc0, &Ho, &DeltH, &DeltHo, &Delt2H, &DelxH, &DelyH, &D, &D0, &Eta, &Eta0, &Eta00,
                   &SourceX, &SourceY, &SourceC, &DelxEta, &DelyEta, &Sponge, &Wsx, &Wsy, &R1s})
@@ -859,6 +871,82 @@ struct Model {
           Vin_X0(j, k) = 0.0;
         }
     }
+    if (p.wavemaker == NHW_WM_RIG_LIN) right_boundary_linear();
+    if (p.wavemaker == NHW_WM_FLUX_LR) flux_left_right();
+  }
+
+  // linear_wave_right_boundary (src/waves.F:762-803): the linear wave of
+  // LEF_LIN given to the east side (BC_Xn = 3), with the same phase and sign
+  // convention as the west one
+  void right_boundary_linear() {
+    const double Segma = 2.0 * pi / p.per_wave;
+    const double Wave_Number = wave_dispersion(Segma);
+    const double Wave_Length = 2.0 * pi / Wave_Number;
+    const double Stokes_Drift = Grav * (p.amp_wave * p.amp_wave) / (Wave_Length / p.per_wave) / p.dep_wave / 8.0;
+    const double Fact = 1.0;
+    const double th = p.theta_wave * pi / 180.;
+    for (int j = 1; j <= Nloc; ++j) {
+      const double Phs_Lag = yc(j) * std::sin(th) * Wave_Number;
+      Ein_Xn(j) = 0.5 * p.amp_wave * std::cos(pi / 2 - Segma * TIME + Phs_Lag);
+      Din_Xn(j) = Ein_Xn(j) + Hfx(Iend1, j);
+    }
+    const double shd = std::sinh(Wave_Number * p.dep_wave);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Phs_Lag = yc(j) * std::sin(th) * Wave_Number;
+        const double Zlev = sigc(k) * Din_Xn(j);
+        const double cs = std::cos(pi / 2 - Segma * TIME + Phs_Lag), sn = std::sin(pi / 2 - Segma * TIME + Phs_Lag);
+        Uin_Xn(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+                       std::cos(th);
+        Win_Xn(j, k) = 0.5 * p.amp_wave * Segma * std::sinh(Wave_Number * Zlev) / shd * sn;
+        Vin_Xn(j, k) = (0.5 * p.amp_wave * Segma * std::cosh(Wave_Number * Zlev) / shd * cs - Stokes_Drift * Fact) *
+                       std::sin(th);
+      }
+  }
+
+  // flux_left_right_boundary (src/nhwave.F:5566-5712) without its sediment
+  // and salinity parts: a logarithmic current of depth-mean 0.115 m/s into
+  // the west side at eta = 0, ramped up by tanh(TIME/TRamp); its volume flux
+  // FluxL leaves through the east side, whose eta, V and W are radiated from
+  // the last two steps and whose U mixes the interior value with the outflow
+  // velocity FluxL/(Din_Xn dy Nglob) of this call and the previous one
+  void flux_left_right() {
+    const double Uavg_Left = (double)0.115f;
+    double FluxL = 0.0;
+    const double Ramp = p.tramp > 0.0 ? std::tanh(TIME / p.tramp) : 1.0;
+    for (int j = 1; j <= Nloc; ++j) {
+      Ein_X0(j) = 0.0;
+      Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+    }
+    const double Ufric = Uavg_Left * Kappa / (std::log(30. * Din_X0(Jbeg) / p.zob));
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Zlev1 = sigc(k) * Din_X0(j);
+        Uin_X0(j, k) = Ufric / Kappa * std::log(30. * Zlev1 / p.zob) * Ramp;
+        FluxL = FluxL + dsig(k) * Din_X0(j) * dy * Uin_X0(j, k);
+        Win_X0(j, k) = 0.0;
+        Vin_X0(j, k) = 0.0;
+      }
+    auto cg = [&](double a, double b, double c) {   // Cg = -(a - b + 1e-16)/(b - c + 1e-16) in [0, 1]
+      const double Cg = -(a - b + kOrlSmall) / (b - c + kOrlSmall);
+      return dmax(dmin(Cg, 1.0), 0.0);
+    };
+    for (int j = 1; j <= Nloc; ++j) {
+      const double Cg = cg(Eta0(Iend, j), Eta00(Iend, j), Eta00(Iend - 1, j));
+      Ein_Xn(j) = (Cg * Eta0(Iend, j) + (1.0 - Cg) * Eta0(Iend + 1, j) + Eta(Iend, j)) / 2.0;
+      Din_Xn(j) = Hfx(Iend + 1, j) + Ein_Xn(j);
+    }
+    Uin_Xni0 = Uin_Xni;
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        Uin_Xni(j, k) = FluxL / (Din_Xn(j) * dy * (double)(float)p.Nglob);
+        double Cg = cg(U0(Iend, j, k), U00(Iend, j, k), U00(Iend - 1, j, k));
+        Uin_Xn(j, k) = (Cg * U(Iend, j, k) + Uin_Xni0(j, k) - Cg * Uin_Xni(j, k) + U(Iend, j, k)) / 2.0;
+        Cg = cg(V0(Iend, j, k), V00(Iend, j, k), V00(Iend - 1, j, k));
+        Vin_Xn(j, k) = (Cg * V0(Iend, j, k) + (1.0 - Cg) * V0(Iend + 1, j, k) + V(Iend, j, k)) / 2.0;
+        Cg = cg(W0(Iend, j, k), W00(Iend, j, k), W00(Iend - 1, j, k));
+        Win_Xn(j, k) = (Cg * W0(Iend, j, k) + (1.0 - Cg) * W0(Iend + 1, j, k) + W(Iend, j, k)) / 2.0;
+      }
   }
 
   double source_area() {
@@ -1293,7 +1381,12 @@ struct Model {
           Ex(Ibeg, j, k) = Zero; Fx(Ibeg, j, k) = hydro(EtaxR(Ibeg, j), Hfx0(Ibeg, j));
           Gx(Ibeg, j, k) = Zero; Hx(Ibeg, j, k) = Zero;
         }
-        if (p.bc_xn != 6) {   // an open (Orlanski) east face keeps its Riemann fluxes
+        if (p.bc_xn == 3) {   // inflow/outflow (src/nhwave.F:2411-2416)
+          Ex(Iend1, j, k) = Din_Xn(j) * Uin_Xn(j, k);
+          Fx(Iend1, j, k) = Din_Xn(j) * Uin_Xn(j, k) * Uin_Xn(j, k) + hydro(Ein_Xn(j), Hfx0(Iend1, j));
+          Gx(Iend1, j, k) = Din_Xn(j) * Uin_Xn(j, k) * Vin_Xn(j, k);
+          Hx(Iend1, j, k) = Din_Xn(j) * Uin_Xn(j, k) * Win_Xn(j, k);
+        } else if (p.bc_xn != 6) {   // an open (Orlanski) east face keeps its Riemann fluxes
           Ex(Iend1, j, k) = Zero; Fx(Iend1, j, k) = hydro(EtaxL(Iend1, j), Hfx0(Iend1, j));
           Gx(Iend1, j, k) = Zero; Hx(Iend1, j, k) = Zero;
         }
@@ -1347,7 +1440,7 @@ struct Model {
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = 2.0 * Din_X0(j) - D(Ibeg + i - 1, j);
       else
         for (int i = 1; i <= Nghost; ++i) D(Ibeg - i, j) = D(Ibeg + i - 1, j);
-      if (p.bc_xn == 6)   // Orlanski radiation (src/nhwave.F:5197-5206)
+      if (p.bc_xn == 6 || p.bc_xn == 3)   // Orlanski radiation (src/nhwave.F:5182-5206)
         for (int i = 1; i <= Nghost; ++i) {
           double Cg = -(Eta0(Iend + i - 1, j) - Eta00(Iend + i - 1, j) + kOrlSmall) /
                       (Eta00(Iend + i - 1, j) - Eta00(Iend + i - 2, j) + kOrlSmall);
@@ -1650,6 +1743,26 @@ struct Model {
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = 1; i <= Nghost; ++i) {
           if (p.bc_xn == 5) break;
+          if (p.bc_xn == 3) {   // inflow/outflow (src/nhwave.F:4547-4572)
+            auto cgf = [&](A3& X0, A3& X00) {
+              const double Cg = -(X0(Iend + i - 1, j, k) - X00(Iend + i - 1, j, k) + kOrlSmall) /
+                                (X00(Iend + i - 1, j, k) - X00(Iend + i - 2, j, k) + kOrlSmall);
+              return dmax(dmin(Cg, 1.0), 0.0);
+            };
+            double Cg = cgf(U0, U00);
+            if (i == 1)
+              U(Iend + i, j, k) = Cg * U(Iend + i - 1, j, k) + Uin_Xni0(j, k) - Cg * Uin_Xni(j, k);
+            else
+              U(Iend + i, j, k) = Cg * U(Iend + i - 1, j, k) + (1.0 - Cg) * U(Iend + i, j, k);
+            Cg = cgf(V0, V00);
+            V(Iend + i, j, k) = Cg * V0(Iend + i - 1, j, k) + (1.0 - Cg) * V0(Iend + i, j, k);
+            Cg = cgf(W0, W00);
+            W(Iend + i, j, k) = Cg * W0(Iend + i - 1, j, k) + (1.0 - Cg) * W0(Iend + i, j, k);
+            DU(Iend + i, j, k) = 2.0 * Din_Xn(j) * Uin_Xn(j, k) - DU(Iend - i + 1, j, k);
+            DV(Iend + i, j, k) = 2.0 * Din_Xn(j) * Vin_Xn(j, k) - DV(Iend - i + 1, j, k);
+            DW(Iend + i, j, k) = 2.0 * Din_Xn(j) * Win_Xn(j, k) - DW(Iend - i + 1, j, k);
+            continue;
+          }
           if (p.bc_xn == 6) {   // Orlanski radiation (src/nhwave.F:4599-4621)
             auto orl = [&](A3& X0, A3& X00) {
               double Cg = -(X0(Iend + i - 1, j, k) - X00(Iend + i - 1, j, k) + kOrlSmall) /
@@ -2141,7 +2254,8 @@ struct Model {
     for (int j = Jbeg; j <= Jend; ++j)
       for (int k = Kbeg; k <= Kend; ++k) {   // src/nhwave.F:1558-1580
         Ex(Ibeg, j, k) = p.bc_x0 == 3 ? Din_X0(j) * Uin_X0(j, k) : Zero;
-        if (p.bc_xn != 6) Ex(Iend1, j, k) = Zero;
+        if (p.bc_xn == 3) Ex(Iend1, j, k) = Din_Xn(j) * Uin_Xn(j, k);   // src/nhwave.F:1580-1581
+        else if (p.bc_xn != 6) Ex(Iend1, j, k) = Zero;
       }
     for (int i = Ibeg; i <= Iend; ++i)
       for (int k = Kbeg; k <= Kend; ++k) { Ey(i, Jbeg, k) = Zero; Ey(i, Jend1, k) = Zero; }

@@ -26,11 +26,12 @@ def _scen(name, precision, **attrs):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,krylov", [("tiny_c2", 0), ("tiny_c3", 0), ("tiny_c4", 0), ("tiny_flume_lin", 0),
-                                         ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2)])
+                                         ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0)])
 def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     """krylov = 2: the GMRES solver, whose basis lies behind the checkpointed
     prefix and is rebuilt by every solve.  tiny_open: the Orlanski boundary's
-    two earlier time levels are part of the checkpointed state; tiny_visc:
+    two earlier time levels are part of the checkpointed state; tiny_flux_lr:
+    so are FLUX_LR's outflow velocities of the last two steps; tiny_visc:
     the sigma slopes the next viscous terms read, and whether eval_turb has
     run, are too."""
     from nhwave_gb300 import fields as F

@@ -153,10 +153,11 @@ def test_ensemble_of_gmres_members_matches_single_steps(precision, gpu_lib):
 @pytest.mark.parametrize("precision", [0, 1])
 def test_ensemble_of_the_added_boundaries_and_viscous_flow(precision, solver, gpu_lib):
     """Members that use the later rows -- viscous flow on a friction bed with
-    friction walls, an Orlanski east side, cnoidal and focused inflow -- step in
+    friction walls, an Orlanski east side, cnoidal and focused inflow, the
+    FLUX_LR current through both ends -- step in
     one ensemble as they step alone (bit for bit with solver 0)."""
     from nhwave_gb300 import fields as F, lib
-    names = ["tiny_visc_fric", "tiny_open", "tiny_flume_con", "tiny_flume_foc"]
+    names = ["tiny_visc_fric", "tiny_open", "tiny_flume_con", "tiny_flume_foc", "tiny_flux_lr"]
     ens = [_member(n, precision) for n in names]
     ref = [_member(n, precision) for n in names]
     with lib.Ensemble(ens, solver=solver) as e:

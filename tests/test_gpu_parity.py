@@ -239,8 +239,10 @@ def test_golden_fixtures(name, gpu_lib):
 
 # tiny_flume_open: LEF_LIN in at the west, out through an Orlanski east side;
 # tiny_flume_stk / _con: second-order Stokes and cnoidal waves fed in
+# tiny_flume_rig / tiny_flux_lr: the east side open to RIG_LIN and to the
+# FLUX_LR current (BC_Xn = 3)
 FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open", "tiny_flume_cur",
-          "tiny_flume_foc", "tiny_flume_tid",
+          "tiny_flume_foc", "tiny_flume_tid", "tiny_flume_rig", "tiny_flux_lr",
           "tiny_fric_log"]   # and the friction law from a roughness height: log() of CUDA and libm
 
 

@@ -497,3 +497,63 @@ def test_tide_sets_the_first_column_depth(oracle_mod):
     ein = 0.5 * p.amp_wave * math.cos(2.0 * pi / 43200.0 * t - pi / 2.0)
     D = o.get(F.D)
     assert np.allclose(D[2:-2, 0:3], p.dep_wave + ein, rtol=0, atol=1e-14)
+
+
+def _pi_sp():
+    return float(np.float32(3.141592653))
+
+
+def test_east_linear_wave_sets_the_east_face_fluxes(oracle_mod):
+    """RIG_LIN through BC_Xn = 3 (linear_wave_right_boundary, src/waves.F:762-803;
+    flux_bc src/nhwave.F:2411-2416): the east face carries Din_Xn Uin_Xn with
+    Ein_Xn = 0.5 A cos(pi/2 - sigma t), Din_Xn = Ein_Xn + h and the linear
+    wave's velocity profile less its Stokes drift, level by level."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_flume_rig")
+    p.tol, p.itmax = 1e-10, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    pi, g = _pi_sp(), float(np.float32(9.81))
+    sigma = 2.0 * pi / p.per_wave
+    k = oracle_mod.lib().orc_wave_number(o._h, sigma)
+    h, A = p.dep_wave, p.amp_wave
+    sd = g * A * A / ((2.0 * pi / k) / p.per_wave) / h / 8.0
+    sigc = o.grid(6)
+    f = p.Mglob + 2                      # the east face Iend1, 0-based
+    for _ in range(30):
+        assert o.step() == 0
+        t = o.scalars().time
+        E = 0.5 * A * math.cos(pi / 2 - sigma * t)
+        Dn = E + h
+        ex = o.get(F.EX)
+        for kk in range(2, p.Kglob + 2):
+            un = 0.5 * A * sigma * math.cosh(k * sigc[kk] * Dn) / math.sinh(k * h) * math.cos(pi / 2 - sigma * t) - sd
+            assert ex[kk, 2:p.Nglob + 2, f] == pytest.approx(Dn * un, rel=1e-12, abs=1e-15)
+
+
+def test_flux_lr_west_inflow_is_the_ramped_log_profile(oracle_mod):
+    """FLUX_LR (flux_left_right_boundary, src/nhwave.F:5566-5712): the west
+    face carries D Uin with eta = 0 and Uin = Ufric/kappa log(30 z/Zob)
+    tanh(t/TRamp), Ufric = 0.115 kappa / log(30 D/Zob); the east side stays
+    open (the volume in the domain grows by less than the volume let in)."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_flux_lr")
+    p.tol, p.itmax = 1e-10, 5000
+    o = oracle_mod.Oracle(p, d, e, u)
+    kappa, uavg = float(np.float32(0.41)), float(np.float32(0.115))
+    sigc, dsig = o.grid(6), o.grid(5)
+    D = float(o.get(F.HFX)[2, 2])         # Hfx(Ibeg, Jbeg): the inflow depth at eta = 0
+    ufric = uavg * kappa / math.log(30.0 * D / p.zob)
+    m0, inflow, t_prev = o.mass(), 0.0, 0.0
+    for _ in range(40):
+        assert o.step() == 0
+        t = o.scalars().time
+        ex = o.get(F.EX)
+        flux = 0.0
+        for kk in range(2, p.Kglob + 2):
+            uin = ufric / kappa * math.log(30.0 * sigc[kk] * D / p.zob) * math.tanh(t / p.tramp)
+            assert ex[kk, 2:p.Nglob + 2, 2] == pytest.approx(D * uin, rel=1e-12)
+            flux += dsig[kk] * D * p.dy * uin * p.Nglob
+        inflow += flux * (t - t_prev)
+        t_prev = t
+    gained = o.mass() - m0
+    assert 0.0 < gained < inflow
