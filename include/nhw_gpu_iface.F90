@@ -51,6 +51,9 @@ module nhw_gpu_iface
   integer(c_int), parameter :: NHW_WM_LEF_TID = 9
   integer(c_int), parameter :: NHW_WM_RIG_LIN = 10
   integer(c_int), parameter :: NHW_WM_FLUX_LR = 11
+  integer(c_int), parameter :: NHW_WM_LEF_JON = 12
+  integer(c_int), parameter :: NHW_WM_LEF_TMA = 13
+  integer(c_int), parameter :: NHW_WM_LEF_SPC = 14
 
   ! ------------------------------------------- enum nhw_slide, nhw_depth_type
   integer(c_int), parameter :: NHW_SLIDE_NONE = 0
@@ -177,6 +180,8 @@ module nhw_gpu_iface
      integer(c_int32_t) :: nwave, component_amp_type
      real(c_double)     :: k_center, f_center, x_breaking, t_breaking, slope_group, normalized_delta_f, depth_comp
      real(c_double)     :: sd_return
+     real(c_double)     :: hm0, tp, freq_min, freq_max
+     integer(c_int32_t) :: numfreq, wave_seed
   end type nhw_params
 
   ! ------------------------------------------------------------ nhw_scalars
@@ -272,6 +277,22 @@ module nhw_gpu_iface
        real(c_double), value :: time, dt
        integer(c_int32_t), value :: run_step
      end function nhw_set_time
+     integer(c_int) function nhw_set_wave_phases(h, n, phases) bind(C, name="nhw_set_wave_phases")
+       import :: c_int, c_int32_t, c_double, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int32_t), value :: n
+       real(c_double), intent(in) :: phases(*)
+     end function nhw_set_wave_phases
+     ! Wave_Spc2d(NumDir, NumFreq) and Random_Phs(NumDir, NumFreq) as the
+     ! reference holds them; phases may be c_null_ptr (seeded phases)
+     integer(c_int) function nhw_set_wave_spectrum(h, numfreq, numdir, freq, dire, spc2d, phases) &
+                                                   bind(C, name="nhw_set_wave_spectrum")
+       import :: c_int, c_int32_t, c_double, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int32_t), value :: numfreq, numdir
+       real(c_double), intent(in) :: freq(*), dire(*), spc2d(*)
+       type(c_ptr), value :: phases
+     end function nhw_set_wave_spectrum
 
      ! ------------------------------------------ the reference's subroutines
      integer(c_int) function nhw_estimate_dt(h) bind(C, name="nhw_estimate_dt")

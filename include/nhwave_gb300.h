@@ -17,7 +17,7 @@
  *
  *   nhw_estimate_dt        <- estimate_dt          src/nhwave.F:3694-3874
  *   nhw_update_bathymetry  <- update_bathymetry    src/nhwave.F:5755-6071 (RIGID_3D)
- *   nhw_update_wave_bc     <- update_wave_bc       src/nhwave.F:5514-5565 (LEF_LIN, LEF_SOL)
+ *   nhw_update_wave_bc     <- update_wave_bc       src/nhwave.F:5514-5565 (the generators of enum nhw_wavemaker)
  *   nhw_update_mask        <- update_mask          src/nhwave.F:5403-5456
  *   nhw_update_vars        <- update_vars          src/nhwave.F:5459-5511
  *   nhw_source_terms       <- source_terms         src/source_terms.F:1-455 (INT_LIN + bed slope)
@@ -77,10 +77,17 @@ enum nhw_precision {
  * the west side (BC_X0 = 3) and out through the east side (BC_Xn = 3) at the
  * same volume flux, with the east values radiated as in the Orlanski
  * condition (flux_left_right_boundary, src/nhwave.F:5566-5712; it uses Zob
- * and TRAMP) */
+ * and TRAMP).  LEF_JON / LEF_TMA: irregular waves through the west side
+ * (BC_X0 = 3), NUMFREQ linear components of a JONSWAP spectrum (TMA: times
+ * the finite-depth factor) of significant height HM0 and peak period TP
+ * (src/initialize.F:880-941, src/waves.F:566-623).  LEF_SPC: irregular,
+ * directional waves through the west side from a 2-D spectrum the driver
+ * passes with nhw_set_wave_spectrum (the reference reads it from spc2d.txt,
+ * src/initialize.F:782-830; src/waves.F:376-513) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
                      NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7,
-                     NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9, NHW_WM_RIG_LIN = 10, NHW_WM_FLUX_LR = 11 };
+                     NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9, NHW_WM_RIG_LIN = 10, NHW_WM_FLUX_LR = 11,
+                     NHW_WM_LEF_JON = 12, NHW_WM_LEF_TMA = 13, NHW_WM_LEF_SPC = 14 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 
@@ -168,6 +175,14 @@ typedef struct nhw_params {
   int32_t nwave, component_amp_type;
   double  k_center, f_center, x_breaking, t_breaking, slope_group, normalized_delta_f, depth_comp;
   double  sd_return;
+  /* JONSWAP / TMA spectrum of LEF_JON / LEF_TMA (src/initialize.F:880-941):
+     significant height Hm0, peak period Tp, NumFreq components at the
+     centres of NumFreq equal bands over [Freq_Min, Freq_Max] (NumFreq <= 500,
+     the reference's MaxNumFreq).  The reference draws each component's phase
+     with the compiler's rand(); here they come from wave_seed (a SplitMix64
+     stream: phase_i = 2 pi u_i) unless nhw_set_wave_phases gives them. */
+  double  hm0, tp, freq_min, freq_max;
+  int32_t numfreq, wave_seed;
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */
@@ -239,6 +254,25 @@ int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* el
 
 int nhw_get_scalars(nhw_handle* h, nhw_scalars* out);
 int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step);
+/* Phases (radians) of the n = NumFreq components of LEF_JON / LEF_TMA, in
+ * place of the ones drawn from wave_seed: the reference's RanPhs
+ * (src/initialize.F:937-940), for a driver that wants its own draw.  Call
+ * it after nhw_setup (which sets the seeded phases); they apply from the
+ * next update_wave_bc.  NHW_ERR_ARG unless the handle runs LEF_JON or
+ * LEF_TMA with n components. */
+int nhw_set_wave_phases(nhw_handle* h, int32_t n, const double* phases);
+/* The 2-D spectrum of LEF_SPC, as the reference reads it from spc2d.txt
+ * (src/initialize.F:783-830): numfreq >= 2 frequencies freq[] (Hz), numdir >= 2
+ * directions dire[] (degrees from the x axis), and the spectral densities
+ * spc2d[] and phases[] (radians) laid out as the Fortran arrays
+ * Wave_Spc2d(NumDir, NumFreq) and Random_Phs(NumDir, NumFreq), direction
+ * fastest, numfreq * numdir <= 12,000.  phases may be NULL: they are then drawn from
+ * wave_seed (the reference draws them with the compiler's rand()).  Call it
+ * after nhw_create and before the first step; the library copies the data.
+ * A checkpoint does not hold the spectrum: after nhw_load_state pass it
+ * again.  NHW_ERR_ARG unless the handle runs LEF_SPC. */
+int nhw_set_wave_spectrum(nhw_handle* h, int32_t numfreq, int32_t numdir, const double* freq,
+                          const double* dire, const double* spc2d, const double* phases);
 
 /* ------------------------------------------- the reference's subroutines */
 int nhw_estimate_dt(nhw_handle* h);

@@ -103,6 +103,17 @@ int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step) {
   return h->s->set_time(time, dt, run_step);
 }
 
+int nhw_set_wave_phases(nhw_handle* h, int32_t n, const double* phases) {
+  NHW_GUARD(h);
+  return h->s->set_wave_phases(n, phases);
+}
+
+int nhw_set_wave_spectrum(nhw_handle* h, int32_t numfreq, int32_t numdir, const double* freq,
+                          const double* dire, const double* spc2d, const double* phases) {
+  NHW_BIND(h);
+  return h->s->set_wave_spectrum(numfreq, numdir, freq, dire, spc2d, phases);
+}
+
 int nhw_estimate_dt(nhw_handle* h) { NHW_GUARD(h); return h->s->estimate_dt(); }
 int nhw_update_bathymetry(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_bathymetry(); return rc ? rc : h->s->sync(); }
 int nhw_update_wave_bc(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->update_wave_bc(); return rc ? rc : h->s->sync(); }

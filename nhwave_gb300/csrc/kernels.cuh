@@ -116,28 +116,31 @@ __global__ void __launch_bounds__(256) k_incols(Dev<T> S, Op op) {
   op(S, S.IB + t % S.M, S.JB + t / S.M);
 }
 // cells over an (nx x ny x nz) box starting at (ox, oy, oz)
+// (32-bit decode: a scenario's boxes hold fewer than 2^32 cells, which the
+// host checks at nhw_create; 64-bit division is a long software sequence)
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_box(Dev<T> S, Op op, int nx, int ny, int nz, int ox, int oy, int oz) {
   if (gated_off(S)) return;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long n = (long long)nx * ny * nz;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned n = (unsigned)nx * (unsigned)ny * (unsigned)nz;
   if (t >= n) return;
-  int i = (int)(t % nx);
-  long long r = t / nx;
-  int j = (int)(r % ny);
-  int k = (int)(r / ny);
-  op(S, ox + i, oy + j, oz + k);
+  const unsigned r = t / (unsigned)nx;
+  const int i = (int)(t - r * (unsigned)nx);
+  const unsigned k = r / (unsigned)ny;
+  const int j = (int)(r - k * (unsigned)ny);
+  op(S, ox + i, oy + j, oz + (int)k);
 }
 // all cells of the ghosted array
 template <class T, class Op>
 __global__ void __launch_bounds__(256) k_allcells(Dev<T> S, Op op) {
   if (gated_off(S)) return;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long n = (long long)S.Mloc * S.Nloc * S.Kloc;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned n = (unsigned)S.Mloc * (unsigned)S.Nloc * (unsigned)S.Kloc;
   if (t >= n) return;
-  int i = (int)(t % S.Mloc);
-  long long r = t / S.Mloc;
-  op(S, i, (int)(r % S.Nloc), (int)(r / S.Nloc));
+  const unsigned r = t / (unsigned)S.Mloc;
+  const int i = (int)(t - r * (unsigned)S.Mloc);
+  const unsigned k = r / (unsigned)S.Nloc;
+  op(S, i, (int)(r - k * (unsigned)S.Nloc), (int)k);
 }
 
 // ------------------------------------------------------------ reductions
@@ -298,6 +301,56 @@ struct OpWaveBC {
         S.Uin[j + Nl * k] = u;
         S.Win[j + Nl * k] = w;
         S.Vin[j + Nl * k] = 0.0;
+      }
+    } else if (S.lef == 12 || S.lef == 13) {   // LEF_JON / LEF_TMA (src/waves.F:566-623)
+      const int nf = S.njon;
+      const double *Wh = S.jon, *sg = S.jon + nf, *wk = S.jon + 2 * nf, *sd = S.jon + 3 * nf;
+      const double *ph = S.jon + 4 * nf, *shd = S.jon + 5 * nf;
+      double E = 0.0;
+      for (int n = 0; n < nf; ++n) E = E + 0.5 * Wh[n] * cos(kPi / 2 - sg[n] * TIME + ph[n]);
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        double u = 0.0, w = 0.0;
+        for (int n = 0; n < nf; ++n) {
+          const double arg = kPi / 2 - sg[n] * TIME + ph[n];
+          u = u + 0.5 * Wh[n] * sg[n] * cosh(wk[n] * Zlev) / shd[n] * cos(arg) - sd[n] * 1.0;
+          w = w + 0.5 * Wh[n] * sg[n] * sinh(wk[n] * Zlev) / shd[n] * sin(arg);
+        }
+        S.Uin[j + Nl * k] = u;
+        S.Win[j + Nl * k] = w;
+        S.Vin[j + Nl * k] = 0.0;
+      }
+    } else if (S.lef == 14) {   // LEF_SPC: directional components (src/waves.F:473-511)
+      const int nc = S.njon;
+      const double *Wh = S.jon, *sg = S.jon + nc, *wk = S.jon + 2 * nc, *sd = S.jon + 3 * nc;
+      const double *ph = S.jon + 4 * nc, *shd = S.jon + 5 * nc, *sth = S.jon + 6 * nc, *cth = S.jon + 7 * nc;
+      double E = 0.0;
+      for (int n = 0; n < nc; ++n) {
+        const double lag = S.yc[j] * sth[n] * wk[n] + ph[n];
+        E = E + 0.5 * Wh[n] * cos(kPi / 2 - sg[n] * TIME + lag);
+      }
+      E = E * tanh(TIME / 20.0);
+      const double Dn = E + hfx;
+      S.Ein[j] = E;
+      S.Din[j] = Dn;
+      if (!inner) return;
+      for (int k = S.KB; k <= S.KE; ++k) {
+        const double Zlev = S.sigc[k] * Dn;
+        double u = 0.0, v = 0.0, w = 0.0;
+        for (int n = 0; n < nc; ++n) {
+          const double arg = kPi / 2 - sg[n] * TIME + (S.yc[j] * sth[n] * wk[n] + ph[n]);
+          const double a = 0.5 * Wh[n] * sg[n] * cosh(wk[n] * Zlev) / shd[n] * cos(arg) - sd[n] * 1.0;
+          u = u + a * cth[n];
+          w = w + 0.5 * Wh[n] * sg[n] * sinh(wk[n] * Zlev) / shd[n] * sin(arg);
+          v = v + a * sth[n];
+        }
+        S.Uin[j + Nl * k] = u;
+        S.Win[j + Nl * k] = w;
+        S.Vin[j + Nl * k] = v;
       }
     } else if (S.lef == 6) {   // LEF_CON: cnoidal wave
       const double A = S.lef_amp, Dep = S.lef_dep, m = S.con_mod, ck = S.con_ck, L = S.con_len, Yt = S.con_ytr;
@@ -1854,32 +1907,43 @@ struct OpSponge {
 // =========================================================================
 template <class T>
 __global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long n = (long long)S.neq;
+  // One thread per water column.  D, hence sqrt(g D), is the column's, and
+  // division is monotonic in the denominator, so the smallest dx/tmp1 of a
+  // column is dx over its largest tmp1 -- the same value, bit for bit, with
+  // two divisions and one square root per column instead of per cell.  The
+  // vertical candidate dsig(k) D / max(|W|, Small) keeps one division per
+  // cell.  A candidate replaces m only if it is smaller, as the reference's
+  // `if(dxonu<tmp2) tmp2=dxonu` (src/nhwave.F:3730-3746): a NaN candidate
+  // leaves m unchanged (tmp1 = max(NaN, Small) is Small, whose quotient is
+  // never the minimum).
+  __shared__ double sh[8];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   double m = kLarge;
-  for (; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = S.IB + (int)(t % S.M);
-    const long long r = t / S.M;
-    const int j = S.JB + (int)(r % S.N), k = S.KB + (int)(r / S.N);
-    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+  if (t < S.M * S.N) {
+    const int i = S.IB + t % S.M, j = S.JB + t / S.M;
+    const long long q = i2(S, i, j);
     const double Dq = S.D[q];
-    // each candidate replaces m only if it is smaller, as the reference's
-    // `if(dxonu<tmp2) tmp2=dxonu` (src/nhwave.F:3730-3746): a NaN candidate
-    // leaves m unchanged
-    double tmp1 = fabs((double)S.U[o]) + sqrt(kGrav * Dq);
-    tmp1 = dmax_(tmp1, kSmall);
-    double x = S.dx / tmp1;
+    const double c = sqrt(kGrav * Dq);
+    double ux = kSmall, vy = kSmall;
+    for (int k = S.KB; k <= S.KE; ++k) {
+      const long long o = i3(S, i, j, k);
+      ux = dmax_(ux, dmax_(fabs((double)S.U[o]) + c, kSmall));
+      vy = dmax_(vy, dmax_(fabs((double)S.V[o]) + c, kSmall));
+      const double x = S.dsig[k] * Dq / dmax_(fabs((double)S.W[o]), kSmall);
+      if (x < m) m = x;
+    }
+    double x = S.dx / ux;
     if (x < m) m = x;
-    tmp1 = fabs((double)S.V[o]) + sqrt(kGrav * Dq);
-    tmp1 = dmax_(tmp1, kSmall);
-    x = S.dy / tmp1;
-    if (x < m) m = x;
-    tmp1 = dmax_(fabs((double)S.W[o]), kSmall);
-    x = S.dsig[k] * Dq / tmp1;
+    x = S.dy / vy;
     if (x < m) m = x;
   }
   for (int o = 16; o > 0; o >>= 1) m = dmin_(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = dmin_(m, sh[w]);
+    atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+  }
 }
 template <class T>
 __global__ void k_dt_finalize(Dev<T> S, int gated) {

@@ -26,6 +26,9 @@ int check_params(const nhw_params& p) {
   if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1) return NHW_ERR_ARG;
   if (!(p.dx > 0) || !(p.dy > 0) || !(p.cfl > 0) || !(p.dt_ini > 0)) return NHW_ERR_ARG;
   if (p.Kglob > 64) return NHW_ERR_UNSUPPORTED;
+  // the ghosted face arrays index cells with 32-bit integers (and neq, the
+  // unknowns of the Poisson system, is an int)
+  if ((long long)(p.Mglob + 5) * (p.Nglob + 5) * (p.Kglob + 5) >= (1LL << 31)) return NHW_ERR_UNSUPPORTED;
   if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
   // viscous flow with constant viscosities only (no k-epsilon / LES), free-slip bed
   if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
@@ -38,7 +41,8 @@ int check_params(const nhw_params& p) {
   if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6 && !(p.bc_xn == 3 && east_in))
     return NHW_ERR_UNSUPPORTED;
   const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ||
-                   p.wavemaker == NHW_WM_FLUX_LR;
+                   p.wavemaker == NHW_WM_FLUX_LR || p.wavemaker == NHW_WM_LEF_JON ||
+                   p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
   // west inflow (BC_X0 = 3) only with a wave or current fed through it
   if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
   if (p.wavemaker == NHW_WM_FLUX_LR && !(p.zob > 0.0)) return NHW_ERR_ARG;   // log-profile inflow
@@ -47,12 +51,13 @@ int check_params(const nhw_params& p) {
   const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
   if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_FLUX_LR) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_SPC) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
   if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && p.wavemaker != NHW_WM_FLUX_LR &&
+      p.wavemaker != NHW_WM_LEF_JON && p.wavemaker != NHW_WM_LEF_TMA && p.wavemaker != NHW_WM_LEF_SPC &&
       !(p.per_wave > 0 && p.dep_wave > 0))
     return NHW_ERR_ARG;
   // FOCUSED: at least two components (the frequency spacing divides by
@@ -61,6 +66,12 @@ int check_params(const nhw_params& p) {
       (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0) ||
        (p.component_amp_type == 1 && !(p.k_center > 0))))
     return NHW_ERR_ARG;
+  if (p.wavemaker == NHW_WM_LEF_SPC && !(p.dep_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) {   // src/initialize.F:880-941
+    if (!(p.hm0 > 0) || !(p.tp > 0) || !(p.freq_min > 0) || !(p.freq_max > p.freq_min) || p.numfreq < 1 ||
+        p.numfreq > 500 || !(p.dep_wave > 0))
+      return NHW_ERR_ARG;
+  }
   if (p.wavemaker == NHW_WM_LEF_CON) {   // the cnoidal parameter and start phase must exist
     double L = 0, Yt = 0, m = 0, Xstart = 0;
     if (!(p.amp_wave > 0) || !cnoidal_params(p.amp_wave, p.dep_wave, p.per_wave, L, Yt, m) ||
@@ -126,6 +137,108 @@ double wave_number(double Segma, double Dep) {
     Wn = Wn_new;
   }
   return Wn;
+}
+
+double wave_phase(int32_t seed, int i) {
+  // SplitMix64, element i + 1 of the stream that starts at the seed
+  uint64_t z = (uint64_t)(uint32_t)seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * 0x1.0p-53 * 2.0 * kPiH;
+}
+
+namespace {
+// JONSWAP (TMA with `tma`) spectrum at NumFreq band centres, scaled to
+// m0 = Hm0^2/16 (src/initialize.F:893-941), then the boundary routine's
+// per-component constants (src/waves.F:580-593).  The reference's boundary
+// routine calls wave_dispersion with three arguments where it takes two
+// (src/waves.F:585), so its wave number is undefined; the wave number here is
+// wave_dispersion's of each component, as the spectral routine computes it
+// (src/waves.F:395).
+void jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out) {
+  const int nf = p.numfreq;
+  const double Dep = p.dep_wave;
+  const double gam = (double)3.3f, sa = (double)0.07f, sb = (double)0.09f;
+  const double Freq_Peak = 1.0 / p.tp;
+  const double DFreq = (p.freq_max - p.freq_min) / nf;
+  std::vector<double> Freq(nf), Spc(nf);
+  for (int i = 1; i <= nf; ++i) {
+    const double F = p.freq_min + 0.5 * DFreq + (i - 1) * DFreq;
+    Freq[i - 1] = F;
+    const double Per = 1.0 / F, Segma = 2.0 * kPiH / Per;
+    const double Celerity = std::sqrt(kGravH * Dep), Wave_Length = Celerity * Per;
+    double k = 2.0 * kPiH / Wave_Length;
+    for (int it = 0;; ++it) {
+      const double th = std::tanh(k * Dep);
+      const double Fk = kGravH * k * th - Segma * Segma;
+      if (std::fabs(Fk) <= (double)1.0e-8f || it > 1000) break;
+      const double Fkdif = kGravH * k * Dep * (1.0 - th * th) + kGravH * th;
+      k = k - Fk / Fkdif;
+    }
+    const double r = Freq_Peak / F, f5 = (F * F) * (F * F) * F, s2 = F < Freq_Peak ? sa * sa : sb * sb;
+    double S = (kGravH * kGravH) / f5 * std::exp(-1.25 * ((r * r) * (r * r))) *
+               std::pow(gam, std::exp(-0.5 * ((F / Freq_Peak - 1.0) * (F / Freq_Peak - 1.0)) / s2));
+    if (tma) {
+      const double th = std::tanh(k * Dep);
+      S = S * (th * th) / (1.0 + 2 * k * Dep / std::sinh(2. * k * Dep));
+    }
+    Spc[i - 1] = S;
+  }
+  double SumInt = 0.0;
+  for (int i = 0; i < nf; ++i) SumInt = SumInt + Spc[i] * DFreq;
+  const double A_Jon = (p.hm0 * p.hm0) / 16.0 / SumInt;
+  out.assign((size_t)kJonSlots * nf, 0.0);
+  const double dfreq = (p.freq_max - p.freq_min) / (double)(float)nf;
+  for (int i = 0; i < nf; ++i) {
+    const double S = Spc[i] * A_Jon;
+    const double Per = 1.0 / Freq[i], Segma = 2.0 * kPiH / Per;
+    const double k = wave_number(Segma, Dep), Wave_Length = 2.0 * kPiH / k;
+    const double Wh = 2.0 * std::sqrt(2.0 * S * dfreq);
+    out[0 * nf + i] = Wh;
+    out[1 * nf + i] = 2.0 * kPiH * Freq[i];   // the per-step loops' Segma = 2 pi Freq
+    out[2 * nf + i] = k;
+    out[3 * nf + i] = kGravH * (Wh * Wh) / (Wave_Length / Per) / Dep / 8.0;
+    out[kJonPhase * nf + i] = wave_phase(p.wave_seed, i);
+    out[5 * nf + i] = std::sinh(k * Dep);
+    out[6 * nf + i] = 0.0;
+    out[7 * nf + i] = 1.0;
+  }
+}
+}  // namespace
+
+bool spectrum_components(const nhw_params& p, int numfreq, int numdir, const double* freq, const double* dire,
+                         const double* spc2d, const double* phases, std::vector<double>& out) {
+  if (numfreq < 2 || numdir < 2 || (long long)numfreq * numdir > 12000 || !freq || !dire || !spc2d) return false;
+  const int nc = numfreq * numdir;
+  const double Dep = p.dep_wave;
+  out.assign((size_t)kJonSlots * nc, 0.0);
+  for (int nfq = 1; nfq <= numfreq; ++nfq)
+    for (int nd = 1; nd <= numdir; ++nd) {
+      const int c = (nd - 1) + numdir * (nfq - 1);
+      const double Per = 1.0 / freq[nfq - 1], Segma = 2.0 * kPiH / Per;
+      const double k = wave_number(Segma, Dep), Wave_Length = 2.0 * kPiH / k;
+      const double Angle = dire[nd - 1] * kPiH / 180.;
+      double dfreq = nfq == 1 ? freq[1] - freq[0]
+                     : nfq == numfreq ? freq[numfreq - 1] - freq[numfreq - 2]
+                                      : 0.5 * (freq[nfq] - freq[nfq - 2]);
+      dfreq = std::fabs(dfreq);
+      double ddir = nd == 1 ? dire[1] - dire[0]
+                    : nd == numdir ? dire[numdir - 1] - dire[numdir - 2]
+                                   : 0.5 * (dire[nd] - dire[nd - 2]);
+      ddir = std::fabs(ddir);
+      const double Wh = 2.0 * std::sqrt(2.0 * spc2d[c] * dfreq * ddir);
+      if (!(Wh == Wh) || !(k > 0)) return false;
+      out[0 * nc + c] = Wh;
+      out[1 * nc + c] = 2.0 * kPiH * freq[nfq - 1];
+      out[2 * nc + c] = k;
+      out[3 * nc + c] = kGravH * (Wh * Wh) / (Wave_Length / Per) / Dep / 8.0;
+      out[kJonPhase * nc + c] = phases ? phases[c] : wave_phase(p.wave_seed, c);
+      out[5 * nc + c] = std::sinh(k * Dep);
+      out[6 * nc + c] = std::sin(Angle);
+      out[7 * nc + c] = std::cos(Angle);
+    }
+  return true;
 }
 
 int host_setup(const nhw_params& p, const double* depth, const double* eta0, const double* uvw0,
@@ -377,6 +490,8 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
       h.foc[nw + n - 1] = xxk;
       h.foc[2 * nw + n - 1] = fi;
     }
+  } else if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) {
+    jonswap_components(p, p.wavemaker == NHW_WM_LEF_TMA, h.jon);
   } else if (p.wavemaker == NHW_WM_LEF_CON) {   // src/waves.F:100-140
     const double A = p.amp_wave, Dep = p.dep_wave;
     double L = 0, Yt = 0, m = 0, Xstart = 0;

@@ -25,6 +25,10 @@ struct HostInit {
   double lef_e2 = 0, lef_u2 = 0;                          // LEF_STK second-order amplitudes
   double con_mod = 0, con_len = 0, con_ytr = 0, con_ck = 0, con_x0 = 0;   // LEF_CON
   std::vector<double> foc;   // FOCUSED: Amp_i [nwave], k_i [nwave], f_i [nwave]
+  // LEF_JON / LEF_TMA components, slot-major [8][NumFreq]: wave height Wh,
+  // angular frequency 2 pi f, wave number, Stokes drift, phase, sinh(k h),
+  // sin and cos of the direction (0 and 1 here; LEF_SPC fills them)
+  std::vector<double> jon;
 };
 
 // Validate parameters against the path's scope; NHW_OK or an error code.
@@ -34,5 +38,14 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
                HostInit& out);
 // Wave number of linear dispersion by Newton iteration (src/waves.F:61-91).
 double wave_number(double segma, double dep);
+// Phase i (radians, [0, 2 pi)) of the irregular boundary waves' stream `seed`.
+double wave_phase(int32_t seed, int i);
+constexpr int kJonSlots = 8;   // Wh, sigma, k, Stokes drift, phase, sinh(k h), sin(theta), cos(theta)
+constexpr int kJonPhase = 4;
+// LEF_SPC components from a 2-D spectrum (src/waves.F:388-465), slot-major
+// [8][numfreq * numdir], component (nfreq, ndir) at ndir + numdir * nfreq;
+// phases == nullptr: the stream of p.wave_seed.  False on a bad spectrum.
+bool spectrum_components(const nhw_params& p, int numfreq, int numdir, const double* freq, const double* dire,
+                         const double* spc2d, const double* phases, std::vector<double>& out);
 
 }  // namespace nhw

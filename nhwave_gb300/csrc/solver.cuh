@@ -41,6 +41,9 @@ class SolverBase {
   virtual int estimate_dt() = 0;
   virtual int update_bathymetry() = 0;
   virtual int update_wave_bc() = 0;
+  virtual int set_wave_phases(int n, const double* phases) = 0;
+  virtual int set_wave_spectrum(int nf, int nd, const double* freq, const double* dire, const double* spc,
+                                const double* phases) = 0;
   virtual int update_mask() = 0;
   virtual int update_vars() = 0;
   virtual int source_terms() = 0;
@@ -187,6 +190,7 @@ class Solver final : public SolverBase {
     if (ev_run0) cudaEventDestroy(ev_run0);
     if (ev_run1) cudaEventDestroy(ev_run1);
     if (arena) cudaFree(arena);
+    if (spc_table) cudaFree(spc_table);
     if (h_sc) cudaFreeHost(h_sc);
     if (h_out) cudaFreeHost(h_out);
     if (ev_fork) cudaEventDestroy(ev_fork);
@@ -276,6 +280,8 @@ class Solver final : public SolverBase {
     S.nwave = p.wavemaker == NHW_WM_FOCUSED ? p.nwave : 0;
     S.foc_xb = p.x_breaking; S.foc_tb = p.t_breaking; S.foc_dc = p.depth_comp; S.foc_sd = p.sd_return;
     if (S.nwave) add((double**)&S.foc, sizeof(double) * 3 * S.nwave);
+    S.njon = (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) ? p.numfreq : 0;
+    if (S.njon) add((double**)&S.jon, sizeof(double) * kJonSlots * S.njon);
     for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds, &S.lv_fint})
       add((double**)lv, sizeof(double) * S.Kloc);
     add((T**)&S.lvT, sizeof(T) * 3 * S.Kloc);
@@ -632,7 +638,7 @@ class Solver final : public SolverBase {
     return NHW_OK;
   }
   void ens_prefix() {   // estimate_dt (gated), bathymetry, mask, update_vars
-    L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+    L("dt_min", [&] { k_dt_min<T><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S); });
     L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, 1); });
     if (S.slide) update_bathymetry();
     update_wave_bc();
@@ -670,7 +676,10 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ? p.wavemaker : 0;
+    S.lef = ((p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) || S.njon ||
+             p.wavemaker == NHW_WM_LEF_SPC) ? p.wavemaker : 0;
+    if (S.njon && !h.jon.empty())   // LEF_JON / LEF_TMA (LEF_SPC's table comes from nhw_set_wave_spectrum)
+      NHW_CU(cudaMemcpyAsync((void*)S.jon, h.jon.data(), sizeof(double) * h.jon.size(), cudaMemcpyHostToDevice, st));
     S.east = p.bc_xn == 3 ? p.wavemaker : 0;   // RIG_LIN or FLUX_LR (check_params)
     if (S.lef == NHW_WM_FOCUSED)
       NHW_CU(cudaMemcpyAsync((void*)S.foc, h.foc.data(), sizeof(double) * h.foc.size(), cudaMemcpyHostToDevice, st));
@@ -780,7 +789,7 @@ class Solver final : public SolverBase {
 
   // -------------------------------------------------- reference subroutines
   int estimate_dt() override {
-    L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+    L("dt_min", [&] { k_dt_min<T><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S); });
     L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, 0); });
     int rc = pull_scalars();
     if (rc) return rc;
@@ -794,8 +803,48 @@ class Solver final : public SolverBase {
     box(OpSlideC{}, S.Mloc + 1, S.Nloc + 1, 1, 0, 0, 0);
     return check();
   }
+  // LEF_SPC: the spectrum's components in a device table of their own
+  // (spc2d.txt's data is an input of the run, like the depth, not state)
+  double* spc_table = nullptr;
+  int set_wave_spectrum(int nf, int nd, const double* freq, const double* dire, const double* spc,
+                        const double* phases) override {
+    if (p.wavemaker != NHW_WM_LEF_SPC) {
+      set_last_error("nhw_set_wave_spectrum: the handle does not run LEF_SPC");
+      return NHW_ERR_ARG;
+    }
+    std::vector<double> tab;
+    if (!spectrum_components(p, nf, nd, freq, dire, spc, phases, tab)) {
+      set_last_error("nhw_set_wave_spectrum: needs 2 <= numfreq, 2 <= numdir, numfreq * numdir <= 12000 and a "
+                     "finite, non-negative spectrum");
+      return NHW_ERR_ARG;
+    }
+    NHW_CU(cudaStreamSynchronize(st));
+    if (spc_table) cudaFree(spc_table);
+    spc_table = nullptr;
+    NHW_CU(cudaMalloc((void**)&spc_table, sizeof(double) * tab.size()));
+    NHW_CU(cudaMemcpy(spc_table, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+    S.jon = spc_table;
+    S.njon = nf * nd;
+    drop_step_graphs();   // captured kernels hold the table's address and size
+    return NHW_OK;
+  }
+  // the reference's RanPhs given by the driver (LEF_JON / LEF_TMA)
+  int set_wave_phases(int n, const double* phases) override {
+    if (!S.njon || n != S.njon || !phases || p.wavemaker == NHW_WM_LEF_SPC) {
+      set_last_error("nhw_set_wave_phases: the handle runs no LEF_JON / LEF_TMA wave of this many components");
+      return NHW_ERR_ARG;
+    }
+    NHW_CU(cudaMemcpyAsync((void*)(S.jon + kJonPhase * S.njon), phases, sizeof(double) * n,
+                           cudaMemcpyHostToDevice, st));
+    NHW_CU(cudaStreamSynchronize(st));
+    return NHW_OK;
+  }
   int update_wave_bc() override {
     if (!S.lef && !S.east) return NHW_OK;
+    if (S.lef == NHW_WM_LEF_SPC && !S.njon) {
+      set_last_error("LEF_SPC: no spectrum yet (nhw_set_wave_spectrum)");
+      return NHW_ERR_STATE;
+    }
     if (S.lef) box(OpWaveBC{}, 1, S.Nloc, 1, 0, 0, 0);
     if (S.east == NHW_WM_RIG_LIN) box(OpWaveBCEast{}, 1, S.Nloc, 1, 0, 0, 0);
     if (S.east == NHW_WM_FLUX_LR) L("flux_lr", [&] { k_flux_lr<T><<<1, 256, 0, st>>>(S); });
@@ -1252,7 +1301,7 @@ class Solver final : public SolverBase {
     S.h_go = use_persistent ? 0 : new_handle();
     if (cap_ok(cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
                "step capture")) {
-      L("dt_min", [&] { k_dt_min<T><<<std::min<unsigned>(cdiv(S.neq, 256), 4096), 256, 0, st>>>(S); });
+      L("dt_min", [&] { k_dt_min<T><<<cdiv((long long)S.M * S.N, 256), 256, 0, st>>>(S); });
       L("dt_finalize", [&] { k_dt_finalize<T><<<1, 1, 0, st>>>(S, gated); });
       if (use_persistent)
         step_body();   // every kernel checks sc->step_go; no loops left on the host side

@@ -117,6 +117,10 @@ struct Dev {
   // point and time, depth_comp, sd_return
   const double* foc;
   int nwave;
+  // LEF_JON / LEF_TMA: [6][njon] components (Wh, 2 pi f, k, Stokes drift,
+  // phase, sinh(k h)), host-computed
+  const double* jon;
+  int njon;
   double foc_xb, foc_tb, foc_dc, foc_sd;
   double *Ein, *Din;               // [Nloc] Ein_X0, Din_X0
   double *Uin, *Vin, *Win;         // [Kloc][Nloc] Uin_X0 .. (index j + Nloc*k)

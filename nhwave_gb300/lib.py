@@ -27,7 +27,7 @@ OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_DT_MIN, ERR_KRYLOV_NOCONV
 # every entry point declared in include/nhwave_gb300.h
 EXPORTS = [
     "nhw_create", "nhw_destroy", "nhw_setup", "nhw_get_field", "nhw_set_field", "nhw_field_shape",
-    "nhw_get_scalars", "nhw_set_time", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc",
+    "nhw_get_scalars", "nhw_set_time", "nhw_set_wave_phases", "nhw_set_wave_spectrum", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc",
     "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
     "nhw_step", "nhw_run", "nhw_mass", "nhw_statistics", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
@@ -91,6 +91,8 @@ def load(path: str | None = None):
     L.nhw_field_shape.argtypes = [vp, i32, P(i32 * 3), P(i32)]
     L.nhw_get_scalars.argtypes = [vp, P(NhwScalars)]
     L.nhw_set_time.argtypes = [vp, dbl, dbl, i32]
+    L.nhw_set_wave_phases.argtypes = [vp, i32, vp]
+    L.nhw_set_wave_spectrum.argtypes = [vp, i32, i32, vp, vp, vp, vp]
     for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc", "nhw_update_mask", "nhw_update_vars",
               "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_synchronize"):
         getattr(L, n).argtypes = [vp]
@@ -273,6 +275,19 @@ class Scenario:
 
     def set_time(self, time: float, dt: float, run_step: int):
         _chk(load().nhw_set_time(self._h, time, dt, run_step), "nhw_set_time")
+
+    def set_wave_spectrum(self, freq, dire, spc2d, phases=None):
+        """LEF_SPC's 2-D spectrum (nhw_set_wave_spectrum): spc2d and phases flat,
+        direction fastest, as read_spc2d returns them."""
+        f, d, s = (np.ascontiguousarray(a, dtype=np.float64) for a in (freq, dire, spc2d))
+        ph = None if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
+        _chk(load().nhw_set_wave_spectrum(self._h, f.size, d.size, _ptr(f), _ptr(d), _ptr(s), _ptr(ph)),
+             "nhw_set_wave_spectrum")
+
+    def set_wave_phases(self, phases):
+        """Phases (radians) of the LEF_JON / LEF_TMA components (nhw_set_wave_phases)."""
+        a = np.ascontiguousarray(phases, dtype=np.float64)
+        _chk(load().nhw_set_wave_phases(self._h, a.size, _ptr(a)), "nhw_set_wave_phases")
 
     def get(self, field: int, out: np.ndarray | None = None) -> np.ndarray:
         """Whole ghosted field as a [k][j][i] array (into ``out`` when given: a

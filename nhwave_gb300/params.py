@@ -14,9 +14,10 @@ import ctypes
 NHW_FP64 = 0
 NHW_FP32_IR = 1
 (WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED,
- WM_LEF_TID, WM_RIG_LIN, WM_FLUX_LR) = range(12)
+ WM_LEF_TID, WM_RIG_LIN, WM_FLUX_LR, WM_LEF_JON, WM_LEF_TMA, WM_LEF_SPC) = range(15)
 # fed through the west boundary (BC_X0 = 3)
-WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID, WM_FLUX_LR)
+WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID, WM_FLUX_LR,
+          WM_LEF_JON, WM_LEF_TMA, WM_LEF_SPC)
 # fed through the east boundary (BC_Xn = 3)
 WM_EAST = (WM_RIG_LIN, WM_FLUX_LR)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
@@ -75,6 +76,8 @@ class NhwParams(ctypes.Structure):
         ("t_breaking", ctypes.c_double), ("slope_group", ctypes.c_double),
         ("normalized_delta_f", ctypes.c_double), ("depth_comp", ctypes.c_double),
         ("sd_return", ctypes.c_double),
+        ("hm0", ctypes.c_double), ("tp", ctypes.c_double), ("freq_min", ctypes.c_double),
+        ("freq_max", ctypes.c_double), ("numfreq", ctypes.c_int32), ("wave_seed", ctypes.c_int32),
     ]
 
     def copy(self) -> "NhwParams":
@@ -196,10 +199,11 @@ def read_input(path: str) -> NhwParams:
     p.depth_type = DEPTH_CELL_GRID if dt_ == "CELL_GRID" else DEPTH_CELL_CENTER
     wm = s("WAVEMAKER", "NONE").upper()
     # a generator of the reference that this path does not build (LEF_SPC,
-    # LEF_JON, INT_IRR, ...) is kept as WM_OTHER and rejected, not run as NONE
+    # INT_IRR, ...) is kept as WM_OTHER and rejected, not run as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
              "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR,
-             "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID, "RIG_LIN": WM_RIG_LIN, "FLUX_LR": WM_FLUX_LR}
+             "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID, "RIG_LIN": WM_RIG_LIN, "FLUX_LR": WM_FLUX_LR,
+             "LEF_JON": WM_LEF_JON, "LEF_TMA": WM_LEF_TMA, "LEF_SPC": WM_LEF_SPC}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
@@ -208,6 +212,9 @@ def read_input(path: str) -> NhwParams:
         if wm[:3] == "INT":
             p.xsource_west, p.xsource_east = f("Xsource_West", 0.0), f("Xsource_East", 0.0)
             p.ysource_suth, p.ysource_nrth = f("Ysource_Suth", 0.0), f("Ysource_Nrth", 0.0)
+    if wm[4:7] in ("JON", "TMA"):   # WaveMaker(5:7), src/initialize.F:888-892
+        p.hm0, p.tp = f("Hm0", 0.0), f("Tp", 0.0)
+        p.freq_min, p.freq_max, p.numfreq = f("Freq_Min", 0.0), f("Freq_Max", 0.0), i("NumFreq", 0)
     if wm[:3] == "FOC":   # src/initialize.F:709-719
         p.nwave, p.component_amp_type = i("nwave", 0), i("Component_Amp_Type", 1)
         p.k_center, p.f_center = f("k_center", 0.0), f("f_center", 0.0)
@@ -237,6 +244,22 @@ def read_input(path: str) -> NhwParams:
     return p
 
 
+def read_spc2d(path: str):
+    """The 2-D spectrum file of LEF_SPC (src/initialize.F:783-819): NumFreq
+    and NumDir, then NumFreq frequencies, NumDir directions and the
+    NumFreq x NumDir densities, direction fastest.  Returns (freq, dire,
+    spc2d) as float64 arrays, spc2d flat in that order (as nhw_set_wave_spectrum
+    takes it)."""
+    import numpy as np
+    with open(path) as fh:
+        vals = fh.read().split()
+    nf, nd = int(float(vals[0])), int(float(vals[1]))
+    rest = np.array([float(v) for v in vals[2:2 + nf + nd + nf * nd]])
+    if rest.size != nf + nd + nf * nd:
+        raise ValueError(f"{path}: expected {nf} + {nd} + {nf * nd} values after the counts")
+    return rest[:nf].copy(), rest[nf:nf + nd].copy(), rest[nf + nd:].copy()
+
+
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
     if p.viscous_flow and (p.ivturb != 1 or p.ihturb != 1):
@@ -245,10 +268,11 @@ def unsupported_reason(p: NhwParams) -> str | None:
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF + WM_EAST:
-        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR, "
-                "FOCUSED, RIG_LIN and FLUX_LR are on the GPU path)")
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, "
+                "LEF_TMA, LEF_SPC, WAV_CUR, FOCUSED, RIG_LIN and FLUX_LR are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
-        return "BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, WAV_CUR, FOCUSED or FLUX_LR wavemaker"
+        return ("BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, LEF_TMA, LEF_SPC, WAV_CUR, "
+                "FOCUSED or FLUX_LR wavemaker")
     if p.bc_xn == 3 and p.wavemaker not in WM_EAST:
         return "BC_Xn=3 needs the RIG_LIN or FLUX_LR wavemaker"
     for name in ("bc_x0", "bc_xn", "bc_y0", "bc_yn"):
@@ -273,7 +297,7 @@ __all__ = [
     "NhwParams", "NhwScalars", "default_params", "read_input", "unsupported_reason", "cells",
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
     "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF_TID", "WM_LEF",
-    "WM_RIG_LIN", "WM_FLUX_LR", "WM_EAST",
+    "WM_RIG_LIN", "WM_FLUX_LR", "WM_LEF_JON", "WM_LEF_TMA", "WM_LEF_SPC", "WM_EAST", "read_spc2d",
     "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",

@@ -97,6 +97,10 @@ def landslide_beach(M=512, N=512, K=10, dx=2.0, **kw):
     p.slope_angle = math.degrees(math.atan(1.0 / 15.0))
     p.slide_angle = 180.0                            # moving towards deep water (-x)
     p.slide_x0, p.slide_y0 = 0.6 * L, 0.5 * N * dx
+    # the Froude cap of the reference's own landslide benchmark input (10);
+    # with 100, the thin layers of the runup reach several hundred m/s and
+    # dt falls below 2 ms about 44 s into the run
+    p.froude_cap = 10.0
     for k, v in kw.items():
         setattr(p, k, v)
     xs = _xc(p) * (1024.0 / L)
@@ -152,19 +156,44 @@ def wave_flume(kind: str = "LIN", M=256, N=4, K=10, dx=0.05, dy=0.05, depth=0.5,
     (WAV_CUR, `cur_wave`, `tramp`) or a focused group (FOCUSED, `nwave` ...);
     sponge layer and wall at the east end,
     walls along the sides; at rest initially."""
-    from .params import WM_FOCUSED, WM_LEF_CON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_TID, WM_WAV_CUR
+    from .params import (WM_FOCUSED, WM_LEF_CON, WM_LEF_JON, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_SPC, WM_LEF_STK,
+                         WM_LEF_TID, WM_LEF_TMA, WM_WAV_CUR)
     p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
                        dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
                        tol=1e-8, itmax=1000, total_time=20.0)
     p.bc_x0 = 3
     p.wavemaker = {"LIN": WM_LEF_LIN, "SOL": WM_LEF_SOL, "STK": WM_LEF_STK, "CON": WM_LEF_CON,
-                   "CUR": WM_WAV_CUR, "FOC": WM_FOCUSED, "TID": WM_LEF_TID}[kind]
+                   "CUR": WM_WAV_CUR, "FOC": WM_FOCUSED, "TID": WM_LEF_TID, "JON": WM_LEF_JON, "TMA": WM_LEF_TMA,
+                   "SPC": WM_LEF_SPC}[kind]
     p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
     p.sponge_on = 1
     p.sponge_east_width = sponge
     for k, v in kw.items():
         setattr(p, k, v)
     return p, np.full(M * N, depth), None, None
+
+
+# ------------------------------------------------------ 2-D spectrum
+def spc_spectrum(nf: int = 8, nd: int = 3, hm0: float = 0.03, fp: float = 0.7, spread_deg: float = 20.0):
+    """A 2-D spectrum for LEF_SPC in spc2d.txt's order (freq [nf], dire [nd],
+    densities flat with direction fastest): a JONSWAP-shaped frequency
+    spectrum over 0.5-1.2 Hz times a cos^2 spreading over +-spread_deg,
+    scaled so that sum S df dtheta = hm0^2/16 with the reference's
+    centred band widths."""
+    freq = np.linspace(0.5, 1.2, nf)
+    dire = np.linspace(-spread_deg, spread_deg, nd)
+    sf = freq ** -5 * np.exp(-1.25 * (fp / freq) ** 4) * 3.3 ** np.exp(-0.5 * ((freq / fp - 1) / 0.08) ** 2)
+    sd = np.cos(np.radians(dire) * 90.0 / (spread_deg * 1.5)) ** 2
+    spc = np.outer(sf, sd)                 # [nf][nd]: direction fastest when flattened
+
+    def widths(a):
+        w = np.empty_like(a)
+        w[0], w[-1] = a[1] - a[0], a[-1] - a[-2]
+        w[1:-1] = 0.5 * (a[2:] - a[:-2])
+        return np.abs(w)
+    m0 = float((spc * np.outer(widths(freq), widths(dire))).sum())
+    spc *= hm0 ** 2 / 16.0 / m0
+    return freq, dire, spc.ravel()
 
 
 # ------------------------------------------------------- east inflows
@@ -268,6 +297,14 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
     elif name == "tiny_open":
         # solitary wave whose front already touches an open (Orlanski, BC_Xn = 6) east side
         out = solitary_channel(M=48, N=4, K=5, x0=3.0, amp=0.1, bc_xn=6, **kw)
+    elif name in ("tiny_flume_jon", "tiny_flume_tma"):
+        # irregular waves of a JONSWAP (TMA) spectrum, Hm0 3 cm, Tp 1.5 s, 24 components over 0.4-1.2 Hz
+        kw = dict(dict(hm0=0.03, tp=1.5, freq_min=0.4, freq_max=1.2, numfreq=24, wave_seed=11), **kw)
+        out = wave_flume(name[-3:].upper(), M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
+    elif name == "tiny_flume_spc":
+        # directional irregular waves from a 2-D spectrum (LEF_SPC; the spectrum itself is
+        # scenarios.spc_spectrum(), passed with set_wave_spectrum); 8 cross-channel rows
+        out = wave_flume("SPC", M=64, N=8, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
     elif name == "tiny_flume_rig":
         # a linear wave given to the east side (RIG_LIN through BC_Xn = 3), wall and sponge at the west
         out = east_flume("RIG", **kw)

@@ -242,9 +242,15 @@ struct Model {
     if (p.bc_xn != 1 && p.bc_xn != 2 && p.bc_xn != 5 && p.bc_xn != 6 && !(p.bc_xn == 3 && east_in))
       return NHW_ERR_UNSUPPORTED;
     const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ||
-                     p.wavemaker == NHW_WM_FLUX_LR;
+                     p.wavemaker == NHW_WM_FLUX_LR || p.wavemaker == NHW_WM_LEF_JON ||
+                     p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
+    if ((p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) &&
+        (!(p.hm0 > 0) || !(p.tp > 0) || !(p.freq_min > 0) || !(p.freq_max > p.freq_min) || p.numfreq < 1 ||
+         p.numfreq > 500 || !(p.dep_wave > 0)))
+      return NHW_ERR_ARG;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.wavemaker == NHW_WM_FLUX_LR && !(p.zob > 0.0)) return NHW_ERR_ARG;
+    if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) jonswap_spectrum();
     if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
       if (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0)) return NHW_ERR_ARG;
       const int nw = p.nwave;
@@ -681,6 +687,181 @@ struct Model {
   // FOCUSED wave group components (src/initialize.F:742-781)
   std::vector<double> Amp_i, k_i, f_i;
 
+  // JONSWAP / TMA spectrum (src/initialize.F:880-941): Freq(i) at the centres
+  // of NumFreq bands over [Freq_Min, Freq_Max], Jon_Spc(i) scaled to
+  // m0 = Hm0^2/16, and the phases RanPhs(i).  The reference draws RanPhs with
+  // the compiler's rand(); here they are element i + 1 of a SplitMix64
+  // stream from WAVE_SEED, times 2 pi, unless set_wave_phases gives them.
+  std::vector<double> Freq, Jon_Spc, RanPhs;
+  static double phase_of(int32_t seed, int i) {
+    uint64_t z = (uint64_t)(uint32_t)seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53 * 2.0 * pi;
+  }
+  void jonswap_spectrum() {
+    const int NumFreq = p.numfreq;
+    const double Dep_Wave = p.dep_wave;
+    const double gam = (double)3.3f, sa = (double)0.07f, sb = (double)0.09f;
+    const double Freq_Peak = 1.0 / p.tp;
+    const double DFreq = (p.freq_max - p.freq_min) / NumFreq;
+    Freq.assign(NumFreq, 0.0); Jon_Spc.assign(NumFreq, 0.0); RanPhs.assign(NumFreq, 0.0);
+    for (int i = 1; i <= NumFreq; ++i) {
+      Freq[i - 1] = p.freq_min + 0.5 * DFreq + (i - 1) * DFreq;
+      const double Per_Wave = 1.0 / Freq[i - 1];
+      const double Segma = 2.0 * pi / Per_Wave;
+      const double Celerity = std::sqrt(Grav * Dep_Wave);
+      const double Wave_Length = Celerity * Per_Wave;
+      double Wave_Number = 2.0 * pi / Wave_Length;
+      int Iter = 0;
+      while (true) {
+        const double Fk = Grav * Wave_Number * std::tanh(Wave_Number * Dep_Wave) - Segma * Segma;
+        if (std::fabs(Fk) <= (double)1.0e-8f || Iter > 1000) break;
+        const double th = std::tanh(Wave_Number * Dep_Wave);
+        const double Fkdif = Grav * Wave_Number * Dep_Wave * (1.0 - th * th) + Grav * std::tanh(Wave_Number * Dep_Wave);
+        Wave_Number = Wave_Number - Fk / Fkdif;
+        Iter = Iter + 1;
+      }
+      const double F = Freq[i - 1], r = Freq_Peak / F;
+      const double s2 = F < Freq_Peak ? sa * sa : sb * sb;
+      Jon_Spc[i - 1] = (Grav * Grav) / ((F * F) * (F * F) * F) * std::exp(-1.25 * ((r * r) * (r * r))) *
+                       std::pow(gam, std::exp(-0.5 * ((F / Freq_Peak - 1.0) * (F / Freq_Peak - 1.0)) / s2));
+      if (p.wavemaker == NHW_WM_LEF_TMA) {
+        const double th = std::tanh(Wave_Number * Dep_Wave);
+        Jon_Spc[i - 1] = Jon_Spc[i - 1] * (th * th) /
+                         (1.0 + 2 * Wave_Number * Dep_Wave / std::sinh(2. * Wave_Number * Dep_Wave));
+      }
+    }
+    double SumInt = Zero;
+    for (int i = 0; i < NumFreq; ++i) SumInt = SumInt + Jon_Spc[i] * DFreq;
+    const double A_Jon = (p.hm0 * p.hm0) / 16.0 / SumInt;
+    for (int i = 0; i < NumFreq; ++i) {
+      Jon_Spc[i] = Jon_Spc[i] * A_Jon;
+      RanPhs[i] = phase_of(p.wave_seed, i);
+    }
+  }
+
+  // LEF_SPC's spectrum (src/initialize.F:783-830): Freq, Dire, Wave_Spc2d
+  // and Random_Phs as (ndir, nfreq) arrays, direction fastest
+  int NumFreq_s = 0, NumDir_s = 0;
+  std::vector<double> Freq_s, Dire_s, Spc2d, Random_Phs;
+
+  // random_wave_left_boundary (src/waves.F:376-513).  The angle adjustment
+  // for periodic lateral sides is skipped by the reference's `goto 100`
+  // (:398), so the direction is Dire itself.
+  void random_left_boundary() {
+    const int NumFreq = NumFreq_s, NumDir = NumDir_s;
+    const double Dep_Wave = p.dep_wave;
+    std::vector<double> Wtheta(NumFreq * NumDir), Wh(NumFreq * NumDir), Stokes_Drift(NumFreq * NumDir),
+        Wnum(NumFreq * NumDir);
+    auto at = [&](int nd, int nfq) { return (nd - 1) + NumDir * (nfq - 1); };
+    for (int nfq = 1; nfq <= NumFreq; ++nfq)
+      for (int nd = 1; nd <= NumDir; ++nd) {
+        const double Per_Wave = 1.0 / Freq_s[nfq - 1];
+        const double Segma = 2.0 * pi / Per_Wave;
+        const double Wave_Number = wave_dispersion(Segma);
+        const double Wave_Length = 2.0 * pi / Wave_Number;
+        const double Angle = Dire_s[nd - 1] * pi / 180.;
+        Wtheta[at(nd, nfq)] = Angle;
+        double dfreq;
+        if (nfq == 1) dfreq = Freq_s[1] - Freq_s[0];
+        else if (nfq == NumFreq) dfreq = Freq_s[NumFreq - 1] - Freq_s[NumFreq - 2];
+        else dfreq = 0.5 * (Freq_s[nfq] - Freq_s[nfq - 2]);
+        dfreq = std::fabs(dfreq);
+        double ddir;
+        if (nd == 1) ddir = Dire_s[1] - Dire_s[0];
+        else if (nd == NumDir) ddir = Dire_s[NumDir - 1] - Dire_s[NumDir - 2];
+        else ddir = 0.5 * (Dire_s[nd] - Dire_s[nd - 2]);
+        ddir = std::fabs(ddir);
+        Wnum[at(nd, nfq)] = Wave_Number;
+        Wh[at(nd, nfq)] = 2.0 * std::sqrt(2.0 * Spc2d[at(nd, nfq)] * dfreq * ddir);
+        Stokes_Drift[at(nd, nfq)] =
+            Grav * (Wh[at(nd, nfq)] * Wh[at(nd, nfq)]) / (Wave_Length / Per_Wave) / Dep_Wave / 8.0;
+      }
+    const double Fact = 1.0;
+    for (int j = 1; j <= Nloc; ++j) {
+      Ein_X0(j) = 0.0;
+      for (int nfq = 1; nfq <= NumFreq; ++nfq)
+        for (int nd = 1; nd <= NumDir; ++nd) {
+          const int c = at(nd, nfq);
+          const double Segma = 2.0 * pi * Freq_s[nfq - 1];
+          const double Phs_Lag = yc(j) * std::sin(Wtheta[c]) * Wnum[c] + Random_Phs[c];
+          Ein_X0(j) = Ein_X0(j) + 0.5 * Wh[c] * std::cos(pi / 2 - Segma * TIME + Phs_Lag);
+        }
+      Ein_X0(j) = Ein_X0(j) * std::tanh(TIME / 20.0);
+      Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+    }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Zlev = sigc(k) * Din_X0(j);
+        Uin_X0(j, k) = 0.0;
+        Win_X0(j, k) = 0.0;
+        Vin_X0(j, k) = 0.0;
+        for (int nfq = 1; nfq <= NumFreq; ++nfq)
+          for (int nd = 1; nd <= NumDir; ++nd) {
+            const int c = at(nd, nfq);
+            const double Segma = 2.0 * pi * Freq_s[nfq - 1];
+            const double Phs_Lag = yc(j) * std::sin(Wtheta[c]) * Wnum[c] + Random_Phs[c];
+            const double sh = std::sinh(Wnum[c] * Dep_Wave);
+            const double arg = pi / 2 - Segma * TIME + Phs_Lag;
+            Uin_X0(j, k) = Uin_X0(j, k) +
+                           (0.5 * Wh[c] * Segma * std::cosh(Wnum[c] * Zlev) / sh * std::cos(arg) - Stokes_Drift[c] * Fact) *
+                               std::cos(Wtheta[c]);
+            Win_X0(j, k) = Win_X0(j, k) + 0.5 * Wh[c] * Segma * std::sinh(Wnum[c] * Zlev) / sh * std::sin(arg);
+            Vin_X0(j, k) = Vin_X0(j, k) +
+                           (0.5 * Wh[c] * Segma * std::cosh(Wnum[c] * Zlev) / sh * std::cos(arg) - Stokes_Drift[c] * Fact) *
+                               std::sin(Wtheta[c]);
+          }
+      }
+  }
+
+  // jonswap_wave_left_boundary (src/waves.F:566-623).  The reference calls
+  // wave_dispersion with three arguments where it takes two (src/waves.F:585),
+  // which leaves its Wave_Number undefined; each component's wave number here
+  // is wave_dispersion's, as random_wave_left_boundary computes it (:395).
+  void jonswap_left_boundary() {
+    const int NumFreq = p.numfreq;
+    const double Dep_Wave = p.dep_wave;
+    std::vector<double> Wh(NumFreq), Wnum(NumFreq), Stokes_Drift(NumFreq);
+    const double dfreq = (p.freq_max - p.freq_min) / (double)(float)NumFreq;
+    for (int n = 0; n < NumFreq; ++n) {
+      const double Per_Wave = 1.0 / Freq[n];
+      const double Segma = 2.0 * pi / Per_Wave;
+      const double Wave_Number = wave_dispersion(Segma);
+      const double Wave_Length = 2.0 * pi / Wave_Number;
+      Wh[n] = 2.0 * std::sqrt(2.0 * Jon_Spc[n] * dfreq);
+      Wnum[n] = Wave_Number;
+      Stokes_Drift[n] = Grav * (Wh[n] * Wh[n]) / (Wave_Length / Per_Wave) / Dep_Wave / 8.0;
+    }
+    const double Fact = 1.0;
+    for (int j = 1; j <= Nloc; ++j) {
+      Ein_X0(j) = 0.0;
+      for (int n = 0; n < NumFreq; ++n) {
+        const double Segma = 2.0 * pi * Freq[n];
+        Ein_X0(j) = Ein_X0(j) + 0.5 * Wh[n] * std::cos(pi / 2 - Segma * TIME + RanPhs[n]);
+      }
+      Din_X0(j) = Ein_X0(j) + Hfx(Ibeg, j);
+    }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Zlev = sigc(k) * Din_X0(j);
+        Uin_X0(j, k) = 0.0;
+        Win_X0(j, k) = 0.0;
+        Vin_X0(j, k) = 0.0;
+        for (int n = 0; n < NumFreq; ++n) {
+          const double Segma = 2.0 * pi * Freq[n];
+          const double sh = std::sinh(Wnum[n] * Dep_Wave);
+          Uin_X0(j, k) = Uin_X0(j, k) +
+                         0.5 * Wh[n] * Segma * std::cosh(Wnum[n] * Zlev) / sh * std::cos(pi / 2 - Segma * TIME + RanPhs[n]) -
+                         Stokes_Drift[n] * Fact;
+          Win_X0(j, k) = Win_X0(j, k) +
+                         0.5 * Wh[n] * Segma * std::sinh(Wnum[n] * Zlev) / sh * std::sin(pi / 2 - Segma * TIME + RanPhs[n]);
+          Vin_X0(j, k) = 0.0;
+        }
+      }
+  }
+
   // Start phase of the cnoidal boundary wave (src/waves.F:106-130):
   // bisection on [0, 1] for the zero crossing of the elevation.
   bool cnoidal_start(double Ytrough, double Mod1, double& Xstart) {
@@ -871,6 +1052,8 @@ struct Model {
           Vin_X0(j, k) = 0.0;
         }
     }
+    if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) jonswap_left_boundary();
+    if (p.wavemaker == NHW_WM_LEF_SPC && NumFreq_s > 0) random_left_boundary();
     if (p.wavemaker == NHW_WM_RIG_LIN) right_boundary_linear();
     if (p.wavemaker == NHW_WM_FLUX_LR) flux_left_right();
   }
@@ -2538,6 +2721,33 @@ void orc_get_scalars(void* o, nhw_scalars* s) {
 void orc_set_time(void* o, double time, double dt, int run_step) {
   Model* m = static_cast<Model*>(o);
   m->TIME = time; m->dt = dt; m->RUN_STEP = run_step;
+}
+// the LEF_JON / LEF_TMA phases RanPhs (n = NumFreq), as nhw_set_wave_phases
+int orc_set_wave_phases(void* o, int n, const double* phases) {
+  Model* m = static_cast<Model*>(o);
+  if (n != (int)m->RanPhs.size() || n == 0 || !phases) return NHW_ERR_ARG;
+  for (int i = 0; i < n; ++i) m->RanPhs[i] = phases[i];
+  return NHW_OK;
+}
+// LEF_SPC's spectrum, as nhw_set_wave_spectrum takes it
+int orc_set_wave_spectrum(void* o, int nf, int nd, const double* freq, const double* dire, const double* spc,
+                          const double* phases) {
+  Model* m = static_cast<Model*>(o);
+  if (m->p.wavemaker != NHW_WM_LEF_SPC || nf < 2 || nd < 2 || !freq || !dire || !spc) return NHW_ERR_ARG;
+  m->NumFreq_s = nf;
+  m->NumDir_s = nd;
+  m->Freq_s.assign(freq, freq + nf);
+  m->Dire_s.assign(dire, dire + nd);
+  m->Spc2d.assign(spc, spc + nf * nd);
+  m->Random_Phs.assign(nf * nd, 0.0);
+  for (int c = 0; c < nf * nd; ++c) m->Random_Phs[c] = phases ? phases[c] : Model::phase_of(m->p.wave_seed, c);
+  return NHW_OK;
+}
+// the west-boundary elevation Ein_X0 (Nloc values) of the last update_wave_bc
+int orc_get_inflow_eta(void* o, double* out) {
+  Model* m = static_cast<Model*>(o);
+  std::memcpy(out, m->Ein_X0.v.data(), m->Ein_X0.v.size() * sizeof(double));
+  return (int)m->Ein_X0.v.size();
 }
 // grid vectors for tests: which = 0 x, 1 xc, 2 y, 3 yc, 4 sig, 5 dsig, 6 sigc
 int orc_get_grid(void* o, int which, double* out) {

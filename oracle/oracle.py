@@ -77,6 +77,9 @@ def lib():
         L.orc_wave_number.restype = dbl
         L.orc_elliptic.argtypes = [i32, dbl, dbl]
         L.orc_elliptic.restype = dbl
+        L.orc_set_wave_phases.argtypes = [vp, i32, vp]
+        L.orc_set_wave_spectrum.argtypes = [vp, i32, i32, vp, vp, vp, vp]
+        L.orc_get_inflow_eta.argtypes = [vp, vp]
         L.orc_cnoidal_wave.argtypes = [dbl, dbl, dbl, vp]
         L.orc_cnoidal_wave.restype = i32
         _lib = L
@@ -172,6 +175,25 @@ class Oracle:
 
     def set_time(self, time, dt, run_step):
         lib().orc_set_time(self._h, time, dt, run_step)
+
+    def set_wave_phases(self, phases):
+        a = np.ascontiguousarray(phases, dtype=np.float64)
+        rc = lib().orc_set_wave_phases(self._h, a.size, _ptr(a))
+        if rc:
+            raise ValueError("set_wave_phases: not a LEF_JON / LEF_TMA scenario of that many components")
+
+    def set_wave_spectrum(self, freq, dire, spc2d, phases=None):
+        f, d, s = (np.ascontiguousarray(a, dtype=np.float64) for a in (freq, dire, spc2d))
+        self._spc = (f, d, s, None if phases is None else np.ascontiguousarray(phases, dtype=np.float64))
+        rc = lib().orc_set_wave_spectrum(self._h, f.size, d.size, _ptr(f), _ptr(d), _ptr(s), _ptr(self._spc[3]))
+        if rc:
+            raise ValueError("set_wave_spectrum: not a LEF_SPC scenario, or fewer than 2 frequencies / directions")
+
+    def inflow_eta(self) -> np.ndarray:
+        """Ein_X0 of the last update_wave_bc (all Nloc rows)."""
+        out = np.empty(self.shape.Nloc)
+        lib().orc_get_inflow_eta(self._h, _ptr(out))
+        return out
 
     def get(self, field: int) -> np.ndarray:
         shp, dtype = self.shape.of(field)

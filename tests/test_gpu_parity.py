@@ -242,7 +242,7 @@ def test_golden_fixtures(name, gpu_lib):
 # tiny_flume_rig / tiny_flux_lr: the east side open to RIG_LIN and to the
 # FLUX_LR current (BC_Xn = 3)
 FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open", "tiny_flume_cur",
-          "tiny_flume_foc", "tiny_flume_tid", "tiny_flume_rig", "tiny_flux_lr",
+          "tiny_flume_foc", "tiny_flume_tid", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon", "tiny_flume_tma",
           "tiny_fric_log"]   # and the friction law from a roughness height: log() of CUDA and libm
 
 
@@ -326,4 +326,59 @@ def test_statistics_like_the_oracle(name, precision, oracle_mod, gpu_lib):
         # absolute floor: in the nearly 2-D submerged bar |V| is roundoff (~1e-19)
         assert abs(a[key] - b[key]) <= lim * abs(b[key]) + 1e-14, f"{name} {key}: {a[key]!r} vs {b[key]!r}"
     assert a["mass_volume"] == pytest.approx(g.mass(), rel=1e-13)
+    g.close()
+
+
+def test_wave_phases_given_by_the_driver(oracle_mod, gpu_lib):
+    """nhw_set_wave_phases: the driver's own phases for the LEF_JON components
+    (the reference's RanPhs) replace the seeded ones; GPU and oracle, given the
+    same phases, step alike, and differently from the seeded run."""
+    from nhwave_gb300 import fields as F
+    g, o = _pair("tiny_flume_jon", oracle_mod)
+    g2, _ = _pair("tiny_flume_jon", oracle_mod)
+    ph = np.random.default_rng(3).uniform(0.0, 2.0 * np.pi, g.params.numfreq)
+    g.set_wave_phases(ph)
+    o.set_wave_phases(ph)
+    for _ in range(10):
+        assert g.step() == 0 and o.step() == 0 and g2.step() == 0
+    sl = o.shape.interior(F.ETA)
+    assert rel_l2(g.get(F.ETA)[sl], o.get(F.ETA)[sl]) < 1e-9
+    assert rel_l2(g2.get(F.ETA)[sl], o.get(F.ETA)[sl]) > 1e-3
+    from nhwave_gb300 import lib
+    with pytest.raises(lib.NhwError):
+        g.set_wave_phases(ph[:-1])
+    g.close()
+    g2.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_spectral_inflow_steps(precision, oracle_mod, gpu_lib):
+    """LEF_SPC: directional irregular waves from a 2-D spectrum passed with
+    nhw_set_wave_spectrum (seeded phases on both sides); FP64 within 1e-9 of
+    the oracle (cos/cosh/tanh of CUDA and libm), FP32+IR eta within 1e-6.
+    Before a spectrum is given, update_wave_bc refuses to run."""
+    from nhwave_gb300 import fields as F, lib, scenarios as S
+    g, o = _pair("tiny_flume_spc", oracle_mod, precision=precision, tol=STEP_TOL if precision == 0 else 1e-10)
+    with pytest.raises(lib.NhwError):
+        g.update_wave_bc()
+    freq, dire, spc = S.spc_spectrum()
+    g.set_wave_spectrum(freq, dire, spc)
+    o.set_wave_spectrum(freq, dire, spc)
+    for n in range(20):
+        assert g.step() == 0 and o.step() == 0
+        assert np.array_equal(g.get(F.MASK), o.get(F.MASK)), f"mask differs after step {n}"
+    sl = o.shape.interior
+    if precision == 0:
+        for f in ("ETA", "P"):
+            fid = getattr(F, f)
+            r = rel_l2(g.get(fid)[sl(fid)], o.get(fid)[sl(fid)])
+            assert r < 1e-9, f"LEF_SPC {f}: rel L2 {r:.3e}"
+        for f in ("U", "V", "W"):
+            r = vel_err(g, o, f)
+            assert r < 1e-9, f"LEF_SPC {f}: {r:.3e}"
+    else:
+        r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
+        assert r < 1e-6, f"LEF_SPC FP32+IR eta rel L2 {r:.3e}"
+    # directional: the cross-channel velocity is not zero
+    assert np.abs(o.get(F.V)[sl(F.V)]).max() > 1e-5
     g.close()

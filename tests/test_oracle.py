@@ -557,3 +557,66 @@ def test_flux_lr_west_inflow_is_the_ramped_log_profile(oracle_mod):
         t_prev = t
     gained = o.mass() - m0
     assert 0.0 < gained < inflow
+
+
+@pytest.mark.parametrize("name", ["tiny_flume_jon", "tiny_flume_tma"])
+def test_jonswap_boundary_elevation_has_the_spectrum_variance(name, oracle_mod):
+    """LEF_JON / LEF_TMA (src/initialize.F:880-941, src/waves.F:566-623): the
+    spectrum is scaled to m0 = Hm0^2/16, and each component's amplitude is
+    Wh/2 with Wh = 2 sqrt(2 S df), so the boundary elevation's variance over a
+    long record is sum S df = Hm0^2/16 (the components' frequencies are
+    distinct, so their cross terms average out)."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make(name)
+    o = oracle_mod.Oracle(p, d, e, u)
+    rec = []
+    for n in range(6000):                   # 600 s at 0.1 s
+        o.set_time(0.1 * n, 0.1, n)
+        o.update_wave_bc()
+        rec.append(o.inflow_eta()[3])
+    rec = np.array(rec)
+    assert abs(rec.mean()) < 0.02 * rec.std()
+    assert rec.var() == pytest.approx(p.hm0 ** 2 / 16.0, rel=0.03)
+    # the phases follow the seed: another seed gives another record with the same variance
+    q = p.copy()
+    q.wave_seed = p.wave_seed + 1
+    o2 = oracle_mod.Oracle(q, d, e, u)
+    o2.set_time(12.3, 0.1, 1)
+    o2.update_wave_bc()
+    o.set_time(12.3, 0.1, 1)
+    o.update_wave_bc()
+    assert o2.inflow_eta()[3] != o.inflow_eta()[3]
+
+
+def test_spectral_inflow_follows_the_component_sum(oracle_mod):
+    """LEF_SPC (random_wave_left_boundary, src/waves.F:376-513): the boundary
+    elevation of row j is tanh(t/20) sum 0.5 Wh cos(pi/2 - 2 pi f t + yc_j
+    sin(theta) k + phase), Wh = 2 sqrt(2 S df dtheta) with the centred band
+    widths, k from the dispersion relation -- restated here in numpy."""
+    from nhwave_gb300 import scenarios as S
+    p, d, e, u = S.make("tiny_flume_spc")
+    o = oracle_mod.Oracle(p, d, e, u)
+    freq, dire, spc = S.spc_spectrum()
+    ph = np.random.default_rng(9).uniform(0.0, 2.0 * np.pi, spc.size)
+    o.set_wave_spectrum(freq, dire, spc, ph)
+    pi = _pi_sp()
+
+    def widths(a):
+        w = np.empty_like(a)
+        w[0], w[-1] = a[1] - a[0], a[-1] - a[-2]
+        w[1:-1] = 0.5 * (a[2:] - a[:-2])
+        return np.abs(w)
+    nd = dire.size
+    kw = np.array([oracle_mod.lib().orc_wave_number(o._h, 2.0 * pi / (1.0 / f)) for f in freq])
+    wh = 2.0 * np.sqrt(2.0 * spc.reshape(freq.size, nd) * np.outer(widths(freq), widths(dire)))
+    th = dire * pi / 180.0
+    yc = o.grid(3)
+    for t in (3.0, 17.5, 41.25):
+        o.set_time(t, 0.1, 1)
+        o.update_wave_bc()
+        got = o.inflow_eta()
+        for j in (2, 5, 9):
+            lag = yc[j] * np.sin(th)[None, :] * kw[:, None] + ph.reshape(freq.size, nd)
+            want = math.tanh(t / 20.0) * float(
+                (0.5 * wh * np.cos(pi / 2 - (2.0 * pi * freq)[:, None] * t + lag)).sum())
+            assert got[j] == pytest.approx(want, rel=1e-11, abs=1e-14)

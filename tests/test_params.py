@@ -82,11 +82,11 @@ def test_out_of_scope_reason(tmp_path):
     p = P.read_input(str(f))
     assert p.bc_z0 == 5 and P.unsupported_reason(p) is None
     # a generator of the reference that the path does not build is rejected, not run as NONE
-    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_JON"))
+    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = INT_IRR"))
     p = P.read_input(str(f))
     assert p.wavemaker == P.WM_OTHER and "WAVEMAKER" in P.unsupported_reason(p)
-    # the cnoidal and Stokes boundary waves are on the path, through BC_X0 = 3
-    for name, wm in (("LEF_CON", P.WM_LEF_CON), ("LEF_STK", P.WM_LEF_STK)):
+    # the cnoidal, Stokes and JONSWAP boundary waves are on the path, through BC_X0 = 3
+    for name, wm in (("LEF_CON", P.WM_LEF_CON), ("LEF_STK", P.WM_LEF_STK), ("LEF_JON", P.WM_LEF_JON)):
         f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = " + name))
         p = P.read_input(str(f))
         assert p.wavemaker == wm
@@ -166,3 +166,18 @@ depth_comp = 0.6
     assert p.wavemaker == P.WM_FOCUSED and p.nwave == 12 and p.component_amp_type == 1
     assert (p.k_center, p.f_center, p.x_breaking, p.t_breaking) == (4.0, 1.1, 6.0, 9.0)
     assert (p.slope_group, p.normalized_delta_f, p.depth_comp) == (0.3, 0.75, 0.6)
+
+
+def test_reader_takes_the_jonswap_keys(tmp_path):
+    """Hm0, Tp, Freq_Min, Freq_Max and NumFreq reach nhw_params for LEF_JON /
+    LEF_TMA (src/initialize.F:888-892); FLUX_LR and RIG_LIN are read as such."""
+    from nhwave_gb300 import params as P
+    f = tmp_path / "input.txt"
+    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = LEF_TMA") +
+                 "\nHm0 = 0.05\nTp = 2.0\nFreq_Min = 0.2\nFreq_Max = 1.5\nNumFreq = 60\n")
+    p = P.read_input(str(f))
+    assert p.wavemaker == P.WM_LEF_TMA
+    assert (p.hm0, p.tp, p.freq_min, p.freq_max, p.numfreq) == (0.05, 2.0, 0.2, 1.5, 60)
+    for name, wm in (("FLUX_LR", P.WM_FLUX_LR), ("RIG_LIN", P.WM_RIG_LIN)):
+        f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = " + name))
+        assert P.read_input(str(f)).wavemaker == wm
