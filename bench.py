@@ -260,12 +260,18 @@ def copy_ceiling(nbytes: int, device: int = 0) -> float:
     return 2.0 * n * 4 / secs / 1e9
 
 
-def roofline(prof, cells, elem_bytes):
+def roofline(prof, cells, elem_bytes, bulk_us=None):
+    """The dominant kernel against the measured HBM peak.  `bulk_us`: its
+    launch time from nhw_time_smoother (launches timed in bulk in a CUDA graph,
+    the L2 evicted before each V-cycle's four); the per-launch event time of
+    the profile pass, which carries the events' own cost, is kept beside it."""
     kern = prof["kernels"]
     total = sum(v[1] for v in kern.values())
     cand = {k: v for k, v in kern.items() if k in ALG_BYTES_PER_CELL}
     name, (launches, tot_ms) = max(cand.items(), key=lambda kv: kv[1][1])
-    avg_s = tot_ms / launches / 1000.0
+    event_s = tot_ms / launches / 1000.0
+    bulk = bulk_us is not None and name == "mg_smooth_l0"
+    avg_s = bulk_us * 1e-6 if bulk else event_s
     alg = ALG_BYTES_PER_CELL[name](elem_bytes) * cells
     achieved = alg / avg_s / 1e9
     peak, peak_kind = load_peaks()
@@ -275,6 +281,10 @@ def roofline(prof, cells, elem_bytes):
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": traffic, "alg_bytes_per_launch": alg, "avg_launch_us": round(avg_s * 1e6, 2),
+            "timing": ("CUDA events around a graph of 50 rounds of the V-cycle's four level-0 half-sweeps, "
+                       "L2 evicted (256 MB write) before each round, writes timed alone and subtracted"
+                       if bulk else "CUDA events around each launch of the profile pass"),
+            "event_us_per_single_launch": round(event_s * 1e6, 2),
             "launches": launches, "kernel_time_shares": shares}
 
 
@@ -401,8 +411,9 @@ def run_c3(local, steps=10, warmup=3):
         if prec == NHW_FP32_IR:
             g.profile(True)
             g.run_timed(3)
-            out[name]["roofline"] = roofline(g.profile_report(), cells, 4)
+            prof = g.profile_report()
             g.profile(False)
+            out[name]["roofline"] = roofline(prof, cells, 4, g.time_smoother(reps=20, flush_bytes=256 << 20))
         g.close()
     a, b = ends["fp32ir"], ends["fp64"]
     sl = (slice(2, -2), slice(2, -2))
@@ -518,10 +529,11 @@ def run_gpu_arm(args):
     g.run_timed(max(1, min(args.steps, 5)))
     prof = g.profile_report()
     g.profile(False)
+    smooth_us = g.time_smoother(reps=50, flush_bytes=256 << 20)
     g.close()
     if args.quick:
         if rank == 0:
-            rl = roofline(prof, cells, 4)
+            rl = roofline(prof, cells, 4, smooth_us)
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                               "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
                               "quick": True, "roofline": rl, "clocks": clocks,
@@ -576,7 +588,7 @@ def run_gpu_arm(args):
 
     line = None
     if rank == 0:
-        rl = roofline(prof, cells, 4)
+        rl = roofline(prof, cells, 4, smooth_us)
         cc = copy_ceiling(rl["alg_bytes_per_launch"], local)
         rl["copy_same_bytes_gbs"] = round(cc, 1)
         rl["frac_of_copy_same_bytes"] = round(rl["achieved"] / cc, 4)

@@ -400,6 +400,13 @@ module nhw_gpu_iface
        character(kind=c_char), intent(out) :: buf(*)
        integer(c_int32_t), value :: buflen
      end function nhw_profile_report
+     integer(c_int) function nhw_time_smoother(h, reps, flush_bytes, us_per_launch) bind(C, name="nhw_time_smoother")
+       import :: c_int, c_int32_t, c_int64_t, c_double, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int32_t), value :: reps
+       integer(c_int64_t), value :: flush_bytes
+       real(c_double), intent(out) :: us_per_launch
+     end function nhw_time_smoother
      integer(c_int) function nhw_abi_sizes(params_bytes, scalars_bytes) bind(C, name="nhw_abi_sizes")
        import :: c_int, c_int32_t
        integer(c_int32_t), intent(out) :: params_bytes, scalars_bytes

@@ -343,6 +343,16 @@ int nhw_run_timed(nhw_handle* h, int32_t nsteps, double* device_ms);
 int nhw_profile(nhw_handle* h, int32_t on);
 int nhw_profile_report(nhw_handle* h, char* buf, int32_t buflen);
 
+/* Device microseconds of one level-0 multigrid half-sweep, the largest
+ * kernel of a non-hydrostatic step, on this handle's current operator (call
+ * it after a step).  Events around single launches add several microseconds
+ * to each, so the launches are timed in bulk: a CUDA graph of `reps` rounds,
+ * each a write of `flush_bytes` bytes (0: none; more than the 129 MB L2
+ * evicts it) followed by the four level-0 half-sweeps of a V-cycle, minus a
+ * graph of the writes alone.  Overwrites a preconditioner scratch vector,
+ * no state.  NHW_ERR_STATE for a hydrostatic handle or one not set up. */
+int nhw_time_smoother(nhw_handle* h, int32_t reps, int64_t flush_bytes, double* us_per_launch);
+
 /* sizeof(nhw_params) and sizeof(nhw_scalars) as compiled into the library,
  * for bindings to check their struct images (no GPU needed). */
 int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes);

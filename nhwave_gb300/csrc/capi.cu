@@ -259,6 +259,11 @@ int nhw_profile_report(nhw_handle* h, char* buf, int32_t buflen) {
   NHW_BIND(h);
   return h->s->profile_report(buf, buflen);
 }
+int nhw_time_smoother(nhw_handle* h, int32_t reps, int64_t flush_bytes, double* us_per_launch) {
+  NHW_GUARD(h);
+  if (!us_per_launch) return NHW_ERR_ARG;
+  return h->s->time_smoother(reps, (long long)flush_bytes, us_per_launch);
+}
 
 int nhw_abi_sizes(int32_t* params_bytes, int32_t* scalars_bytes) {
   if (!params_bytes || !scalars_bytes) return NHW_ERR_ARG;

@@ -305,9 +305,145 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
 // 32 consecutive columns of the colour in that layout, so its loads of C13,
 // the line factors and the cross terms are contiguous; in the natural layout
 // every other column of a row belongs to the other colour and half of each
-// sector read would be the other colour's.  Otherwise as k_mg_smooth_blk.
+// sector read would be the other colour's.
+//
+// FP32 form.  Each thread of a column forms the right-hand sides of
+// kSplitLevels consecutive levels (then the next chunk, blockDim.y chunks on): x of the
+// four neighbouring columns at the chunk's levels and one above and below is
+// loaded once into registers and serves the in-level and cross couplings of
+// every level of the chunk, and all of a chunk's loads issue before the first
+// is used.  One warp then runs the Thomas sweeps in shared memory.  (C2 level
+// 0, FP32, graph of 400 half-sweeps: 7.6 us per launch with levels strided
+// over 7 threads per column, 5.6 us with 4 consecutive levels on each of 5.)
+// The right-hand sides are summed in the order of off_column_c /
+// off_column_pc, so the result is the strided kernel's, bit for bit.
+constexpr int kSplitLevels = 4;      // levels per thread (a chunk)
+constexpr int kSplitRegs = 56;       // no spills; 7 blocks of 32 x 5 threads fit an SM
+constexpr int kSplitMaxThreads = 1024;   // 56 registers x 1024 threads fit the 64K register file
 template <class T, bool kProlong, class In>
-__global__ void __launch_bounds__(1024, 2) k_mg_smooth_split(MGL<T> L, const DevScal* sc, int color, int zero_x,
+__global__ void __maxnreg__(kSplitRegs)
+k_mg_smooth_split(MGL<T> L, const DevScal* sc, int color, int zero_x, Prolong<T> P, In in) {
+  static_assert(sizeof(T) == 4, "the FP64 form takes k_mg_smooth_split_strided");
+  if (sc->conv) return;
+  constexpr int LPT = kSplitLevels;
+  extern __shared__ unsigned char smem_raw[];
+  T* sh = reinterpret_cast<T*>(smem_raw);
+  const int K = L.K, M = L.M, MN = L.M * L.N;
+  T* s_rhs = sh;
+  T* s_a = sh + K * 32;
+  T* s_inv = sh + 2 * K * 32;
+  T* s_cp = sh + 3 * K * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int Mh = (M + 1) >> 1, nmh = Mh * L.N;
+  const int q = blockIdx.x * 32 + tx;
+  const int jj = q / Mh, r = q - jj * Mh, ii = 2 * r + ((color + jj) & 1);
+  const bool valid = jj < L.N && ii < M;
+  const int col = ii + M * jj;
+  const size_t cs = (size_t)K * nmh;
+  const T* sp = L.sp + (size_t)color * cs + q;
+  const bool im = ii > 0, ip = ii < M - 1, jm = jj > 0, jp = jj < L.N - 1;
+  const T* __restrict__ x = L.x;
+  // level 0 couples the columns in a level by the constants cxx, cyy (cxr,
+  // cyr are null there; only coarse levels carry per-cell couplings)
+  const T cxx = L.cxx, cyy = L.cyy;
+  typename Prolong<T>::Stencil sxp{}, sxm{}, syp{}, sym{};
+  if (kProlong && valid && !zero_x) {
+    if (ip) sxp = P.stencil(ii + 1, jj);
+    if (im) sxm = P.stencil(ii - 1, jj);
+    if (jp) syp = P.stencil(ii, jj + 1);
+    if (jm) sym = P.stencil(ii, jj - 1);
+  }
+  for (int k0 = ty * LPT; valid && k0 < K; k0 += blockDim.y * LPT) {
+    // neighbour x at levels k0 - 1 .. k0 + LPT (slot t holds level k0 - 1 + t)
+    T xp[LPT + 2], xm[LPT + 2], yp[LPT + 2], ym[LPT + 2];
+#pragma unroll
+    for (int t = 0; t < LPT + 2; ++t) {
+      const int k = k0 - 1 + t;
+      const bool in_k = !zero_x && k >= 0 && k < K;
+      const int ic = col + MN * k;
+      if (kProlong) {
+        xp[t] = in_k && ip ? P.at(x, ic + 1, sxp, k) : (T)0;
+        xm[t] = in_k && im ? P.at(x, ic - 1, sxm, k) : (T)0;
+        yp[t] = in_k && jp ? P.at(x, ic + M, syp, k) : (T)0;
+        ym[t] = in_k && jm ? P.at(x, ic - M, sym, k) : (T)0;
+      } else {
+        xp[t] = in_k && ip ? x[ic + 1] : (T)0;
+        xm[t] = in_k && im ? x[ic - 1] : (T)0;
+        yp[t] = in_k && jp ? x[ic + M] : (T)0;
+        ym[t] = in_k && jm ? x[ic - M] : (T)0;
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < LPT; ++t) {
+      const int k = k0 + t;
+      if (k < K) {
+        const int ic = col + MN * k;
+        const T* e = sp + (size_t)nmh * k;
+        const T a = e[0], inv = e[2 * cs], cp = e[4 * cs];
+        T off = (T)0;
+        if (!zero_x) {
+          const T c4 = e[6 * cs], c5 = e[8 * cs], c7 = e[10 * cs], c8 = e[12 * cs];
+          const bool km = k > 0, kp = k < K - 1;
+          T s = (T)0;
+          if (kProlong) {   // column by column, as off_column_pc
+            if (ip) { s += cxx * xp[t + 1]; if (kp) s += c7 * xp[t + 2]; if (km) s -= c7 * xp[t]; }
+            if (im) { s += cxx * xm[t + 1]; if (kp) s += c5 * xm[t + 2]; if (km) s -= c5 * xm[t]; }
+            if (jp) { s += cyy * yp[t + 1]; if (kp) s += c8 * yp[t + 2]; if (km) s -= c8 * yp[t]; }
+            if (jm) { s += cyy * ym[t + 1]; if (kp) s += c4 * ym[t + 2]; if (km) s -= c4 * ym[t]; }
+          } else {          // in-level, then the level above, then below, as off_column_c
+            if (ip) s += cxx * xp[t + 1];
+            if (im) s += cxx * xm[t + 1];
+            if (jp) s += cyy * yp[t + 1];
+            if (jm) s += cyy * ym[t + 1];
+            if (kp) {
+              if (ip) s += c7 * xp[t + 2];
+              if (im) s += c5 * xm[t + 2];
+              if (jp) s += c8 * yp[t + 2];
+              if (jm) s += c4 * ym[t + 2];
+            }
+            if (km) {
+              if (ip) s -= c7 * xp[t];
+              if (im) s -= c5 * xm[t];
+              if (jp) s -= c8 * yp[t];
+              if (jm) s -= c4 * ym[t];
+            }
+          }
+          off = s;
+        }
+        s_rhs[k * 32 + tx] = in(sc, ic, ii, jj, k) - off;
+        s_a[k * 32 + tx] = a;
+        s_inv[k * 32 + tx] = inv;
+        s_cp[k * 32 + tx] = cp;
+      }
+    }
+  }
+  __syncthreads();
+  if (ty != 0 || !valid) return;
+  // the Thomas sweeps, unrolled so that the shared-memory loads of several
+  // levels issue ahead of the dependent chain
+  T prev = (T)0;
+#pragma unroll 4
+  for (int k = 0; k < K; ++k) {
+    prev = (s_rhs[k * 32 + tx] - s_a[k * 32 + tx] * prev) * s_inv[k * 32 + tx];
+    s_rhs[k * 32 + tx] = prev;
+  }
+  T z = prev;
+  L.x[col + MN * (K - 1)] = z;
+#pragma unroll 4
+  for (int k = K - 2; k >= 0; --k) {
+    z = s_rhs[k * 32 + tx] - s_cp[k * 32 + tx] * z;
+    L.x[col + MN * k] = z;
+  }
+}
+
+// The same half-sweep for the FP64 form: each thread of a column forms the
+// right-hand sides of the levels ty, ty + blockDim.y, ... (no register
+// window: its doubles would take twice the registers, and with them fewer
+// blocks fit an SM; C2 level 0, graph of 400 half-sweeps: 25.1 us per launch
+// against 27.7-33.8 us for windows of 2-7 levels).  Otherwise as
+// k_mg_smooth_blk.
+template <class T, bool kProlong, class In>
+__global__ void __launch_bounds__(1024, 2) k_mg_smooth_split_strided(MGL<T> L, const DevScal* sc, int color, int zero_x,
                                                           Prolong<T> P, In in) {
   if (sc->conv) return;
   extern __shared__ unsigned char smem_raw[];

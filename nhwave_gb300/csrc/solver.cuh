@@ -62,6 +62,7 @@ class SolverBase {
   virtual int run(int nsteps, int* done) = 0;
   virtual int profile(int on) = 0;
   virtual int profile_report(char* buf, int len) = 0;
+  virtual int time_smoother(int reps, long long flush, double* us) = 0;
   virtual int checkpoint_bytes(size_t* bytes) = 0;
   virtual int save_state(void* host, size_t bytes) = 0;
   virtual int load_state(const void* host, size_t bytes) = 0;
@@ -426,11 +427,19 @@ class Solver final : public SolverBase {
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
-      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, true, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
-      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
-      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
-      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
-      NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      if constexpr (kFP32) {
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, true, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      } else {
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split_strided<T, true, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split_strided<T, false, MgB<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split_strided<T, false, MgInP<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split_strided<T, false, MgInS<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        NHW_CU(cudaFuncSetAttribute(k_mg_smooth_split_strided<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      }
       NHW_CU(cudaFuncSetAttribute(k_mg_smooth_blk<T, false, MgInV<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
     }
     NHW_CU(cudaFuncSetAttribute(k_mg_cta_cycle<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -478,7 +487,15 @@ class Solver final : public SolverBase {
   int pull_scalars() {
     NHW_CU(cudaMemcpyAsync(h_sc, S.sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
     NHW_CU(cudaStreamSynchronize(st));
+    prof_hold();
     return NHW_OK;
+  }
+  // With the per-kernel profiler on, every host round trip leaves the stream
+  // empty, and the launches that follow would reach the GPU at the host's
+  // launch rate (a few microseconds each, events included): hold the stream
+  // for 3 ms while the host enqueues them.  The hold is not a profiled launch.
+  void prof_hold() {
+    if (prof_on) k_hold<<<1, 1, 0, st>>>(3000000ull);
   }
   int sync() override {
     NHW_CU(cudaStreamSynchronize(st));
@@ -986,7 +1003,8 @@ class Solver final : public SolverBase {
         rc = pull_scalars();
         if (rc) return rc;
         if (h_sc->conv != 0) break;
-        if (chunk < 16) chunk *= 2;
+        // (profiling: chunks of 4, about 200 launches, which one hold covers)
+        if (chunk < 16 && !prof_on) chunk *= 2;
       }
       inner_finish();
       L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
@@ -1070,15 +1088,25 @@ class Solver final : public SolverBase {
     L(names[level < 7 ? level : 7], [&] {
       if (Lv.sp) {   // level 0: colour-split operator
         const long long nq = (long long)((Lv.M + 1) / 2) * Lv.N;
-        // blocks of at most 8 threads per column, each loading ceil(K/8)
-        // levels: several times more blocks resident per SM, so a half-sweep
-        // of C2 runs in one wave with 9 Thomas warps per SM instead of 2.25
-        // waves with 3 (13.0 against 16.3 us per launch, FP32+IR)
-        const int lpt = (Lv.K + 7) / 8, by = std::min((Lv.K + lpt - 1) / lpt, 32);
-        if (P.xc)
-          k_mg_smooth_split<T, true, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
-        else
-          k_mg_smooth_split<T, false, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
+        if constexpr (kFP32) {
+          // one thread per column and chunk of kSplitLevels levels: short
+          // blocks, 7 resident per SM, so that a half-sweep of C2 runs in
+          // one wave (with 20 threads per column it took 2.25 waves)
+          const int by = std::min((Lv.K + kSplitLevels - 1) / kSplitLevels, kSplitMaxThreads / 32);
+          if (P.xc)
+            k_mg_smooth_split<T, true, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
+          else
+            k_mg_smooth_split<T, false, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
+        } else {
+          // at most 8 threads per column, each loading ceil(K/8) levels
+          const int lpt = (Lv.K + 7) / 8, by = std::min((Lv.K + lpt - 1) / lpt, 32);
+          if (P.xc)
+            k_mg_smooth_split_strided<T, true, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x,
+                                                                                         P, in);
+          else
+            k_mg_smooth_split_strided<T, false, In><<<cdiv(nq, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x,
+                                                                                          P, in);
+        }
       } else if (P.xc)
         k_mg_smooth_blk<T, true, In><<<cdiv(nthr, 32), dim3(32, by), shm, st>>>(Lv, S.sc, color, zero_x, P, in);
       else
@@ -1211,6 +1239,7 @@ class Solver final : public SolverBase {
     return rc ? rc : worst;
   }
   int step_eager() {
+    prof_hold();
     int rc = estimate_dt();
     if (rc) return rc;
     return step_body();
@@ -1454,6 +1483,72 @@ class Solver final : public SolverBase {
     if (on) { recs.clear(); evused = 0; }
     prof_on = on != 0;
     return NHW_OK;
+  }
+  // Device time of one level-0 half-sweep, the largest kernel of a step.
+  // Events around single launches add several microseconds to each, so the
+  // launches are timed in bulk: a CUDA graph of `reps` rounds, each a write
+  // of `flush` bytes (evicting the L2) and then the four level-0 half-sweeps
+  // of a V-cycle in their order (colour 0 from x = 0, colour 1, colour 1,
+  // colour 0), against a graph of the writes alone.  b is the Krylov residual
+  // and x a preconditioner scratch vector: no state is written.
+  int time_smoother(int reps, long long flush, double* us) override {
+    if (!ready || !S.non_hydro || !use_mg || mg.empty() || !mg[0].sp) return NHW_ERR_STATE;
+    if (reps < 1 || flush < 0) return NHW_ERR_ARG;
+    NHW_CU(cudaStreamSynchronize(st));
+    if (!ev_run0) { NHW_CU(cudaEventCreate(&ev_run0)); NHW_CU(cudaEventCreate(&ev_run1)); }
+    int32_t conv = 0;
+    NHW_CU(cudaMemcpy(&conv, &S.sc->conv, sizeof(conv), cudaMemcpyDeviceToHost));
+    void* fb = nullptr;
+    if (flush > 0) NHW_CU(cudaMalloc(&fb, (size_t)flush));
+    // from here on every path restores conv and frees the buffer
+    int rc = cu(cudaMemset(&S.sc->conv, 0, sizeof(conv)));
+    MGL<T> L0 = mg[0];
+    L0.b = S.kr;
+    L0.x = S.kph;
+    const Prolong<T> none{nullptr, (T)0, 1, 1, 1, 1, 1, 1};
+    const bool was = prof_on;
+    prof_on = false;
+    const long long launches0 = launches;
+    float ms[2] = {0.f, 0.f};
+    for (int pass = 0; pass < 2 && rc == NHW_OK; ++pass) {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      rc = cu(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      if (rc) break;
+      for (int r = 0; r < reps; ++r) {
+        if (fb) cudaMemsetAsync(fb, r & 0xff, (size_t)flush, st);
+        if (pass == 0) {
+          smooth(L0, 0, 1, 0, none, MgB<T>{L0.b});
+          smooth(L0, 1, 0, 0, none, MgB<T>{L0.b});
+          smooth(L0, 1, 0, 0, none, MgB<T>{L0.b});
+          smooth(L0, 0, 0, 0, none, MgB<T>{L0.b});
+        }
+      }
+      rc = cu(cudaStreamEndCapture(st, &g));
+      if (!rc) rc = cu(cudaGraphInstantiate(&ge, g, 0));
+      if (!rc) rc = cu(cudaGraphLaunch(ge, st));   // warm-up
+      if (!rc) rc = cu(cudaEventRecord(ev_run0, st));
+      if (!rc) rc = cu(cudaGraphLaunch(ge, st));
+      if (!rc) rc = cu(cudaEventRecord(ev_run1, st));
+      if (!rc) rc = cu(cudaStreamSynchronize(st));
+      if (!rc) rc = cu(cudaEventElapsedTime(&ms[pass], ev_run0, ev_run1));
+      if (ge) cudaGraphExecDestroy(ge);
+      if (g) cudaGraphDestroy(g);
+    }
+    launches = launches0;
+    prof_on = was;
+    cudaStreamSynchronize(st);
+    if (fb) cudaFree(fb);
+    const int rc2 = cu(cudaMemcpy(&S.sc->conv, &conv, sizeof(conv), cudaMemcpyHostToDevice));
+    if (rc) return rc;
+    if (rc2) return rc2;
+    *us = 1000.0 * ((double)ms[0] - (double)ms[1]) / (4.0 * reps);
+    return check();
+  }
+  int cu(cudaError_t e) {
+    if (e == cudaSuccess) return NHW_OK;
+    set_last_error(std::string("smoother timing: ") + cudaGetErrorString(e));
+    return NHW_ERR_CUDA;
   }
   int profile_report(char* buf, int len) override {
     NHW_CU(cudaStreamSynchronize(st));

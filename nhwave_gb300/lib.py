@@ -31,7 +31,7 @@ EXPORTS = [
     "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
     "nhw_step", "nhw_run", "nhw_mass", "nhw_statistics", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
-    "nhw_profile_report", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
+    "nhw_profile_report", "nhw_time_smoother", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
     "nhw_estimate_dt_noalloc",
     "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
     "nhw_ensemble_get_info", "nhw_ensemble_destroy", "nhw_device_bytes",
@@ -105,6 +105,7 @@ def load(path: str | None = None):
     L.nhw_run_timed.argtypes = [vp, i32, P(dbl)]
     L.nhw_profile.argtypes = [vp, i32]
     L.nhw_profile_report.argtypes = [vp, ctypes.c_char_p, i32]
+    L.nhw_time_smoother.argtypes = [vp, i32, ctypes.c_int64, P(dbl)]
     L.nhw_estimate_dt_noalloc.argtypes = [vp] * 5 + [i32] * 3 + [dbl] * 5 + [vp, vp]
     L.nhw_ensemble_create.argtypes = [P(vp), i32, P(EnsembleOpts), P(vp)]
     L.nhw_ensemble_step.argtypes = [vp, i32]
@@ -253,6 +254,13 @@ class Scenario:
             name, c, t = ln.split()
             out["kernels"][name] = (int(c), float(t))
         return out
+
+    def time_smoother(self, reps: int = 50, flush_bytes: int = 256 << 20) -> float:
+        """Device microseconds of one level-0 multigrid half-sweep (bulk-timed
+        in a CUDA graph, the L2 evicted before each V-cycle's four)."""
+        us = ctypes.c_double(0.0)
+        _chk(load().nhw_time_smoother(self._h, reps, flush_bytes, ctypes.byref(us)), "nhw_time_smoother")
+        return us.value
 
     def synchronize(self):
         return _chk(load().nhw_synchronize(self._h), "nhw_synchronize")

@@ -166,3 +166,31 @@ def test_gmres_matches_bicgstab(name, precision, gpu_lib):
     assert sb.last_rel_residual <= b.params.tol
     # one GMRES iteration is one V-cycle, one BiCGSTAB iteration two
     assert sb.total_krylov_iters <= 2 * sa.total_krylov_iters
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_smoother_timing_leaves_the_run_unchanged(precision, gpu_lib):
+    """nhw_time_smoother times the level-0 half-sweep on the handle's own
+    operator: a positive time, and the next steps equal those of a run that
+    was never timed, bit for bit (only a preconditioner scratch vector and a
+    device buffer of its own are written)."""
+    from nhwave_gb300 import fields as F, lib
+    a, b = _scen("tiny_c2", precision), _scen("tiny_c2", precision)
+    for s in (a, b):
+        s.step()
+    us = a.time_smoother(reps=4, flush_bytes=1 << 20)
+    assert 0.0 < us < 1e4
+    for s in (a, b):
+        for _ in range(2):
+            s.step()
+    for f in FIELDS:
+        fid = getattr(F, f)
+        assert np.array_equal(a.get(fid), b.get(fid)), f
+    assert a.scalars().total_krylov_iters == b.scalars().total_krylov_iters
+    h = _scen("tiny_c2", precision, non_hydro=0)
+    h.step()
+    with pytest.raises(lib.NhwError) as ex:
+        h.time_smoother(reps=2, flush_bytes=0)
+    assert ex.value.status == lib.ERR_STATE
+    for s in (a, b, h):
+        s.close()
