@@ -2185,21 +2185,4 @@ __global__ void k_mass(Dev<T> S, double* out) {
   *out = m;
 }
 
-// Holds the stream for `ns` nanoseconds of the global timer, so that the host
-// can enqueue the launches that follow before the GPU reaches them.  With the
-// per-kernel profiler on, each kernel's event interval then measures the GPU
-// and not the host's launch rate.  Bounded twice: by the timer, and by a poll
-// count of 4 per microsecond asked (each poll sleeps about 1 us at most), in
-// case the timer does not advance.
-static __global__ void k_hold(unsigned long long ns) {
-  unsigned long long t0, t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-  const unsigned long long polls = ns / 250 + 16;
-  for (unsigned long long q = 0; q < polls; ++q) {
-    __nanosleep(500);
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    if (t - t0 >= ns) break;
-  }
-}
-
 }  // namespace nhw

@@ -195,9 +195,15 @@ __device__ __forceinline__ T off_column_p(const MGL<T>& L, const T* __restrict__
 //                  s = r - alpha v, formed on the fine level by the sweep that
 //                  owns each column (colour 0 in the first half-sweep, colour 1
 //                  in the second) and stored -- no launch of their own.
+//
+// A kernel calls bind(sc) once per thread and the bound functor per cell:
+// the scalars that come from the device in FP64 (beta, omega, alpha) are
+// rounded to the storage type once, not once per cell (each conversion of a
+// double runs on the FP64 pipe).
 template <class T>
 struct MgB {
   const T* b;
+  __device__ __forceinline__ MgB bind(const DevScal*) const { return *this; }
   __device__ __forceinline__ T operator()(const DevScal*, int ic, int, int, int) const { return b[ic]; }
 };
 template <class T>
@@ -205,8 +211,15 @@ struct MgInP {
   T* p;
   const T* r;
   const T* v;
-  __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
-    const T val = r[ic] + (T)sc->beta * (p[ic] - (T)sc->omega * v[ic]);
+  T beta = (T)0, omega = (T)0;   // set by bind
+  __device__ __forceinline__ MgInP bind(const DevScal* sc) const {
+    MgInP q = *this;
+    q.beta = (T)sc->beta;
+    q.omega = (T)sc->omega;
+    return q;
+  }
+  __device__ __forceinline__ T operator()(const DevScal*, int ic, int, int, int) const {
+    const T val = r[ic] + beta * (p[ic] - omega * v[ic]);
     p[ic] = val;
     return val;
   }
@@ -216,8 +229,14 @@ struct MgInS {
   T* s;
   const T* r;
   const T* v;
-  __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
-    const T val = r[ic] - (T)sc->alpha * v[ic];
+  T alpha = (T)0;   // set by bind
+  __device__ __forceinline__ MgInS bind(const DevScal* sc) const {
+    MgInS q = *this;
+    q.alpha = (T)sc->alpha;
+    return q;
+  }
+  __device__ __forceinline__ T operator()(const DevScal*, int ic, int, int, int) const {
+    const T val = r[ic] - alpha * v[ic];
     s[ic] = val;
     return val;
   }
@@ -234,6 +253,7 @@ struct MgInV {
   T* V;
   const T* inv;   // (T)(1 / ||w||)
   size_t n;
+  __device__ __forceinline__ MgInV bind(const DevScal*) const { return *this; }
   __device__ __forceinline__ T operator()(const DevScal* sc, int ic, int, int, int) const {
     const T val = w[ic] * *inv;
     V[(size_t)sc->it * n + ic] = val;
@@ -250,6 +270,7 @@ template <class T, bool kProlong, class In>
 __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal* sc, int color, int zero_x,
                                                         Prolong<T> P, In in) {
   if (sc->conv) return;
+  const In inb = in.bind(sc);
   extern __shared__ unsigned char smem_raw[];
   T* sh = reinterpret_cast<T*>(smem_raw);
   const int K = L.K, M = L.M, MN = L.M * L.N, n = L.n;
@@ -272,7 +293,7 @@ __global__ void __launch_bounds__(1024) k_mg_smooth_blk(MGL<T> L, const DevScal*
       const int ic = col + MN * k;
       T off = (T)0;
       if (!zero_x) off = kProlong ? off_column_p(L, L.x, P, ic, ii, jj, k) : off_column(L, L.x, ic, ii, jj, k);
-      rhs = in(sc, ic, ii, jj, k) - off;
+      rhs = inb(sc, ic, ii, jj, k) - off;
       a = k > 0 ? L.coef[2 * n + ic] : (T)0;
       inv = L.linv[ic];
       cp = L.lcp[ic];
@@ -325,6 +346,7 @@ __global__ void __maxnreg__(kSplitRegs)
 k_mg_smooth_split(MGL<T> L, const DevScal* sc, int color, int zero_x, Prolong<T> P, In in) {
   static_assert(sizeof(T) == 4, "the FP64 form takes k_mg_smooth_split_strided");
   if (sc->conv) return;
+  const In inb = in.bind(sc);
   constexpr int LPT = kSplitLevels;
   extern __shared__ unsigned char smem_raw[];
   T* sh = reinterpret_cast<T*>(smem_raw);
@@ -410,7 +432,7 @@ k_mg_smooth_split(MGL<T> L, const DevScal* sc, int color, int zero_x, Prolong<T>
           }
           off = s;
         }
-        s_rhs[k * 32 + tx] = in(sc, ic, ii, jj, k) - off;
+        s_rhs[k * 32 + tx] = inb(sc, ic, ii, jj, k) - off;
         s_a[k * 32 + tx] = a;
         s_inv[k * 32 + tx] = inv;
         s_cp[k * 32 + tx] = cp;
@@ -446,6 +468,7 @@ template <class T, bool kProlong, class In>
 __global__ void __launch_bounds__(1024, 2) k_mg_smooth_split_strided(MGL<T> L, const DevScal* sc, int color, int zero_x,
                                                           Prolong<T> P, In in) {
   if (sc->conv) return;
+  const In inb = in.bind(sc);
   extern __shared__ unsigned char smem_raw[];
   T* sh = reinterpret_cast<T*>(smem_raw);
   const int K = L.K, M = L.M, MN = L.M * L.N;
@@ -475,7 +498,7 @@ __global__ void __launch_bounds__(1024, 2) k_mg_smooth_split_strided(MGL<T> L, c
         off = kProlong ? off_column_pc(L, L.x, P, ic, ii, jj, k, c4, c5, c7, c8)
                        : off_column_c(L, L.x, ic, ii, jj, k, c4, c5, c7, c8);
       }
-      rhs = in(sc, ic, ii, jj, k) - off;
+      rhs = inb(sc, ic, ii, jj, k) - off;
     }
     s_rhs[k * 32 + tx] = rhs;
     s_a[k * 32 + tx] = a;

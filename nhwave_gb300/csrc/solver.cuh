@@ -487,15 +487,7 @@ class Solver final : public SolverBase {
   int pull_scalars() {
     NHW_CU(cudaMemcpyAsync(h_sc, S.sc, sizeof(DevScal), cudaMemcpyDeviceToHost, st));
     NHW_CU(cudaStreamSynchronize(st));
-    prof_hold();
     return NHW_OK;
-  }
-  // With the per-kernel profiler on, every host round trip leaves the stream
-  // empty, and the launches that follow would reach the GPU at the host's
-  // launch rate (a few microseconds each, events included): hold the stream
-  // for 3 ms while the host enqueues them.  The hold is not a profiled launch.
-  void prof_hold() {
-    if (prof_on) k_hold<<<1, 1, 0, st>>>(3000000ull);
   }
   int sync() override {
     NHW_CU(cudaStreamSynchronize(st));
@@ -1003,8 +995,7 @@ class Solver final : public SolverBase {
         rc = pull_scalars();
         if (rc) return rc;
         if (h_sc->conv != 0) break;
-        // (profiling: chunks of 4, about 200 launches, which one hold covers)
-        if (chunk < 16 && !prof_on) chunk *= 2;
+        if (chunk < 16) chunk *= 2;
       }
       inner_finish();
       L("res64", [&] { k_res64<T, false><<<red_blocks(), 256, 0, st>>>(S); });
@@ -1239,7 +1230,6 @@ class Solver final : public SolverBase {
     return rc ? rc : worst;
   }
   int step_eager() {
-    prof_hold();
     int rc = estimate_dt();
     if (rc) return rc;
     return step_body();
