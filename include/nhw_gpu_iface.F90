@@ -54,6 +54,11 @@ module nhw_gpu_iface
   integer(c_int), parameter :: NHW_WM_LEF_JON = 12
   integer(c_int), parameter :: NHW_WM_LEF_TMA = 13
   integer(c_int), parameter :: NHW_WM_LEF_SPC = 14
+  integer(c_int), parameter :: NHW_WM_INT_CON = 15
+  integer(c_int), parameter :: NHW_WM_INT_JON = 16
+  integer(c_int), parameter :: NHW_WM_INT_TMA = 17
+  integer(c_int), parameter :: NHW_WM_INT_SPC = 18
+  integer(c_int), parameter :: NHW_WM_INT_IRR = 19
 
   ! ------------------------------------------- enum nhw_slide, nhw_depth_type
   integer(c_int), parameter :: NHW_SLIDE_NONE = 0

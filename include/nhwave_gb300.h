@@ -20,7 +20,7 @@
  *   nhw_update_wave_bc     <- update_wave_bc       src/nhwave.F:5514-5565 (the generators of enum nhw_wavemaker)
  *   nhw_update_mask        <- update_mask          src/nhwave.F:5403-5456
  *   nhw_update_vars        <- update_vars          src/nhwave.F:5459-5511
- *   nhw_source_terms       <- source_terms         src/source_terms.F:1-455 (INT_LIN + bed slope)
+ *   nhw_source_terms       <- source_terms         src/source_terms.F:1-455 (internal makers + bed slope)
  *   nhw_fluxes             <- fluxes               src/nhwave.F:1686-1714
  *   nhw_eval_duvw          <- eval_duvw(ISTEP)     src/nhwave.F:539-1300 (inviscid path,
  *                             incl. poisson_solver src/pressure.F:63-245 and
@@ -83,11 +83,17 @@ enum nhw_precision {
  * (src/initialize.F:880-941, src/waves.F:566-623).  LEF_SPC: irregular,
  * directional waves through the west side from a 2-D spectrum the driver
  * passes with nhw_set_wave_spectrum (the reference reads it from spc2d.txt,
- * src/initialize.F:782-830; src/waves.F:376-513) */
+ * src/initialize.F:782-830; src/waves.F:376-513).  INT_CON, INT_JON, INT_TMA,
+ * INT_SPC, INT_IRR: the internal source strip fed by a cnoidal wave, by the
+ * JONSWAP / TMA components of LEF_JON / LEF_TMA, by a 2-D spectrum of
+ * densities (spc2d.txt) or by one of component amplitudes with their phases
+ * (irr2d.txt), both passed with nhw_set_wave_spectrum (src/source_terms.F:
+ * 71-340; src/initialize.F:835-876) */
 enum nhw_wavemaker { NHW_WM_NONE = 0, NHW_WM_INT_LIN = 1, NHW_WM_INT_SOL = 2, NHW_WM_LEF_LIN = 3,
                      NHW_WM_LEF_SOL = 4, NHW_WM_LEF_STK = 5, NHW_WM_LEF_CON = 6, NHW_WM_WAV_CUR = 7,
                      NHW_WM_FOCUSED = 8, NHW_WM_LEF_TID = 9, NHW_WM_RIG_LIN = 10, NHW_WM_FLUX_LR = 11,
-                     NHW_WM_LEF_JON = 12, NHW_WM_LEF_TMA = 13, NHW_WM_LEF_SPC = 14 };
+                     NHW_WM_LEF_JON = 12, NHW_WM_LEF_TMA = 13, NHW_WM_LEF_SPC = 14, NHW_WM_INT_CON = 15,
+                     NHW_WM_INT_JON = 16, NHW_WM_INT_TMA = 17, NHW_WM_INT_SPC = 18, NHW_WM_INT_IRR = 19 };
 enum nhw_slide     { NHW_SLIDE_NONE = 0, NHW_SLIDE_RIGID_3D = 1 };
 enum nhw_depth_type { NHW_DEPTH_CELL_CENTER = 0, NHW_DEPTH_CELL_GRID = 1 };
 
@@ -254,12 +260,12 @@ int nhw_field_shape(const nhw_handle* h, int field, int32_t dims[3], int32_t* el
 
 int nhw_get_scalars(nhw_handle* h, nhw_scalars* out);
 int nhw_set_time(nhw_handle* h, double time, double dt, int32_t run_step);
-/* Phases (radians) of the n = NumFreq components of LEF_JON / LEF_TMA, in
+/* Phases (radians) of the n = NumFreq components of a JONSWAP / TMA maker, in
  * place of the ones drawn from wave_seed: the reference's RanPhs
  * (src/initialize.F:937-940), for a driver that wants its own draw.  Call
  * it after nhw_setup (which sets the seeded phases); they apply from the
- * next update_wave_bc.  NHW_ERR_ARG unless the handle runs LEF_JON or
- * LEF_TMA with n components. */
+ * next update_wave_bc (LEF_) or source_terms (INT_).  NHW_ERR_ARG unless
+ * the handle runs LEF_JON, LEF_TMA, INT_JON or INT_TMA with n components. */
 int nhw_set_wave_phases(nhw_handle* h, int32_t n, const double* phases);
 /* The 2-D spectrum of LEF_SPC, as the reference reads it from spc2d.txt
  * (src/initialize.F:783-830): numfreq >= 2 frequencies freq[] (Hz), numdir >= 2
@@ -270,7 +276,12 @@ int nhw_set_wave_phases(nhw_handle* h, int32_t n, const double* phases);
  * wave_seed (the reference draws them with the compiler's rand()).  Call it
  * after nhw_create and before the first step; the library copies the data.
  * A checkpoint does not hold the spectrum: after nhw_load_state pass it
- * again.  NHW_ERR_ARG unless the handle runs LEF_SPC. */
+ * again.  INT_SPC takes the same data; INT_IRR takes component amplitudes
+ * in spc2d[] (the reference's irr2d.txt, src/initialize.F:835-876) and its
+ * phases, which are then required.  The internal makers snap each direction
+ * to the nearest one that the channel width repeats (src/source_terms.F:
+ * 94-136), which needs |direction| <= 90 degrees.  NHW_ERR_ARG unless the
+ * handle runs LEF_SPC, INT_SPC or INT_IRR. */
 int nhw_set_wave_spectrum(nhw_handle* h, int32_t numfreq, int32_t numdir, const double* freq,
                           const double* dire, const double* spc2d, const double* phases);
 

@@ -12,7 +12,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <type_traits>
+#include "../../include/nhwave_gb300.h"
 #include "cnoidal.h"
+#include "components.h"
 #include "state.h"
 
 namespace nhw {
@@ -637,15 +639,41 @@ struct OpSource {
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long c = i2(S, i, j);
     const double time = S.sc->time;
-    if (S.wavemaker != 0 && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys &&
-        S.yc[j] <= S.wm_yn) {
+    const int wm = S.wavemaker;
+    const bool internal = wm == NHW_WM_INT_LIN || wm == NHW_WM_INT_SOL || wm == NHW_WM_INT_CON ||
+                          wm == NHW_WM_INT_JON || wm == NHW_WM_INT_TMA || wm == NHW_WM_INT_SPC ||
+                          wm == NHW_WM_INT_IRR;
+    if (internal && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys && S.yc[j] <= S.wm_yn) {
       const double area = S.sc->source_area;
-      if (S.wavemaker == 1) {
+      if (wm == NHW_WM_INT_LIN) {
         const double phs = S.yc[j] * S.wm_wnumy;
         S.SourceC[c] = S.wm_celerity * S.wm_amp / area * cos(kPi / 2 - S.wm_segma * time + phs);
-      } else {
+      } else if (wm == NHW_WM_INT_SOL) {
         const double ch = cosh(S.wm_atmp * (S.wm_xstart - S.wm_celerity * time));
         S.SourceC[c] = 2.0 * S.wm_celerity / area * S.wm_amp / (ch * ch);
+      } else if (wm == NHW_WM_INT_CON) {   // src/source_terms.F:386-395
+        const double Xcn = cnoidal_cn(S.con_x0 + 2.0 * S.con_ck * (-(time / S.lef_per)), S.con_mod);
+        S.SourceC[c] = 2.0 * S.wm_celerity / area * (S.con_ytr + S.wm_amp * (Xcn * Xcn));
+      } else {
+        // INT_JON / INT_TMA / INT_SPC / INT_IRR: the components' sum, in the
+        // reference's order (frequency outer, direction inner;
+        // src/source_terms.F:84-191, 207-300, 321-338); INT_IRR's eta_mean
+        // is never read by the reference, so 0
+        const int n = S.njon;
+        const double* t = S.jon;
+        const bool jon = wm == NHW_WM_INT_JON || wm == NHW_WM_INT_TMA;
+        const double lag = S.dy / 2.0 + S.yc[j];
+        double acc = 0.0;
+        for (int q = 0; q < n; ++q) {
+          const double segma = t[kIntSegma * n + q], ph = t[kJonPhase * n + q];
+          const double arg = jon ? kPi / 2 - segma * time + ph
+                                 : kPi / 2 - segma * time + lag * t[kIntWnumY * n + q] + ph;
+          if (t[kIntKind * n + q] != 0.0)
+            acc = acc + t[kIntPre * n + q] / area * (t[kIntHalfAmp * n + q] * cos(arg) + 0.0);
+          else
+            acc = acc + t[kIntPre * n + q] / area * cos(arg);
+        }
+        S.SourceC[c] = acc;
       }
     }
     const double m = (double)S.Mask[c];

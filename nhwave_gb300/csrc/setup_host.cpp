@@ -18,7 +18,7 @@ const double kPiH = (double)3.141592653f;
 const double kGravH = (double)9.81f;
 inline double dmx(double a, double b) { return a > b ? a : b; }
 inline double dmn(double a, double b) { return a < b ? a : b; }
-bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m);
+bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m, double* c = nullptr);
 bool cnoidal_start(double Ytrough, double A, double m, double& Xstart);
 }  // namespace
 
@@ -51,13 +51,16 @@ int check_params(const nhw_params& p) {
   const bool fric = p.bc_z0 == 5 || p.bc_x0 == 5 || p.bc_xn == 5 || p.bc_y0 == 5 || p.bc_yn == 5;
   if (fric && p.ibot != 1 && p.ibot != 2) return NHW_ERR_UNSUPPORTED;
   if (fric && p.ibot == 2 && !(p.zob > 0.0)) return NHW_ERR_ARG;
-  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_LEF_SPC) return NHW_ERR_UNSUPPORTED;
+  if (p.wavemaker < 0 || p.wavemaker > NHW_WM_INT_IRR) return NHW_ERR_UNSUPPORTED;
   if (p.krylov_kernel < 0 || p.krylov_kernel > 2) return NHW_ERR_ARG;
   if (p.slide_type < 0 || p.slide_type > 1) return NHW_ERR_UNSUPPORTED;
   if (p.precision != NHW_FP64 && p.precision != NHW_FP32_IR) return NHW_ERR_ARG;
   if (p.time_order < 1 || p.time_order > 3) return NHW_ERR_ARG;
-  if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && p.wavemaker != NHW_WM_FLUX_LR &&
-      p.wavemaker != NHW_WM_LEF_JON && p.wavemaker != NHW_WM_LEF_TMA && p.wavemaker != NHW_WM_LEF_SPC &&
+  const bool spectral = p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA ||
+                        p.wavemaker == NHW_WM_LEF_SPC || p.wavemaker == NHW_WM_INT_JON ||
+                        p.wavemaker == NHW_WM_INT_TMA || p.wavemaker == NHW_WM_INT_SPC ||
+                        p.wavemaker == NHW_WM_INT_IRR;
+  if (p.wavemaker && p.wavemaker != NHW_WM_FOCUSED && p.wavemaker != NHW_WM_FLUX_LR && !spectral &&
       !(p.per_wave > 0 && p.dep_wave > 0))
     return NHW_ERR_ARG;
   // FOCUSED: at least two components (the frequency spacing divides by
@@ -66,13 +69,14 @@ int check_params(const nhw_params& p) {
       (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0) ||
        (p.component_amp_type == 1 && !(p.k_center > 0))))
     return NHW_ERR_ARG;
-  if (p.wavemaker == NHW_WM_LEF_SPC && !(p.dep_wave > 0)) return NHW_ERR_ARG;
-  if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) {   // src/initialize.F:880-941
+  if (spectral && !(p.dep_wave > 0)) return NHW_ERR_ARG;
+  if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_INT_JON ||
+      p.wavemaker == NHW_WM_INT_TMA) {   // src/initialize.F:880-941
     if (!(p.hm0 > 0) || !(p.tp > 0) || !(p.freq_min > 0) || !(p.freq_max > p.freq_min) || p.numfreq < 1 ||
         p.numfreq > 500 || !(p.dep_wave > 0))
       return NHW_ERR_ARG;
   }
-  if (p.wavemaker == NHW_WM_LEF_CON) {   // the cnoidal parameter and start phase must exist
+  if (p.wavemaker == NHW_WM_LEF_CON || p.wavemaker == NHW_WM_INT_CON) {   // the cnoidal parameter and start phase must exist
     double L = 0, Yt = 0, m = 0, Xstart = 0;
     if (!(p.amp_wave > 0) || !cnoidal_params(p.amp_wave, p.dep_wave, p.per_wave, L, Yt, m) ||
         !cnoidal_start(Yt, p.amp_wave, m, Xstart))
@@ -84,8 +88,8 @@ int check_params(const nhw_params& p) {
 namespace {
 // cnoidal (src/waves.F:184-220): Newton iteration for the elliptic parameter
 // m of a cnoidal wave of height H in depth d with period T, then its length
-// L and trough level x2.  Returns false when m leaves (0, 1].
-bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m) {
+// L, trough level x2 and (c) celerity.  Returns false when m leaves (0, 1].
+bool cnoidal_params(double H, double d, double T, double& L, double& x2, double& m, double* c) {
   m = 0.99999999;
   for (int n = 1;; ++n) {
     if (!(m > 0.0 && m <= 1.0)) return false;
@@ -102,6 +106,8 @@ bool cnoidal_params(double H, double d, double T, double& L, double& x2, double&
   if (!(m > 0.0 && m <= 1.0)) return false;
   const double ck = cnoidal_ck(m), ce = cnoidal_ce(m);
   L = 4.0 * ck * d * std::sqrt(m * d / H / 3.0);
+  const double xtemp = -m + 2.0 - 3.0 * ce / ck;
+  if (c) *c = std::sqrt(kGravH * d * (1.0 + H / d / m * xtemp));
   x2 = H / m * (1.0 - m - ce / ck);
   return std::isfinite(L) && std::isfinite(x2);
 }
@@ -156,13 +162,16 @@ namespace {
 // (src/waves.F:585), so its wave number is undefined; the wave number here is
 // wave_dispersion's of each component, as the spectral routine computes it
 // (src/waves.F:395).
-void jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out) {
+// The JONSWAP (TMA) spectrum of src/initialize.F:893-941: NumFreq band
+// centres and their densities scaled to m0 = Hm0^2/16.
+void jonswap_spectrum(const nhw_params& p, bool tma, std::vector<double>& Freq, std::vector<double>& Spc) {
   const int nf = p.numfreq;
   const double Dep = p.dep_wave;
   const double gam = (double)3.3f, sa = (double)0.07f, sb = (double)0.09f;
   const double Freq_Peak = 1.0 / p.tp;
   const double DFreq = (p.freq_max - p.freq_min) / nf;
-  std::vector<double> Freq(nf), Spc(nf);
+  Freq.assign(nf, 0.0);
+  Spc.assign(nf, 0.0);
   for (int i = 1; i <= nf; ++i) {
     const double F = p.freq_min + 0.5 * DFreq + (i - 1) * DFreq;
     Freq[i - 1] = F;
@@ -188,10 +197,23 @@ void jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out)
   double SumInt = 0.0;
   for (int i = 0; i < nf; ++i) SumInt = SumInt + Spc[i] * DFreq;
   const double A_Jon = (p.hm0 * p.hm0) / 16.0 / SumInt;
+  for (int i = 0; i < nf; ++i) Spc[i] = Spc[i] * A_Jon;
+}
+
+// LEF_JON / LEF_TMA: the boundary routine's per-component constants
+// (src/waves.F:580-593).  The reference's boundary routine calls
+// wave_dispersion with three arguments where it takes two (src/waves.F:585),
+// so its wave number is undefined; the wave number here is wave_dispersion's
+// of each component, as the spectral routine computes it (src/waves.F:395).
+void jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out) {
+  const int nf = p.numfreq;
+  const double Dep = p.dep_wave;
+  std::vector<double> Freq, Spc;
+  jonswap_spectrum(p, tma, Freq, Spc);
   out.assign((size_t)kJonSlots * nf, 0.0);
   const double dfreq = (p.freq_max - p.freq_min) / (double)(float)nf;
   for (int i = 0; i < nf; ++i) {
-    const double S = Spc[i] * A_Jon;
+    const double S = Spc[i];
     const double Per = 1.0 / Freq[i], Segma = 2.0 * kPiH / Per;
     const double k = wave_number(Segma, Dep), Wave_Length = 2.0 * kPiH / k;
     const double Wh = 2.0 * std::sqrt(2.0 * S * dfreq);
@@ -203,6 +225,26 @@ void jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out)
     out[5 * nf + i] = std::sinh(k * Dep);
     out[6 * nf + i] = 0.0;
     out[7 * nf + i] = 1.0;
+  }
+}
+
+// INT_JON / INT_TMA (src/source_terms.F:305-340): per component, in the
+// internal makers' layout (setup_host.h), Celerity * Amp_Wave with
+// Amp_Wave = 2 sqrt(2 Jon_Spc DFreq), Segma = 2 pi / Per_Wave and the phase.
+void internal_jonswap_components(const nhw_params& p, bool tma, std::vector<double>& out) {
+  const int nf = p.numfreq;
+  std::vector<double> Freq, Spc;
+  jonswap_spectrum(p, tma, Freq, Spc);
+  out.assign((size_t)kJonSlots * nf, 0.0);
+  const double DFreq = (p.freq_max - p.freq_min) / (double)(float)nf;
+  for (int i = 0; i < nf; ++i) {
+    const double Per = 1.0 / Freq[i], Segma = 2.0 * kPiH / Per;
+    const double k = wave_number(Segma, p.dep_wave), Wave_Length = 2.0 * kPiH / k;
+    const double Celerity = Wave_Length / Per;
+    const double Amp = 2.0 * std::sqrt(2.0 * Spc[i] * DFreq);
+    out[kIntPre * nf + i] = Celerity * Amp;
+    out[kIntSegma * nf + i] = Segma;
+    out[kJonPhase * nf + i] = wave_phase(p.wave_seed, i);
   }
 }
 }  // namespace
@@ -237,6 +279,84 @@ bool spectrum_components(const nhw_params& p, int numfreq, int numdir, const dou
       out[5 * nc + c] = std::sinh(k * Dep);
       out[6 * nc + c] = std::sin(Angle);
       out[7 * nc + c] = std::cos(Angle);
+    }
+  return true;
+}
+
+bool snap_direction(double Angle, double k, int Nglob, double dy, bool irr, double& out) {
+  const double small = (double)1.0e-16f;
+  const double width = Nglob * dy;
+  const int kSnapMax = 10000000;   // the reference's loop has no bound; |Angle| <= 90 deg ends it
+  if (!(k > 0.0)) return false;
+  if (Angle > 0.0) {
+    double tmp3 = 0.0;
+    int nk = 0;
+    while (tmp3 < Angle) {
+      if (++nk > kSnapMax) return false;
+      const double tmp2 = nk * 2.0 * kPiH / width;
+      tmp3 = tmp2 >= k ? 0.5 * kPiH - small : std::asin(tmp2 / k);
+    }
+    const double tmp4 = std::asin((nk - 1) * 2.0 * kPiH / width / k);
+    out = std::fabs(tmp4 - Angle) < std::fabs(Angle - tmp3) ? tmp4 : tmp3;
+  } else if (Angle < 0.0 || !irr) {
+    // (INT_SPC takes this branch for a zero direction too, and keeps zero;
+    // both makers compare with the positive arcsine here)
+    double tmp3 = 0.0;
+    int nk = 0;
+    while (tmp3 > Angle) {
+      if (++nk > kSnapMax) return false;
+      const double tmp2 = nk * 2.0 * kPiH / width;
+      tmp3 = tmp2 >= k ? -0.5 * kPiH + small : -std::asin(tmp2 / k);
+    }
+    const double tmp4 = std::asin((nk - 1) * 2.0 * kPiH / width / k);
+    out = std::fabs(tmp4 - Angle) < std::fabs(Angle - tmp3) ? tmp4 : tmp3;
+  } else {
+    out = 0.0;
+  }
+  return true;
+}
+
+bool internal_spectrum_components(const nhw_params& p, int numfreq, int numdir, const double* freq,
+                                  const double* dire, const double* spc2d, const double* phases,
+                                  std::vector<double>& out) {
+  const bool irr = p.wavemaker == NHW_WM_INT_IRR;
+  if (numfreq < 2 || numdir < 2 || (long long)numfreq * numdir > 12000 || !freq || !dire || !spc2d) return false;
+  if (irr && !phases) return false;   // irr2d.txt holds them
+  const int nc = numfreq * numdir;
+  out.assign((size_t)kJonSlots * nc, 0.0);
+  for (int nfq = 1; nfq <= numfreq; ++nfq)
+    for (int nd = 1; nd <= numdir; ++nd) {
+      const int c = (nd - 1) + numdir * (nfq - 1);
+      const double Per = 1.0 / freq[nfq - 1], Segma = 2.0 * kPiH / Per;
+      const double k = wave_number(Segma, p.dep_wave), Wave_Length = 2.0 * kPiH / k;
+      const double Celerity = Wave_Length / Per;
+      double Angle = 0.0;
+      if (!snap_direction(dire[nd - 1] * kPiH / 180., k, p.Nglob, p.dy, irr, Angle)) return false;
+      double Amp;
+      if (irr) {
+        Amp = 2.0 * spc2d[c];
+      } else {
+        double dfreq = nfq == 1 ? freq[1] - freq[0]
+                       : nfq == numfreq ? freq[numfreq - 1] - freq[numfreq - 2]
+                                        : 0.5 * (freq[nfq] - freq[nfq - 2]);
+        dfreq = std::fabs(dfreq);
+        double ddir = nd == 1 ? dire[1] - dire[0]
+                      : nd == numdir ? dire[numdir - 1] - dire[numdir - 2]
+                                     : 0.5 * (dire[nd] - dire[nd - 2]);
+        ddir = std::fabs(ddir);
+        Amp = 2.0 * std::sqrt(2.0 * spc2d[c] * ddir * dfreq);
+      }
+      if (!(Amp == Amp) || !std::isfinite(Celerity)) return false;
+      if (irr && nfq == 1) {   // 2 Celerity / Source_Area (Amp_Wave/2 cos(..) + eta_mean)
+        out[kIntPre * nc + c] = 2 * Celerity;
+        out[kIntHalfAmp * nc + c] = Amp / 2;
+        out[kIntKind * nc + c] = 1.0;
+      } else {
+        out[kIntPre * nc + c] = Celerity * Amp;
+      }
+      out[kIntSegma * nc + c] = Segma;
+      out[kIntWnumY * nc + c] = k * std::sin(Angle);
+      out[kJonPhase * nc + c] = phases ? phases[c] : wave_phase(p.wave_seed, c);
     }
   return true;
 }
@@ -492,10 +612,14 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
     }
   } else if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) {
     jonswap_components(p, p.wavemaker == NHW_WM_LEF_TMA, h.jon);
-  } else if (p.wavemaker == NHW_WM_LEF_CON) {   // src/waves.F:100-140
+  } else if (p.wavemaker == NHW_WM_INT_JON || p.wavemaker == NHW_WM_INT_TMA) {
+    internal_jonswap_components(p, p.wavemaker == NHW_WM_INT_TMA, h.jon);
+  } else if (p.wavemaker == NHW_WM_LEF_CON || p.wavemaker == NHW_WM_INT_CON) {
+    // src/waves.F:100-140; src/source_terms.F:343-385 (the same start phase)
     const double A = p.amp_wave, Dep = p.dep_wave;
-    double L = 0, Yt = 0, m = 0, Xstart = 0;
-    if (!cnoidal_params(A, Dep, p.per_wave, L, Yt, m)) return NHW_ERR_ARG;
+    double L = 0, Yt = 0, m = 0, Xstart = 0, cel = 0;
+    if (!cnoidal_params(A, Dep, p.per_wave, L, Yt, m, &cel)) return NHW_ERR_ARG;
+    h.wm_celerity = cel;
     if (!cnoidal_start(Yt, A, m, Xstart)) return NHW_ERR_ARG;
     double a[kCnMax], c[kCnMax];
     if (!(std::fabs(c[cn_agm(m, a, c)]) < kCnEps)) return NHW_ERR_ARG;   // sequence must fit kCnMax

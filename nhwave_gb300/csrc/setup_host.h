@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <vector>
 #include "../../include/nhwave_gb300.h"
+#include "components.h"
 
 namespace nhw {
 
@@ -40,12 +41,23 @@ int host_setup(const nhw_params& p, const double* depth, const double* eta0, con
 double wave_number(double segma, double dep);
 // Phase i (radians, [0, 2 pi)) of the irregular boundary waves' stream `seed`.
 double wave_phase(int32_t seed, int i);
-constexpr int kJonSlots = 8;   // Wh, sigma, k, Stokes drift, phase, sinh(k h), sin(theta), cos(theta)
-constexpr int kJonPhase = 4;
+
 // LEF_SPC components from a 2-D spectrum (src/waves.F:388-465), slot-major
 // [8][numfreq * numdir], component (nfreq, ndir) at ndir + numdir * nfreq;
 // phases == nullptr: the stream of p.wave_seed.  False on a bad spectrum.
 bool spectrum_components(const nhw_params& p, int numfreq, int numdir, const double* freq, const double* dire,
                          const double* spc2d, const double* phases, std::vector<double>& out);
+// INT_SPC / INT_IRR components (src/source_terms.F:71-300) in the internal
+// makers' layout, component (nfreq, ndir) at ndir + numdir * nfreq; each
+// direction snapped as the reference does (snap_direction).  INT_IRR takes
+// amplitudes and needs the phases.  False on a bad spectrum.
+bool internal_spectrum_components(const nhw_params& p, int numfreq, int numdir, const double* freq,
+                                  const double* dire, const double* spc2d, const double* phases,
+                                  std::vector<double>& out);
+// A component direction (radians) snapped to the nearest one whose
+// cross-channel wave number nk 2 pi / (Nglob dy) the channel repeats
+// (src/source_terms.F:94-136; INT_IRR's form, irr, keeps a zero direction,
+// :203-247).  False when the search does not end (|Angle| > 90 degrees).
+bool snap_direction(double Angle, double k, int Nglob, double dy, bool irr, double& out);
 
 }  // namespace nhw

@@ -281,7 +281,8 @@ class Solver final : public SolverBase {
     S.nwave = p.wavemaker == NHW_WM_FOCUSED ? p.nwave : 0;
     S.foc_xb = p.x_breaking; S.foc_tb = p.t_breaking; S.foc_dc = p.depth_comp; S.foc_sd = p.sd_return;
     if (S.nwave) add((double**)&S.foc, sizeof(double) * 3 * S.nwave);
-    S.njon = (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) ? p.numfreq : 0;
+    S.njon = (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_INT_JON ||
+              p.wavemaker == NHW_WM_INT_TMA) ? p.numfreq : 0;
     if (S.njon) add((double**)&S.jon, sizeof(double) * kJonSlots * S.njon);
     for (const double** lv : {&S.lv_x, &S.lv_y, &S.lv_up, &S.lv_dn, &S.lv_h, &S.lv_ds, &S.lv_fint})
       add((double**)lv, sizeof(double) * S.Kloc);
@@ -685,9 +686,11 @@ class Solver final : public SolverBase {
     for (int q = 0; q < 3; ++q) { S.alpha[q] = h.alpha[q]; S.beta[q] = h.beta[q]; }
     S.wm_segma = h.wm_segma; S.wm_celerity = h.wm_celerity; S.wm_wnumy = h.wm_wnumy;
     S.wm_atmp = h.wm_atmp; S.wm_xstart = h.wm_xstart;
-    S.lef = ((p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) || S.njon ||
-             p.wavemaker == NHW_WM_LEF_SPC) ? p.wavemaker : 0;
-    if (S.njon && !h.jon.empty())   // LEF_JON / LEF_TMA (LEF_SPC's table comes from nhw_set_wave_spectrum)
+    S.lef = ((p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) || p.wavemaker == NHW_WM_LEF_JON ||
+             p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC) ? p.wavemaker : 0;
+    // LEF_JON / LEF_TMA / INT_JON / INT_TMA (the 2-D spectra's tables come
+    // from nhw_set_wave_spectrum)
+    if (S.njon && !h.jon.empty())
       NHW_CU(cudaMemcpyAsync((void*)S.jon, h.jon.data(), sizeof(double) * h.jon.size(), cudaMemcpyHostToDevice, st));
     S.east = p.bc_xn == 3 ? p.wavemaker : 0;   // RIG_LIN or FLUX_LR (check_params)
     if (S.lef == NHW_WM_FOCUSED)
@@ -817,14 +820,18 @@ class Solver final : public SolverBase {
   double* spc_table = nullptr;
   int set_wave_spectrum(int nf, int nd, const double* freq, const double* dire, const double* spc,
                         const double* phases) override {
-    if (p.wavemaker != NHW_WM_LEF_SPC) {
-      set_last_error("nhw_set_wave_spectrum: the handle does not run LEF_SPC");
+    const bool internal = p.wavemaker == NHW_WM_INT_SPC || p.wavemaker == NHW_WM_INT_IRR;
+    if (p.wavemaker != NHW_WM_LEF_SPC && !internal) {
+      set_last_error("nhw_set_wave_spectrum: the handle runs none of LEF_SPC, INT_SPC, INT_IRR");
       return NHW_ERR_ARG;
     }
     std::vector<double> tab;
-    if (!spectrum_components(p, nf, nd, freq, dire, spc, phases, tab)) {
-      set_last_error("nhw_set_wave_spectrum: needs 2 <= numfreq, 2 <= numdir, numfreq * numdir <= 12000 and a "
-                     "finite, non-negative spectrum");
+    const bool ok = internal ? internal_spectrum_components(p, nf, nd, freq, dire, spc, phases, tab)
+                             : spectrum_components(p, nf, nd, freq, dire, spc, phases, tab);
+    if (!ok) {
+      set_last_error("nhw_set_wave_spectrum: needs 2 <= numfreq, 2 <= numdir, numfreq * numdir <= 12000, a "
+                     "finite, non-negative spectrum, for INT_SPC / INT_IRR directions within 90 degrees of the "
+                     "x axis, and for INT_IRR the phases");
       return NHW_ERR_ARG;
     }
     NHW_CU(cudaStreamSynchronize(st));
@@ -837,10 +844,12 @@ class Solver final : public SolverBase {
     drop_step_graphs();   // captured kernels hold the table's address and size
     return NHW_OK;
   }
-  // the reference's RanPhs given by the driver (LEF_JON / LEF_TMA)
+  // the reference's RanPhs given by the driver (LEF_JON / LEF_TMA / INT_JON / INT_TMA)
   int set_wave_phases(int n, const double* phases) override {
-    if (!S.njon || n != S.njon || !phases || p.wavemaker == NHW_WM_LEF_SPC) {
-      set_last_error("nhw_set_wave_phases: the handle runs no LEF_JON / LEF_TMA wave of this many components");
+    const bool jon = p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA ||
+                     p.wavemaker == NHW_WM_INT_JON || p.wavemaker == NHW_WM_INT_TMA;
+    if (!jon || !S.njon || n != S.njon || !phases) {
+      set_last_error("nhw_set_wave_phases: the handle runs no JONSWAP / TMA wave of this many components");
       return NHW_ERR_ARG;
     }
     NHW_CU(cudaMemcpyAsync((void*)(S.jon + kJonPhase * S.njon), phases, sizeof(double) * n,
@@ -872,6 +881,10 @@ class Solver final : public SolverBase {
     return check();
   }
   int source_terms() override {
+    if ((p.wavemaker == NHW_WM_INT_SPC || p.wavemaker == NHW_WM_INT_IRR) && !S.njon) {
+      set_last_error("INT_SPC / INT_IRR: no spectrum yet (nhw_set_wave_spectrum)");
+      return NHW_ERR_STATE;
+    }
     if (S.wavemaker) L("source_area", [&] { k_single<T><<<1, 1, 0, st>>>(S, 0); });
     incols(OpSource{});
     return check();

@@ -285,15 +285,16 @@ class Scenario:
         _chk(load().nhw_set_time(self._h, time, dt, run_step), "nhw_set_time")
 
     def set_wave_spectrum(self, freq, dire, spc2d, phases=None):
-        """LEF_SPC's 2-D spectrum (nhw_set_wave_spectrum): spc2d and phases flat,
-        direction fastest, as read_spc2d returns them."""
+        """The 2-D spectrum of LEF_SPC / INT_SPC (densities, as read_spc2d
+        returns them) or INT_IRR (amplitudes and phases, as read_irr2d returns
+        them) for nhw_set_wave_spectrum: spc2d and phases flat, direction fastest."""
         f, d, s = (np.ascontiguousarray(a, dtype=np.float64) for a in (freq, dire, spc2d))
         ph = None if phases is None else np.ascontiguousarray(phases, dtype=np.float64)
         _chk(load().nhw_set_wave_spectrum(self._h, f.size, d.size, _ptr(f), _ptr(d), _ptr(s), _ptr(ph)),
              "nhw_set_wave_spectrum")
 
     def set_wave_phases(self, phases):
-        """Phases (radians) of the LEF_JON / LEF_TMA components (nhw_set_wave_phases)."""
+        """Phases (radians) of the LEF_JON / LEF_TMA / INT_JON / INT_TMA components (nhw_set_wave_phases)."""
         a = np.ascontiguousarray(phases, dtype=np.float64)
         _chk(load().nhw_set_wave_phases(self._h, a.size, _ptr(a)), "nhw_set_wave_phases")
 

@@ -14,12 +14,15 @@ import ctypes
 NHW_FP64 = 0
 NHW_FP32_IR = 1
 (WM_NONE, WM_INT_LIN, WM_INT_SOL, WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED,
- WM_LEF_TID, WM_RIG_LIN, WM_FLUX_LR, WM_LEF_JON, WM_LEF_TMA, WM_LEF_SPC) = range(15)
+ WM_LEF_TID, WM_RIG_LIN, WM_FLUX_LR, WM_LEF_JON, WM_LEF_TMA, WM_LEF_SPC, WM_INT_CON, WM_INT_JON, WM_INT_TMA,
+ WM_INT_SPC, WM_INT_IRR) = range(20)
 # fed through the west boundary (BC_X0 = 3)
 WM_LEF = (WM_LEF_LIN, WM_LEF_SOL, WM_LEF_STK, WM_LEF_CON, WM_WAV_CUR, WM_FOCUSED, WM_LEF_TID, WM_FLUX_LR,
           WM_LEF_JON, WM_LEF_TMA, WM_LEF_SPC)
 # fed through the east boundary (BC_Xn = 3)
 WM_EAST = (WM_RIG_LIN, WM_FLUX_LR)
+# internal source strips (src/source_terms.F)
+WM_INT = (WM_INT_LIN, WM_INT_SOL, WM_INT_CON, WM_INT_JON, WM_INT_TMA, WM_INT_SPC, WM_INT_IRR)
 WM_OTHER = -1   # a wavemaker of the reference outside this path (rejected by nhw_create)
 SLIDE_NONE, SLIDE_RIGID_3D = 0, 1
 DEPTH_CELL_CENTER, DEPTH_CELL_GRID = 0, 1
@@ -198,12 +201,13 @@ def read_input(path: str) -> NhwParams:
     dt_ = s("DEPTH_TYPE", "CELL_CENTER").upper()
     p.depth_type = DEPTH_CELL_GRID if dt_ == "CELL_GRID" else DEPTH_CELL_CENTER
     wm = s("WAVEMAKER", "NONE").upper()
-    # a generator of the reference that this path does not build (LEF_SPC,
-    # INT_IRR, ...) is kept as WM_OTHER and rejected, not run as NONE
+    # a generator of the reference that this path does not build is kept as
+    # WM_OTHER and rejected, not run as NONE
     known = {"NONE": WM_NONE, "INT_LIN": WM_INT_LIN, "INT_SOL": WM_INT_SOL, "LEF_LIN": WM_LEF_LIN,
              "LEF_SOL": WM_LEF_SOL, "LEF_STK": WM_LEF_STK, "LEF_CON": WM_LEF_CON, "WAV_CUR": WM_WAV_CUR,
              "FOCUSED": WM_FOCUSED, "LEF_TID": WM_LEF_TID, "RIG_LIN": WM_RIG_LIN, "FLUX_LR": WM_FLUX_LR,
-             "LEF_JON": WM_LEF_JON, "LEF_TMA": WM_LEF_TMA, "LEF_SPC": WM_LEF_SPC}
+             "LEF_JON": WM_LEF_JON, "LEF_TMA": WM_LEF_TMA, "LEF_SPC": WM_LEF_SPC, "INT_CON": WM_INT_CON,
+             "INT_JON": WM_INT_JON, "INT_TMA": WM_INT_TMA, "INT_SPC": WM_INT_SPC, "INT_IRR": WM_INT_IRR}
     p.wavemaker = known.get(wm[:7], WM_OTHER) if wm else WM_NONE
     if wm[:3] in ("LEF", "RIG", "INT", "FLU", "WAV"):
         p.amp_wave, p.per_wave, p.dep_wave = f("AMP", 0.0), f("PER", 1.0), f("DEP", 1.0)
@@ -260,6 +264,24 @@ def read_spc2d(path: str):
     return rest[:nf].copy(), rest[nf:nf + nd].copy(), rest[nf + nd:].copy()
 
 
+def read_irr2d(path: str):
+    """The component file of INT_IRR (src/initialize.F:835-876): NumFreq and
+    NumDir, then NumFreq frequencies, NumDir directions, the NumFreq x NumDir
+    component amplitudes and as many phases, direction fastest.  Returns
+    (freq, dire, amp, phases) as float64 arrays, amp and phases flat in that
+    order (as nhw_set_wave_spectrum takes them)."""
+    import numpy as np
+    with open(path) as fh:
+        vals = fh.read().split()
+    nf, nd = int(float(vals[0])), int(float(vals[1]))
+    n = nf + nd + 2 * nf * nd
+    rest = np.array([float(v) for v in vals[2:2 + n]])
+    if rest.size != n:
+        raise ValueError(f"{path}: expected {nf} + {nd} + 2 x {nf * nd} values after the counts")
+    a = nf + nd
+    return rest[:nf].copy(), rest[nf:a].copy(), rest[a:a + nf * nd].copy(), rest[a + nf * nd:].copy()
+
+
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
     if p.viscous_flow and (p.ivturb != 1 or p.ihturb != 1):
@@ -267,9 +289,10 @@ def unsupported_reason(p: NhwParams) -> str | None:
                 "IVTURB = IHTURB = 1, are on the GPU path; the k-epsilon and LES models are not)")
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
-    if p.wavemaker not in (WM_NONE, WM_INT_LIN, WM_INT_SOL) + WM_LEF + WM_EAST:
-        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, "
-                "LEF_TMA, LEF_SPC, WAV_CUR, FOCUSED, RIG_LIN and FLUX_LR are on the GPU path)")
+    if p.wavemaker not in (WM_NONE,) + WM_INT + WM_LEF + WM_EAST:
+        return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, INT_CON, INT_JON, INT_TMA, INT_SPC, INT_IRR, LEF_LIN, "
+                "LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, LEF_TMA, LEF_SPC, WAV_CUR, FOCUSED, RIG_LIN and "
+                "FLUX_LR are on the GPU path)")
     if p.bc_x0 == 3 and p.wavemaker not in WM_LEF:
         return ("BC_X0=3 needs a LEF_LIN, LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, LEF_TMA, LEF_SPC, WAV_CUR, "
                 "FOCUSED or FLUX_LR wavemaker")
@@ -298,6 +321,7 @@ __all__ = [
     "NHW_FP64", "NHW_FP32_IR", "WM_NONE", "WM_INT_LIN", "WM_INT_SOL", "WM_LEF_LIN", "WM_LEF_SOL",
     "WM_LEF_STK", "WM_LEF_CON", "WM_WAV_CUR", "WM_FOCUSED", "WM_LEF_TID", "WM_LEF",
     "WM_RIG_LIN", "WM_FLUX_LR", "WM_LEF_JON", "WM_LEF_TMA", "WM_LEF_SPC", "WM_EAST", "read_spc2d",
+    "WM_INT_CON", "WM_INT_JON", "WM_INT_TMA", "WM_INT_SPC", "WM_INT_IRR", "WM_INT", "read_irr2d",
     "WM_OTHER",
     "SLIDE_NONE",
     "SLIDE_RIGID_3D", "DEPTH_CELL_CENTER", "DEPTH_CELL_GRID",

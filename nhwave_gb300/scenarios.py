@@ -196,6 +196,47 @@ def spc_spectrum(nf: int = 8, nd: int = 3, hm0: float = 0.03, fp: float = 0.7, s
     return freq, dire, spc.ravel()
 
 
+# ------------------------------------------------- internal sources
+def internal_flume(kind: str = "CON", M=64, N=16, K=5, dx=0.1, dy=0.25, depth=0.5, amp=0.1, per=3.0, **kw):
+    """Flat basin with an internal source strip across it at x = 3.0-3.2 m
+    and 1.5 m sponges at both ends, walls along the sides, at rest: a
+    cnoidal wave (INT_CON, height `amp`, period `per`), the components of a
+    JONSWAP or TMA spectrum (INT_JON / INT_TMA: Hm0 3 cm, Tp 1.5 s, 24
+    components over 0.4-1.2 Hz), or of a 2-D spectrum (INT_SPC, densities)
+    or of given amplitudes and phases (INT_IRR), both passed with
+    set_wave_spectrum.  The channel, 4 m wide, repeats cross-channel wave
+    numbers of 2 pi / 4 m, to which the spectral makers snap their
+    directions."""
+    from .params import WM_INT_CON, WM_INT_IRR, WM_INT_JON, WM_INT_SPC, WM_INT_TMA
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.1 * dx / math.sqrt(GRAV * depth),
+                       dt_min=1e-8, dt_max=1.0, cfl=0.5, min_dep=0.001, non_hydro=1, time_order=3,
+                       tol=1e-8, itmax=1000, total_time=20.0)
+    p.wavemaker = {"CON": WM_INT_CON, "JON": WM_INT_JON, "TMA": WM_INT_TMA, "SPC": WM_INT_SPC,
+                   "IRR": WM_INT_IRR}[kind]
+    p.amp_wave, p.per_wave, p.dep_wave, p.theta_wave = amp, per, depth, 0.0
+    p.xsource_west, p.xsource_east = 3.0, 3.2
+    p.ysource_suth, p.ysource_nrth = 0.0, N * dy
+    if kind in ("JON", "TMA"):
+        p.hm0, p.tp, p.freq_min, p.freq_max, p.numfreq, p.wave_seed = 0.03, 1.5, 0.4, 1.2, 24, 11
+    p.sponge_on = 1
+    p.sponge_west_width = p.sponge_east_width = 1.5
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, np.full(M * N, depth), None, None
+
+
+def irr_components(nf: int = 6, nd: int = 4, amp: float = 0.004, seed: int = 5):
+    """Component data of INT_IRR in irr2d.txt's order: nf frequencies over
+    0.5-1.2 Hz, nd directions over -30..30 degrees, amplitudes (`amp` over
+    the component count, tapered across the band) and seeded phases, flat
+    with direction fastest."""
+    rng = np.random.default_rng(seed)
+    freq = np.linspace(0.5, 1.2, nf)
+    dire = np.linspace(-30.0, 30.0, nd)
+    a = amp / (nf * nd) * np.outer(np.hanning(nf + 2)[1:-1], np.ones(nd)) * 4.0
+    return freq, dire, a.ravel(), rng.uniform(0.0, 2.0 * np.pi, nf * nd)
+
+
 # ------------------------------------------------------- east inflows
 def east_flume(kind: str = "RIG", M=64, N=4, K=5, dx=0.1, dy=0.1, depth=0.5, amp=0.02, per=1.5, **kw):
     """Flumes whose east side is open to a boundary condition (BC_Xn = 3).
@@ -305,6 +346,11 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         # directional irregular waves from a 2-D spectrum (LEF_SPC; the spectrum itself is
         # scenarios.spc_spectrum(), passed with set_wave_spectrum); 8 cross-channel rows
         out = wave_flume("SPC", M=64, N=8, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
+    elif name in ("tiny_int_con", "tiny_int_jon", "tiny_int_tma", "tiny_int_spc", "tiny_int_irr"):
+        # the internal source strip of each spectral or cnoidal maker; INT_SPC's spectrum is
+        # spc_spectrum(8, 5, spread_deg=30), INT_IRR's components irr_components()
+        amp = 0.1 if name.endswith("con") else 0.0
+        out = internal_flume(name[-3:].upper(), amp=amp, **kw)
     elif name == "tiny_flume_rig":
         # a linear wave given to the east side (RIG_LIN through BC_Xn = 3), wall and sponge at the west
         out = east_flume("RIG", **kw)

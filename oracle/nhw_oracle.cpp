@@ -117,10 +117,11 @@ double cnoidal_ce(double mod) {
   return ck * (1.0 - sum);
 }
 // cnoidal (src/waves.F:184-220): Newton iteration for m from 0.99999999,
-// then the wave length l and the trough level x2 (c, the celerity, is unused
-// by the boundary).  False when m leaves (0, 1], where the reference's
-// square roots turn to NaN.
-bool cnoidal(double height, double depth, double period, double& l, double& x2, double& mod) {
+// then the wave length l, the trough level x2 and, when asked for, the
+// celerity c (the boundary does not use it; INT_CON does).  False when m
+// leaves (0, 1], where the reference's square roots turn to NaN.
+bool cnoidal(double height, double depth, double period, double& l, double& x2, double& mod,
+             double* c = nullptr) {
   mod = 0.99999999;
   int n = 0;
   while (true) {
@@ -140,6 +141,8 @@ bool cnoidal(double height, double depth, double period, double& l, double& x2, 
   }
   if (!(mod > 0.0 && mod <= 1.0)) return false;
   l = 4.0 * cnoidal_ck(mod) * depth * std::sqrt(mod * depth / height / 3.0);
+  const double xtemp = -mod + 2.0 - 3.0 * cnoidal_ce(mod) / cnoidal_ck(mod);
+  if (c) *c = std::sqrt(Grav * depth * (1.0 + height / depth / mod * xtemp));
   x2 = height / mod * (1.0 - mod - cnoidal_ce(mod) / cnoidal_ck(mod));
   return std::isfinite(l) && std::isfinite(x2);
 }
@@ -244,13 +247,15 @@ struct Model {
     const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_TID) ||
                      p.wavemaker == NHW_WM_FLUX_LR || p.wavemaker == NHW_WM_LEF_JON ||
                      p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
-    if ((p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) &&
-        (!(p.hm0 > 0) || !(p.tp > 0) || !(p.freq_min > 0) || !(p.freq_max > p.freq_min) || p.numfreq < 1 ||
-         p.numfreq > 500 || !(p.dep_wave > 0)))
+    const bool jon = p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA ||
+                     p.wavemaker == NHW_WM_INT_JON || p.wavemaker == NHW_WM_INT_TMA;
+    if (jon && (!(p.hm0 > 0) || !(p.tp > 0) || !(p.freq_min > 0) || !(p.freq_max > p.freq_min) || p.numfreq < 1 ||
+                p.numfreq > 500 || !(p.dep_wave > 0)))
       return NHW_ERR_ARG;
+    if ((p.wavemaker == NHW_WM_INT_SPC || p.wavemaker == NHW_WM_INT_IRR) && !(p.dep_wave > 0)) return NHW_ERR_ARG;
     if (!(p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5 || (p.bc_x0 == 3 && lef))) return NHW_ERR_UNSUPPORTED;
     if (p.wavemaker == NHW_WM_FLUX_LR && !(p.zob > 0.0)) return NHW_ERR_ARG;
-    if (p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA) jonswap_spectrum();
+    if (jon) jonswap_spectrum();
     if (p.wavemaker == NHW_WM_FOCUSED) {   // components (src/initialize.F:742-781)
       if (p.nwave < 2 || p.nwave > 12000 || !(p.f_center > 0) || !(p.depth_comp > 0)) return NHW_ERR_ARG;
       const int nw = p.nwave;
@@ -278,7 +283,7 @@ struct Model {
       for (int n = 0; n < nw; ++n)
         Amp_i[n] = p.component_amp_type == 1 ? p.slope_group / nw / p.k_center : p.slope_group / nw / k_i[n];
     }
-    if (p.wavemaker == NHW_WM_LEF_CON) {   // the reference stops when these fail
+    if (p.wavemaker == NHW_WM_LEF_CON || p.wavemaker == NHW_WM_INT_CON) {   // the reference stops when these fail
       double l, x2, m, xs;
       if (!(p.amp_wave > 0) || !cnoidal(p.amp_wave, p.dep_wave, p.per_wave, l, x2, m) ||
           !cnoidal_start(x2, m, xs))
@@ -727,7 +732,7 @@ struct Model {
       const double s2 = F < Freq_Peak ? sa * sa : sb * sb;
       Jon_Spc[i - 1] = (Grav * Grav) / ((F * F) * (F * F) * F) * std::exp(-1.25 * ((r * r) * (r * r))) *
                        std::pow(gam, std::exp(-0.5 * ((F / Freq_Peak - 1.0) * (F / Freq_Peak - 1.0)) / s2));
-      if (p.wavemaker == NHW_WM_LEF_TMA) {
+      if (p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_INT_TMA) {
         const double th = std::tanh(Wave_Number * Dep_Wave);
         Jon_Spc[i - 1] = Jon_Spc[i - 1] * (th * th) /
                          (1.0 + 2 * Wave_Number * Dep_Wave / std::sinh(2. * Wave_Number * Dep_Wave));
@@ -1139,6 +1144,101 @@ struct Model {
     return Source_Area;
   }
 
+  // The direction of an internal maker's component snapped to one that the
+  // channel width repeats (src/source_terms.F:94-136 for INT_SPC, 203-247 for
+  // INT_IRR, which keeps a zero direction).  The reference's search has no
+  // bound; a direction beyond 90 degrees never ends it, and is refused here
+  // (false).
+  bool snap_angle(double& Angle, double Wave_Number, bool irr) const {
+    const double width = p.Nglob * dy;
+    const long kMax = 10000000;
+    double tmp1 = Wave_Number, tmp2, tmp3, tmp4;
+    long nk = 0;
+    if (Angle > Zero) {
+      tmp3 = Zero;
+      while (tmp3 < Angle) {
+        nk = nk + 1;
+        if (nk > kMax) return false;
+        tmp2 = nk * 2.0 * pi / width;
+        if (tmp2 >= tmp1) tmp3 = 0.5 * pi - Small;
+        else tmp3 = std::asin(tmp2 / tmp1);
+      }
+      tmp4 = std::asin((nk - 1) * 2.0 * pi / width / tmp1);
+      if (std::fabs(tmp4 - Angle) < std::fabs(Angle - tmp3)) Angle = tmp4;
+      else Angle = tmp3;
+    } else if (!irr || Angle < Zero) {
+      tmp3 = Zero;
+      while (tmp3 > Angle) {
+        nk = nk + 1;
+        if (nk > kMax) return false;
+        tmp2 = nk * 2.0 * pi / width;
+        if (tmp2 >= tmp1) tmp3 = -0.5 * pi + Small;
+        else tmp3 = -std::asin(tmp2 / tmp1);
+      }
+      tmp4 = std::asin((nk - 1) * 2.0 * pi / width / tmp1);
+      if (std::fabs(tmp4 - Angle) < std::fabs(Angle - tmp3)) Angle = tmp4;
+      else Angle = tmp3;
+    } else {
+      Angle = 0.0;
+    }
+    return true;
+  }
+
+  // INT_SPC (src/source_terms.F:71-191) and INT_IRR (:194-302); INT_IRR's
+  // eta_mean is never read by the reference (a zero module variable)
+  bool internal_spectral_source() {
+    const bool irr = p.wavemaker == NHW_WM_INT_IRR;
+    const int NumFreq = NumFreq_s, NumDir = NumDir_s;
+    const double eta_mean = 0.0;
+    const double Source_Area = source_area();
+    auto at = [&](int nd, int nfq) { return (nd - 1) + NumDir * (nfq - 1); };
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) {
+        SourceC(i, j) = Zero;
+        if (!(xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+              yc(j) <= p.ysource_nrth))
+          continue;
+        for (int nfreq = 1; nfreq <= NumFreq; ++nfreq)
+          for (int ndir = 1; ndir <= NumDir; ++ndir) {
+            const double Per_Wave = 1.0 / Freq_s[nfreq - 1];
+            const double Segma = 2.0 * pi / Per_Wave;
+            const double Wave_Number = wave_dispersion(Segma);
+            const double Wave_Length = 2.0 * pi / Wave_Number;
+            const double Celerity = Wave_Length / Per_Wave;
+            double Angle = Dire_s[ndir - 1] * pi / 180.;
+            if (!snap_angle(Angle, Wave_Number, irr)) return false;
+            const double WnumY = Wave_Number * std::sin(Angle);
+            const double Phs_lag = (dy / 2.0 + yc(j)) * WnumY;
+            const double ph = Random_Phs[at(ndir, nfreq)];
+            if (irr) {
+              const double Amp_Wave = 2.0 * Spc2d[at(ndir, nfreq)];
+              if (nfreq == 1)
+                SourceC(i, j) = SourceC(i, j) + 2 * Celerity / Source_Area *
+                                                    (Amp_Wave / 2 * std::cos(pi / 2 - Segma * TIME + Phs_lag + ph) +
+                                                     eta_mean);
+              else
+                SourceC(i, j) = SourceC(i, j) + Celerity * Amp_Wave / Source_Area *
+                                                    std::cos(pi / 2 - Segma * TIME + Phs_lag + ph);
+            } else {
+              double dfreq;
+              if (nfreq == 1) dfreq = Freq_s[1] - Freq_s[0];
+              else if (nfreq == NumFreq) dfreq = Freq_s[NumFreq - 1] - Freq_s[NumFreq - 2];
+              else dfreq = 0.5 * (Freq_s[nfreq] - Freq_s[nfreq - 2]);
+              dfreq = std::fabs(dfreq);
+              double ddir;
+              if (ndir == 1) ddir = Dire_s[1] - Dire_s[0];
+              else if (ndir == NumDir) ddir = Dire_s[NumDir - 1] - Dire_s[NumDir - 2];
+              else ddir = 0.5 * (Dire_s[ndir] - Dire_s[ndir - 2]);
+              ddir = std::fabs(ddir);
+              const double Amp_Wave = 2.0 * std::sqrt(2.0 * Spc2d[at(ndir, nfreq)] * ddir * dfreq);
+              SourceC(i, j) = SourceC(i, j) + Celerity * Amp_Wave / Source_Area *
+                                                  std::cos(pi / 2 - Segma * TIME + Phs_lag + ph);
+            }
+          }
+      }
+    return true;
+  }
+
   void source_terms() {
     if (p.wavemaker == NHW_WM_INT_LIN) {
       const double Segma = 2.0 * pi / p.per_wave;
@@ -1166,6 +1266,42 @@ struct Model {
               yc(j) <= p.ysource_nrth) {
             double ch = std::cosh(Atmp * (Xstart - Celerity * TIME));
             SourceC(i, j) = 2.0 * Celerity / Source_Area * A / (ch * ch);
+          }
+    } else if (p.wavemaker == NHW_WM_INT_SPC || p.wavemaker == NHW_WM_INT_IRR) {
+      if (!internal_spectral_source()) status = NHW_ERR_ARG;
+    } else if (p.wavemaker == NHW_WM_INT_JON || p.wavemaker == NHW_WM_INT_TMA) {
+      // src/source_terms.F:305-340
+      const double Source_Area = source_area();
+      const double DFreq = (p.freq_max - p.freq_min) / (double)(float)p.numfreq;
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          SourceC(i, j) = Zero;
+          if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+              yc(j) <= p.ysource_nrth)
+            for (int nfreq = 1; nfreq <= p.numfreq; ++nfreq) {
+              const double Per_Wave = 1.0 / Freq[nfreq - 1];
+              const double Segma = 2.0 * pi / Per_Wave;
+              const double Wave_Number = wave_dispersion(Segma);
+              const double Wave_Length = 2.0 * pi / Wave_Number;
+              const double Celerity = Wave_Length / Per_Wave;
+              const double Amp_Wave = 2.0 * std::sqrt(2.0 * Jon_Spc[nfreq - 1] * DFreq);
+              SourceC(i, j) = SourceC(i, j) + Celerity * Amp_Wave / Source_Area *
+                                                  std::cos(pi / 2 - Segma * TIME + RanPhs[nfreq - 1]);
+            }
+        }
+    } else if (p.wavemaker == NHW_WM_INT_CON) {
+      // src/source_terms.F:343-395
+      double Wave_Length = 0, Ytrough = 0, Mod1 = 0, Celerity = 0, Xstart = 0;
+      cnoidal(p.amp_wave, p.dep_wave, p.per_wave, Wave_Length, Ytrough, Mod1, &Celerity);
+      cnoidal_start(Ytrough, Mod1, Xstart);
+      const double Source_Area = source_area();
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+              yc(j) <= p.ysource_nrth) {
+            const double cn = cnoidal_cn(Xstart * 0.5 * cnoidal_ck(Mod1) +
+                                             2.0 * cnoidal_ck(Mod1) * (-(TIME / p.per_wave)), Mod1);
+            SourceC(i, j) = 2.0 * Celerity / Source_Area * (Ytrough + p.amp_wave * (cn * cn));
           }
     }
     for (int j = Jbeg; j <= Jend; ++j)
@@ -2729,11 +2865,19 @@ int orc_set_wave_phases(void* o, int n, const double* phases) {
   for (int i = 0; i < n; ++i) m->RanPhs[i] = phases[i];
   return NHW_OK;
 }
-// LEF_SPC's spectrum, as nhw_set_wave_spectrum takes it
+// The 2-D spectrum of LEF_SPC / INT_SPC (densities) or INT_IRR (amplitudes
+// and their phases), as nhw_set_wave_spectrum takes it
 int orc_set_wave_spectrum(void* o, int nf, int nd, const double* freq, const double* dire, const double* spc,
                           const double* phases) {
   Model* m = static_cast<Model*>(o);
-  if (m->p.wavemaker != NHW_WM_LEF_SPC || nf < 2 || nd < 2 || !freq || !dire || !spc) return NHW_ERR_ARG;
+  const int wm = m->p.wavemaker;
+  if ((wm != NHW_WM_LEF_SPC && wm != NHW_WM_INT_SPC && wm != NHW_WM_INT_IRR) || nf < 2 || nd < 2 || !freq ||
+      !dire || !spc)
+    return NHW_ERR_ARG;
+  if (wm == NHW_WM_INT_IRR && !phases) return NHW_ERR_ARG;   // irr2d.txt holds them
+  if (wm != NHW_WM_LEF_SPC)   // the internal makers' direction search ends only within 90 degrees
+    for (int q = 0; q < nd; ++q)
+      if (!(std::fabs(dire[q]) <= 90.0)) return NHW_ERR_ARG;
   m->NumFreq_s = nf;
   m->NumDir_s = nd;
   m->Freq_s.assign(freq, freq + nf);

@@ -187,7 +187,9 @@ class Oracle:
         self._spc = (f, d, s, None if phases is None else np.ascontiguousarray(phases, dtype=np.float64))
         rc = lib().orc_set_wave_spectrum(self._h, f.size, d.size, _ptr(f), _ptr(d), _ptr(s), _ptr(self._spc[3]))
         if rc:
-            raise ValueError("set_wave_spectrum: not a LEF_SPC scenario, or fewer than 2 frequencies / directions")
+            raise ValueError("set_wave_spectrum: not a LEF_SPC / INT_SPC / INT_IRR scenario, fewer than 2 "
+                             "frequencies / directions, an internal maker's direction beyond 90 degrees, or "
+                             "INT_IRR without phases")
 
     def inflow_eta(self) -> np.ndarray:
         """Ein_X0 of the last update_wave_bc (all Nloc rows)."""

@@ -243,6 +243,7 @@ def test_golden_fixtures(name, gpu_lib):
 # FLUX_LR current (BC_Xn = 3)
 FLUMES = ["tiny_flume_lin", "tiny_flume_sol", "tiny_flume_stk", "tiny_flume_con", "tiny_flume_open", "tiny_flume_cur",
           "tiny_flume_foc", "tiny_flume_tid", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon", "tiny_flume_tma",
+          "tiny_int_con", "tiny_int_jon", "tiny_int_tma",
           "tiny_fric_log"]   # and the friction law from a roughness height: log() of CUDA and libm
 
 
@@ -382,3 +383,67 @@ def test_spectral_inflow_steps(precision, oracle_mod, gpu_lib):
     # directional: the cross-channel velocity is not zero
     assert np.abs(o.get(F.V)[sl(F.V)]).max() > 1e-5
     g.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("kind", ["spc", "irr"])
+def test_internal_spectral_source_steps(kind, precision, oracle_mod, gpu_lib):
+    """INT_SPC / INT_IRR: the internal source strip fed by a 2-D spectrum (or
+    INT_IRR's amplitudes and phases) passed with nhw_set_wave_spectrum, the
+    directions snapped to ones the 4 m channel repeats; FP64 within 1e-9 of
+    the oracle (cos of CUDA and libm), FP32+IR eta within 1e-6.  Before a
+    spectrum is given, source_terms refuses to run; a direction beyond 90
+    degrees is refused."""
+    from nhwave_gb300 import fields as F, lib, scenarios as S
+    g, o = _pair(f"tiny_int_{kind}", oracle_mod, precision=precision, tol=STEP_TOL if precision == 0 else 1e-10)
+    with pytest.raises(lib.NhwError):
+        g.source_terms()
+    if kind == "spc":
+        freq, dire, spc = S.spc_spectrum(8, 5, spread_deg=30.0)
+        ph = None
+        with pytest.raises(lib.NhwError):
+            g.set_wave_spectrum(freq, np.array([-30.0, 0.0, 95.0, 10.0, 20.0]), spc)
+    else:
+        freq, dire, spc, ph = S.irr_components()
+        with pytest.raises(lib.NhwError):   # INT_IRR's phases are part of its data
+            g.set_wave_spectrum(freq, dire, spc)
+    g.set_wave_spectrum(freq, dire, spc, ph)
+    o.set_wave_spectrum(freq, dire, spc, ph)
+    for n in range(20):
+        assert g.step() == 0 and o.step() == 0
+        assert np.array_equal(g.get(F.MASK), o.get(F.MASK)), f"mask differs after step {n}"
+    sl = o.shape.interior
+    if precision == 0:
+        for f in ("ETA", "P"):
+            fid = getattr(F, f)
+            r = rel_l2(g.get(fid)[sl(fid)], o.get(fid)[sl(fid)])
+            assert r < 1e-9, f"INT_{kind.upper()} {f}: rel L2 {r:.3e}"
+        for f in ("U", "V", "W"):
+            r = vel_err(g, o, f)
+            assert r < 1e-9, f"INT_{kind.upper()} {f}: {r:.3e}"
+        r = rel_l2(g.get(F.SOURCEC)[sl(F.SOURCEC)], o.get(F.SOURCEC)[sl(F.SOURCEC)])
+        assert r < 1e-10, f"INT_{kind.upper()} SourceC: rel L2 {r:.3e}"
+    else:
+        r = rel_l2(g.get(F.ETA)[sl(F.ETA)], o.get(F.ETA)[sl(F.ETA)])
+        assert r < 1e-6, f"INT_{kind.upper()} FP32+IR eta rel L2 {r:.3e}"
+    # the snapped directions give a cross-channel flow
+    assert np.abs(o.get(F.V)[sl(F.V)]).max() > 1e-6
+    g.close()
+
+
+def test_internal_jonswap_phases_given_by_the_driver(oracle_mod, gpu_lib):
+    """nhw_set_wave_phases on INT_JON: GPU and oracle, given the same phases,
+    step alike, and differently from the seeded run."""
+    from nhwave_gb300 import fields as F
+    g, o = _pair("tiny_int_jon", oracle_mod)
+    g2, _ = _pair("tiny_int_jon", oracle_mod)
+    ph = np.random.default_rng(8).uniform(0.0, 2.0 * np.pi, g.params.numfreq)
+    g.set_wave_phases(ph)
+    o.set_wave_phases(ph)
+    for _ in range(10):
+        assert g.step() == 0 and o.step() == 0 and g2.step() == 0
+    sl = o.shape.interior(F.ETA)
+    assert rel_l2(g.get(F.ETA)[sl], o.get(F.ETA)[sl]) < 1e-9
+    assert rel_l2(g2.get(F.ETA)[sl], o.get(F.ETA)[sl]) > 1e-3
+    g.close()
+    g2.close()

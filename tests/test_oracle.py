@@ -620,3 +620,151 @@ def test_spectral_inflow_follows_the_component_sum(oracle_mod):
             want = math.tanh(t / 20.0) * float(
                 (0.5 * wh * np.cos(pi / 2 - (2.0 * pi * freq)[:, None] * t + lag)).sum())
             assert got[j] == pytest.approx(want, rel=1e-11, abs=1e-14)
+
+
+def _snap(angle, k, width, irr):
+    """The internal makers' direction search (src/source_terms.F:94-136,
+    203-247), restated: the nearest direction whose cross-channel wave number
+    n 2 pi / width the channel repeats."""
+    pi, small = _pi_sp(), float(np.float32(1.0e-16))
+
+    def search(sign):
+        tmp3, nk = 0.0, 0
+        while (tmp3 < angle) if sign > 0 else (tmp3 > angle):
+            nk += 1
+            tmp2 = nk * 2.0 * pi / width
+            tmp3 = sign * (0.5 * pi - small) if tmp2 >= k else sign * math.asin(tmp2 / k)
+        arg = (nk - 1) * 2.0 * pi / width / k
+        tmp4 = math.asin(arg) if abs(arg) <= 1.0 else float("nan")
+        return tmp4 if abs(tmp4 - angle) < abs(angle - tmp3) else tmp3
+    if angle > 0.0:
+        return search(1)
+    if angle < 0.0 or not irr:
+        return search(-1)
+    return 0.0
+
+
+@pytest.mark.parametrize("kind", ["spc", "irr"])
+def test_internal_spectral_source_is_the_component_sum(kind, oracle_mod):
+    """INT_SPC / INT_IRR (src/source_terms.F:71-302): in every cell of the
+    source strip, SourceC = sum over components of C A / Source_Area cos(pi/2
+    - sigma t + (dy/2 + yc_j) k sin(theta) + phase), theta the direction
+    snapped to one the 4 m channel repeats, C = sigma / k, A = 2 sqrt(2 S
+    ddir df) (INT_SPC) or 2 a (INT_IRR, whose first frequency takes the form
+    2 C / Source_Area (A/2 cos + eta_mean), eta_mean = 0); restated here in
+    numpy, and zero outside the strip."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make(f"tiny_int_{kind}")
+    o = oracle_mod.Oracle(p, d, e, u)
+    if kind == "spc":
+        freq, dire, spc = S.spc_spectrum(8, 5, spread_deg=30.0)
+        ph = np.random.default_rng(3).uniform(0.0, 2.0 * np.pi, spc.size)
+    else:
+        freq, dire, spc, ph = S.irr_components()
+    o.set_wave_spectrum(freq, dire, spc, ph)
+    pi = _pi_sp()
+
+    def widths(a):
+        w = np.empty_like(a)
+        w[0], w[-1] = a[1] - a[0], a[-1] - a[-2]
+        w[1:-1] = 0.5 * (a[2:] - a[:-2])
+        return np.abs(w)
+    nf, nd = freq.size, dire.size
+    sig = 2.0 * pi / (1.0 / freq)
+    kw = np.array([oracle_mod.lib().orc_wave_number(o._h, s) for s in sig])
+    cel = (2.0 * pi / kw) / (1.0 / freq)
+    if kind == "spc":
+        amp = 2.0 * np.sqrt(2.0 * spc.reshape(nf, nd) * np.outer(widths(freq), widths(dire)))
+    else:
+        amp = 2.0 * spc.reshape(nf, nd)
+    width = p.Nglob * p.dy
+    th = np.array([[_snap(dd * pi / 180.0, kk, width, kind == "irr") for dd in dire] for kk in kw])
+    # some directions snap to a non-zero cross-channel wave number that the channel repeats
+    ky = kw[:, None] * np.sin(th)
+    assert np.any(np.abs(ky) > 1.0)
+    nz = np.abs(ky) > 1e-12
+    assert np.allclose((ky[nz] / (2.0 * pi / width)), np.round(ky[nz] / (2.0 * pi / width)), atol=1e-9)
+    xc, yc = o.grid(1), o.grid(3)
+    D = o.get(F.D)
+    strip = [i for i in range(2, 2 + p.Mglob) if p.xsource_west <= xc[i] <= p.xsource_east]
+    assert strip
+    area = sum(p.dx * D[3, i] for i in strip)   # Source_Area: row Jbeg + 1
+    for t in (0.7, 4.25):
+        o.set_time(t, 0.01, 1)
+        o.source_terms()
+        got = o.get(F.SOURCEC)
+        for j in (2, 9, 17):
+            arg = pi / 2 - sig[:, None] * t + (p.dy / 2.0 + yc[j]) * ky + ph.reshape(nf, nd)
+            want = float((cel[:, None] * amp / area * np.cos(arg)).sum())
+            for i in strip:
+                assert got[j, i] == pytest.approx(want, rel=1e-10, abs=1e-12)
+        assert np.all(got[2:-2, [i for i in range(2, 2 + p.Mglob) if i not in strip]] == 0.0)
+
+
+@pytest.mark.parametrize("kind", ["jon", "tma"])
+def test_internal_jonswap_source_is_the_component_sum(kind, oracle_mod):
+    """INT_JON / INT_TMA (src/source_terms.F:305-340): SourceC = sum over the
+    NumFreq components of C A / Source_Area cos(pi/2 - sigma t + phase),
+    A = 2 sqrt(2 S DFreq), S the JONSWAP (TMA) spectrum at the band centres
+    scaled to Hm0^2/16 -- restated here in numpy, with the phases given."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make(f"tiny_int_{kind}")
+    o = oracle_mod.Oracle(p, d, e, u)
+    nf = p.numfreq
+    ph = np.random.default_rng(4).uniform(0.0, 2.0 * np.pi, nf)
+    o.set_wave_phases(ph)
+    pi, g = _pi_sp(), float(np.float32(9.81))
+    df = (p.freq_max - p.freq_min) / nf
+    f = p.freq_min + 0.5 * df + np.arange(nf) * df
+    fp = 1.0 / p.tp
+    s2 = np.where(f < fp, float(np.float32(0.07)) ** 2, float(np.float32(0.09)) ** 2)
+    spec = g * g / f ** 5 * np.exp(-1.25 * (fp / f) ** 4) * float(np.float32(3.3)) ** np.exp(
+        -0.5 * (f / fp - 1.0) ** 2 / s2)
+    sig = 2.0 * pi / (1.0 / f)
+    kw = np.array([oracle_mod.lib().orc_wave_number(o._h, s) for s in sig])
+    if kind == "tma":
+        h = p.dep_wave
+        spec = spec * np.tanh(kw * h) ** 2 / (1.0 + 2 * kw * h / np.sinh(2.0 * kw * h))
+    spec *= p.hm0 ** 2 / 16.0 / (spec * df).sum()
+    dfreq = (p.freq_max - p.freq_min) / float(np.float32(nf))   # DFreq = (Freq_Max - Freq_Min) / float(NumFreq)
+    amp = 2.0 * np.sqrt(2.0 * spec * dfreq)
+    cel = (2.0 * pi / kw) / (1.0 / f)
+    xc = o.grid(1)
+    D = o.get(F.D)
+    strip = [i for i in range(2, 2 + p.Mglob) if p.xsource_west <= xc[i] <= p.xsource_east]
+    area = sum(p.dx * D[3, i] for i in strip)
+    for t in (1.3, 9.7):
+        o.set_time(t, 0.01, 1)
+        o.source_terms()
+        got = o.get(F.SOURCEC)
+        want = float((cel * amp / area * np.cos(pi / 2 - sig * t + ph)).sum())
+        for j in (2, 11):
+            for i in strip:
+                assert got[j, i] == pytest.approx(want, rel=1e-9, abs=1e-12)
+
+
+def test_internal_cnoidal_source_has_zero_mean_over_a_period(oracle_mod):
+    """INT_CON (src/source_terms.F:343-395): SourceC = 2 C / Source_Area
+    (Ytrough + H cn^2(...)), and Ytrough puts the cnoidal profile's mean at
+    zero, so over one period the source adds no volume: its mean over 400
+    samples of a period is below 1e-3 of its peak; and its peak-to-trough
+    range is 2 C H / Source_Area."""
+    from nhwave_gb300 import fields as F, scenarios as S
+    p, d, e, u = S.make("tiny_int_con")
+    o = oracle_mod.Oracle(p, d, e, u)
+    xc = o.grid(1)
+    i = next(i for i in range(2, 2 + p.Mglob) if p.xsource_west <= xc[i] <= p.xsource_east)
+    vals = []
+    for n in range(400):
+        o.set_time(p.per_wave * n / 400.0, 0.01, 1)
+        o.source_terms()
+        vals.append(o.get(F.SOURCEC)[5, i])
+    vals = np.array(vals)
+    assert abs(vals.mean()) < 1e-3 * np.abs(vals).max()
+    D = o.get(F.D)
+    strip = [q for q in range(2, 2 + p.Mglob) if p.xsource_west <= xc[q] <= p.xsource_east]
+    area = sum(p.dx * D[3, q] for q in strip)
+    # the cnoidal celerity lies between the shallow-water speeds of the trough and crest depths
+    c_est = (vals.max() - vals.min()) * area / (2.0 * p.amp_wave)
+    g = float(np.float32(9.81))
+    assert math.sqrt(g * (p.dep_wave - p.amp_wave)) < c_est < math.sqrt(g * (p.dep_wave + p.amp_wave))

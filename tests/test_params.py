@@ -81,10 +81,16 @@ def test_out_of_scope_reason(tmp_path):
     f.write_text(SAMPLE.replace("BC_Z0 = 1", "BC_Z0 = 5"))
     p = P.read_input(str(f))
     assert p.bc_z0 == 5 and P.unsupported_reason(p) is None
-    # a generator of the reference that the path does not build is rejected, not run as NONE
-    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = INT_IRR"))
+    # a generator name the reference does not know either is rejected, not run as NONE
+    f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = INT_XYZ"))
     p = P.read_input(str(f))
     assert p.wavemaker == P.WM_OTHER and "WAVEMAKER" in P.unsupported_reason(p)
+    # every internal maker of the reference is on the path (src/source_terms.F)
+    for name, wm in (("INT_CON", P.WM_INT_CON), ("INT_JON", P.WM_INT_JON), ("INT_TMA", P.WM_INT_TMA),
+                     ("INT_SPC", P.WM_INT_SPC), ("INT_IRR", P.WM_INT_IRR)):
+        f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = " + name))
+        p = P.read_input(str(f))
+        assert p.wavemaker == wm and P.unsupported_reason(p) is None, name
     # the cnoidal, Stokes and JONSWAP boundary waves are on the path, through BC_X0 = 3
     for name, wm in (("LEF_CON", P.WM_LEF_CON), ("LEF_STK", P.WM_LEF_STK), ("LEF_JON", P.WM_LEF_JON)):
         f.write_text(SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = " + name))
@@ -92,6 +98,22 @@ def test_out_of_scope_reason(tmp_path):
         assert p.wavemaker == wm
         p.bc_x0 = 3
         assert P.unsupported_reason(p) is None
+
+
+def test_irr2d_reader(tmp_path):
+    """irr2d.txt (src/initialize.F:835-876): counts, frequencies, directions,
+    then amplitudes and phases, direction fastest."""
+    import numpy as np
+    from nhwave_gb300 import params as P
+    f = tmp_path / "irr2d.txt"
+    vals = [2, 3, 0.5, 0.8, -10.0, 0.0, 10.0] + [0.001 * q for q in range(6)] + [0.1 * q for q in range(6)]
+    f.write_text("\n".join(str(v) for v in vals))
+    freq, dire, amp, ph = P.read_irr2d(str(f))
+    assert list(freq) == [0.5, 0.8] and list(dire) == [-10.0, 0.0, 10.0]
+    assert np.allclose(amp, [0.001 * q for q in range(6)]) and np.allclose(ph, [0.1 * q for q in range(6)])
+    f.write_text("\n".join(str(v) for v in vals[:-1]))
+    with pytest.raises(ValueError):
+        P.read_irr2d(str(f))
 
 
 def test_reference_example_inputs_where_present():
