@@ -130,7 +130,15 @@ def run_reference_arm(args):
              for i in range(cores)]
     for pr in procs:
         pr.start()
-    res = [out.get() for _ in procs]
+    import queue as _queue
+    res = []
+    try:
+        for _ in procs:   # a worker that dies would otherwise leave the barrier and this wait hanging
+            res.append(out.get(timeout=900 + 120 * (warmup + args.steps)))
+    except _queue.Empty:
+        for pr in procs:
+            pr.terminate()
+        raise RuntimeError("reference arm: a worker did not finish")
     for pr in procs:
         pr.join()
     cells = sum(r[1] for r in res)
@@ -170,7 +178,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self

@@ -231,14 +231,15 @@ class Solver final : public SolverBase {
     S.froude_on = p.froude_cap_on; S.froude_cap = p.froude_cap;
     S.tol = p.tol; S.itmax = p.itmax;
     S.max_ir = kFP32 ? 12 : 30;
-    // FP32 form: each refinement sweep's BiCGSTAB stops at 2e-4 of its own
+    // Each refinement sweep's BiCGSTAB stops at this fraction of its own
     // starting residual (or at the outer tolerance, if that needs less), and
-    // the next sweep restarts from a fresh FP64 residual.  An FP32 solve
-    // driven deeper converges more slowly per iteration: C2 7.25 -> 6.87
-    // iterations per solve and 10.96 -> 10.58 ms/step, C3 14.97 -> 13.96,
-    // against a floor of 2e-5 (1e-4 to 5e-4 alike; 1e-3 slower again).
-    // FP64 form: one sweep to the tolerance.
-    S.tol_floor = kFP32 ? 2e-4 : 0.0;
+    // the next sweep restarts from a fresh FP64 residual: a Krylov solve
+    // driven deeper converges more slowly per iteration.  FP32 form, against
+    // a floor of 2e-5: C2 7.25 -> 6.87 iterations per solve and 10.96 ->
+    // 10.58 ms/step, C3 14.97 -> 13.96 (1e-4 to 5e-4 alike; 1e-3 slower
+    // again).  FP64 form, against one sweep to the tolerance: C2 46.95 ->
+    // 45.88, C3 61.70 -> 59.34 ms/step (1e-2 and above slower on C3).
+    S.tol_floor = kFP32 ? 2e-4 : 3e-3;
     S.total_time = p.total_time; S.sim_steps = p.sim_steps;
     S.graph_mode = 0; S.h_go = S.h_ir = S.h_inner = 0;
     S.non_hydro = p.non_hydro; S.sponge_on = p.sponge_on;
