@@ -126,7 +126,9 @@ module nhw_gpu_iface
   integer(c_int), parameter :: NHW_F_FZ = 47
   integer(c_int), parameter :: NHW_F_GZ = 48
   integer(c_int), parameter :: NHW_F_HZ = 49
-  integer(c_int), parameter :: NHW_F_COUNT = 50
+  integer(c_int), parameter :: NHW_F_CMUVT = 50
+  integer(c_int), parameter :: NHW_F_CMUHT = 51
+  integer(c_int), parameter :: NHW_F_COUNT = 52
 
   ! ------------------------------------------------------------- nhw_params
   ! The input.txt keys the path reads (src/initialize.F:141-1321), in the C
@@ -337,6 +339,10 @@ module nhw_gpu_iface
        import :: c_int, c_ptr
        type(c_ptr), value :: h
      end function nhw_sponge_damping
+     integer(c_int) function nhw_eval_turb(h) bind(C, name="nhw_eval_turb")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+     end function nhw_eval_turb
 
      ! ------------------------------------------------------ whole steps
      ! time, dt, run_step: pass variables, or c_null_ptr through a c_ptr

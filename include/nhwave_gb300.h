@@ -26,6 +26,8 @@
  *                             incl. poisson_solver src/pressure.F:63-245 and
  *                             generate_coef_rhs src/pressure.F:475-840)
  *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
+ *   nhw_eval_turb          <- eval_turb            src/nhwave.F:6544-6782 (IVTURB, IHTURB 1 and 2;
+ *                             viscous flow only, a no-op otherwise)
  *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
  *   nhw_mass               <- statistics' MassVolume  src/nhwave.F:3139-3148
  *   nhw_statistics         <- statistics               src/nhwave.F:3118-3160
@@ -163,10 +165,12 @@ typedef struct nhw_params {
                                               that do not exist, so its bounded wait runs
                                               out and the solve reports NHW_ERR_TIMEOUT */
   /* viscous flow (read when viscous_flow = 1; src/initialize.F:357, 385-392) */
-  int32_t ivturb, ihturb;                  /* IVTURB IHTURB: 1 constant viscosity       */
+  int32_t ivturb, ihturb;                  /* IVTURB IHTURB: 1 constant viscosity,
+                                              2 subgrid model                          */
   int32_t rng;                             /* RNG: seeding viscosity of the first stage */
   double  cvs, chs;                        /* Cvs Chs: vertical / horizontal eddy
-                                              viscosity of IVTURB = 1 / IHTURB = 1      */
+                                              viscosity of IVTURB = 1 / IHTURB = 1, the
+                                              subgrid models' coefficients with 2     */
   double  schmidt;                         /* Schmidt                                 */
   double  viscous_number;                  /* VISCOUS_NUMBER: dt limit of the explicit
                                               horizontal viscous terms                */
@@ -229,6 +233,8 @@ enum nhw_field {
   NHW_F_EY, NHW_F_FY, NHW_F_GY, NHW_F_HY,
   /* 3-D z faces (Mloc,Nloc,Kloc1) */
   NHW_F_FZ, NHW_F_GZ, NHW_F_HZ,
+  /* 3-D cell (Mloc,Nloc,Kloc): eddy viscosities of eval_turb (viscous flow only) */
+  NHW_F_CMUVT, NHW_F_CMUHT,
   NHW_F_COUNT
 };
 
@@ -295,6 +301,7 @@ int nhw_source_terms(nhw_handle* h);
 int nhw_fluxes(nhw_handle* h);
 int nhw_eval_duvw(nhw_handle* h, int32_t istep);
 int nhw_sponge_damping(nhw_handle* h);
+int nhw_eval_turb(nhw_handle* h);
 
 /* One full time step (estimate_dt ... last RK stage).  The first call
  * captures the step into a CUDA graph whose pressure-solve loops run on the

@@ -1060,15 +1060,15 @@ struct OpVelBcA {
 // thread per (ghost column or ghost row, level); corner columns stay untouched
 // Wall friction factor of a BC = 5 side (src/nhwave.F:4486-4493): h the
 // spacing across the wall, a and b the first interior cell's tangential
-// velocities; Cmu + CmuHt of the cell
+// velocities; Cmu + CmuHt of the cell e (CmuHt = 0 on the inviscid path)
 template <class T>
-__device__ __forceinline__ double wall_phi(const Dev<T>& S, double h, double a, double b) {
+__device__ __forceinline__ double wall_phi(const Dev<T>& S, double h, double a, double b, long long e) {
   double Cdrag = S.cd0;
   if (S.ibot != 1) {
     const double lg = 1. / kKappa * log(30.0 * h / 2.0 / S.zob);
     Cdrag = 1. / (lg * lg);
   }
-  const double cmh = S.viscous ? (S.sc->turb ? S.v_chs : S.v_cmut0) : 0.0;
+  const double cmh = S.CmuHt ? (double)S.CmuHt[e] : 0.0;
   const double Phi = h * Cdrag * sqrt(a * a + b * b) / (S.v_cmu + cmh);
   return dmin_(Phi, 2.0);
 }
@@ -1134,7 +1134,7 @@ struct OpVelBcLat {
       const bool west = i < S.IB;
       const int g = west ? S.IB - i : i - S.IE;   // ghost offset 1, 2
       const long long q = i3(S, mirror(i, S.IB, S.IE), j, k), e = i3(S, west ? S.IB : S.IE, j, k);
-      const double Phi = wall_phi(S, S.dx, (double)S.V[e], (double)S.W[e]);
+      const double Phi = wall_phi(S, S.dx, (double)S.V[e], (double)S.W[e], e);
       const double d = S.D[i2(S, g - 1, j)];   // the reference's D(i,j) with i the ghost offset
       const T u = -S.U[q], v = (T)((1.0 - Phi) * (double)S.V[q]), w = (T)((1.0 - Phi) * (double)S.W[q]);
       S.U[o] = u; S.V[o] = v; S.W[o] = w;
@@ -1143,7 +1143,7 @@ struct OpVelBcLat {
       const bool south = j < S.JB;
       const int g = south ? S.JB - j : j - S.JE;
       const long long q = i3(S, i, mirror(j, S.JB, S.JE), k), e = i3(S, i, south ? S.JB : S.JE, k);
-      const double Phi = wall_phi(S, S.dy, (double)S.U[e], (double)S.W[e]);
+      const double Phi = wall_phi(S, S.dy, (double)S.U[e], (double)S.W[e], e);
       const double d = S.D[i2(S, i, g - 1)];   // D(i,j) with j the ghost offset
       const T u = (T)((1.0 - Phi) * (double)S.U[q]), v = -S.V[q], w = (T)((1.0 - Phi) * (double)S.W[q]);
       S.U[o] = u; S.V[o] = v; S.W[o] = w;
@@ -1188,13 +1188,17 @@ struct OpVelBcB {
     const R Fext_Wind2 = (R)1.0 / Atop * (((R)1 - dye * dye) * (R)S.Wsy[c] - dxe * dye * (R)S.Wsx[c]);
     const R MinDepBC = (R)(double)0.01f;
     const R WzLt = (R)S.zWL[c], WzRb = (R)S.zWR[c], UzLt = (R)S.zUL[c], VzLt = (R)S.zVL[c];
-    const R vtop = (R)(S.sc->turb ? S.visc_top_t : S.visc_top);
     const int KB = S.KB, KE = S.KE;
+    // Small + 0.5 (Cmu + CmuR + CmuVt) at the surface level and the one above;
+    // Cmu + CmuR + CmuVt at the bed level (CmuR = 0; CmuVt = 0 inviscid)
+    const double vtK = S.CmuVt ? (double)S.CmuVt[i3(S, i, j, KE)] : 0.0;
+    const double vtK1 = S.CmuVt ? (double)S.CmuVt[i3(S, i, j, KE + 1)] : 0.0;
+    const double vtB = S.CmuVt ? (double)S.CmuVt[i3(S, i, j, KB)] : 0.0;
+    const R vtop = (R)(S.CmuVt ? kSmall + 0.5 * (S.v_cmu + 0.0 + vtK + S.v_cmu + 0.0 + vtK1) : S.visc_top);
     // bed stress (src/nhwave.F:4806-4847) for BC_Z0 = 2 (no slip) and 5 (friction)
     const R dxh = (R)S.DelxH[c], dyh = (R)S.DelyH[c];
     const R Abot = sqrt((R)1.0 + dxh * dxh + dyh * dyh), Bbot = sqrt((R)1.0 + dxh * dxh);
-    // Cmu + CmuR + CmuVt at the bed level (CmuR = 0)
-    const R nub = (R)(S.v_cmu + 0.0 + (S.viscous ? (S.sc->turb ? S.v_cvs : S.v_cmut0) : 0.0));
+    const R nub = (R)(S.v_cmu + 0.0 + vtB);
     R Fext_Bot1 = (R)0, Fext_Bot2 = (R)0;
     R DelxUzR = (R)0, DelxVzR = (R)0, DelxWzR = (R)0, DelyUzR = (R)0, DelyVzR = (R)0, DelyWzR = (R)0;
     if (S.bc_z0 != 1) {
@@ -1225,7 +1229,7 @@ struct OpVelBcB {
       Fext_Bot1 = Bbot * TauBot1;
       Fext_Bot2 = (dxh * dyh * TauBot1 + Abot * TauBot2) / Bbot;
     }
-    const R vbot = (R)(kSmall + S.v_cmu + 0.0 + (S.viscous ? (S.sc->turb ? S.v_cvs : S.v_cmut0) : 0.0));
+    const R vbot = (R)(kSmall + S.v_cmu + 0.0 + vtB);
     const R UzRb = (R)S.zUR[c], VzRb = (R)S.zVR[c];
     for (int k = 1; k <= NG; ++k) {
       const long long ob = i3(S, i, j, KB - k), oi = i3(S, i, j, KB + k - 1);
@@ -1292,7 +1296,7 @@ struct OpVelBcB {
 // diffusion (src/nhwave.F:6785-7141): the explicit viscous terms of R2-R4,
 // one thread per interior cell, from the stage's starting DU/DV/DW and the
 // sigma slopes of the last sigma_transform (zero before the first one).
-// Cmu = Visc; CmuHt = Cmut_min until eval_turb, then Chs.  Each bracket
+// Cmu = Visc; CmuHt per cell (Cmut_min until eval_turb).  Each bracket
 // keeps the reference's evaluation order (bit-exact in the FP64 form).
 struct OpDiffusion {
   static constexpr const char* kName = "diffusion";
@@ -1318,16 +1322,23 @@ struct OpDiffusion {
     const T* DW = S.DW;
     auto F = [&](const T* a, int ii, int jj, int kk) -> R { return a[i3(S, ii, jj, kk)]; };
     const R dx = (R)S.dx, dy = (R)S.dy;
-    const R cmu = (R)S.v_cmu, cmh = (R)(S.sc->turb ? S.v_chs : S.v_cmut0), sch = (R)S.v_schmidt;
-    const R nuF = (R)0.5 * (cmu + cmu) + (R)0.5 * (cmh + cmh) / sch;
-    const R nuC = cmu + cmh / sch;
+    const R cmu = (R)S.v_cmu, sch = (R)S.v_schmidt;
+    // CmuHt of a cell; face viscosity between two cells; cell viscosity
+    auto H = [&](int ii, int jj, int kk) -> R { return (R)S.CmuHt[i3(S, ii, jj, kk)]; };
+    auto nuF = [&](R ha, R hb) -> R { return (R)0.5 * (cmu + cmu) + (R)0.5 * (ha + hb) / sch; };
+    auto nuC = [&](int ii, int jj, int kk) -> R { return cmu + H(ii, jj, kk) / sch; };
+    const R h0 = H(i, j, k);
+    const R nuE = nuF(H(i + 1, j, k), h0), nuW = nuF(h0, H(i - 1, j, k));
+    const R nuN = nuF(H(i, j + 1, k), h0), nuS = nuF(h0, H(i, j - 1, k));
+    const R cE = nuC(i + 1, j, k), cW = nuC(i - 1, j, k), cN = nuC(i, j + 1, k), cS = nuC(i, j - 1, k);
+    const R cD = nuC(i, j, k - 1), c0 = nuC(i, j, k), cU = nuC(i, j, k + 1);
     const double* dsg = S.dsig;
     const double L1top = dsg[k + 1] / (dsg[k] + dsg[k + 1]), L2top = dsg[k] / (dsg[k] + dsg[k + 1]);
     const double L1bot = dsg[k] / (dsg[k] + dsg[k - 1]), L2bot = dsg[k - 1] / (dsg[k] + dsg[k - 1]);
     const double ck = (dsg[k] + dsg[k + 1]) / 2.0, ck1 = (dsg[k - 1] + dsg[k]) / 2.0;
     const R ac = (R)(-ck / (ck + ck1) / ck1), bc = (R)((ck - ck1) / (ck * ck1)), gc = (R)(ck1 / (ck + ck1) / ck);
-    const R nuH_top = ((R)L1top * cmu + (R)L2top * cmu) + ((R)L1top * cmh + (R)L2top * cmh) / sch;
-    const R nuH_bot = ((R)L1bot * cmu + (R)L2bot * cmu) + ((R)L1bot * cmh + (R)L2bot * cmh) / sch;
+    const R nuH_top = ((R)L1top * cmu + (R)L2top * cmu) + ((R)L1top * h0 + (R)L2top * H(i, j, k + 1)) / sch;
+    const R nuH_bot = ((R)L1bot * cmu + (R)L2bot * cmu) + ((R)L1bot * H(i, j, k - 1) + (R)L2bot * h0) / sch;
     const R Dc = (R)S.D[c], dsk = (R)dsg[k], rck = (R)ck, rck1 = (R)ck1;
     auto s3 = [&](const T* a, bool y, int ii, int jj) -> R {   // a F(k-1) Sc(k-1) + b .. + c ..
       auto sc = [&](int kk) { return y ? Scy(ii, jj, kk) : Scx(ii, jj, kk); };
@@ -1361,47 +1372,133 @@ struct OpDiffusion {
     };
     const R two = (R)2.0;
     S.Dxx[o] =
-        (two * nuF * (F(DU, i + 1, j, k) - F(DU, i, j, k)) / dx - two * nuF * (F(DU, i, j, k) - F(DU, i - 1, j, k)) / dx) / dx +
-        (two * nuC * s3(DU, false, i + 1, j) - two * nuC * s3(DU, false, i - 1, j)) / two / dx +
-        (ac * two * nuC * Scx(i, j, k - 1) * (F(DU, i + 1, j, k - 1) - F(DU, i - 1, j, k - 1)) / two / dx +
-         bc * two * nuC * Scx(i, j, k) * (F(DU, i + 1, j, k) - F(DU, i - 1, j, k)) / two / dx +
-         gc * two * nuC * Scx(i, j, k + 1) * (F(DU, i + 1, j, k + 1) - F(DU, i - 1, j, k + 1)) / two / dx);
+        (two * nuE * (F(DU, i + 1, j, k) - F(DU, i, j, k)) / dx - two * nuW * (F(DU, i, j, k) - F(DU, i - 1, j, k)) / dx) / dx +
+        (two * cE * s3(DU, false, i + 1, j) - two * cW * s3(DU, false, i - 1, j)) / two / dx +
+        (ac * two * cD * Scx(i, j, k - 1) * (F(DU, i + 1, j, k - 1) - F(DU, i - 1, j, k - 1)) / two / dx +
+         bc * two * c0 * Scx(i, j, k) * (F(DU, i + 1, j, k) - F(DU, i - 1, j, k)) / two / dx +
+         gc * two * cU * Scx(i, j, k + 1) * (F(DU, i + 1, j, k + 1) - F(DU, i - 1, j, k + 1)) / two / dx);
     S.Dxy[o] =
-        (nuF * (F(DU, i, j + 1, k) - F(DU, i, j, k)) / dy - nuF * (F(DU, i, j, k) - F(DU, i, j - 1, k)) / dy) / dy +
-        (nuC * s3x((F(DV, i + 1, j + 1, k) - F(DV, i - 1, j + 1, k)) / two / dx, i, j + 1) -
-         nuC * s3x((F(DV, i + 1, j - 1, k) - F(DV, i - 1, j - 1, k)) / two / dx, i, j - 1)) / two / dy +
-        (ac * nuC * Scy(i, j, k - 1) * mixed(k - 1) + bc * nuC * Scy(i, j, k) * mixed(k) +
-         gc * nuC * Scy(i, j, k + 1) * mixed(k + 1)) +
+        (nuN * (F(DU, i, j + 1, k) - F(DU, i, j, k)) / dy - nuS * (F(DU, i, j, k) - F(DU, i, j - 1, k)) / dy) / dy +
+        (cN * s3x((F(DV, i + 1, j + 1, k) - F(DV, i - 1, j + 1, k)) / two / dx, i, j + 1) -
+         cS * s3x((F(DV, i + 1, j - 1, k) - F(DV, i - 1, j - 1, k)) / two / dx, i, j - 1)) / two / dy +
+        (ac * cD * Scy(i, j, k - 1) * mixed(k - 1) + bc * c0 * Scy(i, j, k) * mixed(k) +
+         gc * cU * Scy(i, j, k + 1) * mixed(k + 1)) +
         (yA * Scx(i, j, k - 1) * F(DV, i, j, k - 1) + yB * Scx(i, j, k) * F(DV, i, j, k) +
          yC * Scx(i, j, k + 1) * F(DV, i, j, k + 1));
     S.Dyx[o] =
-        (nuF * (F(DV, i + 1, j, k) - F(DV, i, j, k)) / dx - nuF * (F(DV, i, j, k) - F(DV, i - 1, j, k)) / dx) / dx +
-        (nuC * s3x((F(DU, i + 1, j + 1, k) - F(DU, i + 1, j - 1, k)) / two / dy, i + 1, j) -
-         nuC * s3x((F(DU, i - 1, j + 1, k) - F(DU, i - 1, j - 1, k)) / two / dy, i - 1, j)) / two / dx +
-        (ac * nuC * Scx(i, j, k - 1) * mixed(k - 1) + bc * nuC * Scx(i, j, k) * mixed(k) +
-         gc * nuC * Scx(i, j, k + 1) * mixed(k + 1)) +
+        (nuE * (F(DV, i + 1, j, k) - F(DV, i, j, k)) / dx - nuW * (F(DV, i, j, k) - F(DV, i - 1, j, k)) / dx) / dx +
+        (cE * s3x((F(DU, i + 1, j + 1, k) - F(DU, i + 1, j - 1, k)) / two / dy, i + 1, j) -
+         cW * s3x((F(DU, i - 1, j + 1, k) - F(DU, i - 1, j - 1, k)) / two / dy, i - 1, j)) / two / dx +
+        (ac * cD * Scx(i, j, k - 1) * mixed(k - 1) + bc * c0 * Scx(i, j, k) * mixed(k) +
+         gc * cU * Scx(i, j, k + 1) * mixed(k + 1)) +
         (xA * Scy(i, j, k - 1) * F(DU, i, j, k - 1) + xB * Scy(i, j, k) * F(DU, i, j, k) +
          xC * Scy(i, j, k + 1) * F(DU, i, j, k + 1));
     S.Dyy[o] =
-        (two * nuF * (F(DV, i, j + 1, k) - F(DV, i, j, k)) / dy - two * nuF * (F(DV, i, j, k) - F(DV, i, j - 1, k)) / dy) / dy +
-        (two * nuC * s3(DV, true, i, j + 1) - two * nuC * s3(DV, true, i, j - 1)) / two / dy +
-        (ac * two * nuC * Scy(i, j, k - 1) * (F(DV, i, j + 1, k - 1) - F(DV, i, j - 1, k - 1)) / two / dy +
-         bc * two * nuC * Scy(i, j, k) * (F(DV, i, j + 1, k) - F(DV, i, j - 1, k)) / two / dy +
-         gc * two * nuC * Scy(i, j, k + 1) * (F(DV, i, j + 1, k + 1) - F(DV, i, j - 1, k + 1)) / two / dy);
+        (two * nuN * (F(DV, i, j + 1, k) - F(DV, i, j, k)) / dy - two * nuS * (F(DV, i, j, k) - F(DV, i, j - 1, k)) / dy) / dy +
+        (two * cN * s3(DV, true, i, j + 1) - two * cS * s3(DV, true, i, j - 1)) / two / dy +
+        (ac * two * cD * Scy(i, j, k - 1) * (F(DV, i, j + 1, k - 1) - F(DV, i, j - 1, k - 1)) / two / dy +
+         bc * two * c0 * Scy(i, j, k) * (F(DV, i, j + 1, k) - F(DV, i, j - 1, k)) / two / dy +
+         gc * two * cU * Scy(i, j, k + 1) * (F(DV, i, j + 1, k + 1) - F(DV, i, j - 1, k + 1)) / two / dy);
     S.Dzx[o] =
-        (nuF * (F(DW, i + 1, j, k) - F(DW, i, j, k)) / dx - nuF * (F(DW, i, j, k) - F(DW, i - 1, j, k)) / dx) / dx +
-        (nuC * s3w(false, DU, i + 1, j) - nuC * s3w(false, DU, i - 1, j)) / two / dx +
-        (ac * nuC * Scx(i, j, k - 1) * (F(DW, i + 1, j, k - 1) - F(DW, i - 1, j, k - 1)) / two / dx +
-         bc * nuC * Scx(i, j, k) * (F(DW, i + 1, j, k) - F(DW, i - 1, j, k)) / two / dx +
-         gc * nuC * Scx(i, j, k + 1) * (F(DW, i + 1, j, k + 1) - F(DW, i - 1, j, k + 1)) / two / dx) +
+        (nuE * (F(DW, i + 1, j, k) - F(DW, i, j, k)) / dx - nuW * (F(DW, i, j, k) - F(DW, i - 1, j, k)) / dx) / dx +
+        (cE * s3w(false, DU, i + 1, j) - cW * s3w(false, DU, i - 1, j)) / two / dx +
+        (ac * cD * Scx(i, j, k - 1) * (F(DW, i + 1, j, k - 1) - F(DW, i - 1, j, k - 1)) / two / dx +
+         bc * c0 * Scx(i, j, k) * (F(DW, i + 1, j, k) - F(DW, i - 1, j, k)) / two / dx +
+         gc * cU * Scx(i, j, k + 1) * (F(DW, i + 1, j, k + 1) - F(DW, i - 1, j, k + 1)) / two / dx) +
         (xA * F(DU, i, j, k - 1) / Dc + xB * F(DU, i, j, k) / Dc + xC * F(DU, i, j, k + 1) / Dc);
     S.Dzy[o] =
-        (nuF * (F(DW, i, j + 1, k) - F(DW, i, j, k)) / dy - nuF * (F(DW, i, j, k) - F(DW, i, j - 1, k)) / dy) / dy +
-        (nuC * s3w(true, DV, i, j + 1) - nuC * s3w(true, DV, i, j - 1)) / two / dy +
-        (ac * nuC * Scy(i, j, k - 1) * (F(DW, i, j + 1, k - 1) - F(DW, i, j - 1, k - 1)) / two / dy +
-         bc * nuC * Scy(i, j, k) * (F(DW, i, j + 1, k) - F(DW, i, j - 1, k)) / two / dy +
-         gc * nuC * Scy(i, j, k + 1) * (F(DW, i, j + 1, k + 1) - F(DW, i, j - 1, k + 1)) / two / dy) +
+        (nuN * (F(DW, i, j + 1, k) - F(DW, i, j, k)) / dy - nuS * (F(DW, i, j, k) - F(DW, i, j - 1, k)) / dy) / dy +
+        (cN * s3w(true, DV, i, j + 1) - cS * s3w(true, DV, i, j - 1)) / two / dy +
+        (ac * cD * Scy(i, j, k - 1) * (F(DW, i, j + 1, k - 1) - F(DW, i, j - 1, k - 1)) / two / dy +
+         bc * c0 * Scy(i, j, k) * (F(DW, i, j + 1, k) - F(DW, i, j - 1, k)) / two / dy +
+         gc * cU * Scy(i, j, k + 1) * (F(DW, i, j + 1, k + 1) - F(DW, i, j - 1, k + 1)) / two / dy) +
         (yA * F(DV, i, j, k - 1) / Dc + yB * F(DV, i, j, k) / Dc + yC * F(DV, i, j, k + 1) / Dc);
+  }
+};
+
+// eval_turb (src/nhwave.F:6544-6782), after sponge_damping.  Vertical
+// (every column, ghosts included): IVTURB 1 CmuVt = Cvs; IVTURB 2 the
+// subgrid model CmuVt = Cvs D dsig^2 |d(U,V)/dsigma| on the levels 2 ..
+// Kloc-1 (1-based), the outermost ghost levels copying their neighbours.
+// IHTURB 1 fills CmuHt = Chs here; IHTURB 2 is OpTurbH + OpTurbHGhost.
+// Products in the reference's order, in FP64 (bit-exact in the FP64 form).
+struct OpTurbV {
+  static constexpr const char* kName = "eval_turb_v";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    if (S.ihturb == 1)
+      for (int k = 0; k < S.Kloc; ++k) S.CmuHt[q + S.sz * k] = (T)S.v_chs;
+    if (S.ivturb == 1) {
+      for (int k = 0; k < S.Kloc; ++k) S.CmuVt[q + S.sz * k] = (T)S.v_cvs;
+      return;
+    }
+    const double Dq = S.D[q];
+    T* cv = S.CmuVt + q;
+    for (int k = 1; k <= S.Kloc - 2; ++k) {
+      const long long a = q + S.sz * (k + 1), b = q + S.sz * (k - 1);
+      const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+      const double dU = ((double)S.U[a] - (double)S.U[b]) / ds;
+      const double dV = ((double)S.V[a] - (double)S.V[b]) / ds;
+      cv[S.sz * k] = (T)(S.v_cvs * Dq * (S.dsig[k] * S.dsig[k]) * sqrt(dU * dU + dV * dV));
+    }
+    cv[0] = cv[S.sz];
+    cv[S.sz * (S.Kloc - 1)] = cv[S.sz * (S.Kloc - 2)];
+  }
+};
+// IHTURB 2, interior cells: CmuHt = Chs dx dy sqrt(Sxx^2 + 2 Sxy^2 + Syy^2)
+// with the horizontal strain rates in sigma coordinates; DelxSc / DelySc
+// are the slopes of the last sigma_transform (zero before the first one).
+// The reference's Strxy reads U(i,j+1,j), the row index in place of the
+// level (src/nhwave.F:6695); the level k is read here.
+struct OpTurbH {
+  static constexpr const char* kName = "eval_turb_h";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    auto U = [&](long long x) { return (double)S.U[x]; };
+    auto V = [&](long long x) { return (double)S.V[x]; };
+    double sx = 0.0, sy = 0.0;
+    if (S.sc->sig_set) {
+      sx = (1.0 - S.sigc[k]) / S.scD[q] * S.scHx[q] - S.sigc[k] / S.scD[q] * S.scEx[q];
+      sy = (1.0 - S.sigc[k]) / S.scD[q] * S.scHy[q] - S.sigc[k] / S.scD[q] * S.scEy[q];
+    }
+    const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+    const long long up = o + S.sz, dn = o - S.sz;
+    const double Sxx = (U(o + 1) - U(o - 1)) / (2.0 * S.dx) + (U(up) - U(dn)) / ds * sx;
+    const double Syy = (V(o + S.sy) - V(o - S.sy)) / (2.0 * S.dy) + (V(up) - V(dn)) / ds * sy;
+    const double Sxy = 0.5 * ((U(o + S.sy) - U(o - S.sy)) / (2.0 * S.dy) + (U(up) - U(dn)) / ds * sy +
+                              (V(o + 1) - V(o - 1)) / (2.0 * S.dx) + (V(up) - V(dn)) / ds * sx);
+    S.CmuHt[o] = (T)(S.v_chs * S.dx * S.dy * sqrt(Sxx * Sxx + 2.0 * (Sxy * Sxy) + Syy * Syy));
+  }
+};
+// IHTURB 2, ghosts: CmuHt mirrored across the west/east sides (interior
+// rows and levels), the south/north sides (interior columns i, levels) and
+// the bed/surface (interior columns).  One thread per line, its NG ghosts
+// in the reference's order, so a grid narrower than NG reads what the same
+// line wrote before, as the reference does.  Lines t of the x sides, then
+// of the y sides, then of the vertical.
+struct OpTurbHGhost {
+  static constexpr const char* kName = "eval_turb_ghost";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    T* c = S.CmuHt;
+    const long long nx = (long long)S.N * S.K, ny = (long long)S.M * S.K;
+    long long base, step;
+    int lo, hi;
+    if (t < nx) {
+      base = i3(S, 0, S.JB + (int)(t % S.N), S.KB + (int)(t / S.N)); step = 1; lo = S.IB; hi = S.IE;
+    } else if (t < nx + ny) {
+      const long long u = t - nx;
+      base = i3(S, S.IB + (int)(u % S.M), 0, S.KB + (int)(u / S.M)); step = S.sy; lo = S.JB; hi = S.JE;
+    } else {
+      const long long u = t - nx - ny;
+      base = i3(S, S.IB + (int)(u % S.M), S.JB + (int)(u / S.M), 0); step = S.sz; lo = S.KB; hi = S.KE;
+    }
+    for (int g = 1; g <= NG; ++g) {
+      c[base + step * (lo - g)] = c[base + step * (lo + g - 1)];
+      c[base + step * (hi + g)] = c[base + step * (hi - g + 1)];
+    }
   }
 };
 
@@ -1421,11 +1518,16 @@ struct OpVertVisc {
     if (S.Mask[c] == 0) return;
     const int KB = S.KB, KE = S.KE, n = KE - KB + 1;
     const double dt = S.sc->dt, Dc = S.D[c];
-    const double cvt = S.sc->turb ? S.v_cvs : S.v_cmut0;
-    const double nuz = 0.5 * (S.v_cmu + S.v_cmu) + 0.5 * (cvt + cvt) / S.v_schmidt;
+    // CmuVt of level k and the face viscosity between levels k1 and k2
+    auto vt = [&](int k) { return (double)S.CmuVt[i3(S, i, j, k)]; };
+    auto nuz = [&](int k1, int k2) { return 0.5 * (S.v_cmu + S.v_cmu) + 0.5 * (vt(k1) + vt(k2)) / S.v_schmidt; };
     const double* dsg = S.dsig;
-    auto A = [&](int k) { return k == KB ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsg[k] * (dsg[k] + dsg[k - 1])); };
-    auto C = [&](int k) { return k == KE ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsg[k] * (dsg[k] + dsg[k + 1])); };
+    auto A = [&](int k) {
+      return k == KB ? 0.0 : -dt / (Dc * Dc) * nuz(k - 1, k) / (0.5 * dsg[k] * (dsg[k] + dsg[k - 1]));
+    };
+    auto C = [&](int k) {
+      return k == KE ? 0.0 : -dt / (Dc * Dc) * nuz(k, k + 1) / (0.5 * dsg[k] * (dsg[k] + dsg[k + 1]));
+    };
     const double Wbot = -S.DeltH[c] - (double)S.U[i3(S, i, j, KB)] * S.DelxH[c] - (double)S.V[i3(S, i, j, KB)] * S.DelyH[c];
     const double Wtop = (S.Eta[c] - S.Eta0[c]) / dt + (double)S.U[i3(S, i, j, KE)] * S.DelxEta[c] +
                         (double)S.V[i3(S, i, j, KE)] * S.DelyEta[c];
@@ -1436,7 +1538,7 @@ struct OpVertVisc {
         const double f = (double)Fv[i3(S, i, j, k)];
         if (which < 2) {
           if (k == KB && S.bc_z0 == 2)   // no-slip bed
-            b = 1.0 - C(k) + dt / (Dc * Dc) * (S.v_cmu + 0.0 + cvt / S.v_schmidt) / (0.5 * dsg[k] * dsg[k]);
+            b = 1.0 - C(k) + dt / (Dc * Dc) * (S.v_cmu + 0.0 + vt(k) / S.v_schmidt) / (0.5 * dsg[k] * dsg[k]);
           else
             b = 1.0 - A(k) - C(k);
           if (k == KB && S.bc_z0 == 5) {   // friction law: bed stress in the first right-hand side
@@ -1456,12 +1558,12 @@ struct OpVertVisc {
           }
         } else if (k == KB) {
           const double q = 0.25 * dsg[k] * (dsg[k] + dsg[k - 1]);
-          b = 1.0 - C(k) + dt / (Dc * Dc) * nuz / q;
-          r = f + dt / Dc * nuz / q * Wbot;
+          b = 1.0 - C(k) + dt / (Dc * Dc) * nuz(k - 1, k) / q;
+          r = f + dt / Dc * nuz(k - 1, k) / q * Wbot;
         } else if (k == KE) {
           const double q = 0.25 * dsg[k] * (dsg[k] + dsg[k + 1]);
-          b = 1.0 - A(k) + dt / (Dc * Dc) * nuz / q;
-          r = f + dt / Dc * nuz / q * Wtop;
+          b = 1.0 - A(k) + dt / (Dc * Dc) * nuz(k, k + 1) / q;
+          r = f + dt / Dc * nuz(k, k + 1) / q * Wtop;
         } else {
           b = 1.0 - A(k) - C(k);
           r = f;
@@ -1498,6 +1600,9 @@ struct OpInitDU {
     S.DU[o] = (T)((double)(T)(d * (double)S.U[o]) * m);
     S.DV[o] = (T)((double)(T)(d * (double)S.V[o]) * m);
     S.DW[o] = (T)((double)(T)(d * (double)S.W[o]) * m);
+    // viscous flow: the seeding viscosity Cmut_min, after vel_bc, which so
+    // saw CmuVt = 0 (src/initialize.F:3155, 3172-3195)
+    if (S.CmuVt) S.CmuVt[o] = S.CmuHt[o] = (T)S.v_cmut0;
   }
 };
 
@@ -1943,10 +2048,25 @@ __global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
   // cell.  A candidate replaces m only if it is smaller, as the reference's
   // `if(dxonu<tmp2) tmp2=dxonu` (src/nhwave.F:3730-3746): a NaN candidate
   // leaves m unchanged (tmp1 = max(NaN, Small) is Small, whose quotient is
-  // never the minimum).
+  // never the minimum).  Viscous flow: the limit dx^2 / (|CmuHt| + 1e-16)
+  // over the interior (src/nhwave.F:3812-3832) is, by the same monotonicity,
+  // the one of the largest |CmuHt|, gathered as its bit pattern + 1 (0: no
+  // finite value; NaN cells never give the minimum and are skipped).
   __shared__ double sh[8];
+  __shared__ unsigned long long shh[8];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   double m = kLarge;
+  unsigned long long hb = 0ull;
+  if (t < S.M * S.N && S.CmuHt) {
+    const int i = S.IB + t % S.M, j = S.JB + t / S.M;
+    for (int k = S.KB; k <= S.KE; ++k) {
+      const double a = fabs((double)S.CmuHt[i3(S, i, j, k)]);
+      if (a == a) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(a) + 1ull;
+        if (b > hb) hb = b;
+      }
+    }
+  }
   if (t < S.M * S.N) {
     const int i = S.IB + t % S.M, j = S.JB + t / S.M;
     const long long q = i2(S, i, j);
@@ -1965,12 +2085,20 @@ __global__ void __launch_bounds__(256) k_dt_min(Dev<T> S) {
     x = S.dy / vy;
     if (x < m) m = x;
   }
-  for (int o = 16; o > 0; o >>= 1) m = dmin_(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  for (int o = 16; o > 0; o >>= 1) {
+    m = dmin_(m, __shfl_down_sync(0xffffffffu, m, o));
+    const unsigned long long b = __shfl_down_sync(0xffffffffu, hb, o);
+    if (b > hb) hb = b;
+  }
+  if ((threadIdx.x & 31) == 0) { sh[threadIdx.x >> 5] = m; shh[threadIdx.x >> 5] = hb; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = dmin_(m, sh[w]);
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      m = dmin_(m, sh[w]);
+      if (shh[w] > hb) hb = shh[w];
+    }
     atomicMin(&S.sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
+    if (hb) atomicMax(&S.sc->htmax_bits, hb);
   }
 }
 template <class T>
@@ -1978,6 +2106,8 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
   DevScal* sc = S.sc;
   const double tmp2 = __longlong_as_double((long long)sc->dtmin_bits);
   sc->dtmin_bits = (unsigned long long)__double_as_longlong(kLarge);
+  const unsigned long long hb = sc->htmax_bits;
+  sc->htmax_bits = 0ull;
   // A dt below DT_MIN stops the run for good (src/nhwave.F:3840-3850 stops
   // the program).  The gated form also holds the step back once the run is
   // over (the main loop's TIME < TOTAL_TIME and RUN_STEP < SIM_STEPS test,
@@ -1989,15 +2119,17 @@ __global__ void k_dt_finalize(Dev<T> S, int gated) {
     sc->dt_old = sc->dt;
     const double dt_growth = (double)1.05f * sc->dt_old;
     const double dt_courant = S.cfl * tmp2;
-    // limit of the explicit viscous terms (src/nhwave.F:3812-3832); the
-    // horizontal viscosity is the same in every cell
+    // limit of the explicit viscous terms (src/nhwave.F:3812-3832), from
+    // the largest finite |CmuHt| that k_dt_min found
     double dt_viscous = kLarge;
     if (S.viscous) {
-      const double ch = fabs(sc->turb ? S.v_chs : S.v_cmut0) + (double)1.e-16f;
       double t2 = kLarge;
-      const double ax = S.dx * S.dx / ch, ay = S.dy * S.dy / ch;
-      if (ax < t2) t2 = ax;
-      if (ay < t2) t2 = ay;
+      if (hb) {
+        const double ch = __longlong_as_double((long long)(hb - 1ull)) + (double)1.e-16f;
+        const double ax = S.dx * S.dx / ch, ay = S.dy * S.dy / ch;
+        if (ax < t2) t2 = ax;
+        if (ay < t2) t2 = ay;
+      }
       dt_viscous = S.v_number * t2;
     }
     const double dt = dmin_(dmin_(dmin_(dt_growth, dt_courant), dt_viscous), S.dt_max);

@@ -50,6 +50,7 @@ class SolverBase {
   virtual int fluxes() = 0;
   virtual int eval_duvw(int istep) = 0;
   virtual int sponge_damping() = 0;
+  virtual int eval_turb() = 0;
   virtual int step() = 0;
   virtual int mass(double* m) = 0;
   virtual int statistics(double* out7) = 0;
@@ -98,7 +99,6 @@ template <class T>
 __global__ void k_single(Dev<T> S, int what) {
   if (gated_off(S)) return;
   if (what == 0) OpSourceArea{}(S, 0, 0);
-  else if (what == 1) S.sc->turb = 1;
 }
 // update_vars: D0 = D, Eta0 = Eta (2-D, FP64), DU0/DV0/DW0 = DU/DV/DW (3-D)
 template <class T>
@@ -246,7 +246,6 @@ class Solver final : public SolverBase {
     S.hllc = p.hllc ? 1 : 0;
     S.bc_x0 = p.bc_x0; S.bc_xn = p.bc_xn; S.bc_y0 = p.bc_y0; S.bc_yn = p.bc_yn;
     S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + 0.0 + p.visc + 0.0 + 0.0);
-    S.visc_top_t = S.visc_top;
     S.v_cmu = p.visc;
     S.bc_z0 = p.bc_z0; S.ibot = p.ibot; S.cd0 = p.cd0; S.zob = p.zob;
     S.viscous = p.viscous_flow ? 1 : 0;
@@ -255,8 +254,7 @@ class Solver final : public SolverBase {
       S.v_cmut0 = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (tke * tke) / eps;
       S.v_cmu = p.visc; S.v_cvs = p.cvs; S.v_chs = p.chs;
       S.v_schmidt = p.schmidt; S.v_number = p.viscous_number;
-      S.visc_top = kSmall + 0.5 * (p.visc + 0.0 + S.v_cmut0 + p.visc + 0.0 + S.v_cmut0);
-      S.visc_top_t = kSmall + 0.5 * (p.visc + 0.0 + p.cvs + p.visc + 0.0 + p.cvs);
+      S.ivturb = p.ivturb; S.ihturb = p.ihturb;
     }
     S.wavemaker = p.wavemaker;
     S.wm_amp = p.amp_wave; S.wm_xw = p.xsource_west; S.wm_xe = p.xsource_east;
@@ -312,8 +310,11 @@ class Solver final : public SolverBase {
     }
     if (p.bc_xn == 3)   // FLUX_LR's outflow velocities of this and the previous step (checkpointed state)
       for (double** pp : {&S.Uxni, &S.Uxni0}) add(pp, sizeof(double) * S.Nloc * S.Kloc);
-    if (p.viscous_flow)   // sigma_transform's inputs, read by the next stage (checkpointed state)
+    if (p.viscous_flow) {   // sigma_transform's inputs, read by the next stage, and the
+      // eddy viscosities of the last eval_turb (checkpointed state)
       for (double** pp : {&S.scD, &S.scEx, &S.scEy, &S.scHx, &S.scHy}) add(pp, sizeof(double) * n2);
+      for (T** pp : {&S.CmuVt, &S.CmuHt}) add(pp, sizeof(T) * n3);
+    }
     add(&S.P, sizeof(double) * n3);
     if (p.viscous_flow)   // explicit viscous terms of the stage
       for (T** pp : {&S.Dxx, &S.Dxy, &S.Dyx, &S.Dyy, &S.Dzx, &S.Dzy}) add(pp, sizeof(T) * n3);
@@ -561,6 +562,8 @@ class Solver final : public SolverBase {
       case NHW_F_FZ: return {S.Fz, 0, Ml, Nl, Kl + 1};
       case NHW_F_GZ: return {S.Gz, 0, Ml, Nl, Kl + 1};
       case NHW_F_HZ: return {S.Hz, 0, Ml, Nl, Kl + 1};
+      case NHW_F_CMUVT: return {S.CmuVt, 0, Ml, Nl, Kl};   // null (no field) on the inviscid path
+      case NHW_F_CMUHT: return {S.CmuHt, 0, Ml, Nl, Kl};
       default: return {nullptr, -1, 0, 0, 0};
     }
   }
@@ -674,9 +677,10 @@ class Solver final : public SolverBase {
     for (auto& c : cap_counts) c = 0;
     cap_solves = 0;
   }
-  void ens_stage_tail(int s) {   // eval_duvw after the solve, sponge
+  void ens_stage_tail(int s) {   // eval_duvw after the solve, sponge, eval_turb
     stage_post(s);
     if (S.sponge_on) sponge_damping();
+    launch_turb();
   }
   int pull() { return pull_scalars(); }
   const DevScal& scal() const { return *h_sc; }
@@ -771,7 +775,13 @@ class Solver final : public SolverBase {
     h_sc->rho_dt = kRho0 / p.dt_ini; h_sc->dt_rho = p.dt_ini / kRho0;
     h_sc->dtmin_bits = (unsigned long long)dbits(kLarge);
     NHW_CU(cudaMemcpyAsync(S.sc, h_sc, sizeof(DevScal), cudaMemcpyHostToDevice, st));
-    // initial: vel_bc on the initial velocities, then DU = D*U*Mask
+    // initial: vel_bc on the initial velocities, with CmuVt = CmuHt = 0
+    // (src/initialize.F:2667-2668), then DU = D*U*Mask and the seeding
+    // eddy viscosities
+    if (S.CmuVt) {
+      NHW_CU(cudaMemsetAsync(S.CmuVt, 0, sizeof(T) * n3, st));
+      NHW_CU(cudaMemsetAsync(S.CmuHt, 0, sizeof(T) * n3, st));
+    }
     incols(OpVelBcA{});
     box(OpVelBcLat{}, S.Mloc, S.Nloc, S.K, 0, 0, S.KB);
     incols(OpVelBcB{});
@@ -1209,10 +1219,6 @@ class Solver final : public SolverBase {
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});
-    // eval_turb with IVTURB = IHTURB = 1 (src/nhwave.F:6544-6686): from now
-    // on CmuVt = Cvs, CmuHt = Chs.  The reference calls it after
-    // sponge_damping, which reads no viscosity.
-    if (S.viscous) L("eval_turb", [&] { k_single<T><<<1, 1, 0, st>>>(S, 1); });
   }
   int eval_duvw(int istep) override {
     if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
@@ -1231,6 +1237,21 @@ class Solver final : public SolverBase {
     allcols(OpSponge{});
     return check();
   }
+  // eval_turb (src/nhwave.F:6544-6782): the eddy viscosities CmuVt / CmuHt
+  // the next stage's viscous terms read, from the velocities after
+  // sponge_damping.  Inviscid flow has none.
+  void launch_turb() {
+    if (!S.viscous) return;
+    allcols(OpTurbV{});
+    if (S.ihturb == 2) {
+      cells(OpTurbH{});
+      box(OpTurbHGhost{}, S.N * S.K + S.M * S.K + S.M * S.N, 1, 1, 0, 0, 0);
+    }
+  }
+  int eval_turb() override {
+    launch_turb();
+    return check();
+  }
   // everything of one time step after estimate_dt (src/nhwave.F:119-200)
   int step_body() {
     if (S.slide) update_bathymetry();
@@ -1246,6 +1267,7 @@ class Solver final : public SolverBase {
       if (rc == NHW_ERR_CUDA) return rc;
       if (rc != NHW_OK && worst == NHW_OK) worst = rc;
       if (S.sponge_on) sponge_damping();
+      launch_turb();
     }
     rc = check();
     return rc ? rc : worst;
@@ -1593,6 +1615,8 @@ class Solver final : public SolverBase {
   // counters) and the arena prefix from the grids through P: every array a
   // step reads before writing it.  The Poisson and Krylov arrays after it are
   // rebuilt by every solve and are not saved.
+  // 2: per-cell eddy viscosities of viscous flow in the state prefix
+  static constexpr int32_t kCkptVersion = 2;
   struct CkptHeader {
     char magic[8];
     int32_t version, precision, M, N, K, reserved;
@@ -1608,7 +1632,7 @@ class Solver final : public SolverBase {
     if (!host || bytes < ckpt_size()) return NHW_ERR_ARG;
     CkptHeader h{};
     std::memcpy(h.magic, "NHWCKPT1", 8);
-    h.version = 1;
+    h.version = kCkptVersion;
     h.precision = kFP32 ? NHW_FP32_IR : NHW_FP64;
     h.M = S.M; h.N = S.N; h.K = S.K;
     h.state_bytes = state_bytes;
@@ -1625,7 +1649,7 @@ class Solver final : public SolverBase {
     if (!host || bytes < sizeof(CkptHeader)) return NHW_ERR_ARG;
     CkptHeader h{};
     std::memcpy(&h, host, sizeof(h));
-    if (std::memcmp(h.magic, "NHWCKPT1", 8) != 0 || h.version != 1) {
+    if (std::memcmp(h.magic, "NHWCKPT1", 8) != 0 || h.version != kCkptVersion) {
       set_last_error("nhw_load_state: not a checkpoint of this library");
       return NHW_ERR_ARG;
     }

@@ -59,8 +59,8 @@ struct DevScal {
   // grid barrier of the persistent solve (psolve.cuh)
   unsigned int bar_count, bar_gen;
   int32_t bar_err;
-  int32_t turb;                     // viscous flow: eval_turb has set CmuVt = Cvs, CmuHt = Chs
   int32_t sig_set, pad3_;           // viscous flow: the sigma slopes have been formed once
+  unsigned long long htmax_bits;    // estimate_dt: largest |CmuHt| of the interior (bit pattern)
   double gm_inv;                    // GMRES: 1 / ||w|| of the vector the next iteration normalises
 };
 
@@ -89,12 +89,12 @@ struct Dev {
   // handles.  Eagerly launched kernels have graph_mode = 0.
   int graph_mode;
   unsigned long long h_go, h_ir, h_inner;
-  double visc_top;                 // Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt) before eval_turb
-  double visc_top_t;               // the same after it (viscous flow: CmuVt = Cvs)
-  // viscous flow with constant viscosities (IVTURB = IHTURB = 1): Cmu = Visc;
-  // CmuVt = CmuHt = Cmut_min until eval_turb, then Cvs / Chs; Schmidt;
-  // VISCOUS_NUMBER.  viscous = 0 on the inviscid path.
-  int viscous;
+  double visc_top;                 // inviscid path: Small + 0.5*(Cmu+CmuR+CmuVt+Cmu+CmuR+CmuVt), CmuVt = 0
+  // viscous flow: Cmu = Visc (every cell); CmuVt, CmuHt per cell (below),
+  // Cmut_min from initial, then what eval_turb sets -- Cvs / Chs (IVTURB,
+  // IHTURB = 1) or the subgrid models (2); Schmidt; VISCOUS_NUMBER.
+  // viscous = 0 on the inviscid path, where CmuVt = CmuHt = 0.
+  int viscous, ivturb, ihturb;
   double v_cmu, v_cmut0, v_cvs, v_chs, v_schmidt, v_number;
   // bed (BC_Z0): 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   int bc_z0, ibot;
@@ -145,6 +145,7 @@ struct Dev {
   // the last sigma_transform, from which the viscous terms form DelxSc /
   // DelySc (cell levels) and DelxSl / DelySl (faces) of that moment
   double *scD, *scEx, *scEy, *scHx, *scHy;
+  T *CmuVt, *CmuHt;                // viscous flow: eddy viscosities per cell (ghosted 3-D), else nullptr
   double *Hfx, *Hfy, *Hfx0, *Hfy0, *DelxH, *DelyH, *DeltH, *DeltHo, *Delt2H;
   double *DelxEta, *DelyEta, *SourceX, *SourceY, *SourceC, *Sponge, *R1, *Wsx, *Wsy;
   double *EtaxL, *EtaxR, *EtayL, *EtayR;

@@ -30,7 +30,7 @@ EXPORTS = [
     "nhw_get_scalars", "nhw_set_time", "nhw_set_wave_phases", "nhw_set_wave_spectrum", "nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc",
     "nhw_update_mask",
     "nhw_update_vars", "nhw_source_terms", "nhw_fluxes", "nhw_eval_duvw", "nhw_sponge_damping",
-    "nhw_step", "nhw_run", "nhw_mass", "nhw_statistics", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
+    "nhw_eval_turb", "nhw_step", "nhw_run", "nhw_mass", "nhw_statistics", "nhw_synchronize", "nhw_run_timed", "nhw_profile",
     "nhw_profile_report", "nhw_time_smoother", "nhw_abi_sizes", "nhw_status_string", "nhw_last_error",
     "nhw_estimate_dt_noalloc",
     "nhw_ensemble_create", "nhw_ensemble_step", "nhw_ensemble_run_timed", "nhw_ensemble_tune",
@@ -94,7 +94,7 @@ def load(path: str | None = None):
     L.nhw_set_wave_phases.argtypes = [vp, i32, vp]
     L.nhw_set_wave_spectrum.argtypes = [vp, i32, i32, vp, vp, vp, vp]
     for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc", "nhw_update_mask", "nhw_update_vars",
-              "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_synchronize"):
+              "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_eval_turb", "nhw_synchronize"):
         getattr(L, n).argtypes = [vp]
     L.nhw_eval_duvw.argtypes = [vp, i32]
     L.nhw_step.argtypes = [vp, P(dbl), P(dbl), P(i32)]
@@ -212,6 +212,9 @@ class Scenario:
 
     def sponge_damping(self):
         return _chk(load().nhw_sponge_damping(self._h), "sponge_damping")
+
+    def eval_turb(self):
+        return _chk(load().nhw_eval_turb(self._h), "eval_turb")
 
     def step(self):
         return _chk(load().nhw_step(self._h, None, None, None), "nhw_step")

@@ -284,9 +284,9 @@ def read_irr2d(path: str):
 
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
-    if p.viscous_flow and (p.ivturb != 1 or p.ihturb != 1):
-        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (only constant viscosities, "
-                "IVTURB = IHTURB = 1, are on the GPU path; the k-epsilon and LES models are not)")
+    if p.viscous_flow and (p.ivturb not in (1, 2) or p.ihturb not in (1, 2)):
+        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (constant viscosities (1) and the "
+                "subgrid models (2) are on the GPU path; the k-epsilon and LES closures are not)")
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE,) + WM_INT + WM_LEF + WM_EAST:

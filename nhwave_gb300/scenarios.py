@@ -314,6 +314,15 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.005, chs=0.01, bc_z0=5, bc_y0=5, bc_yn=5, bc_xn=5,
                        ibot=1, cd0=0.006), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_visc_sgs":
+        # the small submerged bar with the subgrid eddy viscosities (IVTURB = IHTURB = 2)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.2, chs=0.2, ivturb=2, ihturb=2), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_visc_sgs_fric":
+        # tiny_visc_sgs with the friction law on the bed and on the south, north and east walls
+        kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.2, chs=0.2, ivturb=2, ihturb=2, bc_z0=5, bc_y0=5,
+                       bc_yn=5, bc_xn=5, ibot=1, cd0=0.006), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_fric_log":
         # the inviscid small bar with the friction law on the bed and the side walls, from a
         # roughness height (Ibot = 2)

@@ -27,7 +27,7 @@
 //   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
 //   diffusion                  src/nhwave.F:6785-7141
 //   trig                       src/nhwave.F:13182-13224
-//   eval_turb (IVTURB=IHTURB=1) src/nhwave.F:6544-6686
+//   eval_turb (IVTURB, IHTURB 1, 2) src/nhwave.F:6544-6782
 //   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
 //                              Orlanski east side, bed stress)
 //   update_wave_bc             src/nhwave.F:5514-5565, 5715-5750; src/waves.F:92-370,
@@ -221,12 +221,13 @@ struct Model {
   // Poisson system (Coef(neqns,15), Rhs(neqns); src/mod_global.F:239-243)
   int neqns = 0;
   std::vector<double> Coef, Rhs;
-  // Cmu = Visc, CmuR = CmuVt = 0 on the inviscid path (src/initialize.F:2663-2666).
-  // With VISCOUS_FLOW and IVTURB = IHTURB = 1 every cell holds the same
-  // viscosities, so they are scalars here: CmuVt = CmuHt = Cmut_min from
-  // initial (src/initialize.F:3172-3195) until the first eval_turb sets
-  // CmuVt = Cvs, CmuHt = Chs (src/nhwave.F:6650-6686).
-  double Cmu = 0, CmuR = 0, CmuVt = 0, CmuHt = 0;
+  // Cmu = Visc and CmuR = 0 in every cell (no sediment rheology), so they
+  // are scalars here; CmuVt and CmuHt are zero on the inviscid path
+  // (src/initialize.F:2663-2668), Cmut_min in every cell from initial with
+  // VISCOUS_FLOW (:3172-3195), then what eval_turb sets (src/nhwave.F:
+  // 6544-6782): Cvs / Chs, or the subgrid models of IVTURB / IHTURB = 2.
+  double Cmu = 0, CmuR = 0;
+  A3 CmuVt, CmuHt;
   // viscous flow: face sigma slopes (sigma_transform) and the explicit
   // viscous terms of diffusion (src/nhwave.F:6785-7141)
   A3 DelxSl, DelySl, Diffxx, Diffxy, Diffyx, Diffyy, Diffzx, Diffzy;
@@ -236,7 +237,7 @@ struct Model {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
     if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
-    if (p.viscous_flow && (p.ivturb != 1 || p.ihturb != 1)) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && (p.ivturb < 1 || p.ivturb > 2 || p.ihturb < 1 || p.ihturb > 2)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
@@ -317,7 +318,7 @@ struct Model {
     for (A3* a : {&U, &V, &W, &DU, &DV, &DW, &DU0, &DV0, &DW0, &U0, &V0, &W0, &U00, &V00, &W00, &P, &DelxU,
                   &DelyU, &DelzU, &DelxV,
                   &DelyV, &DelzV, &DelxW, &DelyW, &DelzW, &DelxDU, &DelyDU, &DelxDV, &DelyDV,
-                  &DelxDW, &DelyDW, &DelxSc, &DelySc})
+                  &DelxDW, &DelyDW, &DelxSc, &DelySc, &CmuVt, &CmuHt})
       a->init(Mloc, Nloc, Kloc);
     for (A3* a : {&Omega, &Uf, &Vf, &Wf, &UzL, &UzR, &VzL, &VzR, &WzL, &WzR, &Fz, &Gz, &Hz})
       a->init(Mloc, Nloc, Kloc1);
@@ -485,13 +486,7 @@ struct Model {
   void initial(const double* eta0, const double* uvw0) {
     TIME = Zero; RUN_STEP = 0; dt = p.dt_ini;
     Sponge.fill(1.0);
-    Cmu = p.visc; CmuR = 0.0; CmuVt = 0.0; CmuHt = 0.0;
-    if (p.viscous_flow) {   // seeding values (src/initialize.F:3172-3195)
-      const double Tke_min = (double)1.e-9f, Eps_min = (double)1.e-9f;
-      const double Cmut_min = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (Tke_min * Tke_min) / Eps_min;
-      CmuHt = Cmut_min;
-      CmuVt = Cmut_min;
-    }
+    Cmu = p.visc; CmuR = 0.0; CmuVt.fill(0.0); CmuHt.fill(0.0);
     Eta.fill(0.0);
     const int Mg = p.Mglob, Ng = p.Nglob, Kg = p.Kglob;
     if (eta0 || uvw0) {
@@ -529,6 +524,14 @@ struct Model {
           DV(i, j, k) = D(i, j) * V(i, j, k) * Mask(i, j);
           DW(i, j, k) = D(i, j) * W(i, j, k) * Mask(i, j);
         }
+    // seeding values (src/initialize.F:3172-3195), after vel_bc, which so
+    // saw CmuVt = 0
+    if (p.viscous_flow) {
+      const double Tke_min = (double)1.e-9f, Eps_min = (double)1.e-9f;
+      const double Cmut_min = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (Tke_min * Tke_min) / Eps_min;
+      CmuHt.fill(Cmut_min);
+      CmuVt.fill(Cmut_min);
+    }
     if (p.time_order == 3) {
       It_Order = 3;
       ALPHA[0] = 0.0; ALPHA[1] = (double)(3.0f / 4.0f); ALPHA[2] = (double)(1.0f / 3.0f);
@@ -577,9 +580,9 @@ struct Model {
       for (int k = Kbeg; k <= Kend; ++k)
         for (int j = Jbeg; j <= Jend; ++j)
           for (int i = Ibeg; i <= Iend; ++i) {
-            double tmp1 = dx * dx / (std::fabs(CmuHt) + (double)1.e-16f);
+            double tmp1 = dx * dx / (std::fabs(CmuHt(i, j, k)) + (double)1.e-16f);
             if (tmp1 < tmp2) tmp2 = tmp1;
-            tmp1 = dy * dy / (std::fabs(CmuHt) + (double)1.e-16f);
+            tmp1 = dy * dy / (std::fabs(CmuHt(i, j, k)) + (double)1.e-16f);
             if (tmp1 < tmp2) tmp2 = tmp1;
           }
       dt_viscous = p.viscous_number * tmp2;
@@ -1793,17 +1796,17 @@ struct Model {
   }
 
   // -------------------------------------------------------------- diffusion
-  // Explicit part of the viscous terms (src/nhwave.F:6785-7141) for uniform
-  // viscosities: Diffxx/Diffxy enter R2, Diffyx/Diffyy R3, Diffzx/Diffzy
+  // Explicit part of the viscous terms (src/nhwave.F:6785-7141), with the
+  // cells' CmuHt: Diffxx/Diffxy enter R2, Diffyx/Diffyy R3, Diffzx/Diffzy
   // R4 (the reference also forms Diffxz/Diffyz, which nothing reads).
   // The sigma slopes are those of the last sigma_transform; D is the
   // current one.  Every bracket keeps the reference's evaluation order.
   void diffusion() {
     for (A3* a : {&Diffxx, &Diffxy, &Diffyx, &Diffyy, &Diffzx, &Diffzy}) a->fill(0.0);
     const double Schmidt = p.schmidt;
-    // face and cell viscosities of uniform Cmu / CmuHt
-    const double nuF = 0.5 * (Cmu + Cmu) + 0.5 * (CmuHt + CmuHt) / Schmidt;
-    const double nuC = Cmu + CmuHt / Schmidt;
+    // face viscosity between cells a and b, and cell viscosity
+    auto nuF = [&](double ha, double hb) { return 0.5 * (Cmu + Cmu) + 0.5 * (ha + hb) / Schmidt; };
+    auto nuC = [&](int ii, int jj, int kk) { return Cmu + CmuHt(ii, jj, kk) / Schmidt; };
     for (int k = Kbeg; k <= Kend; ++k) {
       const double L1top = dsig(k + 1) / (dsig(k) + dsig(k + 1)), L2top = dsig(k) / (dsig(k) + dsig(k + 1));
       const double L1bot = dsig(k) / (dsig(k) + dsig(k - 1)), L2bot = dsig(k - 1) / (dsig(k) + dsig(k - 1));
@@ -1811,12 +1814,17 @@ struct Model {
       const double ac = -dsigck / (dsigck + dsigck1) / dsigck1;
       const double bc = (dsigck - dsigck1) / (dsigck * dsigck1);
       const double gc = dsigck1 / (dsigck + dsigck1) / dsigck;
-      const double nuH_top = (L1top * Cmu + L2top * Cmu) + (L1top * CmuHt + L2top * CmuHt) / Schmidt;
-      const double nuH_bot = (L1bot * Cmu + L2bot * Cmu) + (L1bot * CmuHt + L2bot * CmuHt) / Schmidt;
       for (int j = Jbeg; j <= Jend; ++j)
         for (int i = Ibeg; i <= Iend; ++i) {
           if (Mask(i, j) == 0) continue;
           const double Dc = D(i, j);
+          const double nuH_top = (L1top * Cmu + L2top * Cmu) + (L1top * CmuHt(i, j, k) + L2top * CmuHt(i, j, k + 1)) / Schmidt;
+          const double nuH_bot = (L1bot * Cmu + L2bot * Cmu) + (L1bot * CmuHt(i, j, k - 1) + L2bot * CmuHt(i, j, k)) / Schmidt;
+          const double H = CmuHt(i, j, k);
+          const double nuE = nuF(CmuHt(i + 1, j, k), H), nuW = nuF(H, CmuHt(i - 1, j, k));
+          const double nuN = nuF(CmuHt(i, j + 1, k), H), nuS = nuF(H, CmuHt(i, j - 1, k));
+          const double cE = nuC(i + 1, j, k), cW = nuC(i - 1, j, k), cN = nuC(i, j + 1, k), cS = nuC(i, j - 1, k);
+          const double cD = nuC(i, j, k - 1), c0 = nuC(i, j, k), cU = nuC(i, j, k + 1);
           // three-level sums  a F(k-1) G(k-1) + b F(k) G(k) + c F(k+1) G(k+1)
           auto s3 = [&](A3& F, A3& G, int ii, int jj) {
             return ac * F(ii, jj, k - 1) * G(ii, jj, k - 1) + bc * F(ii, jj, k) * G(ii, jj, k) +
@@ -1848,51 +1856,51 @@ struct Model {
           vco(DelySl, yA, yB, yC);
           // d/dx[2 nu d/dx DU] + d/dx[2 nu d/dsigma(DU Sx)] + d/dsigma[2 nu Sx d/dx DU]
           Diffxx(i, j, k) =
-              (2.0 * nuF * (DU(i + 1, j, k) - DU(i, j, k)) / dx - 2.0 * nuF * (DU(i, j, k) - DU(i - 1, j, k)) / dx) / dx +
-              (2.0 * nuC * s3(DU, DelxSc, i + 1, j) - 2.0 * nuC * s3(DU, DelxSc, i - 1, j)) / 2.0 / dx +
-              (ac * 2.0 * nuC * DelxSc(i, j, k - 1) * (DU(i + 1, j, k - 1) - DU(i - 1, j, k - 1)) / 2.0 / dx +
-               bc * 2.0 * nuC * DelxSc(i, j, k) * (DU(i + 1, j, k) - DU(i - 1, j, k)) / 2.0 / dx +
-               gc * 2.0 * nuC * DelxSc(i, j, k + 1) * (DU(i + 1, j, k + 1) - DU(i - 1, j, k + 1)) / 2.0 / dx);
+              (2.0 * nuE * (DU(i + 1, j, k) - DU(i, j, k)) / dx - 2.0 * nuW * (DU(i, j, k) - DU(i - 1, j, k)) / dx) / dx +
+              (2.0 * cE * s3(DU, DelxSc, i + 1, j) - 2.0 * cW * s3(DU, DelxSc, i - 1, j)) / 2.0 / dx +
+              (ac * 2.0 * cD * DelxSc(i, j, k - 1) * (DU(i + 1, j, k - 1) - DU(i - 1, j, k - 1)) / 2.0 / dx +
+               bc * 2.0 * c0 * DelxSc(i, j, k) * (DU(i + 1, j, k) - DU(i - 1, j, k)) / 2.0 / dx +
+               gc * 2.0 * cU * DelxSc(i, j, k + 1) * (DU(i + 1, j, k + 1) - DU(i - 1, j, k + 1)) / 2.0 / dx);
           auto mixed = [&](int kk) {   // d/dy DU + d/dx DV at level kk
             return (DU(i, j + 1, kk) - DU(i, j - 1, kk)) / 2.0 / dy + (DV(i + 1, j, kk) - DV(i - 1, j, kk)) / 2.0 / dx;
           };
           Diffxy(i, j, k) =
-              (nuF * (DU(i, j + 1, k) - DU(i, j, k)) / dy - nuF * (DU(i, j, k) - DU(i, j - 1, k)) / dy) / dy +
-              (nuC * s3x((DV(i + 1, j + 1, k) - DV(i - 1, j + 1, k)) / 2.0 / dx, i, j + 1) -
-               nuC * s3x((DV(i + 1, j - 1, k) - DV(i - 1, j - 1, k)) / 2.0 / dx, i, j - 1)) /
+              (nuN * (DU(i, j + 1, k) - DU(i, j, k)) / dy - nuS * (DU(i, j, k) - DU(i, j - 1, k)) / dy) / dy +
+              (cN * s3x((DV(i + 1, j + 1, k) - DV(i - 1, j + 1, k)) / 2.0 / dx, i, j + 1) -
+               cS * s3x((DV(i + 1, j - 1, k) - DV(i - 1, j - 1, k)) / 2.0 / dx, i, j - 1)) /
                   2.0 / dy +
-              (ac * nuC * DelySc(i, j, k - 1) * mixed(k - 1) + bc * nuC * DelySc(i, j, k) * mixed(k) +
-               gc * nuC * DelySc(i, j, k + 1) * mixed(k + 1)) +
+              (ac * cD * DelySc(i, j, k - 1) * mixed(k - 1) + bc * c0 * DelySc(i, j, k) * mixed(k) +
+               gc * cU * DelySc(i, j, k + 1) * mixed(k + 1)) +
               (yA * DelxSc(i, j, k - 1) * DV(i, j, k - 1) + yB * DelxSc(i, j, k) * DV(i, j, k) +
                yC * DelxSc(i, j, k + 1) * DV(i, j, k + 1));
           Diffyx(i, j, k) =
-              (nuF * (DV(i + 1, j, k) - DV(i, j, k)) / dx - nuF * (DV(i, j, k) - DV(i - 1, j, k)) / dx) / dx +
-              (nuC * s3x((DU(i + 1, j + 1, k) - DU(i + 1, j - 1, k)) / 2.0 / dy, i + 1, j) -
-               nuC * s3x((DU(i - 1, j + 1, k) - DU(i - 1, j - 1, k)) / 2.0 / dy, i - 1, j)) /
+              (nuE * (DV(i + 1, j, k) - DV(i, j, k)) / dx - nuW * (DV(i, j, k) - DV(i - 1, j, k)) / dx) / dx +
+              (cE * s3x((DU(i + 1, j + 1, k) - DU(i + 1, j - 1, k)) / 2.0 / dy, i + 1, j) -
+               cW * s3x((DU(i - 1, j + 1, k) - DU(i - 1, j - 1, k)) / 2.0 / dy, i - 1, j)) /
                   2.0 / dx +
-              (ac * nuC * DelxSc(i, j, k - 1) * mixed(k - 1) + bc * nuC * DelxSc(i, j, k) * mixed(k) +
-               gc * nuC * DelxSc(i, j, k + 1) * mixed(k + 1)) +
+              (ac * cD * DelxSc(i, j, k - 1) * mixed(k - 1) + bc * c0 * DelxSc(i, j, k) * mixed(k) +
+               gc * cU * DelxSc(i, j, k + 1) * mixed(k + 1)) +
               (xA * DelySc(i, j, k - 1) * DU(i, j, k - 1) + xB * DelySc(i, j, k) * DU(i, j, k) +
                xC * DelySc(i, j, k + 1) * DU(i, j, k + 1));
           Diffyy(i, j, k) =
-              (2.0 * nuF * (DV(i, j + 1, k) - DV(i, j, k)) / dy - 2.0 * nuF * (DV(i, j, k) - DV(i, j - 1, k)) / dy) / dy +
-              (2.0 * nuC * s3(DV, DelySc, i, j + 1) - 2.0 * nuC * s3(DV, DelySc, i, j - 1)) / 2.0 / dy +
-              (ac * 2.0 * nuC * DelySc(i, j, k - 1) * (DV(i, j + 1, k - 1) - DV(i, j - 1, k - 1)) / 2.0 / dy +
-               bc * 2.0 * nuC * DelySc(i, j, k) * (DV(i, j + 1, k) - DV(i, j - 1, k)) / 2.0 / dy +
-               gc * 2.0 * nuC * DelySc(i, j, k + 1) * (DV(i, j + 1, k + 1) - DV(i, j - 1, k + 1)) / 2.0 / dy);
+              (2.0 * nuN * (DV(i, j + 1, k) - DV(i, j, k)) / dy - 2.0 * nuS * (DV(i, j, k) - DV(i, j - 1, k)) / dy) / dy +
+              (2.0 * cN * s3(DV, DelySc, i, j + 1) - 2.0 * cS * s3(DV, DelySc, i, j - 1)) / 2.0 / dy +
+              (ac * 2.0 * cD * DelySc(i, j, k - 1) * (DV(i, j + 1, k - 1) - DV(i, j - 1, k - 1)) / 2.0 / dy +
+               bc * 2.0 * c0 * DelySc(i, j, k) * (DV(i, j + 1, k) - DV(i, j - 1, k)) / 2.0 / dy +
+               gc * 2.0 * cU * DelySc(i, j, k + 1) * (DV(i, j + 1, k + 1) - DV(i, j - 1, k + 1)) / 2.0 / dy);
           Diffzx(i, j, k) =
-              (nuF * (DW(i + 1, j, k) - DW(i, j, k)) / dx - nuF * (DW(i, j, k) - DW(i - 1, j, k)) / dx) / dx +
-              (nuC * s3w(DelxSc, DU, i + 1, j) - nuC * s3w(DelxSc, DU, i - 1, j)) / 2.0 / dx +
-              (ac * nuC * DelxSc(i, j, k - 1) * (DW(i + 1, j, k - 1) - DW(i - 1, j, k - 1)) / 2.0 / dx +
-               bc * nuC * DelxSc(i, j, k) * (DW(i + 1, j, k) - DW(i - 1, j, k)) / 2.0 / dx +
-               gc * nuC * DelxSc(i, j, k + 1) * (DW(i + 1, j, k + 1) - DW(i - 1, j, k + 1)) / 2.0 / dx) +
+              (nuE * (DW(i + 1, j, k) - DW(i, j, k)) / dx - nuW * (DW(i, j, k) - DW(i - 1, j, k)) / dx) / dx +
+              (cE * s3w(DelxSc, DU, i + 1, j) - cW * s3w(DelxSc, DU, i - 1, j)) / 2.0 / dx +
+              (ac * cD * DelxSc(i, j, k - 1) * (DW(i + 1, j, k - 1) - DW(i - 1, j, k - 1)) / 2.0 / dx +
+               bc * c0 * DelxSc(i, j, k) * (DW(i + 1, j, k) - DW(i - 1, j, k)) / 2.0 / dx +
+               gc * cU * DelxSc(i, j, k + 1) * (DW(i + 1, j, k + 1) - DW(i - 1, j, k + 1)) / 2.0 / dx) +
               (xA * DU(i, j, k - 1) / Dc + xB * DU(i, j, k) / Dc + xC * DU(i, j, k + 1) / Dc);
           Diffzy(i, j, k) =
-              (nuF * (DW(i, j + 1, k) - DW(i, j, k)) / dy - nuF * (DW(i, j, k) - DW(i, j - 1, k)) / dy) / dy +
-              (nuC * s3w(DelySc, DV, i, j + 1) - nuC * s3w(DelySc, DV, i, j - 1)) / 2.0 / dy +
-              (ac * nuC * DelySc(i, j, k - 1) * (DW(i, j + 1, k - 1) - DW(i, j - 1, k - 1)) / 2.0 / dy +
-               bc * nuC * DelySc(i, j, k) * (DW(i, j + 1, k) - DW(i, j - 1, k)) / 2.0 / dy +
-               gc * nuC * DelySc(i, j, k + 1) * (DW(i, j + 1, k + 1) - DW(i, j - 1, k + 1)) / 2.0 / dy) +
+              (nuN * (DW(i, j + 1, k) - DW(i, j, k)) / dy - nuS * (DW(i, j, k) - DW(i, j - 1, k)) / dy) / dy +
+              (cN * s3w(DelySc, DV, i, j + 1) - cS * s3w(DelySc, DV, i, j - 1)) / 2.0 / dy +
+              (ac * cD * DelySc(i, j, k - 1) * (DW(i, j + 1, k - 1) - DW(i, j - 1, k - 1)) / 2.0 / dy +
+               bc * c0 * DelySc(i, j, k) * (DW(i, j + 1, k) - DW(i, j - 1, k)) / 2.0 / dy +
+               gc * cU * DelySc(i, j, k + 1) * (DW(i, j + 1, k + 1) - DW(i, j - 1, k + 1)) / 2.0 / dy) +
               (yA * DV(i, j, k - 1) / Dc + yB * DV(i, j, k) / Dc + yC * DV(i, j, k + 1) / Dc);
         }
     }
@@ -1923,16 +1931,18 @@ struct Model {
     const int n = Kend - Kbeg + 1;
     std::vector<double> A(n), B(n), C(n), Rhs(n), X(n);
     const double Schmidt = p.schmidt, Dc = D(i, j);
-    // face viscosity between levels k1 and k2 (uniform Cmu, CmuR, CmuVt)
-    const double nuz = 0.5 * (((Cmu + Cmu) + CmuR) + CmuR) + 0.5 * (CmuVt + CmuVt) / Schmidt;
+    // face viscosity between levels k1 and k2 (Cmu and CmuR uniform)
+    auto nuz = [&](int k1, int k2) {
+      return 0.5 * (((Cmu + Cmu) + CmuR) + CmuR) + 0.5 * (CmuVt(i, j, k1) + CmuVt(i, j, k2)) / Schmidt;
+    };
     A3& F = which == 0 ? DU : which == 1 ? DV : DW;
     for (int k = Kbeg; k <= Kend; ++k) {
       const int q = k - Kbeg;
-      A[q] = k == Kbeg ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k - 1)));
-      C[q] = k == Kend ? 0.0 : -dt / (Dc * Dc) * nuz / (0.5 * dsig(k) * (dsig(k) + dsig(k + 1)));
+      A[q] = k == Kbeg ? 0.0 : -dt / (Dc * Dc) * nuz(k - 1, k) / (0.5 * dsig(k) * (dsig(k) + dsig(k - 1)));
+      C[q] = k == Kend ? 0.0 : -dt / (Dc * Dc) * nuz(k, k + 1) / (0.5 * dsig(k) * (dsig(k) + dsig(k + 1)));
       if (which < 2) {
         if (k == Kbeg && p.bc_z0 == 2)
-          B[q] = 1.0 - C[q] + dt / (Dc * Dc) * (Cmu + CmuR + CmuVt / Schmidt) / (0.5 * dsig(k) * dsig(k));
+          B[q] = 1.0 - C[q] + dt / (Dc * Dc) * (Cmu + CmuR + CmuVt(i, j, k) / Schmidt) / (0.5 * dsig(k) * dsig(k));
         else
           B[q] = 1.0 - A[q] - C[q];
         if (k == Kbeg && p.bc_z0 == 5) {
@@ -1951,13 +1961,13 @@ struct Model {
           Rhs[q] = F(i, j, k);
         }
       } else if (k == Kbeg) {
-        B[q] = 1.0 - C[q] + dt / (Dc * Dc) * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1)));
+        B[q] = 1.0 - C[q] + dt / (Dc * Dc) * nuz(k - 1, k) / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1)));
         const double Wbot = -DeltH(i, j) - U(i, j, Kbeg) * DelxH(i, j) - V(i, j, Kbeg) * DelyH(i, j);
-        Rhs[q] = F(i, j, k) + dt / Dc * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1))) * Wbot;
+        Rhs[q] = F(i, j, k) + dt / Dc * nuz(k - 1, k) / (0.25 * dsig(k) * (dsig(k) + dsig(k - 1))) * Wbot;
       } else if (k == Kend) {
-        B[q] = 1.0 - A[q] + dt / (Dc * Dc) * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1)));
+        B[q] = 1.0 - A[q] + dt / (Dc * Dc) * nuz(k, k + 1) / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1)));
         const double Wtop = (Eta(i, j) - Eta0(i, j)) / dt + U(i, j, Kend) * DelxEta(i, j) + V(i, j, Kend) * DelyEta(i, j);
-        Rhs[q] = F(i, j, k) + dt / Dc * nuz / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1))) * Wtop;
+        Rhs[q] = F(i, j, k) + dt / Dc * nuz(k, k + 1) / (0.25 * dsig(k) * (dsig(k) + dsig(k + 1))) * Wtop;
       } else {
         B[q] = 1.0 - A[q] - C[q];
         Rhs[q] = F(i, j, k);
@@ -1970,14 +1980,14 @@ struct Model {
   // ------------------------------------------------------- get_UVW/vel_bc
   // Wall friction factor of a BC = 5 side (src/nhwave.F:4486-4493): h is the
   // grid spacing across the wall, a and b the tangential velocities of the
-  // first interior cell
-  double wall_phi(double h, double a, double b) const {
+  // first interior cell, ht its CmuHt
+  double wall_phi(double h, double a, double b, double ht) const {
     double Cdrag = p.cd0;
     if (p.ibot != 1) {
       const double lg = 1. / Kappa * std::log(30.0 * h / 2.0 / p.zob);
       Cdrag = 1. / (lg * lg);
     }
-    const double Phi = h * Cdrag * std::sqrt(a * a + b * b) / (Cmu + CmuHt);
+    const double Phi = h * Cdrag * std::sqrt(a * a + b * b) / (Cmu + ht);
     return dmin(Phi, 2.0);
   }
 
@@ -1991,7 +2001,7 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int j = Jbeg; j <= Jend; ++j) {
         if (p.bc_x0 == 5) {
-          const double Phi = wall_phi(dx, V(Ibeg, j, k), W(Ibeg, j, k));
+          const double Phi = wall_phi(dx, V(Ibeg, j, k), W(Ibeg, j, k), CmuHt(Ibeg, j, k));
           for (int i = 1; i <= Nghost; ++i) {
             U(Ibeg - i, j, k) = -U(Ibeg + i - 1, j, k);
             V(Ibeg - i, j, k) = (1.0 - Phi) * V(Ibeg + i - 1, j, k);
@@ -2002,7 +2012,7 @@ struct Model {
           }
         }
         if (p.bc_xn == 5) {
-          const double Phi = wall_phi(dx, V(Iend, j, k), W(Iend, j, k));
+          const double Phi = wall_phi(dx, V(Iend, j, k), W(Iend, j, k), CmuHt(Iend, j, k));
           for (int i = 1; i <= Nghost; ++i) {
             U(Iend + i, j, k) = -U(Iend - i + 1, j, k);
             V(Iend + i, j, k) = (1.0 - Phi) * V(Iend - i + 1, j, k);
@@ -2016,7 +2026,7 @@ struct Model {
     for (int k = Kbeg; k <= Kend; ++k)
       for (int i = Ibeg; i <= Iend; ++i) {
         if (p.bc_y0 == 5) {
-          const double Phi = wall_phi(dy, U(i, Jbeg, k), W(i, Jbeg, k));
+          const double Phi = wall_phi(dy, U(i, Jbeg, k), W(i, Jbeg, k), CmuHt(i, Jbeg, k));
           for (int j = 1; j <= Nghost; ++j) {
             U(i, Jbeg - j, k) = (1.0 - Phi) * U(i, Jbeg + j - 1, k);
             V(i, Jbeg - j, k) = -V(i, Jbeg + j - 1, k);
@@ -2027,7 +2037,7 @@ struct Model {
           }
         }
         if (p.bc_yn == 5) {
-          const double Phi = wall_phi(dy, U(i, Jend, k), W(i, Jend, k));
+          const double Phi = wall_phi(dy, U(i, Jend, k), W(i, Jend, k), CmuHt(i, Jend, k));
           for (int j = 1; j <= Nghost; ++j) {
             U(i, Jend + j, k) = (1.0 - Phi) * U(i, Jend - j + 1, k);
             V(i, Jend + j, k) = -V(i, Jend - j + 1, k);
@@ -2143,9 +2153,11 @@ struct Model {
       delyFun_3D(UzR, DelyUzR); delyFun_3D(VzR, DelyVzR); delyFun_3D(WzR, DelyWzR);
     }
     const double MinDepBC = (double)0.01f;
-    const double visc_top = Small + 0.5 * (Cmu + CmuR + CmuVt + Cmu + CmuR + CmuVt);
     for (int j = Jbeg; j <= Jend; ++j)
       for (int i = Ibeg; i <= Iend; ++i) {
+        const double visc_top =
+            Small + 0.5 * (Cmu + CmuR + CmuVt(i, j, Kend) + Cmu + CmuR + CmuVt(i, j, Kend + 1));
+        const double visc_bot = Cmu + CmuR + CmuVt(i, j, Kbeg);
         const double dxe = DelxEta(i, j), dye = DelyEta(i, j), Dij = D(i, j);
         const double Atop = std::sqrt(1.0 + dxe * dxe + dye * dye);
         const double Fext_Wind1 = 1.0 / Atop * ((1 - dxe * dxe) * Wsx(i, j) - dxe * dye * Wsy(i, j));
@@ -2164,11 +2176,11 @@ struct Model {
           const double Dz1 = 0.5 * Dij * dsig(Kbeg) / Abot;
           const double Z0 = p.zob / 30.0;
           double Cdrag = p.ibot == 1 ? p.cd0 : (Kappa / std::log(Dz1 / Z0)) * (Kappa / std::log(Dz1 / Z0));
-          Cdrag = dmin(Cdrag, (Cmu + CmuR + CmuVt) / Dz1 / (DUmag + Small) * Dij);
+          Cdrag = dmin(Cdrag, visc_bot / Dz1 / (DUmag + Small) * Dij);
           double TauBot1 = Zero, TauBot2 = Zero;
           if (p.bc_z0 == 2) {
-            TauBot1 = DUprime / Dij / Dz1 * (Cmu + CmuR + CmuVt);
-            TauBot2 = DVprime / Dij / Dz1 * (Cmu + CmuR + CmuVt);
+            TauBot1 = DUprime / Dij / Dz1 * visc_bot;
+            TauBot2 = DVprime / Dij / Dz1 * visc_bot;
           } else if (p.bc_z0 == 5) {
             TauBot1 = Cdrag * DUprime * DUmag / (Dij * Dij);
             TauBot2 = Cdrag * DVprime * DUmag / (Dij * Dij);
@@ -2184,7 +2196,7 @@ struct Model {
             DV(i, j, Kbeg - k) = DV(i, j, Kbeg + k - 1);
           } else {   // stress ghosts (src/nhwave.F:4869-4903)
             const double dsb = sigc(Kbeg + k - 1) - sigc(Kbeg - k);
-            const double vb = Small + Cmu + CmuR + CmuVt;
+            const double vb = Small + Cmu + CmuR + CmuVt(i, j, Kbeg);
             DU(i, j, Kbeg - k) = DU(i, j, Kbeg + k - 1) -
                 dsb * (Fext_Bot1 * (Dij * Dij / Abot / vb) +
                        dxh * (DW(i, j, Kbeg + k - 1) - Dij * WzR(i, j, Kbeg)) / (dsb / 2.0) +
@@ -2684,13 +2696,69 @@ struct Model {
         }
     get_UVW();
     get_Omega();
-    // eval_turb (src/nhwave.F:6544-6686) with IVTURB = IHTURB = 1.  The
-    // reference calls it after sponge_damping, which reads no viscosity.
-    if (p.viscous_flow) {
-      CmuVt = p.cvs;
-      CmuHt = p.chs;
-    }
     return st;
+  }
+
+  // eval_turb (src/nhwave.F:6544-6782), called after sponge_damping.
+  // Vertical: IVTURB 1 CmuVt = Cvs; 2 the subgrid model CmuVt = Cvs D
+  // dsig^2 |d(U,V)/dsigma| on every level but the outermost ghosts, which
+  // copy their neighbours.  Horizontal: IHTURB 1 CmuHt = Chs; 2 CmuHt = Chs
+  // dx dy |S| from the horizontal strain rates, then mirrored into the
+  // ghosts of the sides (interior rows) and of the bed and surface
+  // (interior columns).  The reference's Strxy reads U(i,j+1,j), the row
+  // index where the level belongs (:6695); the level k is used here.
+  void eval_turb() {
+    if (!p.viscous_flow) return;
+    if (p.ivturb == 1) {
+      CmuVt.fill(p.cvs);
+    } else {
+      for (int i = 1; i <= Mloc; ++i)
+        for (int j = 1; j <= Nloc; ++j) {
+          for (int k = 2; k <= Kloc - 1; ++k) {
+            const double DelsU = (U(i, j, k + 1) - U(i, j, k - 1)) / (sigc(k + 1) - sigc(k - 1));
+            const double DelsV = (V(i, j, k + 1) - V(i, j, k - 1)) / (sigc(k + 1) - sigc(k - 1));
+            CmuVt(i, j, k) = p.cvs * D(i, j) * (dsig(k) * dsig(k)) * std::sqrt(DelsU * DelsU + DelsV * DelsV);
+          }
+          CmuVt(i, j, 1) = CmuVt(i, j, 2);
+          CmuVt(i, j, Kloc) = CmuVt(i, j, Kloc - 1);
+        }
+    }
+    if (p.ihturb == 1) {
+      CmuHt.fill(p.chs);
+      return;
+    }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          const double ds = sigc(k + 1) - sigc(k - 1);
+          const double Strxx = (U(i + 1, j, k) - U(i - 1, j, k)) / (2.0 * dx) +
+                               (U(i, j, k + 1) - U(i, j, k - 1)) / ds * DelxSc(i, j, k);
+          const double Stryy = (V(i, j + 1, k) - V(i, j - 1, k)) / (2.0 * dy) +
+                               (V(i, j, k + 1) - V(i, j, k - 1)) / ds * DelySc(i, j, k);
+          const double Strxy = 0.5 * ((U(i, j + 1, k) - U(i, j - 1, k)) / (2.0 * dy) +
+                                      (U(i, j, k + 1) - U(i, j, k - 1)) / ds * DelySc(i, j, k) +
+                                      (V(i + 1, j, k) - V(i - 1, j, k)) / (2.0 * dx) +
+                                      (V(i, j, k + 1) - V(i, j, k - 1)) / ds * DelxSc(i, j, k));
+          CmuHt(i, j, k) = p.chs * dx * dy * std::sqrt(Strxx * Strxx + 2.0 * (Strxy * Strxy) + Stryy * Stryy);
+        }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) {
+          CmuHt(Ibeg - i, j, k) = CmuHt(Ibeg + i - 1, j, k);
+          CmuHt(Iend + i, j, k) = CmuHt(Iend - i + 1, j, k);
+        }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) {
+          CmuHt(i, Jbeg - j, k) = CmuHt(i, Jbeg + j - 1, k);
+          CmuHt(i, Jend + j, k) = CmuHt(i, Jend - j + 1, k);
+        }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) {
+          CmuHt(i, j, Kbeg - k) = CmuHt(i, j, Kbeg + k - 1);
+          CmuHt(i, j, Kend + k) = CmuHt(i, j, Kend - k + 1);
+        }
   }
 
   void sponge_damping() {
@@ -2725,6 +2793,7 @@ struct Model {
       int e = eval_duvw(s);
       if (e != NHW_OK && worst == NHW_OK) worst = e;
       if (p.sponge_on) sponge_damping();
+      eval_turb();
     }
     if (worst == NHW_ERR_NAN) status = worst;
     return worst;
@@ -2795,6 +2864,7 @@ struct Model {
       case NHW_F_HX: a3(Hx); break; case NHW_F_EY: a3(Ey); break; case NHW_F_FY: a3(Fy); break;
       case NHW_F_GY: a3(Gy); break; case NHW_F_HY: a3(Hy); break; case NHW_F_FZ: a3(Fz); break;
       case NHW_F_GZ: a3(Gz); break; case NHW_F_HZ: a3(Hz); break;
+      case NHW_F_CMUVT: a3(CmuVt); break; case NHW_F_CMUHT: a3(CmuHt); break;
       default: break;
     }
     return r;
@@ -2827,6 +2897,7 @@ void orc_update_mask(void* o) { static_cast<Model*>(o)->update_mask(); }
 void orc_update_wave_bc(void* o) { static_cast<Model*>(o)->update_wave_bc(); }
 void orc_update_vars(void* o) { Model* m = static_cast<Model*>(o); m->update_wind(); m->update_vars(); }
 void orc_source_terms(void* o) { static_cast<Model*>(o)->source_terms(); }
+void orc_eval_turb(void* o) { static_cast<Model*>(o)->eval_turb(); }
 void orc_fluxes(void* o) { static_cast<Model*>(o)->fluxes(); }
 int orc_eval_duvw(void* o, int istep) { return static_cast<Model*>(o)->eval_duvw(istep); }
 void orc_sponge_damping(void* o) { static_cast<Model*>(o)->sponge_damping(); }

@@ -55,7 +55,7 @@ def lib():
             getattr(L, name).argtypes = [vp]
         L.orc_eval_duvw.argtypes = [vp, i32]
         for name in ("orc_update_bathymetry", "orc_update_wave_bc", "orc_update_mask", "orc_update_vars",
-                     "orc_source_terms", "orc_fluxes", "orc_sponge_damping",
+                     "orc_source_terms", "orc_fluxes", "orc_sponge_damping", "orc_eval_turb",
                      "orc_generate_coef_rhs"):
             getattr(L, name).argtypes = [vp]
             getattr(L, name).restype = None
@@ -148,6 +148,9 @@ class Oracle:
 
     def sponge_damping(self):
         lib().orc_sponge_damping(self._h)
+
+    def eval_turb(self):
+        lib().orc_eval_turb(self._h)
 
     def step(self):
         return lib().orc_step(self._h)
@@ -264,6 +267,7 @@ def run_scenario(name: str, steps: int, tol: float = 1e-13, pinned: bool = False
                     raise RuntimeError(f"oracle eval_duvw: {rc}")
                 if o.params.sponge_on:
                     o.sponge_damping()
+                o.eval_turb()
         else:
             rc = o.step()
             if rc:

@@ -26,14 +26,15 @@ def _scen(name, precision, **attrs):
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,krylov", [("tiny_c2", 0), ("tiny_c3", 0), ("tiny_c4", 0), ("tiny_flume_lin", 0),
-                                         ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0)])
+                                         ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0),
+                                         ("tiny_visc_sgs", 0)])
 def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     """krylov = 2: the GMRES solver, whose basis lies behind the checkpointed
     prefix and is rebuilt by every solve.  tiny_open: the Orlanski boundary's
     two earlier time levels are part of the checkpointed state; tiny_flux_lr:
     so are FLUX_LR's outflow velocities of the last two steps; tiny_visc:
-    the sigma slopes the next viscous terms read, and whether eval_turb has
-    run, are too."""
+    the sigma slopes the next viscous terms read are too; tiny_visc_sgs: and
+    the cells' eddy viscosities of the last eval_turb."""
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, krylov_kernel=krylov)
     for _ in range(4):
@@ -49,7 +50,7 @@ def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     sa, sb = a.scalars(), b.scalars()
     assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
     assert sa.total_krylov_iters == sb.total_krylov_iters
-    for f in FIELDS:
+    for f in FIELDS + (["CMUVT", "CMUHT"] if a.params.viscous_flow else []):
         fid = getattr(F, f)
         assert np.array_equal(a.get(fid), b.get(fid)), f"{name} {f}"
 

@@ -16,10 +16,11 @@ pytestmark = pytest.mark.gpu
 CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east
 # side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
-# in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds),
-# and wall friction (BC = 5) on the sides
+# in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds;
+# the subgrid eddy viscosities, IVTURB = IHTURB = 2), and wall friction
+# (BC = 5) on the sides
 MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric",
-                      "tiny_wallfric"]
+                      "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_wallfric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -114,6 +115,9 @@ def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
             if g.params.sponge_on:
                 g.sponge_damping(); o.sponge_damping()
                 _cmp_exact(g, o, ["D", "ETA"] + STATE3D, f"sponge {rnd}.{s}")
+            if g.params.viscous_flow:
+                g.eval_turb(); o.eval_turb()
+                _cmp_exact(g, o, ["CMUVT", "CMUHT"], f"eval_turb {rnd}.{s}")
     g.close()
 
 
@@ -142,6 +146,7 @@ def step_pinned(g, o):
             assert obj.eval_duvw(s) == 0
             if obj.params.sponge_on:
                 obj.sponge_damping()
+            obj.eval_turb()
 
 
 @pytest.mark.parametrize("name", MORE_CASES)

@@ -380,6 +380,43 @@ def test_viscous_horizontal_mode_decays_at_the_diffusion_rate(oracle_mod):
     assert amps[1] / amps[0] == pytest.approx(math.exp(-0.05 * lam * t), rel=0.01)
 
 
+def test_subgrid_eddy_viscosities_of_a_linear_flow(oracle_mod):
+    """eval_turb with IVTURB = IHTURB = 2 (src/nhwave.F:6653-6665, 6686-6774)
+    on U = a sigma + b x, V = W = 0 in a flat 1 m deep channel before the
+    first sigma_transform (sigma slopes zero): dU/dsigma = a, so CmuVt =
+    Cvs D dsig^2 |a| on the levels with both neighbours in the water; the
+    only strain rate is dU/dx = b, so CmuHt = Chs dx dy |b| away from the
+    side walls, mirrored into the ghosts.  The viscous time-step limit is
+    VISCOUS_NUMBER min(dx^2, dy^2) over the largest CmuHt."""
+    from nhwave_gb300 import default_params, fields as F
+    M, N, K, dx, dy, a, b, cvs, chs = 16, 3, 6, 0.2, 0.25, 0.03, 0.002, 0.15, 0.12
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.01, dt_max=1.0, tol=1e-10, itmax=2000,
+                       viscous_flow=1, visc=1e-6, cvs=cvs, chs=chs, ivturb=2, ihturb=2)
+    sig = (np.arange(K) + 0.5) / K
+    x = (np.arange(M) + 0.5) * dx
+    uvw = np.zeros((3, K, N, M))
+    uvw[0] = a * sig[:, None, None] + b * x[None, None, :]
+    o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
+    # the seeding viscosity Cmut_min = 0.09 Tke_min^2 / Eps_min (src/initialize.F:3178-3191)
+    assert np.allclose(o.get(F.CMUVT), 9.0e-2 * 1e-9, rtol=1e-6)
+    o.eval_turb()
+    ng = F.NG
+    cv, ch = o.get(F.CMUVT), o.get(F.CMUHT)
+    # (sigma levels and dsig are default-real values of the reference: 1e-6)
+    inner = (slice(ng + 1, ng + K - 1), slice(ng, ng + N), slice(ng, ng + M))
+    assert cv[inner] == pytest.approx(np.full(cv[inner].shape, cvs / K ** 2 * a), rel=1e-6)
+    cols = (slice(ng, ng + K), slice(ng, ng + N), slice(ng + 1, ng + M - 1))
+    assert ch[cols] == pytest.approx(np.full(ch[cols].shape, chs * dx * dy * b), rel=1e-9)
+    # ghosts mirror the interior across each side
+    for gi in range(1, ng + 1):
+        assert np.array_equal(ch[ng:ng + K, ng:ng + N, ng - gi], ch[ng:ng + K, ng:ng + N, ng + gi - 1])
+        assert np.array_equal(ch[ng - gi, ng:ng + N, ng:ng + M], ch[ng + gi - 1, ng:ng + N, ng:ng + M])
+        assert np.array_equal(ch[ng:ng + K, ng + N - 1 + gi, ng:ng + M], ch[ng:ng + K, ng + N - gi, ng:ng + M])
+    assert o.estimate_dt() == 0
+    top = np.abs(ch[ng:ng + K, ng:ng + N, ng:ng + M]).max()
+    assert o.scalars().dt == pytest.approx(min(1.05 * 0.01, p.viscous_number * min(dx, dy) ** 2 / top), rel=1e-6)
+
+
 def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):
     """VISCOUS_FLOW = T with zero viscosities: the tridiagonal systems are the
     identity and the explicit terms vanish, so the run equals the inviscid
