@@ -128,7 +128,11 @@ module nhw_gpu_iface
   integer(c_int), parameter :: NHW_F_HZ = 49
   integer(c_int), parameter :: NHW_F_CMUVT = 50
   integer(c_int), parameter :: NHW_F_CMUHT = 51
-  integer(c_int), parameter :: NHW_F_COUNT = 52
+  integer(c_int), parameter :: NHW_F_TKE = 52
+  integer(c_int), parameter :: NHW_F_EPS = 53
+  integer(c_int), parameter :: NHW_F_DTKE = 54
+  integer(c_int), parameter :: NHW_F_DEPS = 55
+  integer(c_int), parameter :: NHW_F_COUNT = 56
 
   ! ------------------------------------------------------------- nhw_params
   ! The input.txt keys the path reads (src/initialize.F:141-1321), in the C
@@ -189,6 +193,7 @@ module nhw_gpu_iface
      real(c_double)     :: sd_return
      real(c_double)     :: hm0, tp, freq_min, freq_max
      integer(c_int32_t) :: numfreq, wave_seed
+     integer(c_int32_t) :: prod_type
   end type nhw_params
 
   ! ------------------------------------------------------------ nhw_scalars
@@ -339,9 +344,10 @@ module nhw_gpu_iface
        import :: c_int, c_ptr
        type(c_ptr), value :: h
      end function nhw_sponge_damping
-     integer(c_int) function nhw_eval_turb(h) bind(C, name="nhw_eval_turb")
-       import :: c_int, c_ptr
+     integer(c_int) function nhw_eval_turb(h, istep) bind(C, name="nhw_eval_turb")
+       import :: c_int, c_int32_t, c_ptr
        type(c_ptr), value :: h
+       integer(c_int32_t), value :: istep
      end function nhw_eval_turb
 
      ! ------------------------------------------------------ whole steps

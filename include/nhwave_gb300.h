@@ -26,7 +26,8 @@
  *                             incl. poisson_solver src/pressure.F:63-245 and
  *                             generate_coef_rhs src/pressure.F:475-840)
  *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
- *   nhw_eval_turb          <- eval_turb            src/nhwave.F:6544-6782 (IVTURB, IHTURB 1 and 2;
+ *   nhw_eval_turb          <- eval_turb(ISTEP)     src/nhwave.F:6544-6782 (IVTURB 1, 2, 10 with
+ *                             kepsilon_3D :10030-11114; IHTURB 1, 2, >= 10;
  *                             viscous flow only, a no-op otherwise)
  *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
  *   nhw_mass               <- statistics' MassVolume  src/nhwave.F:3139-3148
@@ -193,6 +194,10 @@ typedef struct nhw_params {
      stream: phase_i = 2 pi u_i) unless nhw_set_wave_phases gives them. */
   double  hm0, tp, freq_min, freq_max;
   int32_t numfreq, wave_seed;
+  /* k-epsilon closure of IVTURB = 10 (src/initialize.F:388): PRODTYPE 1
+     production from the vertical shear of U and V, 2 from the vertical
+     shear, otherwise (3 in every example input) the full 3-D production */
+  int32_t prod_type;
 } nhw_params;
 
 /* Scalars the driver reads back after a step (module GLOBAL scalars). */
@@ -235,6 +240,8 @@ enum nhw_field {
   NHW_F_FZ, NHW_F_GZ, NHW_F_HZ,
   /* 3-D cell (Mloc,Nloc,Kloc): eddy viscosities of eval_turb (viscous flow only) */
   NHW_F_CMUVT, NHW_F_CMUHT,
+  /* 3-D cell (Mloc,Nloc,Kloc): k-epsilon state (viscous flow only) */
+  NHW_F_TKE, NHW_F_EPS, NHW_F_DTKE, NHW_F_DEPS,
   NHW_F_COUNT
 };
 
@@ -301,7 +308,7 @@ int nhw_source_terms(nhw_handle* h);
 int nhw_fluxes(nhw_handle* h);
 int nhw_eval_duvw(nhw_handle* h, int32_t istep);
 int nhw_sponge_damping(nhw_handle* h);
-int nhw_eval_turb(nhw_handle* h);
+int nhw_eval_turb(nhw_handle* h, int32_t istep);
 
 /* One full time step (estimate_dt ... last RK stage).  The first call
  * captures the step into a CUDA graph whose pressure-solve loops run on the

@@ -128,7 +128,11 @@ int nhw_eval_duvw(nhw_handle* h, int32_t istep) {
   return rs ? rs : rc;
 }
 int nhw_sponge_damping(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->sponge_damping(); return rc ? rc : h->s->sync(); }
-int nhw_eval_turb(nhw_handle* h) { NHW_GUARD(h); int rc = h->s->eval_turb(); return rc ? rc : h->s->sync(); }
+int nhw_eval_turb(nhw_handle* h, int32_t istep) {
+  NHW_GUARD(h);
+  int rc = h->s->eval_turb(istep);
+  return rc ? rc : h->s->sync();
+}
 
 int nhw_step(nhw_handle* h, double* time, double* dt, int32_t* run_step) {
   NHW_GUARD(h);

@@ -1420,30 +1420,34 @@ struct OpDiffusion {
 // (every column, ghosts included): IVTURB 1 CmuVt = Cvs; IVTURB 2 the
 // subgrid model CmuVt = Cvs D dsig^2 |d(U,V)/dsigma| on the levels 2 ..
 // Kloc-1 (1-based), the outermost ghost levels copying their neighbours.
-// IHTURB 1 fills CmuHt = Chs here; IHTURB 2 is OpTurbH + OpTurbHGhost.
+// IHTURB 1 fills CmuHt = Chs here and IHTURB >= 10 copies CmuVt, after the
+// vertical model (k-epsilon's kernels run first); IHTURB 2 is OpTurbH +
+// OpTurbHGhost.
 // Products in the reference's order, in FP64 (bit-exact in the FP64 form).
 struct OpTurbV {
   static constexpr const char* kName = "eval_turb_v";
   template <class T>
   __device__ void operator()(const Dev<T>& S, int i, int j) const {
     const long long q = i2(S, i, j);
+    T* cv = S.CmuVt + q;
+    if (S.ivturb == 1) {
+      for (int k = 0; k < S.Kloc; ++k) cv[S.sz * k] = (T)S.v_cvs;
+    } else if (S.ivturb == 2) {
+      const double Dq = S.D[q];
+      for (int k = 1; k <= S.Kloc - 2; ++k) {
+        const long long a = q + S.sz * (k + 1), b = q + S.sz * (k - 1);
+        const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+        const double dU = ((double)S.U[a] - (double)S.U[b]) / ds;
+        const double dV = ((double)S.V[a] - (double)S.V[b]) / ds;
+        cv[S.sz * k] = (T)(S.v_cvs * Dq * (S.dsig[k] * S.dsig[k]) * sqrt(dU * dU + dV * dV));
+      }
+      cv[0] = cv[S.sz];
+      cv[S.sz * (S.Kloc - 1)] = cv[S.sz * (S.Kloc - 2)];
+    }   // IVTURB = 10: the k-epsilon kernels set CmuVt before this one
     if (S.ihturb == 1)
       for (int k = 0; k < S.Kloc; ++k) S.CmuHt[q + S.sz * k] = (T)S.v_chs;
-    if (S.ivturb == 1) {
-      for (int k = 0; k < S.Kloc; ++k) S.CmuVt[q + S.sz * k] = (T)S.v_cvs;
-      return;
-    }
-    const double Dq = S.D[q];
-    T* cv = S.CmuVt + q;
-    for (int k = 1; k <= S.Kloc - 2; ++k) {
-      const long long a = q + S.sz * (k + 1), b = q + S.sz * (k - 1);
-      const double ds = S.sigc[k + 1] - S.sigc[k - 1];
-      const double dU = ((double)S.U[a] - (double)S.U[b]) / ds;
-      const double dV = ((double)S.V[a] - (double)S.V[b]) / ds;
-      cv[S.sz * k] = (T)(S.v_cvs * Dq * (S.dsig[k] * S.dsig[k]) * sqrt(dU * dU + dV * dV));
-    }
-    cv[0] = cv[S.sz];
-    cv[S.sz * (S.Kloc - 1)] = cv[S.sz * (S.Kloc - 2)];
+    else if (S.ihturb >= 10)   // the 3-D model's length scales in every direction
+      for (int k = 0; k < S.Kloc; ++k) S.CmuHt[q + S.sz * k] = cv[S.sz * k];
   }
 };
 // IHTURB 2, interior cells: CmuHt = Chs dx dy sqrt(Sxx^2 + 2 Sxy^2 + Syy^2)
@@ -1499,6 +1503,484 @@ struct OpTurbHGhost {
       c[base + step * (lo - g)] = c[base + step * (lo + g - 1)];
       c[base + step * (hi + g)] = c[base + step * (hi - g + 1)];
     }
+  }
+};
+
+// =========================================================================
+//   k-epsilon closure, IVTURB = 10 (kepsilon_3D, src/nhwave.F:10030-11114)
+// =========================================================================
+// Barotropic flow: Rho = Rho0 (src/initialize.F:2561), so the buoyancy
+// production is zero.  Everything is evaluated in FP64 in the reference's
+// order (bit-exact in the FP64 form).  The reference leaves alpha_c,
+// beta_c, gamma_c of the interior vertical coefficients unset; the three-
+// point weights of the momentum equations (src/nhwave.F:6826-6828) stand in.
+constexpr double kTkeMin = (double)1.e-9f, kEpsMin = (double)1.e-9f;
+
+// limited horizontal slopes (delxFun_3D / delyFun_3D) of U and V as
+// get_Omega leaves them (uv = 1, before sponge_damping), or of W as fluxes
+// leaves them (uv = 0), at the interior cells the production reads
+struct OpKeSlopes {
+  static constexpr const char* kName = "ke_slopes";
+  int uv;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    const bool dry = S.Mask[q] == 0;
+    auto sx = [&](const T* a) -> T {
+      return dry ? (T)0 : (T)lim_slope<double>((double)a[o - 1], (double)a[o], (double)a[o + 1], S.dx, S.dx);
+    };
+    auto sy = [&](const T* a) -> T {
+      return dry ? (T)0 : (T)lim_slope<double>((double)a[o - S.sy], (double)a[o], (double)a[o + S.sy], S.dy, S.dy);
+    };
+    if (uv) {
+      S.keDxU[o] = sx(S.U); S.keDyU[o] = sy(S.U);
+      S.keDxV[o] = sx(S.V); S.keDyV[o] = sy(S.V);
+    } else {
+      S.keDxW[o] = sx(S.W); S.keDyW[o] = sy(S.W);
+    }
+  }
+};
+
+// surface face values of tke and epsilon (construct_3D_z over the limited
+// vertical slope, interior columns; zero elsewhere), floored at Tke_min /
+// Eps_min (src/nhwave.F:10321-10334); every column
+struct OpKeTop {
+  static constexpr const char* kName = "ke_surface_values";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    double tk = 0.0, ep = 0.0;
+    if (i >= S.IB && i <= S.IE && j >= S.JB && j <= S.JE) {
+      const int K = S.KE;
+      auto top = [&](const T* a) {
+        const double am = (double)a[i3(S, i, j, K - 1)], a0 = (double)a[i3(S, i, j, K)], ap = (double)a[i3(S, i, j, K + 1)];
+        const double t1 = (ap - a0) / (S.sigc[K + 1] - S.sigc[K]);
+        const double t2 = (a0 - am) / (S.sigc[K] - S.sigc[K - 1]);
+        const double dz = (fabs(t1) + fabs(t2)) < kSmall ? 0.0 : limiter(t1, t2);
+        return a0 + 0.5 * S.dsig[K] * dz;
+      };
+      tk = top(S.Tke);
+      ep = top(S.Eps);
+    }
+    S.keTopK[q] = dmax_(tk, kTkeMin);
+    S.keTopE[q] = dmax_(ep, kEpsMin);
+  }
+};
+
+// HLPA face value (src/nhwave.F:7809-7847)
+__device__ __forceinline__ double ke_hlpa(double Uw, double Fww, double Fw, double Fp, double Fe) {
+  double h = 0.0;
+  if (Uw >= 0.0) {
+    const double a = fabs(Fp - 2.0 * Fw + Fww) < fabs(Fp - Fww) ? 1.0 : 0.0;
+    h = fabs(Fp - Fww) <= (double)1.e-16f ? Fw : Fw + a * (Fp - Fw) * (Fw - Fww) / (Fp - Fww);
+  }
+  if (Uw < 0.0) {
+    const double a = fabs(Fw - 2.0 * Fp + Fe) < fabs(Fw - Fe) ? 1.0 : 0.0;
+    h = fabs(Fw - Fe) <= (double)1.e-16f ? Fp : Fp + a * (Fw - Fp) * (Fp - Fe) / (Fw - Fe);
+  }
+  return h;
+}
+
+// shear production of the nonlinear model (ke_model = 2, src/nhwave.F:
+// 10139-10274): Reynolds stresses from the velocity gradient G, contracted
+// with G per PRODTYPE (1 vertical shear of U, V; 2 vertical shear; else 3-D)
+__device__ inline double ke_production(const double (&G)[3][3], double tk, double ep, int prod_type) {
+  const double c23 = (double)(2.0f / 3.0f), c13 = (double)(1.0f / 3.0f);
+  double smax = 0.0;
+  for (int n = 0; n < 3; ++n)
+    if (fabs(G[n][n]) > smax) smax = fabs(G[n][n]);
+  smax = smax * tk / ep;
+  const double c_d = c23 * (1.0 / ((double)7.4f + 2.0 * smax));
+  double dmx = 0.0;
+  for (int n = 0; n < 3; ++n)
+    for (int m = 0; m < 3; ++m)
+      if (fabs(G[n][m]) > dmx) dmx = fabs(G[n][m]);
+  dmx = dmx * tk / ep;
+  const double c_1 = 1.0 / ((double)185.2f + 3.0 * (dmx * dmx));
+  const double c_2 = -(1.0 / (58.5 + 2.0 * (dmx * dmx)));
+  const double c_3 = 1.0 / ((double)370.4f + 3.0 * (dmx * dmx));
+  const double tk2 = tk * tk, tk3 = tk * tk * tk, ep2 = ep * ep;
+  const int n1 = prod_type == 1 ? 2 : 3, m0 = (prod_type == 1 || prod_type == 2) ? 2 : 0;
+  double P = 0.0;
+  for (int n = 0; n < 3; ++n)
+    for (int m = 0; m < 3; ++m) {
+      const double dl = n == m ? 1.0 : 0.0;
+      double r = c_d * tk2 / ep * (G[n][m] + G[m][n]) - c23 * tk * dl;
+      for (int l = 0; l < 3; ++l) {
+        r = r + c_1 * tk3 / ep2 * (G[n][l] * G[l][m] + G[m][l] * G[l][n]);
+        for (int g = 0; g < 3; ++g) r = r - c23 * c_1 * tk3 / ep2 * G[l][g] * G[g][l] * dl;
+      }
+      for (int g = 0; g < 3; ++g) {
+        r = r + c_2 * tk3 / ep2 * G[n][g] * G[m][g];
+        for (int l = 0; l < 3; ++l) r = r - c13 * c_2 * tk3 / ep2 * G[l][g] * G[l][g] * dl;
+      }
+      for (int g = 0; g < 3; ++g) {
+        r = r + c_3 * tk3 / ep2 * G[g][n] * G[g][m];
+        for (int l = 0; l < 3; ++l) r = r - c13 * c_3 * tk3 / ep2 * G[l][g] * G[l][g] * dl;
+      }
+      if (n < n1 && m >= m0) P = P + r * G[n][m];
+    }
+  return P;
+}
+
+// one interior column of kepsilon_3D: production, the epsilon equation
+// (HLPA advection, horizontal diffusion, source, implicit vertical
+// diffusion with the bed and surface terms), its SSP-RK combination and
+// floor, the same for tke (whose source reads the new DEps), then the bed
+// wall function and the surface gradient condition (src/nhwave.F:10100-
+// 10858).  The column's own snapshot gives DelxSc / DelySc / DelxSl /
+// DelySl; neighbours are read only through Tke, Eps, CmuHt, D, U, V, W, Ex,
+// Ey, Omega, Mask and the surface values, which no thread writes here.
+struct OpKeColumn {
+  static constexpr const char* kName = "kepsilon_column";
+  static constexpr int kMaxK = 64;   // Kglob <= 64 (nhw_create)
+  int istep;                         // 0-based stage
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const double Dc = S.D[q];
+    const int mk = S.Mask[q];
+    const double Dmin = S.ke_dmin, dt = S.sc->dt, cmu = S.v_cmu, cmuR = 0.0;
+    const bool rng = S.ke_rng != 0;
+    const double c1e = rng ? (double)1.42f : (double)1.44f;
+    double c2e = rng ? 0.0 : (double)1.92f;
+    const double c3e = 0.0, Prod_b = 0.0;
+    const double cmiu = rng ? (double)0.085f : (double)0.09f;
+    const double Sche = rng ? (double)0.72f : (double)1.3f, Schk = rng ? (double)0.72f : 1.0;
+    const int KB = S.KB, KE = S.KE, n = KE - KB + 1;
+    const double* sigc = S.sigc;
+    const double* sig = S.sig;
+    const double* dsig = S.dsig;
+    const bool set = S.sc->sig_set != 0;
+    auto slope = [&](const double* lev, bool y, int kk) -> double {
+      if (!set) return 0.0;
+      return (1.0 - lev[kk]) / S.scD[q] * (y ? S.scHy[q] : S.scHx[q]) - lev[kk] / S.scD[q] * (y ? S.scEy[q] : S.scEx[q]);
+    };
+    auto Scx = [&](int kk) { return slope(sigc, false, kk); };
+    auto Scy = [&](int kk) { return slope(sigc, true, kk); };
+    auto Slx = [&](int kk) { return slope(sig, false, kk); };
+    auto Sly = [&](int kk) { return slope(sig, true, kk); };
+    auto at = [&](const T* a, int kk) -> double { return (double)a[i3(S, i, j, kk)]; };
+    auto ds = [&](int kk) { return sigc[kk + 1] - sigc[kk - 1]; };
+    const double dxh = S.DelxH[q], dyh = S.DelyH[q], dxe = S.DelxEta[q], dye = S.DelyEta[q];
+    // production (zero in shallow or dry columns; no negative production at the surface)
+    double prod[kMaxK];
+    for (int k = KB; k <= KE; ++k) {
+      double P = 0.0;
+      if (Dc >= Dmin && mk == 1) {
+        double G[3][3];
+        const double dU = at(S.U, k + 1) - at(S.U, k - 1), dV = at(S.V, k + 1) - at(S.V, k - 1);
+        const double dW = at(S.W, k + 1) - at(S.W, k - 1);
+        G[0][0] = at(S.keDxU, k) + dU / ds(k) * Scx(k);
+        G[0][1] = at(S.keDyU, k) + dU / ds(k) * Scy(k);
+        G[0][2] = 1.0 / Dc * dU / ds(k);
+        G[1][0] = at(S.keDxV, k) + dV / ds(k) * Scx(k);
+        G[1][1] = at(S.keDyV, k) + dV / ds(k) * Scy(k);
+        G[1][2] = 1.0 / Dc * dV / ds(k);
+        G[2][0] = at(S.keDxW, k) + dW / ds(k) * Scx(k);
+        G[2][1] = at(S.keDyW, k) + dW / ds(k) * Scy(k);
+        G[2][2] = 1.0 / Dc * dW / ds(k);
+        P = ke_production(G, at(S.Tke, k), at(S.Eps, k), S.ke_prod);
+        if (k == KE && P < 0.0) P = 0.0;
+      }
+      prod[k - KB] = P;
+    }
+    // adv_scalar_hlpa with flux_scalar_bc (src/nhwave.F:7604-7806, 7850-7986)
+    auto scx = [&](const T* Phi, int f, int k) -> double {
+      if ((f <= S.IE && S.Mask[i2(S, f, j)] == 0) || (f - 1 >= S.IB && S.Mask[i2(S, f - 1, j)] == 0)) return 0.0;
+      if (f == S.IE + 1) return 0.0;
+      const long long o = i3(S, f, j, k);
+      const double u = (double)S.Ex[o];
+      if (f == S.IB) {
+        if (S.bc_x0 == 1 || S.bc_x0 == 2 || S.bc_x0 == 5) return 0.0;
+        if (S.bc_x0 == 3) return u * 0.0;
+      }
+      return u * ke_hlpa(u, (double)Phi[o - 2], (double)Phi[o - 1], (double)Phi[o], (double)Phi[o + 1]);
+    };
+    auto scy = [&](const T* Phi, int f, int k) -> double {
+      if ((f <= S.JE && S.Mask[i2(S, i, f)] == 0) || (f - 1 >= S.JB && S.Mask[i2(S, i, f - 1)] == 0)) return 0.0;
+      if (f == S.JB && (S.bc_y0 == 1 || S.bc_y0 == 2 || S.bc_y0 == 5)) return 0.0;
+      if (f == S.JE + 1 && (S.bc_yn == 1 || S.bc_yn == 2 || S.bc_yn == 5)) return 0.0;
+      const long long o = i3(S, i, f, k);
+      const long long y = S.sy;
+      const double v = (double)S.Ey[o];
+      return v * ke_hlpa(v, (double)Phi[o - 2 * y], (double)Phi[o - y], (double)Phi[o], (double)Phi[o + y]);
+    };
+    auto scz = [&](const T* Phi, int f) -> double {
+      if (f == KB || f == KE + 1) return 0.0;
+      const long long o = i3(S, i, j, f);
+      const long long z = S.sz;
+      const double w = (double)S.Omega[o];
+      return w * ke_hlpa(w, (double)Phi[o - 2 * z], (double)Phi[o - z], (double)Phi[o], (double)Phi[o + z]);
+    };
+    auto r5 = [&](const T* Phi, double SchtH, int k) -> double {
+      if (mk == 0) return 0.0;
+      auto nu = [&](double ha, double hb) { return 0.5 * (cmu + cmu) + 0.5 * (ha + hb) / SchtH; };
+      auto H = [&](int ii, int jj) { return (double)S.CmuHt[i3(S, ii, jj, k)]; };
+      auto Dq = [&](int ii, int jj) { return S.D[i2(S, ii, jj)]; };
+      auto Ph = [&](int ii, int jj) { return (double)Phi[i3(S, ii, jj, k)]; };
+      const double Sdx = 0.5 *
+                         (nu(H(i + 1, j), H(i, j)) * (Dq(i + 1, j) + Dq(i, j)) * (Ph(i + 1, j) - Ph(i, j)) -
+                          nu(H(i, j), H(i - 1, j)) * (Dq(i, j) + Dq(i - 1, j)) * (Ph(i, j) - Ph(i - 1, j))) /
+                         (S.dx * S.dx);
+      const double Sdy = 0.5 *
+                         (nu(H(i, j + 1), H(i, j)) * (Dq(i, j + 1) + Dq(i, j)) * (Ph(i, j + 1) - Ph(i, j)) -
+                          nu(H(i, j), H(i, j - 1)) * (Dq(i, j) + Dq(i, j - 1)) * (Ph(i, j) - Ph(i, j - 1))) /
+                         (S.dy * S.dy);
+      return -(1.0 / S.dx * (scx(Phi, i + 1, k) - scx(Phi, i, k))) - 1.0 / S.dy * (scy(Phi, j + 1, k) - scy(Phi, j, k)) -
+             1.0 / dsig[k] * (scz(Phi, k + 1) - scz(Phi, k)) + Sdx + Sdy;
+    };
+    double A[kMaxK], B[kMaxK], C[kMaxK], X[kMaxK];
+    // one equation: eq = 2 epsilon, 1 tke
+    auto column = [&](int eq) {
+      const T* Old = eq == 2 ? S.Eps : S.Tke;
+      T* Dv = eq == 2 ? S.DEps : S.DTke;
+      const double zL = eq == 2 ? S.keTopE[q] : S.keTopK[q];
+      const double Sch = eq == 2 ? Sche : Schk;
+      const double DxD = (dxh + dxe) / Dc, DyD = (dyh + dye) / Dc;
+      for (int k = KB; k <= KE; ++k) {
+        const int m = k - KB;
+        const double L1top = dsig[k + 1] / (dsig[k] + dsig[k + 1]), L2top = dsig[k] / (dsig[k] + dsig[k + 1]);
+        const double L1bot = dsig[k] / (dsig[k] + dsig[k - 1]), L2bot = dsig[k - 1] / (dsig[k] + dsig[k - 1]);
+        const double dsigck = (dsig[k] + dsig[k + 1]) / 2.0, dsigck1 = (dsig[k - 1] + dsig[k]) / 2.0;
+        const double alpha_c = -dsigck / (dsigck + dsigck1) / dsigck1;
+        const double beta_c = (dsigck - dsigck1) / (dsigck * dsigck1);
+        const double gamma_c = dsigck1 / (dsigck + dsigck1) / dsigck;
+        const double nuV_top = (L1top * cmu + L2top * cmu) + (L1top * cmuR + L2top * cmuR) +
+                               (L1top * at(S.CmuVt, k) + L2top * at(S.CmuVt, k + 1)) / Sch;
+        const double nuH_top = (L1top * cmu + L2top * cmu) + (L1top * cmuR + L2top * cmuR) +
+                               (L1top * at(S.CmuHt, k) + L2top * at(S.CmuHt, k + 1)) / Sch;
+        const double nuV_bot = (L1bot * cmu + L2bot * cmu) + (L1bot * cmuR + L2bot * cmuR) +
+                               (L1bot * at(S.CmuVt, k - 1) + L2bot * at(S.CmuVt, k)) / Sch;
+        const double nuH_bot = (L1bot * cmu + L2bot * cmu) + (L1bot * cmuR + L2bot * cmuR) +
+                               (L1bot * at(S.CmuHt, k - 1) + L2bot * at(S.CmuHt, k)) / Sch;
+        double r = r5(Old, Sch, k);
+        if (eq == 2) r = r + c1e * Dc * (prod[m] + c3e * Prod_b) * at(S.Eps, k) / at(S.Tke, k);
+        else r = r + Dc * (prod[m] + Prod_b) - at(S.DEps, k);
+        if (k == KB) {
+          r = r - (-(nuH_bot * (dxh * DxD + dyh * DyD) * at(Old, k))) / dsig[k] +
+              (dsig[k] - dsigck) / (dsig[k] * dsig[k] / 2.0 * (dsigck + dsig[k] / 2.0)) *
+                  (nuH_top * (Slx(k + 1) * dxh + Sly(k + 1) * dyh) + nuV_top / Dc) * at(Old, k);
+        } else if (k == KE) {
+          r = r + ((nuH_top * (dxe * dxe + dye * dye) + nuV_top) / (Dc * Dc) * (at(Old, k + 1) - at(Old, k)) * Dc / dsigck -
+                   nuH_top * (-(dxe * DxD) - dye * DyD) * zL) /
+                      dsig[k] +
+              (dsig[k] - dsigck1) / (dsig[k] * dsig[k] / 2.0 * (dsigck1 + dsig[k] / 2.0)) *
+                  (nuH_bot * (-(Slx(k) * dxe) - Sly(k) * dye) + nuV_bot / Dc) * zL;
+        }
+        auto top = [&](int kk) { return nuH_top * (Slx(k + 1) * Scx(kk) + Sly(k + 1) * Scy(kk)) + nuV_top / (Dc * Dc); };
+        auto bot = [&](int kk) { return nuH_bot * (Slx(k) * Scx(kk) + Sly(k) * Scy(kk)) + nuV_bot / (Dc * Dc); };
+        if (k == KB) A[m] = 0.0;
+        else if (k == KE) A[m] = -dt * (3.0 / 2.0 * bot(k - 1) / (dsigck1 * (dsigck1 + dsig[k] / 2.0)));
+        else
+          A[m] = -dt * ((top(k - 1) - bot(k - 1)) * alpha_c / dsig[k] +
+                        (top(k - 1) + bot(k - 1)) / (dsigck1 * (dsigck1 + dsigck)));
+        if (k == KB) C[m] = -dt * (3.0 / 2.0 * top(k + 1) / (dsigck * (dsigck + dsig[k] / 2.0)));
+        else if (k == KE) C[m] = 0.0;
+        else
+          C[m] = -dt * ((top(k + 1) - bot(k + 1)) * gamma_c / dsig[k] +
+                        (top(k + 1) + bot(k + 1)) / (dsigck * (dsigck1 + dsigck)));
+        double b0 = 1.0;
+        if (eq == 2) {
+          if (rng) {   // c2e of Yakhot et al. (1992) from the strain rate
+            const double dUs = (at(S.U, k + 1) - at(S.U, k - 1)) / ds(k), dVs = (at(S.V, k + 1) - at(S.V, k - 1)) / ds(k);
+            const double dWs = (at(S.W, k + 1) - at(S.W, k - 1)) / ds(k);
+            const double S11 = at(S.keDxU, k) + dUs * Scx(k);
+            const double S22 = at(S.keDyV, k) + dVs * Scy(k);
+            const double S33 = 1.0 / Dc * (at(S.W, k + 1) - at(S.W, k - 1)) / ds(k);
+            const double S12 = 0.5 * (at(S.keDyU, k) + dUs * Scy(k) + at(S.keDxV, k) + dVs * Scx(k));
+            const double S13 = 0.5 * ((at(S.U, k + 1) - at(S.U, k - 1)) / ds(k) / Dc + at(S.keDxW, k) + dWs * Scx(k));
+            const double S23 = 0.5 * ((at(S.V, k + 1) - at(S.V, k - 1)) / ds(k) / Dc + at(S.keDyW, k) + dWs * Scy(k));
+            const double lambda = at(S.Tke, k) / at(S.Eps, k) *
+                                  sqrt(2.0 * (S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23)));
+            const double l3 = lambda * lambda * lambda;
+            c2e = (double)1.68f + cmiu * l3 * (1.0 - lambda / (double)4.38f) / (1.0 + (double)0.012f * l3);
+            c2e = dmax_(0.0, dmin_(c2e, 4.0));
+          }
+          b0 = 1.0 + dt * c2e * at(S.Eps, k) / at(S.Tke, k);
+        }
+        if (k == KB) B[m] = b0 - dt * (-(3.0 / 2.0 - dsigck / dsig[k]) * top(k) / (dsig[k] / 2.0 * dsigck));
+        else if (k == KE) B[m] = b0 - dt * (-(3.0 / 2.0 - dsigck1 / dsig[k]) * bot(k) / (dsig[k] / 2.0 * dsigck1));
+        else B[m] = b0 - dt * ((top(k) - bot(k)) * beta_c / dsig[k] - (top(k) + bot(k)) / (dsigck * dsigck1));
+        X[m] = at(Dv, k) + dt * r;
+      }
+      // trig (src/nhwave.F:13182-13224): elimination in place, then back substitution
+      for (int m = 1; m < n; ++m) {
+        const double coeff = A[m] / B[m - 1];
+        B[m] = B[m] - coeff * C[m - 1];
+        X[m] = X[m] - coeff * X[m - 1];
+      }
+      X[n - 1] = X[n - 1] / B[n - 1];
+      for (int m = n - 2; m >= 0; --m) X[m] = (X[m] - C[m] * X[m + 1]) / B[m];
+      for (int k = KB; k <= KE; ++k) Dv[i3(S, i, j, k)] = (T)X[k - KB];
+    };
+    auto rk = [&](T* Dv, const T* Dv0, double vmin) {
+      if (!(Dc >= Dmin && mk == 1)) return;
+      const double al = S.alpha[istep], be = S.beta[istep];
+      for (int k = KB; k <= KE; ++k) {
+        const long long o = i3(S, i, j, k);
+        const double v = al * (double)Dv0[o] + be * (double)Dv[o];
+        Dv[o] = (T)dmax_(v, Dc * vmin);
+      }
+    };
+    const bool solve = !(Dc < Dmin && mk == 0);
+    if (solve) column(2);
+    rk(S.DEps, S.DEps0, kEpsMin);
+    if (solve) column(1);
+    rk(S.DTke, S.DTke0, kTkeMin);
+    // bed: wall function (src/nhwave.F:10776-10831)
+    if (!(Dc < Dmin || mk == 0)) {
+      const long long ob = i3(S, i, j, KB);
+      const double Abot = sqrt(1.0 + dxh * dxh + dyh * dyh), Bbot = sqrt(1.0 + dxh * dxh);
+      const double du = (double)S.DU[ob], dv = (double)S.DV[ob], dw = (double)S.DW[ob];
+      const double DUprime = (du - dxh * dw) / Bbot;
+      const double DVprime = (-(dxh * dyh * du) + (1.0 + dxh * dxh) * dv - dyh * dw) / Abot / Bbot;
+      const double DUmag = sqrt(DUprime * DUprime + DVprime * DVprime);
+      double Tkeb = kTkeMin, Epsb = kEpsMin;
+      if (!(DUmag / Dc < (double)1.e-6f)) {
+        const double Dz1 = 0.5 * Dc * dsig[KB] / Abot;
+        double Cdrag;
+        if (S.ibot == 1) Cdrag = S.cd0;
+        else {
+          const double t = kKappa / log(Dz1 / (S.zob / 30.0));
+          Cdrag = t * t;
+        }
+        Cdrag = dmin_(Cdrag, (cmu + cmuR + at(S.CmuVt, KB)) / Dz1 / (DUmag + kSmall) * Dc);
+        const double Ustar = sqrt(Cdrag) * DUmag / Dc;
+        Tkeb = dmax_(Ustar * Ustar / sqrt(cmiu), kTkeMin);
+        Epsb = dmax_(Ustar * Ustar * Ustar / (kKappa * Dz1), kEpsMin);
+      }
+      const T tb = (T)(Dc * Tkeb), eb = (T)(Dc * Epsb);
+      for (int k = 0; k <= NG; ++k) {
+        S.DTke[ob - S.sz * k] = tb;
+        S.DEps[ob - S.sz * k] = eb;
+      }
+    }
+    // surface: gradient condition (Derakhti et al. 2015, eq. 60) with the
+    // limited slopes of the surface values
+    if (!(mk == 0 || Dc < Dmin)) {
+      auto tsl = [&](const double* top, bool y) {
+        const long long st = y ? S.sy : 1;
+        const double h = y ? S.dy : S.dx;
+        return lim_slope<double>(top[q - st], top[q], top[q + st], h, h);
+      };
+      const double gK = dxe * tsl(S.keTopK, false) + dye * tsl(S.keTopK, true);
+      const double gE = dxe * tsl(S.keTopE, false) + dye * tsl(S.keTopE, true);
+      const double Atop = sqrt(1.0 + dxe * dxe + dye * dye);
+      for (int k = 1; k <= NG; ++k) {
+        const double f = (sigc[KE + k] - sigc[KE - k + 1]) * (Dc * Dc) / (Atop * Atop);
+        S.DTke[i3(S, i, j, KE + k)] = (T)(at(S.DTke, KE - k + 1) + f * gK);
+        S.DEps[i3(S, i, j, KE + k)] = (T)(at(S.DEps, KE - k + 1) + f * gE);
+      }
+    }
+  }
+};
+
+// wall function of a friction wall (BC = 5) at one cell (src/nhwave.F:
+// 10870-11023): u* from the drag coefficient (Ibot 1) or the log law at
+// half a cell width h/2 (Ibot 2)
+template <class T>
+__device__ inline void ke_wall(const Dev<T>& S, int i, int j, int k, double Umag, double h) {
+  const double cmiu = S.ke_rng ? (double)0.085f : (double)0.09f;
+  double Tkeb = kTkeMin, Epsb = kEpsMin;
+  if (!(Umag < (double)1.e-6f)) {
+    const double FricU = S.ibot == 1 ? sqrt(S.cd0) * Umag : Umag / (1.0 / kKappa * log(30.0 * h / 2.0 / S.zob));
+    Tkeb = FricU * FricU / sqrt(cmiu);
+    Epsb = FricU * FricU * FricU / (kKappa * h / 2.0);
+  }
+  const double Dq = S.D[i2(S, i, j)];
+  S.DTke[i3(S, i, j, k)] = (T)(Dq * Tkeb);
+  S.DEps[i3(S, i, j, k)] = (T)(Dq * Epsb);
+}
+// west and east sides: one thread per interior row and level (every level)
+struct OpKeSidesX {
+  static constexpr const char* kName = "ke_sides_x";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    const int j = S.JB + t % S.N, k = t / S.N;
+    auto speed = [&](int i) {
+      const long long o = i3(S, i, j, k);
+      return sqrt((double)S.V[o] * (double)S.V[o] + (double)S.W[o] * (double)S.W[o]);
+    };
+    auto mirror = [&](int lo, int sgn) {   // DTke(lo - sgn g) = DTke(lo + sgn (g - 1))
+      for (int g = 1; g <= NG; ++g) {
+        const long long d = i3(S, lo - sgn * g, j, k), s = i3(S, lo + sgn * (g - 1), j, k);
+        S.DTke[d] = S.DTke[s];
+        S.DEps[d] = S.DEps[s];
+      }
+    };
+    if (S.bc_x0 == 5) ke_wall(S, S.IB, j, k, speed(S.IB), S.dx);
+    mirror(S.IB, 1);
+    if (S.bc_xn == 5) ke_wall(S, S.IE, j, k, speed(S.IE), S.dx);
+    mirror(S.IE, -1);
+  }
+};
+// south and north sides: one thread per column i (ghosts included) and level
+struct OpKeSidesY {
+  static constexpr const char* kName = "ke_sides_y";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    const int i = t % S.Mloc, k = t / S.Mloc;
+    auto speed = [&](int j) {
+      const long long o = i3(S, i, j, k);
+      return sqrt((double)S.U[o] * (double)S.U[o] + (double)S.W[o] * (double)S.W[o]);
+    };
+    auto mirror = [&](int lo, int sgn) {
+      for (int g = 1; g <= NG; ++g) {
+        const long long d = i3(S, i, lo - sgn * g, k), s = i3(S, i, lo + sgn * (g - 1), k);
+        S.DTke[d] = S.DTke[s];
+        S.DEps[d] = S.DEps[s];
+      }
+    };
+    if (S.bc_y0 == 5) ke_wall(S, i, S.JB, k, speed(S.JB), S.dy);
+    mirror(S.JB, 1);
+    if (S.bc_yn == 5) ke_wall(S, i, S.JE, k, speed(S.JE), S.dy);
+    mirror(S.JE, -1);
+  }
+};
+// tke, epsilon and CmuVt = cmiu k^2 / eps in every cell (Cmut_min where k or
+// eps is below 1e-6, and in shallow or dry columns, which are reset to the
+// floors); CmuVt's ghost levels copy the outermost interior ones; the
+// source region of an INT_, LEF_ or FOCUSED maker is reset too
+// (src/nhwave.F:11039-11100)
+struct OpKeFinal {
+  static constexpr const char* kName = "ke_update";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const double Dq = S.D[q];
+    const double cmiu = S.ke_rng ? (double)0.085f : (double)0.09f;
+    const bool wet = Dq >= S.ke_dmin && S.Mask[q] == 1;
+    const bool quiet = S.ke_quiet && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys && S.yc[j] <= S.wm_yn;
+    for (int k = 0; k < S.Kloc; ++k) {
+      const long long o = q + S.sz * k;
+      if (wet) {
+        const T tk = (T)((double)S.DTke[o] / Dq), ep = (T)((double)S.DEps[o] / Dq);
+        S.Tke[o] = tk;
+        S.Eps[o] = ep;
+        const double a = (double)tk, b = (double)ep;
+        S.CmuVt[o] = (a < (double)1.e-6f || b < (double)1.e-6f) ? (T)S.v_cmut0 : (T)(cmiu * (a * a) / b);
+      } else {
+        S.Tke[o] = (T)kTkeMin;
+        S.Eps[o] = (T)kEpsMin;
+        S.DTke[o] = (T)(Dq * kTkeMin);
+        S.DEps[o] = (T)(Dq * kEpsMin);
+        S.CmuVt[o] = (T)S.v_cmut0;
+      }
+    }
+    for (int g = 1; g <= NG; ++g) {
+      S.CmuVt[q + S.sz * (S.KB - g)] = S.CmuVt[q + S.sz * S.KB];
+      S.CmuVt[q + S.sz * (S.KE + g)] = S.CmuVt[q + S.sz * S.KE];
+    }
+    if (quiet)
+      for (int k = 0; k < S.Kloc; ++k) {
+        const long long o = q + S.sz * k;
+        S.Tke[o] = (T)kTkeMin;
+        S.Eps[o] = (T)kEpsMin;
+        S.DTke[o] = (T)(Dq * kTkeMin);
+        S.DEps[o] = (T)(Dq * kEpsMin);
+        S.CmuVt[o] = (T)S.v_cmut0;
+      }
   }
 };
 
@@ -1601,8 +2083,16 @@ struct OpInitDU {
     S.DV[o] = (T)((double)(T)(d * (double)S.V[o]) * m);
     S.DW[o] = (T)((double)(T)(d * (double)S.W[o]) * m);
     // viscous flow: the seeding viscosity Cmut_min, after vel_bc, which so
-    // saw CmuVt = 0 (src/initialize.F:3155, 3172-3195)
+    // saw CmuVt = 0, and k-epsilon's seeds (src/initialize.F:3155, 3172-3195)
     if (S.CmuVt) S.CmuVt[o] = S.CmuHt[o] = (T)S.v_cmut0;
+    if (S.Tke) {
+      S.Tke[o] = (T)kTkeMin;
+      S.Eps[o] = (T)kEpsMin;
+      S.DTke[o] = (T)(d * kTkeMin * m);
+      S.DEps[o] = (T)(d * kEpsMin * m);
+      S.DTke0[o] = (T)0;
+      S.DEps0[o] = (T)0;
+    }
   }
 };
 

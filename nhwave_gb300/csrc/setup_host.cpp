@@ -30,10 +30,11 @@ int check_params(const nhw_params& p) {
   // unknowns of the Poisson system, is an int)
   if ((long long)(p.Mglob + 5) * (p.Nglob + 5) * (p.Kglob + 5) >= (1LL << 31)) return NHW_ERR_UNSUPPORTED;
   if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
-  // viscous flow with constant viscosities (IVTURB / IHTURB 1) or the subgrid
-  // models (2); the k-epsilon / LES closures (3, 10, 20, 30) are not built
-  if (p.viscous_flow && (p.ivturb < 1 || p.ivturb > 2 || p.ihturb < 1 || p.ihturb > 2))
-    return NHW_ERR_UNSUPPORTED;
+  // viscous flow: IVTURB 1 constant, 2 subgrid, 10 the 3-D k-epsilon model;
+  // IHTURB 1, 2 or >= 10 (CmuHt = CmuVt).  The 2-D k-epsilon (3) and the LES
+  // closures (20, 30) are not built
+  if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10)) return NHW_ERR_UNSUPPORTED;
+  if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
   // lateral sides: 1 free slip, 2 no slip, 5 wall friction; BC_Xn = 6 Orlanski
   for (int b : {p.bc_y0, p.bc_yn})

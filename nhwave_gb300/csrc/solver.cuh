@@ -50,7 +50,7 @@ class SolverBase {
   virtual int fluxes() = 0;
   virtual int eval_duvw(int istep) = 0;
   virtual int sponge_damping() = 0;
-  virtual int eval_turb() = 0;
+  virtual int eval_turb(int istep) = 0;
   virtual int step() = 0;
   virtual int mass(double* m) = 0;
   virtual int statistics(double* out7) = 0;
@@ -108,6 +108,10 @@ __global__ void __launch_bounds__(256) k_update_vars(Dev<T> S, long long n2, lon
     S.DU0[t] = S.DU[t];
     S.DV0[t] = S.DV[t];
     S.DW0[t] = S.DW[t];
+    if (S.DTke0) {   // k-epsilon (src/nhwave.F:5483-5484)
+      S.DTke0[t] = S.DTke[t];
+      S.DEps0[t] = S.DEps[t];
+    }
     if (S.U0) {   // Orlanski boundary: the previous step's velocities move back one level
       S.U00[t] = S.U0[t]; S.V00[t] = S.V0[t]; S.W00[t] = S.W0[t];
       S.U0[t] = S.U[t]; S.V0[t] = S.V[t]; S.W0[t] = S.W[t];
@@ -255,6 +259,12 @@ class Solver final : public SolverBase {
       S.v_cmu = p.visc; S.v_cvs = p.cvs; S.v_chs = p.chs;
       S.v_schmidt = p.schmidt; S.v_number = p.viscous_number;
       S.ivturb = p.ivturb; S.ihturb = p.ihturb;
+      S.ke_rng = p.rng ? 1 : 0; S.ke_prod = p.prod_type; S.ke_dmin = 2.0 * p.min_dep;
+      const int w = p.wavemaker;   // WaveMaker(1:3) is INT, LEF or FOC
+      S.ke_quiet = (w == NHW_WM_INT_LIN || w == NHW_WM_INT_SOL || w == NHW_WM_INT_CON || w == NHW_WM_INT_JON ||
+                    w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR || w == NHW_WM_LEF_LIN ||
+                    w == NHW_WM_LEF_SOL || w == NHW_WM_LEF_STK || w == NHW_WM_LEF_CON || w == NHW_WM_LEF_TID ||
+                    w == NHW_WM_LEF_JON || w == NHW_WM_LEF_TMA || w == NHW_WM_LEF_SPC || w == NHW_WM_FOCUSED) ? 1 : 0;
     }
     S.wavemaker = p.wavemaker;
     S.wm_amp = p.amp_wave; S.wm_xw = p.xsource_west; S.wm_xe = p.xsource_east;
@@ -315,9 +325,16 @@ class Solver final : public SolverBase {
       for (double** pp : {&S.scD, &S.scEx, &S.scEy, &S.scHx, &S.scHy}) add(pp, sizeof(double) * n2);
       for (T** pp : {&S.CmuVt, &S.CmuHt}) add(pp, sizeof(T) * n3);
     }
+    const bool ke = p.viscous_flow && p.ivturb == 10;
+    if (ke)   // k-epsilon state (checkpointed)
+      for (T** pp : {&S.Tke, &S.Eps, &S.DTke, &S.DEps, &S.DTke0, &S.DEps0}) add(pp, sizeof(T) * n3);
     add(&S.P, sizeof(double) * n3);
     if (p.viscous_flow)   // explicit viscous terms of the stage
       for (T** pp : {&S.Dxx, &S.Dxy, &S.Dyx, &S.Dyy, &S.Dzx, &S.Dzy}) add(pp, sizeof(T) * n3);
+    if (ke) {   // slopes the production reads, surface values of the stage
+      for (T** pp : {&S.keDxU, &S.keDyU, &S.keDxV, &S.keDyV, &S.keDxW, &S.keDyW}) add(pp, sizeof(T) * n3);
+      for (double** pp : {&S.keTopK, &S.keTopE}) add(pp, sizeof(double) * n2);
+    }
     // west-boundary wave values, recomputed every step (after the checkpointed state)
     add(&S.Ein, sizeof(double) * S.Nloc);
     add(&S.Din, sizeof(double) * S.Nloc);
@@ -564,6 +581,10 @@ class Solver final : public SolverBase {
       case NHW_F_HZ: return {S.Hz, 0, Ml, Nl, Kl + 1};
       case NHW_F_CMUVT: return {S.CmuVt, 0, Ml, Nl, Kl};   // null (no field) on the inviscid path
       case NHW_F_CMUHT: return {S.CmuHt, 0, Ml, Nl, Kl};
+      case NHW_F_TKE: return {S.Tke, 0, Ml, Nl, Kl};   // null (no field) unless IVTURB = 10
+      case NHW_F_EPS: return {S.Eps, 0, Ml, Nl, Kl};
+      case NHW_F_DTKE: return {S.DTke, 0, Ml, Nl, Kl};
+      case NHW_F_DEPS: return {S.DEps, 0, Ml, Nl, Kl};
       default: return {nullptr, -1, 0, 0, 0};
     }
   }
@@ -680,7 +701,7 @@ class Solver final : public SolverBase {
   void ens_stage_tail(int s) {   // eval_duvw after the solve, sponge, eval_turb
     stage_post(s);
     if (S.sponge_on) sponge_damping();
-    launch_turb();
+    launch_turb(s);
   }
   int pull() { return pull_scalars(); }
   const DevScal& scal() const { return *h_sc; }
@@ -781,6 +802,12 @@ class Solver final : public SolverBase {
     if (S.CmuVt) {
       NHW_CU(cudaMemsetAsync(S.CmuVt, 0, sizeof(T) * n3, st));
       NHW_CU(cudaMemsetAsync(S.CmuHt, 0, sizeof(T) * n3, st));
+    }
+    if (S.Tke) {   // k-epsilon scratch of a previous set-up (the state is seeded below)
+      T* ks[] = {S.keDxU, S.keDyU, S.keDxV, S.keDyV, S.keDxW, S.keDyW};
+      for (T* a : ks) {
+        NHW_CU(cudaMemsetAsync(a, 0, sizeof(T) * n3, st));
+      }
     }
     incols(OpVelBcA{});
     box(OpVelBcLat{}, S.Mloc, S.Nloc, S.K, 0, 0, S.KB);
@@ -913,6 +940,7 @@ class Solver final : public SolverBase {
     box(OpFluxX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpFluxY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     box(OpFluxZ{}, S.M, S.N, S.K + 1, S.IB, S.JB, S.KB);
+    if (S.Tke) cells(OpKeSlopes{0});   // delxyzFun's DelxW / DelyW, read by k-epsilon
     return check();
   }
   void get_uvw() {
@@ -1219,6 +1247,7 @@ class Solver final : public SolverBase {
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});
+    if (S.Tke) cells(OpKeSlopes{1});   // get_Omega's DelxU .. DelyV, before sponge_damping
   }
   int eval_duvw(int istep) override {
     if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
@@ -1237,19 +1266,28 @@ class Solver final : public SolverBase {
     allcols(OpSponge{});
     return check();
   }
-  // eval_turb (src/nhwave.F:6544-6782): the eddy viscosities CmuVt / CmuHt
-  // the next stage's viscous terms read, from the velocities after
-  // sponge_damping.  Inviscid flow has none.
-  void launch_turb() {
+  // eval_turb (src/nhwave.F:6544-6782) of stage s (0-based): the eddy
+  // viscosities CmuVt / CmuHt the next stage's viscous terms read, from the
+  // velocities after sponge_damping; with IVTURB = 10 the k-epsilon step
+  // first.  Inviscid flow has none.
+  void launch_turb(int s) {
     if (!S.viscous) return;
+    if (S.Tke) {
+      allcols(OpKeTop{});
+      incols(OpKeColumn{s});
+      box(OpKeSidesX{}, S.N * S.Kloc, 1, 1, 0, 0, 0);
+      box(OpKeSidesY{}, S.Mloc * S.Kloc, 1, 1, 0, 0, 0);
+      allcols(OpKeFinal{});
+    }
     allcols(OpTurbV{});
     if (S.ihturb == 2) {
       cells(OpTurbH{});
       box(OpTurbHGhost{}, S.N * S.K + S.M * S.K + S.M * S.N, 1, 1, 0, 0, 0);
     }
   }
-  int eval_turb() override {
-    launch_turb();
+  int eval_turb(int istep) override {
+    if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
+    launch_turb(istep - 1);
     return check();
   }
   // everything of one time step after estimate_dt (src/nhwave.F:119-200)
@@ -1267,7 +1305,7 @@ class Solver final : public SolverBase {
       if (rc == NHW_ERR_CUDA) return rc;
       if (rc != NHW_OK && worst == NHW_OK) worst = rc;
       if (S.sponge_on) sponge_damping();
-      launch_turb();
+      launch_turb(s - 1);
     }
     rc = check();
     return rc ? rc : worst;
@@ -1615,7 +1653,8 @@ class Solver final : public SolverBase {
   // counters) and the arena prefix from the grids through P: every array a
   // step reads before writing it.  The Poisson and Krylov arrays after it are
   // rebuilt by every solve and are not saved.
-  // 2: per-cell eddy viscosities of viscous flow in the state prefix
+  // 2: per-cell eddy viscosities of viscous flow and the k-epsilon state
+  // in the state prefix
   static constexpr int32_t kCkptVersion = 2;
   struct CkptHeader {
     char magic[8];

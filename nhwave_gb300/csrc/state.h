@@ -96,6 +96,11 @@ struct Dev {
   // viscous = 0 on the inviscid path, where CmuVt = CmuHt = 0.
   int viscous, ivturb, ihturb;
   double v_cmu, v_cmut0, v_cvs, v_chs, v_schmidt, v_number;
+  // k-epsilon closure (IVTURB = 10): RNG variant, PRODTYPE, Dmin = 2 MinDep;
+  // ke_quiet: an INT_, LEF_ or FOCUSED maker, whose source region is kept
+  // free of turbulence
+  int ke_rng, ke_prod, ke_quiet;
+  double ke_dmin;
   // bed (BC_Z0): 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   int bc_z0, ibot;
   double cd0, zob;
@@ -187,6 +192,13 @@ struct Dev {
   // explicit viscous terms of the stage (viscous flow only, else nullptr):
   // Diffxx, Diffxy (into R2), Diffyx, Diffyy (R3), Diffzx, Diffzy (R4)
   T *Dxx, *Dxy, *Dyx, *Dyy, *Dzx, *Dzy;
+  // k-epsilon (IVTURB = 10, else nullptr): tke, epsilon, their depth
+  // integrals and the step's starting integrals (checkpointed state); the
+  // limited horizontal slopes of U, V (from get_Omega) and W (from fluxes)
+  // the production reads; the floored surface values of tke and epsilon
+  T *Tke, *Eps, *DTke, *DEps, *DTke0, *DEps0;
+  T *keDxU, *keDyU, *keDxV, *keDyV, *keDxW, *keDyW;
+  double *keTopK, *keTopE;
   // GMRES (krylov.cuh): basis V [kGmMax+1][neq], preconditioned basis Z
   // [kGmMax][neq], Hessenberg / rotations / g / y in FP64 (gm), the current
   // column, y and 1/||w|| in T (gmT), wide reduction partials; nullptr unless

@@ -21,6 +21,7 @@ NAMES = [
     "EY", "FY", "GY", "HY",
     "FZ", "GZ", "HZ",
     "CMUVT", "CMUHT",
+    "TKE", "EPS", "DTKE", "DEPS",
 ]
 for _i, _n in enumerate(NAMES):
     globals()[_n] = _i
@@ -38,7 +39,8 @@ for _n in ("HFY", "HFY0", "ETAYL", "ETAYR"):
     _CLASS[_n] = Y2
 for _n in ("MASK", "MASK_STRUCT", "MASK9"):
     _CLASS[_n] = I2
-for _n in ("U", "V", "W", "DU", "DV", "DW", "DU0", "DV0", "DW0", "P", "CMUVT", "CMUHT"):
+for _n in ("U", "V", "W", "DU", "DV", "DW", "DU0", "DV0", "DW0", "P", "CMUVT", "CMUHT", "TKE", "EPS", "DTKE",
+           "DEPS"):
     _CLASS[_n] = C3
 for _n in ("OMEGA", "FZ", "GZ", "HZ"):
     _CLASS[_n] = Z3

@@ -94,9 +94,10 @@ def load(path: str | None = None):
     L.nhw_set_wave_phases.argtypes = [vp, i32, vp]
     L.nhw_set_wave_spectrum.argtypes = [vp, i32, i32, vp, vp, vp, vp]
     for n in ("nhw_estimate_dt", "nhw_update_bathymetry", "nhw_update_wave_bc", "nhw_update_mask", "nhw_update_vars",
-              "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_eval_turb", "nhw_synchronize"):
+              "nhw_source_terms", "nhw_fluxes", "nhw_sponge_damping", "nhw_synchronize"):
         getattr(L, n).argtypes = [vp]
     L.nhw_eval_duvw.argtypes = [vp, i32]
+    L.nhw_eval_turb.argtypes = [vp, i32]
     L.nhw_step.argtypes = [vp, P(dbl), P(dbl), P(i32)]
     L.nhw_run.argtypes = [vp, i32, P(i32)]
     L.nhw_mass.argtypes = [vp, P(dbl)]
@@ -213,8 +214,8 @@ class Scenario:
     def sponge_damping(self):
         return _chk(load().nhw_sponge_damping(self._h), "sponge_damping")
 
-    def eval_turb(self):
-        return _chk(load().nhw_eval_turb(self._h), "eval_turb")
+    def eval_turb(self, istep: int):
+        return _chk(load().nhw_eval_turb(self._h, istep), "eval_turb")
 
     def step(self):
         return _chk(load().nhw_step(self._h, None, None, None), "nhw_step")

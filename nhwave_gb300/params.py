@@ -81,6 +81,7 @@ class NhwParams(ctypes.Structure):
         ("sd_return", ctypes.c_double),
         ("hm0", ctypes.c_double), ("tp", ctypes.c_double), ("freq_min", ctypes.c_double),
         ("freq_max", ctypes.c_double), ("numfreq", ctypes.c_int32), ("wave_seed", ctypes.c_int32),
+        ("prod_type", ctypes.c_int32),
     ]
 
     def copy(self) -> "NhwParams":
@@ -124,6 +125,7 @@ def default_params(**kw) -> NhwParams:
     p.slide_type = SLIDE_NONE
     p.precision = NHW_FP64
     p.ivturb = p.ihturb = 1
+    p.prod_type = 3
     p.cvs = p.chs = 0.0
     p.schmidt, p.viscous_number = 1.0, 1.0 / 6.0
     p.ibot, p.cd0, p.zob = 1, 0.0, 1e-4
@@ -197,6 +199,7 @@ def read_input(path: str) -> NhwParams:
         p.ivturb, p.ihturb, p.rng = i("IVTURB", 1), i("IHTURB", 1), _logical(kv.get("RNG", "F"))
         p.cvs, p.chs, p.schmidt = f("Cvs", 0.0), f("Chs", 0.0), f("Schmidt", 1.0)
         p.viscous_number = f("VISCOUS_NUMBER", 1.0 / 6.0)
+        p.prod_type = i("PRODTYPE", 3)
     p.wind_u, p.wind_v = f("WindU", 0.0), f("WindV", 0.0)
     dt_ = s("DEPTH_TYPE", "CELL_CENTER").upper()
     p.depth_type = DEPTH_CELL_GRID if dt_ == "CELL_GRID" else DEPTH_CELL_CENTER
@@ -284,9 +287,10 @@ def read_irr2d(path: str):
 
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
-    if p.viscous_flow and (p.ivturb not in (1, 2) or p.ihturb not in (1, 2)):
-        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (constant viscosities (1) and the "
-                "subgrid models (2) are on the GPU path; the k-epsilon and LES closures are not)")
+    if p.viscous_flow and (p.ivturb not in (1, 2, 10) or not (p.ihturb in (1, 2) or p.ihturb >= 10)):
+        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (constant viscosities (1), the subgrid "
+                "models (2) and the 3-D k-epsilon model (10) are on the GPU path; the 2-D k-epsilon (3) and the "
+                "LES closures (20, 30) are not)")
     if not p.barotropic:
         return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE,) + WM_INT + WM_LEF + WM_EAST:

@@ -323,6 +323,18 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         kw = dict(dict(viscous_flow=1, visc=1e-6, cvs=0.2, chs=0.2, ivturb=2, ihturb=2, bc_z0=5, bc_y0=5,
                        bc_yn=5, bc_xn=5, ibot=1, cd0=0.006), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_ke":
+        # the small submerged bar with the 3-D k-epsilon closure (IVTURB = IHTURB = 10, PRODTYPE 3)
+        # on a friction-law bed; tests seed tke and epsilon above their floors
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=10, ihturb=10, prod_type=3, bc_z0=5, ibot=1, cd0=0.006),
+                  **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_ke_rng":
+        # tiny_ke with the RNG variant, vertical-shear production (PRODTYPE 2) and friction
+        # walls (BC = 5) on the south, north and east sides with a roughness height (Ibot = 2)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=10, ihturb=10, rng=1, prod_type=2, bc_z0=5, bc_y0=5,
+                       bc_yn=5, bc_xn=5, ibot=2, zob=1e-3), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_fric_log":
         # the inviscid small bar with the friction law on the bed and the side walls, from a
         # roughness height (Ibot = 2)

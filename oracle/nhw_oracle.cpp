@@ -27,7 +27,9 @@
 //   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
 //   diffusion                  src/nhwave.F:6785-7141
 //   trig                       src/nhwave.F:13182-13224
-//   eval_turb (IVTURB, IHTURB 1, 2) src/nhwave.F:6544-6782
+//   eval_turb (IVTURB 1, 2, 10; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
+//   kepsilon_3D                src/nhwave.F:10030-11114, adv_scalar_hlpa 7604-7806,
+//                              hlpa 7809-7847, flux_scalar_bc 7850-7986
 //   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
 //                              Orlanski east side, bed stress)
 //   update_wave_bc             src/nhwave.F:5514-5565, 5715-5750; src/waves.F:92-370,
@@ -228,6 +230,12 @@ struct Model {
   // 6544-6782): Cvs / Chs, or the subgrid models of IVTURB / IHTURB = 2.
   double Cmu = 0, CmuR = 0;
   A3 CmuVt, CmuHt;
+  // k-epsilon state (src/mod_global.F:229): Tke, Eps and their depth
+  // integrals DTke, DEps with the step's starting values DTke0, DEps0;
+  // seeded by initial with Tke_min, Eps_min (src/initialize.F:3172-3193)
+  A3 Tke, Eps, DTke, DEps, DTke0, DEps0;
+  const double Tke_min = (double)1.e-9f, Eps_min = (double)1.e-9f;
+  double Cmut_min = 0.0;
   // viscous flow: face sigma slopes (sigma_transform) and the explicit
   // viscous terms of diffusion (src/nhwave.F:6785-7141)
   A3 DelxSl, DelySl, Diffxx, Diffxy, Diffyx, Diffyy, Diffzx, Diffzy;
@@ -237,7 +245,9 @@ struct Model {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
     if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
-    if (p.viscous_flow && (p.ivturb < 1 || p.ivturb > 2 || p.ihturb < 1 || p.ihturb > 2)) return NHW_ERR_UNSUPPORTED;
+    // IVTURB 1, 2, 10 (k-epsilon) and IHTURB 1, 2, >= 10 (CmuHt = CmuVt)
+    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10)) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
       if (b != 1 && b != 2 && b != 5) return NHW_ERR_UNSUPPORTED;
@@ -325,6 +335,7 @@ struct Model {
     if (p.viscous_flow) {
       DelxSl.init(Mloc, Nloc, Kloc1); DelySl.init(Mloc, Nloc, Kloc1);
       for (A3* a : {&Diffxx, &Diffxy, &Diffyx, &Diffyy, &Diffzx, &Diffzy}) a->init(Mloc, Nloc, Kloc);
+      for (A3* a : {&Tke, &Eps, &DTke, &DEps, &DTke0, &DEps0}) a->init(Mloc, Nloc, Kloc);
     }
     for (A3* a : {&UxL, &UxR, &VxL, &VxR, &WxL, &WxR, &DUxL, &DUxR, &DVxL, &DVxR, &DWxL, &DWxR,
                   &SxL, &SxR, &SxS, &ExL, &ExR, &FxL, &FxR, &GxL, &GxR, &HxL, &HxR, &Ex, &Fx,
@@ -525,12 +536,21 @@ struct Model {
           DW(i, j, k) = D(i, j) * W(i, j, k) * Mask(i, j);
         }
     // seeding values (src/initialize.F:3172-3195), after vel_bc, which so
-    // saw CmuVt = 0
+    // saw CmuVt = 0; DTke0 = DEps0 = 0 (:2950-2951)
     if (p.viscous_flow) {
-      const double Tke_min = (double)1.e-9f, Eps_min = (double)1.e-9f;
-      const double Cmut_min = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (Tke_min * Tke_min) / Eps_min;
+      Cmut_min = (p.rng ? (double)8.5e-2f : (double)9.0e-2f) * (Tke_min * Tke_min) / Eps_min;
       CmuHt.fill(Cmut_min);
       CmuVt.fill(Cmut_min);
+      Tke.fill(Tke_min);
+      Eps.fill(Eps_min);
+      for (int k = 1; k <= Kloc; ++k)
+        for (int j = 1; j <= Nloc; ++j)
+          for (int i = 1; i <= Mloc; ++i) {
+            DTke(i, j, k) = D(i, j) * Tke(i, j, k) * Mask(i, j);
+            DEps(i, j, k) = D(i, j) * Eps(i, j, k) * Mask(i, j);
+          }
+      DTke0.fill(0.0);
+      DEps0.fill(0.0);
     }
     if (p.time_order == 3) {
       It_Order = 3;
@@ -674,6 +694,7 @@ struct Model {
   void update_vars() {
     Eta00 = Eta0; U00 = U0; V00 = V0; W00 = W0;
     D0 = D; Eta0 = Eta; U0 = U; V0 = V; W0 = W; DU0 = DU; DV0 = DV; DW0 = DW;
+    if (p.viscous_flow) { DTke0 = DTke; DEps0 = DEps; }   // src/nhwave.F:5483-5484
   }
 
   // --------------------------------------------------------- source_terms
@@ -2699,6 +2720,444 @@ struct Model {
     return st;
   }
 
+  // ------------------------------------------------------------ k-epsilon
+  // HLPA upwinding of a face value (src/nhwave.F:7809-7847)
+  static double hlpa(double Uw, double Fww, double Fw, double Fp, double Fe) {
+    double h = 0.0;
+    if (Uw >= Zero) {
+      const double a = std::fabs(Fp - 2.0 * Fw + Fww) < std::fabs(Fp - Fww) ? 1.0 : 0.0;
+      h = std::fabs(Fp - Fww) <= (double)1.e-16f ? Fw : Fw + a * (Fp - Fw) * (Fw - Fww) / (Fp - Fww);
+    }
+    if (Uw < Zero) {
+      const double a = std::fabs(Fw - 2.0 * Fp + Fe) < std::fabs(Fw - Fe) ? 1.0 : 0.0;
+      h = std::fabs(Fw - Fe) <= (double)1.e-16f ? Fp : Fp + a * (Fw - Fp) * (Fp - Fe) / (Fw - Fe);
+    }
+    return h;
+  }
+  // adv_scalar_hlpa (src/nhwave.F:7604-7806) with flux_scalar_bc (:7850-
+  // 7986): R5 = -div(HLPA fluxes of Phi by Ex, Ey, Omega) + the horizontal
+  // diffusion of Phi; IVAR 1 tke, 2 epsilon.  The boundary scalar of a
+  // BC_X0 = 3 side is zero (no salinity or sediment).
+  void adv_scalar_hlpa(A3& Phi, A3& R5, int IVAR) {
+    A3 Scalx, Scaly, Scalz;
+    Scalx.init(Mloc1, Nloc, Kloc); Scaly.init(Mloc, Nloc1, Kloc); Scalz.init(Mloc, Nloc, Kloc1);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend + 1; ++i) {
+          const double u = Ex(i, j, k);
+          Scalx(i, j, k) = u * hlpa(u, Phi(i - 2, j, k), Phi(i - 1, j, k), Phi(i, j, k), Phi(i + 1, j, k));
+        }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend + 1; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          const double v = Ey(i, j, k);
+          Scaly(i, j, k) = v * hlpa(v, Phi(i, j - 2, k), Phi(i, j - 1, k), Phi(i, j, k), Phi(i, j + 1, k));
+        }
+    for (int k = Kbeg + 1; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          const double w = Omega(i, j, k);
+          Scalz(i, j, k) = w * hlpa(w, Phi(i, j, k - 2), Phi(i, j, k - 1), Phi(i, j, k), Phi(i, j, k + 1));
+        }
+    // flux_scalar_bc
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        if (p.bc_x0 == 1 || p.bc_x0 == 2 || p.bc_x0 == 5) Scalx(Ibeg, j, k) = Zero;
+        else if (p.bc_x0 == 3) Scalx(Ibeg, j, k) = Ex(Ibeg, j, k) * 0.0;
+        Scalx(Iend1, j, k) = Zero;
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        if (p.bc_y0 == 1 || p.bc_y0 == 2 || p.bc_y0 == 5) Scaly(i, Jbeg, k) = Zero;
+        if (p.bc_yn == 1 || p.bc_yn == 2 || p.bc_yn == 5) Scaly(i, Jend1, k) = Zero;
+      }
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (Mask(i, j) == 0) {
+            Scalx(i, j, k) = Zero; Scalx(i + 1, j, k) = Zero;
+            Scaly(i, j, k) = Zero; Scaly(i, j + 1, k) = Zero;
+          }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int i = Ibeg; i <= Iend; ++i) { Scalz(i, j, Kbeg) = Zero; Scalz(i, j, Kend1) = Zero; }
+    const double SchtH = IVAR == 1 ? (p.rng ? (double)0.72f : 1.0) : (p.rng ? (double)0.72f : (double)1.3f);
+    R5.fill(0.0);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) {
+          if (Mask(i, j) == 0) continue;
+          auto nu = [&](double ha, double hb) { return 0.5 * (Cmu + Cmu) + 0.5 * (ha + hb) / SchtH; };
+          const double Sdiffx =
+              0.5 * (nu(CmuHt(i + 1, j, k), CmuHt(i, j, k)) * (D(i + 1, j) + D(i, j)) * (Phi(i + 1, j, k) - Phi(i, j, k)) -
+                     nu(CmuHt(i, j, k), CmuHt(i - 1, j, k)) * (D(i, j) + D(i - 1, j)) * (Phi(i, j, k) - Phi(i - 1, j, k))) /
+              (dx * dx);
+          const double Sdiffy =
+              0.5 * (nu(CmuHt(i, j + 1, k), CmuHt(i, j, k)) * (D(i, j + 1) + D(i, j)) * (Phi(i, j + 1, k) - Phi(i, j, k)) -
+                     nu(CmuHt(i, j, k), CmuHt(i, j - 1, k)) * (D(i, j) + D(i, j - 1)) * (Phi(i, j, k) - Phi(i, j - 1, k))) /
+              (dy * dy);
+          R5(i, j, k) = -(1.0 / dx * (Scalx(i + 1, j, k) - Scalx(i, j, k))) - 1.0 / dy * (Scaly(i, j + 1, k) - Scaly(i, j, k)) -
+                        1.0 / dsig(k) * (Scalz(i, j, k + 1) - Scalz(i, j, k)) + Sdiffx + Sdiffy;
+        }
+  }
+  // Shear production of the nonlinear k-epsilon model (ke_model = 2, Lin
+  // and Liu 1998; src/nhwave.F:10139-10274) at one cell: the Reynolds
+  // stresses from the velocity gradient G (limited horizontal slopes plus
+  // the sigma-slope terms) contracted with G per PRODTYPE (1: vertical
+  // shear of U, V; 2: vertical shear; otherwise full 3-D).  (2./3.) and
+  // (1./3.) are default-real quotients.
+  static double ke_production(const double G[3][3], double tk, double ep, int prod_type) {
+    const double c23 = (double)(2.0f / 3.0f), c13 = (double)(1.0f / 3.0f);
+    double smax = Zero;
+    for (int n = 0; n < 3; ++n)
+      if (std::fabs(G[n][n]) > smax) smax = std::fabs(G[n][n]);
+    smax = smax * tk / ep;
+    const double c_d = c23 * (1.0 / ((double)7.4f + 2.0 * smax));
+    double dmx = Zero;
+    for (int n = 0; n < 3; ++n)
+      for (int m = 0; m < 3; ++m)
+        if (std::fabs(G[n][m]) > dmx) dmx = std::fabs(G[n][m]);
+    dmx = dmx * tk / ep;
+    const double c_1 = 1.0 / ((double)185.2f + 3.0 * (dmx * dmx));
+    const double c_2 = -(1.0 / (58.5 + 2.0 * (dmx * dmx)));
+    const double c_3 = 1.0 / ((double)370.4f + 3.0 * (dmx * dmx));
+    const double tk2 = tk * tk, tk3 = tk * tk * tk, ep2 = ep * ep;
+    double RS[3][3];
+    for (int n = 0; n < 3; ++n)
+      for (int m = 0; m < 3; ++m) {
+        const double dl = n == m ? 1.0 : 0.0;
+        double r = c_d * tk2 / ep * (G[n][m] + G[m][n]) - c23 * tk * dl;
+        for (int l = 0; l < 3; ++l) {
+          r = r + c_1 * tk3 / ep2 * (G[n][l] * G[l][m] + G[m][l] * G[l][n]);
+          for (int g = 0; g < 3; ++g) r = r - c23 * c_1 * tk3 / ep2 * G[l][g] * G[g][l] * dl;
+        }
+        for (int g = 0; g < 3; ++g) {
+          r = r + c_2 * tk3 / ep2 * G[n][g] * G[m][g];
+          for (int l = 0; l < 3; ++l) r = r - c13 * c_2 * tk3 / ep2 * G[l][g] * G[l][g] * dl;
+        }
+        for (int g = 0; g < 3; ++g) {
+          r = r + c_3 * tk3 / ep2 * G[g][n] * G[g][m];
+          for (int l = 0; l < 3; ++l) r = r - c13 * c_3 * tk3 / ep2 * G[l][g] * G[l][g] * dl;
+        }
+        RS[n][m] = r;
+      }
+    double P = Zero;
+    const int n1 = prod_type == 1 ? 2 : 3, m0 = (prod_type == 1 || prod_type == 2) ? 2 : 0;
+    for (int n = 0; n < n1; ++n)
+      for (int m = m0; m < 3; ++m) P = P + RS[n][m] * G[n][m];
+    return P;
+  }
+  // kepsilon_3D (src/nhwave.F:10030-11114): the k-epsilon closure of
+  // IVTURB = 10 with the nonlinear production, the RNG variant (RNG = T),
+  // HLPA advection, implicit vertical diffusion, wall functions at the bed
+  // and on friction walls (BC = 5), the gradient condition at the surface,
+  // then CmuVt = cmiu k^2 / eps.  Barotropic: Rho = Rho0 everywhere
+  // (src/initialize.F:2561), so the buoyancy production is zero.  The
+  // reference leaves alpha_c, beta_c and gamma_c of its interior vertical
+  // coefficients unset (locals never assigned); they are taken here as the
+  // three-point weights the momentum equations use (src/nhwave.F:6826-6828).
+  void kepsilon_3D(int istep) {
+    const double Dmin = 2.0 * MinDep;
+    const bool rng = p.rng != 0;
+    const double c1e = rng ? (double)1.42f : (double)1.44f;
+    double c2e = rng ? 0.0 : (double)1.92f;
+    const double c3e = 0.0;
+    const double cmiu = rng ? (double)0.085f : (double)0.09f;
+    const double Sche = rng ? (double)0.72f : (double)1.3f, Schk = rng ? (double)0.72f : 1.0;
+    A3 Tke_Old = Tke, Eps_Old = Eps;
+    A3 Prod_s, R5;
+    Prod_s.init(Mloc, Nloc, Kloc); R5.init(Mloc, Nloc, Kloc);
+    auto ds = [&](int k) { return sigc(k + 1) - sigc(k - 1); };
+    auto vel_grad = [&](int i, int j, int k, double G[3][3]) {
+      const double dU = U(i, j, k + 1) - U(i, j, k - 1), dV = V(i, j, k + 1) - V(i, j, k - 1);
+      const double dW = W(i, j, k + 1) - W(i, j, k - 1);
+      G[0][0] = DelxU(i, j, k) + dU / ds(k) * DelxSc(i, j, k);
+      G[0][1] = DelyU(i, j, k) + dU / ds(k) * DelySc(i, j, k);
+      G[0][2] = 1.0 / D(i, j) * dU / ds(k);
+      G[1][0] = DelxV(i, j, k) + dV / ds(k) * DelxSc(i, j, k);
+      G[1][1] = DelyV(i, j, k) + dV / ds(k) * DelySc(i, j, k);
+      G[1][2] = 1.0 / D(i, j) * dV / ds(k);
+      G[2][0] = DelxW(i, j, k) + dW / ds(k) * DelxSc(i, j, k);
+      G[2][1] = DelyW(i, j, k) + dW / ds(k) * DelySc(i, j, k);
+      G[2][2] = 1.0 / D(i, j) * dW / ds(k);
+    };
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          if (!(D(i, j) >= Dmin && Mask(i, j) == 1)) continue;
+          double G[3][3];
+          vel_grad(i, j, k, G);
+          double P = ke_production(G, Tke_Old(i, j, k), Eps_Old(i, j, k), p.prod_type);
+          if (k == Kend && P < 0.0) P = Zero;   // no negative production at the surface
+          Prod_s(i, j, k) = P;
+        }
+    const double Prod_b = 0.0;
+    // surface values of tke and epsilon (construct_3D_z, floored) and their
+    // limited horizontal slopes, for the gradient condition at the surface
+    A3 DelzTke, DelzEps, TkezL, TkezR, EpszL, EpszR, DelxTkezL, DelxEpszL, DelyTkezL, DelyEpszL;
+    DelzTke.init(Mloc, Nloc, Kloc); DelzEps.init(Mloc, Nloc, Kloc);
+    for (A3* a : {&TkezL, &TkezR, &EpszL, &EpszR, &DelxTkezL, &DelxEpszL, &DelyTkezL, &DelyEpszL})
+      a->init(Mloc, Nloc, Kloc1);
+    delzFun_3D(Tke_Old, DelzTke);
+    delzFun_3D(Eps_Old, DelzEps);
+    construct_3D_z(Tke_Old, DelzTke, TkezL, TkezR);
+    construct_3D_z(Eps_Old, DelzEps, EpszL, EpszR);
+    for (double& v : TkezL.v) v = dmax(v, Tke_min);
+    for (double& v : TkezR.v) v = dmax(v, Tke_min);
+    for (double& v : EpszL.v) v = dmax(v, Eps_min);
+    for (double& v : EpszR.v) v = dmax(v, Eps_min);
+    delxFun_3D(TkezL, DelxTkezL);
+    delxFun_3D(EpszL, DelxEpszL);
+    delyFun_3D(TkezL, DelyTkezL);
+    delyFun_3D(EpszL, DelyEpszL);
+    const int n = Kend - Kbeg + 1;
+    std::vector<double> Ac(n), Bc(n), Cc(n), Rhs0(n), Xsol(n);
+    // one column of the epsilon (eq = 2) or tke (eq = 1) equation
+    auto column = [&](int i, int j, int eq) {
+      A3& Old = eq == 2 ? Eps_Old : Tke_Old;
+      A3& zL = eq == 2 ? EpszL : TkezL;
+      A3& Dv = eq == 2 ? DEps : DTke;
+      const double Sch = eq == 2 ? Sche : Schk;
+      const double Dc = D(i, j);
+      const double DxD = (DelxH(i, j) + DelxEta(i, j)) / Dc, DyD = (DelyH(i, j) + DelyEta(i, j)) / Dc;
+      int q = 0;
+      for (int k = Kbeg; k <= Kend; ++k) {
+        const double L1top = dsig(k + 1) / (dsig(k) + dsig(k + 1)), L2top = dsig(k) / (dsig(k) + dsig(k + 1));
+        const double L1bot = dsig(k) / (dsig(k) + dsig(k - 1)), L2bot = dsig(k - 1) / (dsig(k) + dsig(k - 1));
+        const double dsigck = (dsig(k) + dsig(k + 1)) / 2.0, dsigck1 = (dsig(k - 1) + dsig(k)) / 2.0;
+        const double alpha_c = -dsigck / (dsigck + dsigck1) / dsigck1;
+        const double beta_c = (dsigck - dsigck1) / (dsigck * dsigck1);
+        const double gamma_c = dsigck1 / (dsigck + dsigck1) / dsigck;
+        const double nuV_top = (L1top * Cmu + L2top * Cmu) + (L1top * CmuR + L2top * CmuR) +
+                               (L1top * CmuVt(i, j, k) + L2top * CmuVt(i, j, k + 1)) / Sch;
+        const double nuH_top = (L1top * Cmu + L2top * Cmu) + (L1top * CmuR + L2top * CmuR) +
+                               (L1top * CmuHt(i, j, k) + L2top * CmuHt(i, j, k + 1)) / Sch;
+        const double nuV_bot = (L1bot * Cmu + L2bot * Cmu) + (L1bot * CmuR + L2bot * CmuR) +
+                               (L1bot * CmuVt(i, j, k - 1) + L2bot * CmuVt(i, j, k)) / Sch;
+        const double nuH_bot = (L1bot * Cmu + L2bot * Cmu) + (L1bot * CmuR + L2bot * CmuR) +
+                               (L1bot * CmuHt(i, j, k - 1) + L2bot * CmuHt(i, j, k)) / Sch;
+        double r = R5(i, j, k);
+        if (eq == 2) r = r + c1e * Dc * (Prod_s(i, j, k) + c3e * Prod_b) * Eps_Old(i, j, k) / Tke_Old(i, j, k);
+        else r = r + Dc * (Prod_s(i, j, k) + Prod_b) - DEps(i, j, k);
+        if (k == Kbeg) {
+          r = r - (-(nuH_bot * (DelxH(i, j) * DxD + DelyH(i, j) * DyD) * Old(i, j, k))) / dsig(k) +
+              (dsig(k) - dsigck) / (dsig(k) * dsig(k) / 2.0 * (dsigck + dsig(k) / 2.0)) *
+                  (nuH_top * (DelxSl(i, j, k + 1) * DelxH(i, j) + DelySl(i, j, k + 1) * DelyH(i, j)) + nuV_top / Dc) *
+                  Old(i, j, k);
+        } else if (k == Kend) {
+          r = r + ((nuH_top * (DelxEta(i, j) * DelxEta(i, j) + DelyEta(i, j) * DelyEta(i, j)) + nuV_top) / (Dc * Dc) *
+                       (Old(i, j, k + 1) - Old(i, j, k)) * Dc / dsigck -
+                   nuH_top * (-(DelxEta(i, j) * DxD) - DelyEta(i, j) * DyD) * zL(i, j, k + 1)) /
+                      dsig(k) +
+              (dsig(k) - dsigck1) / (dsig(k) * dsig(k) / 2.0 * (dsigck1 + dsig(k) / 2.0)) *
+                  (nuH_bot * (-(DelxSl(i, j, k) * DelxEta(i, j)) - DelySl(i, j, k) * DelyEta(i, j)) + nuV_bot / Dc) *
+                  zL(i, j, k + 1);
+        }
+        // sigma-coupled vertical diffusion a . (nu_top Sl_top S_kk - nu_bot Sl_bot S_kk) + nu/D^2 at level kk
+        auto top = [&](int kk) {
+          return nuH_top * (DelxSl(i, j, k + 1) * DelxSc(i, j, kk) + DelySl(i, j, k + 1) * DelySc(i, j, kk)) +
+                 nuV_top / (Dc * Dc);
+        };
+        auto bot = [&](int kk) {
+          return nuH_bot * (DelxSl(i, j, k) * DelxSc(i, j, kk) + DelySl(i, j, k) * DelySc(i, j, kk)) +
+                 nuV_bot / (Dc * Dc);
+        };
+        if (k == Kbeg) Ac[q] = 0.0;
+        else if (k == Kend) Ac[q] = -dt * (3.0 / 2.0 * bot(k - 1) / (dsigck1 * (dsigck1 + dsig(k) / 2.0)));
+        else
+          Ac[q] = -dt * ((top(k - 1) - bot(k - 1)) * alpha_c / dsig(k) +
+                         (top(k - 1) + bot(k - 1)) / (dsigck1 * (dsigck1 + dsigck)));
+        if (k == Kbeg) Cc[q] = -dt * (3.0 / 2.0 * top(k + 1) / (dsigck * (dsigck + dsig(k) / 2.0)));
+        else if (k == Kend) Cc[q] = 0.0;
+        else
+          Cc[q] = -dt * ((top(k + 1) - bot(k + 1)) * gamma_c / dsig(k) +
+                         (top(k + 1) + bot(k + 1)) / (dsigck * (dsigck1 + dsigck)));
+        double b0 = 1.0;
+        if (eq == 2) {
+          if (rng) {   // c2e of Yakhot et al. (1992) from the strain rate
+            const double dUs = (U(i, j, k + 1) - U(i, j, k - 1)) / ds(k), dVs = (V(i, j, k + 1) - V(i, j, k - 1)) / ds(k);
+            const double dWs = (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+            const double S11 = DelxU(i, j, k) + dUs * DelxSc(i, j, k);
+            const double S22 = DelyV(i, j, k) + dVs * DelySc(i, j, k);
+            const double S33 = 1.0 / Dc * (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+            const double S12 = 0.5 * (DelyU(i, j, k) + dUs * DelySc(i, j, k) + DelxV(i, j, k) + dVs * DelxSc(i, j, k));
+            const double S13 = 0.5 * ((U(i, j, k + 1) - U(i, j, k - 1)) / ds(k) / Dc + DelxW(i, j, k) + dWs * DelxSc(i, j, k));
+            const double S23 = 0.5 * ((V(i, j, k + 1) - V(i, j, k - 1)) / ds(k) / Dc + DelyW(i, j, k) + dWs * DelySc(i, j, k));
+            const double lambda = Tke_Old(i, j, k) / Eps_Old(i, j, k) *
+                                  std::sqrt(2.0 * (S11 * S11 + S22 * S22 + S33 * S33 +
+                                                   2.0 * (S12 * S12 + S13 * S13 + S23 * S23)));
+            const double l3 = lambda * lambda * lambda;
+            c2e = (double)1.68f + cmiu * l3 * (1.0 - lambda / (double)4.38f) / (1.0 + (double)0.012f * l3);
+            c2e = dmax(0.0, dmin(c2e, 4.0));
+          }
+          b0 = 1.0 + dt * c2e * Eps_Old(i, j, k) / Tke_Old(i, j, k);
+        }
+        if (k == Kbeg) Bc[q] = b0 - dt * (-(3.0 / 2.0 - dsigck / dsig(k)) * top(k) / (dsig(k) / 2.0 * dsigck));
+        else if (k == Kend) Bc[q] = b0 - dt * (-(3.0 / 2.0 - dsigck1 / dsig(k)) * bot(k) / (dsig(k) / 2.0 * dsigck1));
+        else
+          Bc[q] = b0 - dt * ((top(k) - bot(k)) * beta_c / dsig(k) - (top(k) + bot(k)) / (dsigck * dsigck1));
+        Rhs0[q] = Dv(i, j, k) + dt * r;
+        ++q;
+      }
+      trig(Ac, Bc, Cc, Rhs0, Xsol, n);
+      q = 0;
+      for (int k = Kbeg; k <= Kend; ++k) Dv(i, j, k) = Xsol[q++];
+    };
+    auto rk = [&](A3& Dv, A3& Dv0, double vmin) {
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int j = Jbeg; j <= Jend; ++j)
+          for (int k = Kbeg; k <= Kend; ++k)
+            if (D(i, j) >= Dmin && Mask(i, j) == 1) {
+              Dv(i, j, k) = ALPHA[istep - 1] * Dv0(i, j, k) + BETA[istep - 1] * Dv(i, j, k);
+              Dv(i, j, k) = dmax(Dv(i, j, k), D(i, j) * vmin);
+            }
+    };
+    // epsilon, then tke (whose source reads the new DEps); a column is
+    // skipped only where it is both shallower than Dmin and dry
+    adv_scalar_hlpa(Eps_Old, R5, 2);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        if (!(D(i, j) < Dmin && Mask(i, j) == 0)) column(i, j, 2);
+    rk(DEps, DEps0, Eps_min);
+    adv_scalar_hlpa(Tke_Old, R5, 1);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        if (!(D(i, j) < Dmin && Mask(i, j) == 0)) column(i, j, 1);
+    rk(DTke, DTke0, Tke_min);
+    // bed: wall function (src/nhwave.F:10776-10831)
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double dxh = DelxH(i, j), dyh = DelyH(i, j);
+        const double Abot = std::sqrt(1.0 + dxh * dxh + dyh * dyh), Bbot = std::sqrt(1.0 + dxh * dxh);
+        const double DUprime = (DU(i, j, Kbeg) - dxh * DW(i, j, Kbeg)) / Bbot;
+        const double DVprime =
+            (-(dxh * dyh * DU(i, j, Kbeg)) + (1.0 + dxh * dxh) * DV(i, j, Kbeg) - dyh * DW(i, j, Kbeg)) / Abot / Bbot;
+        const double DUmag = std::sqrt(DUprime * DUprime + DVprime * DVprime);
+        if (D(i, j) < Dmin || Mask(i, j) == 0) continue;
+        double Tkeb, Epsb;
+        if (DUmag / D(i, j) < (double)1.e-6f) {
+          Tkeb = Tke_min; Epsb = Eps_min;
+        } else {
+          const double Dz1 = 0.5 * D(i, j) * dsig(Kbeg) / Abot;
+          const double Z0 = p.zob / 30.0;
+          double Cdrag;
+          if (p.ibot == 1) Cdrag = p.cd0;
+          else { const double t = Kappa / std::log(Dz1 / Z0); Cdrag = t * t; }
+          Cdrag = dmin(Cdrag, (Cmu + CmuR + CmuVt(i, j, Kbeg)) / Dz1 / (DUmag + Small) * D(i, j));
+          const double Ustar = std::sqrt(Cdrag) * DUmag / D(i, j);
+          Tkeb = dmax(Ustar * Ustar / std::sqrt(cmiu), Tke_min);
+          Epsb = dmax(Ustar * Ustar * Ustar / (Kappa * Dz1), Eps_min);
+        }
+        DTke(i, j, Kbeg) = D(i, j) * Tkeb;
+        DEps(i, j, Kbeg) = D(i, j) * Epsb;
+        for (int k = 1; k <= Nghost; ++k) {
+          DTke(i, j, Kbeg - k) = DTke(i, j, Kbeg);
+          DEps(i, j, Kbeg - k) = DEps(i, j, Kbeg);
+        }
+      }
+    // surface: gradient condition (Derakhti et al. 2015, eq. 60)
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        if (Mask(i, j) == 0 || D(i, j) < Dmin) continue;
+        for (int k = 1; k <= Nghost; ++k) {
+          const double dxe = DelxEta(i, j), dye = DelyEta(i, j);
+          const double Atop = std::sqrt(1.0 + dxe * dxe + dye * dye);
+          const double f = (sigc(Kend + k) - sigc(Kend - k + 1)) * (D(i, j) * D(i, j)) / (Atop * Atop);
+          DTke(i, j, Kend + k) = DTke(i, j, Kend - k + 1) + f * (dxe * DelxTkezL(i, j, Kend1) + dye * DelyTkezL(i, j, Kend1));
+          DEps(i, j, Kend + k) = DEps(i, j, Kend - k + 1) + f * (dxe * DelxEpszL(i, j, Kend1) + dye * DelyEpszL(i, j, Kend1));
+        }
+      }
+    // side walls: wall function on friction walls (BC = 5), then mirrors
+    auto wall = [&](int ii, int jj, int kk, double Umag, double h) {
+      double Tkeb, Epsb;
+      if (Umag < (double)1.e-6f) {
+        Tkeb = Tke_min; Epsb = Eps_min;
+      } else {
+        const double FricU = p.ibot == 1 ? std::sqrt(p.cd0) * Umag : Umag / (1.0 / Kappa * std::log(30.0 * h / 2.0 / p.zob));
+        Tkeb = FricU * FricU / std::sqrt(cmiu);
+        Epsb = FricU * FricU * FricU / (Kappa * h / 2.0);
+      }
+      DTke(ii, jj, kk) = D(ii, jj) * Tkeb;
+      DEps(ii, jj, kk) = D(ii, jj) * Epsb;
+    };
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = 1; k <= Kloc; ++k) {
+        if (p.bc_x0 == 5) wall(Ibeg, j, k, std::sqrt(V(Ibeg, j, k) * V(Ibeg, j, k) + W(Ibeg, j, k) * W(Ibeg, j, k)), dx);
+        for (int i = 1; i <= Nghost; ++i) {
+          DTke(Ibeg - i, j, k) = DTke(Ibeg + i - 1, j, k);
+          DEps(Ibeg - i, j, k) = DEps(Ibeg + i - 1, j, k);
+        }
+      }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = 1; k <= Kloc; ++k) {
+        if (p.bc_xn == 5) wall(Iend, j, k, std::sqrt(V(Iend, j, k) * V(Iend, j, k) + W(Iend, j, k) * W(Iend, j, k)), dx);
+        for (int i = 1; i <= Nghost; ++i) {
+          DTke(Iend + i, j, k) = DTke(Iend - i + 1, j, k);
+          DEps(Iend + i, j, k) = DEps(Iend - i + 1, j, k);
+        }
+      }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int k = 1; k <= Kloc; ++k) {
+        if (p.bc_y0 == 5) wall(i, Jbeg, k, std::sqrt(U(i, Jbeg, k) * U(i, Jbeg, k) + W(i, Jbeg, k) * W(i, Jbeg, k)), dy);
+        for (int j = 1; j <= Nghost; ++j) {
+          DTke(i, Jbeg - j, k) = DTke(i, Jbeg + j - 1, k);
+          DEps(i, Jbeg - j, k) = DEps(i, Jbeg + j - 1, k);
+        }
+      }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int k = 1; k <= Kloc; ++k) {
+        if (p.bc_yn == 5) wall(i, Jend, k, std::sqrt(U(i, Jend, k) * U(i, Jend, k) + W(i, Jend, k) * W(i, Jend, k)), dy);
+        for (int j = 1; j <= Nghost; ++j) {
+          DTke(i, Jend + j, k) = DTke(i, Jend - j + 1, k);
+          DEps(i, Jend + j, k) = DEps(i, Jend - j + 1, k);
+        }
+      }
+    // tke, epsilon and the eddy viscosity in every cell
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int k = 1; k <= Kloc; ++k) {
+          if (D(i, j) >= Dmin && Mask(i, j) == 1) {
+            Tke(i, j, k) = DTke(i, j, k) / D(i, j);
+            Eps(i, j, k) = DEps(i, j, k) / D(i, j);
+            if (Tke(i, j, k) < (double)1.e-6f || Eps(i, j, k) < (double)1.e-6f) CmuVt(i, j, k) = Cmut_min;
+            else CmuVt(i, j, k) = cmiu * (Tke(i, j, k) * Tke(i, j, k)) / Eps(i, j, k);
+          } else {
+            Tke(i, j, k) = Tke_min;
+            Eps(i, j, k) = Eps_min;
+            DTke(i, j, k) = D(i, j) * Tke_min;
+            DEps(i, j, k) = D(i, j) * Eps_min;
+            CmuVt(i, j, k) = Cmut_min;
+          }
+        }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int k = 1; k <= Nghost; ++k) {
+          CmuVt(i, j, Kbeg - k) = CmuVt(i, j, Kbeg);
+          CmuVt(i, j, Kend + k) = CmuVt(i, j, Kend);
+        }
+    // no turbulence in the wavemaker's source region (INT_, LEF_ and FOCUSED)
+    if (ke_quiet_maker()) {
+      for (int k = 1; k <= Kloc; ++k)
+        for (int j = 1; j <= Nloc; ++j)
+          for (int i = 1; i <= Mloc; ++i)
+            if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+                yc(j) <= p.ysource_nrth) {
+              Tke(i, j, k) = Tke_min;
+              Eps(i, j, k) = Eps_min;
+              DTke(i, j, k) = D(i, j) * Tke_min;
+              DEps(i, j, k) = D(i, j) * Eps_min;
+              CmuVt(i, j, k) = Cmut_min;
+            }
+    }
+  }
+  // WaveMaker(1:3) is INT, LEF or FOC
+  bool ke_quiet_maker() const {
+    const int w = p.wavemaker;
+    return w == NHW_WM_INT_LIN || w == NHW_WM_INT_SOL || w == NHW_WM_INT_CON || w == NHW_WM_INT_JON ||
+           w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR || w == NHW_WM_LEF_LIN ||
+           w == NHW_WM_LEF_SOL || w == NHW_WM_LEF_STK || w == NHW_WM_LEF_CON || w == NHW_WM_LEF_TID ||
+           w == NHW_WM_LEF_JON || w == NHW_WM_LEF_TMA || w == NHW_WM_LEF_SPC || w == NHW_WM_FOCUSED;
+  }
+
   // eval_turb (src/nhwave.F:6544-6782), called after sponge_damping.
   // Vertical: IVTURB 1 CmuVt = Cvs; 2 the subgrid model CmuVt = Cvs D
   // dsig^2 |d(U,V)/dsigma| on every level but the outermost ghosts, which
@@ -2707,10 +3166,12 @@ struct Model {
   // ghosts of the sides (interior rows) and of the bed and surface
   // (interior columns).  The reference's Strxy reads U(i,j+1,j), the row
   // index where the level belongs (:6695); the level k is used here.
-  void eval_turb() {
+  void eval_turb(int istep) {
     if (!p.viscous_flow) return;
     if (p.ivturb == 1) {
       CmuVt.fill(p.cvs);
+    } else if (p.ivturb == 10) {
+      kepsilon_3D(istep);
     } else {
       for (int i = 1; i <= Mloc; ++i)
         for (int j = 1; j <= Nloc; ++j) {
@@ -2725,6 +3186,10 @@ struct Model {
     }
     if (p.ihturb == 1) {
       CmuHt.fill(p.chs);
+      return;
+    }
+    if (p.ihturb >= 10) {   // the 3-D model's length scales in every direction
+      CmuHt = CmuVt;
       return;
     }
     for (int i = Ibeg; i <= Iend; ++i)
@@ -2793,7 +3258,7 @@ struct Model {
       int e = eval_duvw(s);
       if (e != NHW_OK && worst == NHW_OK) worst = e;
       if (p.sponge_on) sponge_damping();
-      eval_turb();
+      eval_turb(s);
     }
     if (worst == NHW_ERR_NAN) status = worst;
     return worst;
@@ -2865,6 +3330,8 @@ struct Model {
       case NHW_F_GY: a3(Gy); break; case NHW_F_HY: a3(Hy); break; case NHW_F_FZ: a3(Fz); break;
       case NHW_F_GZ: a3(Gz); break; case NHW_F_HZ: a3(Hz); break;
       case NHW_F_CMUVT: a3(CmuVt); break; case NHW_F_CMUHT: a3(CmuHt); break;
+      case NHW_F_TKE: a3(Tke); break; case NHW_F_EPS: a3(Eps); break;
+      case NHW_F_DTKE: a3(DTke); break; case NHW_F_DEPS: a3(DEps); break;
       default: break;
     }
     return r;
@@ -2897,7 +3364,7 @@ void orc_update_mask(void* o) { static_cast<Model*>(o)->update_mask(); }
 void orc_update_wave_bc(void* o) { static_cast<Model*>(o)->update_wave_bc(); }
 void orc_update_vars(void* o) { Model* m = static_cast<Model*>(o); m->update_wind(); m->update_vars(); }
 void orc_source_terms(void* o) { static_cast<Model*>(o)->source_terms(); }
-void orc_eval_turb(void* o) { static_cast<Model*>(o)->eval_turb(); }
+void orc_eval_turb(void* o, int istep) { static_cast<Model*>(o)->eval_turb(istep); }
 void orc_fluxes(void* o) { static_cast<Model*>(o)->fluxes(); }
 int orc_eval_duvw(void* o, int istep) { return static_cast<Model*>(o)->eval_duvw(istep); }
 void orc_sponge_damping(void* o) { static_cast<Model*>(o)->sponge_damping(); }

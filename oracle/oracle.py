@@ -54,8 +54,10 @@ def lib():
         for name in ("orc_estimate_dt", "orc_step"):
             getattr(L, name).argtypes = [vp]
         L.orc_eval_duvw.argtypes = [vp, i32]
+        L.orc_eval_turb.argtypes = [vp, i32]
+        L.orc_eval_turb.restype = None
         for name in ("orc_update_bathymetry", "orc_update_wave_bc", "orc_update_mask", "orc_update_vars",
-                     "orc_source_terms", "orc_fluxes", "orc_sponge_damping", "orc_eval_turb",
+                     "orc_source_terms", "orc_fluxes", "orc_sponge_damping",
                      "orc_generate_coef_rhs"):
             getattr(L, name).argtypes = [vp]
             getattr(L, name).restype = None
@@ -149,8 +151,8 @@ class Oracle:
     def sponge_damping(self):
         lib().orc_sponge_damping(self._h)
 
-    def eval_turb(self):
-        lib().orc_eval_turb(self._h)
+    def eval_turb(self, istep: int):
+        lib().orc_eval_turb(self._h, istep)
 
     def step(self):
         return lib().orc_step(self._h)
@@ -267,7 +269,7 @@ def run_scenario(name: str, steps: int, tol: float = 1e-13, pinned: bool = False
                     raise RuntimeError(f"oracle eval_duvw: {rc}")
                 if o.params.sponge_on:
                     o.sponge_damping()
-                o.eval_turb()
+                o.eval_turb(s)
         else:
             rc = o.step()
             if rc:

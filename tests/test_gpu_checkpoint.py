@@ -9,6 +9,8 @@ ends with the same bits as one served without interruption."""
 import numpy as np
 import pytest
 
+from conftest import seed_ke
+
 pytestmark = pytest.mark.gpu
 
 FIELDS = ["ETA", "D", "HC", "U", "V", "W", "DU", "P", "OMEGA", "MASK", "ETAXL", "HFX0", "DELT2H"]
@@ -21,20 +23,24 @@ def _scen(name, precision, **attrs):
     p.itmax = 5000
     for k, v in attrs.items():
         setattr(p, k, v)
-    return lib.Scenario(p, d, e, u)
+    s = lib.Scenario(p, d, e, u)
+    if p.viscous_flow and p.ivturb == 10:
+        seed_ke(s)
+    return s
 
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,krylov", [("tiny_c2", 0), ("tiny_c3", 0), ("tiny_c4", 0), ("tiny_flume_lin", 0),
                                          ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0),
-                                         ("tiny_visc_sgs", 0)])
+                                         ("tiny_visc_sgs", 0), ("tiny_ke_rng", 0)])
 def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     """krylov = 2: the GMRES solver, whose basis lies behind the checkpointed
     prefix and is rebuilt by every solve.  tiny_open: the Orlanski boundary's
     two earlier time levels are part of the checkpointed state; tiny_flux_lr:
     so are FLUX_LR's outflow velocities of the last two steps; tiny_visc:
     the sigma slopes the next viscous terms read are too; tiny_visc_sgs: and
-    the cells' eddy viscosities of the last eval_turb."""
+    the cells' eddy viscosities of the last eval_turb; tiny_ke_rng: and the
+    k-epsilon state."""
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, krylov_kernel=krylov)
     for _ in range(4):
@@ -50,7 +56,9 @@ def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     sa, sb = a.scalars(), b.scalars()
     assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
     assert sa.total_krylov_iters == sb.total_krylov_iters
-    for f in FIELDS + (["CMUVT", "CMUHT"] if a.params.viscous_flow else []):
+    extra = (["CMUVT", "CMUHT"] if a.params.viscous_flow else []) + \
+        (["TKE", "EPS", "DTKE", "DEPS"] if a.params.viscous_flow and a.params.ivturb == 10 else [])
+    for f in FIELDS + extra:
         fid = getattr(F, f)
         assert np.array_equal(a.get(fid), b.get(fid)), f"{name} {f}"
 

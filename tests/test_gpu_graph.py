@@ -8,6 +8,8 @@ run gate of nhw_run (TOTAL_TIME / SIM_STEPS) and the solver counters.
 import numpy as np
 import pytest
 
+from conftest import seed_ke
+
 pytestmark = pytest.mark.gpu
 
 FIELDS = ["D", "ETA", "HC", "U", "V", "W", "DU", "DV", "DW", "P", "OMEGA", "MASK"]
@@ -20,7 +22,10 @@ def _scen(name, precision, **attrs):
     p.itmax = 5000
     for k, v in attrs.items():
         setattr(p, k, v)
-    return lib.Scenario(p, d, e, u)
+    s = lib.Scenario(p, d, e, u)
+    if p.viscous_flow and p.ivturb == 10:
+        seed_ke(s)
+    return s
 
 
 def _routines(s):
@@ -37,14 +42,14 @@ def _routines(s):
         s.eval_duvw(st)
         if s.params.sponge_on:
             s.sponge_damping()
-        s.eval_turb()
+        s.eval_turb(st)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4", "tiny_flume_lin", "tiny_flume_sol",
                                   "tiny_flume_stk", "tiny_flume_con", "tiny_flume_cur", "tiny_flume_foc", "tiny_flume_tid", "tiny_open",
                                   "tiny_flume_open", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon",
-                                  "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric"])
+                                  "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng"])
 def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, hllc=hllc)
@@ -56,7 +61,8 @@ def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
         assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
         assert sa.total_krylov_iters == sb.total_krylov_iters
         assert sa.poisson_solves == sb.poisson_solves
-        for f in FIELDS:
+        ke = ["TKE", "EPS", "CMUVT", "CMUHT"] if a.params.viscous_flow and a.params.ivturb == 10 else []
+        for f in FIELDS + ke:
             fid = getattr(F, f)
             x, y = a.get(fid), b.get(fid)
             bad = np.argwhere(x != y)

@@ -9,7 +9,7 @@ FP32+IR form: eta within 1e-6 relative L2 of the FP64 oracle, masks bit-exact.
 import numpy as np
 import pytest
 
-from conftest import rel_l2
+from conftest import rel_l2, seed_ke
 
 pytestmark = pytest.mark.gpu
 
@@ -17,10 +17,11 @@ CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # plus a solitary wave leaving through an open (Orlanski, BC_Xn = 6) east
 # side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
 # in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds;
-# the subgrid eddy viscosities, IVTURB = IHTURB = 2), and wall friction
-# (BC = 5) on the sides
+# the subgrid eddy viscosities, IVTURB = IHTURB = 2; the k-epsilon closure,
+# IVTURB = IHTURB = 10, standard and RNG, from seeded turbulence), and wall
+# friction (BC = 5) on the sides
 MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric",
-                      "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_wallfric"]
+                      "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng", "tiny_wallfric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -49,6 +50,8 @@ def _pair(name, oracle_mod, precision=0, tol=STEP_TOL, seed=7, **kw):
     q = p.copy()
     q.precision = 0
     o = oracle_mod.Oracle(q, d, e, u)
+    if p.viscous_flow and p.ivturb == 10:
+        seed_ke(g, o)
     return g, o
 
 
@@ -116,8 +119,9 @@ def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
                 g.sponge_damping(); o.sponge_damping()
                 _cmp_exact(g, o, ["D", "ETA"] + STATE3D, f"sponge {rnd}.{s}")
             if g.params.viscous_flow:
-                g.eval_turb(); o.eval_turb()
-                _cmp_exact(g, o, ["CMUVT", "CMUHT"], f"eval_turb {rnd}.{s}")
+                g.eval_turb(s); o.eval_turb(s)
+                ke = ["TKE", "EPS", "DTKE", "DEPS"] if g.params.ivturb == 10 else []
+                _cmp_exact(g, o, ["CMUVT", "CMUHT"] + ke, f"eval_turb {rnd}.{s}")
     g.close()
 
 
@@ -146,7 +150,7 @@ def step_pinned(g, o):
             assert obj.eval_duvw(s) == 0
             if obj.params.sponge_on:
                 obj.sponge_damping()
-            obj.eval_turb()
+            obj.eval_turb(s)
 
 
 @pytest.mark.parametrize("name", MORE_CASES)

@@ -399,7 +399,7 @@ def test_subgrid_eddy_viscosities_of_a_linear_flow(oracle_mod):
     o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
     # the seeding viscosity Cmut_min = 0.09 Tke_min^2 / Eps_min (src/initialize.F:3178-3191)
     assert np.allclose(o.get(F.CMUVT), 9.0e-2 * 1e-9, rtol=1e-6)
-    o.eval_turb()
+    o.eval_turb(1)
     ng = F.NG
     cv, ch = o.get(F.CMUVT), o.get(F.CMUHT)
     # (sigma levels and dsig are default-real values of the reference: 1e-6)
@@ -415,6 +415,93 @@ def test_subgrid_eddy_viscosities_of_a_linear_flow(oracle_mod):
     assert o.estimate_dt() == 0
     top = np.abs(ch[ng:ng + K, ng:ng + N, ng:ng + M]).max()
     assert o.scalars().dt == pytest.approx(min(1.05 * 0.01, p.viscous_number * min(dx, dy) ** 2 / top), rel=1e-6)
+
+
+def _ke_channel(oracle_mod, k0, e0, u_of_sigma=None, M=8, N=3, K=6, **kw):
+    """Flat 1 m deep channel with the k-epsilon closure (IVTURB = IHTURB =
+    10), uniform tke k0 and epsilon e0 in every cell, and an optional
+    current U(sigma); returns the oracle."""
+    from nhwave_gb300 import default_params, fields as F
+    kw = dict(dict(visc=1e-6), **kw)
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.5, dt_ini=0.01, dt_max=0.01, tol=1e-12, itmax=2000,
+                       viscous_flow=1, ivturb=10, ihturb=10, **kw)
+    uvw = np.zeros((3, K, N, M))
+    if u_of_sigma is not None:
+        uvw[0] = u_of_sigma((np.arange(K) + 0.5) / K)[:, None, None]
+    o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
+    D = o.get(F.D)[None]
+    shp = o.get(F.TKE).shape
+    o.set(F.TKE, np.full(shp, k0)); o.set(F.EPS, np.full(shp, e0))
+    o.set(F.DTKE, D * k0 * np.ones(shp)); o.set(F.DEPS, D * e0 * np.ones(shp))
+    return o
+
+
+def _ke_stage(o, istep=1):
+    assert o.estimate_dt() == 0
+    o.update_vars(); o.source_terms(); o.fluxes()
+    assert o.eval_duvw(istep) == 0
+    o.eval_turb(istep)
+
+
+def test_ke_uniform_turbulence_decays_by_the_implicit_step(oracle_mod):
+    """kepsilon_3D (src/nhwave.F:10030-11114) in still water with uniform
+    tke k0 and epsilon e0: no production, advection or diffusion, so the
+    first stage's implicit step gives eps1 = e0 / (1 + dt c2e e0 / k0) and
+    k1 = k0 - dt eps1 above the bed level (whose wall function resets it),
+    and CmuVt = cmiu k1^2 / eps1; CmuHt = CmuVt (IHTURB = 10)."""
+    from nhwave_gb300 import fields as F
+    k0, e0 = 1e-3, 1e-4
+    o = _ke_channel(oracle_mod, k0, e0)
+    _ke_stage(o)
+    dt = o.scalars().dt
+    ng, K = F.NG, 6
+    c2e, cmiu = float(np.float32(1.92)), float(np.float32(0.09))
+    e1 = e0 / (1 + dt * c2e * e0 / k0)
+    k1 = k0 - dt * e1
+    inner = (slice(ng + 1, ng + K), slice(ng, ng + 3), slice(ng, ng + 8))
+    assert o.get(F.EPS)[inner] == pytest.approx(np.full((K - 1, 3, 8), e1), rel=1e-12)
+    assert o.get(F.TKE)[inner] == pytest.approx(np.full((K - 1, 3, 8), k1), rel=1e-12)
+    assert o.get(F.CMUVT)[inner] == pytest.approx(np.full((K - 1, 3, 8), cmiu * k1 * k1 / e1), rel=1e-12)
+    assert np.array_equal(o.get(F.CMUHT), o.get(F.CMUVT))
+    # still water over the bed: the wall function gives the floors there
+    assert np.all(o.get(F.TKE)[ng, ng:ng + 3, ng:ng + 8] == pytest.approx(1e-9, rel=1e-6))
+
+
+def test_ke_bed_wall_function_of_a_current(oracle_mod):
+    """The bed condition of kepsilon_3D (src/nhwave.F:10776-10831): under a
+    current, the first level's tke is u*^2 / sqrt(cmiu) and epsilon
+    u*^3 / (Kappa Dz1), with u* = sqrt(Cdrag) |DU| / D and Cdrag the drag
+    coefficient Cd0 capped by the viscous limit (Cmu + CmuVt) D / (Dz1 |DU|)."""
+    from nhwave_gb300 import fields as F
+    K = 6
+    o = _ke_channel(oracle_mod, 1e-4, 1e-5, lambda s: 0.3 + 0.0 * s, K=K, visc=1e-3, bc_z0=5, ibot=1, cd0=0.003)
+    cv_bed = o.get(F.CMUVT)[F.NG].copy()
+    _ke_stage(o)
+    ng = F.NG
+    du = o.get(F.DU)[ng, ng + 1, ng + 3]
+    D = o.get(F.D)[ng + 1, ng + 3]
+    dz1 = 0.5 * D * float(np.float32(1.0) / np.float32(K))
+    cd = min(0.003, (1e-3 + cv_bed[ng + 1, ng + 3]) / dz1 / (abs(du) + 1e-16) * D)
+    us = math.sqrt(cd) * abs(du) / D
+    kappa, cmiu = float(np.float32(0.41)), float(np.float32(0.09))
+    assert o.get(F.TKE)[ng, ng + 1, ng + 3] == pytest.approx(us * us / math.sqrt(cmiu), rel=1e-12)
+    assert o.get(F.EPS)[ng, ng + 1, ng + 3] == pytest.approx(us ** 3 / (kappa * dz1), rel=1e-12)
+
+
+def test_ke_shear_produces_turbulence(oracle_mod):
+    """The nonlinear production (src/nhwave.F:10139-10274): a sheared current
+    U = 2 sigma keeps more tke above the bed level than still water from the
+    same seeds, for every production form (PRODTYPE 1, 2, 3) and RNG."""
+    from nhwave_gb300 import fields as F
+    ng, K = F.NG, 6
+    for prod, rng in ((3, 0), (2, 0), (1, 1)):
+        kept = []
+        for shear in (None, lambda s: 2.0 * s):
+            o = _ke_channel(oracle_mod, 1e-4, 1e-5, shear, prod_type=prod, rng=rng)
+            for _ in range(10):
+                assert o.step() == 0
+            kept.append(o.get(F.TKE)[ng + 1:ng + K, ng + 1, ng + 4].mean())
+        assert kept[1] > 1.05 * kept[0], (prod, rng, kept)
 
 
 def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):

@@ -170,7 +170,10 @@ Zob = 2.e-4
     assert (p.visc, p.schmidt, p.cvs, p.chs, p.viscous_number) == (2e-6, 0.7, 0.003, 0.02, 0.2)
     assert (p.bc_z0, p.bc_y0, p.ibot, p.cd0, p.zob) == (5, 5, 2, 0.004, 2e-4)
     assert P.unsupported_reason(p) is None
-    f.write_text(text.replace("IVTURB = 1", "IVTURB = 10"))
+    f.write_text(text.replace("IVTURB = 1", "IVTURB = 10").replace("IHTURB = 1", "IHTURB = 10") + "PRODTYPE = 2\n")
+    q = P.read_input(str(f))
+    assert (q.ivturb, q.ihturb, q.prod_type) == (10, 10, 2) and P.unsupported_reason(q) is None
+    f.write_text(text.replace("IVTURB = 1", "IVTURB = 20"))
     assert "IVTURB" in P.unsupported_reason(P.read_input(str(f)))
     foc = SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = FOCUSED") + """
 nwave = 12
