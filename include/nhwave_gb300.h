@@ -119,7 +119,10 @@ typedef struct nhw_params {
   int32_t hllc;                            /* HLLC: 1 HLLC face fluxes, 0 HLL          */
   int32_t viscous_flow;                    /* VISCOUS_FLOW: 1 needs IVTURB = IHTURB = 1
                                               (constant eddy viscosities)             */
-  int32_t barotropic;                      /* BAROTROPIC (must be 1)                  */
+  int32_t barotropic;                      /* BAROTROPIC; 0 runs the same path: the
+                                              density is Rho0 everywhere (no salinity,
+                                              temperature, sediment or bubbles), so the
+                                              baroclinic gradient is zero            */
   int32_t itmax; double tol;               /* ITMAX TOL                               */
   int32_t bc_x0, bc_xn, bc_y0, bc_yn;      /* BC_X0 BC_Xn BC_Y0 BC_Yn: 1 free-slip wall,
                                               2 no-slip wall, 5 wall friction; BC_X0 = 3

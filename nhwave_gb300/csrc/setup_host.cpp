@@ -29,7 +29,11 @@ int check_params(const nhw_params& p) {
   // the ghosted face arrays index cells with 32-bit integers (and neq, the
   // unknowns of the Poisson system, is an int)
   if ((long long)(p.Mglob + 5) * (p.Nglob + 5) * (p.Kglob + 5) >= (1LL << 31)) return NHW_ERR_UNSUPPORTED;
-  if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
+  // BAROTROPIC = F adds baropg_z's baroclinic pressure gradient (src/nhwave.F:
+  // 573, 13038-13179).  Without salinity, temperature, sediment or bubbles the
+  // density stays Rho0 (src/initialize.F:2561), Rho - Rho0 is zero, and so are
+  // DRhoX and DRhoY (signed zeros, which leave R2 and R3 unchanged): the flag
+  // runs the same path.
   // viscous flow: IVTURB 1 constant, 2 subgrid, 10 the 3-D k-epsilon model;
   // IHTURB 1, 2 or >= 10 (CmuHt = CmuVt).  The 2-D k-epsilon (3) and the LES
   // closures (20, 30) are not built

@@ -291,8 +291,6 @@ def unsupported_reason(p: NhwParams) -> str | None:
         return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (constant viscosities (1), the subgrid "
                 "models (2) and the 3-D k-epsilon model (10) are on the GPU path; the 2-D k-epsilon (3) and the "
                 "LES closures (20, 30) are not)")
-    if not p.barotropic:
-        return "BAROTROPIC=F (baroclinic terms are outside the GPU path)"
     if p.wavemaker not in (WM_NONE,) + WM_INT + WM_LEF + WM_EAST:
         return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, INT_CON, INT_JON, INT_TMA, INT_SPC, INT_IRR, LEF_LIN, "
                 "LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, LEF_TMA, LEF_SPC, WAV_CUR, FOCUSED, RIG_LIN and "

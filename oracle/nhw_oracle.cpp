@@ -244,7 +244,9 @@ struct Model {
   int create(const nhw_params& q) {
     p = q;
     if (p.Mglob < 1 || p.Nglob < 1 || p.Kglob < 1 || !(p.dx > 0) || !(p.dy > 0)) return NHW_ERR_ARG;
-    if (!p.barotropic) return NHW_ERR_UNSUPPORTED;
+    // BAROTROPIC = F: baropg_z (src/nhwave.F:13038-13179) of the uniform
+    // density Rho0 (no salinity, temperature, sediment or bubbles) gives
+    // DRhoX = DRhoY = 0, so the flag runs the same path
     // IVTURB 1, 2, 10 (k-epsilon) and IHTURB 1, 2, >= 10 (CmuHt = CmuVt)
     if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;

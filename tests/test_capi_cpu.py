@@ -43,8 +43,7 @@ def test_status_strings(gpu_lib):
     assert "DT_MIN" in lib.status_string(lib.ERR_DT_MIN)
 
 
-@pytest.mark.parametrize("field,value", [("barotropic", 0),
-                                         ("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 3), ("Kglob", 65),
+@pytest.mark.parametrize("field,value", [("bc_x0", 3), ("bc_xn", 3), ("bc_yn", 6), ("bc_z0", 3), ("Kglob", 65),
                                          ("wavemaker", -1)])
 def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     from nhwave_gb300 import default_params, lib

@@ -201,3 +201,20 @@ def test_smoother_timing_leaves_the_run_unchanged(precision, gpu_lib):
     assert ex.value.status == lib.ERR_STATE
     for s in (a, b, h):
         s.close()
+
+
+@pytest.mark.parametrize("name", ["tiny_c2", "tiny_ke"])
+def test_baroclinic_flag_runs_the_same_path(name, gpu_lib):
+    """BAROTROPIC = F adds baropg_z's gradient of Rho - Rho0 (src/nhwave.F:
+    573, 13038-13179), which is zero for the uniform density of a run without
+    salinity, temperature, sediment or bubbles: the run equals BAROTROPIC = T
+    bit for bit."""
+    from nhwave_gb300 import fields as F
+    a = _scen(name, 0)
+    b = _scen(name, 0, barotropic=0)
+    for _ in range(3):
+        a.step()
+        b.step()
+    for f in FIELDS:
+        fid = getattr(F, f)
+        assert np.array_equal(a.get(fid), b.get(fid)), f
