@@ -1443,7 +1443,10 @@ struct OpTurbV {
       }
       cv[0] = cv[S.sz];
       cv[S.sz * (S.Kloc - 1)] = cv[S.sz * (S.Kloc - 2)];
-    }   // IVTURB = 10: the k-epsilon kernels set CmuVt before this one
+    }   // IVTURB = 10 and 20: the k-epsilon / LES kernels set CmuVt before this one
+    if (S.ivturb == 20 && S.les_int && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys &&
+        S.yc[j] <= S.wm_yn)   // no turbulence in an INT_ maker's source region
+      for (int k = 0; k < S.Kloc; ++k) cv[S.sz * k] = (T)0;
     if (S.ihturb == 1)
       for (int k = 0; k < S.Kloc; ++k) S.CmuHt[q + S.sz * k] = (T)S.v_chs;
     else if (S.ihturb >= 10)   // the 3-D model's length scales in every direction
@@ -1981,6 +1984,108 @@ struct OpKeFinal {
         S.DEps[o] = (T)(Dq * kEpsMin);
         S.CmuVt[o] = (T)S.v_cmut0;
       }
+  }
+};
+
+// =========================================================================
+//   Smagorinsky LES closure, IVTURB = 20 (les_3D, src/nhwave.F:8545-8729)
+// =========================================================================
+// CmuVt = (Cvs Delta)^2 sqrt(2 SijSij), Delta = (dx dy dsig D)^(1/3), in wet
+// cells deeper than 0.02 m (others keep their value); the bed's wall
+// function; mirrors; no eddy viscosity at the first column of a LEF_ maker
+// or (in OpTurbV) in an INT_ maker's source region.  pow, log and exp are
+// CUDA's, whose last bit may differ from the host libm's.  The smooth-wall
+// iteration stops after kLesIter steps (the reference iterates until it
+// converges).
+constexpr int kLesIter = 200;
+struct OpLesCell {
+  static constexpr const char* kName = "les_cells";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    const double Dq = S.D[q];
+    if (!(S.Mask9[q] == 1 && Dq > (double)0.02f)) return;
+    double sx = 0.0, sy = 0.0;   // DelxSc, DelySc of the last sigma_transform
+    if (S.sc->sig_set) {
+      sx = (1.0 - S.sigc[k]) / S.scD[q] * S.scHx[q] - S.sigc[k] / S.scD[q] * S.scEx[q];
+      sy = (1.0 - S.sigc[k]) / S.scD[q] * S.scHy[q] - S.sigc[k] / S.scD[q] * S.scEy[q];
+    }
+    auto U = [&](long long x) { return (double)S.U[x]; };
+    auto V = [&](long long x) { return (double)S.V[x]; };
+    auto W = [&](long long x) { return (double)S.W[x]; };
+    const long long up = o + S.sz, dn = o - S.sz, e = o + 1, w = o - 1, n = o + S.sy, s = o - S.sy;
+    const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+    const double dUs = (U(up) - U(dn)) / ds, dVs = (V(up) - V(dn)) / ds, dWs = (W(up) - W(dn)) / ds;
+    const double S11 = (U(e) - U(w)) / (2.0 * S.dx) + dUs * sx;
+    const double S22 = (V(n) - V(s)) / (2.0 * S.dy) + dVs * sy;
+    const double S33 = 1.0 / Dq * (W(up) - W(dn)) / ds;
+    const double S12 = 0.5 * ((U(n) - U(s)) / (2.0 * S.dy) + dUs * sy + (V(e) - V(w)) / (2.0 * S.dx) + dVs * sx);
+    const double S13 = 0.5 * (dUs / Dq + (W(e) - W(w)) / (2.0 * S.dx) + dWs * sx);
+    const double S23 = 0.5 * (dVs / Dq + (W(n) - W(s)) / (2.0 * S.dy) + dWs * sy);
+    const double SijSij = S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23);
+    const double Filter = pow(S.dx * S.dy * S.dsig[k] * Dq, (double)(1.0f / 3.0f));
+    const double cf = S.v_cvs * Filter;
+    S.CmuVt[o] = (T)(cf * cf * sqrt(2.0 * SijSij));
+  }
+};
+// the bed's wall function and the bed / surface ghosts of one interior column
+struct OpLesColumn {
+  static constexpr const char* kName = "les_bed";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j), ob = i3(S, i, j, S.KB);
+    const double kap = (double)0.41f, cmu = S.v_cmu;
+    const double u = (double)S.U[ob], v = (double)S.V[ob];
+    const double Umag = sqrt(u * u + v * v);
+    double cb;
+    if (Umag < (double)1.e-6f) {
+      cb = cmu;
+    } else {
+      const double Zdis = 0.5 * S.dsig[S.KB] * S.D[q];
+      double FricU;
+      if (S.zob >= (double)0.1f) {
+        FricU = Umag / ((double)(1.0f / 0.41f) * log(30.0 * Zdis / S.zob));
+      } else {
+        double X0 = (double)0.05f, Xn = X0;
+        const double Xa = log(9.0 * Umag * Zdis / cmu);
+        for (int it = 0; it < kLesIter; ++it) {
+          Xn = X0 + (kap - X0 * (Xa + log(X0))) / (1.0 + kap / X0);
+          if (!(fabs((Xn - X0) / X0) > (double)1.e-8f && Xn > 0.0)) break;
+          X0 = Xn;
+        }
+        FricU = Xn * Umag;
+      }
+      const double e = 1.0 - exp(-Zdis * FricU / cmu / 19.0);
+      cb = kap * Zdis * FricU * (e * e);
+    }
+    T* c = S.CmuVt;
+    c[ob] = (T)cb;
+    for (int g = 1; g <= NG; ++g) {
+      c[ob - S.sz * g] = c[ob + S.sz * (g - 1)];
+      c[i3(S, i, j, S.KE + g)] = c[i3(S, i, j, S.KE - g + 1)];
+    }
+  }
+};
+// the side mirrors: y = 0 the west and east sides (interior rows and
+// levels; the west first zeroes the first column of a LEF_ maker), y = 1
+// the south and north sides (interior columns and levels), launched after,
+// as the reference's loops run
+struct OpLesSides {
+  static constexpr const char* kName = "les_sides";
+  int y;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    T* c = S.CmuVt;
+    if (!y) {
+      const int j = S.JB + t % S.N, k = S.KB + t / S.N;
+      if (S.les_lef) c[i3(S, S.IB, j, k)] = (T)0;
+      for (int g = 1; g <= NG; ++g) c[i3(S, S.IB - g, j, k)] = c[i3(S, S.IB + g - 1, j, k)];
+      for (int g = 1; g <= NG; ++g) c[i3(S, S.IE + g, j, k)] = c[i3(S, S.IE - g + 1, j, k)];
+    } else {
+      const int i = S.IB + t % S.M, k = S.KB + t / S.M;
+      for (int g = 1; g <= NG; ++g) c[i3(S, i, S.JB - g, k)] = c[i3(S, i, S.JB + g - 1, k)];
+      for (int g = 1; g <= NG; ++g) c[i3(S, i, S.JE + g, k)] = c[i3(S, i, S.JE - g + 1, k)];
+    }
   }
 };
 

@@ -265,6 +265,10 @@ class Solver final : public SolverBase {
                     w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR || w == NHW_WM_LEF_LIN ||
                     w == NHW_WM_LEF_SOL || w == NHW_WM_LEF_STK || w == NHW_WM_LEF_CON || w == NHW_WM_LEF_TID ||
                     w == NHW_WM_LEF_JON || w == NHW_WM_LEF_TMA || w == NHW_WM_LEF_SPC || w == NHW_WM_FOCUSED) ? 1 : 0;
+      S.les_lef = ((w >= NHW_WM_LEF_LIN && w <= NHW_WM_LEF_CON) || w == NHW_WM_LEF_TID || w == NHW_WM_LEF_JON ||
+                   w == NHW_WM_LEF_TMA || w == NHW_WM_LEF_SPC) ? 1 : 0;
+      S.les_int = (w == NHW_WM_INT_LIN || w == NHW_WM_INT_SOL || w == NHW_WM_INT_CON || w == NHW_WM_INT_JON ||
+                   w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR) ? 1 : 0;
     }
     S.wavemaker = p.wavemaker;
     S.wm_amp = p.amp_wave; S.wm_xw = p.xsource_west; S.wm_xe = p.xsource_east;
@@ -1278,6 +1282,12 @@ class Solver final : public SolverBase {
       box(OpKeSidesX{}, S.N * S.Kloc, 1, 1, 0, 0, 0);
       box(OpKeSidesY{}, S.Mloc * S.Kloc, 1, 1, 0, 0, 0);
       allcols(OpKeFinal{});
+    }
+    if (S.ivturb == 20) {
+      cells(OpLesCell{});
+      incols(OpLesColumn{});
+      box(OpLesSides{0}, S.N * S.K, 1, 1, 0, 0, 0);
+      box(OpLesSides{1}, S.M * S.K, 1, 1, 0, 0, 0);
     }
     allcols(OpTurbV{});
     if (S.ihturb == 2) {

@@ -100,6 +100,9 @@ struct Dev {
   // ke_quiet: an INT_, LEF_ or FOCUSED maker, whose source region is kept
   // free of turbulence
   int ke_rng, ke_prod, ke_quiet;
+  // LES closure (IVTURB = 20): a LEF_ maker (first column kept laminar), an
+  // INT_ maker (source region kept laminar)
+  int les_lef, les_int;
   double ke_dmin;
   // bed (BC_Z0): 1 free slip, 2 no slip, 5 friction law with Ibot 1 (Cd0) or 2 (Zob)
   int bc_z0, ibot;

@@ -335,6 +335,10 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=10, ihturb=10, rng=1, prod_type=2, bc_z0=5, bc_y0=5,
                        bc_yn=5, bc_xn=5, ibot=2, zob=1e-3), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_les":
+        # the small submerged bar with the Smagorinsky LES closure (IVTURB = 20, CmuHt = CmuVt)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=20, ihturb=20, cvs=0.1), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_fric_log":
         # the inviscid small bar with the friction law on the bed and the side walls, from a
         # roughness height (Ibot = 2)

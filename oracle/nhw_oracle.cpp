@@ -27,7 +27,8 @@
 //   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
 //   diffusion                  src/nhwave.F:6785-7141
 //   trig                       src/nhwave.F:13182-13224
-//   eval_turb (IVTURB 1, 2, 10; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
+//   eval_turb (IVTURB 1, 2, 10, 20; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
+//   les_3D                     src/nhwave.F:8545-8729
 //   kepsilon_3D                src/nhwave.F:10030-11114, adv_scalar_hlpa 7604-7806,
 //                              hlpa 7809-7847, flux_scalar_bc 7850-7986
 //   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
@@ -248,7 +249,8 @@ struct Model {
     // density Rho0 (no salinity, temperature, sediment or bubbles) gives
     // DRhoX = DRhoY = 0, so the flag runs the same path
     // IVTURB 1, 2, 10 (k-epsilon) and IHTURB 1, 2, >= 10 (CmuHt = CmuVt)
-    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10)) return NHW_ERR_UNSUPPORTED;
+    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10 || p.ivturb == 20))
+      return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
     for (int b : {p.bc_y0, p.bc_yn})
@@ -3160,6 +3162,95 @@ struct Model {
            w == NHW_WM_LEF_JON || w == NHW_WM_LEF_TMA || w == NHW_WM_LEF_SPC || w == NHW_WM_FOCUSED;
   }
 
+  // les_3D (src/nhwave.F:8545-8729): the Smagorinsky closure of IVTURB = 20.
+  // CmuVt = (Cvs Delta)^2 sqrt(2 SijSij) with the filter width Delta =
+  // (dx dy dsig D)^(1/3) in wet cells of depth above 0.02 m (others keep
+  // their value); at the bed a wall function: log law of a rough wall
+  // (Zob >= 0.1) or the smooth wall's friction velocity from a fixed-point
+  // iteration, damped by van Driest's (1 - exp(-z+/19))^2; mirrors into the
+  // ghosts; no eddy viscosity at the first column of a LEF_ maker or in an
+  // INT_ maker's source region.  The reference iterates the smooth-wall law
+  // until it converges; the iteration stops after kLesIter steps here.  Eps,
+  // an output of the LES closure, is not formed.
+  static constexpr int kLesIter = 200;
+  void les_3D() {
+    const double Dmin = (double)0.02f, Cvs = p.cvs;
+    auto ds = [&](int k) { return sigc(k + 1) - sigc(k - 1); };
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          if (!(Mask9(i, j) == 1 && D(i, j) > Dmin)) continue;
+          const double dUs = (U(i, j, k + 1) - U(i, j, k - 1)) / ds(k), dVs = (V(i, j, k + 1) - V(i, j, k - 1)) / ds(k);
+          const double dWs = (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+          const double S11 = (U(i + 1, j, k) - U(i - 1, j, k)) / (2.0 * dx) + dUs * DelxSc(i, j, k);
+          const double S22 = (V(i, j + 1, k) - V(i, j - 1, k)) / (2.0 * dy) + dVs * DelySc(i, j, k);
+          const double S33 = 1.0 / D(i, j) * (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+          const double S12 = 0.5 * ((U(i, j + 1, k) - U(i, j - 1, k)) / (2.0 * dy) + dUs * DelySc(i, j, k) +
+                                    (V(i + 1, j, k) - V(i - 1, j, k)) / (2.0 * dx) + dVs * DelxSc(i, j, k));
+          const double S13 = 0.5 * (dUs / D(i, j) + (W(i + 1, j, k) - W(i - 1, j, k)) / (2.0 * dx) + dWs * DelxSc(i, j, k));
+          const double S23 = 0.5 * (dVs / D(i, j) + (W(i, j + 1, k) - W(i, j - 1, k)) / (2.0 * dy) + dWs * DelySc(i, j, k));
+          const double SijSij = S11 * S11 + S22 * S22 + S33 * S33 + 2.0 * (S12 * S12 + S13 * S13 + S23 * S23);
+          const double Filter = std::pow(dx * dy * dsig(k) * D(i, j), (double)(1.0f / 3.0f));
+          const double cf = Cvs * Filter;
+          CmuVt(i, j, k) = cf * cf * std::sqrt(2.0 * SijSij);
+        }
+    const double kap = (double)0.41f;
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Umag = std::sqrt(U(i, j, Kbeg) * U(i, j, Kbeg) + V(i, j, Kbeg) * V(i, j, Kbeg));
+        if (Umag < (double)1.e-6f) {
+          CmuVt(i, j, Kbeg) = Cmu;
+        } else {
+          const double Zdis = 0.5 * dsig(Kbeg) * D(i, j);
+          double FricU;
+          if (p.zob >= (double)0.1f) {
+            FricU = Umag / ((double)(1.0f / 0.41f) * std::log(30.0 * Zdis / p.zob));   // 1.0/0.41 folded in default real
+          } else {
+            double X0 = (double)0.05f, Xn = X0;
+            const double Xa = std::log(9.0 * Umag * Zdis / Cmu);
+            for (int it = 0; it < kLesIter; ++it) {
+              Xn = X0 + (kap - X0 * (Xa + std::log(X0))) / (1.0 + kap / X0);
+              if (!(std::fabs((Xn - X0) / X0) > (double)1.e-8f && Xn > 0.0)) break;
+              X0 = Xn;
+            }
+            FricU = Xn * Umag;
+          }
+          const double e = 1.0 - std::exp(-Zdis * FricU / Cmu / 19.0);
+          CmuVt(i, j, Kbeg) = kap * Zdis * FricU * (e * e);
+        }
+        for (int k = 1; k <= Nghost; ++k) CmuVt(i, j, Kbeg - k) = CmuVt(i, j, Kbeg + k - 1);
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) CmuVt(i, j, Kend + k) = CmuVt(i, j, Kend - k + 1);
+    const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON) || p.wavemaker == NHW_WM_LEF_TID ||
+                     p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        if (lef) CmuVt(Ibeg, j, k) = Zero;   // no turbulence at the wave generation region
+        for (int i = 1; i <= Nghost; ++i) CmuVt(Ibeg - i, j, k) = CmuVt(Ibeg + i - 1, j, k);
+      }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) CmuVt(Iend + i, j, k) = CmuVt(Iend - i + 1, j, k);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) CmuVt(i, Jbeg - j, k) = CmuVt(i, Jbeg + j - 1, k);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) CmuVt(i, Jend + j, k) = CmuVt(i, Jend - j + 1, k);
+    const int w = p.wavemaker;
+    const bool int_maker = w == NHW_WM_INT_LIN || w == NHW_WM_INT_SOL || w == NHW_WM_INT_CON || w == NHW_WM_INT_JON ||
+                           w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR;
+    if (int_maker)   // no turbulence in the internal wavemaker region
+      for (int k = 1; k <= Kloc; ++k)
+        for (int j = 1; j <= Nloc; ++j)
+          for (int i = 1; i <= Mloc; ++i)
+            if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+                yc(j) <= p.ysource_nrth)
+              CmuVt(i, j, k) = Zero;
+  }
+
   // eval_turb (src/nhwave.F:6544-6782), called after sponge_damping.
   // Vertical: IVTURB 1 CmuVt = Cvs; 2 the subgrid model CmuVt = Cvs D
   // dsig^2 |d(U,V)/dsigma| on every level but the outermost ghosts, which
@@ -3174,6 +3265,8 @@ struct Model {
       CmuVt.fill(p.cvs);
     } else if (p.ivturb == 10) {
       kepsilon_3D(istep);
+    } else if (p.ivturb == 20) {
+      les_3D();
     } else {
       for (int i = 1; i <= Mloc; ++i)
         for (int j = 1; j <= Nloc; ++j) {

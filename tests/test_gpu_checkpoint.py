@@ -32,7 +32,7 @@ def _scen(name, precision, **attrs):
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,krylov", [("tiny_c2", 0), ("tiny_c3", 0), ("tiny_c4", 0), ("tiny_flume_lin", 0),
                                          ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0),
-                                         ("tiny_visc_sgs", 0), ("tiny_ke_rng", 0)])
+                                         ("tiny_visc_sgs", 0), ("tiny_ke_rng", 0), ("tiny_les", 0)])
 def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     """krylov = 2: the GMRES solver, whose basis lies behind the checkpointed
     prefix and is rebuilt by every solve.  tiny_open: the Orlanski boundary's

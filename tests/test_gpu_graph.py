@@ -49,7 +49,8 @@ def _routines(s):
 @pytest.mark.parametrize("name", ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4", "tiny_flume_lin", "tiny_flume_sol",
                                   "tiny_flume_stk", "tiny_flume_con", "tiny_flume_cur", "tiny_flume_foc", "tiny_flume_tid", "tiny_open",
                                   "tiny_flume_open", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon",
-                                  "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng"])
+                                  "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng",
+                                  "tiny_les"])
 def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, hllc=hllc)

@@ -504,6 +504,40 @@ def test_ke_shear_produces_turbulence(oracle_mod):
         assert kept[1] > 1.05 * kept[0], (prod, rng, kept)
 
 
+def test_les_smagorinsky_viscosity_and_smooth_wall_law(oracle_mod):
+    """les_3D (src/nhwave.F:8545-8729) on a shear U = a sigma in a flat 1 m
+    deep channel before the first sigma_transform: the only strain rate is
+    S13 = a / (2 D), so CmuVt = (Cvs Delta)^2 a / D with Delta = (dx dy
+    dsig D)^(1/3) on the levels whose neighbours are in the water, away
+    from the end walls.  At the
+    bed the smooth-wall law U/u* = ln(9 z u*/nu) / kappa at z = dsig D / 2
+    gives CmuVt = kappa z u* (1 - exp(-z u*/(19 nu)))^2."""
+    from scipy.optimize import brentq
+    from nhwave_gb300 import default_params, fields as F
+    M, N, K, dx, dy, a, cvs, nu = 12, 3, 6, 0.2, 0.25, 0.2, 0.1, 1e-6
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.01, dt_max=1.0, tol=1e-10, itmax=2000,
+                       viscous_flow=1, visc=nu, cvs=cvs, ivturb=20, ihturb=20, zob=1e-4)
+    sig = (np.arange(K) + 0.5) / K
+    uvw = np.zeros((3, K, N, M))
+    uvw[0] = a * sig[:, None, None]
+    o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
+    o.eval_turb(1)
+    ng = F.NG
+    cv = o.get(F.CMUVT)
+    ds = float(np.float32(1.0) / np.float32(K))
+    delta = (dx * dy * ds * 1.0) ** float(np.float32(1.0) / np.float32(3.0))
+    # away from the end walls, whose mirrored U adds dU/dx
+    inner = (slice(ng + 1, ng + K - 1), slice(ng, ng + N), slice(ng + 1, ng + M - 1))
+    assert cv[inner] == pytest.approx(np.full(cv[inner].shape, (cvs * delta) ** 2 * a), rel=1e-6)
+    kap, z, ub = float(np.float32(0.41)), 0.5 * ds, a * 0.5 / K
+    x = brentq(lambda x: x * (math.log(9.0 * ub * z / nu) + math.log(x)) - kap, 1e-3, 1.0, xtol=1e-15)
+    us = x * ub
+    expect = kap * z * us * (1.0 - math.exp(-z * us / nu / 19.0)) ** 2
+    assert cv[ng, ng:ng + N, ng:ng + M] == pytest.approx(np.full((N, M), expect), rel=1e-6)
+    cols = (slice(ng, ng + N), slice(ng, ng + M))
+    assert np.array_equal(cv[ng - 1][cols], cv[ng][cols]) and np.array_equal(o.get(F.CMUHT), cv)
+
+
 def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):
     """VISCOUS_FLOW = T with zero viscosities: the tridiagonal systems are the
     identity and the explicit terms vanish, so the run equals the inviscid
