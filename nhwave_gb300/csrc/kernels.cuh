@@ -1584,6 +1584,58 @@ __device__ __forceinline__ double ke_hlpa(double Uw, double Fww, double Fw, doub
   return h;
 }
 
+// adv_scalar_hlpa with flux_scalar_bc (src/nhwave.F:7604-7806, 7850-7986) at
+// one interior cell: minus the divergence of the HLPA fluxes of Phi by Ex,
+// Ey and Omega (the boundary scalar of a BC_X0 = 3 side is zero; faces of
+// dry cells carry none) plus the horizontal diffusion with Cmu + CmuHt /
+// SchtH; zero in a dry cell
+template <class T>
+__device__ double ke_r5(const Dev<T>& S, int i, int j, int k, const T* Phi, double SchtH) {
+  if (S.Mask[i2(S, i, j)] == 0) return 0.0;
+  auto scx = [&](int f) -> double {
+    if ((f <= S.IE && S.Mask[i2(S, f, j)] == 0) || (f - 1 >= S.IB && S.Mask[i2(S, f - 1, j)] == 0)) return 0.0;
+    if (f == S.IE + 1) return 0.0;
+    const long long o = i3(S, f, j, k);
+    const double u = (double)S.Ex[o];
+    if (f == S.IB) {
+      if (S.bc_x0 == 1 || S.bc_x0 == 2 || S.bc_x0 == 5) return 0.0;
+      if (S.bc_x0 == 3) return u * 0.0;
+    }
+    return u * ke_hlpa(u, (double)Phi[o - 2], (double)Phi[o - 1], (double)Phi[o], (double)Phi[o + 1]);
+  };
+  auto scy = [&](int f) -> double {
+    if ((f <= S.JE && S.Mask[i2(S, i, f)] == 0) || (f - 1 >= S.JB && S.Mask[i2(S, i, f - 1)] == 0)) return 0.0;
+    if (f == S.JB && (S.bc_y0 == 1 || S.bc_y0 == 2 || S.bc_y0 == 5)) return 0.0;
+    if (f == S.JE + 1 && (S.bc_yn == 1 || S.bc_yn == 2 || S.bc_yn == 5)) return 0.0;
+    const long long o = i3(S, i, f, k);
+    const long long y = S.sy;
+    const double v = (double)S.Ey[o];
+    return v * ke_hlpa(v, (double)Phi[o - 2 * y], (double)Phi[o - y], (double)Phi[o], (double)Phi[o + y]);
+  };
+  auto scz = [&](int f) -> double {
+    if (f == S.KB || f == S.KE + 1) return 0.0;
+    const long long o = i3(S, i, j, f);
+    const long long z = S.sz;
+    const double w = (double)S.Omega[o];
+    return w * ke_hlpa(w, (double)Phi[o - 2 * z], (double)Phi[o - z], (double)Phi[o], (double)Phi[o + z]);
+  };
+  const double cmu = S.v_cmu;
+  auto nu = [&](double ha, double hb) { return 0.5 * (cmu + cmu) + 0.5 * (ha + hb) / SchtH; };
+  auto H = [&](int ii, int jj) { return (double)S.CmuHt[i3(S, ii, jj, k)]; };
+  auto Dq = [&](int ii, int jj) { return S.D[i2(S, ii, jj)]; };
+  auto Ph = [&](int ii, int jj) { return (double)Phi[i3(S, ii, jj, k)]; };
+  const double Sdx = 0.5 *
+                     (nu(H(i + 1, j), H(i, j)) * (Dq(i + 1, j) + Dq(i, j)) * (Ph(i + 1, j) - Ph(i, j)) -
+                      nu(H(i, j), H(i - 1, j)) * (Dq(i, j) + Dq(i - 1, j)) * (Ph(i, j) - Ph(i - 1, j))) /
+                     (S.dx * S.dx);
+  const double Sdy = 0.5 *
+                     (nu(H(i, j + 1), H(i, j)) * (Dq(i, j + 1) + Dq(i, j)) * (Ph(i, j + 1) - Ph(i, j)) -
+                      nu(H(i, j), H(i, j - 1)) * (Dq(i, j) + Dq(i, j - 1)) * (Ph(i, j) - Ph(i, j - 1))) /
+                     (S.dy * S.dy);
+  return -(1.0 / S.dx * (scx(i + 1) - scx(i))) - 1.0 / S.dy * (scy(j + 1) - scy(j)) -
+         1.0 / S.dsig[k] * (scz(k + 1) - scz(k)) + Sdx + Sdy;
+}
+
 // shear production of the nonlinear model (ke_model = 2, src/nhwave.F:
 // 10139-10274): Reynolds stresses from the velocity gradient G, contracted
 // with G per PRODTYPE (1 vertical shear of U, V; 2 vertical shear; else 3-D)
@@ -1688,51 +1740,6 @@ struct OpKeColumn {
       }
       prod[k - KB] = P;
     }
-    // adv_scalar_hlpa with flux_scalar_bc (src/nhwave.F:7604-7806, 7850-7986)
-    auto scx = [&](const T* Phi, int f, int k) -> double {
-      if ((f <= S.IE && S.Mask[i2(S, f, j)] == 0) || (f - 1 >= S.IB && S.Mask[i2(S, f - 1, j)] == 0)) return 0.0;
-      if (f == S.IE + 1) return 0.0;
-      const long long o = i3(S, f, j, k);
-      const double u = (double)S.Ex[o];
-      if (f == S.IB) {
-        if (S.bc_x0 == 1 || S.bc_x0 == 2 || S.bc_x0 == 5) return 0.0;
-        if (S.bc_x0 == 3) return u * 0.0;
-      }
-      return u * ke_hlpa(u, (double)Phi[o - 2], (double)Phi[o - 1], (double)Phi[o], (double)Phi[o + 1]);
-    };
-    auto scy = [&](const T* Phi, int f, int k) -> double {
-      if ((f <= S.JE && S.Mask[i2(S, i, f)] == 0) || (f - 1 >= S.JB && S.Mask[i2(S, i, f - 1)] == 0)) return 0.0;
-      if (f == S.JB && (S.bc_y0 == 1 || S.bc_y0 == 2 || S.bc_y0 == 5)) return 0.0;
-      if (f == S.JE + 1 && (S.bc_yn == 1 || S.bc_yn == 2 || S.bc_yn == 5)) return 0.0;
-      const long long o = i3(S, i, f, k);
-      const long long y = S.sy;
-      const double v = (double)S.Ey[o];
-      return v * ke_hlpa(v, (double)Phi[o - 2 * y], (double)Phi[o - y], (double)Phi[o], (double)Phi[o + y]);
-    };
-    auto scz = [&](const T* Phi, int f) -> double {
-      if (f == KB || f == KE + 1) return 0.0;
-      const long long o = i3(S, i, j, f);
-      const long long z = S.sz;
-      const double w = (double)S.Omega[o];
-      return w * ke_hlpa(w, (double)Phi[o - 2 * z], (double)Phi[o - z], (double)Phi[o], (double)Phi[o + z]);
-    };
-    auto r5 = [&](const T* Phi, double SchtH, int k) -> double {
-      if (mk == 0) return 0.0;
-      auto nu = [&](double ha, double hb) { return 0.5 * (cmu + cmu) + 0.5 * (ha + hb) / SchtH; };
-      auto H = [&](int ii, int jj) { return (double)S.CmuHt[i3(S, ii, jj, k)]; };
-      auto Dq = [&](int ii, int jj) { return S.D[i2(S, ii, jj)]; };
-      auto Ph = [&](int ii, int jj) { return (double)Phi[i3(S, ii, jj, k)]; };
-      const double Sdx = 0.5 *
-                         (nu(H(i + 1, j), H(i, j)) * (Dq(i + 1, j) + Dq(i, j)) * (Ph(i + 1, j) - Ph(i, j)) -
-                          nu(H(i, j), H(i - 1, j)) * (Dq(i, j) + Dq(i - 1, j)) * (Ph(i, j) - Ph(i - 1, j))) /
-                         (S.dx * S.dx);
-      const double Sdy = 0.5 *
-                         (nu(H(i, j + 1), H(i, j)) * (Dq(i, j + 1) + Dq(i, j)) * (Ph(i, j + 1) - Ph(i, j)) -
-                          nu(H(i, j), H(i, j - 1)) * (Dq(i, j) + Dq(i, j - 1)) * (Ph(i, j) - Ph(i, j - 1))) /
-                         (S.dy * S.dy);
-      return -(1.0 / S.dx * (scx(Phi, i + 1, k) - scx(Phi, i, k))) - 1.0 / S.dy * (scy(Phi, j + 1, k) - scy(Phi, j, k)) -
-             1.0 / dsig[k] * (scz(Phi, k + 1) - scz(Phi, k)) + Sdx + Sdy;
-    };
     double A[kMaxK], B[kMaxK], C[kMaxK], X[kMaxK];
     // one equation: eq = 2 epsilon, 1 tke
     auto column = [&](int eq) {
@@ -1757,7 +1764,7 @@ struct OpKeColumn {
                                (L1bot * at(S.CmuVt, k - 1) + L2bot * at(S.CmuVt, k)) / Sch;
         const double nuH_bot = (L1bot * cmu + L2bot * cmu) + (L1bot * cmuR + L2bot * cmuR) +
                                (L1bot * at(S.CmuHt, k - 1) + L2bot * at(S.CmuHt, k)) / Sch;
-        double r = r5(Old, Sch, k);
+        double r = ke_r5(S, i, j, k, Old, Sch);
         if (eq == 2) r = r + c1e * Dc * (prod[m] + c3e * Prod_b) * at(S.Eps, k) / at(S.Tke, k);
         else r = r + Dc * (prod[m] + Prod_b) - at(S.DEps, k);
         if (k == KB) {
@@ -2085,6 +2092,175 @@ struct OpLesSides {
       const int i = S.IB + t % S.M, k = S.KB + t / S.M;
       for (int g = 1; g <= NG; ++g) c[i3(S, i, S.JB - g, k)] = c[i3(S, i, S.JB + g - 1, k)];
       for (int g = 1; g <= NG; ++g) c[i3(S, i, S.JE + g, k)] = c[i3(S, i, S.JE - g + 1, k)];
+    }
+  }
+};
+
+// =========================================================================
+//   2-D k-epsilon closure, IVTURB = 3 (kepsilon, src/nhwave.F:11117-11524)
+// =========================================================================
+// Production from the vertical shear, CmuVt (U_z^2 + V_z^2); the HLPA
+// residual of kepsilon_3D; plain implicit vertical diffusion; the bed's
+// smooth-wall friction velocity (the bounded iteration of les_3D); mirrors;
+// the floors in the first six columns of a LEF_ maker and in an INT_ maker's
+// source region.  Shallow means D < 0.01 m here.
+constexpr double kKe2Dmin = (double)0.01f;
+struct OpKe2Column {
+  static constexpr const char* kName = "kepsilon2d_column";
+  static constexpr int kMaxK = 64;   // Kglob <= 64 (nhw_create)
+  int istep;                         // 0-based stage
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const double Dc = S.D[q], Dmin = kKe2Dmin, dt = S.sc->dt, cmu = S.v_cmu;
+    const int mk = S.Mask[q];
+    const double c1e = (double)1.44f, c2e = (double)1.92f, c3e = 0.0, cmiu = (double)0.09f;
+    const double Sche = (double)1.3f, Schk = 1.0, Prod_b = 0.0;
+    const bool rng = S.ke_rng != 0;   // adv_scalar_hlpa's Schmidt numbers follow RNG
+    const int KB = S.KB, KE = S.KE, n = KE - KB + 1;
+    const double* dsig = S.dsig;
+    auto at = [&](const T* a, int kk) -> double { return (double)a[i3(S, i, j, kk)]; };
+    double prod[kMaxK];
+    for (int k = KB; k <= KE; ++k) {
+      double P = 0.0;
+      if (Dc >= Dmin && mk == 1) {
+        const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+        const double uz = (at(S.U, k + 1) - at(S.U, k - 1)) / ds / Dc;
+        const double vz = (at(S.V, k + 1) - at(S.V, k - 1)) / ds / Dc;
+        P = at(S.CmuVt, k) * (uz * uz + vz * vz);
+      }
+      prod[k - KB] = P;
+    }
+    double A[kMaxK], B[kMaxK], C[kMaxK], X[kMaxK];
+    auto column = [&](int eq) {
+      const T* Old = eq == 2 ? S.Eps : S.Tke;
+      T* Dv = eq == 2 ? S.DEps : S.DTke;
+      const double Sch = eq == 2 ? Sche : Schk;
+      const double SchtH = rng ? (double)0.72f : (eq == 2 ? (double)1.3f : 1.0);
+      for (int k = KB; k <= KE; ++k) {
+        const int m = k - KB;
+        double r = ke_r5(S, i, j, k, Old, SchtH);
+        if (eq == 2) r = r + c1e * Dc * (prod[m] + c3e * Prod_b) * at(S.Eps, k) / at(S.Tke, k);
+        else r = r + Dc * (prod[m] + Prod_b) - at(S.DEps, k);
+        A[m] = k == KB ? 0.0
+                       : -dt / (Dc * Dc) * (0.5 * (cmu + cmu) + 0.5 * (at(S.CmuVt, k - 1) + at(S.CmuVt, k)) / Sch) /
+                             (0.5 * dsig[k] * (dsig[k] + dsig[k - 1]));
+        C[m] = k == KE ? 0.0
+                       : -dt / (Dc * Dc) * (0.5 * (cmu + cmu) + 0.5 * (at(S.CmuVt, k) + at(S.CmuVt, k + 1)) / Sch) /
+                             (0.5 * dsig[k] * (dsig[k] + dsig[k + 1]));
+        B[m] = 1.0 - A[m] - C[m];
+        if (eq == 2) B[m] = B[m] + dt * c2e * at(S.Eps, k) / at(S.Tke, k);
+        X[m] = at(Dv, k) + dt * r;
+      }
+      for (int m = 1; m < n; ++m) {   // trig (src/nhwave.F:13182-13224)
+        const double coeff = A[m] / B[m - 1];
+        B[m] = B[m] - coeff * C[m - 1];
+        X[m] = X[m] - coeff * X[m - 1];
+      }
+      X[n - 1] = X[n - 1] / B[n - 1];
+      for (int m = n - 2; m >= 0; --m) X[m] = (X[m] - C[m] * X[m + 1]) / B[m];
+      for (int k = KB; k <= KE; ++k) Dv[i3(S, i, j, k)] = (T)X[k - KB];
+    };
+    auto rk = [&](T* Dv, const T* Dv0, double vmin) {
+      if (!(Dc >= Dmin && mk == 1)) return;
+      const double al = S.alpha[istep], be = S.beta[istep];
+      for (int k = KB; k <= KE; ++k) {
+        const long long o = i3(S, i, j, k);
+        const double v = al * (double)Dv0[o] + be * (double)Dv[o];
+        Dv[o] = (T)dmax_(v, Dc * vmin);
+      }
+    };
+    const bool solve = !(Dc < Dmin && mk == 0);
+    if (solve) column(2);
+    rk(S.DEps, S.DEps0, kEpsMin);
+    if (solve) column(1);
+    rk(S.DTke, S.DTke0, kTkeMin);
+    // bed: smooth-wall law (columns with a bed velocity, deep enough and wet)
+    const double ub = at(S.U, KB), vb = at(S.V, KB);
+    const double Umag = sqrt(ub * ub + vb * vb);
+    if (!(Umag < (double)1.e-6f || Dc < Dmin || mk == 0)) {
+      const double kap = (double)0.41f;
+      const double Zdis = 0.5 * dsig[KB] * Dc;
+      double X0 = (double)0.05f, Xn = X0;
+      const double Xa = log(9.0 * Umag * Zdis / cmu);
+      for (int it = 0; it < kLesIter; ++it) {
+        Xn = X0 + (kap - X0 * (Xa + log(X0))) / (1.0 + kap / X0);
+        if (!(fabs((Xn - X0) / X0) > (double)1.e-8f && Xn > 0.0)) break;
+        X0 = Xn;
+      }
+      const double FricU = Xn * Umag;
+      const long long ob = i3(S, i, j, KB);
+      S.DTke[ob] = (T)(Dc * (FricU * FricU / sqrt(cmiu)));
+      S.DEps[ob] = (T)(Dc * (FricU * FricU * FricU / (kKappa * Zdis)));
+      for (int g = 1; g <= NG; ++g) {
+        S.DTke[ob - S.sz * g] = S.DTke[ob + S.sz * (g - 1)];
+        S.DEps[ob - S.sz * g] = S.DEps[ob + S.sz * (g - 1)];
+      }
+    }
+    for (int g = 1; g <= NG; ++g) {   // surface
+      const long long d = i3(S, i, j, KE + g), s = i3(S, i, j, KE - g + 1);
+      S.DTke[d] = S.DTke[s];
+      S.DEps[d] = S.DEps[s];
+    }
+  }
+};
+// sides: y = 0 west (after the floors in the first six columns of a LEF_
+// maker) and east, one thread per interior row and level; y = 1 south and
+// north, one thread per interior column and level, launched after
+struct OpKe2Sides {
+  static constexpr const char* kName = "kepsilon2d_sides";
+  int y;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    auto mir = [&](long long d, long long s) {
+      S.DTke[d] = S.DTke[s];
+      S.DEps[d] = S.DEps[s];
+    };
+    if (!y) {
+      const int j = S.JB + t % S.N, k = S.KB + t / S.N;
+      if (S.les_lef)
+        for (int i = S.IB; i <= S.IB + 5 && i < S.Mloc; ++i) {
+          const long long o = i3(S, i, j, k);
+          const double Dq = S.D[i2(S, i, j)];
+          S.Tke[o] = (T)kTkeMin;
+          S.Eps[o] = (T)kEpsMin;
+          S.DTke[o] = (T)(Dq * kTkeMin);
+          S.DEps[o] = (T)(Dq * kEpsMin);
+          S.CmuVt[o] = (T)S.v_cmut0;
+        }
+      for (int g = 1; g <= NG; ++g) mir(i3(S, S.IB - g, j, k), i3(S, S.IB + g - 1, j, k));
+      for (int g = 1; g <= NG; ++g) mir(i3(S, S.IE + g, j, k), i3(S, S.IE - g + 1, j, k));
+    } else {
+      const int i = S.IB + t % S.M, k = S.KB + t / S.M;
+      for (int g = 1; g <= NG; ++g) mir(i3(S, i, S.JB - g, k), i3(S, i, S.JB + g - 1, k));
+      for (int g = 1; g <= NG; ++g) mir(i3(S, i, S.JE + g, k), i3(S, i, S.JE - g + 1, k));
+    }
+  }
+};
+// tke, epsilon and CmuVt = cmiu k^2 / eps in every cell (the floors in
+// shallow or dry columns), then an INT_ maker's source region at the floors
+struct OpKe2Final {
+  static constexpr const char* kName = "kepsilon2d_update";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j) const {
+    const long long q = i2(S, i, j);
+    const double Dq = S.D[q], cmiu = (double)0.09f;
+    const bool wet = Dq >= kKe2Dmin && S.Mask[q] == 1;
+    const bool quiet = S.les_int && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys && S.yc[j] <= S.wm_yn;
+    for (int k = 0; k < S.Kloc; ++k) {
+      const long long o = q + S.sz * k;
+      if (wet && !quiet) {
+        const T tk = (T)((double)S.DTke[o] / Dq), ep = (T)((double)S.DEps[o] / Dq);
+        S.Tke[o] = tk;
+        S.Eps[o] = ep;
+        S.CmuVt[o] = (T)(cmiu * ((double)tk * (double)tk) / (double)ep);
+      } else {
+        S.Tke[o] = (T)kTkeMin;
+        S.Eps[o] = (T)kEpsMin;
+        S.DTke[o] = (T)(Dq * kTkeMin);
+        S.DEps[o] = (T)(Dq * kEpsMin);
+        S.CmuVt[o] = (T)S.v_cmut0;
+      }
     }
   }
 };

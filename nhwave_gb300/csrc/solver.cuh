@@ -329,13 +329,13 @@ class Solver final : public SolverBase {
       for (double** pp : {&S.scD, &S.scEx, &S.scEy, &S.scHx, &S.scHy}) add(pp, sizeof(double) * n2);
       for (T** pp : {&S.CmuVt, &S.CmuHt}) add(pp, sizeof(T) * n3);
     }
-    const bool ke = p.viscous_flow && p.ivturb == 10;
+    const bool ke = p.viscous_flow && (p.ivturb == 10 || p.ivturb == 3);
     if (ke)   // k-epsilon state (checkpointed)
       for (T** pp : {&S.Tke, &S.Eps, &S.DTke, &S.DEps, &S.DTke0, &S.DEps0}) add(pp, sizeof(T) * n3);
     add(&S.P, sizeof(double) * n3);
     if (p.viscous_flow)   // explicit viscous terms of the stage
       for (T** pp : {&S.Dxx, &S.Dxy, &S.Dyx, &S.Dyy, &S.Dzx, &S.Dzy}) add(pp, sizeof(T) * n3);
-    if (ke) {   // slopes the production reads, surface values of the stage
+    if (ke && p.ivturb == 10) {   // slopes the 3-D production reads, surface values of the stage
       for (T** pp : {&S.keDxU, &S.keDyU, &S.keDxV, &S.keDyV, &S.keDxW, &S.keDyW}) add(pp, sizeof(T) * n3);
       for (double** pp : {&S.keTopK, &S.keTopE}) add(pp, sizeof(double) * n2);
     }
@@ -807,7 +807,7 @@ class Solver final : public SolverBase {
       NHW_CU(cudaMemsetAsync(S.CmuVt, 0, sizeof(T) * n3, st));
       NHW_CU(cudaMemsetAsync(S.CmuHt, 0, sizeof(T) * n3, st));
     }
-    if (S.Tke) {   // k-epsilon scratch of a previous set-up (the state is seeded below)
+    if (S.keDxU) {   // k-epsilon scratch of a previous set-up (the state is seeded below)
       T* ks[] = {S.keDxU, S.keDyU, S.keDxV, S.keDyV, S.keDxW, S.keDyW};
       for (T* a : ks) {
         NHW_CU(cudaMemsetAsync(a, 0, sizeof(T) * n3, st));
@@ -944,7 +944,7 @@ class Solver final : public SolverBase {
     box(OpFluxX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpFluxY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     box(OpFluxZ{}, S.M, S.N, S.K + 1, S.IB, S.JB, S.KB);
-    if (S.Tke) cells(OpKeSlopes{0});   // delxyzFun's DelxW / DelyW, read by k-epsilon
+    if (S.keDxW) cells(OpKeSlopes{0});   // delxyzFun's DelxW / DelyW, read by the 3-D k-epsilon
     return check();
   }
   void get_uvw() {
@@ -1251,7 +1251,7 @@ class Solver final : public SolverBase {
     box(OpOmegaX{}, S.M + 1, S.N, S.K, S.IB, S.JB, S.KB);
     box(OpOmegaY{}, S.M, S.N + 1, S.K, S.IB, S.JB, S.KB);
     incols(OpOmegaScan{});
-    if (S.Tke) cells(OpKeSlopes{1});   // get_Omega's DelxU .. DelyV, before sponge_damping
+    if (S.keDxU) cells(OpKeSlopes{1});   // get_Omega's DelxU .. DelyV, before sponge_damping
   }
   int eval_duvw(int istep) override {
     if (istep < 1 || istep > it_order) return NHW_ERR_ARG;
@@ -1276,12 +1276,18 @@ class Solver final : public SolverBase {
   // first.  Inviscid flow has none.
   void launch_turb(int s) {
     if (!S.viscous) return;
-    if (S.Tke) {
+    if (S.ivturb == 10) {
       allcols(OpKeTop{});
       incols(OpKeColumn{s});
       box(OpKeSidesX{}, S.N * S.Kloc, 1, 1, 0, 0, 0);
       box(OpKeSidesY{}, S.Mloc * S.Kloc, 1, 1, 0, 0, 0);
       allcols(OpKeFinal{});
+    }
+    if (S.ivturb == 3) {
+      incols(OpKe2Column{s});
+      box(OpKe2Sides{0}, S.N * S.K, 1, 1, 0, 0, 0);
+      box(OpKe2Sides{1}, S.M * S.K, 1, 1, 0, 0, 0);
+      allcols(OpKe2Final{});
     }
     if (S.ivturb == 20) {
       cells(OpLesCell{});

@@ -335,6 +335,16 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=10, ihturb=10, rng=1, prod_type=2, bc_z0=5, bc_y0=5,
                        bc_yn=5, bc_xn=5, ibot=2, zob=1e-3), **kw)
         out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_ke2":
+        # the small submerged bar with the 2-D k-epsilon closure (IVTURB = 3, CmuHt = CmuVt); tests seed
+        # tke and epsilon above their floors
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=3, ihturb=10), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
+    elif name == "tiny_flume_ke2":
+        # the linear-wave flume (LEF_LIN) with the 2-D k-epsilon closure, whose first six columns
+        # stay at the floors
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=3, ihturb=1, chs=0.001), **kw)
+        out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
     elif name == "tiny_les":
         # the small submerged bar with the Smagorinsky LES closure (IVTURB = 20, CmuHt = CmuVt)
         kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=20, ihturb=20, cvs=0.1), **kw)

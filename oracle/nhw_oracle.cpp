@@ -27,8 +27,9 @@
 //   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
 //   diffusion                  src/nhwave.F:6785-7141
 //   trig                       src/nhwave.F:13182-13224
-//   eval_turb (IVTURB 1, 2, 10, 20; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
+//   eval_turb (IVTURB 1, 2, 3, 10, 20; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
 //   les_3D                     src/nhwave.F:8545-8729
+//   kepsilon (2-D, IVTURB = 3) src/nhwave.F:11117-11524
 //   kepsilon_3D                src/nhwave.F:10030-11114, adv_scalar_hlpa 7604-7806,
 //                              hlpa 7809-7847, flux_scalar_bc 7850-7986
 //   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
@@ -249,7 +250,7 @@ struct Model {
     // density Rho0 (no salinity, temperature, sediment or bubbles) gives
     // DRhoX = DRhoY = 0, so the flag runs the same path
     // IVTURB 1, 2, 10 (k-epsilon) and IHTURB 1, 2, >= 10 (CmuHt = CmuVt)
-    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 10 || p.ivturb == 20))
+    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 3 || p.ivturb == 10 || p.ivturb == 20))
       return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
@@ -3251,6 +3252,166 @@ struct Model {
               CmuVt(i, j, k) = Zero;
   }
 
+  // kepsilon (src/nhwave.F:11117-11524): the 2-D k-epsilon closure of
+  // IVTURB = 3.  Production from the vertical shear only, CmuVt (U_z^2 +
+  // V_z^2); HLPA advection and horizontal diffusion as kepsilon_3D's; plain
+  // implicit vertical diffusion; at the bed the smooth-wall law's friction
+  // velocity (the fixed-point iteration of les_3D, bounded at kLesIter
+  // steps; the reference's is not), mirrors elsewhere; the first six columns
+  // of a LEF_ maker and an INT_ maker's source region kept at the floors.
+  // The reference also stores U_z / D and V_z / D in DelzU / DelzV, which
+  // the next fluxes recompute before any read.
+  void kepsilon_2D(int istep) {
+    const double Dmin = (double)0.01f;
+    const double c1e = (double)1.44f, c2e = (double)1.92f, c3e = 0.0, cmiu = (double)0.09f;
+    const double Sche = (double)1.3f, Schk = 1.0, Prod_b = 0.0;
+    A3 Tke_Old = Tke, Eps_Old = Eps, Prod_s, R5;
+    Prod_s.init(Mloc, Nloc, Kloc); R5.init(Mloc, Nloc, Kloc);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k)
+          if (D(i, j) >= Dmin && Mask(i, j) == 1) {
+            const double ds = sigc(k + 1) - sigc(k - 1);
+            const double uz = (U(i, j, k + 1) - U(i, j, k - 1)) / ds / D(i, j);
+            const double vz = (V(i, j, k + 1) - V(i, j, k - 1)) / ds / D(i, j);
+            Prod_s(i, j, k) = CmuVt(i, j, k) * (uz * uz + vz * vz);
+          }
+    const int n = Kend - Kbeg + 1;
+    std::vector<double> Ac(n), Bc(n), Cc(n), Rhs0(n), Xsol(n);
+    auto column = [&](int i, int j, int eq) {
+      A3& Dv = eq == 2 ? DEps : DTke;
+      const double Sch = eq == 2 ? Sche : Schk, Dc = D(i, j);
+      int q = 0;
+      for (int k = Kbeg; k <= Kend; ++k, ++q) {
+        double r = R5(i, j, k);
+        if (eq == 2) r = r + c1e * Dc * (Prod_s(i, j, k) + c3e * Prod_b) * Eps_Old(i, j, k) / Tke_Old(i, j, k);
+        else r = r + Dc * (Prod_s(i, j, k) + Prod_b) - DEps(i, j, k);
+        Ac[q] = k == Kbeg ? 0.0
+                          : -dt / (Dc * Dc) * (0.5 * (Cmu + Cmu) + 0.5 * (CmuVt(i, j, k - 1) + CmuVt(i, j, k)) / Sch) /
+                                (0.5 * dsig(k) * (dsig(k) + dsig(k - 1)));
+        Cc[q] = k == Kend ? 0.0
+                          : -dt / (Dc * Dc) * (0.5 * (Cmu + Cmu) + 0.5 * (CmuVt(i, j, k) + CmuVt(i, j, k + 1)) / Sch) /
+                                (0.5 * dsig(k) * (dsig(k) + dsig(k + 1)));
+        Bc[q] = 1.0 - Ac[q] - Cc[q];
+        if (eq == 2) Bc[q] = Bc[q] + dt * c2e * Eps_Old(i, j, k) / Tke_Old(i, j, k);
+        Rhs0[q] = Dv(i, j, k) + dt * r;
+      }
+      trig(Ac, Bc, Cc, Rhs0, Xsol, n);
+      q = 0;
+      for (int k = Kbeg; k <= Kend; ++k) Dv(i, j, k) = Xsol[q++];
+    };
+    auto rk = [&](A3& Dv, A3& Dv0, double vmin) {
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int j = Jbeg; j <= Jend; ++j)
+          for (int k = Kbeg; k <= Kend; ++k)
+            if (D(i, j) >= Dmin && Mask(i, j) == 1) {
+              Dv(i, j, k) = ALPHA[istep - 1] * Dv0(i, j, k) + BETA[istep - 1] * Dv(i, j, k);
+              Dv(i, j, k) = dmax(Dv(i, j, k), D(i, j) * vmin);
+            }
+    };
+    adv_scalar_hlpa(Eps_Old, R5, 2);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        if (!(D(i, j) < Dmin && Mask(i, j) == 0)) column(i, j, 2);
+    rk(DEps, DEps0, Eps_min);
+    adv_scalar_hlpa(Tke_Old, R5, 1);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        if (!(D(i, j) < Dmin && Mask(i, j) == 0)) column(i, j, 1);
+    rk(DTke, DTke0, Tke_min);
+    const double kap = (double)0.41f;
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j) {
+        const double Umag = std::sqrt(U(i, j, Kbeg) * U(i, j, Kbeg) + V(i, j, Kbeg) * V(i, j, Kbeg));
+        if (Umag < (double)1.e-6f || D(i, j) < Dmin || Mask(i, j) == 0) continue;
+        const double Zdis = 0.5 * dsig(Kbeg) * D(i, j);
+        double X0 = (double)0.05f, Xn = X0;
+        const double Xa = std::log(9.0 * Umag * Zdis / Cmu);
+        for (int it = 0; it < kLesIter; ++it) {
+          Xn = X0 + (kap - X0 * (Xa + std::log(X0))) / (1.0 + kap / X0);
+          if (!(std::fabs((Xn - X0) / X0) > (double)1.e-8f && Xn > 0.0)) break;
+          X0 = Xn;
+        }
+        const double FricU = Xn * Umag;
+        DTke(i, j, Kbeg) = D(i, j) * (FricU * FricU / std::sqrt(cmiu));
+        DEps(i, j, Kbeg) = D(i, j) * (FricU * FricU * FricU / (Kappa * Zdis));
+        for (int k = 1; k <= Nghost; ++k) {
+          DTke(i, j, Kbeg - k) = DTke(i, j, Kbeg + k - 1);
+          DEps(i, j, Kbeg - k) = DEps(i, j, Kbeg + k - 1);
+        }
+      }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) {
+          DTke(i, j, Kend + k) = DTke(i, j, Kend - k + 1);
+          DEps(i, j, Kend + k) = DEps(i, j, Kend - k + 1);
+        }
+    const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON) || p.wavemaker == NHW_WM_LEF_TID ||
+                     p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        if (lef)   // the first six columns (within the array)
+          for (int i = Ibeg; i <= Ibeg + 5 && i <= Mloc; ++i) {
+            Tke(i, j, k) = Tke_min;
+            Eps(i, j, k) = Eps_min;
+            DTke(i, j, k) = D(i, j) * Tke_min;
+            DEps(i, j, k) = D(i, j) * Eps_min;
+            CmuVt(i, j, k) = Cmut_min;
+          }
+        for (int i = 1; i <= Nghost; ++i) {
+          DTke(Ibeg - i, j, k) = DTke(Ibeg + i - 1, j, k);
+          DEps(Ibeg - i, j, k) = DEps(Ibeg + i - 1, j, k);
+        }
+      }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) {
+          DTke(Iend + i, j, k) = DTke(Iend - i + 1, j, k);
+          DEps(Iend + i, j, k) = DEps(Iend - i + 1, j, k);
+        }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) {
+          DTke(i, Jbeg - j, k) = DTke(i, Jbeg + j - 1, k);
+          DEps(i, Jbeg - j, k) = DEps(i, Jbeg + j - 1, k);
+        }
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) {
+          DTke(i, Jend + j, k) = DTke(i, Jend - j + 1, k);
+          DEps(i, Jend + j, k) = DEps(i, Jend - j + 1, k);
+        }
+    for (int i = 1; i <= Mloc; ++i)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int k = 1; k <= Kloc; ++k) {
+          if (D(i, j) >= Dmin && Mask(i, j) == 1) {
+            Tke(i, j, k) = DTke(i, j, k) / D(i, j);
+            Eps(i, j, k) = DEps(i, j, k) / D(i, j);
+            CmuVt(i, j, k) = cmiu * (Tke(i, j, k) * Tke(i, j, k)) / Eps(i, j, k);
+          } else {
+            Tke(i, j, k) = Tke_min;
+            Eps(i, j, k) = Eps_min;
+            DTke(i, j, k) = D(i, j) * Tke_min;
+            DEps(i, j, k) = D(i, j) * Eps_min;
+            CmuVt(i, j, k) = Cmut_min;
+          }
+        }
+    const int w = p.wavemaker;
+    if (w == NHW_WM_INT_LIN || w == NHW_WM_INT_SOL || w == NHW_WM_INT_CON || w == NHW_WM_INT_JON ||
+        w == NHW_WM_INT_TMA || w == NHW_WM_INT_SPC || w == NHW_WM_INT_IRR)
+      for (int k = 1; k <= Kloc; ++k)
+        for (int j = 1; j <= Nloc; ++j)
+          for (int i = 1; i <= Mloc; ++i)
+            if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+                yc(j) <= p.ysource_nrth) {
+              Tke(i, j, k) = Tke_min;
+              Eps(i, j, k) = Eps_min;
+              DTke(i, j, k) = D(i, j) * Tke_min;
+              DEps(i, j, k) = D(i, j) * Eps_min;
+              CmuVt(i, j, k) = Cmut_min;
+            }
+  }
+
   // eval_turb (src/nhwave.F:6544-6782), called after sponge_damping.
   // Vertical: IVTURB 1 CmuVt = Cvs; 2 the subgrid model CmuVt = Cvs D
   // dsig^2 |d(U,V)/dsigma| on every level but the outermost ghosts, which
@@ -3267,6 +3428,8 @@ struct Model {
       kepsilon_3D(istep);
     } else if (p.ivturb == 20) {
       les_3D();
+    } else if (p.ivturb == 3) {
+      kepsilon_2D(istep);
     } else {
       for (int i = 1; i <= Mloc; ++i)
         for (int j = 1; j <= Nloc; ++j) {

@@ -24,7 +24,7 @@ def _scen(name, precision, **attrs):
     for k, v in attrs.items():
         setattr(p, k, v)
     s = lib.Scenario(p, d, e, u)
-    if p.viscous_flow and p.ivturb == 10:
+    if p.viscous_flow and p.ivturb in (3, 10):
         seed_ke(s)
     return s
 
@@ -32,7 +32,8 @@ def _scen(name, precision, **attrs):
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name,krylov", [("tiny_c2", 0), ("tiny_c3", 0), ("tiny_c4", 0), ("tiny_flume_lin", 0),
                                          ("tiny_open", 0), ("tiny_visc", 0), ("tiny_c2", 2), ("tiny_flux_lr", 0),
-                                         ("tiny_visc_sgs", 0), ("tiny_ke_rng", 0), ("tiny_les", 0)])
+                                         ("tiny_visc_sgs", 0), ("tiny_ke_rng", 0), ("tiny_les", 0),
+                                         ("tiny_ke2", 0)])
 def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     """krylov = 2: the GMRES solver, whose basis lies behind the checkpointed
     prefix and is rebuilt by every solve.  tiny_open: the Orlanski boundary's
@@ -57,7 +58,7 @@ def test_resume_continues_bit_for_bit(name, krylov, precision, gpu_lib):
     assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
     assert sa.total_krylov_iters == sb.total_krylov_iters
     extra = (["CMUVT", "CMUHT"] if a.params.viscous_flow else []) + \
-        (["TKE", "EPS", "DTKE", "DEPS"] if a.params.viscous_flow and a.params.ivturb == 10 else [])
+        (["TKE", "EPS", "DTKE", "DEPS"] if a.params.viscous_flow and a.params.ivturb in (3, 10) else [])
     for f in FIELDS + extra:
         fid = getattr(F, f)
         assert np.array_equal(a.get(fid), b.get(fid)), f"{name} {f}"

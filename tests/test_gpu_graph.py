@@ -23,7 +23,7 @@ def _scen(name, precision, **attrs):
     for k, v in attrs.items():
         setattr(p, k, v)
     s = lib.Scenario(p, d, e, u)
-    if p.viscous_flow and p.ivturb == 10:
+    if p.viscous_flow and p.ivturb in (3, 10):
         seed_ke(s)
     return s
 
@@ -50,7 +50,7 @@ def _routines(s):
                                   "tiny_flume_stk", "tiny_flume_con", "tiny_flume_cur", "tiny_flume_foc", "tiny_flume_tid", "tiny_open",
                                   "tiny_flume_open", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon",
                                   "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng",
-                                  "tiny_les"])
+                                  "tiny_les", "tiny_ke2", "tiny_flume_ke2"])
 def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, hllc=hllc)
@@ -62,7 +62,7 @@ def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
         assert (sa.time, sa.dt, sa.run_step) == (sb.time, sb.dt, sb.run_step)
         assert sa.total_krylov_iters == sb.total_krylov_iters
         assert sa.poisson_solves == sb.poisson_solves
-        ke = ["TKE", "EPS", "CMUVT", "CMUHT"] if a.params.viscous_flow and a.params.ivturb == 10 else []
+        ke = ["TKE", "EPS", "CMUVT", "CMUHT"] if a.params.viscous_flow and a.params.ivturb in (3, 10) else []
         for f in FIELDS + ke:
             fid = getattr(F, f)
             x, y = a.get(fid), b.get(fid)

@@ -18,10 +18,12 @@ CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # side, and the small submerged bar with constant viscosities (VISCOUS_FLOW;
 # in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds;
 # the subgrid eddy viscosities, IVTURB = IHTURB = 2; the k-epsilon closure,
-# IVTURB = IHTURB = 10, standard and RNG, from seeded turbulence; the
-# Smagorinsky LES, IVTURB = 20), and wall friction (BC = 5) on the sides
+# IVTURB = IHTURB = 10, standard and RNG, and the 2-D one, IVTURB = 3, from
+# seeded turbulence; the Smagorinsky LES, IVTURB = 20), and wall friction
+# (BC = 5) on the sides
 MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric",
-                      "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng", "tiny_les", "tiny_wallfric"]
+                      "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng", "tiny_ke2", "tiny_flume_ke2",
+                      "tiny_les", "tiny_wallfric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -50,7 +52,7 @@ def _pair(name, oracle_mod, precision=0, tol=STEP_TOL, seed=7, **kw):
     q = p.copy()
     q.precision = 0
     o = oracle_mod.Oracle(q, d, e, u)
-    if p.viscous_flow and p.ivturb == 10:
+    if p.viscous_flow and p.ivturb in (3, 10):
         seed_ke(g, o)
     return g, o
 
@@ -128,7 +130,7 @@ def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
                         r = rel_l2(g.get(fid), o.get(fid))
                         assert r < 1e-13, f"eval_turb {rnd}.{s}: {n} rel {r:.3e}"
                         g.set(fid, o.get(fid))
-                ke = ["TKE", "EPS", "DTKE", "DEPS"] if g.params.ivturb == 10 else []
+                ke = ["TKE", "EPS", "DTKE", "DEPS"] if g.params.ivturb in (3, 10) else []
                 _cmp_exact(g, o, ["CMUVT", "CMUHT"] + ke, f"eval_turb {rnd}.{s}")
     g.close()
 

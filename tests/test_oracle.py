@@ -504,6 +504,33 @@ def test_ke_shear_produces_turbulence(oracle_mod):
         assert kept[1] > 1.05 * kept[0], (prod, rng, kept)
 
 
+def test_ke2_uniform_turbulence_decays_by_the_implicit_step(oracle_mod):
+    """kepsilon (src/nhwave.F:11117-11524, IVTURB = 3) in still water with
+    uniform tke k0 and epsilon e0: no production, advection or diffusion and,
+    with no bed velocity, no wall function, so every level takes eps1 = e0 /
+    (1 + dt c2e e0 / k0), k1 = k0 - dt eps1 and CmuVt = cmiu k1^2 / eps1."""
+    from nhwave_gb300 import default_params, fields as F
+    M, N, K, k0, e0 = 8, 3, 6, 1e-3, 1e-4
+    p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=0.5, dy=0.5, dt_ini=0.01, dt_max=0.01, tol=1e-12, itmax=2000,
+                       viscous_flow=1, visc=1e-6, ivturb=3, ihturb=10)
+    o = oracle_mod.Oracle(p, np.ones(M * N))
+    D = o.get(F.D)[None]
+    shp = o.get(F.TKE).shape
+    o.set(F.TKE, np.full(shp, k0)); o.set(F.EPS, np.full(shp, e0))
+    o.set(F.DTKE, D * k0 * np.ones(shp)); o.set(F.DEPS, D * e0 * np.ones(shp))
+    _ke_stage(o)
+    dt = o.scalars().dt
+    ng = F.NG
+    e1 = e0 / (1 + dt * float(np.float32(1.92)) * e0 / k0)
+    k1 = k0 - dt * e1
+    inner = (slice(ng, ng + K), slice(ng, ng + N), slice(ng, ng + M))
+    assert o.get(F.EPS)[inner] == pytest.approx(np.full((K, N, M), e1), rel=1e-12)
+    assert o.get(F.TKE)[inner] == pytest.approx(np.full((K, N, M), k1), rel=1e-12)
+    cmiu = float(np.float32(0.09))
+    assert o.get(F.CMUVT)[inner] == pytest.approx(np.full((K, N, M), cmiu * k1 * k1 / e1), rel=1e-12)
+    assert np.array_equal(o.get(F.CMUHT), o.get(F.CMUVT))
+
+
 def test_les_smagorinsky_viscosity_and_smooth_wall_law(oracle_mod):
     """les_3D (src/nhwave.F:8545-8729) on a shear U = a sigma in a flat 1 m
     deep channel before the first sigma_transform: the only strain rate is
