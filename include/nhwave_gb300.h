@@ -26,8 +26,9 @@
  *                             incl. poisson_solver src/pressure.F:63-245 and
  *                             generate_coef_rhs src/pressure.F:475-840)
  *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
- *   nhw_eval_turb          <- eval_turb(ISTEP)     src/nhwave.F:6544-6782 (IVTURB 1, 2, 10 with
- *                             kepsilon_3D :10030-11114, 20 with les_3D :8545-8729;
+ *   nhw_eval_turb          <- eval_turb(ISTEP)     src/nhwave.F:6544-6782 (IVTURB 1, 2, 3 with
+ *                             kepsilon :11117-11524, 10 with kepsilon_3D :10030-11114,
+ *                             20 with les_3D :8545-8729;
  *                             IHTURB 1, 2, >= 10;
  *                             viscous flow only, a no-op otherwise)
  *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
@@ -171,8 +172,8 @@ typedef struct nhw_params {
                                               out and the solve reports NHW_ERR_TIMEOUT */
   /* viscous flow (read when viscous_flow = 1; src/initialize.F:357, 385-392) */
   int32_t ivturb, ihturb;                  /* IVTURB IHTURB: 1 constant viscosity,
-                                              2 subgrid model; IVTURB 10 3-D
-                                              k-epsilon, 20 Smagorinsky LES; IHTURB
+                                              2 subgrid model; IVTURB 3 / 10 2-D /
+                                              3-D k-epsilon, 20 Smagorinsky LES; IHTURB
                                               >= 10 takes CmuHt = CmuVt                */
   int32_t rng;                             /* RNG: seeding viscosity of the first stage */
   double  cvs, chs;                        /* Cvs Chs: vertical / horizontal eddy
