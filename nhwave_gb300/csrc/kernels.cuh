@@ -1444,8 +1444,10 @@ struct OpTurbV {
       cv[0] = cv[S.sz];
       cv[S.sz * (S.Kloc - 1)] = cv[S.sz * (S.Kloc - 2)];
     }   // IVTURB = 10 and 20: the k-epsilon / LES kernels set CmuVt before this one
-    if (S.ivturb == 20 && S.les_int && S.xc[i] >= S.wm_xw && S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys &&
-        S.yc[j] <= S.wm_yn)   // no turbulence in an INT_ maker's source region
+    // no turbulence in an INT_ maker's source region (LES), or in an INT_,
+    // LEF_ or FOCUSED maker's (dynamic LES)
+    if (((S.ivturb == 20 && S.les_int) || (S.ivturb == 30 && S.ke_quiet)) && S.xc[i] >= S.wm_xw &&
+        S.xc[i] <= S.wm_xe && S.yc[j] >= S.wm_ys && S.yc[j] <= S.wm_yn)
       for (int k = 0; k < S.Kloc; ++k) cv[S.sz * k] = (T)0;
     if (S.ihturb == 1)
       for (int k = 0; k < S.Kloc; ++k) S.CmuHt[q + S.sz * k] = (T)S.v_chs;
@@ -2262,6 +2264,201 @@ struct OpKe2Final {
         S.CmuVt[o] = (T)S.v_cmut0;
       }
     }
+  }
+};
+
+// =========================================================================
+//   dynamic Smagorinsky LES, IVTURB = 30 (les_dyn, src/nhwave.F:7989-8542)
+// =========================================================================
+// Scratch fields of n3 cells each, from S.ld: 0-5 Sij (S11 S22 S33 S12 S23
+// S13), 6 |S| = sqrt(2 SijSij), 7-12 the test-filtered |S|Sij, 13-18
+// filtered Sij, 19 filtered |S|, 20-25 filtered u_i u_j (uu vv ww uv vw uw),
+// 26-28 filtered u_i, 29 the clipped coefficient, 30 its smoothed value.
+// Every kernel writes every cell it owns (zero where the reference leaves
+// zero); ghosts then follow the reference's mirror loops.
+constexpr double kLdDmin = (double)0.02f;
+template <class T>
+__device__ __forceinline__ T* ldf(const Dev<T>& S, int f) { return S.ld + S.ld_n * f; }
+template <class T>
+__device__ __forceinline__ bool ld_interior(const Dev<T>& S, int i, int j, int k) {
+  return i >= S.IB && i <= S.IE && j >= S.JB && j <= S.JE && k >= S.KB && k <= S.KE;
+}
+// the strain rates of wet interior cells deeper than 0.02 m (zero elsewhere)
+struct OpLdStrain {
+  static constexpr const char* kName = "lesdyn_strain";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long q = i2(S, i, j), o = i3(S, i, j, k);
+    double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const double Dq = S.D[q];
+    if (ld_interior(S, i, j, k) && S.Mask[q] == 1 && Dq > kLdDmin) {
+      double sx = 0.0, sy = 0.0;
+      if (S.sc->sig_set) {
+        sx = (1.0 - S.sigc[k]) / S.scD[q] * S.scHx[q] - S.sigc[k] / S.scD[q] * S.scEx[q];
+        sy = (1.0 - S.sigc[k]) / S.scD[q] * S.scHy[q] - S.sigc[k] / S.scD[q] * S.scEy[q];
+      }
+      auto U = [&](long long x) { return (double)S.U[x]; };
+      auto V = [&](long long x) { return (double)S.V[x]; };
+      auto W = [&](long long x) { return (double)S.W[x]; };
+      const long long up = o + S.sz, dn = o - S.sz, e = o + 1, w = o - 1, n = o + S.sy, so = o - S.sy;
+      const double ds = S.sigc[k + 1] - S.sigc[k - 1];
+      const double dUs = (U(up) - U(dn)) / ds, dVs = (V(up) - V(dn)) / ds, dWs = (W(up) - W(dn)) / ds;
+      s[0] = (U(e) - U(w)) / (2.0 * S.dx) + dUs * sx;
+      s[1] = (V(n) - V(so)) / (2.0 * S.dy) + dVs * sy;
+      s[2] = 1.0 / Dq * (W(up) - W(dn)) / ds;
+      s[3] = 0.5 * ((U(n) - U(so)) / (2.0 * S.dy) + dUs * sy + (V(e) - V(w)) / (2.0 * S.dx) + dVs * sx);
+      s[4] = 0.5 * (dVs / Dq + (W(n) - W(so)) / (2.0 * S.dy) + dWs * sy);
+      s[5] = 0.5 * (dUs / Dq + (W(e) - W(w)) / (2.0 * S.dx) + dWs * sx);
+    }
+    for (int c = 0; c < 6; ++c) ldf(S, c)[o] = (T)s[c];
+  }
+};
+// ghost mirrors of scratch fields [f0, f1) (f0 < 0: CmuVt) along one group
+// of lines: grp 0 the bed then the surface of an interior column, 1 the
+// west then the east side of an interior row and level, 2 the south then
+// (north_all, or the last field alone) the north side of an interior column
+// and level -- each line in the reference's order
+struct OpLdMirror {
+  static constexpr const char* kName = "lesdyn_mirror";
+  int grp, f0, f1, north_all;
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int t, int, int) const {
+    const int fa = f0 < 0 ? 0 : f0, fb = f0 < 0 ? 1 : f1;
+    for (int f = fa; f < fb; ++f) {
+      T* a = f0 < 0 ? S.CmuVt : ldf(S, f);
+      if (grp == 0) {
+        const int i = S.IB + t % S.M, j = S.JB + t / S.M;
+        for (int g = 1; g <= NG; ++g) a[i3(S, i, j, S.KB - g)] = a[i3(S, i, j, S.KB + g - 1)];
+        for (int g = 1; g <= NG; ++g) a[i3(S, i, j, S.KE + g)] = a[i3(S, i, j, S.KE - g + 1)];
+      } else if (grp == 1) {
+        const int j = S.JB + t % S.N, k = S.KB + t / S.N;
+        for (int g = 1; g <= NG; ++g) a[i3(S, S.IB - g, j, k)] = a[i3(S, S.IB + g - 1, j, k)];
+        for (int g = 1; g <= NG; ++g) a[i3(S, S.IE + g, j, k)] = a[i3(S, S.IE - g + 1, j, k)];
+      } else {
+        const int i = S.IB + t % S.M, k = S.KB + t / S.M;
+        for (int g = 1; g <= NG; ++g) a[i3(S, i, S.JB - g, k)] = a[i3(S, i, S.JB + g - 1, k)];
+        if (north_all || f == fb - 1)
+          for (int g = 1; g <= NG; ++g) a[i3(S, i, S.JE + g, k)] = a[i3(S, i, S.JE - g + 1, k)];
+      }
+    }
+  }
+};
+// |S| in every cell deeper than 0.02 m (zero elsewhere)
+struct OpLdSab {
+  static constexpr const char* kName = "lesdyn_sab";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    double v = 0.0;
+    if (S.D[i2(S, i, j)] > kLdDmin) {
+      double s[6];
+      for (int c = 0; c < 6; ++c) s[c] = (double)ldf(S, c)[o];
+      const double a = s[0] * s[0] + s[1] * s[1] + s[2] * s[2] + 2.0 * (s[3] * s[3] + s[4] * s[4] + s[5] * s[5]);
+      v = sqrt(2.0 * a);
+    }
+    ldf(S, 6)[o] = (T)v;
+  }
+};
+// the separable [1 w 1] filter of src/nhwave.F:8412-8452 at an interior
+// cell, in the reference's order: x sums, then y, then z, times fact
+template <class F>
+__device__ __forceinline__ double ld_filter_at(F P, int i, int j, int k, double w, double fact) {
+  auto s1 = [&](int jj, int kk) { return P(i - 1, jj, kk) + w * P(i, jj, kk) + P(i + 1, jj, kk); };
+  auto s2 = [&](int kk) { return s1(j - 1, kk) + w * s1(j, kk) + s1(j + 1, kk); };
+  return fact * (s2(k - 1) + w * s2(k) + s2(k + 1));
+}
+// the 22 test-filtered fields (weit 2, fact 1/64) at interior cells, zero
+// elsewhere; |S|Sij is zero where D <= 0.02 m
+struct OpLdFilter {
+  static constexpr const char* kName = "lesdyn_filter";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    if (!ld_interior(S, i, j, k)) {
+      for (int f = 7; f <= 28; ++f) ldf(S, f)[o] = (T)0;
+      return;
+    }
+    const double fact = 1.0 / 64.0;
+    for (int f = 7; f <= 28; ++f) {
+      auto P = [&](int ii, int jj, int kk) -> double {
+        const long long x = i3(S, ii, jj, kk);
+        if (f <= 12) return S.D[i2(S, ii, jj)] > kLdDmin ? (double)ldf(S, 6)[x] * (double)ldf(S, f - 7)[x] : 0.0;
+        if (f <= 18) return (double)ldf(S, f - 13)[x];
+        if (f == 19) return (double)ldf(S, 6)[x];
+        const double u = (double)S.U[x], v = (double)S.V[x], ww = (double)S.W[x];
+        switch (f) {
+          case 20: return u * u;
+          case 21: return v * v;
+          case 22: return ww * ww;
+          case 23: return u * v;
+          case 24: return v * ww;
+          case 25: return u * ww;
+          case 26: return u;
+          case 27: return v;
+          default: return ww;
+        }
+      };
+      ldf(S, f)[o] = (T)ld_filter_at(P, i, j, k, 2.0, fact);
+    }
+  }
+};
+// the coefficient -LijMij / (2 MijMij) / Delta^2, clipped to [0, 0.04], in
+// every cell (Delta = (dx dy D dsig)^(1/3))
+struct OpLdCoef {
+  static constexpr const char* kName = "lesdyn_coef";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    const double Dq = S.D[i2(S, i, j)];
+    auto F = [&](int f) { return (double)ldf(S, f)[o]; };
+    double M[6], L[6];
+    for (int n = 0; n < 6; ++n) M[n] = 4.0 * F(19) * F(13 + n) - F(7 + n);
+    L[0] = F(20) - F(26) * F(26);
+    L[1] = F(21) - F(27) * F(27);
+    L[2] = F(22) - F(28) * F(28);
+    L[3] = F(23) - F(26) * F(27);
+    L[4] = F(24) - F(27) * F(28);
+    L[5] = F(25) - F(28) * F(26);
+    double MM = 0.0, LM = 0.0;
+    if (Dq > kLdDmin) {
+      MM = M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + 2.0 * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+      LM = L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + 2.0 * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]);
+    }
+    double c = 0.5 * (-LM) / (MM + (double)1.e-16f);
+    const double FW = pow(S.dx * S.dy * Dq * S.dsig[k], (double)(1.0f / 3.0f));
+    c = c / (FW * FW);
+    if (c < 0.0) c = 0.0;
+    if (c > (double)0.04f) c = (double)0.04f;
+    ldf(S, 29)[o] = (T)c;
+  }
+};
+// the coefficient smoothed (weit 1, fact 1/27) at interior cells, zero elsewhere
+struct OpLdSmooth {
+  static constexpr const char* kName = "lesdyn_smooth";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    if (!ld_interior(S, i, j, k)) {
+      ldf(S, 30)[o] = (T)0;
+      return;
+    }
+    auto P = [&](int ii, int jj, int kk) -> double { return (double)ldf(S, 29)[i3(S, ii, jj, kk)]; };
+    ldf(S, 30)[o] = (T)ld_filter_at(P, i, j, k, 1.0, (double)(1.0f / 27.0f));
+  }
+};
+// CmuVt = max(C Delta^2 |S|, 0) in interior cells deeper than 0.02 m, zero elsewhere
+struct OpLdVisc {
+  static constexpr const char* kName = "lesdyn_visc";
+  template <class T>
+  __device__ void operator()(const Dev<T>& S, int i, int j, int k) const {
+    const long long o = i3(S, i, j, k);
+    const double Dq = S.D[i2(S, i, j)];
+    double v = 0.0;
+    if (ld_interior(S, i, j, k) && Dq > kLdDmin) {
+      const double FW = pow(S.dx * S.dy * Dq * S.dsig[k], (double)(1.0f / 3.0f));
+      v = dmax_((double)ldf(S, 30)[o] * (FW * FW) * (double)ldf(S, 6)[o], 0.0);
+    }
+    S.CmuVt[o] = (T)v;
   }
 };
 

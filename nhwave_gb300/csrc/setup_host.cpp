@@ -35,9 +35,10 @@ int check_params(const nhw_params& p) {
   // DRhoX and DRhoY (signed zeros, which leave R2 and R3 unchanged): the flag
   // runs the same path.
   // viscous flow: IVTURB 1 constant, 2 subgrid, 3 the 2-D and 10 the 3-D
-  // k-epsilon model, 20 the Smagorinsky LES; IHTURB 1, 2 or >= 10 (CmuHt =
-  // CmuVt).  The dynamic LES (30) is not built
-  if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 3 || p.ivturb == 10 || p.ivturb == 20))
+  // k-epsilon model, 20 the Smagorinsky and 30 the dynamic LES; IHTURB 1, 2
+  // or >= 10 (CmuHt = CmuVt)
+  if (p.viscous_flow &&
+      !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 3 || p.ivturb == 10 || p.ivturb == 20 || p.ivturb == 30))
     return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
   if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;

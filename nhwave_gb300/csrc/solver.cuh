@@ -335,6 +335,10 @@ class Solver final : public SolverBase {
     add(&S.P, sizeof(double) * n3);
     if (p.viscous_flow)   // explicit viscous terms of the stage
       for (T** pp : {&S.Dxx, &S.Dxy, &S.Dyx, &S.Dyy, &S.Dzx, &S.Dzy}) add(pp, sizeof(T) * n3);
+    if (p.viscous_flow && p.ivturb == 30) {   // dynamic LES scratch
+      S.ld_n = (long long)n3;
+      add(&S.ld, sizeof(T) * n3 * 31);
+    }
     if (ke && p.ivturb == 10) {   // slopes the 3-D production reads, surface values of the stage
       for (T** pp : {&S.keDxU, &S.keDyU, &S.keDxV, &S.keDyV, &S.keDxW, &S.keDyW}) add(pp, sizeof(T) * n3);
       for (double** pp : {&S.keTopK, &S.keTopE}) add(pp, sizeof(double) * n2);
@@ -1288,6 +1292,30 @@ class Solver final : public SolverBase {
       box(OpKe2Sides{0}, S.N * S.K, 1, 1, 0, 0, 0);
       box(OpKe2Sides{1}, S.M * S.K, 1, 1, 0, 0, 0);
       allcols(OpKe2Final{});
+    }
+    if (S.ivturb == 30) {   // les_dyn (src/nhwave.F:7989-8410)
+      auto every = [&](auto op) {
+        L(decltype(op)::kName, [&] {
+          k_allcells<T, decltype(op)><<<cdiv((long long)S.Mloc * S.Nloc * S.Kloc, 256), 256, 0, st>>>(S, op);
+        });
+      };
+      auto mirror = [&](int f0, int f1, int north_all) {
+        box(OpLdMirror{0, f0, f1, north_all}, S.M * S.N, 1, 1, 0, 0, 0);
+        box(OpLdMirror{1, f0, f1, north_all}, S.N * S.K, 1, 1, 0, 0, 0);
+        box(OpLdMirror{2, f0, f1, north_all}, S.M * S.K, 1, 1, 0, 0, 0);
+      };
+      every(OpLdStrain{});
+      mirror(0, 6, 0);   // Sij: the reference's north loop writes the sixth component only
+      every(OpLdSab{});
+      every(OpLdFilter{});
+      mirror(7, 29, 1);
+      every(OpLdCoef{});
+      every(OpLdSmooth{});
+      mirror(30, 31, 1);
+      every(OpLdVisc{});
+      box(OpLdMirror{0, -1, 0, 1}, S.M * S.N, 1, 1, 0, 0, 0);   // CmuVt: bed and surface, then the sides
+      box(OpLesSides{0}, S.N * S.K, 1, 1, 0, 0, 0);
+      box(OpLesSides{1}, S.M * S.K, 1, 1, 0, 0, 0);
     }
     if (S.ivturb == 20) {
       cells(OpLesCell{});

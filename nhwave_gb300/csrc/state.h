@@ -202,6 +202,9 @@ struct Dev {
   T *Tke, *Eps, *DTke, *DEps, *DTke0, *DEps0;
   T *keDxU, *keDyU, *keDxV, *keDyV, *keDxW, *keDyW;
   double *keTopK, *keTopE;
+  // dynamic LES (IVTURB = 30, else nullptr): 31 scratch fields of ld_n cells
+  T* ld;
+  long long ld_n;
   // GMRES (krylov.cuh): basis V [kGmMax+1][neq], preconditioned basis Z
   // [kGmMax][neq], Hessenberg / rotations / g / y in FP64 (gm), the current
   // column, y and 1/||w|| in T (gmT), wide reduction partials; nullptr unless

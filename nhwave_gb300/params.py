@@ -287,10 +287,9 @@ def read_irr2d(path: str):
 
 def unsupported_reason(p: NhwParams) -> str | None:
     """Why a parameter set falls outside this path (None when it is inside)."""
-    if p.viscous_flow and (p.ivturb not in (1, 2, 3, 10, 20) or not (p.ihturb in (1, 2) or p.ihturb >= 10)):
-        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (constant viscosities (1), the subgrid "
-                "models (2), the 2-D and 3-D k-epsilon models (3, 10) and the Smagorinsky LES (20) are on the GPU "
-                "path; the dynamic LES (30) is not)")
+    if p.viscous_flow and (p.ivturb not in (1, 2, 3, 10, 20, 30) or not (p.ihturb in (1, 2) or p.ihturb >= 10)):
+        return (f"VISCOUS_FLOW=T with IVTURB={p.ivturb}, IHTURB={p.ihturb} (the GPU path has IVTURB 1 constant, 2 "
+                "subgrid, 3 and 10 k-epsilon, 20 and 30 LES, and IHTURB 1, 2 or >= 10)")
     if p.wavemaker not in (WM_NONE,) + WM_INT + WM_LEF + WM_EAST:
         return ("WAVEMAKER (only NONE, INT_LIN, INT_SOL, INT_CON, INT_JON, INT_TMA, INT_SPC, INT_IRR, LEF_LIN, "
                 "LEF_SOL, LEF_STK, LEF_CON, LEF_TID, LEF_JON, LEF_TMA, LEF_SPC, WAV_CUR, FOCUSED, RIG_LIN and "

@@ -345,6 +345,10 @@ def make(name: str, precision: int = NHW_FP64, seed: int = 0, **kw):
         # stay at the floors
         kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=3, ihturb=1, chs=0.001), **kw)
         out = wave_flume("LIN", M=64, N=4, K=5, dx=0.1, dy=0.1, sponge=1.5, **kw)
+    elif name == "tiny_lesdyn":
+        # the small submerged bar with the dynamic Smagorinsky LES (IVTURB = 30, CmuHt = CmuVt)
+        kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=30, ihturb=30), **kw)
+        out = submerged_bar(M=96, N=6, K=6, dx=25.6 / 96, dy=0.2, **kw)
     elif name == "tiny_les":
         # the small submerged bar with the Smagorinsky LES closure (IVTURB = 20, CmuHt = CmuVt)
         kw = dict(dict(viscous_flow=1, visc=1e-6, ivturb=20, ihturb=20, cvs=0.1), **kw)

@@ -27,9 +27,10 @@
 //   eval_duvw                  src/nhwave.F:539-1300 (with the implicit vertical viscous step)
 //   diffusion                  src/nhwave.F:6785-7141
 //   trig                       src/nhwave.F:13182-13224
-//   eval_turb (IVTURB 1, 2, 3, 10, 20; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
+//   eval_turb (IVTURB 1, 2, 3, 10, 20, 30; IHTURB 1, 2, >= 10) src/nhwave.F:6544-6782
 //   les_3D                     src/nhwave.F:8545-8729
 //   kepsilon (2-D, IVTURB = 3) src/nhwave.F:11117-11524
+//   les_dyn, filter            src/nhwave.F:7989-8410, 8412-8542
 //   kepsilon_3D                src/nhwave.F:10030-11114, adv_scalar_hlpa 7604-7806,
 //                              hlpa 7809-7847, flux_scalar_bc 7850-7986
 //   get_UVW / vel_bc / KBC     src/nhwave.F:1651-1683, 4416-5117 (walls 1/2/5, inflow,
@@ -250,7 +251,8 @@ struct Model {
     // density Rho0 (no salinity, temperature, sediment or bubbles) gives
     // DRhoX = DRhoY = 0, so the flag runs the same path
     // IVTURB 1, 2, 10 (k-epsilon) and IHTURB 1, 2, >= 10 (CmuHt = CmuVt)
-    if (p.viscous_flow && !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 3 || p.ivturb == 10 || p.ivturb == 20))
+    if (p.viscous_flow &&
+        !(p.ivturb == 1 || p.ivturb == 2 || p.ivturb == 3 || p.ivturb == 10 || p.ivturb == 20 || p.ivturb == 30))
       return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && !(p.ihturb == 1 || p.ihturb == 2 || p.ihturb >= 10)) return NHW_ERR_UNSUPPORTED;
     if (p.viscous_flow && (!(p.schmidt != 0.0) || !(p.viscous_number > 0.0))) return NHW_ERR_ARG;
@@ -3412,6 +3414,186 @@ struct Model {
             }
   }
 
+  // filter of les_dyn (src/nhwave.F:8412-8542): the separable [1 weit 1]
+  // smoother in x (interior columns i, every j, k), y (interior i, j; every
+  // k) and z (interior cells) scaled by fact, then mirrored into the ghosts
+  // of the bed / surface (interior columns), the west / east sides
+  // (interior rows and levels) and the south / north sides (interior
+  // columns and levels); every other ghost is zero
+  void les_filter(A3& In, A3& Out, double weit, double fact) {
+    A3 S1, S2;
+    S1.init(Mloc, Nloc, Kloc); S2.init(Mloc, Nloc, Kloc);
+    Out.fill(0.0);
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) S1(i, j, k) = In(i - 1, j, k) + weit * In(i, j, k) + In(i + 1, j, k);
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i) S2(i, j, k) = S1(i, j - 1, k) + weit * S1(i, j, k) + S1(i, j + 1, k);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          Out(i, j, k) = fact * (S2(i, j, k - 1) + weit * S2(i, j, k) + S2(i, j, k + 1));
+    les_mirror(Out, true);
+  }
+  // ghost mirrors of les_dyn's fields in the reference's loop order: the
+  // bed, then the surface (interior columns); the west, then the east
+  // sides (interior rows and levels); the south, then (if north) the north
+  // side (interior columns and levels)
+  void les_mirror(A3& a, bool north) {
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) a(i, j, Kbeg - k) = a(i, j, Kbeg + k - 1);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) a(i, j, Kend + k) = a(i, j, Kend - k + 1);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) a(Ibeg - i, j, k) = a(Ibeg + i - 1, j, k);
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) a(Iend + i, j, k) = a(Iend - i + 1, j, k);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) a(i, Jbeg - j, k) = a(i, Jbeg + j - 1, k);
+    if (north)
+      for (int i = Ibeg; i <= Iend; ++i)
+        for (int k = Kbeg; k <= Kend; ++k)
+          for (int j = 1; j <= Nghost; ++j) a(i, Jend + j, k) = a(i, Jend - j + 1, k);
+  }
+  // les_dyn (src/nhwave.F:7989-8410): the dynamic Smagorinsky closure of
+  // IVTURB = 30 (Germano identity with Lilly's least squares).  The strain
+  // rates Sij of wet interior cells deeper than 0.02 m and their ghosts
+  // (the reference's north mirror copies the sixth component only, once per
+  // component, and that is kept); |S| = sqrt(2 SijSij); the test-filtered
+  // (weit 2, 1/64) Sij, |S|Sij, |S|, u_i u_j and u_i give Mij and Lij, the
+  // coefficient -LijMij / (2 MijMij) / Delta^2 clipped to [0, 0.04] and
+  // smoothed (weit 1, 1/27); CmuVt = C Delta^2 |S| in interior cells deeper
+  // than 0.02 m, zero elsewhere, then the ghosts and quiet maker regions as
+  // in les_3D.  |S|Sij of cells at most 0.02 m deep, which the reference
+  // leaves unset, is zero here.
+  void les_dyn() {
+    const double Dmin = (double)0.02f;
+    std::vector<A3> Sij(6);
+    for (A3& a : Sij) a.init(Mloc, Nloc, Kloc);
+    auto ds = [&](int k) { return sigc(k + 1) - sigc(k - 1); };
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = Kbeg; k <= Kend; ++k) {
+          if (!(Mask(i, j) == 1 && D(i, j) > Dmin)) continue;
+          const double dUs = (U(i, j, k + 1) - U(i, j, k - 1)) / ds(k), dVs = (V(i, j, k + 1) - V(i, j, k - 1)) / ds(k);
+          const double dWs = (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+          Sij[0](i, j, k) = (U(i + 1, j, k) - U(i - 1, j, k)) / (2.0 * dx) + dUs * DelxSc(i, j, k);
+          Sij[1](i, j, k) = (V(i, j + 1, k) - V(i, j - 1, k)) / (2.0 * dy) + dVs * DelySc(i, j, k);
+          Sij[2](i, j, k) = 1.0 / D(i, j) * (W(i, j, k + 1) - W(i, j, k - 1)) / ds(k);
+          Sij[3](i, j, k) = 0.5 * ((U(i, j + 1, k) - U(i, j - 1, k)) / (2.0 * dy) + dUs * DelySc(i, j, k) +
+                                   (V(i + 1, j, k) - V(i - 1, j, k)) / (2.0 * dx) + dVs * DelxSc(i, j, k));
+          Sij[4](i, j, k) = 0.5 * (dVs / D(i, j) + (W(i, j + 1, k) - W(i, j - 1, k)) / (2.0 * dy) + dWs * DelySc(i, j, k));
+          Sij[5](i, j, k) = 0.5 * (dUs / D(i, j) + (W(i + 1, j, k) - W(i - 1, j, k)) / (2.0 * dx) + dWs * DelxSc(i, j, k));
+        }
+    // the components are mirrored one by one (their loops do not mix), and
+    // the reference's north loop writes the sixth component only
+    for (int n = 0; n < 6; ++n) les_mirror(Sij[n], n == 5);
+    A3 Sab;
+    Sab.init(Mloc, Nloc, Kloc);
+    std::vector<A3> SabSij(6);
+    for (A3& a : SabSij) a.init(Mloc, Nloc, Kloc);
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          if (!(D(i, j) > Dmin)) continue;
+          auto s = [&](int n) { return Sij[n](i, j, k); };
+          const double a = s(0) * s(0) + s(1) * s(1) + s(2) * s(2) + 2.0 * (s(3) * s(3) + s(4) * s(4) + s(5) * s(5));
+          Sab(i, j, k) = std::sqrt(2.0 * a);
+          for (int n = 0; n < 6; ++n) SabSij[n](i, j, k) = Sab(i, j, k) * s(n);
+        }
+    const double fact1 = 1.0 / 64.0;
+    std::vector<A3> FSabSij(6), FSij(6), Uij(6), FUij(6), Ui(3), FUi(3);
+    A3 FSab;
+    for (int n = 0; n < 6; ++n) {
+      FSabSij[n].init(Mloc, Nloc, Kloc); FSij[n].init(Mloc, Nloc, Kloc);
+      les_filter(SabSij[n], FSabSij[n], 2.0, fact1);
+      les_filter(Sij[n], FSij[n], 2.0, fact1);
+    }
+    FSab.init(Mloc, Nloc, Kloc);
+    les_filter(Sab, FSab, 2.0, fact1);
+    for (int n = 0; n < 6; ++n) { Uij[n].init(Mloc, Nloc, Kloc); FUij[n].init(Mloc, Nloc, Kloc); }
+    for (int n = 0; n < 3; ++n) { Ui[n].init(Mloc, Nloc, Kloc); FUi[n].init(Mloc, Nloc, Kloc); }
+    for (size_t c = 0; c < U.v.size(); ++c) {
+      const double u = U.v[c], v = V.v[c], w = W.v[c];
+      Uij[0].v[c] = u * u; Uij[1].v[c] = v * v; Uij[2].v[c] = w * w;
+      Uij[3].v[c] = u * v; Uij[4].v[c] = v * w; Uij[5].v[c] = u * w;
+      Ui[0].v[c] = u; Ui[1].v[c] = v; Ui[2].v[c] = w;
+    }
+    for (int n = 0; n < 6; ++n) les_filter(Uij[n], FUij[n], 2.0, fact1);
+    for (int n = 0; n < 3; ++n) les_filter(Ui[n], FUi[n], 2.0, fact1);
+    A3 Smag, FW;
+    Smag.init(Mloc, Nloc, Kloc); FW.init(Mloc, Nloc, Kloc);
+    const double alpha2 = 4.0;
+    for (int k = 1; k <= Kloc; ++k)
+      for (int j = 1; j <= Nloc; ++j)
+        for (int i = 1; i <= Mloc; ++i) {
+          double M[6], L[6];
+          for (int n = 0; n < 6; ++n) M[n] = alpha2 * FSab(i, j, k) * FSij[n](i, j, k) - FSabSij[n](i, j, k);
+          auto fu = [&](int n) { return FUi[n](i, j, k); };
+          L[0] = FUij[0](i, j, k) - fu(0) * fu(0);
+          L[1] = FUij[1](i, j, k) - fu(1) * fu(1);
+          L[2] = FUij[2](i, j, k) - fu(2) * fu(2);
+          L[3] = FUij[3](i, j, k) - fu(0) * fu(1);
+          L[4] = FUij[4](i, j, k) - fu(1) * fu(2);
+          L[5] = FUij[5](i, j, k) - fu(2) * fu(0);
+          double MM = 0.0, LM = 0.0;
+          if (D(i, j) > Dmin) {
+            MM = M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + 2.0 * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+            LM = L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + 2.0 * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]);
+          }
+          double c = 0.5 * (-LM) / (MM + (double)1.e-16f);
+          FW(i, j, k) = std::pow(dx * dy * D(i, j) * dsig(k), (double)(1.0f / 3.0f));
+          c = c / (FW(i, j, k) * FW(i, j, k));
+          if (c < 0.0) c = 0.0;
+          if (c > (double)0.04f) c = (double)0.04f;
+          Smag(i, j, k) = c;
+        }
+    A3 FC;
+    FC.init(Mloc, Nloc, Kloc);
+    les_filter(Smag, FC, 1.0, (double)(1.0f / 27.0f));
+    CmuVt.fill(0.0);
+    for (int k = Kbeg; k <= Kend; ++k)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int i = Ibeg; i <= Iend; ++i)
+          if (D(i, j) > Dmin)
+            CmuVt(i, j, k) = dmax(FC(i, j, k) * (FW(i, j, k) * FW(i, j, k)) * Sab(i, j, k), 0.0);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) CmuVt(i, j, Kbeg - k) = CmuVt(i, j, Kbeg + k - 1);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int j = Jbeg; j <= Jend; ++j)
+        for (int k = 1; k <= Nghost; ++k) CmuVt(i, j, Kend + k) = CmuVt(i, j, Kend - k + 1);
+    const bool lef = (p.wavemaker >= NHW_WM_LEF_LIN && p.wavemaker <= NHW_WM_LEF_CON) || p.wavemaker == NHW_WM_LEF_TID ||
+                     p.wavemaker == NHW_WM_LEF_JON || p.wavemaker == NHW_WM_LEF_TMA || p.wavemaker == NHW_WM_LEF_SPC;
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k) {
+        if (lef) CmuVt(Ibeg, j, k) = Zero;
+        for (int i = 1; i <= Nghost; ++i) CmuVt(Ibeg - i, j, k) = CmuVt(Ibeg + i - 1, j, k);
+      }
+    for (int j = Jbeg; j <= Jend; ++j)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int i = 1; i <= Nghost; ++i) CmuVt(Iend + i, j, k) = CmuVt(Iend - i + 1, j, k);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) CmuVt(i, Jbeg - j, k) = CmuVt(i, Jbeg + j - 1, k);
+    for (int i = Ibeg; i <= Iend; ++i)
+      for (int k = Kbeg; k <= Kend; ++k)
+        for (int j = 1; j <= Nghost; ++j) CmuVt(i, Jend + j, k) = CmuVt(i, Jend - j + 1, k);
+    if (ke_quiet_maker())
+      for (int k = 1; k <= Kloc; ++k)
+        for (int j = 1; j <= Nloc; ++j)
+          for (int i = 1; i <= Mloc; ++i)
+            if (xc(i) >= p.xsource_west && xc(i) <= p.xsource_east && yc(j) >= p.ysource_suth &&
+                yc(j) <= p.ysource_nrth)
+              CmuVt(i, j, k) = Zero;
+  }
+
   // eval_turb (src/nhwave.F:6544-6782), called after sponge_damping.
   // Vertical: IVTURB 1 CmuVt = Cvs; 2 the subgrid model CmuVt = Cvs D
   // dsig^2 |d(U,V)/dsigma| on every level but the outermost ghosts, which
@@ -3430,6 +3612,8 @@ struct Model {
       les_3D();
     } else if (p.ivturb == 3) {
       kepsilon_2D(istep);
+    } else if (p.ivturb == 30) {
+      les_dyn();
     } else {
       for (int i = 1; i <= Mloc; ++i)
         for (int j = 1; j <= Nloc; ++j) {

@@ -53,13 +53,12 @@ def test_out_of_scope_options_rejected_on_host(field, value, gpu_lib):
     assert st == lib.ERR_UNSUPPORTED and not h.value
 
 
-@pytest.mark.parametrize("fields", [dict(ivturb=4), dict(ivturb=30, ihturb=10), dict(ivturb=11),
+@pytest.mark.parametrize("fields", [dict(ivturb=4), dict(ivturb=31, ihturb=10), dict(ivturb=11),
                                     dict(ivturb=2, ihturb=0), dict(ivturb=10, ihturb=3)])
 def test_viscous_closures_outside_the_path_rejected(fields, gpu_lib):
     """VISCOUS_FLOW = T runs with IVTURB 1 (constant viscosity), 2 (subgrid
-    model), 3 / 10 (2-D / 3-D k-epsilon) or 20 (Smagorinsky LES) and IHTURB
-    1, 2 or >= 10; the dynamic LES (30) and other codes are rejected on the
-    host."""
+    model), 3 / 10 (2-D / 3-D k-epsilon) or 20 / 30 (Smagorinsky / dynamic
+    LES) and IHTURB 1, 2 or >= 10; other codes are rejected on the host."""
     from nhwave_gb300 import default_params, lib
     p = default_params(viscous_flow=1, **fields)
     h = ctypes.c_void_p()

@@ -50,7 +50,7 @@ def _routines(s):
                                   "tiny_flume_stk", "tiny_flume_con", "tiny_flume_cur", "tiny_flume_foc", "tiny_flume_tid", "tiny_open",
                                   "tiny_flume_open", "tiny_flume_rig", "tiny_flux_lr", "tiny_flume_jon",
                                   "tiny_visc", "tiny_visc_fric", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng",
-                                  "tiny_les", "tiny_ke2", "tiny_flume_ke2"])
+                                  "tiny_les", "tiny_lesdyn", "tiny_ke2", "tiny_flume_ke2"])
 def test_graph_step_equals_routines(name, precision, gpu_lib, hllc=0):
     from nhwave_gb300 import fields as F
     a = _scen(name, precision, hllc=hllc)

@@ -19,11 +19,11 @@ CASES = ["tiny_c1", "tiny_c2", "tiny_c3", "tiny_c4"]
 # in tiny_visc_dt the viscous limit sets dt; no-slip and friction-law beds;
 # the subgrid eddy viscosities, IVTURB = IHTURB = 2; the k-epsilon closure,
 # IVTURB = IHTURB = 10, standard and RNG, and the 2-D one, IVTURB = 3, from
-# seeded turbulence; the Smagorinsky LES, IVTURB = 20), and wall friction
-# (BC = 5) on the sides
+# seeded turbulence; the Smagorinsky and dynamic LES, IVTURB = 20 and 30),
+# and wall friction (BC = 5) on the sides
 MORE_CASES = CASES + ["tiny_open", "tiny_visc", "tiny_visc_dt", "tiny_visc_noslip", "tiny_visc_fric",
                       "tiny_visc_sgs", "tiny_visc_sgs_fric", "tiny_ke", "tiny_ke_rng", "tiny_ke2", "tiny_flume_ke2",
-                      "tiny_les", "tiny_wallfric"]
+                      "tiny_les", "tiny_lesdyn", "tiny_wallfric"]
 STATE2D = ["D", "ETA", "HC", "HFX0", "HFY0", "DELXH", "DELYH", "ETAXL", "ETAXR", "ETAYL", "ETAYR"]
 STATE3D = ["U", "V", "W", "DU", "DV", "DW"]
 
@@ -122,7 +122,7 @@ def test_explicit_routines_bit_exact(name, hllc, oracle_mod, gpu_lib):
                 _cmp_exact(g, o, ["D", "ETA"] + STATE3D, f"sponge {rnd}.{s}")
             if g.params.viscous_flow:
                 g.eval_turb(s); o.eval_turb(s)
-                if g.params.ivturb == 20:
+                if g.params.ivturb in (20, 30):
                     # the LES filter width and wall function use pow/log/exp: CUDA's
                     # and the host libm's may differ in the last bit; pin after
                     for n in ("CMUVT", "CMUHT"):

@@ -565,6 +565,34 @@ def test_les_smagorinsky_viscosity_and_smooth_wall_law(oracle_mod):
     assert np.array_equal(cv[ng - 1][cols], cv[ng][cols]) and np.array_equal(o.get(F.CMUHT), cv)
 
 
+def test_les_dyn_coefficient_of_a_linear_strain(oracle_mod):
+    """les_dyn (src/nhwave.F:7989-8542) on U = a x in a flat 1 m deep channel
+    before the first sigma_transform: S11 = a is the only strain rate, the
+    test filter keeps linear fields, and the [1 2 1]/4 filter of u^2 adds
+    (a dx)^2 / 2, so L11 = (a dx)^2 / 2 and M11 = 3 |S| a with |S| = sqrt(2)
+    |a|.  The coefficient -L11 M11 / (2 M11^2) / Delta^2 is clipped to zero
+    under stretching (a > 0); under compression (a < 0) it is dx^2 / (12
+    sqrt(2) Delta^2) and CmuVt = C Delta^2 |S| = |a| dx^2 / 12 (times 27 x
+    the default-real 1/27 of the smoothing filter), away from the walls,
+    the bed and the surface."""
+    from nhwave_gb300 import default_params, fields as F
+    M, N, K, dx, dy = 32, 15, 8, 0.1, 0.5
+    ng = F.NG
+    out = []
+    for a in (0.3, -0.3):
+        p = default_params(Mglob=M, Nglob=N, Kglob=K, dx=dx, dy=dy, dt_ini=0.01, dt_max=1.0, tol=1e-10,
+                           itmax=2000, viscous_flow=1, visc=1e-6, ivturb=30, ihturb=30)
+        x = (np.arange(M) + 0.5) * dx
+        uvw = np.zeros((3, K, N, M))
+        uvw[0] = a * (x - x.mean())[None, None, :]
+        o = oracle_mod.Oracle(p, np.ones(M * N), None, uvw.ravel())
+        o.eval_turb(1)
+        out.append(o.get(F.CMUVT)[ng + 3:ng + K - 3, ng + N // 2, ng + 4:ng + M - 4])
+    assert np.all(out[0] == 0.0)
+    expect = 0.3 * dx * dx / 12.0 * 27.0 * float(np.float32(1.0) / np.float32(27.0))
+    assert out[1] == pytest.approx(np.full(out[1].shape, expect), rel=1e-12)
+
+
 def test_viscous_without_viscosity_is_the_inviscid_run(oracle_mod):
     """VISCOUS_FLOW = T with zero viscosities: the tridiagonal systems are the
     identity and the explicit terms vanish, so the run equals the inviscid

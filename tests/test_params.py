@@ -172,7 +172,7 @@ Zob = 2.e-4
     f.write_text(text.replace("IVTURB = 1", "IVTURB = 10").replace("IHTURB = 1", "IHTURB = 10") + "PRODTYPE = 2\n")
     q = P.read_input(str(f))
     assert (q.ivturb, q.ihturb, q.prod_type) == (10, 10, 2) and P.unsupported_reason(q) is None
-    f.write_text(text.replace("IVTURB = 1", "IVTURB = 30"))
+    f.write_text(text.replace("IVTURB = 1", "IVTURB = 40"))
     assert "IVTURB" in P.unsupported_reason(P.read_input(str(f)))
     foc = SAMPLE.replace("WAVEMAKER = INT_LIN", "WAVEMAKER = FOCUSED") + """
 nwave = 12
