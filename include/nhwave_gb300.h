@@ -28,7 +28,7 @@
  *   nhw_sponge_damping     <- sponge_damping       src/nhwave.F:6463-6502
  *   nhw_eval_turb          <- eval_turb(ISTEP)     src/nhwave.F:6544-6782 (IVTURB 1, 2, 3 with
  *                             kepsilon :11117-11524, 10 with kepsilon_3D :10030-11114,
- *                             20 with les_3D :8545-8729;
+ *                             20 with les_3D :8545-8729, 30 with les_dyn :7989-8542;
  *                             IHTURB 1, 2, >= 10;
  *                             viscous flow only, a no-op otherwise)
  *   nhw_step               <- one pass of the do-while body src/nhwave.F:119-258
@@ -173,7 +173,8 @@ typedef struct nhw_params {
   /* viscous flow (read when viscous_flow = 1; src/initialize.F:357, 385-392) */
   int32_t ivturb, ihturb;                  /* IVTURB IHTURB: 1 constant viscosity,
                                               2 subgrid model; IVTURB 3 / 10 2-D /
-                                              3-D k-epsilon, 20 Smagorinsky LES; IHTURB
+                                              3-D k-epsilon, 20 / 30 Smagorinsky /
+                                              dynamic LES; IHTURB
                                               >= 10 takes CmuHt = CmuVt                */
   int32_t rng;                             /* RNG: seeding viscosity of the first stage */
   double  cvs, chs;                        /* Cvs Chs: vertical / horizontal eddy
