@@ -16,7 +16,7 @@ their pressure solves sharing persistent cooperative launches.
 import numpy as np
 import pytest
 
-from conftest import rel_l2
+from conftest import rel_l2, seed_ke
 
 pytestmark = pytest.mark.gpu
 
@@ -178,3 +178,29 @@ def test_ensemble_of_the_added_boundaries_and_viscous_flow(precision, solver, gp
                 den = max(np.linalg.norm(b.get(fid)[sl]), 1e-30)
                 r = np.linalg.norm(a.get(fid)[sl] - b.get(fid)[sl]) / den
                 assert r < lim, f"{n} {f}: {r:.3e}"
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ensemble_of_the_turbulence_closures(precision, gpu_lib):
+    """Members with the subgrid model, the 3-D and 2-D k-epsilon closures
+    (from the same seeded turbulence) and the Smagorinsky and dynamic LES
+    step in one ensemble bit for bit as they step alone, eddy viscosities
+    and k-epsilon state included."""
+    from nhwave_gb300 import fields as F, lib
+    names = ["tiny_visc_sgs", "tiny_ke_rng", "tiny_ke2", "tiny_les", "tiny_lesdyn"]
+    ens = [_member(n, precision) for n in names]
+    ref = [_member(n, precision) for n in names]
+    for a, b in zip(ens, ref):
+        if a.params.ivturb in (3, 10):
+            seed_ke(a, b)
+    with lib.Ensemble(ens, solver=0) as e:
+        for _ in range(3):
+            assert e.step(1) == 0
+            for r in ref:
+                assert r.step() == 0
+    for n, a, b in zip(names, ens, ref):
+        assert a.scalars().run_step == b.scalars().run_step == 3
+        fields = ["ETA", "P", "U", "W", "CMUVT", "CMUHT"] + (["TKE", "EPS"] if a.params.ivturb in (3, 10) else [])
+        for f in fields:
+            fid = getattr(F, f)
+            assert np.array_equal(a.get(fid), b.get(fid)), f"{n} {f} differs"
