@@ -488,6 +488,26 @@ def test_ke_bed_wall_function_of_a_current(oracle_mod):
     assert o.get(F.EPS)[ng, ng + 1, ng + 3] == pytest.approx(us ** 3 / (kappa * dz1), rel=1e-12)
 
 
+def test_ke_side_wall_function_along_a_friction_wall(oracle_mod):
+    """The friction-wall condition of kepsilon_3D (BC_Y0 = 5, src/nhwave.F:
+    10956-10987): along a south wall the first row takes tke u*^2 / sqrt(cmiu)
+    and epsilon u*^3 / (kappa dy / 2) with u* = sqrt(Cd0) |(U, W)| of that
+    row, on every level, mirrored into the ghost rows."""
+    from nhwave_gb300 import fields as F
+    K = 6
+    o = _ke_channel(oracle_mod, 1e-4, 1e-5, lambda s: 0.2 + 0.0 * s, K=K, N=4, bc_y0=5, ibot=1, cd0=0.004)
+    _ke_stage(o)
+    ng = F.NG
+    u, w = o.get(F.U)[:, ng, :], o.get(F.W)[:, ng, :]
+    fric = math.sqrt(0.004) * np.sqrt(u * u + w * w)
+    kap, cmiu = float(np.float32(0.41)), float(np.float32(0.09))
+    cols, levs = slice(ng, ng + 8), slice(ng, ng + K)
+    tk, ep = o.get(F.TKE), o.get(F.EPS)
+    assert tk[levs, ng, cols] == pytest.approx((fric * fric / math.sqrt(cmiu))[levs, cols], rel=1e-12)
+    assert ep[levs, ng, cols] == pytest.approx((fric ** 3 / (kap * 0.5 / 2.0))[levs, cols], rel=1e-12)
+    assert np.array_equal(tk[levs, ng - 1, cols], tk[levs, ng, cols])
+
+
 def test_ke_shear_produces_turbulence(oracle_mod):
     """The nonlinear production (src/nhwave.F:10139-10274): a sheared current
     U = 2 sigma keeps more tke above the bed level than still water from the
