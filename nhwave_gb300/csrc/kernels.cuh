@@ -2989,16 +2989,16 @@ struct OpSponge {
         S.DU[o] = rd * u;
         S.DV[o] = rd * v;
       }
-      return;
-    }
-    for (int k = 0; k < S.Kloc; ++k) {
-      const long long o = i3(S, i, j, k);
-      const double u = ((double)S.U[o] - Ucur) * sp + Ucur;
-      const double v = (double)S.V[o] * sp;
-      S.U[o] = (T)u;
-      S.V[o] = (T)v;
-      S.DU[o] = (T)(d * (double)(T)u);
-      S.DV[o] = (T)(d * (double)(T)v);
+    } else {
+      for (int k = 0; k < S.Kloc; ++k) {
+        const long long o = i3(S, i, j, k);
+        const double u = ((double)S.U[o] - Ucur) * sp + Ucur;
+        const double v = (double)S.V[o] * sp;
+        S.U[o] = (T)u;
+        S.V[o] = (T)v;
+        S.DU[o] = (T)(d * (double)(T)u);
+        S.DV[o] = (T)(d * (double)(T)v);
+      }
     }
   }
 };
